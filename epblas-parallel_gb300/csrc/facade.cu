@@ -1,0 +1,630 @@
+// The drop-in boundary: extern "C" Fortran-ABI entry points.
+//
+// Each routine is written once as a template over the integer type and
+// instantiated twice, as `name_` (int, LP64) and `name_64_` (int64_t, ILP64),
+// mirroring EPBLAS_FACADE_PAIR (src/epblas-parallel/common/epblas_facade.h:
+// 63-65). Scalars arrive by pointer and are read on the host; arrays may be
+// host or device memory (see runtime.h). Quick returns and special scalar
+// values follow the reference's *_core functions line for line; the checks
+// the reference does not have (leading dimensions, flag letters, null
+// pointers) record an error and leave the outputs untouched.
+#include <cctype>
+#include <cstring>
+
+#include "gemm.h"
+#include "l1.h"
+#include "level3.h"
+#include "runtime.h"
+
+namespace mw {
+
+namespace {
+
+inline char up(const char *c) { return (char)std::toupper((unsigned char)*c); }
+// blas_trans_real (common/blas_char.h:36): 'C' folds to 'T'.
+inline char trans_real(const char *c)
+{
+    char t = up(c);
+    return t == 'C' ? 'T' : t;
+}
+
+inline dd_host rd(const mwblas_real64x2 *p) { return dd_host{p->limbs[0], p->limbs[1]}; }
+inline cdd_host cd(const mwblas_complex64x2 *p)
+{
+    return cdd_host{{p->re.limbs[0], p->re.limbs[1]}, {p->im.limbs[0], p->im.limbs[1]}};
+}
+// mf_pred.h:28-32
+inline bool eq0(dd_host a) { return a.hi == 0.0 && a.lo == 0.0; }
+inline bool eq1(dd_host a) { return a.hi == 1.0 && a.lo == 0.0; }
+inline bool ceq0(cdd_host a) { return eq0(a.re) && eq0(a.im); }
+inline bool ceq1(cdd_host a) { return eq1(a.re) && eq0(a.im); }
+inline int beta_kind(dd_host b) { return eq0(b) ? 0 : (eq1(b) ? 1 : 2); }
+inline int beta_kind(cdd_host b) { return ceq0(b) ? 0 : (ceq1(b) ? 1 : 2); }
+
+int g_engine_init = -1;
+int g_engine = MWBLAS_GEMM_AUTO;
+int g_ozaki_bits = 0;
+
+int engine()
+{
+    if (g_engine_init < 0) {
+        g_engine_init = 1;
+        const char *e = getenv("MWBLAS_GEMM");
+        if (e) {
+            if (!strcmp(e, "plain")) g_engine = MWBLAS_GEMM_PLAIN;
+            else if (!strcmp(e, "ozaki")) g_engine = MWBLAS_GEMM_OZAKI;
+        }
+    }
+    return g_engine;
+}
+
+// A scope that owns staged arrays and releases them on every exit path.
+struct Scope {
+    const char *routine;
+    std::vector<Staged *> items;
+    explicit Scope(const char *r) : routine(r) { clear_error(); }
+    Staged &add(Staged &s)
+    {
+        items.push_back(&s);
+        return s;
+    }
+    ~Scope()
+    {
+        for (Staged *s : items) release(*s);
+    }
+};
+
+}  // namespace
+
+// ---- GEMM dispatch shared by mgemm_/wgemm_ and the level-3 routines ---------------
+
+bool run_gemm(GemmArgs &g, bool cplx, int force_engine, const char *routine)
+{
+    int eng = force_engine >= 0 ? force_engine : engine();
+    if (eng == MWBLAS_GEMM_AUTO) {
+        // The tensor-core scheme wins once the k-dimension and the output tile
+        // count amortise its operand conversion.
+        double work = (double)g.m * (double)g.n * (double)g.k;
+        eng = (work >= 64.0 * 64.0 * 64.0 * 8.0 && g.k >= 32) ? MWBLAS_GEMM_OZAKI : MWBLAS_GEMM_PLAIN;
+        if (!ozaki_available()) eng = MWBLAS_GEMM_PLAIN;
+    }
+    if (eng == MWBLAS_GEMM_OZAKI) {
+        if (!ozaki_available()) {
+            set_error(routine, MWBLAS_ERR_UNSUPPORTED, "tensor-core engine unavailable on this device");
+            return false;
+        }
+        return cplx ? gemm_ozaki_cplx(g, g_ozaki_bits, routine) : gemm_ozaki_real(g, g_ozaki_bits, routine);
+    }
+    return cplx ? gemm_plain_cplx(g, routine) : gemm_plain_real(g, routine);
+}
+
+namespace {
+
+// ---- mgemm / wgemm ------------------------------------------------------------------
+
+template <typename INT>
+void gemm_entry(const char *routine, bool cplx, int force_engine, const char *transa, const char *transb,
+                const INT *m, const INT *n, const INT *k, const void *alpha, const void *a, const INT *lda,
+                const void *b, const INT *ldb, const void *beta, void *c, const INT *ldc)
+{
+    Scope sc(routine);
+    if (!transa || !transb || !m || !n || !k || !alpha || !beta || !lda || !ldb || !ldc) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char TA = cplx ? up(transa) : trans_real(transa);
+    char TB = cplx ? up(transb) : trans_real(transb);
+    int64_t M = *m, N = *n, K = *k;
+    if (!(TA == 'N' || TA == 'T' || TA == 'C')) { set_error(routine, 1, "invalid transa"); return; }
+    if (!(TB == 'N' || TB == 'T' || TB == 'C')) { set_error(routine, 2, "invalid transb"); return; }
+    // mgemm_parallel.cpp:66: m <= 0 || n <= 0 returns before touching C.
+    if (M <= 0 || N <= 0) return;
+    if (K < 0) K = 0;
+    int64_t nrowa = (TA == 'N') ? M : K, nrowb = (TB == 'N') ? K : N;
+    if (*lda < (nrowa > 1 ? nrowa : 1)) { set_error(routine, 8, "lda too small"); return; }
+    if (*ldb < (nrowb > 1 ? nrowb : 1)) { set_error(routine, 10, "ldb too small"); return; }
+    if (*ldc < (M > 1 ? M : 1)) { set_error(routine, 13, "ldc too small"); return; }
+    if (!c) { set_error(routine, 12, "null C"); return; }
+
+    GemmArgs g;
+    g.m = M; g.n = N; g.k = K;
+    g.ta = TA != 'N'; g.tb = TB != 'N';
+    g.ca = TA == 'C'; g.cb = TB == 'C';
+    bool alpha0;
+    if (cplx) {
+        g.calpha = cd((const mwblas_complex64x2 *)alpha);
+        g.cbeta = cd((const mwblas_complex64x2 *)beta);
+        g.beta_kind = beta_kind(g.cbeta);
+        alpha0 = ceq0(g.calpha);
+    } else {
+        g.alpha = rd((const mwblas_real64x2 *)alpha);
+        g.beta = rd((const mwblas_real64x2 *)beta);
+        g.beta_kind = beta_kind(g.beta);
+        alpha0 = eq0(g.alpha);
+    }
+    bool compute = !(alpha0 || K == 0);
+    if (compute && (!a || !b)) { set_error(routine, a ? 9 : 7, "null A or B"); return; }
+    if (!ensure_device(routine)) return;
+    size_t es = cplx ? 32 : 16;
+
+    Staged SA, SB, SC;
+    sc.add(SA); sc.add(SB); sc.add(SC);
+    // C is read unless beta == 0.
+    if (!stage_matrix(SC, c, M, N, *ldc, es, g.beta_kind != 0, routine)) return;
+    g.C = SC.dev; g.ldc = *ldc;
+    if (!compute) {
+        // beta pre-pass only (mgemm_parallel.cpp:68-78)
+        if (cplx) launch_scale_matrix_c(M, N, g.cbeta, g.beta_kind, g.C, g.ldc);
+        else launch_scale_matrix(M, N, g.beta, g.beta_kind, g.C, g.ldc);
+    } else {
+        if (!stage_matrix(SA, a, nrowa, TA == 'N' ? K : M, *lda, es, true, routine)) return;
+        if (!stage_matrix(SB, b, nrowb, TB == 'N' ? N : K, *ldb, es, true, routine)) return;
+        g.A = SA.dev; g.lda = *lda;
+        g.B = SB.dev; g.ldb = *ldb;
+        if (!run_gemm(g, cplx, force_engine, routine)) return;
+    }
+    if (!unstage_matrix(SC, routine)) return;
+    finish(routine);
+}
+
+// ---- msyrk / wherk ------------------------------------------------------------------
+
+template <typename INT>
+void syrk_entry(const char *routine, bool herm, const char *uplo, const char *trans, const INT *n, const INT *k,
+                const mwblas_real64x2 *alpha, const void *a, const INT *lda, const mwblas_real64x2 *beta, void *c,
+                const INT *ldc)
+{
+    Scope sc(routine);
+    if (!uplo || !trans || !n || !k || !alpha || !beta || !lda || !ldc) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char U = up(uplo);
+    char T = up(trans);
+    if (!herm && T == 'C') T = 'T';          // msyrk_parallel.cpp:53-54
+    if (herm && T == 'T') T = 'C';           // wherk_serial.cpp:412-433 treats non-'N' as 'C'
+    if (U != 'U' && U != 'L') { set_error(routine, 1, "invalid uplo"); return; }
+    if (T != 'N' && T != (herm ? 'C' : 'T')) { set_error(routine, 2, "invalid trans"); return; }
+    int64_t N = *n, K = *k;
+    if (N < 0) { set_error(routine, 3, "n < 0"); return; }
+    if (K < 0) { set_error(routine, 4, "k < 0"); return; }
+    if (N == 0) return;
+    int64_t nrowa = (T == 'N') ? N : K;
+    if (*lda < (nrowa > 1 ? nrowa : 1)) { set_error(routine, 7, "lda too small"); return; }
+    if (*ldc < (N > 1 ? N : 1)) { set_error(routine, 10, "ldc too small"); return; }
+    if (!c) { set_error(routine, 9, "null C"); return; }
+    dd_host al = rd(alpha), be = rd(beta);
+    int bk = beta_kind(be);
+    bool compute = !(eq0(al) || K == 0);
+    // msyrk_parallel.cpp:57-65 / wherk_parallel.cpp:57-70
+    if (!compute && bk == 1 && !herm) return;
+    if (compute && !a) { set_error(routine, 6, "null A"); return; }
+    if (!ensure_device(routine)) return;
+    size_t es = herm ? 32 : 16;
+    int ul = (U == 'U') ? 1 : 2;
+    Staged SA, SC;
+    sc.add(SA); sc.add(SC);
+    if (!stage_matrix(SC, c, N, N, *ldc, es, true, routine)) return;
+    if (!compute) {
+        if (herm) launch_scale_matrix_c(N, N, cdd_host{be, {0.0, 0.0}}, bk, SC.dev, *ldc, ul, true);
+        else launch_scale_matrix(N, N, be, bk, SC.dev, *ldc, ul);
+    } else {
+        if (!stage_matrix(SA, a, nrowa, T == 'N' ? K : N, *lda, es, true, routine)) return;
+        GemmArgs g;
+        g.alpha = al;
+        g.beta = be;
+        g.calpha = cdd_host{al, {0.0, 0.0}};
+        g.cbeta = cdd_host{be, {0.0, 0.0}};
+        g.beta_kind = bk;
+        if (!syrk_device(herm, herm, ul, T != 'N', N, K, SA.dev, *lda, g, SC.dev, *ldc, routine)) return;
+    }
+    if (!unstage_matrix(SC, routine)) return;
+    finish(routine);
+}
+
+// ---- mtrsm --------------------------------------------------------------------------------
+
+template <typename INT>
+void trsm_entry(const char *routine, const char *side, const char *uplo, const char *transa, const char *diag,
+                const INT *m, const INT *n, const mwblas_real64x2 *alpha, const void *a, const INT *lda, void *b,
+                const INT *ldb)
+{
+    Scope sc(routine);
+    if (!side || !uplo || !transa || !diag || !m || !n || !alpha || !lda || !ldb) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char S = up(side), U = up(uplo), T = trans_real(transa), D = up(diag);
+    if (S != 'L' && S != 'R') { set_error(routine, 1, "invalid side"); return; }
+    if (U != 'U' && U != 'L') { set_error(routine, 2, "invalid uplo"); return; }
+    if (T != 'N' && T != 'T') { set_error(routine, 3, "invalid transa"); return; }
+    if (D != 'U' && D != 'N') { set_error(routine, 4, "invalid diag"); return; }
+    int64_t M = *m, N = *n;
+    if (M < 0) { set_error(routine, 5, "m < 0"); return; }
+    if (N < 0) { set_error(routine, 6, "n < 0"); return; }
+    if (M == 0 || N == 0) return;   // mtrsm_parallel.cpp:57
+    int64_t na = (S == 'L') ? M : N;
+    if (*lda < (na > 1 ? na : 1)) { set_error(routine, 9, "lda too small"); return; }
+    if (*ldb < (M > 1 ? M : 1)) { set_error(routine, 11, "ldb too small"); return; }
+    if (!b) { set_error(routine, 10, "null B"); return; }
+    dd_host al = rd(alpha);
+    if (!eq0(al) && !a) { set_error(routine, 8, "null A"); return; }
+    if (!ensure_device(routine)) return;
+    Staged SA, SB;
+    sc.add(SA); sc.add(SB);
+    bool zero = eq0(al);   // mtrsm_parallel.cpp:59: alpha == 0 zeroes B
+    if (!stage_matrix(SB, b, M, N, *ldb, 16, !zero, routine)) return;
+    if (zero) {
+        launch_zero_matrix(M, N, SB.dev, *ldb);
+    } else {
+        if (!stage_matrix(SA, a, na, na, *lda, 16, true, routine)) return;
+        if (!trsm_device(S, U, T, D, M, N, al, SA.dev, *lda, SB.dev, *ldb, routine)) return;
+    }
+    if (!unstage_matrix(SB, routine)) return;
+    finish(routine);
+}
+
+// ---- mgemv --------------------------------------------------------------------------------
+
+template <typename INT>
+void gemv_entry(const char *routine, const char *trans, const INT *m, const INT *n, const mwblas_real64x2 *alpha,
+                const void *a, const INT *lda, const void *x, const INT *incx, const mwblas_real64x2 *beta, void *y,
+                const INT *incy)
+{
+    Scope sc(routine);
+    if (!trans || !m || !n || !alpha || !lda || !incx || !beta || !incy) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char T = trans_real(trans);
+    if (T != 'N' && T != 'T') { set_error(routine, 1, "invalid trans"); return; }
+    int64_t M = *m, N = *n;
+    if (M < 0) { set_error(routine, 2, "m < 0"); return; }
+    if (N < 0) { set_error(routine, 3, "n < 0"); return; }
+    if (*lda < (M > 1 ? M : 1)) { set_error(routine, 6, "lda too small"); return; }
+    if (*incx == 0) { set_error(routine, 8, "incx == 0"); return; }
+    if (*incy == 0) { set_error(routine, 11, "incy == 0"); return; }
+    if (M == 0 || N == 0) return;   // mgemv.cpp:252
+    if (!y) { set_error(routine, 10, "null y"); return; }
+    dd_host al = rd(alpha), be = rd(beta);
+    int bk = beta_kind(be);
+    if (eq0(al) && bk == 1) return;
+    if (!eq0(al) && (!a || !x)) { set_error(routine, a ? 7 : 5, "null A or x"); return; }
+    if (!ensure_device(routine)) return;
+    int64_t lenx = (T == 'N') ? N : M, leny = (T == 'N') ? M : N;
+    Staged SA, SX, SY;
+    sc.add(SA); sc.add(SX); sc.add(SY);
+    int64_t dix = *incx, diy;
+    if (!stage_vector(SY, y, leny, *incy, 16, bk != 0, diy, routine)) return;
+    if (!eq0(al)) {
+        if (!stage_matrix(SA, a, M, N, *lda, 16, true, routine)) return;
+        if (!stage_vector(SX, x, lenx, *incx, 16, true, dix, routine)) return;
+    }
+    if (!gemv_device(T != 'N', M, N, al, SA.dev, *lda, SX.dev, dix, be, bk, SY.dev, diy, routine)) return;
+    if (!unstage_vector(SY, routine)) return;
+    finish(routine);
+}
+
+// ---- level 1 --------------------------------------------------------------------------
+
+// Thresholds of the reference's threaded unit-stride paths.
+constexpr int64_t kScalOmpMin = 2048;   // MSCAL_OMP_MIN, WSCAL_OMP_MIN, WMSCAL_OMP_MIN
+constexpr int64_t kAxpyOmpMin = 2048;   // MAXPY_OMP_MIN
+
+template <typename INT>
+void scal_entry(const char *routine, int kind, const INT *n, const void *alpha, void *x, const INT *incx)
+{
+    // kind: 0 mscal (real), 1 wscal (complex alpha), 2 wmscal (real alpha, complex x)
+    Scope sc(routine);
+    if (!n || !alpha || !incx) { set_error(routine, 1, "null argument pointer"); return; }
+    int64_t N = *n, inc = *incx;
+    if (N <= 0) return;
+    if (kind == 1) {
+        if (ceq1(cd((const mwblas_complex64x2 *)alpha))) return;
+    } else {
+        if (eq1(rd((const mwblas_real64x2 *)alpha))) return;
+    }
+    if (!x) { set_error(routine, 3, "null x"); return; }
+    if (!ensure_device(routine)) return;
+    size_t es = kind == 0 ? 16 : 32;
+    Staged SX;
+    sc.add(SX);
+    int64_t dinc;
+    if (!stage_vector(SX, x, N, inc, es, true, dinc, routine)) return;
+    int64_t team = (inc == 1) ? l1_team(N, kScalOmpMin) : 1;
+    if (kind == 0) launch_mscal(N, rd((const mwblas_real64x2 *)alpha), SX.dev, dinc, team);
+    else if (kind == 1) launch_wscal(N, cd((const mwblas_complex64x2 *)alpha), SX.dev, dinc, team);
+    else launch_wmscal(N, rd((const mwblas_real64x2 *)alpha), SX.dev, dinc, team);
+    if (!unstage_vector(SX, routine)) return;
+    finish(routine);
+}
+
+template <typename INT>
+void axpy_entry(const char *routine, const INT *n, const mwblas_real64x2 *alpha, const void *x, const INT *incx,
+                void *y, const INT *incy)
+{
+    Scope sc(routine);
+    if (!n || !alpha || !incx || !incy) { set_error(routine, 1, "null argument pointer"); return; }
+    int64_t N = *n;
+    dd_host a = rd(alpha);
+    // maxpy.cpp:99
+    if (N <= 0 || eq0(a)) return;
+    if (!x || !y) { set_error(routine, x ? 5 : 3, "null vector"); return; }
+    if (!ensure_device(routine)) return;
+    Staged SX, SY;
+    sc.add(SX); sc.add(SY);
+    int64_t dix, diy;
+    if (!stage_vector(SX, x, N, *incx, 16, true, dix, routine)) return;
+    if (!stage_vector(SY, y, N, *incy, 16, true, diy, routine)) return;
+    int64_t team = (*incx == 1 && *incy == 1) ? l1_team(N, kAxpyOmpMin) : 1;
+    launch_maxpy(N, a, SX.dev, dix, SY.dev, diy, team);
+    if (!unstage_vector(SY, routine)) return;
+    finish(routine);
+}
+
+template <typename INT>
+void copy_entry(const char *routine, bool cplx, const INT *n, const void *x, const INT *incx, void *y,
+                const INT *incy)
+{
+    Scope sc(routine);
+    if (!n || !incx || !incy) { set_error(routine, 1, "null argument pointer"); return; }
+    int64_t N = *n;
+    if (N <= 0) return;
+    if (!x || !y) { set_error(routine, x ? 4 : 2, "null vector"); return; }
+    if (!ensure_device(routine)) return;
+    size_t es = cplx ? 32 : 16;
+    Staged SX, SY;
+    sc.add(SX); sc.add(SY);
+    int64_t dix, diy;
+    if (!stage_vector(SX, x, N, *incx, es, true, dix, routine)) return;
+    // y is write-only, except that a zero increment writes one element.
+    if (!stage_vector(SY, y, N, *incy, es, false, diy, routine)) return;
+    launch_copy(N, SX.dev, dix, SY.dev, diy, cplx ? 2 : 1);
+    if (!unstage_vector(SY, routine)) return;
+    finish(routine);
+}
+
+template <typename INT>
+void swap_entry(const char *routine, bool cplx, const INT *n, void *x, const INT *incx, void *y, const INT *incy)
+{
+    Scope sc(routine);
+    if (!n || !incx || !incy) { set_error(routine, 1, "null argument pointer"); return; }
+    int64_t N = *n;
+    if (N <= 0) return;
+    if (!x || !y) { set_error(routine, x ? 4 : 2, "null vector"); return; }
+    if (!ensure_device(routine)) return;
+    size_t es = cplx ? 32 : 16;
+    Staged SX, SY;
+    sc.add(SX); sc.add(SY);
+    int64_t dix, diy;
+    if (!stage_vector(SX, x, N, *incx, es, true, dix, routine)) return;
+    if (!stage_vector(SY, y, N, *incy, es, true, diy, routine)) return;
+    launch_swap(N, SX.dev, dix, SY.dev, diy, cplx ? 2 : 1);
+    if (!unstage_vector(SX, routine)) return;
+    if (!unstage_vector(SY, routine)) return;
+    finish(routine);
+}
+
+template <typename INT>
+int64_t iamax_entry(const char *routine, bool cplx, const INT *n, const void *x, const INT *incx)
+{
+    Scope sc(routine);
+    if (!n || !incx) { set_error(routine, 1, "null argument pointer"); return 0; }
+    int64_t N = *n, inc = *incx;
+    // imamax.cpp:180-181
+    if (N < 1 || inc <= 0) return 0;
+    if (N == 1) return 1;
+    if (!x) { set_error(routine, 2, "null x"); return 0; }
+    if (!ensure_device(routine)) return 0;
+    Staged SX;
+    sc.add(SX);
+    int64_t dinc;
+    if (!stage_vector(SX, x, N, inc, cplx ? 32 : 16, true, dinc, routine)) return 0;
+    int64_t idx = -1;
+    if (!launch_iamax(N, SX.dev, dinc, cplx, &idx, routine)) return 0;
+    return idx + 1;
+}
+
+template <typename INT>
+mwblas_real64x2 dot_entry(const char *routine, const INT *n, const void *x, const INT *incx, const void *y,
+                          const INT *incy)
+{
+    Scope sc(routine);
+    mwblas_real64x2 r{{0.0, 0.0}};
+    if (!n || !incx || !incy) { set_error(routine, 1, "null argument pointer"); return r; }
+    int64_t N = *n;
+    if (N <= 0) return r;
+    if (!x || !y) { set_error(routine, x ? 4 : 2, "null vector"); return r; }
+    if (!ensure_device(routine)) return r;
+    Staged SX, SY;
+    sc.add(SX); sc.add(SY);
+    int64_t dix, diy;
+    if (!stage_vector(SX, x, N, *incx, 16, true, dix, routine)) return r;
+    if (!stage_vector(SY, y, N, *incy, 16, true, diy, routine)) return r;
+    dd_host out{0.0, 0.0};
+    if (!launch_mdot(N, SX.dev, dix, SY.dev, diy, &out, routine)) return r;
+    r.limbs[0] = out.hi;
+    r.limbs[1] = out.lo;
+    return r;
+}
+
+}  // namespace
+}  // namespace mw
+
+using mw::dd_host;
+typedef mwblas_real64x2 TR;
+typedef mwblas_complex64x2 TC;
+
+extern "C" {
+
+// ---- level 3 -----------------------------------------------------------------------------
+
+#define MW_GEMM_PAIR(NAME, T, CPLX, ENG)                                                                          \
+    void NAME##_(const char *ta, const char *tb, const int *m, const int *n, const int *k, const T *alpha,      \
+                 const T *a, const int *lda, const T *b, const int *ldb, const T *beta, T *c, const int *ldc)   \
+    {                                                                                                           \
+        mw::gemm_entry<int>(#NAME, CPLX, ENG, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc);            \
+    }                                                                                                           \
+    void NAME##_64_(const char *ta, const char *tb, const int64_t *m, const int64_t *n, const int64_t *k,      \
+                    const T *alpha, const T *a, const int64_t *lda, const T *b, const int64_t *ldb,             \
+                    const T *beta, T *c, const int64_t *ldc)                                                    \
+    {                                                                                                           \
+        mw::gemm_entry<int64_t>(#NAME, CPLX, ENG, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc);        \
+    }
+
+MW_GEMM_PAIR(mgemm, TR, false, -1)
+MW_GEMM_PAIR(wgemm, TC, true, -1)
+#undef MW_GEMM_PAIR
+
+#define MW_SYRK_PAIR(NAME, VT, HERM)                                                                              \
+    void NAME##_(const char *uplo, const char *trans, const int *n, const int *k, const TR *alpha, const VT *a,  \
+                 const int *lda, const TR *beta, VT *c, const int *ldc)                                         \
+    {                                                                                                           \
+        mw::syrk_entry<int>(#NAME, HERM, uplo, trans, n, k, alpha, a, lda, beta, c, ldc);                        \
+    }                                                                                                           \
+    void NAME##_64_(const char *uplo, const char *trans, const int64_t *n, const int64_t *k, const TR *alpha,   \
+                    const VT *a, const int64_t *lda, const TR *beta, VT *c, const int64_t *ldc)                 \
+    {                                                                                                           \
+        mw::syrk_entry<int64_t>(#NAME, HERM, uplo, trans, n, k, alpha, a, lda, beta, c, ldc);                    \
+    }
+MW_SYRK_PAIR(msyrk, TR, false)
+MW_SYRK_PAIR(wherk, TC, true)
+#undef MW_SYRK_PAIR
+
+void mtrsm_(const char *side, const char *uplo, const char *transa, const char *diag, const int *m, const int *n,
+            const TR *alpha, const TR *a, const int *lda, TR *b, const int *ldb)
+{
+    mw::trsm_entry<int>("mtrsm", side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb);
+}
+void mtrsm_64_(const char *side, const char *uplo, const char *transa, const char *diag, const int64_t *m,
+               const int64_t *n, const TR *alpha, const TR *a, const int64_t *lda, TR *b, const int64_t *ldb)
+{
+    mw::trsm_entry<int64_t>("mtrsm", side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb);
+}
+
+// ---- level 2 -----------------------------------------------------------------------------
+
+void mgemv_(const char *trans, const int *m, const int *n, const TR *alpha, const TR *a, const int *lda, const TR *x,
+            const int *incx, const TR *beta, TR *y, const int *incy)
+{
+    mw::gemv_entry<int>("mgemv", trans, m, n, alpha, a, lda, x, incx, beta, y, incy);
+}
+void mgemv_64_(const char *trans, const int64_t *m, const int64_t *n, const TR *alpha, const TR *a,
+               const int64_t *lda, const TR *x, const int64_t *incx, const TR *beta, TR *y, const int64_t *incy)
+{
+    mw::gemv_entry<int64_t>("mgemv", trans, m, n, alpha, a, lda, x, incx, beta, y, incy);
+}
+
+void mgemm_plain_64_(const char *ta, const char *tb, const int64_t *m, const int64_t *n, const int64_t *k,
+                     const TR *alpha, const TR *a, const int64_t *lda, const TR *b, const int64_t *ldb,
+                     const TR *beta, TR *c, const int64_t *ldc)
+{
+    mw::gemm_entry<int64_t>("mgemm_plain", false, MWBLAS_GEMM_PLAIN, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta,
+                            c, ldc);
+}
+
+void mgemm_ozaki_64_(const char *ta, const char *tb, const int64_t *m, const int64_t *n, const int64_t *k,
+                     const TR *alpha, const TR *a, const int64_t *lda, const TR *b, const int64_t *ldb,
+                     const TR *beta, TR *c, const int64_t *ldc)
+{
+    mw::gemm_entry<int64_t>("mgemm_ozaki", false, MWBLAS_GEMM_OZAKI, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta,
+                            c, ldc);
+}
+
+int mwblas_set_gemm_engine(int engine)
+{
+    int prev = mw::engine();
+    if (engine >= MWBLAS_GEMM_AUTO && engine <= MWBLAS_GEMM_OZAKI) mw::g_engine = engine;
+    return prev;
+}
+int mwblas_get_gemm_engine(void) { return mw::engine(); }
+int mwblas_set_ozaki_bits(int bits)
+{
+    int prev = mw::g_ozaki_bits;
+    mw::g_ozaki_bits = bits < 0 ? 0 : bits;
+    return prev;
+}
+int mwblas_last_ozaki_moduli(void) { return mw::ozaki_last_moduli(); }
+
+// ---- level 1 -----------------------------------------------------------------------------
+
+void mscal_(const int *n, const TR *alpha, TR *x, const int *incx) { mw::scal_entry<int>("mscal", 0, n, alpha, x, incx); }
+void mscal_64_(const int64_t *n, const TR *alpha, TR *x, const int64_t *incx)
+{
+    mw::scal_entry<int64_t>("mscal", 0, n, alpha, x, incx);
+}
+void wscal_(const int *n, const TC *alpha, TC *x, const int *incx) { mw::scal_entry<int>("wscal", 1, n, alpha, x, incx); }
+void wscal_64_(const int64_t *n, const TC *alpha, TC *x, const int64_t *incx)
+{
+    mw::scal_entry<int64_t>("wscal", 1, n, alpha, x, incx);
+}
+void wmscal_(const int *n, const TR *alpha, TC *x, const int *incx) { mw::scal_entry<int>("wmscal", 2, n, alpha, x, incx); }
+void wmscal_64_(const int64_t *n, const TR *alpha, TC *x, const int64_t *incx)
+{
+    mw::scal_entry<int64_t>("wmscal", 2, n, alpha, x, incx);
+}
+
+void maxpy_(const int *n, const TR *alpha, const TR *x, const int *incx, TR *y, const int *incy)
+{
+    mw::axpy_entry<int>("maxpy", n, alpha, x, incx, y, incy);
+}
+void maxpy_64_(const int64_t *n, const TR *alpha, const TR *x, const int64_t *incx, TR *y, const int64_t *incy)
+{
+    mw::axpy_entry<int64_t>("maxpy", n, alpha, x, incx, y, incy);
+}
+
+void mcopy_(const int *n, const TR *x, const int *incx, TR *y, const int *incy)
+{
+    mw::copy_entry<int>("mcopy", false, n, x, incx, y, incy);
+}
+void mcopy_64_(const int64_t *n, const TR *x, const int64_t *incx, TR *y, const int64_t *incy)
+{
+    mw::copy_entry<int64_t>("mcopy", false, n, x, incx, y, incy);
+}
+void wcopy_(const int *n, const TC *x, const int *incx, TC *y, const int *incy)
+{
+    mw::copy_entry<int>("wcopy", true, n, x, incx, y, incy);
+}
+void wcopy_64_(const int64_t *n, const TC *x, const int64_t *incx, TC *y, const int64_t *incy)
+{
+    mw::copy_entry<int64_t>("wcopy", true, n, x, incx, y, incy);
+}
+
+void mswap_(const int *n, TR *x, const int *incx, TR *y, const int *incy)
+{
+    mw::swap_entry<int>("mswap", false, n, x, incx, y, incy);
+}
+void mswap_64_(const int64_t *n, TR *x, const int64_t *incx, TR *y, const int64_t *incy)
+{
+    mw::swap_entry<int64_t>("mswap", false, n, x, incx, y, incy);
+}
+void wswap_(const int *n, TC *x, const int *incx, TC *y, const int *incy)
+{
+    mw::swap_entry<int>("wswap", true, n, x, incx, y, incy);
+}
+void wswap_64_(const int64_t *n, TC *x, const int64_t *incx, TC *y, const int64_t *incy)
+{
+    mw::swap_entry<int64_t>("wswap", true, n, x, incx, y, incy);
+}
+
+int imamax_(const int *n, const TR *x, const int *incx) { return (int)mw::iamax_entry<int>("imamax", false, n, x, incx); }
+int64_t imamax_64_(const int64_t *n, const TR *x, const int64_t *incx)
+{
+    return mw::iamax_entry<int64_t>("imamax", false, n, x, incx);
+}
+int iwamax_(const int *n, const TC *x, const int *incx) { return (int)mw::iamax_entry<int>("iwamax", true, n, x, incx); }
+int64_t iwamax_64_(const int64_t *n, const TC *x, const int64_t *incx)
+{
+    return mw::iamax_entry<int64_t>("iwamax", true, n, x, incx);
+}
+
+TR mdot_(const int *n, const TR *x, const int *incx, const TR *y, const int *incy)
+{
+    return mw::dot_entry<int>("mdot", n, x, incx, y, incy);
+}
+TR mdot_64_(const int64_t *n, const TR *x, const int64_t *incx, const TR *y, const int64_t *incy)
+{
+    return mw::dot_entry<int64_t>("mdot", n, x, incx, y, incy);
+}
+
+}  // extern "C"

@@ -1,0 +1,154 @@
+// Double-double GEMV: y := alpha*op(A)*x + beta*y (mgemv.cpp:237-275).
+//
+// beta pre-pass first (mf_kernels.h:63-68: beta == 0 zeroes y, beta == 1
+// leaves it), then nothing more when alpha == 0, as in the reference.
+//
+// NoTrans: thread per row, the columns split into chunks over grid.y so the
+// whole GPU streams A once; per-chunk partial sums go to scratch and a second
+// kernel folds them in a fixed order and applies y += alpha*s.
+// Trans: block per column (A's columns are contiguous), warp-shuffle and
+// shared-memory reduction, then y_j += alpha*s (mgemv.cpp:229-233).
+// Products accumulate as TwoProduct + TwoSum into a (sum, error) pair,
+// renormalised every 32 terms, the lo*lo product dropped as in mdot.cpp:60-64.
+#include "dd.cuh"
+#include "level3.h"
+#include "runtime.h"
+
+namespace mw {
+
+namespace {
+
+__device__ __forceinline__ int64_t vidx(int64_t i, int64_t n, int64_t inc)
+{
+    return inc >= 0 ? i * inc : (n - 1 - i) * (-inc);
+}
+
+__device__ __forceinline__ void acc_prod(double &s, double &e, double2 a, double2 b)
+{
+    double p, pe, t;
+    dd::two_prod(a.x, b.x, p, pe);
+    e = __fma_rn(a.x, b.y, e);
+    e = __fma_rn(a.y, b.x, e);
+    e = __dadd_rn(e, pe);
+    dd::two_sum(s, p, s, t);
+    e = __dadd_rn(e, t);
+}
+
+__global__ void k_scale_vec(int64_t n, dd::real beta, int beta_kind, double2 *y, int64_t incy)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 *p = y + vidx(i, n, incy);
+        if (beta_kind == 0) *p = make_double2(0.0, 0.0);
+        else dd::store(p, dd::mul_exact(beta, dd::load(p)));
+    }
+}
+
+__global__ void k_gemv_n_partial(int64_t m, int64_t n, const double2 *A, int64_t lda, const double2 *x, int64_t incx,
+                                 int64_t chunk, double2 *part)
+{
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+    double s = 0.0, e = 0.0;
+    int cnt = 0;
+    for (int64_t j = j0; j < j1; ++j) {
+        acc_prod(s, e, A[i + j * lda], x[vidx(j, n, incx)]);
+        if (++cnt == 32) {
+            dd::fast_two_sum(s, e, s, e);
+            cnt = 0;
+        }
+    }
+    double h, l;
+    dd::two_sum(s, e, h, l);
+    part[blockIdx.y * m + i] = make_double2(h, l);
+}
+
+__global__ void k_gemv_n_final(int64_t m, int nchunks, const double2 *part, dd::real alpha, double2 *y,
+                               int64_t incy)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        dd::real s = dd::load(part + i);
+        for (int c = 1; c < nchunks; ++c) s = dd::add_fast(s, dd::load(part + (int64_t)c * m + i));
+        double2 *py = y + vidx(i, m, incy);
+        dd::store(py, dd::add_exact(dd::load(py), dd::mul_exact(alpha, s)));
+    }
+}
+
+__global__ void k_gemv_t(int64_t m, int64_t n, const double2 *A, int64_t lda, const double2 *x, int64_t incx,
+                         dd::real alpha, double2 *y, int64_t incy)
+{
+    __shared__ double2 sh[32];
+    int64_t j = blockIdx.x;
+    const double2 *col = A + j * lda;
+    double s = 0.0, e = 0.0;
+    int cnt = 0;
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+        acc_prod(s, e, col[i], x[vidx(i, m, incx)]);
+        if (++cnt == 32) {
+            dd::fast_two_sum(s, e, s, e);
+            cnt = 0;
+        }
+    }
+    dd::real v;
+    dd::two_sum(s, e, v.hi, v.lo);
+    for (int off = 16; off > 0; off >>= 1)
+        v = dd::add_fast(v, dd::make(__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)));
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = make_double2(v.hi, v.lo);
+    __syncthreads();
+    if (wid == 0) {
+        v = (lane < (int)(blockDim.x >> 5)) ? dd::load(&sh[lane]) : dd::make(0.0, 0.0);
+        for (int off = 16; off > 0; off >>= 1)
+            v = dd::add_fast(v,
+                             dd::make(__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)));
+        if (lane == 0) {
+            double2 *py = y + vidx(j, n, incy);
+            dd::store(py, dd::add_exact(dd::load(py), dd::mul_exact(alpha, v)));
+        }
+    }
+}
+
+}  // namespace
+
+bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A, int64_t lda, const void *x,
+                 int64_t incx, dd_host beta, int beta_kind, void *y, int64_t incy, const char *routine)
+{
+    int64_t leny = trans ? n : m;
+    int sms = device_sm_count();
+    if (beta_kind != 1) {
+        int64_t blocks = (leny + 255) / 256;
+        if (blocks > sms * 8) blocks = sms * 8;
+        k_scale_vec<<<(unsigned)blocks, 256, 0, stream()>>>(leny, dd::make(beta.hi, beta.lo), beta_kind, (double2 *)y,
+                                                            incy);
+        count_launch();
+    }
+    if (alpha.hi == 0.0 && alpha.lo == 0.0) return true;
+    dd::real al = dd::make(alpha.hi, alpha.lo);
+    if (!trans) {
+        int64_t rowblocks = (m + 255) / 256;
+        int64_t want = 4 * (int64_t)sms;
+        int64_t nchunks = (want + rowblocks - 1) / rowblocks;
+        if (nchunks > n) nchunks = n;
+        if (nchunks > 4096) nchunks = 4096;
+        if (nchunks < 1) nchunks = 1;
+        int64_t chunk = (n + nchunks - 1) / nchunks;
+        nchunks = (n + chunk - 1) / chunk;
+        double2 *part = (double2 *)dev_alloc(sizeof(double2) * (size_t)(nchunks * m), routine);
+        if (!part) return false;
+        dim3 grid((unsigned)rowblocks, (unsigned)nchunks);
+        k_gemv_n_partial<<<grid, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, (const double2 *)x, incx, chunk,
+                                                     part);
+        int64_t fb = (m + 255) / 256;
+        if (fb > sms * 8) fb = sms * 8;
+        k_gemv_n_final<<<(unsigned)fb, 256, 0, stream()>>>(m, (int)nchunks, part, al, (double2 *)y, incy);
+        count_launch(2);
+        dev_free(part);
+    } else {
+        k_gemv_t<<<(unsigned)n, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, (const double2 *)x, incx, al,
+                                                    (double2 *)y, incy);
+        count_launch();
+    }
+    return true;
+}
+
+}  // namespace mw

@@ -1,0 +1,469 @@
+// Level-1 double-double kernels: SCAL, AXPY, COPY, SWAP, I*AMAX, DOT and the
+// complex twins.
+//
+// Bit-exactness. The reference's unit-stride SCAL/AXPY run the FMA-fused
+// "fast" product on the first (len & ~3) elements of each OpenMP slice and the
+// scalar-operator product on the remaining 0..3 (mscal.cpp:42-58,
+// maxpy.cpp:42-58, wscal.cpp, wmscal.cpp), where the slices are the balanced
+// front-loaded partition of blas_part_bound (common/blas_omp.h:79-84). Every
+// element is independent, so a kernel that knows the team size T reproduces
+// the same per-element operation sequence on any grid: element i is a "tail"
+// element iff its offset inside its slice is >= (slice length & ~3).
+// Strided calls use the scalar operators for every element (mscal.cpp:96-100).
+// A zero increment on an output makes the reference's loop sequential
+// (the same element is updated n times in order); those calls run a
+// single-thread kernel that repeats the loop literally.
+#include "dd.cuh"
+#include "l1.h"
+#include "runtime.h"
+
+namespace mw {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+// Offset of logical element i for a BLAS vector (negative inc starts at the
+// far end).
+__device__ __forceinline__ int64_t vidx(int64_t i, int64_t n, int64_t inc)
+{
+    return inc >= 0 ? i * inc : (n - 1 - i) * (-inc);
+}
+
+// True when element i (0-based, unit stride) falls in the scalar tail of its
+// slice under a T-way blas_part_bound partition of [0, n).
+__device__ __forceinline__ bool in_tail(int64_t i, int64_t n, int64_t T)
+{
+    int64_t base = n / T, rem = n % T;
+    int64_t lo, len;
+    int64_t big = rem * (base + 1);
+    if (i < big) {
+        int64_t t = i / (base + 1);
+        lo = t * (base + 1);
+        len = base + 1;
+    } else {
+        int64_t t = rem + (i - big) / base;
+        lo = t * base + rem;
+        len = base;
+    }
+    return (i - lo) >= (len & ~(int64_t)3);
+}
+
+int grid_for(int64_t n)
+{
+    int64_t blocks = (n + kThreads - 1) / kThreads;
+    int64_t cap = (int64_t)device_sm_count() * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (int)blocks;
+}
+
+// ---- SCAL ----------------------------------------------------------------
+
+__global__ void k_mscal_unit(int64_t n, dd::real alpha, double2 *x, int64_t T)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        dd::real v = dd::load(x + i);
+        v = in_tail(i, n, T) ? dd::mul_exact(v, alpha) : dd::mul_fast(v, alpha);
+        dd::store(x + i, v);
+    }
+}
+
+__global__ void k_mscal_strided(int64_t n, dd::real alpha, double2 *x, int64_t inc)
+{
+    if (inc == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            dd::real v = dd::load(x);
+            for (int64_t i = 0; i < n; ++i) v = dd::mul_exact(v, alpha);
+            dd::store(x, v);
+        }
+        return;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 *p = x + vidx(i, n, inc);
+        dd::store(p, dd::mul_exact(dd::load(p), alpha));
+    }
+}
+
+__global__ void k_wscal_unit(int64_t n, dd::cplx alpha, double2 *x, int64_t T)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        dd::cplx v = dd::cload(x + 2 * i);
+        v = in_tail(i, n, T) ? dd::cmul_exact(v, alpha) : dd::cmul_fast(v, alpha);
+        dd::cstore(x + 2 * i, v);
+    }
+}
+
+__global__ void k_wscal_strided(int64_t n, dd::cplx alpha, double2 *x, int64_t inc)
+{
+    if (inc == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            dd::cplx v = dd::cload(x);
+            for (int64_t i = 0; i < n; ++i) v = dd::cmul_exact(v, alpha);
+            dd::cstore(x, v);
+        }
+        return;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 *p = x + 2 * vidx(i, n, inc);
+        dd::cstore(p, dd::cmul_exact(dd::cload(p), alpha));
+    }
+}
+
+__global__ void k_wmscal_unit(int64_t n, dd::real alpha, double2 *x, int64_t T)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        dd::cplx v = dd::cload(x + 2 * i);
+        if (in_tail(i, n, T)) {
+            v.re = dd::mul_exact(v.re, alpha);
+            v.im = dd::mul_exact(v.im, alpha);
+        } else {
+            v.re = dd::mul_fast(v.re, alpha);
+            v.im = dd::mul_fast(v.im, alpha);
+        }
+        dd::cstore(x + 2 * i, v);
+    }
+}
+
+__global__ void k_wmscal_strided(int64_t n, dd::real alpha, double2 *x, int64_t inc)
+{
+    if (inc == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            dd::cplx v = dd::cload(x);
+            for (int64_t i = 0; i < n; ++i) {
+                v.re = dd::mul_exact(v.re, alpha);
+                v.im = dd::mul_exact(v.im, alpha);
+            }
+            dd::cstore(x, v);
+        }
+        return;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 *p = x + 2 * vidx(i, n, inc);
+        dd::cplx v = dd::cload(p);
+        v.re = dd::mul_exact(v.re, alpha);
+        v.im = dd::mul_exact(v.im, alpha);
+        dd::cstore(p, v);
+    }
+}
+
+// ---- AXPY ------------------------------------------------------------------
+
+__global__ void k_maxpy_unit(int64_t n, dd::real alpha, const double2 *x, double2 *y, int64_t T)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        dd::real xv = dd::load(x + i), yv = dd::load(y + i);
+        dd::real r;
+        if (in_tail(i, n, T))
+            r = dd::add_exact(yv, dd::mul_exact(alpha, xv));
+        else
+            r = dd::add_fast(yv, dd::mul_fast(alpha, xv));
+        dd::store(y + i, r);
+    }
+}
+
+__global__ void k_maxpy_strided(int64_t n, dd::real alpha, const double2 *x, int64_t incx, double2 *y,
+                                int64_t incy)
+{
+    if (incy == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            dd::real yv = dd::load(y);
+            for (int64_t i = 0; i < n; ++i)
+                yv = dd::add_exact(yv, dd::mul_exact(alpha, dd::load(x + vidx(i, n, incx))));
+            dd::store(y, yv);
+        }
+        return;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 *py = y + vidx(i, n, incy);
+        dd::real xv = dd::load(x + vidx(i, n, incx));
+        dd::store(py, dd::add_exact(dd::load(py), dd::mul_exact(alpha, xv)));
+    }
+}
+
+// ---- COPY / SWAP -----------------------------------------------------------
+
+// elem2 = number of double2 words per element (1 real, 2 complex).
+__global__ void k_copy(int64_t n, const double2 *x, int64_t incx, double2 *y, int64_t incy, int elem2)
+{
+    if (incy == 0) {
+        // Sequential reference loop: the last logical element wins.
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            const double2 *src = x + elem2 * vidx(n - 1, n, incx);
+            for (int w = 0; w < elem2; ++w) y[w] = src[w];
+        }
+        return;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 *src = x + elem2 * vidx(i, n, incx);
+        double2 *dst = y + elem2 * vidx(i, n, incy);
+        for (int w = 0; w < elem2; ++w) dst[w] = src[w];
+    }
+}
+
+__global__ void k_swap(int64_t n, double2 *x, int64_t incx, double2 *y, int64_t incy, int elem2)
+{
+    if (incx == 0 || incy == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            for (int64_t i = 0; i < n; ++i) {
+                double2 *px = x + elem2 * vidx(i, n, incx);
+                double2 *py = y + elem2 * vidx(i, n, incy);
+                for (int w = 0; w < elem2; ++w) {
+                    double2 t = px[w];
+                    px[w] = py[w];
+                    py[w] = t;
+                }
+            }
+        }
+        return;
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 *px = x + elem2 * vidx(i, n, incx);
+        double2 *py = y + elem2 * vidx(i, n, incy);
+        for (int w = 0; w < elem2; ++w) {
+            double2 t = px[w];
+            px[w] = py[w];
+            py[w] = t;
+        }
+    }
+}
+
+// ---- I*AMAX ------------------------------------------------------------------
+// Key: lexicographic (|hi|, sign-adjusted lo) maximum, lowest index on ties
+// (imamax.cpp:43-72, mf_pred.h:60-63). Complex magnitude |re|+|im| uses the
+// scalar-operator add (iwamax.cpp:36-76).
+
+struct AmaxKey {
+    double h, l;
+    int64_t idx;   // 0-based; -1 = empty
+};
+
+__device__ __forceinline__ bool amax_better(const AmaxKey &a, const AmaxKey &b)
+{
+    if (a.idx < 0) return false;
+    if (b.idx < 0) return true;
+    if (a.h > b.h || (a.h == b.h && a.l > b.l)) return true;
+    if (a.h == b.h && a.l == b.l && a.idx < b.idx) return true;
+    return false;
+}
+
+__device__ __forceinline__ AmaxKey amax_shfl(const AmaxKey &k, int off)
+{
+    AmaxKey r;
+    r.h = __shfl_down_sync(0xffffffffu, k.h, off);
+    r.l = __shfl_down_sync(0xffffffffu, k.l, off);
+    r.idx = __shfl_down_sync(0xffffffffu, k.idx, off);
+    return r;
+}
+
+__device__ AmaxKey amax_block_reduce(AmaxKey k)
+{
+    __shared__ AmaxKey sh[kThreads / 32];
+    for (int off = 16; off > 0; off >>= 1) {
+        AmaxKey o = amax_shfl(k, off);
+        if (amax_better(o, k)) k = o;
+    }
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = k;
+    __syncthreads();
+    if (wid == 0) {
+        k = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : AmaxKey{0.0, 0.0, -1};
+        for (int off = 16; off > 0; off >>= 1) {
+            AmaxKey o = amax_shfl(k, off);
+            if (amax_better(o, k)) k = o;
+        }
+    }
+    return k;
+}
+
+template <bool CPLX>
+__global__ void k_iamax_partial(int64_t n, const double2 *x, int64_t inc, AmaxKey *part)
+{
+    AmaxKey best{0.0, 0.0, -1};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        dd::real m;
+        if (CPLX) {
+            const double2 *p = x + 2 * vidx(i, n, inc);
+            m = dd::add_exact(dd::mag(dd::load(p)), dd::mag(dd::load(p + 1)));
+        } else {
+            m = dd::mag(dd::load(x + vidx(i, n, inc)));
+        }
+        AmaxKey c{m.hi, m.lo, i};
+        if (amax_better(c, best)) best = c;
+    }
+    best = amax_block_reduce(best);
+    if (threadIdx.x == 0) part[blockIdx.x] = best;
+}
+
+__global__ void k_iamax_final(int nparts, const AmaxKey *part, int64_t *out)
+{
+    AmaxKey best{0.0, 0.0, -1};
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x)
+        if (amax_better(part[i], best)) best = part[i];
+    best = amax_block_reduce(best);
+    if (threadIdx.x == 0) *out = best.idx;
+}
+
+// ---- DOT ---------------------------------------------------------------------
+// Per-thread double-double accumulation (TwoProduct + TwoSum, the lo x lo
+// product dropped as in mdot.cpp:60-64), renormalised every 32 elements; block
+// and grid partials combine with the fast DD add in a fixed order, so the
+// result is deterministic for a given n and device.
+
+__device__ __forceinline__ dd::real dd_shfl(dd::real v, int off)
+{
+    return dd::make(__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off));
+}
+
+__device__ dd::real dd_block_sum(dd::real v)
+{
+    __shared__ double2 sh[kThreads / 32];
+    for (int off = 16; off > 0; off >>= 1) v = dd::add_fast(v, dd_shfl(v, off));
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = make_double2(v.hi, v.lo);
+    __syncthreads();
+    if (wid == 0) {
+        v = (lane < (int)(blockDim.x >> 5)) ? dd::load(&sh[lane]) : dd::make(0.0, 0.0);
+        for (int off = 16; off > 0; off >>= 1) v = dd::add_fast(v, dd_shfl(v, off));
+    }
+    return v;
+}
+
+__global__ void k_mdot_partial(int64_t n, const double2 *x, int64_t incx, const double2 *y, int64_t incy,
+                               double2 *part)
+{
+    double s = 0.0, e = 0.0;
+    int cnt = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double2 xv = x[vidx(i, n, incx)];
+        double2 yv = y[vidx(i, n, incy)];
+        double p, pe, t;
+        dd::two_prod(xv.x, yv.x, p, pe);
+        e = __fma_rn(xv.x, yv.y, e);
+        e = __fma_rn(xv.y, yv.x, e);
+        e = __dadd_rn(e, pe);
+        dd::two_sum(s, p, s, t);
+        e = __dadd_rn(e, t);
+        if (++cnt == 32) {
+            dd::fast_two_sum(s, e, s, e);
+            cnt = 0;
+        }
+    }
+    dd::real acc;
+    dd::two_sum(s, e, acc.hi, acc.lo);
+    acc = dd_block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = make_double2(acc.hi, acc.lo);
+}
+
+__global__ void k_mdot_final(int nparts, const double2 *part, double2 *out)
+{
+    dd::real acc = dd::make(0.0, 0.0);
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc = dd::add_fast(acc, dd::load(part + i));
+    acc = dd_block_sum(acc);
+    if (threadIdx.x == 0) *out = make_double2(acc.hi, acc.lo);
+}
+
+}  // namespace
+
+// ---- launchers ---------------------------------------------------------------
+
+void launch_mscal(int64_t n, dd_host alpha, void *x, int64_t inc, int64_t team)
+{
+    dd::real a = dd::make(alpha.hi, alpha.lo);
+    if (inc == 1)
+        k_mscal_unit<<<grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, team);
+    else
+        k_mscal_strided<<<inc == 0 ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, inc);
+    count_launch();
+}
+
+void launch_wscal(int64_t n, cdd_host alpha, void *x, int64_t inc, int64_t team)
+{
+    dd::cplx a;
+    a.re = dd::make(alpha.re.hi, alpha.re.lo);
+    a.im = dd::make(alpha.im.hi, alpha.im.lo);
+    if (inc == 1)
+        k_wscal_unit<<<grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, team);
+    else
+        k_wscal_strided<<<inc == 0 ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, inc);
+    count_launch();
+}
+
+void launch_wmscal(int64_t n, dd_host alpha, void *x, int64_t inc, int64_t team)
+{
+    dd::real a = dd::make(alpha.hi, alpha.lo);
+    if (inc == 1)
+        k_wmscal_unit<<<grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, team);
+    else
+        k_wmscal_strided<<<inc == 0 ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, inc);
+    count_launch();
+}
+
+void launch_maxpy(int64_t n, dd_host alpha, const void *x, int64_t incx, void *y, int64_t incy, int64_t team)
+{
+    dd::real a = dd::make(alpha.hi, alpha.lo);
+    if (incx == 1 && incy == 1)
+        k_maxpy_unit<<<grid_for(n), kThreads, 0, stream()>>>(n, a, (const double2 *)x, (double2 *)y, team);
+    else
+        k_maxpy_strided<<<incy == 0 ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, a, (const double2 *)x, incx,
+                                                                               (double2 *)y, incy);
+    count_launch();
+}
+
+void launch_copy(int64_t n, const void *x, int64_t incx, void *y, int64_t incy, int elem2)
+{
+    k_copy<<<incy == 0 ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, (const double2 *)x, incx, (double2 *)y,
+                                                                  incy, elem2);
+    count_launch();
+}
+
+void launch_swap(int64_t n, void *x, int64_t incx, void *y, int64_t incy, int elem2)
+{
+    bool seq = (incx == 0 || incy == 0);
+    k_swap<<<seq ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, (double2 *)x, incx, (double2 *)y, incy, elem2);
+    count_launch();
+}
+
+bool launch_iamax(int64_t n, const void *x, int64_t inc, bool cplx, int64_t *result_host, const char *routine)
+{
+    int g = grid_for(n);
+    size_t bytes = (size_t)g * sizeof(AmaxKey) + 64;
+    char *scratch = (char *)dev_alloc(bytes, routine);
+    if (!scratch) return false;
+    AmaxKey *part = (AmaxKey *)scratch;
+    int64_t *out = (int64_t *)(scratch + (((size_t)g * sizeof(AmaxKey) + 15) / 16) * 16);
+    if (cplx)
+        k_iamax_partial<true><<<g, kThreads, 0, stream()>>>(n, (const double2 *)x, inc, part);
+    else
+        k_iamax_partial<false><<<g, kThreads, 0, stream()>>>(n, (const double2 *)x, inc, part);
+    k_iamax_final<<<1, kThreads, 0, stream()>>>(g, part, out);
+    count_launch(2);
+    bool ok = cuda_ok(cudaMemcpyAsync(result_host, out, sizeof(int64_t), cudaMemcpyDeviceToHost, stream()), routine,
+                      "iamax result readback");
+    dev_free(scratch);
+    if (!ok) return false;
+    return cuda_ok(cudaStreamSynchronize(stream()), routine, "iamax sync");
+}
+
+bool launch_mdot(int64_t n, const void *x, int64_t incx, const void *y, int64_t incy, dd_host *result_host,
+                 const char *routine)
+{
+    int g = grid_for(n);
+    size_t bytes = (size_t)(g + 1) * sizeof(double2);
+    double2 *part = (double2 *)dev_alloc(bytes, routine);
+    if (!part) return false;
+    k_mdot_partial<<<g, kThreads, 0, stream()>>>(n, (const double2 *)x, incx, (const double2 *)y, incy, part);
+    k_mdot_final<<<1, kThreads, 0, stream()>>>(g, part, part + g);
+    count_launch(2);
+    double2 r;
+    bool ok = cuda_ok(cudaMemcpyAsync(&r, part + g, sizeof(double2), cudaMemcpyDeviceToHost, stream()), routine,
+                      "dot result readback");
+    dev_free(part);
+    if (!ok) return false;
+    if (!cuda_ok(cudaStreamSynchronize(stream()), routine, "dot sync")) return false;
+    result_host->hi = r.x;
+    result_host->lo = r.y;
+    return true;
+}
+
+}  // namespace mw

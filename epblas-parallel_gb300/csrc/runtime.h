@@ -1,0 +1,108 @@
+// Host runtime shared by every entry point of libmwblas_gb300.so.
+//
+// The reference library is a plain synchronous BLAS over host memory with no
+// handles and no argument checking (src/epblas-parallel/common/
+// epblas_facade.h:1-56). This runtime keeps that calling model: every entry
+// point returns with its outputs complete. Around it, it adds what a GPU
+// implementation needs:
+//   * per-host-thread stream (cudaStreamPerThread unless the caller set one);
+//   * stream-ordered device scratch from the device's default memory pool;
+//   * staging of host arrays into device memory and back (pointers the
+//     caller already has on the device are used in place);
+//   * a thread-local last-error record plus an optional error hook, because
+//     a GPU call can fail where the CPU reference could not.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/mwblas_gb300.h"
+
+namespace mw {
+
+// ---- errors ---------------------------------------------------------------
+
+// Records (routine, info, message) as this thread's last error and calls the
+// user hook if one is installed. info > 0: position of a bad argument
+// (Netlib convention). info < 0: MWBLAS_ERR_* runtime failure.
+void set_error(const char *routine, int info, const std::string &message);
+void clear_error();
+
+// Checks a CUDA runtime status; on failure records it against `routine` and
+// returns false.
+bool cuda_ok(cudaError_t st, const char *routine, const char *what);
+
+// ---- context ----------------------------------------------------------------
+
+cudaStream_t stream();
+bool sync_on_return();
+int device_sm_count();
+// Ensures a CUDA device is present and the per-device runtime is set up.
+bool ensure_device(const char *routine);
+
+// ---- device memory ----------------------------------------------------------
+
+// Stream-ordered allocation from the current device's pool. Returns nullptr
+// and records MWBLAS_ERR_ALLOC on failure (also when the allocation-failure
+// test hook fires).
+void *dev_alloc(size_t bytes, const char *routine);
+void dev_free(void *p);
+
+// True when the pointer is device or managed memory that kernels may use.
+bool is_device_pointer(const void *p);
+
+// A device view of a caller array. If the caller's pointer is already device
+// memory it is used in place; otherwise a scratch copy is made.
+struct Staged {
+    void *dev = nullptr;       // device address kernels use
+    const void *host = nullptr;
+    bool owned = false;        // scratch allocated by us
+    size_t elem = 0;
+    int64_t rows = 0, cols = 0, ld = 0;   // matrix shape (column-major)
+    int64_t n = 0, inc = 0;               // vector shape
+    bool is_vector = false;
+};
+
+// Matrix rows x cols with leading dimension ld (elements of `elem` bytes).
+// copy_in=false allocates without copying (pure outputs).
+bool stage_matrix(Staged &s, const void *host, int64_t rows, int64_t cols, int64_t ld,
+                  size_t elem, bool copy_in, const char *routine);
+// Writes a staged matrix back (only the rows x cols block; padding rows of the
+// caller's array are never written).
+bool unstage_matrix(Staged &s, const char *routine);
+
+// Vector of n logical elements with increment inc (BLAS convention: a
+// negative increment starts at the far end). A staged host vector is
+// compacted; the device increment is returned in `dev_inc` (+1, -1 or 0).
+bool stage_vector(Staged &s, const void *host, int64_t n, int64_t inc, size_t elem,
+                  bool copy_in, int64_t &dev_inc, const char *routine);
+bool unstage_vector(Staged &s, const char *routine);
+
+void release(Staged &s);
+
+// Synchronises the library stream when the call is synchronous; records any
+// asynchronous error against `routine`.
+bool finish(const char *routine);
+
+// ---- reference threading policy --------------------------------------------
+
+// Team size the reference would use for a threaded level-1 sweep of n
+// elements with threshold `omp_min` (the *_OMP_MIN constants of the reference
+// L1 files). Reproduces blas_omp_should_thread() (common/blas_omp.h:59-65):
+// 1 when n <= omp_min, when the OpenMP runtime reports a single thread, or
+// when the caller is already inside a parallel region. A value set through
+// mwblas_set_l1_partition() overrides the runtime query.
+int64_t l1_team(int64_t n, int64_t omp_min);
+
+// ---- launch bookkeeping -----------------------------------------------------
+
+// Counts kernel launches issued by the library (for benchmarking claims).
+void count_launch(int64_t k = 1);
+
+// Device-side status word that bounded device waits write to on timeout.
+int *device_status_word();
+bool check_device_status(const char *routine);
+
+}  // namespace mw

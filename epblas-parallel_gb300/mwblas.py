@@ -1,0 +1,259 @@
+"""ctypes binding of the mwblas C ABI (include/mwblas_gb300.h).
+
+The binding is written against the Fortran-style symbols, so the same class
+drives any library that exports them: libmwblas_gb300.so (the GB300 library),
+or a build of the reference epblas-parallel mwblas. This is the binding a
+Python caller of the reference would write; INTEGRATION.md shows it.
+
+Double-double arrays are numpy float64 arrays whose last axis holds the two
+limbs (hi, lo). A column-major m x n matrix with leading dimension ld is a
+C-ordered numpy array of shape (n, ld, 2) (element (i, j) at [j, i]); complex
+matrices have shape (n, ld, 2, 2) ([..., 0, :] real part, [..., 1, :]
+imaginary part). Arrays may also be passed as raw integer addresses (device
+pointers from torch, for example).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_LIB = os.path.join(HERE, "libmwblas_gb300.so")
+
+
+class Real64x2(C.Structure):
+    _fields_ = [("limbs", C.c_double * 2)]
+
+    def to_tuple(self):
+        return (self.limbs[0], self.limbs[1])
+
+
+class Complex64x2(C.Structure):
+    _fields_ = [("re", Real64x2), ("im", Real64x2)]
+
+
+_i64 = C.c_int64
+_i32 = C.c_int
+_p = C.c_void_p
+_ch = C.c_char_p
+
+
+def _ptr(a):
+    """Address of a numpy array / torch tensor / integer / None."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+def real(x) -> Real64x2:
+    """Real64x2 from a float, a (hi, lo) pair or a numpy array of two."""
+    if isinstance(x, Real64x2):
+        return x
+    if np.ndim(x) == 0:
+        return Real64x2((C.c_double * 2)(float(x), 0.0))
+    a = np.asarray(x, dtype=np.float64).reshape(2)
+    return Real64x2((C.c_double * 2)(a[0], a[1]))
+
+
+def cplx(x) -> Complex64x2:
+    """Complex64x2 from a python complex or an array of shape (2, 2)."""
+    if isinstance(x, Complex64x2):
+        return x
+    if isinstance(x, complex) or np.ndim(x) == 0:
+        z = complex(x)
+        return Complex64x2(real(z.real), real(z.imag))
+    a = np.asarray(x, dtype=np.float64).reshape(2, 2)
+    return Complex64x2(real(a[0]), real(a[1]))
+
+
+class MWBlas:
+    """Binding of one library exporting the mwblas Fortran-style ABI."""
+
+    def __init__(self, path: str = DEFAULT_LIB, extensions: bool = True):
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"{path} not found (build it first)")
+        self.path = path
+        self.lib = C.CDLL(path, mode=C.RTLD_GLOBAL)
+        L = self.lib
+        R, Cx = C.POINTER(Real64x2), C.POINTER(Complex64x2)
+        for suf, I in (("_", _i32), ("_64_", _i64)):
+            PI = C.POINTER(I)
+            self._sig("mgemm" + suf, None, [_ch, _ch, PI, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
+            self._sig("wgemm" + suf, None, [_ch, _ch, PI, PI, PI, Cx, _p, PI, _p, PI, Cx, _p, PI])
+            self._sig("msyrk" + suf, None, [_ch, _ch, PI, PI, R, _p, PI, R, _p, PI])
+            self._sig("wherk" + suf, None, [_ch, _ch, PI, PI, R, _p, PI, R, _p, PI])
+            self._sig("mtrsm" + suf, None, [_ch, _ch, _ch, _ch, PI, PI, R, _p, PI, _p, PI])
+            self._sig("mgemv" + suf, None, [_ch, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
+            self._sig("mdot" + suf, Real64x2, [PI, _p, PI, _p, PI])
+            self._sig("maxpy" + suf, None, [PI, R, _p, PI, _p, PI])
+            self._sig("mscal" + suf, None, [PI, R, _p, PI])
+            self._sig("wscal" + suf, None, [PI, Cx, _p, PI])
+            self._sig("wmscal" + suf, None, [PI, R, _p, PI])
+            self._sig("mcopy" + suf, None, [PI, _p, PI, _p, PI])
+            self._sig("wcopy" + suf, None, [PI, _p, PI, _p, PI])
+            self._sig("mswap" + suf, None, [PI, _p, PI, _p, PI])
+            self._sig("wswap" + suf, None, [PI, _p, PI, _p, PI])
+            self._sig("imamax" + suf, I, [PI, _p, PI])
+            self._sig("iwamax" + suf, I, [PI, _p, PI])
+        self.has_ext = extensions and hasattr(L, "mwblas_version")
+        if self.has_ext:
+            PI = C.POINTER(_i64)
+            self._sig("mgemm_plain_64_", None, [_ch, _ch, PI, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
+            self._sig("mgemm_ozaki_64_", None, [_ch, _ch, PI, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
+            self._sig("mwblas_set_gemm_engine", _i32, [_i32])
+            self._sig("mwblas_get_gemm_engine", _i32, [])
+            self._sig("mwblas_set_ozaki_bits", _i32, [_i32])
+            self._sig("mwblas_last_ozaki_moduli", _i32, [])
+            self._sig("mwblas_set_l1_partition", _i64, [_i64])
+            self._sig("mwblas_set_stream", _i32, [_p])
+            self._sig("mwblas_set_sync", _i32, [_i32])
+            self._sig("mwblas_last_error", _i32, [])
+            self._sig("mwblas_last_error_message", _ch, [])
+            self._sig("mwblas_last_error_routine", _ch, [])
+            self._sig("mwblas_clear_error", None, [])
+            self._sig("mwblas_debug_fail_alloc_after", None, [_i64])
+            self._sig("mwblas_launch_count", _i64, [])
+            self._sig("mwblas_version", _ch, [])
+            if hasattr(L, "mgemm_grouped"):
+                self._sig("mgemm_grouped", _i32,
+                          [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p])
+            if hasattr(L, "mtrsm_grouped"):
+                self._sig("mtrsm_grouped", _i32,
+                          [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p])
+
+    def _sig(self, name, res, args):
+        f = getattr(self.lib, name, None)
+        if f is None:
+            return
+        f.restype = res
+        f.argtypes = args
+
+    # ---- helpers -------------------------------------------------------------------------
+    @staticmethod
+    def _I(v, wide=True):
+        return C.byref(_i64(v) if wide else _i32(v))
+
+    def last_error(self):
+        if not self.has_ext:
+            return 0, ""
+        return self.lib.mwblas_last_error(), self.lib.mwblas_last_error_message().decode()
+
+    # ---- level 3 -----------------------------------------------------------------------
+    def mgemm(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, wide=True, engine=None):
+        I = lambda v: self._I(v, wide)
+        if engine is None:
+            f = self.lib.mgemm_64_ if wide else self.lib.mgemm_
+        else:
+            f = {"plain": self.lib.mgemm_plain_64_, "ozaki": self.lib.mgemm_ozaki_64_}[engine]
+            I = lambda v: self._I(v, True)
+        f(ta.encode(), tb.encode(), I(m), I(n), I(k), C.byref(real(alpha)), _ptr(a), I(lda), _ptr(b), I(ldb),
+          C.byref(real(beta)), _ptr(c), I(ldc))
+
+    def wgemm(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = self.lib.wgemm_64_ if wide else self.lib.wgemm_
+        f(ta.encode(), tb.encode(), I(m), I(n), I(k), C.byref(cplx(alpha)), _ptr(a), I(lda), _ptr(b), I(ldb),
+          C.byref(cplx(beta)), _ptr(c), I(ldc))
+
+    def msyrk(self, uplo, trans, n, k, alpha, a, lda, beta, c, ldc, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = self.lib.msyrk_64_ if wide else self.lib.msyrk_
+        f(uplo.encode(), trans.encode(), I(n), I(k), C.byref(real(alpha)), _ptr(a), I(lda), C.byref(real(beta)),
+          _ptr(c), I(ldc))
+
+    def wherk(self, uplo, trans, n, k, alpha, a, lda, beta, c, ldc, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = self.lib.wherk_64_ if wide else self.lib.wherk_
+        f(uplo.encode(), trans.encode(), I(n), I(k), C.byref(real(alpha)), _ptr(a), I(lda), C.byref(real(beta)),
+          _ptr(c), I(ldc))
+
+    def mtrsm(self, side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = self.lib.mtrsm_64_ if wide else self.lib.mtrsm_
+        f(side.encode(), uplo.encode(), transa.encode(), diag.encode(), I(m), I(n), C.byref(real(alpha)), _ptr(a),
+          I(lda), _ptr(b), I(ldb))
+
+    # ---- level 2 -----------------------------------------------------------------------
+    def mgemv(self, trans, m, n, alpha, a, lda, x, incx, beta, y, incy, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = self.lib.mgemv_64_ if wide else self.lib.mgemv_
+        f(trans.encode(), I(m), I(n), C.byref(real(alpha)), _ptr(a), I(lda), _ptr(x), I(incx), C.byref(real(beta)),
+          _ptr(y), I(incy))
+
+    # ---- level 1 -----------------------------------------------------------------------
+    def mdot(self, n, x, incx, y, incy, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = self.lib.mdot_64_ if wide else self.lib.mdot_
+        r = f(I(n), _ptr(x), I(incx), _ptr(y), I(incy))
+        return r.to_tuple()
+
+    def maxpy(self, n, alpha, x, incx, y, incy, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = self.lib.maxpy_64_ if wide else self.lib.maxpy_
+        f(I(n), C.byref(real(alpha)), _ptr(x), I(incx), _ptr(y), I(incy))
+
+    def mscal(self, n, alpha, x, incx, wide=True):
+        I = lambda v: self._I(v, wide)
+        (self.lib.mscal_64_ if wide else self.lib.mscal_)(I(n), C.byref(real(alpha)), _ptr(x), I(incx))
+
+    def wscal(self, n, alpha, x, incx, wide=True):
+        I = lambda v: self._I(v, wide)
+        (self.lib.wscal_64_ if wide else self.lib.wscal_)(I(n), C.byref(cplx(alpha)), _ptr(x), I(incx))
+
+    def wmscal(self, n, alpha, x, incx, wide=True):
+        I = lambda v: self._I(v, wide)
+        (self.lib.wmscal_64_ if wide else self.lib.wmscal_)(I(n), C.byref(real(alpha)), _ptr(x), I(incx))
+
+    def mcopy(self, n, x, incx, y, incy, wide=True, cplx_=False):
+        I = lambda v: self._I(v, wide)
+        name = ("wcopy" if cplx_ else "mcopy") + ("_64_" if wide else "_")
+        getattr(self.lib, name)(I(n), _ptr(x), I(incx), _ptr(y), I(incy))
+
+    def mswap(self, n, x, incx, y, incy, wide=True, cplx_=False):
+        I = lambda v: self._I(v, wide)
+        name = ("wswap" if cplx_ else "mswap") + ("_64_" if wide else "_")
+        getattr(self.lib, name)(I(n), _ptr(x), I(incx), _ptr(y), I(incy))
+
+    def imamax(self, n, x, incx, wide=True, cplx_=False):
+        I = lambda v: self._I(v, wide)
+        name = ("iwamax" if cplx_ else "imamax") + ("_64_" if wide else "_")
+        return int(getattr(self.lib, name)(I(n), _ptr(x), I(incx)))
+
+
+# ---- array helpers -----------------------------------------------------------------------
+
+def dd_normalize(hi, lo):
+    """Renormalises (hi, lo) pairs so that |lo| <= ulp(hi)/2 (fast two-sum)."""
+    s = hi + lo
+    e = lo - (s - hi)
+    return s, e
+
+
+def random_dd(rng, shape, scale=1.0):
+    """hi ~ U[-1,1)*scale, lo = hi * 2^-53 * U[-1,1), renormalised."""
+    hi = (rng.random(shape) * 2.0 - 1.0) * scale
+    lo = hi * 2.0 ** -53 * (rng.random(shape) * 2.0 - 1.0)
+    hi, lo = dd_normalize(hi, lo)
+    return np.stack([hi, lo], axis=-1)
+
+
+def random_cdd(rng, shape, scale=1.0):
+    return np.stack([random_dd(rng, shape, scale), random_dd(rng, shape, scale)], axis=-2)
+
+
+def dd_matrix(rng, m, n, ld=None, cplx_=False, fill=None):
+    """Column-major DD matrix as (n, ld, 2) [or (n, ld, 2, 2)], padding rows = fill."""
+    ld = max(1, m) if ld is None else ld
+    shape = (n, ld)
+    a = random_cdd(rng, shape) if cplx_ else random_dd(rng, shape)
+    if fill is not None and ld > m:
+        a[:, m:] = fill
+    return np.ascontiguousarray(a)

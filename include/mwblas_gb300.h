@@ -1,0 +1,259 @@
+/*
+ * mwblas_gb300.h — C ABI of libmwblas_gb300.so, a double-double ("mw") BLAS
+ * for one NVIDIA GB300 (sm_103a).
+ *
+ * Drop-in boundary. Every routine below exports the same Fortran-style
+ * by-reference symbols as the reference library epblas-parallel::mwblas:
+ * an LP64 `name_` taking `int *` sizes and an ILP64 `name_64_` taking
+ * `int64_t *` sizes, generated in the reference by EPBLAS_FACADE_PAIR
+ * (src/epblas-parallel/common/epblas_facade.h:63-65). As in the reference:
+ *   - hidden Fortran string-length arguments are NOT declared
+ *     (epblas_facade.h:24-35);
+ *   - flag characters are case-insensitive; real routines fold 'C' to 'T'
+ *     (common/blas_char.h:33-39);
+ *   - arrays are column-major with leading dimensions, owned by the caller;
+ *   - every call returns with its outputs complete (synchronous BLAS).
+ * Arrays may be host memory (staged through device memory by the library) or
+ * device/managed memory (used in place, no copies).
+ *
+ * Differences from the reference, which has no argument checking at all
+ * (invalid arguments are undefined behaviour there): invalid leading
+ * dimensions, flags or unreachable memory are reported through
+ * mwblas_last_error() and the optional error hook, and the outputs are left
+ * untouched. Sizes <= 0 are quick returns exactly as in the reference.
+ *
+ * The element types are layout-compatible with the reference's
+ * multifloats::float64x2 / complex64x2 (mgemm_parallel.cpp:20-22).
+ */
+#ifndef MWBLAS_GB300_H
+#define MWBLAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* double-double: value = limbs[0] + limbs[1], |limbs[1]| <= ulp(limbs[0])/2 */
+typedef struct { double limbs[2]; } mwblas_real64x2;
+/* complex double-double */
+typedef struct { mwblas_real64x2 re, im; } mwblas_complex64x2;
+
+#define MWBLAS_R mwblas_real64x2
+#define MWBLAS_C mwblas_complex64x2
+
+/* ======================= Level 3 ======================================= */
+
+/* C := alpha*op(A)*op(B) + beta*C.  Replaces mgemm_/mgemm_64_
+ * (multifloats/mgemm_parallel.cpp:44-191, facade epblas_facade.h:234-240). */
+void mgemm_(const char *transa, const char *transb, const int *m, const int *n,
+            const int *k, const MWBLAS_R *alpha, const MWBLAS_R *a, const int *lda,
+            const MWBLAS_R *b, const int *ldb, const MWBLAS_R *beta, MWBLAS_R *c,
+            const int *ldc);
+void mgemm_64_(const char *transa, const char *transb, const int64_t *m,
+               const int64_t *n, const int64_t *k, const MWBLAS_R *alpha,
+               const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *b,
+               const int64_t *ldb, const MWBLAS_R *beta, MWBLAS_R *c,
+               const int64_t *ldc);
+
+/* Complex C := alpha*op(A)*op(B) + beta*C, op in {N,T,C}.  Replaces
+ * wgemm_/wgemm_64_ (multifloats/wgemm_parallel.cpp:44-200). */
+void wgemm_(const char *transa, const char *transb, const int *m, const int *n,
+            const int *k, const MWBLAS_C *alpha, const MWBLAS_C *a, const int *lda,
+            const MWBLAS_C *b, const int *ldb, const MWBLAS_C *beta, MWBLAS_C *c,
+            const int *ldc);
+void wgemm_64_(const char *transa, const char *transb, const int64_t *m,
+               const int64_t *n, const int64_t *k, const MWBLAS_C *alpha,
+               const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *b,
+               const int64_t *ldb, const MWBLAS_C *beta, MWBLAS_C *c,
+               const int64_t *ldc);
+
+/* C := alpha*A*A**T + beta*C (trans='N') or alpha*A**T*A + beta*C, on the
+ * uplo triangle only.  Replaces msyrk_/msyrk_64_
+ * (multifloats/msyrk_parallel.cpp:36-90, facade epblas_facade.h:259-265). */
+void msyrk_(const char *uplo, const char *trans, const int *n, const int *k,
+            const MWBLAS_R *alpha, const MWBLAS_R *a, const int *lda,
+            const MWBLAS_R *beta, MWBLAS_R *c, const int *ldc);
+void msyrk_64_(const char *uplo, const char *trans, const int64_t *n,
+               const int64_t *k, const MWBLAS_R *alpha, const MWBLAS_R *a,
+               const int64_t *lda, const MWBLAS_R *beta, MWBLAS_R *c,
+               const int64_t *ldc);
+
+/* Hermitian rank-k update with real alpha/beta; the imaginary part of the
+ * diagonal is set to zero.  Replaces wherk_/wherk_64_
+ * (multifloats/wherk_parallel.cpp:40-88, wherk_serial.cpp:369-405). */
+void wherk_(const char *uplo, const char *trans, const int *n, const int *k,
+            const MWBLAS_R *alpha, const MWBLAS_C *a, const int *lda,
+            const MWBLAS_R *beta, MWBLAS_C *c, const int *ldc);
+void wherk_64_(const char *uplo, const char *trans, const int64_t *n,
+               const int64_t *k, const MWBLAS_R *alpha, const MWBLAS_C *a,
+               const int64_t *lda, const MWBLAS_R *beta, MWBLAS_C *c,
+               const int64_t *ldc);
+
+/* Triangular solve op(A)*X = alpha*B (side='L') or X*op(A) = alpha*B
+ * (side='R'); B is overwritten by X.  Replaces mtrsm_/mtrsm_64_
+ * (multifloats/mtrsm_parallel.cpp:36-105, facade epblas_facade.h:276-282). */
+void mtrsm_(const char *side, const char *uplo, const char *transa, const char *diag,
+            const int *m, const int *n, const MWBLAS_R *alpha, const MWBLAS_R *a,
+            const int *lda, MWBLAS_R *b, const int *ldb);
+void mtrsm_64_(const char *side, const char *uplo, const char *transa,
+               const char *diag, const int64_t *m, const int64_t *n,
+               const MWBLAS_R *alpha, const MWBLAS_R *a, const int64_t *lda,
+               MWBLAS_R *b, const int64_t *ldb);
+
+/* ======================= Level 2 ======================================= */
+
+/* y := alpha*op(A)*x + beta*y.  Replaces mgemv_/mgemv_64_
+ * (multifloats/mgemv.cpp:237-280, facade epblas_facade.h:132-138). */
+void mgemv_(const char *trans, const int *m, const int *n, const MWBLAS_R *alpha,
+            const MWBLAS_R *a, const int *lda, const MWBLAS_R *x, const int *incx,
+            const MWBLAS_R *beta, MWBLAS_R *y, const int *incy);
+void mgemv_64_(const char *trans, const int64_t *m, const int64_t *n,
+               const MWBLAS_R *alpha, const MWBLAS_R *a, const int64_t *lda,
+               const MWBLAS_R *x, const int64_t *incx, const MWBLAS_R *beta,
+               MWBLAS_R *y, const int64_t *incy);
+
+/* ======================= Level 1 ======================================= */
+
+/* sum x(i)*y(i).  Replaces mdot_/mdot_64_ (multifloats/mdot.cpp:127-148). */
+MWBLAS_R mdot_(const int *n, const MWBLAS_R *x, const int *incx, const MWBLAS_R *y,
+               const int *incy);
+MWBLAS_R mdot_64_(const int64_t *n, const MWBLAS_R *x, const int64_t *incx,
+                  const MWBLAS_R *y, const int64_t *incy);
+
+/* y := alpha*x + y, bit-exact to the reference (multifloats/maxpy.cpp:42-113). */
+void maxpy_(const int *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int *incx,
+            MWBLAS_R *y, const int *incy);
+void maxpy_64_(const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *x,
+               const int64_t *incx, MWBLAS_R *y, const int64_t *incy);
+
+/* x := alpha*x, bit-exact to the reference (multifloats/mscal.cpp:42-104). */
+void mscal_(const int *n, const MWBLAS_R *alpha, MWBLAS_R *x, const int *incx);
+void mscal_64_(const int64_t *n, const MWBLAS_R *alpha, MWBLAS_R *x,
+               const int64_t *incx);
+
+/* y := x (multifloats/mcopy.cpp:30-58). */
+void mcopy_(const int *n, const MWBLAS_R *x, const int *incx, MWBLAS_R *y,
+            const int *incy);
+void mcopy_64_(const int64_t *n, const MWBLAS_R *x, const int64_t *incx, MWBLAS_R *y,
+               const int64_t *incy);
+
+/* x <-> y (multifloats/mswap.cpp:40-70). */
+void mswap_(const int *n, MWBLAS_R *x, const int *incx, MWBLAS_R *y, const int *incy);
+void mswap_64_(const int64_t *n, MWBLAS_R *x, const int64_t *incx, MWBLAS_R *y,
+               const int64_t *incy);
+
+/* 1-based index of the first element of maximal |x|, lexicographic
+ * double-double compare (multifloats/imamax.cpp:178-203). */
+int imamax_(const int *n, const MWBLAS_R *x, const int *incx);
+int64_t imamax_64_(const int64_t *n, const MWBLAS_R *x, const int64_t *incx);
+
+/* complex x := alpha*x, bit-exact (multifloats/wscal.cpp). */
+void wscal_(const int *n, const MWBLAS_C *alpha, MWBLAS_C *x, const int *incx);
+void wscal_64_(const int64_t *n, const MWBLAS_C *alpha, MWBLAS_C *x,
+               const int64_t *incx);
+
+/* complex x := alpha*x with real alpha, bit-exact (multifloats/wmscal.cpp). */
+void wmscal_(const int *n, const MWBLAS_R *alpha, MWBLAS_C *x, const int *incx);
+void wmscal_64_(const int64_t *n, const MWBLAS_R *alpha, MWBLAS_C *x,
+                const int64_t *incx);
+
+/* complex y := x (multifloats/wcopy.cpp). */
+void wcopy_(const int *n, const MWBLAS_C *x, const int *incx, MWBLAS_C *y,
+            const int *incy);
+void wcopy_64_(const int64_t *n, const MWBLAS_C *x, const int64_t *incx, MWBLAS_C *y,
+               const int64_t *incy);
+
+/* complex x <-> y (multifloats/wswap.cpp). */
+void wswap_(const int *n, MWBLAS_C *x, const int *incx, MWBLAS_C *y, const int *incy);
+void wswap_64_(const int64_t *n, MWBLAS_C *x, const int64_t *incx, MWBLAS_C *y,
+               const int64_t *incy);
+
+/* 1-based argmax of |re|+|im| (multifloats/iwamax.cpp:174-200). */
+int iwamax_(const int *n, const MWBLAS_C *x, const int *incx);
+int64_t iwamax_64_(const int64_t *n, const MWBLAS_C *x, const int64_t *incx);
+
+/* ======================= Extensions (no reference counterpart) ========== */
+
+/* GEMM engine selection for mgemm_/wgemm_ and the level-3 routines built on
+ * them.  MWBLAS_GEMM_AUTO picks by size; PLAIN is the FP64 error-free-
+ * transform kernel; OZAKI is the integer-exact tensor-core scheme.  The
+ * MWBLAS_GEMM environment variable ("auto", "plain", "ozaki") sets the
+ * initial value. */
+enum { MWBLAS_GEMM_AUTO = 0, MWBLAS_GEMM_PLAIN = 1, MWBLAS_GEMM_OZAKI = 2 };
+int mwblas_set_gemm_engine(int engine);   /* returns the previous value */
+int mwblas_get_gemm_engine(void);
+
+/* Same arguments as mgemm_64_, forcing one engine. */
+void mgemm_plain_64_(const char *transa, const char *transb, const int64_t *m,
+                     const int64_t *n, const int64_t *k, const MWBLAS_R *alpha,
+                     const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *b,
+                     const int64_t *ldb, const MWBLAS_R *beta, MWBLAS_R *c,
+                     const int64_t *ldc);
+void mgemm_ozaki_64_(const char *transa, const char *transb, const int64_t *m,
+                     const int64_t *n, const int64_t *k, const MWBLAS_R *alpha,
+                     const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *b,
+                     const int64_t *ldb, const MWBLAS_R *beta, MWBLAS_R *c,
+                     const int64_t *ldc);
+
+/* Ozaki scheme controls.  bits = significant bits kept per scaled operand
+ * row/column (0 = automatic from the operands' exponent range); the number
+ * of moduli (integer GEMMs) follows from bits and k.  Returns the previous
+ * value. */
+int mwblas_set_ozaki_bits(int bits);
+/* Moduli count used by the most recent Ozaki GEMM on this thread. */
+int mwblas_last_ozaki_moduli(void);
+
+/* Team size used to reproduce the reference's per-thread body/tail split in
+ * the bit-exact level-1 routines (mscal/maxpy/wscal/wmscal).  0 = follow the
+ * calling process's OpenMP settings exactly as the reference does
+ * (omp_get_max_threads() and omp_in_parallel() when an OpenMP runtime is
+ * loaded, else OMP_NUM_THREADS, else the CPU count).  Returns the previous
+ * value. */
+int64_t mwblas_set_l1_partition(int64_t team);
+
+/* Stream control.  By default every call runs on the calling host thread's
+ * per-thread default stream and synchronises before returning.  With a
+ * user stream and sync disabled, calls on device pointers return as soon as
+ * their work is enqueued (host-pointer calls always synchronise). */
+int mwblas_set_stream(void *cuda_stream);       /* cudaStream_t; NULL = default */
+int mwblas_set_sync(int sync);                  /* returns previous */
+
+/* Errors. */
+enum {
+    MWBLAS_OK = 0,
+    MWBLAS_ERR_CUDA = -1,       /* CUDA runtime error */
+    MWBLAS_ERR_ALLOC = -2,      /* device allocation failed */
+    MWBLAS_ERR_DEVICE = -3,     /* no usable sm_103 device */
+    MWBLAS_ERR_TIMEOUT = -4,    /* a bounded device wait gave up */
+    MWBLAS_ERR_UNSUPPORTED = -5 /* argument combination not implemented */
+};
+typedef void (*mwblas_error_hook)(const char *routine, int info, const char *message);
+/* Installs a hook called on every recorded error; returns the previous one. */
+mwblas_error_hook mwblas_set_error_hook(mwblas_error_hook hook);
+/* Last error recorded on this thread (0 if none since mwblas_clear_error). */
+int mwblas_last_error(void);
+const char *mwblas_last_error_message(void);
+const char *mwblas_last_error_routine(void);
+void mwblas_clear_error(void);
+
+/* Test hook: the next `count` device allocations succeed, the one after
+ * fails (negative = never fail).  Used to test error propagation without a
+ * GPU fault. */
+void mwblas_debug_fail_alloc_after(int64_t count);
+
+/* Number of kernels this library has launched in the process. */
+int64_t mwblas_launch_count(void);
+
+/* Library version string. */
+const char *mwblas_version(void);
+
+#undef MWBLAS_R
+#undef MWBLAS_C
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MWBLAS_GB300_H */

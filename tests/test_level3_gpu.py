@@ -1,0 +1,219 @@
+"""Level-2/3 parity on the GPU, through the C ABI.
+
+Every result is compared with the binary128 oracle using the reference's
+normwise error (fuzz_util_body.fypp:242-271) and its tolerances:
+GEMM/SYRK/HERK max(10, 4k) * 2^-104, TRSM max(20, 8 na^2) * 2^-104 on a
+diagonally dominant triangle (fuzz_mtrsm.fypp:67-117), GEMV max(10, 4 max(m,n))
+* 2^-104 (fuzz_mgemv.fypp:65). Padding rows of leading dimensions and the
+off-uplo triangle carry sentinels that must come back untouched
+(fuzz_util_body.fypp:224-240). The reference's own outputs from the golden
+fixtures are checked the same way.
+"""
+import numpy as np
+import pytest
+
+from conftest import mwb, orc
+
+pytestmark = pytest.mark.gpu
+
+SENT = -7.37e18
+ENGINES = ["plain"]
+
+
+def alpha_beta(rng, cplx_=False):
+    def scal():
+        if cplx_:
+            return mwb.random_cdd(rng, ())
+        v = mwb.random_dd(rng, ())
+        return v
+    r = rng.random()
+    beta = scal() if r < 0.6 else (np.zeros((2, 2)) if cplx_ else np.zeros(2)) if r < 0.8 else \
+        (np.array([[1.0, 0], [0, 0]]) if cplx_ else np.array([1.0, 0.0]))
+    return scal(), beta
+
+
+def op_norm(alpha, k, A, B, beta, C0):
+    return orc.dd_abs(alpha) * k * orc.dd_absmax(A) * orc.dd_absmax(B) + orc.dd_abs(beta) * orc.dd_absmax(C0)
+
+
+def check_sentinel(C, m):
+    if C.shape[1] > m:
+        assert np.all(C[:, m:] == SENT), "leading-dimension padding was written"
+
+
+@pytest.mark.parametrize("engine", ENGINES)
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T"), ("C", "N")])
+def test_mgemm_random(gpu, oracle, rng, engine, ta, tb):
+    for (m, n, k) in [(1, 1, 1), (7, 5, 3), (33, 17, 65), (64, 64, 64), (130, 70, 257), (257, 129, 100)]:
+        pad = int(rng.integers(0, 3))
+        lda = (m if ta == "N" else k) + pad
+        ldb = (k if tb == "N" else n) + pad
+        ldc = m + 1 + pad
+        A = mwb.dd_matrix(rng, m if ta == "N" else k, k if ta == "N" else m, lda)
+        B = mwb.dd_matrix(rng, k if tb == "N" else n, n if tb == "N" else k, ldb)
+        C0 = mwb.dd_matrix(rng, m, n, ldc, fill=SENT)
+        al, be = alpha_beta(rng)
+        want = oracle.qgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0.copy(), ldc)
+        got = C0.copy()
+        gpu.mgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, got, ldc, engine=engine)
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        check_sentinel(got, m)
+        err = orc.normwise_error(got[:, :m], want[:, :m], op_norm(al, k, A, B, be, C0[:, :m]))
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (m, n, k, err)
+
+
+def test_mgemm_lp64_and_special_scalars(gpu, oracle, rng):
+    m, n, k = 40, 30, 20
+    A = mwb.dd_matrix(rng, m, k); B = mwb.dd_matrix(rng, k, n)
+    C0 = mwb.dd_matrix(rng, m, n)
+    # alpha = 0: only the beta pass (mgemm_parallel.cpp:68-78)
+    got = C0.copy()
+    gpu.mgemm("N", "N", m, n, k, 0.0, A, m, B, k, 2.0, got, m, wide=False)
+    want = C0.copy(); oracle.qgemm("N", "N", m, n, k, np.zeros(2), A, m, B, k, np.array([2.0, 0.0]), want, m)
+    assert orc.normwise_error(got, want, 2 * orc.dd_absmax(C0)) <= 4 * orc.EPS_DD
+    # beta = 0 must not read C: NaN in C is overwritten
+    got = np.full_like(C0, np.nan)
+    gpu.mgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, got, m)
+    assert np.all(np.isfinite(got))
+    # k = 0 with beta = 1 leaves C bit-identical
+    got = C0.copy()
+    gpu.mgemm("N", "N", m, n, 0, 1.0, A, m, B, 1, 1.0, got, m)
+    np.testing.assert_array_equal(got, C0)
+
+
+def test_wgemm_random(gpu, oracle, rng):
+    for ta, tb in [("N", "N"), ("N", "C"), ("C", "T"), ("T", "N"), ("C", "C")]:
+        for (m, n, k) in [(5, 3, 2), (33, 31, 40), (70, 65, 129)]:
+            lda = (m if ta == "N" else k) + 1
+            ldb = (k if tb == "N" else n)
+            ldc = m + 2
+            A = mwb.dd_matrix(rng, m if ta == "N" else k, k if ta == "N" else m, lda, cplx_=True)
+            B = mwb.dd_matrix(rng, k if tb == "N" else n, n if tb == "N" else k, ldb, cplx_=True)
+            C0 = mwb.dd_matrix(rng, m, n, ldc, cplx_=True, fill=SENT)
+            al, be = alpha_beta(rng, True)
+            want = oracle.qwgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0.copy(), ldc)
+            got = C0.copy()
+            gpu.wgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, got, ldc)
+            assert gpu.last_error()[0] == 0, gpu.last_error()
+            check_sentinel(got, m)
+            opn = op_norm(al, k, A, B, be, C0[:, :m]) * 2
+            err = orc.normwise_error(got[:, :m], want[:, :m], opn)
+            assert err <= max(10, 4 * k) * orc.EPS_DD, (ta, tb, m, n, k, err)
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+@pytest.mark.parametrize("trans", ["N", "T"])
+def test_msyrk(gpu, oracle, rng, uplo, trans):
+    for (n, k) in [(1, 1), (9, 4), (65, 33), (130, 70)]:
+        lda = (n if trans == "N" else k) + 1
+        ldc = n + 2
+        A = mwb.dd_matrix(rng, n if trans == "N" else k, k if trans == "N" else n, lda)
+        C0 = mwb.dd_matrix(rng, n, n, ldc, fill=SENT)
+        off = np.triu_indices(n, 1) if uplo == "L" else np.tril_indices(n, -1)
+        C0[off[1], off[0]] = SENT          # (j, i) storage: mark the other triangle
+        al, be = alpha_beta(rng)
+        want = C0.copy(); oracle.qsyrk(uplo, trans, n, k, al, A, lda, be, want, ldc)
+        got = C0.copy()
+        gpu.msyrk(uplo, trans, n, k, al, A, lda, be, got, ldc)
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        check_sentinel(got, n)
+        assert np.all(got[off[1], off[0]] == SENT), "off-triangle written"
+        tri = np.tril_indices(n) if uplo == "L" else np.triu_indices(n)
+        g, w = got[tri[1], tri[0]], want[tri[1], tri[0]]
+        err = orc.normwise_error(g, w, op_norm(al, k, A, A, be, C0[tri[1], tri[0]]))
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (n, k, err)
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+@pytest.mark.parametrize("trans", ["N", "C"])
+def test_wherk(gpu, oracle, rng, uplo, trans):
+    for (n, k) in [(1, 2), (9, 4), (40, 65)]:
+        lda = (n if trans == "N" else k)
+        ldc = n + 1
+        A = mwb.dd_matrix(rng, n if trans == "N" else k, k if trans == "N" else n, lda, cplx_=True)
+        C0 = mwb.dd_matrix(rng, n, n, ldc, cplx_=True, fill=SENT)
+        al, be = alpha_beta(rng)
+        want = C0.copy(); oracle.qherk(uplo, trans, n, k, al, A, lda, be, want, ldc)
+        got = C0.copy()
+        gpu.wherk(uplo, trans, n, k, al, A, lda, be, got, ldc)
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        check_sentinel(got, n)
+        d = np.arange(n)
+        assert np.all(got[d, d, 1] == 0.0), "HERK diagonal must be real"
+        tri = np.tril_indices(n) if uplo == "L" else np.triu_indices(n)
+        g, w = got[tri[1], tri[0]], want[tri[1], tri[0]]
+        err = orc.normwise_error(g, w, 2 * op_norm(al, k, A, A, be, C0[tri[1], tri[0]]))
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (n, k, err)
+
+
+def dominant_triangle(rng, na, lda):
+    A = mwb.dd_matrix(rng, na, na, lda)
+    A[..., 0] /= na
+    A[..., 1] /= na
+    for d in range(na):
+        A[d, d] = (1.0 + rng.random(), 0.0)
+    return A
+
+
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("uplo", ["U", "L"])
+@pytest.mark.parametrize("ta", ["N", "T"])
+@pytest.mark.parametrize("diag", ["N", "U"])
+def test_mtrsm(gpu, oracle, rng, side, uplo, ta, diag):
+    for (m, n) in [(1, 1), (7, 5), (70, 33), (150, 20)]:
+        if side == "R":
+            m, n = n, m
+        na = m if side == "L" else n
+        lda, ldb = na + 1, m + 1
+        A = dominant_triangle(rng, na, lda)
+        B0 = mwb.dd_matrix(rng, m, n, ldb, fill=SENT)
+        al = mwb.random_dd(rng, ())
+        want = B0.copy(); oracle.qtrsm(side, uplo, ta, diag, m, n, al, A, lda, want, ldb)
+        got = B0.copy()
+        gpu.mtrsm(side, uplo, ta, diag, m, n, al, A, lda, got, ldb)
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        check_sentinel(got, m)
+        err = orc.normwise_error(got[:, :m], want[:, :m], orc.dd_abs(al) * orc.dd_absmax(B0[:, :m]))
+        assert err <= max(20, 8 * na * na) * orc.EPS_DD, (m, n, err)
+
+
+@pytest.mark.parametrize("trans", ["N", "T"])
+def test_mgemv(gpu, oracle, rng, trans):
+    for (m, n, incx, incy) in [(1, 1, 1, 1), (17, 9, 1, 1), (300, 70, 2, -1), (70, 300, -3, 2), (1000, 4000, 1, 1)]:
+        lda = m + 3
+        A = mwb.dd_matrix(rng, m, n, lda, fill=SENT)
+        lx, ly = (n, m) if trans == "N" else (m, n)
+        x = mwb.random_dd(rng, (1 + (lx - 1) * abs(incx),))
+        y0 = mwb.random_dd(rng, (1 + (ly - 1) * abs(incy),))
+        al, be = alpha_beta(rng)
+        want = y0.copy(); oracle.qgemv(trans, m, n, al, A, lda, x, incx, be, want, incy)
+        got = y0.copy()
+        gpu.mgemv(trans, m, n, al, A, lda, x, incx, be, got, incy)
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        opn = orc.dd_abs(al) * lx * orc.dd_absmax(A[:, :m]) * orc.dd_absmax(x) + orc.dd_abs(be) * orc.dd_absmax(y0)
+        err = orc.normwise_error(got, want, opn)
+        assert err <= max(10, 4 * max(m, n)) * orc.EPS_DD, (m, n, err)
+
+
+def test_golden_reference_outputs(gpu, golden):
+    """GPU results agree with the reference's own outputs within its tolerances."""
+    z, meta = golden
+    for c in meta["l3"]:
+        k = c["key"]
+        if c["kind"] == "gemm":
+            got = z[k + "_C"].copy()
+            gpu.mgemm(c["ta"], c["tb"], c["m"], c["n"], c["k"], z[k + "_alpha"], z[k + "_A"], c["lda"],
+                      z[k + "_B"], c["ldb"], z[k + "_beta"], got, c["ldc"])
+            opn = op_norm(z[k + "_alpha"], c["k"], z[k + "_A"], z[k + "_B"], z[k + "_beta"], z[k + "_C"])
+            tol = max(10, 4 * c["k"]) * orc.EPS_DD
+            m = c["m"]
+            assert orc.normwise_error(got[:, :m], z[k + "_q"][:, :m], opn) <= tol, k
+            assert orc.normwise_error(got[:, :m], z[k + "_ref"][:, :m], opn) <= 2 * tol, k
+        elif c["kind"] == "trsm":
+            got = z[k + "_B"].copy()
+            gpu.mtrsm(c["side"], c["uplo"], c["ta"], c["diag"], c["m"], c["n"], z[k + "_alpha"], z[k + "_A"],
+                      c["lda"], got, c["ldb"])
+            na = c["m"] if c["side"] == "L" else c["n"]
+            opn = orc.dd_abs(z[k + "_alpha"]) * orc.dd_absmax(z[k + "_B"][:, :c["m"]])
+            tol = max(20, 8 * na * na) * orc.EPS_DD
+            assert orc.normwise_error(got[:, :c["m"]], z[k + "_q"][:, :c["m"]], opn) <= tol, k
