@@ -332,9 +332,10 @@ void scal_entry(const char *routine, int kind, const INT *n, const void *alpha, 
     int64_t dinc;
     if (!stage_vector(SX, x, N, inc, es, true, dinc, routine)) return;
     int64_t team = (inc == 1) ? l1_team(N, kScalOmpMin) : 1;
-    if (kind == 0) launch_mscal(N, rd((const mwblas_real64x2 *)alpha), SX.dev, dinc, team);
-    else if (kind == 1) launch_wscal(N, cd((const mwblas_complex64x2 *)alpha), SX.dev, dinc, team);
-    else launch_wmscal(N, rd((const mwblas_real64x2 *)alpha), SX.dev, dinc, team);
+    bool unit = (inc == 1);
+    if (kind == 0) launch_mscal(N, rd((const mwblas_real64x2 *)alpha), SX.dev, dinc, unit, team);
+    else if (kind == 1) launch_wscal(N, cd((const mwblas_complex64x2 *)alpha), SX.dev, dinc, unit, team);
+    else launch_wmscal(N, rd((const mwblas_real64x2 *)alpha), SX.dev, dinc, unit, team);
     if (!unstage_vector(SX, routine)) return;
     finish(routine);
 }
@@ -356,8 +357,9 @@ void axpy_entry(const char *routine, const INT *n, const mwblas_real64x2 *alpha,
     int64_t dix, diy;
     if (!stage_vector(SX, x, N, *incx, 16, true, dix, routine)) return;
     if (!stage_vector(SY, y, N, *incy, 16, true, diy, routine)) return;
-    int64_t team = (*incx == 1 && *incy == 1) ? l1_team(N, kAxpyOmpMin) : 1;
-    launch_maxpy(N, a, SX.dev, dix, SY.dev, diy, team);
+    bool unit = (*incx == 1 && *incy == 1);
+    int64_t team = unit ? l1_team(N, kAxpyOmpMin) : 1;
+    launch_maxpy(N, a, SX.dev, dix, SY.dev, diy, unit, team);
     if (!unstage_vector(SY, routine)) return;
     finish(routine);
 }

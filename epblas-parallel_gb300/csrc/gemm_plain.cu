@@ -80,6 +80,18 @@ __global__ void k_exp_cols(int64_t rows, int64_t cols, const double2 *M, int64_t
     if (lane == 0) out[j] = e;
 }
 
+// Exponent offset of sigma above ea + eb: a fold block holds at most
+// min(KB, k) steps of `per_step` products, each below 2^(ea+eb+2); sigma's
+// binade must keep every partial sum below half of 2^E with one more bit of
+// room for the rounding of the extracted high parts.
+int sigma_shift(int KB, int64_t k, int per_step)
+{
+    int64_t terms = (k < KB ? k : KB) * per_step;
+    int lg = 0;
+    while (((int64_t)1 << lg) < terms) ++lg;
+    return lg + 4;
+}
+
 __device__ __forceinline__ double make_sigma(int ea, int eb, int shift)
 {
     int e;
@@ -96,15 +108,13 @@ template <int BM, int BN, int TM, int TN, bool TA, bool TB, int KB>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
     k_gemm_plain(int64_t m, int64_t n, int64_t k, dd::real alpha, const double2 *__restrict__ A, int64_t lda,
                  const double2 *__restrict__ B, int64_t ldb, dd::real beta, int beta_kind, double2 *C, int64_t ldc,
-                 const int *__restrict__ ea, const int *__restrict__ eb, int uplo)
+                 const int *__restrict__ ea, const int *__restrict__ eb, int uplo, int SHIFT)
 {
     constexpr int NTX = BM / TM;   // threads along rows
     constexpr int NTY = BN / TN;   // threads along columns
     constexpr int NT = NTX * NTY;
     constexpr int BK = 8;
     static_assert(KB % BK == 0, "fold interval must be a multiple of the k-slab");
-    constexpr int LOG2KB = (KB == 8) ? 3 : (KB == 16) ? 4 : (KB == 32) ? 5 : 6;
-    constexpr int SHIFT = LOG2KB + 4;
 
     __shared__ double2 sA[BK][BM];
     __shared__ double2 sB[BK][BN];
@@ -255,7 +265,8 @@ void dispatch_plain(const GemmArgs &g, const int *ea, const int *eb)
     double2 *C = (double2 *)g.C;
 #define MW_LAUNCH(TA, TB)                                                                                     \
     k_gemm_plain<BM, BN, TM, TN, TA, TB, KB><<<grid, block, 0, stream()>>>(g.m, g.n, g.k, al, A, g.lda, B, g.ldb, \
-                                                                          be, g.beta_kind, C, g.ldc, ea, eb, g.uplo)
+                                                                          be, g.beta_kind, C, g.ldc, ea, eb, g.uplo, \
+                                                                          sigma_shift(KB, g.k, 1))
     if (!g.ta && !g.tb) MW_LAUNCH(false, false);
     else if (!g.ta && g.tb) MW_LAUNCH(false, true);
     else if (g.ta && !g.tb) MW_LAUNCH(true, false);
@@ -299,14 +310,13 @@ template <int BM, int BN, int TM, int TN, bool TA, bool TB, bool CA, bool CB, in
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
     k_gemm_plain_c(int64_t m, int64_t n, int64_t k, dd::cplx alpha, const double2 *__restrict__ A, int64_t lda,
                    const double2 *__restrict__ B, int64_t ldb, dd::cplx beta, int beta_kind, double2 *C,
-                   int64_t ldc, const int *__restrict__ ea, const int *__restrict__ eb, int uplo, int herm)
+                   int64_t ldc, const int *__restrict__ ea, const int *__restrict__ eb, int uplo, int herm,
+                   int SHIFT)
 {
     constexpr int NTX = BM / TM;
     constexpr int NTY = BN / TN;
     constexpr int NT = NTX * NTY;
     constexpr int BK = 8;
-    constexpr int LOG2KB = (KB == 8) ? 3 : (KB == 16) ? 4 : (KB == 32) ? 5 : 6;
-    constexpr int SHIFT = LOG2KB + 5;   // two products per part per step
 
     __shared__ double2 sA[BK][BM][2];
     __shared__ double2 sB[BK][BN][2];
@@ -471,7 +481,7 @@ void launch_plain_c(const GemmArgs &g, const int *ea, const int *eb)
     be.im = dd::make(g.cbeta.im.hi, g.cbeta.im.lo);
     k_gemm_plain_c<BM, BN, TM, TN, TA, TB, CA, CB, KB><<<grid, block, 0, stream()>>>(
         g.m, g.n, g.k, al, (const double2 *)g.A, g.lda, (const double2 *)g.B, g.ldb, be, g.beta_kind,
-        (double2 *)g.C, g.ldc, ea, eb, g.uplo, g.herm ? 1 : 0);
+        (double2 *)g.C, g.ldc, ea, eb, g.uplo, g.herm ? 1 : 0, sigma_shift(KB, g.k, 2));
     count_launch();
 }
 

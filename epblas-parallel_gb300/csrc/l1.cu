@@ -367,42 +367,43 @@ __global__ void k_mdot_final(int nparts, const double2 *part, double2 *out)
 
 // ---- launchers ---------------------------------------------------------------
 
-void launch_mscal(int64_t n, dd_host alpha, void *x, int64_t inc, int64_t team)
+void launch_mscal(int64_t n, dd_host alpha, void *x, int64_t inc, bool unit, int64_t team)
 {
     dd::real a = dd::make(alpha.hi, alpha.lo);
-    if (inc == 1)
+    if (unit)
         k_mscal_unit<<<grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, team);
     else
         k_mscal_strided<<<inc == 0 ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, inc);
     count_launch();
 }
 
-void launch_wscal(int64_t n, cdd_host alpha, void *x, int64_t inc, int64_t team)
+void launch_wscal(int64_t n, cdd_host alpha, void *x, int64_t inc, bool unit, int64_t team)
 {
     dd::cplx a;
     a.re = dd::make(alpha.re.hi, alpha.re.lo);
     a.im = dd::make(alpha.im.hi, alpha.im.lo);
-    if (inc == 1)
+    if (unit)
         k_wscal_unit<<<grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, team);
     else
         k_wscal_strided<<<inc == 0 ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, inc);
     count_launch();
 }
 
-void launch_wmscal(int64_t n, dd_host alpha, void *x, int64_t inc, int64_t team)
+void launch_wmscal(int64_t n, dd_host alpha, void *x, int64_t inc, bool unit, int64_t team)
 {
     dd::real a = dd::make(alpha.hi, alpha.lo);
-    if (inc == 1)
+    if (unit)
         k_wmscal_unit<<<grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, team);
     else
         k_wmscal_strided<<<inc == 0 ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, a, (double2 *)x, inc);
     count_launch();
 }
 
-void launch_maxpy(int64_t n, dd_host alpha, const void *x, int64_t incx, void *y, int64_t incy, int64_t team)
+void launch_maxpy(int64_t n, dd_host alpha, const void *x, int64_t incx, void *y, int64_t incy, bool unit,
+                  int64_t team)
 {
     dd::real a = dd::make(alpha.hi, alpha.lo);
-    if (incx == 1 && incy == 1)
+    if (unit)
         k_maxpy_unit<<<grid_for(n), kThreads, 0, stream()>>>(n, a, (const double2 *)x, (double2 *)y, team);
     else
         k_maxpy_strided<<<incy == 0 ? 1 : grid_for(n), kThreads, 0, stream()>>>(n, a, (const double2 *)x, incx,
