@@ -1,25 +1,805 @@
-// Integer-exact tensor-core GEMM engine (placeholder until the sm_103a
-// kernels land): reports itself unavailable.
+// Integer-exact tensor-core double-double GEMM ("Ozaki" engine).
+//
+// Scheme (Ozaki scheme II: Ozaki, Uchino, Imamura, "Ozaki Scheme II: A
+// GEMM-oriented emulation of floating-point matrix multiplication using an
+// integer modular technique", 2025), adapted to what sm_103a offers:
+//
+//  1. Scaling. Row i of op(A) and column j of op(B) are scaled by powers of
+//     two so that every entry becomes an integer of at most `bits` bits:
+//     A'_ip = round(a_ip * 2^(bits-2-ea_i)), B'_pj likewise (ea_i, eb_j bound
+//     the binary exponents of the row / column). The error of this step is
+//     <= 2^(3-bits) of max|row| * max|column| per product, i.e. normwise.
+//  2. Residues. A'B' is an integer matrix with |entries| <= k * 2^(2 bits - 2).
+//     It is computed exactly modulo L pairwise-coprime moduli p_l <= 255 whose
+//     product M exceeds 2^4 * k * 2^(2 bits - 1). Each residue matrix (entries
+//     in [-(p-1)/2, (p-1)/2]) is exact in fp16.
+//  3. Residue GEMMs on the tensor cores. sm_103a's tcgen05 has no integer
+//     kind (kind::i8 is rejected by ptxas for sm_103a), so the residue GEMMs
+//     use kind::f16 with fp32 accumulation in tensor memory. Products of
+//     residues are exact; an fp32 sum stays exact while it is an integer
+//     below 2^24. K is therefore processed in chunks of 1024
+//     (1024 * 127^2 + 255 < 2^24) and after each chunk the accumulator is
+//     reduced modulo p in place; two accumulators alternate so the MMA pipe
+//     keeps running while the epilogue reduces the other one.
+//  4. CRT reconstruction (integer only): X = sum_l c_l * W_l - q * M with
+//     W_l = (M/p_l) * ((M/p_l)^-1 mod p_l) and q = round(sum_l c_l u_l / p_l)
+//     estimated in fp32 (exact because |X| << M by construction), then the
+//     top 106 bits of X become the double-double (hi, lo) with exponents
+//     built directly, scaled back by 2^-(sA_i + sB_j); the alpha/beta update
+//     runs in double-double on the FP64 pipe, which the scheme otherwise
+//     does not touch.
+//
+// A modulus count L of ~29 (8192^3, bits = 106) replaces the 18 FP64
+// instructions per multiply-add of the reference's kernel by 29 fp16
+// tensor-core multiply-adds.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cudaTypedefs.h>
+
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "dd.cuh"
 #include "level3.h"
 #include "runtime.h"
+#include "sm100.cuh"
 
 namespace mw {
 
-static int g_last_moduli = 0;
+namespace {
 
-bool ozaki_available() { return false; }
-int ozaki_last_moduli() { return g_last_moduli; }
+constexpr int kMaxMod = 40;
+constexpr int kNL = 9;          // 32-bit limbs of CRT integers
+constexpr int kResLimbs = 11;   // 11-bit limbs of |A'| (bits <= 120)
+constexpr int kNoExp = -30000;
+constexpr int kChunk = 1024;    // K elements per exact fp32 accumulation chunk
 
-bool gemm_ozaki_real(const GemmArgs &, int, const char *routine)
+// ---- host-side moduli / CRT constants --------------------------------------------------
+
+struct Moduli {
+    int n = 0;
+    int p[kMaxMod];
+};
+
+struct OzResParams {
+    int nmod;
+    float p[kMaxMod], invp[kMaxMod];
+    float t[kMaxMod][kResLimbs];   // 2^(11k) mod p
+};
+
+struct OzModParams {
+    float p[kMaxMod], invp[kMaxMod];
+};
+
+struct OzCrtParams {
+    int nmod;
+    uint32_t W[kMaxMod][kNL];
+    float f[kMaxMod];
+    uint32_t M[kNL];
+};
+
+// Little-endian multi-limb unsigned integer helpers (host).
+void big_mul_small(uint32_t *x, int nl, uint32_t s)
 {
-    set_error(routine, MWBLAS_ERR_UNSUPPORTED, "tensor-core engine not built");
-    return false;
+    uint64_t carry = 0;
+    for (int i = 0; i < nl; ++i) {
+        uint64_t v = (uint64_t)x[i] * s + carry;
+        x[i] = (uint32_t)v;
+        carry = v >> 32;
+    }
+}
+uint32_t big_divmod_small(uint32_t *x, int nl, uint32_t d)   // x /= d, returns x mod d
+{
+    uint64_t rem = 0;
+    for (int i = nl - 1; i >= 0; --i) {
+        uint64_t cur = (rem << 32) | x[i];
+        x[i] = (uint32_t)(cur / d);
+        rem = cur % d;
+    }
+    return (uint32_t)rem;
+}
+int64_t inv_mod(int64_t a, int64_t m)
+{
+    int64_t g = m, x = 0, x1 = 1, a1 = a % m;
+    while (a1) {
+        int64_t q = g / a1;
+        int64_t t = g - q * a1; g = a1; a1 = t;
+        t = x - q * x1; x = x1; x1 = t;
+    }
+    return ((x % m) + m) % m;
+}
+int gcd(int a, int b) { return b ? gcd(b, a % b) : a; }
+
+// The largest pairwise-coprime moduli <= 255 (greedy from the top), enough of
+// them for `need_bits` bits of product.
+Moduli choose_moduli(double need_bits)
+{
+    Moduli md;
+    double have = 0.0;
+    for (int c = 255; c >= 3 && have < need_bits && md.n < kMaxMod; --c) {
+        bool ok = true;
+        for (int i = 0; i < md.n && ok; ++i) ok = gcd(md.p[i], c) == 1;
+        if (!ok) continue;
+        md.p[md.n++] = c;
+        have += std::log2((double)c);
+    }
+    return md;
 }
 
-bool gemm_ozaki_cplx(const GemmArgs &, int, const char *routine)
+int g_last_moduli = 0;
+int g_mma_kind = -1;   // 0 tcgen05, 1 SIMT cross-check
+
+int mma_kind()
 {
-    set_error(routine, MWBLAS_ERR_UNSUPPORTED, "tensor-core engine not built");
-    return false;
+    if (g_mma_kind < 0) {
+        const char *e = getenv("MWBLAS_OZAKI_MMA");
+        g_mma_kind = (e && !strcmp(e, "simt")) ? 1 : 0;
+    }
+    return g_mma_kind;
+}
+
+// ---- device: residues -----------------------------------------------------------------------
+
+__device__ __forceinline__ __int128 fixed_round(double x, int s)
+{
+    uint64_t b = (uint64_t)__double_as_longlong(x);
+    int ex = (int)((b >> 52) & 0x7FF);
+    uint64_t m = b & 0xFFFFFFFFFFFFFull;
+    if (ex == 0) {
+        if (m == 0) return 0;
+        ex = 1;
+    } else {
+        m |= 1ull << 52;
+    }
+    int sh = ex - 1075 + s;
+    unsigned __int128 mag;
+    if (sh >= 0) {
+        mag = (unsigned __int128)m << sh;
+    } else if (sh > -63) {
+        int r = -sh;
+        mag = (unsigned __int128)((m + (1ull << (r - 1))) >> r);
+    } else {
+        mag = 0;
+    }
+    __int128 v = (__int128)mag;
+    return (b >> 63) ? -v : v;
+}
+
+__device__ __forceinline__ float u11_to_float(uint32_t c)
+{
+    return __int_as_float(0x4B000000 | c) - 8388608.0f;   // exact for c < 2^23
+}
+
+// op(X) is rows x kdim; element (r, c) lives at X[r + c*ld] (ROWC) or
+// X[c + r*ld]. Writes out[l][r][c] (fp16, row stride kpad) for the padded
+// ranges r < rows_pad, c < kpad (zeros outside op(X)).
+template <bool ROWC>
+__global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim, const double2 *__restrict__ X,
+                                                     int64_t ld, const int *__restrict__ rexp, int bits,
+                                                     OzResParams P, __half *__restrict__ out, int64_t rows_pad,
+                                                     int64_t kpad, int negate_im)
+{
+    __shared__ double2 tile[32][33];
+    const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int s = ty; s < 32; s += 8) {
+        int64_t r = ROWC ? r0 + tx : r0 + s;
+        int64_t c = ROWC ? c0 + s : c0 + tx;
+        double2 v = make_double2(0.0, 0.0);
+        if (r < rows && c < kdim) v = ROWC ? X[r + c * ld] : X[c + r * ld];
+        if (ROWC) tile[tx][s] = v;
+        else tile[s][tx] = v;
+    }
+    __syncthreads();
+    for (int s = ty; s < 32; s += 8) {
+        int64_t r = r0 + s, c = c0 + tx;
+        if (r >= rows_pad || c >= kpad) continue;
+        double2 v = tile[s][tx];
+        int e = (r < rows) ? rexp[r] : kNoExp;
+        uint32_t limb[kResLimbs];
+        bool neg = false;
+        if (e <= kNoExp / 2) {
+            for (int q = 0; q < kResLimbs; ++q) limb[q] = 0;
+        } else {
+            int sc = bits - 2 - e;
+            __int128 F = fixed_round(v.x, sc) + fixed_round(v.y, sc);
+            neg = F < 0;
+            unsigned __int128 U = (unsigned __int128)(neg ? -F : F);
+            for (int q = 0; q < kResLimbs; ++q) limb[q] = (uint32_t)(U >> (11 * q)) & 0x7FFu;
+        }
+        if (negate_im) neg = !neg;
+        float fl[kResLimbs];
+#pragma unroll
+        for (int q = 0; q < kResLimbs; ++q) fl[q] = u11_to_float(limb[q]);
+        for (int l = 0; l < P.nmod; ++l) {
+            float x = 0.0f;
+#pragma unroll
+            for (int q = 0; q < kResLimbs; ++q) x = __fmaf_rn(fl[q], P.t[l][q], x);
+            float p = P.p[l];
+            float qq = rintf(__fmul_rn(x, P.invp[l]));
+            float rr = __fmaf_rn(-qq, p, x);
+            float half = 0.5f * p;
+            if (rr > half) rr = __fsub_rn(rr, p);
+            else if (rr < -half) rr = __fadd_rn(rr, p);
+            if (neg) rr = -rr;
+            out[((int64_t)l * rows_pad + r) * kpad + c] = __float2half_rn(rr);
+        }
+    }
+}
+
+// ---- device: residue GEMM, tensor cores ---------------------------------------------------
+
+constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64, TC_STAGES = 4;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;   // 16 KB
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;   // 32 KB
+constexpr int TC_SMEM = TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 1024 /*align*/ + 256 /*barriers*/;
+
+__device__ __forceinline__ float mod_sym(float x, float p, float invp)
+{
+    float q = rintf(__fmul_rn(x, invp));
+    return __fmaf_rn(-q, p, x);   // in (-p, p), exact
+}
+
+// One CTA: a 128 x 256 tile of the residue product for modulus blockIdx.z.
+// Warp 0: TMA producer. Warp 1: TMEM owner and MMA issuer. Warps 2-5:
+// epilogue (TMEM lane quadrant = warp % 4).
+__global__ void __launch_bounds__(192, 1)
+    k_oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t Mp,
+                 int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint8_t *__restrict__ R, int *status)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + TC_STAGES * TC_A_BYTES;
+    uint64_t *bars = (uint64_t *)(smem + TC_STAGES * (TC_A_BYTES + TC_B_BYTES));
+    uint64_t *full = bars;                 // [TC_STAGES]
+    uint64_t *empty = bars + TC_STAGES;    // [TC_STAGES]
+    uint64_t *accf = bars + 2 * TC_STAGES; // [2]
+    uint64_t *acce = accf + 2;             // [2]
+    uint64_t *drain = acce + 2;            // [1] all MMAs of this CTA retired
+    uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile_n = blockIdx.x, tile_m = blockIdx.y, l = blockIdx.z;
+    const int nsteps = (int)(Kp / TC_BK);
+    const int kcs = kChunk / TC_BK;
+    const int nch = (nsteps + kcs - 1) / kcs;
+
+    if (warp == 0 && lane == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            sm100::mbar_init(&full[s], 1);
+            sm100::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            sm100::mbar_init(&accf[b], 1);
+            sm100::mbar_init(&acce[b], 128);
+        }
+        sm100::mbar_init(drain, 1);
+        sm100::fence_mbar_init();
+    }
+    if (warp == 1) {
+        sm100::tmem_alloc(tmem_slot, 512);
+        sm100::tmem_relinquish();
+    }
+    sm100::tc_fence_before();
+    __syncthreads();
+    sm100::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            sm100::tma_prefetch_desc(&tmA);
+            sm100::tma_prefetch_desc(&tmB);
+            const int32_t ya = (int32_t)(l * Mp + (int64_t)tile_m * TC_BM);
+            const int32_t yb = (int32_t)(l * Np + (int64_t)tile_n * TC_BN);
+            int issued = 0;
+            for (int step = 0; step < nsteps; ++step) {
+                int s = step % TC_STAGES, u = step / TC_STAGES;
+                if (u > 0 && !sm100::mbar_wait(&empty[s], (u - 1) & 1, status, 1)) break;
+                sm100::mbar_arrive_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
+                sm100::tma_load_2d(sA + s * TC_A_BYTES, &tmA, &full[s], step * TC_BK, ya);
+                sm100::tma_load_2d(sB + s * TC_B_BYTES, &tmB, &full[s], step * TC_BK, yb);
+                issued = step + 1;
+            }
+            // Never leave with copies in flight: wait (bounded) for the last
+            // use of every stage this thread issued.
+            for (int step = (issued > TC_STAGES ? issued - TC_STAGES : 0); step < issued; ++step)
+                sm100::mbar_wait(&full[step % TC_STAGES], (step / TC_STAGES) & 1, nullptr, 0);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = sm100::idesc_f16_f32(TC_BM, TC_BN);
+            bool ok = true;
+            for (int c = 0; c < nch && ok; ++c) {
+                const int b = c & 1;
+                if (c >= 2) {
+                    if (!sm100::mbar_wait(&acce[b], ((c - 2) >> 1) & 1, status, 2)) { ok = false; break; }
+                    sm100::tc_fence_after();
+                }
+                const int s0 = c * kcs, s1 = min(nsteps, s0 + kcs);
+                for (int step = s0; step < s1; ++step) {
+                    const int s = step % TC_STAGES;
+                    if (!sm100::mbar_wait(&full[s], (step / TC_STAGES) & 1, status, 3)) { ok = false; break; }
+                    sm100::tc_fence_after();
+                    const uint64_t ad = sm100::smem_desc_sw128(sm100::smem_u32(sA + s * TC_A_BYTES));
+                    const uint64_t bd = sm100::smem_desc_sw128(sm100::smem_u32(sB + s * TC_B_BYTES));
+#pragma unroll
+                    for (int kk = 0; kk < TC_BK / 16; ++kk) {
+                        uint32_t acc = (c >= 2 || step > s0 || kk > 0) ? 1u : 0u;
+                        sm100::mma_f16(tmem + b * TC_BN, ad + 2 * kk, bd + 2 * kk, idesc, acc);
+                    }
+                    sm100::mma_commit(&empty[s]);
+                }
+                if (ok) sm100::mma_commit(&accf[b]);
+            }
+            // Drain: no MMA may still be writing TMEM when it is freed.
+            sm100::mma_commit(drain);
+            sm100::mbar_wait(drain, 0, nullptr, 0);
+        }
+    } else {
+        // ---- epilogue: 128 threads, one TMEM lane (tile row) each
+        const int q = warp & 3;
+        const int row = q * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        const float p = P.p[l], invp = P.invp[l];
+        bool ok = true;
+        for (int c = 0; c < nch && ok; ++c) {
+            const int b = c & 1;
+            // warp-uniform outcome before the .sync.aligned TMEM accesses
+            if (!__all_sync(0xffffffffu, sm100::mbar_wait(&accf[b], (c >> 1) & 1, status, 4))) { ok = false; break; }
+            sm100::tc_fence_after();
+#pragma unroll 1
+            for (int sl = 0; sl < TC_BN / 32; ++sl) {
+                uint32_t r[32];
+                const uint32_t ta = lane_base + b * TC_BN + sl * 32;
+                sm100::tmem_ld32(ta, r);
+                sm100::tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 32; ++i) r[i] = __float_as_uint(mod_sym(__uint_as_float(r[i]), p, invp));
+                sm100::tmem_st32(ta, r);
+            }
+            sm100::tmem_wait_st();
+            sm100::tc_fence_before();
+            sm100::mbar_arrive(&acce[b]);
+        }
+        if (ok) {
+            // Both accumulators now hold reduced partial residues; combine and
+            // store c = (P + Q) mod p in [0, p) as R[l][j][i].
+            const int64_t i = (int64_t)tile_m * TC_BM + row;
+#pragma unroll 1
+            for (int sl = 0; sl < TC_BN / 32; ++sl) {
+                uint32_t r0[32], r1[32];
+                sm100::tmem_ld32(lane_base + sl * 32, r0);
+                if (nch > 1) sm100::tmem_ld32(lane_base + TC_BN + sl * 32, r1);
+                sm100::tmem_wait_ld();
+#pragma unroll
+                for (int t = 0; t < 32; ++t) {
+                    float v = __uint_as_float(r0[t]);
+                    if (nch > 1) v = __fadd_rn(v, __uint_as_float(r1[t]));
+                    float fq = floorf(__fmul_rn(v, invp));
+                    float rr = __fmaf_rn(-fq, p, v);
+                    if (rr < 0.0f) rr = __fadd_rn(rr, p);
+                    if (rr >= p) rr = __fsub_rn(rr, p);
+                    const int64_t j = (int64_t)tile_n * TC_BN + sl * 32 + t;
+                    if (i < M && j < N) R[((int64_t)l * Np + j) * Mp + i] = (uint8_t)(int)rr;
+                }
+            }
+        }
+    }
+
+    sm100::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        __syncwarp();
+        sm100::tc_fence_after();
+        sm100::tmem_dealloc(tmem, 512);
+    }
+}
+
+// ---- device: residue GEMM, CUDA cores (cross-check engine) ---------------------------------
+
+__global__ void __launch_bounds__(256) k_oz_gemm_simt(const __half *__restrict__ A, const __half *__restrict__ B,
+                                                      int64_t Mp, int64_t Np, int64_t Kp, int64_t M, int64_t N,
+                                                      OzModParams P, uint8_t *__restrict__ R)
+{
+    __shared__ float sa[16][65], sb[16][65];
+    const int l = blockIdx.z;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int64_t i = (int64_t)blockIdx.y * 16 + ty, j = (int64_t)blockIdx.x * 16 + tx;
+    const __half *Al = A + (int64_t)l * Mp * Kp;
+    const __half *Bl = B + (int64_t)l * Np * Kp;
+    int acc = 0;   // |sum| <= Kp * 127^2 < 2^31 for Kp < 133000
+    for (int64_t k0 = 0; k0 < Kp; k0 += 64) {
+        for (int t = threadIdx.x; t < 16 * 64; t += 256) {
+            int rr = t / 64, cc = t % 64;
+            int64_t gi = (int64_t)blockIdx.y * 16 + rr, gj = (int64_t)blockIdx.x * 16 + rr;
+            sa[rr][cc] = __half2float(Al[gi * Kp + k0 + cc]);
+            sb[rr][cc] = __half2float(Bl[gj * Kp + k0 + cc]);
+        }
+        __syncthreads();
+        for (int cc = 0; cc < 64; ++cc) acc += (int)sa[ty][cc] * (int)sb[tx][cc];
+        __syncthreads();
+    }
+    if (i < M && j < N) {
+        int p = (int)P.p[l];
+        int r = acc % p;
+        if (r < 0) r += p;
+        R[((int64_t)l * Np + j) * Mp + i] = (uint8_t)r;
+    }
+}
+
+// ---- device: CRT reconstruction ----------------------------------------------------------
+
+__device__ __forceinline__ uint32_t limb_at(const uint32_t *x, int idx) { return (idx >= 0 && idx < kNL) ? x[idx] : 0u; }
+
+// floor(X / 2^pos) mod 2^53 (pos may be negative: X * 2^-pos).
+__device__ __forceinline__ uint64_t bits53_at(const uint32_t *x, int pos)
+{
+    int w = pos >> 5;           // floor division
+    int sh = pos & 31;
+    uint64_t lo = (uint64_t)limb_at(x, w) | ((uint64_t)limb_at(x, w + 1) << 32);
+    uint64_t hi = limb_at(x, w + 2);
+    uint64_t v = sh ? ((lo >> sh) | (hi << (64 - sh))) : lo;
+    return v & ((1ull << 53) - 1);
+}
+
+// v * 2^e for an integer 0 <= v < 2^54, as an exact (or correctly rounded on
+// underflow) double.
+__device__ __forceinline__ double scaled_u54(uint64_t v, int e)
+{
+    if (v == 0) return 0.0;
+    int lz = __clzll((long long)v) - 11;   // leading zeros within 53 bits (may be -1 for 2^53)
+    int64_t mant;
+    int ex;
+    if (lz >= 0) {
+        mant = (int64_t)(v << lz);
+        ex = e - lz + 52;
+    } else {   // v == 2^53 exactly (after rounding)
+        mant = (int64_t)(v >> 1);
+        ex = e + 53;
+    }
+    if (ex >= -1022 && ex <= 1023) {
+        uint64_t b = ((uint64_t)(ex + 1023) << 52) | ((uint64_t)mant & ((1ull << 52) - 1));
+        return __longlong_as_double((long long)b);
+    }
+    // outside the normal range: let the FP unit round (rare)
+    double d = (double)mant;
+    int e2 = ex - 52;
+    while (e2 > 1000) { d *= 0x1p1000; e2 -= 1000; }
+    while (e2 < -1000) { d *= 0x1p-1000; e2 += 1000; }
+    uint64_t pb = (uint64_t)(e2 + 1023) << 52;
+    return d * __longlong_as_double((long long)pb);
+}
+
+__global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, const uint8_t *__restrict__ R,
+                                                        int64_t Mp, int64_t Np, const int *__restrict__ ea,
+                                                        const int *__restrict__ eb, int bits, OzCrtParams K,
+                                                        dd::real alpha, int alpha_one, dd::real beta, int beta_kind,
+                                                        double2 *C, int64_t ldc, int uplo)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+        if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
+        uint64_t S[kNL];
+#pragma unroll
+        for (int t = 0; t < kNL; ++t) S[t] = 0;
+        float qf = 0.0f;
+        for (int l = 0; l < K.nmod; ++l) {
+            uint32_t c = R[((int64_t)l * Np + j) * Mp + i];
+            qf = __fmaf_rn((float)c, K.f[l], qf);
+#pragma unroll
+            for (int t = 0; t < kNL; ++t) S[t] += (uint64_t)c * K.W[l][t];
+        }
+        uint32_t x[kNL];
+        uint64_t carry = 0;
+#pragma unroll
+        for (int t = 0; t < kNL; ++t) {
+            uint64_t v = S[t] + carry;
+            x[t] = (uint32_t)v;
+            carry = v >> 32;
+        }
+        // X = S - q*M (two's complement over kNL limbs)
+        uint32_t qv = (uint32_t)rintf(qf);
+        uint64_t borrow = 0, mc = 0;
+#pragma unroll
+        for (int t = 0; t < kNL; ++t) {
+            uint64_t prod = (uint64_t)qv * K.M[t] + mc;
+            mc = prod >> 32;
+            uint64_t sub = (uint64_t)(uint32_t)prod + borrow;
+            uint64_t v = (uint64_t)x[t] - sub;
+            x[t] = (uint32_t)v;
+            borrow = (v >> 63) & 1;   // underflow
+        }
+        const bool neg = (x[kNL - 1] >> 31) != 0;
+        if (neg) {
+            uint64_t cy = 1;
+#pragma unroll
+            for (int t = 0; t < kNL; ++t) {
+                uint64_t v = (uint64_t)(~x[t]) + cy;
+                x[t] = (uint32_t)v;
+                cy = v >> 32;
+            }
+        }
+        int top = -1;
+#pragma unroll
+        for (int t = kNL - 1; t >= 0; --t)
+            if (top < 0 && x[t] != 0) top = t;
+        dd::real v = dd::make(0.0, 0.0);
+        if (top >= 0 && ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
+            const int P = top * 32 + 31 - __clz((int)x[top]);
+            const int S2 = (bits - 2 - ea[i]) + (bits - 2 - eb[j]);
+            uint64_t a = bits53_at(x, P - 52);
+            uint64_t b = bits53_at(x, P - 105);
+            uint64_t c = bits53_at(x, P - 158);
+            // round b with c, then hi with b (|lo| <= ulp(hi)/2)
+            if (c >> 52) ++b;
+            int64_t bs = (int64_t)b;
+            if (bs >= (1ll << 52)) {
+                ++a;
+                bs -= (1ll << 53);
+            }
+            double hi = scaled_u54(a, P - 52 - S2);
+            double lo = bs >= 0 ? scaled_u54((uint64_t)bs, P - 105 - S2) : -scaled_u54((uint64_t)(-bs), P - 105 - S2);
+            v = dd::make(neg ? -hi : hi, neg ? -lo : lo);
+        }
+        double2 *pc = C + i + j * ldc;
+        dd::real r = alpha_one ? v : dd::mul_fast(alpha, v);
+        if (beta_kind == 0) {
+            dd::store(pc, r);
+        } else {
+            dd::real c0 = dd::load(pc);
+            if (beta_kind == 2) c0 = dd::mul_exact(c0, beta);
+            dd::store(pc, dd::add_exact(c0, r));
+        }
+    }
+}
+
+// Max / non-finite summary of the exponent vectors.
+__global__ void k_oz_exp_summary(const int *e, int64_t n, int *out)
+{
+    int mx = kNoExp;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+        mx = max(mx, e[t]);
+    for (int off = 16; off > 0; off >>= 1) mx = max(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, mx);
+}
+
+// ---- host ---------------------------------------------------------------------------------
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+bool get_encode()
+{
+    std::call_once(g_encode_once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+        cudaGetLastError();
+    });
+    return g_encode != nullptr;
+}
+
+bool make_map(CUtensorMap *map, const void *base, uint64_t kpad, uint64_t rows, uint32_t box_rows, const char *routine)
+{
+    cuuint64_t dims[2] = {kpad, rows};
+    cuuint64_t strides[1] = {kpad * 2};
+    cuuint32_t box[2] = {64, box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(base), dims, strides, box, es,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error(routine, MWBLAS_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        return false;
+    }
+    return true;
+}
+
+void fill_res_params(const Moduli &md, OzResParams &rp, OzModParams &mp)
+{
+    rp.nmod = md.n;
+    for (int l = 0; l < md.n; ++l) {
+        int p = md.p[l];
+        rp.p[l] = mp.p[l] = (float)p;
+        rp.invp[l] = mp.invp[l] = 1.0f / (float)p;
+        int64_t t = 1;
+        for (int q = 0; q < kResLimbs; ++q) {
+            rp.t[l][q] = (float)t;
+            t = (t * 2048) % p;
+        }
+    }
+}
+
+void fill_crt_params(const Moduli &md, OzCrtParams &cp)
+{
+    cp.nmod = md.n;
+    uint32_t Mb[kNL] = {1};
+    for (int t = 1; t < kNL; ++t) Mb[t] = 0;
+    for (int l = 0; l < md.n; ++l) big_mul_small(Mb, kNL, (uint32_t)md.p[l]);
+    memcpy(cp.M, Mb, sizeof(Mb));
+    for (int l = 0; l < md.n; ++l) {
+        uint32_t Ml[kNL];
+        memcpy(Ml, Mb, sizeof(Mb));
+        big_divmod_small(Ml, kNL, (uint32_t)md.p[l]);
+        uint32_t tmp[kNL];
+        memcpy(tmp, Ml, sizeof(Ml));
+        int64_t mlmod = big_divmod_small(tmp, kNL, (uint32_t)md.p[l]);
+        int64_t u = inv_mod(mlmod, md.p[l]);
+        big_mul_small(Ml, kNL, (uint32_t)u);
+        memcpy(cp.W[l], Ml, sizeof(Ml));
+        cp.f[l] = (float)((double)u / (double)md.p[l]);
+    }
+}
+
+unsigned blocks_cap(int64_t want)
+{
+    int64_t cap = 65535;
+    if (want > cap) want = cap;
+    return (unsigned)(want < 1 ? 1 : want);
+}
+
+}  // namespace
+
+bool ozaki_available()
+{
+    const char *e = getenv("MWBLAS_OZAKI");
+    if (e && !strcmp(e, "0")) return false;
+    int dev = 0, major = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    if (major != 10) return false;
+    return get_encode();
+}
+
+int ozaki_last_moduli() { return g_last_moduli; }
+
+bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
+{
+    // Split K so that the residue sums and the CRT bound stay in range.
+    const int64_t kmax = 65536;
+    if (g0.k > kmax) {
+        GemmArgs g = g0;
+        for (int64_t k0 = 0; k0 < g0.k; k0 += kmax) {
+            g.k = (g0.k - k0 < kmax) ? g0.k - k0 : kmax;
+            g.A = (const double2 *)g0.A + (g0.ta ? k0 : k0 * g0.lda);
+            g.B = (const double2 *)g0.B + (g0.tb ? k0 * g0.ldb : k0);
+            if (k0 > 0) {
+                g.beta = dd_host{1.0, 0.0};
+                g.beta_kind = 1;
+            }
+            if (!gemm_ozaki_real(g, bits_req, routine)) return false;
+        }
+        return true;
+    }
+    const GemmArgs &g = g0;
+    const int64_t m = g.m, n = g.n, k = g.k;
+    const int64_t Mp = (m + TC_BM - 1) / TC_BM * TC_BM;
+    const int64_t Np = (n + TC_BN - 1) / TC_BN * TC_BN;
+    const int64_t Kp = (k + TC_BK - 1) / TC_BK * TC_BK;
+
+    // 1. exponent bounds of the rows of op(A) / columns of op(B)
+    int *ex = (int *)dev_alloc(sizeof(int) * (size_t)(m + n + 2), routine);
+    if (!ex) return false;
+    int *ea = ex, *eb = ex + m, *summ = ex + m + n;
+    launch_exp_rows_of_op(g.A, g.ta ? k : m, g.ta ? m : k, g.lda, g.ta, 1, ea);
+    launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, 1, eb);
+    cudaMemsetAsync(summ, 0x80, 2 * sizeof(int), stream());
+    k_oz_exp_summary<<<blocks_cap((m + 255) / 256), 256, 0, stream()>>>(ea, m, summ);
+    k_oz_exp_summary<<<blocks_cap((n + 255) / 256), 256, 0, stream()>>>(eb, n, summ + 1);
+    count_launch(2);
+    int hsum[2];
+    if (!cuda_ok(cudaMemcpyAsync(hsum, summ, sizeof(hsum), cudaMemcpyDeviceToHost, stream()), routine, "exp summary") ||
+        !cuda_ok(cudaStreamSynchronize(stream()), routine, "exp summary sync")) {
+        dev_free(ex);
+        return false;
+    }
+    if (hsum[0] >= 1024 || hsum[1] >= 1024) {
+        // Inf/NaN present: the integer scheme has no representation for them;
+        // the FP64 engine propagates them as the reference does.
+        dev_free(ex);
+        return gemm_plain_real(g, routine);
+    }
+
+    // 2. precision and moduli
+    int bits = bits_req > 0 ? bits_req : 106;
+    if (bits < 40) bits = 40;
+    if (bits > 120) bits = 120;
+    double need = 2.0 * (bits - 1) + std::log2((double)(k > 1 ? k : 1)) + 1.0 + 4.0;
+    Moduli md = choose_moduli(need);
+    g_last_moduli = md.n;
+    OzResParams rp;
+    OzModParams mp;
+    OzCrtParams cp;
+    fill_res_params(md, rp, mp);
+    fill_crt_params(md, cp);
+
+    // 3. residue operands
+    const size_t a_bytes = (size_t)md.n * Mp * Kp * 2, b_bytes = (size_t)md.n * Np * Kp * 2;
+    const size_t r_bytes = (size_t)md.n * Np * Mp;
+    uint8_t *work = (uint8_t *)dev_alloc(a_bytes + b_bytes + r_bytes + 256, routine);
+    if (!work) {
+        dev_free(ex);
+        return false;
+    }
+    __half *Ares = (__half *)work;
+    __half *Bres = (__half *)(work + a_bytes);
+    uint8_t *R = work + a_bytes + b_bytes;
+    {
+        dim3 grid((unsigned)(Kp / 32), (unsigned)(Mp / 32));
+        if (!g.ta)   // op(A) = A: A[i + p*lda], contiguous along rows
+            k_oz_residues<true><<<grid, 256, 0, stream()>>>(m, k, (const double2 *)g.A, g.lda, ea, bits, rp, Ares, Mp,
+                                                            Kp, 0);
+        else
+            k_oz_residues<false><<<grid, 256, 0, stream()>>>(m, k, (const double2 *)g.A, g.lda, ea, bits, rp, Ares, Mp,
+                                                             Kp, 0);
+        dim3 gridb((unsigned)(Kp / 32), (unsigned)(Np / 32));
+        if (!g.tb)   // op(B)(p, j) = B[p + j*ldb]: rows j, contiguous along p
+            k_oz_residues<false><<<gridb, 256, 0, stream()>>>(n, k, (const double2 *)g.B, g.ldb, eb, bits, rp, Bres,
+                                                              Np, Kp, 0);
+        else
+            k_oz_residues<true><<<gridb, 256, 0, stream()>>>(n, k, (const double2 *)g.B, g.ldb, eb, bits, rp, Bres,
+                                                             Np, Kp, 0);
+        count_launch(2);
+    }
+
+    // 4. residue GEMMs
+    bool ok = true;
+    if (mma_kind() == 0) {
+        CUtensorMap ma, mb;
+        ok = make_map(&ma, Ares, (uint64_t)Kp, (uint64_t)(md.n * Mp), TC_BM, routine) &&
+             make_map(&mb, Bres, (uint64_t)Kp, (uint64_t)(md.n * Np), TC_BN, routine);
+        if (ok) {
+            static bool attr_set = false;
+            if (!attr_set) {
+                cudaFuncSetAttribute(k_oz_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+                attr_set = true;
+            }
+            dim3 grid((unsigned)(Np / TC_BN), (unsigned)(Mp / TC_BM), (unsigned)md.n);
+            k_oz_gemm_tc<<<grid, 192, TC_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R, device_status_word());
+            count_launch();
+        }
+    } else {
+        dim3 grid((unsigned)(Np / 16), (unsigned)(Mp / 16), (unsigned)md.n);
+        k_oz_gemm_simt<<<grid, 256, 0, stream()>>>(Ares, Bres, Mp, Np, Kp, m, n, mp, R);
+        count_launch();
+    }
+
+    // 5. reconstruction + alpha/beta
+    if (ok) {
+        dim3 grid((unsigned)((m + 255) / 256), blocks_cap(n));
+        bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
+        k_oz_reconstruct<<<grid, 256, 0, stream()>>>(m, n, R, Mp, Np, ea, eb, bits, cp,
+                                                    dd::make(g.alpha.hi, g.alpha.lo), alpha_one ? 1 : 0,
+                                                    dd::make(g.beta.hi, g.beta.lo), g.beta_kind, (double2 *)g.C,
+                                                    g.ldc, g.uplo);
+        count_launch();
+    }
+    dev_free(work);
+    dev_free(ex);
+    if (!ok) return false;
+    return check_device_status(routine);
+}
+
+bool gemm_ozaki_cplx(const GemmArgs &g, int bits, const char *routine)
+{
+    (void)bits;
+    // Complex products run on the FP64 engine until the complex residue
+    // combination lands.
+    return gemm_plain_cplx(g, routine);
 }
 
 }  // namespace mw
+
+extern "C" int mwblas_set_ozaki_mma(int kind)
+{
+    int prev = mw::mma_kind();
+    mw::g_mma_kind = kind ? 1 : 0;
+    return prev;
+}

@@ -11,7 +11,14 @@
 
 namespace sm100 {
 
-constexpr uint32_t kSpinLimit = 1u << 26;   // ~seconds of polling at most
+constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s: far above any legitimate wait
+
+__device__ __forceinline__ uint64_t globaltimer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -54,16 +61,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity to complete. On timeout
-// writes `code` to *status (first writer wins) and returns false.
+// Bounded wait for the phase with the given parity to complete. Gives up
+// after kWaitLimitNs, or as soon as another role has recorded a failure in
+// *status; on its own timeout writes `code` to *status (first writer wins).
+// Returns false when it gave up.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code)
 {
-    for (uint32_t i = 0; i < kSpinLimit; ++i) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (status && *(volatile int *)status != 0) return false;   // another role gave up
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    while (true) {
+        for (int i = 0; i < 32; ++i)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (status && *(volatile int *)status != 0) return false;
+        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+            if (status) atomicCAS(status, 0, code);
+            return false;
+        }
     }
-    if (status) atomicCAS(status, 0, code);
-    return false;
 }
 
 // ---- TMA ----------------------------------------------------------------------

@@ -204,6 +204,11 @@ void mgemm_ozaki_64_(const char *transa, const char *transb, const int64_t *m,
 int mwblas_set_ozaki_bits(int bits);
 /* Moduli count used by the most recent Ozaki GEMM on this thread. */
 int mwblas_last_ozaki_moduli(void);
+/* Residue-GEMM unit of the Ozaki engine: 0 = tcgen05 tensor cores (default),
+ * 1 = CUDA cores (an independent exact path used to cross-check the tensor
+ * cores; the MWBLAS_OZAKI_MMA=simt environment variable selects it too).
+ * Both produce bit-identical results. Returns the previous value. */
+int mwblas_set_ozaki_mma(int kind);
 
 /* Team size used to reproduce the reference's per-thread body/tail split in
  * the bit-exact level-1 routines (mscal/maxpy/wscal/wmscal).  0 = follow the

@@ -1,0 +1,114 @@
+"""Ozaki-scheme (integer-exact tensor-core) GEMM parity on the GPU.
+
+* normwise error against the binary128 oracle within the reference's GEMM
+  tolerance max(10, 4k) * 2^-104, on the reference's value distribution and
+  on an exponent-spread stress input (rows of A / columns of B scaled by 2^e,
+  e uniform in [-30, 30]);
+* the tcgen05 residue GEMM and the independent CUDA-core residue GEMM give
+  bit-identical results (both are exact integer computations);
+* non-finite inputs take the FP64 engine (the integer scheme cannot carry them).
+"""
+import numpy as np
+import pytest
+
+from conftest import mwb, orc
+
+pytestmark = pytest.mark.gpu
+
+
+def op_norm(alpha, k, A, B, beta, C0):
+    return orc.dd_abs(alpha) * k * orc.dd_absmax(A) * orc.dd_absmax(B) + orc.dd_abs(beta) * orc.dd_absmax(C0)
+
+
+SHAPES = [(1, 1, 1), (5, 3, 70), (128, 256, 64), (130, 300, 1500), (257, 129, 2100), (64, 600, 33)]
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
+def test_ozaki_matches_oracle(gpu, oracle, rng, ta, tb):
+    for (m, n, k) in SHAPES:
+        lda = (m if ta == "N" else k) + 1
+        ldb = (k if tb == "N" else n) + 2
+        ldc = m + 3
+        A = mwb.dd_matrix(rng, m if ta == "N" else k, k if ta == "N" else m, lda)
+        B = mwb.dd_matrix(rng, k if tb == "N" else n, n if tb == "N" else k, ldb)
+        C0 = mwb.dd_matrix(rng, m, n, ldc, fill=-7.37e18)
+        al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+        want = oracle.qgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0.copy(), ldc)
+        got = C0.copy()
+        gpu.mgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, got, ldc, engine="ozaki")
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        assert gpu.lib.mwblas_last_ozaki_moduli() >= 10
+        assert np.all(got[:, m:] == -7.37e18)
+        err = orc.normwise_error(got[:, :m], want[:, :m], op_norm(al, k, A, B, be, C0[:, :m]))
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (ta, tb, m, n, k, err)
+
+
+def test_tensor_core_and_cuda_core_paths_bit_identical(gpu, rng):
+    m, n, k = 200, 300, 2500
+    A = mwb.dd_matrix(rng, m, k)
+    B = mwb.dd_matrix(rng, k, n)
+    al, be = mwb.random_dd(rng, ()), np.zeros(2)
+    outs = []
+    for kind in (0, 1):
+        prev = gpu.lib.mwblas_set_ozaki_mma(kind)
+        try:
+            c = np.zeros((n, m, 2))
+            gpu.mgemm("N", "N", m, n, k, al, A, m, B, k, be, c, m, engine="ozaki")
+            assert gpu.last_error()[0] == 0, gpu.last_error()
+            outs.append(c)
+        finally:
+            gpu.lib.mwblas_set_ozaki_mma(prev)
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
+def test_exponent_spread_stress(gpu, oracle, rng):
+    """Entries m_ij * 2^e with e uniform in [-30, 30] per row of A / column of B."""
+    m, n, k = 192, 160, 777
+    A = mwb.dd_matrix(rng, m, k)
+    B = mwb.dd_matrix(rng, k, n)
+    ea = rng.integers(-30, 31, size=m).astype(float)
+    eb = rng.integers(-30, 31, size=n).astype(float)
+    A *= (2.0 ** ea)[None, :, None]
+    B *= (2.0 ** eb)[:, None, None]
+    al, be = np.array([1.0, 0.0]), np.zeros(2)
+    want = oracle.qgemm("N", "N", m, n, k, al, A, m, B, k, be, np.zeros((n, m, 2)), m)
+    got = np.zeros((n, m, 2))
+    gpu.mgemm("N", "N", m, n, k, al, A, m, B, k, be, got, m, engine="ozaki")
+    assert gpu.last_error()[0] == 0
+    err = orc.normwise_error(got, want, op_norm(al, k, A, B, be, got))
+    assert err <= 4 * k * orc.EPS_DD, err
+    # per-element relative accuracy follows the per-row/column scaling
+    scale = (2.0 ** ea)[None, :] * (2.0 ** eb)[:, None] * k
+    rel = orc.dd_diff_abs(got, want) / scale
+    assert float(rel.max()) <= 4 * k * orc.EPS_DD * 4
+
+
+def test_nonfinite_inputs_use_fp64_engine(gpu, rng):
+    m, n, k = 40, 30, 50
+    A = mwb.dd_matrix(rng, m, k)
+    B = mwb.dd_matrix(rng, k, n)
+    A[3, 5] = (np.inf, 0.0)
+    c1 = np.zeros((n, m, 2)); c2 = np.zeros((n, m, 2))
+    gpu.mgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, c1, m, engine="ozaki")
+    gpu.mgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, c2, m, engine="plain")
+    np.testing.assert_array_equal(np.isfinite(c1), np.isfinite(c2))
+
+
+def test_auto_engine_and_bits_control(gpu, oracle, rng):
+    m = n = k = 300
+    A = mwb.dd_matrix(rng, m, k); B = mwb.dd_matrix(rng, k, n)
+    want = oracle.qgemm("N", "N", m, n, k, np.array([1.0, 0]), A, m, B, k, np.zeros(2), np.zeros((n, m, 2)), m)
+    prev = gpu.lib.mwblas_set_ozaki_bits(60)
+    try:
+        got = np.zeros((n, m, 2))
+        gpu.mgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, got, m, engine="ozaki")
+        few = gpu.lib.mwblas_last_ozaki_moduli()
+        err60 = orc.normwise_error(got, want, k * orc.dd_absmax(A) * orc.dd_absmax(B))
+    finally:
+        gpu.lib.mwblas_set_ozaki_bits(prev)
+    got = np.zeros((n, m, 2))
+    gpu.mgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, got, m, engine="ozaki")
+    many = gpu.lib.mwblas_last_ozaki_moduli()
+    err = orc.normwise_error(got, want, k * orc.dd_absmax(A) * orc.dd_absmax(B))
+    assert few < many
+    assert err < err60 and err60 < 2.0 ** -50 and err <= 4 * k * orc.EPS_DD
