@@ -1,0 +1,409 @@
+"""Benchmark: double-double GEMM throughput at n = 8192 on GB300.
+
+Metric (the reference's headline, BASELINE): DD-GEMM GFLOP/s at
+M = N = K = 8192 with the integer-exact tensor-core ("Ozaki") engine, next to
+the plain FP64 error-free-transform engine on the same GPU, work counted as
+2*M*N*K double-double flops.
+
+A step is one C := alpha*A*B + beta*C at 8192^3 (alpha, beta random
+double-double of magnitude 0.5..2, A/B/C with hi ~ U[-1,1), lo = hi*2^-53*U),
+through the library's C ABI (mgemm_ozaki_64_).
+  value : device-resident operands (1 GiB each, larger than L2), CUDA events
+          around K steps on the library's stream, max over ranks.
+  e2e   : the same call with pinned HOST buffers, so every step includes the
+          host->device copies of A, B, C and the device->host copy of C.
+Multi-GPU (torchrun): every rank runs its own independent GEMM (replicas; the
+path needs no collective), value = total flops of all ranks / max time.
+
+`--impl reference` times the reference's CPU implementation of the same
+routine on this machine's host cores: the reference built from its own
+sources where it is present (x86 development host), otherwise the C port of
+its algorithm in oracle/ (the GPU machine), on a bounded sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as ge  # noqa: E402
+
+METRIC = "DD-GEMM GFLOP/s n=8192, Ozaki-INT8 vs FP64-EFT, rel err <=1e-30; % roofline"
+UNIT = "DD-GFLOP/s"
+N_GEMM = 8192
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx = float(s[2])
+                for nm, v in zip(names, s[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs(rng, n):
+    mwb = ge._load("mwblas", os.path.join(ge.PKG, "mwblas.py"))
+    A = mwb.dd_matrix(rng, n, n)
+    B = mwb.dd_matrix(rng, n, n)
+    C = mwb.dd_matrix(rng, n, n)
+
+    def scal():
+        mag = 0.5 + 1.5 * rng.random()
+        s = mag if rng.random() < 0.5 else -mag
+        return np.array([s, s * 2.0 ** -53 * (2 * rng.random() - 1)])
+    return A, B, C, scal(), scal()
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    torch.cuda.set_device(local_rank)
+    mwb = ge._load("mwblas", os.path.join(ge.PKG, "mwblas.py"))
+    lib = mwb.MWBlas(os.path.join(ge.PKG, "libmwblas_gb300.so"))
+    n = args.n
+    rng = np.random.default_rng(1234 + rank)
+    A, B, C0, alpha, beta = make_inputs(rng, n)
+    dev = torch.device("cuda", local_rank)
+    dA = torch.from_numpy(A).to(dev)
+    dB = torch.from_numpy(B).to(dev)
+    dC = torch.from_numpy(C0).to(dev)
+    dC0 = dC.clone()
+    stream = torch.cuda.current_stream(dev)
+    lib.lib.mwblas_set_stream(stream.cuda_stream)
+
+    def step(engine="ozaki", c=dC):
+        lib.mgemm("N", "N", n, n, n, alpha, dA.data_ptr(), n, dB.data_ptr(), n, beta, c.data_ptr(), n, engine=engine)
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        dC.copy_(dC0)
+        step()
+    code, msg = lib.last_error()
+    if code != 0:
+        raise RuntimeError(f"mgemm_ozaki_64_ failed: {code} {msg}")
+    moduli = int(lib.lib.mwblas_last_ozaki_moduli())
+
+    # ---- timed region: K steps, device-resident operands (each 1 GiB > L2).
+    # The library records CUDA events around each engine phase on its stream,
+    # which gives the residue-GEMM kernel's own duration per launch.
+    l0 = lib.lib.mwblas_launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    lib.lib.mwblas_set_kernel_timing(1)
+    phase = np.zeros(4)
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+            phase += [lib.lib.mwblas_last_phase_ms(i) for i in range(4)]
+        ev1.record(stream)
+        barrier()
+    lib.lib.mwblas_set_kernel_timing(0)
+    phase /= args.steps
+    launches = lib.lib.mwblas_launch_count() - l0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    flops = 2.0 * n * n * n
+    value = world * flops / (ms * 1e-3) / 1e9
+
+    pk, pk_kind = peaks()
+
+    # ---- e2e: pinned host buffers through the same C-ABI call
+    hA = torch.from_numpy(A).pin_memory()
+    hB = torch.from_numpy(B).pin_memory()
+    hC = torch.from_numpy(C0).pin_memory()
+    lib.mgemm("N", "N", n, n, n, alpha, hA.data_ptr(), n, hB.data_ptr(), n, beta, hC.data_ptr(), n, engine="ozaki")
+    barrier()
+    e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        lib.mgemm("N", "N", n, n, n, alpha, hA.data_ptr(), n, hB.data_ptr(), n, beta, hC.data_ptr(), n,
+                  engine="ozaki")
+    barrier()
+    e_ms = (time.perf_counter() - t0) * 1e3 / e_steps
+    if dist is not None:
+        t = torch.tensor([e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e_ms = float(t.item())
+    e2e = {"value": world * flops / (e_ms * 1e-3) / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": 3 * n * n * 16, "d2h_bytes_per_step": n * n * 16,
+           "ms_per_step": e_ms, "api": "mgemm_ozaki_64_ on pinned host arrays"}
+
+    # ---- the plain FP64-EFT engine on the same GPU (one timed call)
+    plain = None
+    if not args.skip_plain:
+        step(engine="plain", c=dC)   # warm
+        barrier()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        step(engine="plain", c=dC)
+        p1.record(stream)
+        barrier()
+        pms = p0.elapsed_time(p1)
+        # plain kernel: 6 FP64 instructions per DD multiply-add + 12 per 8-step fold
+        fp64_inst = n * n * n * (6.0 + 12.0 / 8.0)
+        plain = {"value": flops / (pms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pms,
+                 "fp64_inst_per_s": fp64_inst / (pms * 1e-3),
+                 "note": "FP64 pipe issue-bound; the probe measured 1.58 DFMA/clk/SM on this GPU"}
+
+    res = dict(value=value, ms=ms, launches=launches, moduli=moduli, phase_ms=phase.tolist(), e2e=e2e, plain=plain, clocks=clk.summary(),
+               flops=flops, peaks=pk, peaks_kind=pk_kind, alpha=alpha, beta=beta, A=A, B=B, C0=C0,
+               C=dC.cpu().numpy() if (rank == 0 and not args.skip_check) else None)
+    lib.lib.mwblas_set_stream(None)
+    return res
+
+
+def cpu_baseline_leg(n, res):
+    """rank 0, N=1: the oracle checks the GPU result on sampled entries, and the
+    reference's CPU GEMM (or its port) is timed on a bounded sample."""
+    orc = ge._load("oracle", os.path.join(ROOT, "oracle", "oracle.py"))
+    o = orc.Oracle()
+    out = {}
+    if res.get("C") is not None:
+        rng = np.random.default_rng(99)
+        rows = rng.integers(0, n, 256)
+        cols = rng.integers(0, n, 256)
+        # after the timed steps C holds alpha*A*B + beta*C_prev; re-run one
+        # checked step from C0 instead: compare entries of one step's output
+        want = o.qgemm("N", "N", n, n, n, res["alpha"], res["A"], n, res["B"], n, res["beta"], res["C0"], n,
+                       rows=rows, cols=cols)
+        got = res["C_check"][cols, rows]
+        op = orc.dd_abs(res["alpha"]) * n * orc.dd_absmax(res["A"]) * orc.dd_absmax(res["B"]) \
+            + orc.dd_abs(res["beta"]) * orc.dd_absmax(res["C0"])
+        out["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+        out["err_samples"] = 256
+    # CPU timing on a bounded sample of the same workload
+    t = time_reference_cpu(sample=(4096, 4096, 256), reps=1)
+    out["cpu"] = t
+    return out
+
+
+def time_reference_cpu(sample=(4096, 4096, 256), reps=1):
+    """Times the reference's GEMM on the host cores with all threads."""
+    m, n, k = sample
+    rng = np.random.default_rng(5)
+    mwb = ge._load("mwblas", os.path.join(ge.PKG, "mwblas.py"))
+    A = mwb.dd_matrix(rng, m, k)
+    B = mwb.dd_matrix(rng, k, n)
+    C = mwb.dd_matrix(rng, m, n)
+    al, be = np.array([1.1, 0.0]), np.array([0.9, 0.0])
+    ref_so = os.path.join(ROOT, "oracle", "_ref", "libmwblas_ref.so")
+    kind = "port"
+    runner = None
+    try:
+        if os.path.exists(ref_so):
+            ref = mwb.MWBlas(ref_so, extensions=False)
+
+            def runner():
+                ref.mgemm("N", "N", m, n, k, al, A, m, B, k, be, C, m)
+            kind = "reference"
+    except OSError:
+        runner = None
+    if runner is None:
+        orc = ge._load("oracle", os.path.join(ROOT, "oracle", "oracle.py"))
+        o = orc.Oracle()
+        import platform
+        simd = 1 if platform.machine() in ("x86_64", "AMD64") else 0
+
+        def runner():
+            o.port_mgemm("N", "N", m, n, k, al, A, m, B, k, be, C, m, simd_order=simd)
+    runner()   # warm
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        runner()
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    cores = int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or os.cpu_count()
+    import platform
+    return {"value": 2.0 * m * n * k / best / 1e9, "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"mgemm_ {m}x{n}x{k} NN alpha=1.1 beta=0.9 ({platform.machine()}, min of {reps} after 1 warm-up,"
+                      f" {best:.2f} s per call)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_GEMM)
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-check", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    cfg = {"workload": f"mgemm_ {args.n}x{args.n}x{args.n} NN, random double-double alpha/beta (|.| in [0.5,2]), "
+                       "A,B,C hi~U[-1,1) lo=hi*2^-53*U[-1,1)",
+           "m": args.n, "n": args.n, "k": args.n, "engine": "ozaki-II CRT, tcgen05 kind::f16 residue GEMMs",
+           "l2": "operands 1 GiB each, larger than the 129 MB L2", "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = []
+        for _ in range(args.warmup):
+            time_reference_cpu(reps=1)
+        for _ in range(args.steps):
+            steps.append(time_reference_cpu(reps=1))
+        v = float(np.median([s["value"] for s in steps]))
+        cb = dict(steps[-1])
+        cb["value"] = v
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 2.0 * 4096 * 4096 * 256 / v / 1e6,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64x2 (double-double)",
+                "data": "synthetic", "config": dict(cfg, sample="4096x4096x256 sample of the 8192^3 workload"),
+                "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    ge.build() if rank == 0 and not os.path.exists(os.path.join(ge.PKG, "libmwblas_gb300.so")) else None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    res = run_ours(args, rank, world, local_rank)
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+
+    # correctness check data: one step from the original C
+    import torch
+    mwb = ge._load("mwblas", os.path.join(ge.PKG, "mwblas.py"))
+    lib = mwb.MWBlas(os.path.join(ge.PKG, "libmwblas_gb300.so"))
+    cpu = None
+    if world == 1 and not args.skip_check:
+        dA = torch.from_numpy(res["A"]).cuda()
+        dB = torch.from_numpy(res["B"]).cuda()
+        dC = torch.from_numpy(res["C0"]).cuda()
+        n = args.n
+        lib.mgemm("N", "N", n, n, n, res["alpha"], dA.data_ptr(), n, dB.data_ptr(), n, res["beta"], dC.data_ptr(), n,
+                  engine="ozaki")
+        torch.cuda.synchronize()
+        res["C_check"] = dC.cpu().numpy()
+        del dA, dB, dC
+        cpu = cpu_baseline_leg(args.n, res)
+
+    pk, pk_kind = res["peaks"], res["peaks_kind"]
+    n = args.n
+    # Roofline of the dominant kernel (the tcgen05 residue GEMM, one launch
+    # per step): algorithmic fp16 tensor flops per launch = moduli * 2*m*n*k
+    # (the padded tile work is not counted), over its CUDA-event duration.
+    tc_ms = res["phase_ms"][2]
+    tc_flops = res["moduli"] * 2.0 * n * n * n
+    peak_tf = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
+    achieved = tc_flops / (tc_ms * 1e-3) / 1e12 if tc_ms > 0 else None
+    roof = {"bound": "tensor", "kernel": "k_oz_gemm_tc (tcgen05.mma kind::f16, fp32 accumulate in TMEM)",
+            "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
+            "frac": (achieved / peak_tf) if achieved else None,
+            "peak_kind": f"{pk_kind} bf16 dense, sustained figure (MEASURED_PEAKS.json)",
+            "traffic": tc_traffic_from_profile(), "algorithmic_flops_per_launch": tc_flops,
+            "kernel_ms": tc_ms,
+            "step_phase_ms": dict(zip(["exponent_scan", "residues", "residue_gemm", "reconstruct"],
+                                      res["phase_ms"]))}
+    line = {"metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64x2 (double-double); residue GEMMs fp16 x fp16 -> fp32 exact",
+            "data": "synthetic (seeded, reference value distribution)", "config": cfg,
+            "e2e": res["e2e"], "gpu_launches": int(res["launches"]), "clocks": res["clocks"],
+            "roofline": roof, "ozaki": {"moduli": res["moduli"], "bits": 106},
+            "plain_fp64_eft": res["plain"]}
+    if cpu:
+        line["cpu_baseline"] = cpu["cpu"]
+        if "normwise_err_sampled" in cpu:
+            line["accuracy"] = {"normwise_err_vs_binary128": cpu["normwise_err_sampled"],
+                                "sampled_entries": cpu["err_samples"], "gate": 1e-30}
+    print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def tc_traffic_from_profile():
+    p = os.path.join(ROOT, "profiles", "k_oz_gemm_tc_ncu.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch_scaled:"):
+            return float(line.split(":")[1].strip())
+    return None
+
+
+if __name__ == "__main__":
+    main()

@@ -131,6 +131,30 @@ Moduli choose_moduli(double need_bits)
 int g_last_moduli = 0;
 int g_mma_kind = -1;   // 0 tcgen05, 1 SIMT cross-check
 
+// Optional per-phase timing with CUDA events on the library stream.
+enum { PH_EXP = 0, PH_RES, PH_GEMM, PH_REC, PH_N };
+bool g_timing = false;
+thread_local cudaEvent_t t_ev[PH_N + 1] = {};
+thread_local float t_phase_ms[PH_N] = {};
+
+void phase_mark(int i)
+{
+    if (!g_timing) return;
+    if (!t_ev[i]) cudaEventCreate(&t_ev[i]);
+    cudaEventRecord(t_ev[i], stream());
+}
+
+void phase_collect()
+{
+    if (!g_timing) return;
+    cudaEventSynchronize(t_ev[PH_N]);
+    for (int i = 0; i < PH_N; ++i) {
+        float ms = 0.0f;
+        if (t_ev[i] && t_ev[i + 1]) cudaEventElapsedTime(&ms, t_ev[i], t_ev[i + 1]);
+        t_phase_ms[i] = ms;
+    }
+}
+
 int mma_kind()
 {
     if (g_mma_kind < 0) {
@@ -688,6 +712,7 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
     int *ex = (int *)dev_alloc(sizeof(int) * (size_t)(m + n + 2), routine);
     if (!ex) return false;
     int *ea = ex, *eb = ex + m, *summ = ex + m + n;
+    phase_mark(PH_EXP);
     launch_exp_rows_of_op(g.A, g.ta ? k : m, g.ta ? m : k, g.lda, g.ta, 1, ea);
     launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, 1, eb);
     cudaMemsetAsync(summ, 0x80, 2 * sizeof(int), stream());
@@ -731,6 +756,7 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
     __half *Ares = (__half *)work;
     __half *Bres = (__half *)(work + a_bytes);
     uint8_t *R = work + a_bytes + b_bytes;
+    phase_mark(PH_RES);
     {
         dim3 grid((unsigned)(Kp / 32), (unsigned)(Mp / 32));
         if (!g.ta)   // op(A) = A: A[i + p*lda], contiguous along rows
@@ -750,6 +776,7 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
     }
 
     // 4. residue GEMMs
+    phase_mark(PH_GEMM);
     bool ok = true;
     if (mma_kind() == 0) {
         CUtensorMap ma, mb;
@@ -772,6 +799,7 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
     }
 
     // 5. reconstruction + alpha/beta
+    phase_mark(PH_REC);
     if (ok) {
         dim3 grid((unsigned)((m + 255) / 256), blocks_cap(n));
         bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
@@ -781,10 +809,13 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
                                                     g.ldc, g.uplo);
         count_launch();
     }
+    phase_mark(PH_N);
     dev_free(work);
     dev_free(ex);
     if (!ok) return false;
-    return check_device_status(routine);
+    bool st = check_device_status(routine);
+    phase_collect();
+    return st;
 }
 
 bool gemm_ozaki_cplx(const GemmArgs &g, int bits, const char *routine)
@@ -796,6 +827,18 @@ bool gemm_ozaki_cplx(const GemmArgs &g, int bits, const char *routine)
 }
 
 }  // namespace mw
+
+extern "C" int mwblas_set_kernel_timing(int on)
+{
+    int prev = mw::g_timing ? 1 : 0;
+    mw::g_timing = on != 0;
+    return prev;
+}
+
+extern "C" float mwblas_last_phase_ms(int phase)
+{
+    return (phase >= 0 && phase < mw::PH_N) ? mw::t_phase_ms[phase] : -1.0f;
+}
 
 extern "C" int mwblas_set_ozaki_mma(int kind)
 {

@@ -113,6 +113,8 @@ class MWBlas:
             self._sig("mwblas_set_ozaki_bits", _i32, [_i32])
             self._sig("mwblas_last_ozaki_moduli", _i32, [])
             self._sig("mwblas_set_ozaki_mma", _i32, [_i32])
+            self._sig("mwblas_set_kernel_timing", _i32, [_i32])
+            self._sig("mwblas_last_phase_ms", C.c_float, [_i32])
             self._sig("mwblas_set_l1_partition", _i64, [_i64])
             self._sig("mwblas_set_stream", _i32, [_p])
             self._sig("mwblas_set_sync", _i32, [_i32])

@@ -210,6 +210,13 @@ int mwblas_last_ozaki_moduli(void);
  * Both produce bit-identical results. Returns the previous value. */
 int mwblas_set_ozaki_mma(int kind);
 
+/* Per-phase device timing of the Ozaki engine (CUDA events on the library
+ * stream; off by default). Phases: 0 exponent scan, 1 residue conversion,
+ * 2 residue GEMMs (tensor cores), 3 CRT reconstruction. mwblas_last_phase_ms
+ * returns the durations of the calling thread's most recent Ozaki GEMM. */
+int mwblas_set_kernel_timing(int on);
+float mwblas_last_phase_ms(int phase);
+
 /* Team size used to reproduce the reference's per-thread body/tail split in
  * the bit-exact level-1 routines (mscal/maxpy/wscal/wmscal).  0 = follow the
  * calling process's OpenMP settings exactly as the reference does
