@@ -69,14 +69,16 @@ struct OzResParams {
     float t[kMaxMod][kResLimbs];   // 2^(11k) mod p
 };
 
+// Per residue-GEMM batch entry z (component * nmod + modulus).
 struct OzModParams {
-    float p[kMaxMod], invp[kMaxMod];
+    float p[3 * kMaxMod], invp[3 * kMaxMod];
 };
 
 struct OzCrtParams {
     int nmod;
     uint32_t W[kMaxMod][kNL];
     float f[kMaxMod];
+    float pm[kMaxMod];
     uint32_t M[kNL];
 };
 
@@ -199,56 +201,97 @@ __device__ __forceinline__ float u11_to_float(uint32_t c)
 // op(X) is rows x kdim; element (r, c) lives at X[r + c*ld] (ROWC) or
 // X[c + r*ld]. Writes out[l][r][c] (fp16, row stride kpad) for the padded
 // ranges r < rows_pad, c < kpad (zeros outside op(X)).
-template <bool ROWC>
+// Integer image F = round(v * 2^sc) of a double-double, as sign and 11-bit
+// limbs of |F| (bits <= 120 keeps |F| below 2^121).
+__device__ __forceinline__ void to_limbs(double2 v, int sc, float (&fl)[kResLimbs], bool &neg)
+{
+    __int128 F = fixed_round(v.x, sc) + fixed_round(v.y, sc);
+    neg = F < 0;
+    unsigned __int128 U = (unsigned __int128)(neg ? -F : F);
+#pragma unroll
+    for (int q = 0; q < kResLimbs; ++q) fl[q] = u11_to_float((uint32_t)(U >> (11 * q)) & 0x7FFu);
+}
+
+// Symmetric residue of +-|F| (limbs) modulo P.p[l], exact in fp32.
+__device__ __forceinline__ float sym_residue(const float (&fl)[kResLimbs], bool neg, const OzResParams &P, int l)
+{
+    float x = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kResLimbs; ++q) x = __fmaf_rn(fl[q], P.t[l][q], x);
+    float p = P.p[l];
+    float qq = rintf(__fmul_rn(x, P.invp[l]));
+    float rr = __fmaf_rn(-qq, p, x);
+    float half = 0.5f * p;
+    if (rr > half) rr = __fsub_rn(rr, p);
+    else if (rr < -half) rr = __fadd_rn(rr, p);
+    return neg ? -rr : rr;
+}
+
+// op(X) is rows x kdim; element (r, c) lives at X[r + c*ld] (ROWC) or
+// X[c + r*ld] (complex elements are two double2). Writes the residues for
+// every modulus as fp16, out[comp][l][r][c] (row stride kpad, component stride
+// nmod*rows_pad*kpad), over the padded ranges r < rows_pad, c < kpad (zeros
+// outside op(X)). Real: one component. Complex: the real part, the imaginary
+// part (negated when `conj`) and their sum, for the 3-product (Karatsuba)
+// complex multiply.
+template <bool ROWC, bool CPLX>
 __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim, const double2 *__restrict__ X,
                                                      int64_t ld, const int *__restrict__ rexp, int bits,
                                                      OzResParams P, __half *__restrict__ out, int64_t rows_pad,
-                                                     int64_t kpad, int negate_im)
+                                                     int64_t kpad, int conj)
 {
-    __shared__ double2 tile[32][33];
+    constexpr int E = CPLX ? 2 : 1;
+    __shared__ double2 tile[32][33][E];
     const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     for (int s = ty; s < 32; s += 8) {
         int64_t r = ROWC ? r0 + tx : r0 + s;
         int64_t c = ROWC ? c0 + s : c0 + tx;
-        double2 v = make_double2(0.0, 0.0);
-        if (r < rows && c < kdim) v = ROWC ? X[r + c * ld] : X[c + r * ld];
-        if (ROWC) tile[tx][s] = v;
-        else tile[s][tx] = v;
+        double2 v[E];
+#pragma unroll
+        for (int w = 0; w < E; ++w) v[w] = make_double2(0.0, 0.0);
+        if (r < rows && c < kdim) {
+            const double2 *src = X + E * (ROWC ? r + c * ld : c + r * ld);
+#pragma unroll
+            for (int w = 0; w < E; ++w) v[w] = src[w];
+        }
+#pragma unroll
+        for (int w = 0; w < E; ++w) {
+            if (ROWC) tile[tx][s][w] = v[w];
+            else tile[s][tx][w] = v[w];
+        }
     }
     __syncthreads();
+    const int64_t cstride = (int64_t)P.nmod * rows_pad * kpad;
     for (int s = ty; s < 32; s += 8) {
         int64_t r = r0 + s, c = c0 + tx;
         if (r >= rows_pad || c >= kpad) continue;
-        double2 v = tile[s][tx];
         int e = (r < rows) ? rexp[r] : kNoExp;
-        uint32_t limb[kResLimbs];
-        bool neg = false;
-        if (e <= kNoExp / 2) {
-            for (int q = 0; q < kResLimbs; ++q) limb[q] = 0;
+        const bool live = e > kNoExp / 2;
+        const int sc = bits - 2 - e;
+        float fr[kResLimbs], fi[kResLimbs];
+        bool nr = false, ni = false;
+        if (live) {
+            to_limbs(tile[s][tx][0], sc, fr, nr);
+            if (CPLX) to_limbs(tile[s][tx][E - 1], sc, fi, ni);
         } else {
-            int sc = bits - 2 - e;
-            __int128 F = fixed_round(v.x, sc) + fixed_round(v.y, sc);
-            neg = F < 0;
-            unsigned __int128 U = (unsigned __int128)(neg ? -F : F);
-            for (int q = 0; q < kResLimbs; ++q) limb[q] = (uint32_t)(U >> (11 * q)) & 0x7FFu;
+#pragma unroll
+            for (int q = 0; q < kResLimbs; ++q) fr[q] = fi[q] = 0.0f;
         }
-        if (negate_im) neg = !neg;
-        float fl[kResLimbs];
-#pragma unroll
-        for (int q = 0; q < kResLimbs; ++q) fl[q] = u11_to_float(limb[q]);
+        if (CPLX && conj) ni = !ni;
         for (int l = 0; l < P.nmod; ++l) {
-            float x = 0.0f;
-#pragma unroll
-            for (int q = 0; q < kResLimbs; ++q) x = __fmaf_rn(fl[q], P.t[l][q], x);
-            float p = P.p[l];
-            float qq = rintf(__fmul_rn(x, P.invp[l]));
-            float rr = __fmaf_rn(-qq, p, x);
-            float half = 0.5f * p;
-            if (rr > half) rr = __fsub_rn(rr, p);
-            else if (rr < -half) rr = __fadd_rn(rr, p);
-            if (neg) rr = -rr;
-            out[((int64_t)l * rows_pad + r) * kpad + c] = __float2half_rn(rr);
+            const int64_t o = ((int64_t)l * rows_pad + r) * kpad + c;
+            float rr = sym_residue(fr, nr, P, l);
+            out[o] = __float2half_rn(rr);
+            if (CPLX) {
+                float ii = sym_residue(fi, ni, P, l);
+                float ss = __fadd_rn(rr, ii);
+                float p = P.p[l], half = 0.5f * p;
+                if (ss > half) ss = __fsub_rn(ss, p);
+                else if (ss < -half) ss = __fadd_rn(ss, p);
+                out[cstride + o] = __float2half_rn(ii);
+                out[2 * cstride + o] = __float2half_rn(ss);
+            }
         }
     }
 }
@@ -271,8 +314,14 @@ __device__ __forceinline__ float mod_sym(float x, float p, float invp)
 // epilogue (TMEM lane quadrant = warp % 4).
 __global__ void __launch_bounds__(192, 1)
     k_oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t Mp,
-                 int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint8_t *__restrict__ R, int *status)
+                 int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint8_t *__restrict__ R, int *status,
+                 int uplo)
 {
+    // Triangular output (SYRK/HERK): tiles wholly outside the triangle do no work.
+    {
+        const int64_t i0 = (int64_t)blockIdx.y * TC_BM, j0 = (int64_t)blockIdx.x * TC_BN;
+        if ((uplo == 1 && i0 > j0 + TC_BN - 1) || (uplo == 2 && i0 + TC_BM - 1 < j0)) return;
+    }
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
@@ -581,6 +630,123 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, co
     }
 }
 
+// CRT of one residue vector c[l] (values in [0, p_l)) into a double-double
+// scaled by 2^-S2.
+__device__ __forceinline__ dd::real crt_to_dd(const uint32_t *c, const OzCrtParams &K, int S2)
+{
+    uint64_t S[kNL];
+#pragma unroll
+    for (int t = 0; t < kNL; ++t) S[t] = 0;
+    float qf = 0.0f;
+    for (int l = 0; l < K.nmod; ++l) {
+        qf = __fmaf_rn((float)c[l], K.f[l], qf);
+#pragma unroll
+        for (int t = 0; t < kNL; ++t) S[t] += (uint64_t)c[l] * K.W[l][t];
+    }
+    uint32_t x[kNL];
+    uint64_t carry = 0;
+#pragma unroll
+    for (int t = 0; t < kNL; ++t) {
+        uint64_t v = S[t] + carry;
+        x[t] = (uint32_t)v;
+        carry = v >> 32;
+    }
+    uint32_t qv = (uint32_t)rintf(qf);
+    uint64_t borrow = 0, mc = 0;
+#pragma unroll
+    for (int t = 0; t < kNL; ++t) {
+        uint64_t prod = (uint64_t)qv * K.M[t] + mc;
+        mc = prod >> 32;
+        uint64_t sub = (uint64_t)(uint32_t)prod + borrow;
+        uint64_t v = (uint64_t)x[t] - sub;
+        x[t] = (uint32_t)v;
+        borrow = (v >> 63) & 1;
+    }
+    const bool neg = (x[kNL - 1] >> 31) != 0;
+    if (neg) {
+        uint64_t cy = 1;
+#pragma unroll
+        for (int t = 0; t < kNL; ++t) {
+            uint64_t v = (uint64_t)(~x[t]) + cy;
+            x[t] = (uint32_t)v;
+            cy = v >> 32;
+        }
+    }
+    int top = -1;
+#pragma unroll
+    for (int t = kNL - 1; t >= 0; --t)
+        if (top < 0 && x[t] != 0) top = t;
+    if (top < 0) return dd::make(0.0, 0.0);
+    const int P = top * 32 + 31 - __clz((int)x[top]);
+    uint64_t a = bits53_at(x, P - 52);
+    uint64_t b = bits53_at(x, P - 105);
+    uint64_t cc = bits53_at(x, P - 158);
+    if (cc >> 52) ++b;
+    int64_t bs = (int64_t)b;
+    if (bs >= (1ll << 52)) {
+        ++a;
+        bs -= (1ll << 53);
+    }
+    double hi = scaled_u54(a, P - 52 - S2);
+    double lo = bs >= 0 ? scaled_u54((uint64_t)bs, P - 105 - S2) : -scaled_u54((uint64_t)(-bs), P - 105 - S2);
+    return neg ? dd::make(-hi, -lo) : dd::make(hi, lo);
+}
+
+// Complex: R holds the residues of P1 = Ar*Br, P2 = Ai*Bi and
+// P3 = (Ar+Ai)*(Br+Bi) as components 0..2; Re = P1 - P2, Im = P3 - P1 - P2.
+__global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, const uint8_t *__restrict__ R,
+                                                          int64_t Mp, int64_t Np, const int *__restrict__ ea,
+                                                          const int *__restrict__ eb, int bits, OzCrtParams K,
+                                                          dd::cplx alpha, int alpha_one, dd::cplx beta,
+                                                          int beta_kind, double2 *C, int64_t ldc, int uplo, int herm,
+                                                          int real_beta)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int64_t cstride = (int64_t)K.nmod * Np * Mp;
+    for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+        if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
+        uint32_t cre[kMaxMod], cim[kMaxMod];
+        for (int l = 0; l < K.nmod; ++l) {
+            const int64_t o = ((int64_t)l * Np + j) * Mp + i;
+            int p = (int)K.pm[l];
+            int p1 = R[o], p2 = R[cstride + o], p3 = R[2 * cstride + o];
+            int re = p1 - p2;
+            if (re < 0) re += p;
+            int im = p3 - p1 - p2;
+            im %= p;
+            if (im < 0) im += p;
+            cre[l] = (uint32_t)re;
+            cim[l] = (uint32_t)im;
+        }
+        dd::cplx v;
+        v.re = dd::make(0.0, 0.0);
+        v.im = v.re;
+        if (ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
+            const int S2 = (bits - 2 - ea[i]) + (bits - 2 - eb[j]);
+            v.re = crt_to_dd(cre, K, S2);
+            v.im = crt_to_dd(cim, K, S2);
+        }
+        double2 *pc = C + 2 * (i + j * ldc);
+        dd::cplx r = alpha_one ? v : dd::cmul_fast(alpha, v);
+        dd::cplx out = r;
+        if (beta_kind != 0) {
+            dd::cplx c0 = dd::cload(pc);
+            if (beta_kind == 2) {
+                if (real_beta) {
+                    c0.re = dd::mul_exact(beta.re, c0.re);
+                    c0.im = dd::mul_exact(beta.re, c0.im);
+                } else {
+                    c0 = dd::cmul_exact(c0, beta);
+                }
+            }
+            out = dd::cadd_exact(c0, r);
+        }
+        if (herm && i == j) out.im = dd::make(0.0, 0.0);
+        dd::cstore(pc, out);
+    }
+}
+
 // Max / non-finite summary of the exponent vectors.
 __global__ void k_oz_exp_summary(const int *e, int64_t n, int *out)
 {
@@ -631,8 +797,12 @@ void fill_res_params(const Moduli &md, OzResParams &rp, OzModParams &mp)
     rp.nmod = md.n;
     for (int l = 0; l < md.n; ++l) {
         int p = md.p[l];
-        rp.p[l] = mp.p[l] = (float)p;
-        rp.invp[l] = mp.invp[l] = 1.0f / (float)p;
+        rp.p[l] = (float)p;
+        rp.invp[l] = 1.0f / (float)p;
+        for (int comp = 0; comp < 3; ++comp) {
+            mp.p[comp * md.n + l] = (float)p;
+            mp.invp[comp * md.n + l] = 1.0f / (float)p;
+        }
         int64_t t = 1;
         for (int q = 0; q < kResLimbs; ++q) {
             rp.t[l][q] = (float)t;
@@ -659,6 +829,7 @@ void fill_crt_params(const Moduli &md, OzCrtParams &cp)
         big_mul_small(Ml, kNL, (uint32_t)u);
         memcpy(cp.W[l], Ml, sizeof(Ml));
         cp.f[l] = (float)((double)u / (double)md.p[l]);
+        cp.pm[l] = (float)md.p[l];
     }
 }
 
@@ -684,21 +855,25 @@ bool ozaki_available()
 
 int ozaki_last_moduli() { return g_last_moduli; }
 
-bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
+namespace {
+
+bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine)
 {
     // Split K so that the residue sums and the CRT bound stay in range.
     const int64_t kmax = 65536;
+    const int E = cplx ? 2 : 1;
     if (g0.k > kmax) {
         GemmArgs g = g0;
         for (int64_t k0 = 0; k0 < g0.k; k0 += kmax) {
             g.k = (g0.k - k0 < kmax) ? g0.k - k0 : kmax;
-            g.A = (const double2 *)g0.A + (g0.ta ? k0 : k0 * g0.lda);
-            g.B = (const double2 *)g0.B + (g0.tb ? k0 * g0.ldb : k0);
+            g.A = (const double2 *)g0.A + E * (g0.ta ? k0 : k0 * g0.lda);
+            g.B = (const double2 *)g0.B + E * (g0.tb ? k0 * g0.ldb : k0);
             if (k0 > 0) {
                 g.beta = dd_host{1.0, 0.0};
+                g.cbeta = cdd_host{{1.0, 0.0}, {0.0, 0.0}};
                 g.beta_kind = 1;
             }
-            if (!gemm_ozaki_real(g, bits_req, routine)) return false;
+            if (!gemm_ozaki(g, cplx, bits_req, routine)) return false;
         }
         return true;
     }
@@ -707,14 +882,18 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
     const int64_t Mp = (m + TC_BM - 1) / TC_BM * TC_BM;
     const int64_t Np = (n + TC_BN - 1) / TC_BN * TC_BN;
     const int64_t Kp = (k + TC_BK - 1) / TC_BK * TC_BK;
+    const int nc = cplx ? 3 : 1;
+    // Real SYRK (op(B) = op(A)^T on the same array): op(B)'s residue rows are
+    // op(A)'s, so one conversion serves both operands.
+    const bool shared_ops = !cplx && g.uplo != 0 && g.A == g.B && g.lda == g.ldb && g.ta != g.tb && m == n;
 
     // 1. exponent bounds of the rows of op(A) / columns of op(B)
     int *ex = (int *)dev_alloc(sizeof(int) * (size_t)(m + n + 2), routine);
     if (!ex) return false;
     int *ea = ex, *eb = ex + m, *summ = ex + m + n;
     phase_mark(PH_EXP);
-    launch_exp_rows_of_op(g.A, g.ta ? k : m, g.ta ? m : k, g.lda, g.ta, 1, ea);
-    launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, 1, eb);
+    launch_exp_rows_of_op(g.A, g.ta ? k : m, g.ta ? m : k, g.lda, g.ta, E, ea);
+    launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, E, eb);
     cudaMemsetAsync(summ, 0x80, 2 * sizeof(int), stream());
     k_oz_exp_summary<<<blocks_cap((m + 255) / 256), 256, 0, stream()>>>(ea, m, summ);
     k_oz_exp_summary<<<blocks_cap((n + 255) / 256), 256, 0, stream()>>>(eb, n, summ + 1);
@@ -729,14 +908,14 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
         // Inf/NaN present: the integer scheme has no representation for them;
         // the FP64 engine propagates them as the reference does.
         dev_free(ex);
-        return gemm_plain_real(g, routine);
+        return cplx ? gemm_plain_cplx(g, routine) : gemm_plain_real(g, routine);
     }
 
-    // 2. precision and moduli
+    // 2. precision and moduli (complex: |Re|, |Im| <= 2k * 2^(2bits-2))
     int bits = bits_req > 0 ? bits_req : 106;
     if (bits < 40) bits = 40;
     if (bits > 120) bits = 120;
-    double need = 2.0 * (bits - 1) + std::log2((double)(k > 1 ? k : 1)) + 1.0 + 4.0;
+    double need = 2.0 * (bits - 1) + std::log2((double)(k > 1 ? k : 1)) + 1.0 + 4.0 + (cplx ? 1.0 : 0.0);
     Moduli md = choose_moduli(need);
     g_last_moduli = md.n;
     OzResParams rp;
@@ -745,55 +924,66 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
     fill_res_params(md, rp, mp);
     fill_crt_params(md, cp);
 
-    // 3. residue operands
-    const size_t a_bytes = (size_t)md.n * Mp * Kp * 2, b_bytes = (size_t)md.n * Np * Kp * 2;
-    const size_t r_bytes = (size_t)md.n * Np * Mp;
+    // 3. residue operands: [comp][modulus][row][k] fp16
+    const size_t a_bytes = (size_t)nc * md.n * Mp * Kp * 2;
+    const size_t b_bytes = shared_ops ? 0 : (size_t)nc * md.n * Np * Kp * 2;
+    const size_t r_bytes = (size_t)nc * md.n * Np * Mp;
     uint8_t *work = (uint8_t *)dev_alloc(a_bytes + b_bytes + r_bytes + 256, routine);
     if (!work) {
         dev_free(ex);
         return false;
     }
     __half *Ares = (__half *)work;
-    __half *Bres = (__half *)(work + a_bytes);
+    __half *Bres = shared_ops ? Ares : (__half *)(work + a_bytes);
     uint8_t *R = work + a_bytes + b_bytes;
     phase_mark(PH_RES);
     {
+        // op(A) = A: A[i + p*lda] is contiguous along rows; op(A) = A^T along k.
+        // op(B)(p, j) = B[p + j*ldb] is contiguous along k; op(B) = B^T along rows j.
         dim3 grid((unsigned)(Kp / 32), (unsigned)(Mp / 32));
-        if (!g.ta)   // op(A) = A: A[i + p*lda], contiguous along rows
-            k_oz_residues<true><<<grid, 256, 0, stream()>>>(m, k, (const double2 *)g.A, g.lda, ea, bits, rp, Ares, Mp,
-                                                            Kp, 0);
-        else
-            k_oz_residues<false><<<grid, 256, 0, stream()>>>(m, k, (const double2 *)g.A, g.lda, ea, bits, rp, Ares, Mp,
-                                                             Kp, 0);
-        dim3 gridb((unsigned)(Kp / 32), (unsigned)(Np / 32));
-        if (!g.tb)   // op(B)(p, j) = B[p + j*ldb]: rows j, contiguous along p
-            k_oz_residues<false><<<gridb, 256, 0, stream()>>>(n, k, (const double2 *)g.B, g.ldb, eb, bits, rp, Bres,
-                                                              Np, Kp, 0);
-        else
-            k_oz_residues<true><<<gridb, 256, 0, stream()>>>(n, k, (const double2 *)g.B, g.ldb, eb, bits, rp, Bres,
-                                                             Np, Kp, 0);
-        count_launch(2);
+        const double2 *Ad = (const double2 *)g.A, *Bd = (const double2 *)g.B;
+        if (cplx) {
+            if (!g.ta) k_oz_residues<true, true><<<grid, 256, 0, stream()>>>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
+            else k_oz_residues<false, true><<<grid, 256, 0, stream()>>>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
+        } else {
+            if (!g.ta) k_oz_residues<true, false><<<grid, 256, 0, stream()>>>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
+            else k_oz_residues<false, false><<<grid, 256, 0, stream()>>>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
+        }
+        count_launch();
+        if (!shared_ops) {
+            dim3 gridb((unsigned)(Kp / 32), (unsigned)(Np / 32));
+            if (cplx) {
+                if (!g.tb) k_oz_residues<false, true><<<gridb, 256, 0, stream()>>>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, g.cb);
+                else k_oz_residues<true, true><<<gridb, 256, 0, stream()>>>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, g.cb);
+            } else {
+                if (!g.tb) k_oz_residues<false, false><<<gridb, 256, 0, stream()>>>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, 0);
+                else k_oz_residues<true, false><<<gridb, 256, 0, stream()>>>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, 0);
+            }
+            count_launch();
+        }
     }
 
-    // 4. residue GEMMs
+    // 4. residue GEMMs, one batch entry per (component, modulus)
     phase_mark(PH_GEMM);
     bool ok = true;
+    const int nz = nc * md.n;
     if (mma_kind() == 0) {
         CUtensorMap ma, mb;
-        ok = make_map(&ma, Ares, (uint64_t)Kp, (uint64_t)(md.n * Mp), TC_BM, routine) &&
-             make_map(&mb, Bres, (uint64_t)Kp, (uint64_t)(md.n * Np), TC_BN, routine);
+        ok = make_map(&ma, Ares, (uint64_t)Kp, (uint64_t)(nz * Mp), TC_BM, routine) &&
+             make_map(&mb, Bres, (uint64_t)Kp, (uint64_t)(nz * Np), TC_BN, routine);
         if (ok) {
             static bool attr_set = false;
             if (!attr_set) {
                 cudaFuncSetAttribute(k_oz_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
                 attr_set = true;
             }
-            dim3 grid((unsigned)(Np / TC_BN), (unsigned)(Mp / TC_BM), (unsigned)md.n);
-            k_oz_gemm_tc<<<grid, 192, TC_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R, device_status_word());
+            dim3 grid((unsigned)(Np / TC_BN), (unsigned)(Mp / TC_BM), (unsigned)nz);
+            k_oz_gemm_tc<<<grid, 192, TC_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R, device_status_word(),
+                                                           g.uplo);
             count_launch();
         }
     } else {
-        dim3 grid((unsigned)(Np / 16), (unsigned)(Mp / 16), (unsigned)md.n);
+        dim3 grid((unsigned)(Np / 16), (unsigned)(Mp / 16), (unsigned)nz);
         k_oz_gemm_simt<<<grid, 256, 0, stream()>>>(Ares, Bres, Mp, Np, Kp, m, n, mp, R);
         count_launch();
     }
@@ -802,11 +992,24 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
     phase_mark(PH_REC);
     if (ok) {
         dim3 grid((unsigned)((m + 255) / 256), blocks_cap(n));
-        bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
-        k_oz_reconstruct<<<grid, 256, 0, stream()>>>(m, n, R, Mp, Np, ea, eb, bits, cp,
-                                                    dd::make(g.alpha.hi, g.alpha.lo), alpha_one ? 1 : 0,
-                                                    dd::make(g.beta.hi, g.beta.lo), g.beta_kind, (double2 *)g.C,
-                                                    g.ldc, g.uplo);
+        if (!cplx) {
+            bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
+            k_oz_reconstruct<<<grid, 256, 0, stream()>>>(m, n, R, Mp, Np, ea, eb, bits, cp,
+                                                        dd::make(g.alpha.hi, g.alpha.lo), alpha_one ? 1 : 0,
+                                                        dd::make(g.beta.hi, g.beta.lo), g.beta_kind, (double2 *)g.C,
+                                                        g.ldc, g.uplo);
+        } else {
+            dd::cplx al, be;
+            al.re = dd::make(g.calpha.re.hi, g.calpha.re.lo);
+            al.im = dd::make(g.calpha.im.hi, g.calpha.im.lo);
+            be.re = dd::make(g.cbeta.re.hi, g.cbeta.re.lo);
+            be.im = dd::make(g.cbeta.im.hi, g.cbeta.im.lo);
+            bool alpha_one = (g.calpha.re.hi == 1.0 && g.calpha.re.lo == 0.0 && g.calpha.im.hi == 0.0 &&
+                              g.calpha.im.lo == 0.0);
+            k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>(m, n, R, Mp, Np, ea, eb, bits, cp, al, alpha_one ? 1 : 0,
+                                                          be, g.beta_kind, (double2 *)g.C, g.ldc, g.uplo,
+                                                          g.herm ? 1 : 0, g.herm ? 1 : 0);
+        }
         count_launch();
     }
     phase_mark(PH_N);
@@ -818,13 +1021,10 @@ bool gemm_ozaki_real(const GemmArgs &g0, int bits_req, const char *routine)
     return st;
 }
 
-bool gemm_ozaki_cplx(const GemmArgs &g, int bits, const char *routine)
-{
-    (void)bits;
-    // Complex products run on the FP64 engine until the complex residue
-    // combination lands.
-    return gemm_plain_cplx(g, routine);
-}
+}  // namespace
+
+bool gemm_ozaki_real(const GemmArgs &g, int bits, const char *routine) { return gemm_ozaki(g, false, bits, routine); }
+bool gemm_ozaki_cplx(const GemmArgs &g, int bits, const char *routine) { return gemm_ozaki(g, true, bits, routine); }
 
 }  // namespace mw
 

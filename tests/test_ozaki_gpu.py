@@ -112,3 +112,118 @@ def test_auto_engine_and_bits_control(gpu, oracle, rng):
     err = orc.normwise_error(got, want, k * orc.dd_absmax(A) * orc.dd_absmax(B))
     assert few < many
     assert err < err60 and err60 < 2.0 ** -50 and err <= 4 * k * orc.EPS_DD
+
+
+class engine:
+    """Forces the GEMM engine for every routine built on it (wgemm_, msyrk_...)."""
+
+    def __init__(self, lib, which):
+        self.lib, self.which = lib, which
+
+    def __enter__(self):
+        self.prev = self.lib.lib.mwblas_set_gemm_engine(self.which)
+
+    def __exit__(self, *a):
+        self.lib.lib.mwblas_set_gemm_engine(self.prev)
+
+
+OZAKI, PLAIN = 2, 1
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "C"), ("C", "T"), ("T", "C")])
+def test_ozaki_complex_matches_oracle(gpu, oracle, rng, ta, tb):
+    for (m, n, k) in [(3, 2, 5), (130, 257, 1100), (64, 33, 40)]:
+        lda = (m if ta == "N" else k) + 1
+        ldb = (k if tb == "N" else n)
+        ldc = m + 2
+        A = mwb.dd_matrix(rng, m if ta == "N" else k, k if ta == "N" else m, lda, cplx_=True)
+        B = mwb.dd_matrix(rng, k if tb == "N" else n, n if tb == "N" else k, ldb, cplx_=True)
+        C0 = mwb.dd_matrix(rng, m, n, ldc, cplx_=True)
+        al, be = mwb.random_cdd(rng, ()), mwb.random_cdd(rng, ())
+        want = oracle.qwgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0.copy(), ldc)
+        got = C0.copy()
+        with engine(gpu, OZAKI):
+            gpu.wgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, got, ldc)
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        opn = 2 * op_norm(al, k, A, B, be, C0[:, :m])
+        err = orc.normwise_error(got[:, :m], want[:, :m], opn)
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (ta, tb, m, n, k, err)
+
+
+def test_ozaki_complex_tc_equals_cuda_core(gpu, rng):
+    m, n, k = 140, 270, 1300
+    A = mwb.dd_matrix(rng, m, k, cplx_=True)
+    B = mwb.dd_matrix(rng, k, n, cplx_=True)
+    outs = []
+    for kind in (0, 1):
+        prev = gpu.lib.mwblas_set_ozaki_mma(kind)
+        try:
+            c = np.zeros((n, m, 2, 2))
+            with engine(gpu, OZAKI):
+                gpu.wgemm("N", "C", m, n, k, 1.0, A, m, B, n, 0.0, c, m)
+            outs.append(c)
+        finally:
+            gpu.lib.mwblas_set_ozaki_mma(prev)
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+@pytest.mark.parametrize("trans", ["N", "T"])
+def test_ozaki_syrk(gpu, oracle, rng, uplo, trans):
+    n, k = 300, 700
+    lda = (n if trans == "N" else k)
+    A = mwb.dd_matrix(rng, n if trans == "N" else k, k if trans == "N" else n, lda)
+    C0 = mwb.dd_matrix(rng, n, n)
+    off = np.triu_indices(n, 1) if uplo == "L" else np.tril_indices(n, -1)
+    C0[off[1], off[0]] = -7.37e18
+    al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+    want = C0.copy(); oracle.qsyrk(uplo, trans, n, k, al, A, lda, be, want, n)
+    got = C0.copy()
+    with engine(gpu, OZAKI):
+        gpu.msyrk(uplo, trans, n, k, al, A, lda, be, got, n)
+    assert gpu.last_error()[0] == 0
+    assert np.all(got[off[1], off[0]] == -7.37e18)
+    tri = np.tril_indices(n) if uplo == "L" else np.triu_indices(n)
+    err = orc.normwise_error(got[tri[1], tri[0]], want[tri[1], tri[0]], op_norm(al, k, A, A, be, C0[tri[1], tri[0]]))
+    assert err <= 4 * k * orc.EPS_DD, err
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+@pytest.mark.parametrize("trans", ["N", "C"])
+def test_ozaki_herk(gpu, oracle, rng, uplo, trans):
+    n, k = 200, 300
+    lda = (n if trans == "N" else k)
+    A = mwb.dd_matrix(rng, n if trans == "N" else k, k if trans == "N" else n, lda, cplx_=True)
+    C0 = mwb.dd_matrix(rng, n, n, cplx_=True)
+    al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+    want = C0.copy(); oracle.qherk(uplo, trans, n, k, al, A, lda, be, want, n)
+    got = C0.copy()
+    with engine(gpu, OZAKI):
+        gpu.wherk(uplo, trans, n, k, al, A, lda, be, got, n)
+    assert gpu.last_error()[0] == 0
+    d = np.arange(n)
+    assert np.all(got[d, d, 1] == 0.0)
+    tri = np.tril_indices(n) if uplo == "L" else np.triu_indices(n)
+    err = orc.normwise_error(got[tri[1], tri[0]], want[tri[1], tri[0]],
+                             2 * op_norm(al, k, A, A, be, C0[tri[1], tri[0]]))
+    assert err <= 4 * k * orc.EPS_DD, err
+
+
+def test_ozaki_trsm_trailing_updates(gpu, oracle, rng):
+    """Blocked TRSM whose trailing GEMMs run on the Ozaki engine."""
+    m, n = 400, 96
+    A = mwb.dd_matrix(rng, m, m)
+    A[..., 0] /= m
+    A[..., 1] /= m
+    for d in range(m):
+        A[d, d] = (1.0 + rng.random(), 0.0)
+    B0 = mwb.dd_matrix(rng, m, n)
+    al = mwb.random_dd(rng, ())
+    for uplo in ("L", "U"):
+        want = B0.copy(); oracle.qtrsm("L", uplo, "N", "N", m, n, al, A, m, want, m)
+        got = B0.copy()
+        with engine(gpu, OZAKI):
+            gpu.mtrsm("L", uplo, "N", "N", m, n, al, A, m, got, m)
+        assert gpu.last_error()[0] == 0
+        err = orc.normwise_error(got, want, orc.dd_abs(al) * orc.dd_absmax(B0))
+        assert err <= max(20, 8 * m * m) * orc.EPS_DD
