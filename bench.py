@@ -396,7 +396,7 @@ def main():
 
 
 def tc_traffic_from_profile():
-    p = os.path.join(ROOT, "profiles", "k_oz_gemm_tc_ncu.txt")
+    p = os.path.join(ROOT, "profiles", "k_oz_gemm_tc_4096_ncu.txt")
     if not os.path.exists(p):
         return None
     for line in open(p):
