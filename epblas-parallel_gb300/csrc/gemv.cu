@@ -10,6 +10,8 @@
 // shared-memory reduction, then y_j += alpha*s (mgemv.cpp:229-233).
 // Products accumulate as TwoProduct + TwoSum into a (sum, error) pair,
 // renormalised every 32 terms, the lo*lo product dropped as in mdot.cpp:60-64.
+#include <mutex>
+
 #include "dd.cuh"
 #include "level3.h"
 #include "runtime.h"
@@ -152,3 +154,111 @@ bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A,
 }
 
 }  // namespace mw
+
+// ---- GEMV without device allocation ----------------------------------------------------
+//
+// For callers that must not allocate device memory on the call path: code whose
+// device memory is owned by its own allocator under a fixed budget (cudaMalloc
+// there would bypass the budget), and code that cannot afford the driver
+// allocator's locking or cudaFree's device-wide synchronisation while other
+// work is in flight. mgemv_ itself allocates the per-chunk partial sums of
+// the no-transpose kernel (and staging copies of host arrays); this variant
+// keeps the partial sums in a file-scope device array instead.
+//
+// The array below is the only scratch. It is 1 MiB (65536 double-double
+// partial sums), every GPU that loads the library holds it until the process
+// exits, and all calls share it: two calls whose kernels overlap on the GPU
+// (different streams, or different host threads) race on it. Nothing in it
+// needs to start at zero: every entry a call reads was written earlier by the
+// same call. The host learns its device address once per device, with that
+// device current, on the first call made on that device; that first call
+// should therefore come before any stream capture.
+
+namespace mw {
+namespace {
+
+constexpr int64_t kNoAllocScratch = 65536;   // double2 entries (1 MiB)
+static __device__ __align__(256) double2 g_gemv_noalloc_scratch[kNoAllocScratch];
+
+std::mutex g_noalloc_mu;
+double2 *g_noalloc_addr[64] = {};
+
+}  // namespace
+}  // namespace mw
+
+extern "C" int mgemv_n_noalloc(int64_t m, int64_t n, const mwblas_real64x2 *alpha, const mwblas_real64x2 *a,
+                               int64_t lda, const mwblas_real64x2 *x, int64_t incx, const mwblas_real64x2 *beta,
+                               mwblas_real64x2 *y, int64_t incy, void *cuda_stream)
+{
+    using namespace mw;
+    const char *routine = "mgemv_n_noalloc";
+    clear_error();
+    if (!alpha || !beta) { set_error(routine, 3, "null alpha or beta"); return 3; }
+    if (m < 0) { set_error(routine, 1, "m < 0"); return 1; }
+    if (n < 0) { set_error(routine, 2, "n < 0"); return 2; }
+    if (lda < (m > 1 ? m : 1)) { set_error(routine, 5, "lda too small"); return 5; }
+    if (incx == 0) { set_error(routine, 7, "incx == 0"); return 7; }
+    if (incy == 0) { set_error(routine, 10, "incy == 0"); return 10; }
+    if (m > kNoAllocScratch) {
+        set_error(routine, 1, "m exceeds the 65536-row limit of the fixed 1 MiB scratch array");
+        return 1;
+    }
+    if (m == 0 || n == 0) return 0;
+    const dd_host al{alpha->limbs[0], alpha->limbs[1]}, be{beta->limbs[0], beta->limbs[1]};
+    const bool alpha0 = (al.hi == 0.0 && al.lo == 0.0);
+    const int bk = (be.hi == 0.0 && be.lo == 0.0) ? 0 : ((be.hi == 1.0 && be.lo == 0.0) ? 1 : 2);
+    if (alpha0 && bk == 1) return 0;
+    if (!y || !is_device_pointer(y) || (!alpha0 && (!a || !x || !is_device_pointer(a) || !is_device_pointer(x)))) {
+        set_error(routine, 9, "A, x and y must be device or managed memory (this entry point stages nothing)");
+        return 9;
+    }
+    int dev = 0;
+    if (!cuda_ok(cudaGetDevice(&dev), routine, "cudaGetDevice")) return MWBLAS_ERR_CUDA;
+    if (dev < 0 || dev >= 64) { set_error(routine, MWBLAS_ERR_DEVICE, "device ordinal out of range"); return MWBLAS_ERR_DEVICE; }
+    double2 *scratch;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            cudaError_t st = cudaGetSymbolAddress(&p, g_gemv_noalloc_scratch);
+            if (st != cudaSuccess) {
+                cuda_ok(st, routine, "cudaGetSymbolAddress(scratch)");
+                return MWBLAS_ERR_CUDA;
+            }
+            g_noalloc_addr[dev] = (double2 *)p;
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 148;
+    cudaStream_t s = cuda_stream ? (cudaStream_t)cuda_stream : stream();
+    if (bk != 1) {
+        int64_t blocks = (m + 255) / 256;
+        if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
+        k_scale_vec<<<(unsigned)blocks, 256, 0, s>>>(m, dd::make(be.hi, be.lo), bk, (double2 *)y, incy);
+        count_launch();
+    }
+    if (!alpha0) {
+        int64_t rowblocks = (m + 255) / 256;
+        int64_t nchunks = (4 * (int64_t)sms + rowblocks - 1) / rowblocks;
+        if (nchunks > kNoAllocScratch / m) nchunks = kNoAllocScratch / m;
+        if (nchunks > n) nchunks = n;
+        if (nchunks < 1) nchunks = 1;
+        int64_t chunk = (n + nchunks - 1) / nchunks;
+        nchunks = (n + chunk - 1) / chunk;
+        dim3 grid((unsigned)rowblocks, (unsigned)nchunks);
+        k_gemv_n_partial<<<grid, 256, 0, s>>>(m, n, (const double2 *)a, lda, (const double2 *)x, incx, chunk, scratch);
+        int64_t fb = (m + 255) / 256;
+        if (fb > (int64_t)sms * 8) fb = (int64_t)sms * 8;
+        k_gemv_n_final<<<(unsigned)fb, 256, 0, s>>>(m, (int)nchunks, scratch, dd::make(al.hi, al.lo), (double2 *)y,
+                                                     incy);
+        count_launch(2);
+    }
+    cudaError_t st = cudaGetLastError();
+    if (st != cudaSuccess) {
+        cuda_ok(st, routine, "kernel launch");
+        return MWBLAS_ERR_CUDA;
+    }
+    return 0;
+}

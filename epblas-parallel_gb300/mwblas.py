@@ -125,6 +125,7 @@ class MWBlas:
             self._sig("mwblas_debug_fail_alloc_after", None, [_i64])
             self._sig("mwblas_launch_count", _i64, [])
             self._sig("mwblas_version", _ch, [])
+            self._sig("mgemv_n_noalloc", _i32, [_i64, _i64, R, _p, _i64, _p, _i64, R, _p, _i64, _p])
             if hasattr(L, "mgemm_grouped"):
                 self._sig("mgemm_grouped", _i32,
                           [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p])
@@ -190,6 +191,11 @@ class MWBlas:
         f = self.lib.mgemv_64_ if wide else self.lib.mgemv_
         f(trans.encode(), I(m), I(n), C.byref(real(alpha)), _ptr(a), I(lda), _ptr(x), I(incx), C.byref(real(beta)),
           _ptr(y), I(incy))
+
+    def mgemv_n_noalloc(self, m, n, alpha, a, lda, x, incx, beta, y, incy, stream=None):
+        """y := alpha*A*x + beta*y on device arrays without any device allocation."""
+        return int(self.lib.mgemv_n_noalloc(m, n, C.byref(real(alpha)), _ptr(a), lda, _ptr(x), incx,
+                                            C.byref(real(beta)), _ptr(y), incy, stream))
 
     # ---- level 1 -----------------------------------------------------------------------
     def mdot(self, n, x, incx, y, incy, wide=True):

@@ -258,6 +258,23 @@ void mwblas_debug_fail_alloc_after(int64_t count);
 /* Number of kernels this library has launched in the process. */
 int64_t mwblas_launch_count(void);
 
+/* y := alpha*A*x + beta*y (no transpose) without allocating any device memory,
+ * for callers that must not allocate on the call path (a framework whose own
+ * allocator owns the device memory under a fixed budget, or code that cannot
+ * afford the driver allocator's locks or cudaFree's device-wide sync). No
+ * counterpart in the reference. A, x and y must already be device or managed
+ * memory; nothing is staged. The kernel's partial sums live in a fixed 1 MiB
+ * device array (65536 double-double values) that the library holds on every
+ * GPU until exit, so m may not exceed 65536 (larger m is rejected with info 1).
+ * All calls share that array: calls whose kernels overlap on the GPU race. The
+ * first call on a device looks up the array's device address (do it before
+ * any stream capture). Work is enqueued on `cuda_stream` (NULL: the library's
+ * stream) and the call returns without synchronising. Returns 0, a positive
+ * argument position, or a negative MWBLAS_ERR_* code. */
+int mgemv_n_noalloc(int64_t m, int64_t n, const mwblas_real64x2 *alpha, const mwblas_real64x2 *a, int64_t lda,
+                    const mwblas_real64x2 *x, int64_t incx, const mwblas_real64x2 *beta, mwblas_real64x2 *y,
+                    int64_t incy, void *cuda_stream);
+
 /* Library version string. */
 const char *mwblas_version(void);
 
