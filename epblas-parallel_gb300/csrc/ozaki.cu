@@ -10,15 +10,15 @@
 //     the binary exponents of the row / column). The error of this step is
 //     <= 2^(3-bits) of max|row| * max|column| per product, i.e. normwise.
 //  2. Residues. A'B' is an integer matrix with |entries| <= k * 2^(2 bits - 2).
-//     It is computed exactly modulo L pairwise-coprime moduli p_l <= 255 whose
+//     It is computed exactly modulo L pairwise-coprime moduli p_l <= 361 whose
 //     product M exceeds 2^4 * k * 2^(2 bits - 1). Each residue matrix (entries
-//     in [-(p-1)/2, (p-1)/2]) is exact in fp16.
+//     in [-(p-1)/2, (p-1)/2], |r| <= 180) is exact in fp16.
 //  3. Residue GEMMs on the tensor cores. sm_103a's tcgen05 has no integer
 //     kind (kind::i8 is rejected by ptxas for sm_103a), so the residue GEMMs
 //     use kind::f16 with fp32 accumulation in tensor memory. Products of
 //     residues are exact; an fp32 sum stays exact while it is an integer
-//     below 2^24. K is therefore processed in chunks of 1024
-//     (1024 * 127^2 + 255 < 2^24) and after each chunk the accumulator is
+//     below 2^24. K is therefore processed in chunks of 512
+//     (512 * 180^2 + 361 < 2^24) and after each chunk the accumulator is
 //     reduced modulo p in place; two accumulators alternate so the MMA pipe
 //     keeps running while the epilogue reduces the other one.
 //  4. CRT reconstruction (integer only): X = sum_l c_l * W_l - q * M with
@@ -29,13 +29,14 @@
 //     runs in double-double on the FP64 pipe, which the scheme otherwise
 //     does not touch.
 //
-// A modulus count L of ~29 (8192^3, bits = 106) replaces the 18 FP64
-// instructions per multiply-add of the reference's kernel by 29 fp16
+// A modulus count L of ~27 (8192^3, bits = 106) replaces the 18 FP64
+// instructions per multiply-add of the reference's kernel by 27 fp16
 // tensor-core multiply-adds.
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -45,6 +46,7 @@
 #include "level3.h"
 #include "runtime.h"
 #include "sm100.cuh"
+#include "xfloat.cuh"
 
 namespace mw {
 
@@ -54,7 +56,8 @@ constexpr int kMaxMod = 40;
 constexpr int kNL = 9;          // 32-bit limbs of CRT integers
 constexpr int kResLimbs = 11;   // 11-bit limbs of |A'| (bits <= 120)
 constexpr int kNoExp = -30000;
-constexpr int kChunk = 1024;    // K elements per exact fp32 accumulation chunk
+constexpr int kMaxP = 361;      // largest modulus: residues |r| <= 180 are exact in fp16
+constexpr int kChunk = 512;     // K per exact fp32 chunk: 512 * 180^2 + 361 < 2^24
 
 // ---- host-side moduli / CRT constants --------------------------------------------------
 
@@ -114,13 +117,13 @@ int64_t inv_mod(int64_t a, int64_t m)
 }
 int gcd(int a, int b) { return b ? gcd(b, a % b) : a; }
 
-// The largest pairwise-coprime moduli <= 255 (greedy from the top), enough of
-// them for `need_bits` bits of product.
+// The largest pairwise-coprime moduli <= kMaxP (greedy from the top), enough
+// of them for `need_bits` bits of product.
 Moduli choose_moduli(double need_bits)
 {
     Moduli md;
     double have = 0.0;
-    for (int c = 255; c >= 3 && have < need_bits && md.n < kMaxMod; --c) {
+    for (int c = kMaxP; c >= 3 && have < need_bits && md.n < kMaxMod; --c) {
         bool ok = true;
         for (int i = 0; i < md.n && ok; ++i) ok = gcd(md.p[i], c) == 1;
         if (!ok) continue;
@@ -212,19 +215,45 @@ __device__ __forceinline__ void to_limbs(double2 v, int sc, float (&fl)[kResLimb
     for (int q = 0; q < kResLimbs; ++q) fl[q] = u11_to_float((uint32_t)(U >> (11 * q)) & 0x7FFu);
 }
 
-// Symmetric residue of +-|F| (limbs) modulo P.p[l], exact in fp32.
-__device__ __forceinline__ float sym_residue(const float (&fl)[kResLimbs], bool neg, const OzResParams &P, int l)
+// Symmetric residue of +-|F| (11-bit limbs) modulo p, exact in fp32: the
+// limb dot product stays below 11 * 2047 * 361 < 2^24.
+__device__ __forceinline__ float sym_residue4(const float (&fl)[kResLimbs], bool neg, float4 t0, float4 t1, float4 t2,
+                                              float p, float invp)
 {
-    float x = 0.0f;
-#pragma unroll
-    for (int q = 0; q < kResLimbs; ++q) x = __fmaf_rn(fl[q], P.t[l][q], x);
-    float p = P.p[l];
-    float qq = rintf(__fmul_rn(x, P.invp[l]));
-    float rr = __fmaf_rn(-qq, p, x);
+    float x = __fmul_rn(fl[0], t0.x);
+    x = __fmaf_rn(fl[1], t0.y, x);
+    x = __fmaf_rn(fl[2], t0.z, x);
+    x = __fmaf_rn(fl[3], t0.w, x);
+    x = __fmaf_rn(fl[4], t1.x, x);
+    x = __fmaf_rn(fl[5], t1.y, x);
+    x = __fmaf_rn(fl[6], t1.z, x);
+    x = __fmaf_rn(fl[7], t1.w, x);
+    x = __fmaf_rn(fl[8], t2.x, x);
+    x = __fmaf_rn(fl[9], t2.y, x);
+    x = __fmaf_rn(fl[10], t2.z, x);
+    float qq = rintf(__fmul_rn(x, invp));
+    float rr = __fmaf_rn(-qq, p, x);   // in (-p, p)
     float half = 0.5f * p;
-    if (rr > half) rr = __fsub_rn(rr, p);
-    else if (rr < -half) rr = __fadd_rn(rr, p);
+    rr = (rr > half) ? __fsub_rn(rr, p) : rr;
+    rr = (rr < -half) ? __fadd_rn(rr, p) : rr;
     return neg ? -rr : rr;
+}
+
+__device__ __forceinline__ float sym_wrap(float v, float p)
+{
+    float half = 0.5f * p;
+    v = (v > half) ? __fsub_rn(v, p) : v;
+    return (v < -half) ? __fadd_rn(v, p) : v;
+}
+
+__device__ __forceinline__ void store4h(__half *dst, const float (&v)[4])
+{
+    __half2 a = __floats2half2_rn(v[0], v[1]);
+    __half2 b = __floats2half2_rn(v[2], v[3]);
+    uint2 u;
+    u.x = *reinterpret_cast<uint32_t *>(&a);
+    u.y = *reinterpret_cast<uint32_t *>(&b);
+    *reinterpret_cast<uint2 *>(dst) = u;
 }
 
 // op(X) is rows x kdim; element (r, c) lives at X[r + c*ld] (ROWC) or
@@ -233,7 +262,9 @@ __device__ __forceinline__ float sym_residue(const float (&fl)[kResLimbs], bool 
 // nmod*rows_pad*kpad), over the padded ranges r < rows_pad, c < kpad (zeros
 // outside op(X)). Real: one component. Complex: the real part, the imaginary
 // part (negated when `conj`) and their sum, for the 3-product (Karatsuba)
-// complex multiply.
+// complex multiply. A block converts a 32 x 32 tile; each thread converts four
+// consecutive elements of one row, so every modulus constant read from shared
+// memory serves four elements and the four residues leave as one 8-byte store.
 template <bool ROWC, bool CPLX>
 __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim, const double2 *__restrict__ X,
                                                      int64_t ld, const int *__restrict__ rexp, int bits,
@@ -242,57 +273,86 @@ __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim,
 {
     constexpr int E = CPLX ? 2 : 1;
     __shared__ double2 tile[32][33][E];
+    __shared__ __align__(16) float s_t[kMaxMod][12];
+    __shared__ float s_p[kMaxMod], s_ip[kMaxMod];
+    const int nmod = P.nmod;
+    for (int i = threadIdx.x; i < nmod * 12; i += blockDim.x) {
+        int l = i / 12, q = i % 12;
+        s_t[l][q] = (q < kResLimbs) ? P.t[l][q] : 0.0f;
+    }
+    for (int i = threadIdx.x; i < nmod; i += blockDim.x) {
+        s_p[i] = P.p[i];
+        s_ip[i] = P.invp[i];
+    }
     const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int s = ty; s < 32; s += 8) {
-        int64_t r = ROWC ? r0 + tx : r0 + s;
-        int64_t c = ROWC ? c0 + s : c0 + tx;
-        double2 v[E];
+    {
+        const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+        for (int s = ty; s < 32; s += 8) {
+            int64_t r = ROWC ? r0 + tx : r0 + s;
+            int64_t c = ROWC ? c0 + s : c0 + tx;
+            double2 v[E];
 #pragma unroll
-        for (int w = 0; w < E; ++w) v[w] = make_double2(0.0, 0.0);
-        if (r < rows && c < kdim) {
-            const double2 *src = X + E * (ROWC ? r + c * ld : c + r * ld);
+            for (int w = 0; w < E; ++w) v[w] = make_double2(0.0, 0.0);
+            if (r < rows && c < kdim) {
+                const double2 *src = X + E * (ROWC ? r + c * ld : c + r * ld);
 #pragma unroll
-            for (int w = 0; w < E; ++w) v[w] = src[w];
-        }
+                for (int w = 0; w < E; ++w) v[w] = src[w];
+            }
 #pragma unroll
-        for (int w = 0; w < E; ++w) {
-            if (ROWC) tile[tx][s][w] = v[w];
-            else tile[s][tx][w] = v[w];
+            for (int w = 0; w < E; ++w) {
+                if (ROWC) tile[tx][s][w] = v[w];
+                else tile[s][tx][w] = v[w];
+            }
         }
     }
     __syncthreads();
-    const int64_t cstride = (int64_t)P.nmod * rows_pad * kpad;
-    for (int s = ty; s < 32; s += 8) {
-        int64_t r = r0 + s, c = c0 + tx;
-        if (r >= rows_pad || c >= kpad) continue;
-        int e = (r < rows) ? rexp[r] : kNoExp;
-        const bool live = e > kNoExp / 2;
-        const int sc = bits - 2 - e;
-        float fr[kResLimbs], fi[kResLimbs];
-        bool nr = false, ni = false;
+    const int s = threadIdx.x >> 3, cg = (threadIdx.x & 7) * 4;
+    const int64_t r = r0 + s, cb = c0 + cg;
+    if (r >= rows_pad || cb >= kpad) return;
+    const int e = (r < rows) ? rexp[r] : kNoExp;
+    const bool live = e > kNoExp / 2;
+    const int sc = bits - 2 - e;
+    float fr[4][kResLimbs], fi[CPLX ? 4 : 1][kResLimbs];
+    bool nr[4], ni[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        nr[v] = ni[v] = false;
         if (live) {
-            to_limbs(tile[s][tx][0], sc, fr, nr);
-            if (CPLX) to_limbs(tile[s][tx][E - 1], sc, fi, ni);
+            to_limbs(tile[s][cg + v][0], sc, fr[v], nr[v]);
+            if (CPLX) {
+                to_limbs(tile[s][cg + v][E - 1], sc, fi[CPLX ? v : 0], ni[v]);
+                if (conj) ni[v] = !ni[v];
+            }
         } else {
 #pragma unroll
-            for (int q = 0; q < kResLimbs; ++q) fr[q] = fi[q] = 0.0f;
-        }
-        if (CPLX && conj) ni = !ni;
-        for (int l = 0; l < P.nmod; ++l) {
-            const int64_t o = ((int64_t)l * rows_pad + r) * kpad + c;
-            float rr = sym_residue(fr, nr, P, l);
-            out[o] = __float2half_rn(rr);
-            if (CPLX) {
-                float ii = sym_residue(fi, ni, P, l);
-                float ss = __fadd_rn(rr, ii);
-                float p = P.p[l], half = 0.5f * p;
-                if (ss > half) ss = __fsub_rn(ss, p);
-                else if (ss < -half) ss = __fadd_rn(ss, p);
-                out[cstride + o] = __float2half_rn(ii);
-                out[2 * cstride + o] = __float2half_rn(ss);
+            for (int q = 0; q < kResLimbs; ++q) {
+                fr[v][q] = 0.0f;
+                if (CPLX) fi[CPLX ? v : 0][q] = 0.0f;
             }
         }
+    }
+    const int64_t cstride = (int64_t)nmod * rows_pad * kpad;
+    __half *o = out + (r * kpad + cb);
+    for (int l = 0; l < nmod; ++l) {
+        const float4 t0 = *reinterpret_cast<const float4 *>(&s_t[l][0]);
+        const float4 t1 = *reinterpret_cast<const float4 *>(&s_t[l][4]);
+        const float4 t2 = *reinterpret_cast<const float4 *>(&s_t[l][8]);
+        const float p = s_p[l], ip = s_ip[l];
+        float rr[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) rr[v] = sym_residue4(fr[v], nr[v], t0, t1, t2, p, ip);
+        store4h(o, rr);
+        if (CPLX) {
+            float ii[4], ss[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                ii[v] = sym_residue4(fi[CPLX ? v : 0], ni[v], t0, t1, t2, p, ip);
+                ss[v] = sym_wrap(__fadd_rn(rr[v], ii[v]), p);
+            }
+            store4h(o + cstride, ii);
+            store4h(o + 2 * cstride, ss);
+        }
+        o += rows_pad * kpad;
     }
 }
 
@@ -314,7 +374,7 @@ __device__ __forceinline__ float mod_sym(float x, float p, float invp)
 // epilogue (TMEM lane quadrant = warp % 4).
 __global__ void __launch_bounds__(192, 1)
     k_oz_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t Mp,
-                 int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint8_t *__restrict__ R, int *status,
+                 int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint16_t *__restrict__ R, int *status,
                  int uplo)
 {
     // Triangular output (SYRK/HERK): tiles wholly outside the triangle do no work.
@@ -456,7 +516,7 @@ __global__ void __launch_bounds__(192, 1)
                     if (rr < 0.0f) rr = __fadd_rn(rr, p);
                     if (rr >= p) rr = __fsub_rn(rr, p);
                     const int64_t j = (int64_t)tile_n * TC_BN + sl * 32 + t;
-                    if (i < M && j < N) R[((int64_t)l * Np + j) * Mp + i] = (uint8_t)(int)rr;
+                    if (i < M && j < N) R[((int64_t)l * Np + j) * Mp + i] = (uint16_t)(int)rr;
                 }
             }
         }
@@ -475,7 +535,7 @@ __global__ void __launch_bounds__(192, 1)
 
 __global__ void __launch_bounds__(256) k_oz_gemm_simt(const __half *__restrict__ A, const __half *__restrict__ B,
                                                       int64_t Mp, int64_t Np, int64_t Kp, int64_t M, int64_t N,
-                                                      OzModParams P, uint8_t *__restrict__ R)
+                                                      OzModParams P, uint16_t *__restrict__ R)
 {
     __shared__ float sa[16][65], sb[16][65];
     const int l = blockIdx.z;
@@ -483,7 +543,7 @@ __global__ void __launch_bounds__(256) k_oz_gemm_simt(const __half *__restrict__
     const int64_t i = (int64_t)blockIdx.y * 16 + ty, j = (int64_t)blockIdx.x * 16 + tx;
     const __half *Al = A + (int64_t)l * Mp * Kp;
     const __half *Bl = B + (int64_t)l * Np * Kp;
-    int acc = 0;   // |sum| <= Kp * 127^2 < 2^31 for Kp < 133000
+    long long acc = 0;   // |sum| <= Kp * 180^2
     for (int64_t k0 = 0; k0 < Kp; k0 += 64) {
         for (int t = threadIdx.x; t < 16 * 64; t += 256) {
             int rr = t / 64, cc = t % 64;
@@ -492,14 +552,14 @@ __global__ void __launch_bounds__(256) k_oz_gemm_simt(const __half *__restrict__
             sb[rr][cc] = __half2float(Bl[gj * Kp + k0 + cc]);
         }
         __syncthreads();
-        for (int cc = 0; cc < 64; ++cc) acc += (int)sa[ty][cc] * (int)sb[tx][cc];
+        for (int cc = 0; cc < 64; ++cc) acc += (long long)((int)sa[ty][cc] * (int)sb[tx][cc]);
         __syncthreads();
     }
     if (i < M && j < N) {
         int p = (int)P.p[l];
-        int r = acc % p;
+        int r = (int)(acc % p);
         if (r < 0) r += p;
-        R[((int64_t)l * Np + j) * Mp + i] = (uint8_t)r;
+        R[((int64_t)l * Np + j) * Mp + i] = (uint16_t)r;
     }
 }
 
@@ -507,65 +567,55 @@ __global__ void __launch_bounds__(256) k_oz_gemm_simt(const __half *__restrict__
 
 __device__ __forceinline__ uint32_t limb_at(const uint32_t *x, int idx) { return (idx >= 0 && idx < kNL) ? x[idx] : 0u; }
 
-// floor(X / 2^pos) mod 2^53 (pos may be negative: X * 2^-pos).
-__device__ __forceinline__ uint64_t bits53_at(const uint32_t *x, int pos)
+using xfp::XF;
+using xfp::xf_add;
+using xfp::xf_from_dd;
+using xfp::xf_mul;
+
+__device__ __forceinline__ dd::real xf_dd(const XF &x)
 {
-    int w = pos >> 5;           // floor division
-    int sh = pos & 31;
-    uint64_t lo = (uint64_t)limb_at(x, w) | ((uint64_t)limb_at(x, w + 1) << 32);
-    uint64_t hi = limb_at(x, w + 2);
-    uint64_t v = sh ? ((lo >> sh) | (hi << (64 - sh))) : lo;
-    return v & ((1ull << 53) - 1);
+    dd::real r;
+    xfp::xf_to_dd(x, r.hi, r.lo);
+    return r;
 }
 
-// v * 2^e for an integer 0 <= v < 2^54, as an exact (or correctly rounded on
-// underflow) double.
-__device__ __forceinline__ double scaled_u54(uint64_t v, int e)
+// Shared-memory copy of the CRT constants (broadcast reads).
+struct CrtSmem {
+    uint32_t W[kMaxMod][kNL];
+    float f[kMaxMod];
+    uint32_t pm[kMaxMod];
+    uint32_t M[kNL];
+};
+
+__device__ __forceinline__ void crt_smem_fill(CrtSmem &sm, const OzCrtParams &K)
 {
-    if (v == 0) return 0.0;
-    int lz = __clzll((long long)v) - 11;   // leading zeros within 53 bits (may be -1 for 2^53)
-    int64_t mant;
-    int ex;
-    if (lz >= 0) {
-        mant = (int64_t)(v << lz);
-        ex = e - lz + 52;
-    } else {   // v == 2^53 exactly (after rounding)
-        mant = (int64_t)(v >> 1);
-        ex = e + 53;
+    for (int i = threadIdx.x; i < K.nmod * kNL; i += blockDim.x) sm.W[i / kNL][i % kNL] = K.W[i / kNL][i % kNL];
+    for (int i = threadIdx.x; i < K.nmod; i += blockDim.x) {
+        sm.f[i] = K.f[i];
+        sm.pm[i] = (uint32_t)K.pm[i];
     }
-    if (ex >= -1022 && ex <= 1023) {
-        uint64_t b = ((uint64_t)(ex + 1023) << 52) | ((uint64_t)mant & ((1ull << 52) - 1));
-        return __longlong_as_double((long long)b);
-    }
-    // outside the normal range: let the FP unit round (rare)
-    double d = (double)mant;
-    int e2 = ex - 52;
-    while (e2 > 1000) { d *= 0x1p1000; e2 -= 1000; }
-    while (e2 < -1000) { d *= 0x1p-1000; e2 += 1000; }
-    uint64_t pb = (uint64_t)(e2 + 1023) << 52;
-    return d * __longlong_as_double((long long)pb);
+    for (int i = threadIdx.x; i < kNL; i += blockDim.x) sm.M[i] = K.M[i];
 }
 
-__global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, const uint8_t *__restrict__ R,
-                                                        int64_t Mp, int64_t Np, const int *__restrict__ ea,
-                                                        const int *__restrict__ eb, int bits, OzCrtParams K,
-                                                        dd::real alpha, int alpha_one, dd::real beta, int beta_kind,
-                                                        double2 *C, int64_t ldc, int uplo)
-{
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
-        if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
-        uint64_t S[kNL];
+// CRT accumulator: X = sum_l c_l W_l - q M, q = round(sum_l c_l u_l / p_l).
+struct CrtAcc {
+    uint64_t S[kNL];
+    float qf;
+    __device__ __forceinline__ void reset()
+    {
 #pragma unroll
         for (int t = 0; t < kNL; ++t) S[t] = 0;
-        float qf = 0.0f;
-        for (int l = 0; l < K.nmod; ++l) {
-            uint32_t c = R[((int64_t)l * Np + j) * Mp + i];
-            qf = __fmaf_rn((float)c, K.f[l], qf);
+        qf = 0.0f;
+    }
+    __device__ __forceinline__ void add(const CrtSmem &K, int l, uint32_t cl)
+    {
+        qf = __fmaf_rn((float)cl, K.f[l], qf);
 #pragma unroll
-            for (int t = 0; t < kNL; ++t) S[t] += (uint64_t)c * K.W[l][t];
-        }
+        for (int t = 0; t < kNL; ++t) S[t] += (uint64_t)cl * K.W[l][t];
+    }
+    // Top 128 bits of X, as an extended float scaled by 2^-S2.
+    __device__ __forceinline__ XF finish(const CrtSmem &K, int S2) const
+    {
         uint32_t x[kNL];
         uint64_t carry = 0;
 #pragma unroll
@@ -574,7 +624,6 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, co
             x[t] = (uint32_t)v;
             carry = v >> 32;
         }
-        // X = S - q*M (two's complement over kNL limbs)
         uint32_t qv = (uint32_t)rintf(qf);
         uint64_t borrow = 0, mc = 0;
 #pragma unroll
@@ -584,7 +633,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, co
             uint64_t sub = (uint64_t)(uint32_t)prod + borrow;
             uint64_t v = (uint64_t)x[t] - sub;
             x[t] = (uint32_t)v;
-            borrow = (v >> 63) & 1;   // underflow
+            borrow = (v >> 63) & 1;
         }
         const bool neg = (x[kNL - 1] >> 31) != 0;
         if (neg) {
@@ -600,149 +649,162 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, co
 #pragma unroll
         for (int t = kNL - 1; t >= 0; --t)
             if (top < 0 && x[t] != 0) top = t;
-        dd::real v = dd::make(0.0, 0.0);
-        if (top >= 0 && ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
-            const int P = top * 32 + 31 - __clz((int)x[top]);
-            const int S2 = (bits - 2 - ea[i]) + (bits - 2 - eb[j]);
-            uint64_t a = bits53_at(x, P - 52);
-            uint64_t b = bits53_at(x, P - 105);
-            uint64_t c = bits53_at(x, P - 158);
-            // round b with c, then hi with b (|lo| <= ulp(hi)/2)
-            if (c >> 52) ++b;
-            int64_t bs = (int64_t)b;
-            if (bs >= (1ll << 52)) {
-                ++a;
-                bs -= (1ll << 53);
-            }
-            double hi = scaled_u54(a, P - 52 - S2);
-            double lo = bs >= 0 ? scaled_u54((uint64_t)bs, P - 105 - S2) : -scaled_u54((uint64_t)(-bs), P - 105 - S2);
-            v = dd::make(neg ? -hi : hi, neg ? -lo : lo);
+        XF r;
+        if (top < 0) {
+            r.zero = true; r.neg = false; r.m = 0; r.e = 0;
+            return r;
         }
-        double2 *pc = C + i + j * ldc;
-        dd::real r = alpha_one ? v : dd::mul_fast(alpha, v);
-        if (beta_kind == 0) {
-            dd::store(pc, r);
-        } else {
-            dd::real c0 = dd::load(pc);
-            if (beta_kind == 2) c0 = dd::mul_exact(c0, beta);
-            dd::store(pc, dd::add_exact(c0, r));
-        }
+        // 128-bit window [P-127, P] below the leading bit P
+        const int z = __clz((int)x[top]);
+        const int P = top * 32 + 31 - z;
+        uint64_t w0 = ((uint64_t)limb_at(x, top) << 32) | limb_at(x, top - 1);
+        uint64_t w1 = ((uint64_t)limb_at(x, top - 2) << 32) | limb_at(x, top - 3);
+        uint64_t w2 = (uint64_t)limb_at(x, top - 4) << 32;
+        unsigned __int128 m = ((unsigned __int128)w0 << 64) | w1;
+        if (z) m = (m << z) | (w2 >> (64 - z));
+        r.neg = neg;
+        r.zero = false;
+        r.m = m;
+        r.e = P - 127 - S2;
+        return r;
     }
-}
+};
 
-// CRT of one residue vector c[l] (values in [0, p_l)) into a double-double
-// scaled by 2^-S2.
-__device__ __forceinline__ dd::real crt_to_dd(const uint32_t *c, const OzCrtParams &K, int S2)
+// C(i, j) := alpha * X(i, j) * 2^-S2 + beta * C(i, j), real.
+__global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, const uint16_t *__restrict__ R,
+                                                        int64_t Mp, int64_t Np, const int *__restrict__ ea,
+                                                        const int *__restrict__ eb, int bits, OzCrtParams K,
+                                                        dd::real alpha, int alpha_one, dd::real beta, int beta_kind,
+                                                        double2 *C, int64_t ldc, int uplo)
 {
-    uint64_t S[kNL];
-#pragma unroll
-    for (int t = 0; t < kNL; ++t) S[t] = 0;
-    float qf = 0.0f;
-    for (int l = 0; l < K.nmod; ++l) {
-        qf = __fmaf_rn((float)c[l], K.f[l], qf);
-#pragma unroll
-        for (int t = 0; t < kNL; ++t) S[t] += (uint64_t)c[l] * K.W[l][t];
-    }
-    uint32_t x[kNL];
-    uint64_t carry = 0;
-#pragma unroll
-    for (int t = 0; t < kNL; ++t) {
-        uint64_t v = S[t] + carry;
-        x[t] = (uint32_t)v;
-        carry = v >> 32;
-    }
-    uint32_t qv = (uint32_t)rintf(qf);
-    uint64_t borrow = 0, mc = 0;
-#pragma unroll
-    for (int t = 0; t < kNL; ++t) {
-        uint64_t prod = (uint64_t)qv * K.M[t] + mc;
-        mc = prod >> 32;
-        uint64_t sub = (uint64_t)(uint32_t)prod + borrow;
-        uint64_t v = (uint64_t)x[t] - sub;
-        x[t] = (uint32_t)v;
-        borrow = (v >> 63) & 1;
-    }
-    const bool neg = (x[kNL - 1] >> 31) != 0;
-    if (neg) {
-        uint64_t cy = 1;
-#pragma unroll
-        for (int t = 0; t < kNL; ++t) {
-            uint64_t v = (uint64_t)(~x[t]) + cy;
-            x[t] = (uint32_t)v;
-            cy = v >> 32;
+    __shared__ CrtSmem sm;
+    crt_smem_fill(sm, K);
+    __syncthreads();
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int nmod = K.nmod;
+    const XF xa = xf_from_dd(alpha.hi, alpha.lo), xb = xf_from_dd(beta.hi, beta.lo);
+    for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+        if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
+        XF v;
+        v.zero = true; v.neg = false; v.m = 0; v.e = 0;
+        if (ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
+            CrtAcc acc;
+            acc.reset();
+            const uint16_t *rp = R + j * Mp + i;
+            for (int l = 0; l < nmod; ++l) acc.add(sm, l, rp[(int64_t)l * Np * Mp]);
+            v = acc.finish(sm, (bits - 2 - ea[i]) + (bits - 2 - eb[j]));
         }
+        if (!alpha_one) v = xf_mul(xa, v);
+        double2 *pc = C + i + j * ldc;
+        if (beta_kind != 0) {
+            double2 c0 = *pc;
+            if (!isfinite(c0.x)) {
+                // non-finite C: the double-double operators propagate it
+                dd::real cv = dd::make(c0.x, c0.y);
+                if (beta_kind == 2) cv = dd::mul_exact(cv, beta);
+                dd::store(pc, dd::add_exact(cv, xf_dd(v)));
+                continue;
+            }
+            XF xc = xf_from_dd(c0.x, c0.y);
+            if (beta_kind == 2) xc = xf_mul(xb, xc);
+            v = xf_add(v, xc);
+        }
+        dd::store(pc, xf_dd(v));
     }
-    int top = -1;
-#pragma unroll
-    for (int t = kNL - 1; t >= 0; --t)
-        if (top < 0 && x[t] != 0) top = t;
-    if (top < 0) return dd::make(0.0, 0.0);
-    const int P = top * 32 + 31 - __clz((int)x[top]);
-    uint64_t a = bits53_at(x, P - 52);
-    uint64_t b = bits53_at(x, P - 105);
-    uint64_t cc = bits53_at(x, P - 158);
-    if (cc >> 52) ++b;
-    int64_t bs = (int64_t)b;
-    if (bs >= (1ll << 52)) {
-        ++a;
-        bs -= (1ll << 53);
-    }
-    double hi = scaled_u54(a, P - 52 - S2);
-    double lo = bs >= 0 ? scaled_u54((uint64_t)bs, P - 105 - S2) : -scaled_u54((uint64_t)(-bs), P - 105 - S2);
-    return neg ? dd::make(-hi, -lo) : dd::make(hi, lo);
 }
 
 // Complex: R holds the residues of P1 = Ar*Br, P2 = Ai*Bi and
 // P3 = (Ar+Ai)*(Br+Bi) as components 0..2; Re = P1 - P2, Im = P3 - P1 - P2.
-__global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, const uint8_t *__restrict__ R,
+__global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, const uint16_t *__restrict__ R,
                                                           int64_t Mp, int64_t Np, const int *__restrict__ ea,
                                                           const int *__restrict__ eb, int bits, OzCrtParams K,
                                                           dd::cplx alpha, int alpha_one, dd::cplx beta,
                                                           int beta_kind, double2 *C, int64_t ldc, int uplo, int herm,
                                                           int real_beta)
 {
+    __shared__ CrtSmem sm;
+    crt_smem_fill(sm, K);
+    __syncthreads();
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= m) return;
-    const int64_t cstride = (int64_t)K.nmod * Np * Mp;
+    const int nmod = K.nmod;
+    const int64_t cstride = (int64_t)nmod * Np * Mp;
+    const XF ar = xf_from_dd(alpha.re.hi, alpha.re.lo), ai = xf_from_dd(alpha.im.hi, alpha.im.lo);
+    const XF br = xf_from_dd(beta.re.hi, beta.re.lo), bi = xf_from_dd(beta.im.hi, beta.im.lo);
     for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
         if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
-        uint32_t cre[kMaxMod], cim[kMaxMod];
-        for (int l = 0; l < K.nmod; ++l) {
-            const int64_t o = ((int64_t)l * Np + j) * Mp + i;
-            int p = (int)K.pm[l];
-            int p1 = R[o], p2 = R[cstride + o], p3 = R[2 * cstride + o];
-            int re = p1 - p2;
-            if (re < 0) re += p;
-            int im = p3 - p1 - p2;
-            im %= p;
-            if (im < 0) im += p;
-            cre[l] = (uint32_t)re;
-            cim[l] = (uint32_t)im;
-        }
-        dd::cplx v;
-        v.re = dd::make(0.0, 0.0);
-        v.im = v.re;
+        XF vr, vi;
+        vr.zero = vi.zero = true; vr.neg = vi.neg = false; vr.m = vi.m = 0; vr.e = vi.e = 0;
         if (ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
+            CrtAcc accr, acci;
+            accr.reset();
+            acci.reset();
+            for (int l = 0; l < nmod; ++l) {
+                const int64_t o = ((int64_t)l * Np + j) * Mp + i;
+                const int p = (int)sm.pm[l];
+                const int p1 = R[o], p2 = R[cstride + o], p3 = R[2 * cstride + o];
+                int re = p1 - p2;
+                if (re < 0) re += p;
+                int im = p3 - p1 - p2;
+                if (im < 0) im += p;
+                if (im < 0) im += p;
+                accr.add(sm, l, (uint32_t)re);
+                acci.add(sm, l, (uint32_t)im);
+            }
             const int S2 = (bits - 2 - ea[i]) + (bits - 2 - eb[j]);
-            v.re = crt_to_dd(cre, K, S2);
-            v.im = crt_to_dd(cim, K, S2);
+            vr = accr.finish(sm, S2);
+            vi = acci.finish(sm, S2);
+        }
+        XF rr = vr, ri = vi;
+        if (!alpha_one) {
+            XF t = xf_mul(ai, vi);
+            t.neg = !t.neg;
+            rr = xf_add(xf_mul(ar, vr), t);
+            ri = xf_add(xf_mul(ar, vi), xf_mul(ai, vr));
         }
         double2 *pc = C + 2 * (i + j * ldc);
-        dd::cplx r = alpha_one ? v : dd::cmul_fast(alpha, v);
-        dd::cplx out = r;
         if (beta_kind != 0) {
-            dd::cplx c0 = dd::cload(pc);
+            double2 c0r = pc[0], c0i = pc[1];
+            if (!isfinite(c0r.x) || !isfinite(c0i.x)) {
+                dd::cplx c0;
+                c0.re = dd::make(c0r.x, c0r.y);
+                c0.im = dd::make(c0i.x, c0i.y);
+                if (beta_kind == 2) {
+                    if (real_beta) {
+                        c0.re = dd::mul_exact(beta.re, c0.re);
+                        c0.im = dd::mul_exact(beta.re, c0.im);
+                    } else {
+                        c0 = dd::cmul_exact(c0, beta);
+                    }
+                }
+                dd::cplx out;
+                out.re = dd::add_exact(c0.re, xf_dd(rr));
+                out.im = dd::add_exact(c0.im, xf_dd(ri));
+                if (herm && i == j) out.im = dd::make(0.0, 0.0);
+                dd::cstore(pc, out);
+                continue;
+            }
+            XF cr = xf_from_dd(c0r.x, c0r.y), ci = xf_from_dd(c0i.x, c0i.y);
             if (beta_kind == 2) {
                 if (real_beta) {
-                    c0.re = dd::mul_exact(beta.re, c0.re);
-                    c0.im = dd::mul_exact(beta.re, c0.im);
+                    cr = xf_mul(br, cr);
+                    ci = xf_mul(br, ci);
                 } else {
-                    c0 = dd::cmul_exact(c0, beta);
+                    XF t = xf_mul(bi, ci);
+                    t.neg = !t.neg;
+                    XF nr = xf_add(xf_mul(br, cr), t);
+                    XF ni = xf_add(xf_mul(br, ci), xf_mul(bi, cr));
+                    cr = nr;
+                    ci = ni;
                 }
             }
-            out = dd::cadd_exact(c0, r);
+            rr = xf_add(rr, cr);
+            ri = xf_add(ri, ci);
         }
-        if (herm && i == j) out.im = dd::make(0.0, 0.0);
+        dd::cplx out;
+        out.re = xf_dd(rr);
+        out.im = (herm && i == j) ? dd::make(0.0, 0.0) : xf_dd(ri);
         dd::cstore(pc, out);
     }
 }
@@ -879,13 +941,14 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     }
     const GemmArgs &g = g0;
     const int64_t m = g.m, n = g.n, k = g.k;
-    const int64_t Mp = (m + TC_BM - 1) / TC_BM * TC_BM;
-    const int64_t Np = (n + TC_BN - 1) / TC_BN * TC_BN;
-    const int64_t Kp = (k + TC_BK - 1) / TC_BK * TC_BK;
     const int nc = cplx ? 3 : 1;
     // Real SYRK (op(B) = op(A)^T on the same array): op(B)'s residue rows are
-    // op(A)'s, so one conversion serves both operands.
+    // op(A)'s, so one conversion serves both operands; both then use the same
+    // per-modulus row padding.
     const bool shared_ops = !cplx && g.uplo != 0 && g.A == g.B && g.lda == g.ldb && g.ta != g.tb && m == n;
+    const int64_t Np = (n + TC_BN - 1) / TC_BN * TC_BN;
+    const int64_t Mp = shared_ops ? Np : (m + TC_BM - 1) / TC_BM * TC_BM;
+    const int64_t Kp = (k + TC_BK - 1) / TC_BK * TC_BK;
 
     // 1. exponent bounds of the rows of op(A) / columns of op(B)
     int *ex = (int *)dev_alloc(sizeof(int) * (size_t)(m + n + 2), routine);
@@ -904,8 +967,12 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         dev_free(ex);
         return false;
     }
-    if (hsum[0] >= 1024 || hsum[1] >= 1024) {
-        // Inf/NaN present: the integer scheme has no representation for them;
+    const bool scal_nonfinite =
+        cplx ? !(std::isfinite(g.calpha.re.hi) && std::isfinite(g.calpha.im.hi) && std::isfinite(g.cbeta.re.hi) &&
+                 std::isfinite(g.cbeta.im.hi))
+             : !(std::isfinite(g.alpha.hi) && std::isfinite(g.beta.hi));
+    if (hsum[0] >= 1024 || hsum[1] >= 1024 || scal_nonfinite) {
+        // Inf/NaN in A, B, alpha or beta: the integer scheme cannot carry them;
         // the FP64 engine propagates them as the reference does.
         dev_free(ex);
         return cplx ? gemm_plain_cplx(g, routine) : gemm_plain_real(g, routine);
@@ -927,7 +994,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     // 3. residue operands: [comp][modulus][row][k] fp16
     const size_t a_bytes = (size_t)nc * md.n * Mp * Kp * 2;
     const size_t b_bytes = shared_ops ? 0 : (size_t)nc * md.n * Np * Kp * 2;
-    const size_t r_bytes = (size_t)nc * md.n * Np * Mp;
+    const size_t r_bytes = (size_t)nc * md.n * Np * Mp * sizeof(uint16_t);
     uint8_t *work = (uint8_t *)dev_alloc(a_bytes + b_bytes + r_bytes + 256, routine);
     if (!work) {
         dev_free(ex);
@@ -935,7 +1002,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     }
     __half *Ares = (__half *)work;
     __half *Bres = shared_ops ? Ares : (__half *)(work + a_bytes);
-    uint8_t *R = work + a_bytes + b_bytes;
+    uint16_t *R = (uint16_t *)(work + a_bytes + b_bytes);
     phase_mark(PH_RES);
     {
         // op(A) = A: A[i + p*lda] is contiguous along rows; op(A) = A^T along k.

@@ -1,0 +1,99 @@
+"""CPU check of the CRT reconstruction's integer extended-float arithmetic.
+
+epblas-parallel_gb300/csrc/xfloat.cuh is __host__ __device__; this test
+compiles it for the host (tests/xfloat_harness.cpp) and compares conversions,
+products, sums and the alpha*x + beta*c update with exact rational arithmetic.
+"""
+import ctypes as C
+import os
+import subprocess
+import tempfile
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def xf():
+    d = tempfile.mkdtemp()
+    so = os.path.join(d, "libxf.so")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", os.path.join(HERE, "xfloat_harness.cpp"),
+                    "-o", so], check=True)
+    lib = C.CDLL(so)
+    D = C.c_double
+    P = C.POINTER(D)
+    lib.xf_roundtrip.argtypes = [D, D, P, P]
+    lib.xf_mul_dd.argtypes = [D, D, D, D, P, P]
+    lib.xf_add_dd.argtypes = [D, D, D, D, P, P]
+    lib.xf_axpby.argtypes = [D] * 8 + [P, P]
+    return lib
+
+
+def call(f, *args):
+    h, l = C.c_double(), C.c_double()
+    f(*args, C.byref(h), C.byref(l))
+    return h.value, l.value
+
+
+def dd(rng, scale_exp):
+    hi = (rng.random() * 2 - 1) * 2.0 ** scale_exp
+    lo = hi * 2.0 ** -53 * (rng.random() * 2 - 1)
+    s = hi + lo
+    return s, lo - (s - hi)
+
+
+def exact(h, l):
+    return Fraction(h) + Fraction(l)
+
+
+def normalized(h, l):
+    return h + l == h
+
+
+def test_roundtrip_is_exact(xf):
+    rng = np.random.default_rng(1)
+    cases = [(0.0, 0.0), (1.0, 0.0), (-1.0, 2.0 ** -60), (2.0 ** -1000, 2.0 ** -1060), (3.0, -2.0 ** -52)]
+    cases += [dd(rng, int(e)) for e in rng.integers(-300, 300, 500)]
+    for h, l in cases:
+        oh, ol = call(xf.xf_roundtrip, h, l)
+        assert exact(oh, ol) == exact(h, l) or abs(exact(oh, ol) - exact(h, l)) <= abs(exact(h, l)) * Fraction(2) ** -126
+        assert normalized(oh, ol)
+
+
+def test_products(xf):
+    rng = np.random.default_rng(2)
+    for _ in range(1000):
+        a = dd(rng, int(rng.integers(-100, 100)))
+        b = dd(rng, int(rng.integers(-100, 100)))
+        oh, ol = call(xf.xf_mul_dd, *a, *b)
+        ex = exact(*a) * exact(*b)
+        assert abs(exact(oh, ol) - ex) <= abs(ex) * Fraction(2) ** -105, (a, b)
+        assert normalized(oh, ol)
+
+
+def test_sums_including_cancellation(xf):
+    rng = np.random.default_rng(3)
+    for t in range(1000):
+        a = dd(rng, int(rng.integers(-60, 60)))
+        if t % 3 == 0:
+            b = (-a[0], -a[1] * 0.5)            # heavy cancellation
+        else:
+            b = dd(rng, int(rng.integers(-60, 60)))
+        oh, ol = call(xf.xf_add_dd, *a, *b)
+        ex = exact(*a) + exact(*b)
+        scale = max(abs(exact(*a)), abs(exact(*b)))
+        assert abs(exact(oh, ol) - ex) <= scale * Fraction(2) ** -105 + abs(ex) * Fraction(2) ** -105
+        assert normalized(oh, ol)
+
+
+def test_alpha_x_plus_beta_c(xf):
+    rng = np.random.default_rng(4)
+    for _ in range(500):
+        al, x, be, c = (dd(rng, int(rng.integers(-40, 40))) for _ in range(4))
+        oh, ol = call(xf.xf_axpby, *al, *x, *be, *c)
+        ex = exact(*al) * exact(*x) + exact(*be) * exact(*c)
+        scale = abs(exact(*al) * exact(*x)) + abs(exact(*be) * exact(*c))
+        assert abs(exact(oh, ol) - ex) <= scale * Fraction(2) ** -104

@@ -1,0 +1,33 @@
+// Host-side harness for epblas-parallel_gb300/csrc/xfloat.cuh (the integer
+// extended-float arithmetic of the CRT reconstruction), compiled with g++ by
+// tests/test_xfloat.py so the device code's logic is checked on the CPU.
+#include "../epblas-parallel_gb300/csrc/xfloat.cuh"
+
+extern "C" {
+
+void xf_roundtrip(double hi, double lo, double *oh, double *ol)
+{
+    xfp::XF x = xfp::xf_from_dd(hi, lo);
+    xfp::xf_to_dd(x, *oh, *ol);
+}
+
+void xf_mul_dd(double ah, double al, double bh, double bl, double *oh, double *ol)
+{
+    xfp::xf_to_dd(xfp::xf_mul(xfp::xf_from_dd(ah, al), xfp::xf_from_dd(bh, bl)), *oh, *ol);
+}
+
+void xf_add_dd(double ah, double al, double bh, double bl, double *oh, double *ol)
+{
+    xfp::xf_to_dd(xfp::xf_add(xfp::xf_from_dd(ah, al), xfp::xf_from_dd(bh, bl)), *oh, *ol);
+}
+
+// alpha * a + beta * c, the reconstruction's update
+void xf_axpby(double alh, double all, double ah, double al, double beh, double bel, double ch, double cl, double *oh,
+              double *ol)
+{
+    xfp::XF v = xfp::xf_mul(xfp::xf_from_dd(alh, all), xfp::xf_from_dd(ah, al));
+    xfp::XF w = xfp::xf_mul(xfp::xf_from_dd(beh, bel), xfp::xf_from_dd(ch, cl));
+    xfp::xf_to_dd(xfp::xf_add(v, w), *oh, *ol);
+}
+
+}
