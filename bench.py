@@ -1,6 +1,6 @@
 """Benchmark: double-double GEMM throughput at n = 8192 on GB300.
 
-Metric (the reference's headline, BASELINE): DD-GEMM GFLOP/s at
+Metric (the reference's headline): DD-GEMM GFLOP/s at
 M = N = K = 8192 with the integer-exact tensor-core ("Ozaki") engine, next to
 the plain FP64 error-free-transform engine on the same GPU, work counted as
 2*M*N*K double-double flops.
@@ -299,8 +299,18 @@ def main():
     ap.add_argument("--n", type=int, default=N_GEMM)
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-check", action="store_true")
+    ap.add_argument("--workload", default="gemm", choices=WORKLOADS,
+                    help="gemm: the headline line; the others measure one routine of the level-1/2/3 mix")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.workload != "gemm":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "secondary workloads have no CPU reference arm"}))
+            return
+        if not os.path.exists(os.path.join(ge.PKG, "libmwblas_gb300.so")):
+            ge.build()
+        run_workload(args)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -403,6 +413,334 @@ def tc_traffic_from_profile():
         if line.startswith("dram_bytes_per_launch_scaled:"):
             return float(line.split(":")[1].strip())
     return None
+
+
+# ---------------------------------------------------------------------------
+# Secondary workloads (--workload ...): the level-1/2/3 mix and the batched
+# workloads, each printed as one JSON line of the same shape as the headline.
+# ---------------------------------------------------------------------------
+
+WORKLOADS = ("gemm", "stress", "syrk", "herk", "trsm", "gemv", "dot", "axpy", "batched_gemm", "batched_trsm")
+
+
+def _dev_dd(torch, shape, gen, dev, cplx_=False):
+    """Device DD array (..., 2) [(..., 2, 2) complex]: hi ~ U[-1,1), lo = hi*2^-53*U[-1,1), renormalised."""
+    def one():
+        hi = torch.rand(shape, generator=gen, device=dev, dtype=torch.float64) * 2 - 1
+        lo = hi * 2.0 ** -53 * (torch.rand(shape, generator=gen, device=dev, dtype=torch.float64) * 2 - 1)
+        s = hi + lo
+        return torch.stack([s, lo - (s - hi)], -1)
+    return torch.stack([one(), one()], -2) if cplx_ else one()
+
+
+def _timed(torch, fn, steps, warmup, stream, reset=None, gpu=0):
+    """Per-step CUDA events on the library's stream; `reset` runs between steps, untimed."""
+    for _ in range(warmup):
+        if reset:
+            reset()
+        fn()
+    torch.cuda.synchronize()
+    ms = 0.0
+    with ClockSampler(gpu) as clk:
+        for _ in range(steps):
+            if reset:
+                reset()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+    return ms / steps, clk.summary()
+
+
+def run_workload(args):
+    import torch
+    mwb = ge._load("mwblas", os.path.join(ge.PKG, "mwblas.py"))
+    orc = ge._load("oracle", os.path.join(ROOT, "oracle", "oracle.py"))
+    lib = mwb.MWBlas(os.path.join(ge.PKG, "libmwblas_gb300.so"))
+    o = orc.Oracle() if not args.skip_check else None
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    lib.lib.mwblas_set_stream(stream.cuda_stream)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(4321)
+    rng = np.random.default_rng(4321)
+    pk, pk_kind = peaks()
+    w = args.workload
+    hb = lambda t: t.cpu().numpy()
+    al = np.array([1.25, 1.25 * 2.0 ** -55])
+    be = np.array([-0.75, 0.75 * 2.0 ** -56])
+    check = {}
+    roof = None
+    l0 = lib.lib.mwblas_launch_count()
+
+    if w == "stress":
+        # Exponent-spread stress input: A(i,:) = U[1,2)*sign * 2^e_i, B(:,j) = ... * 2^f_j,
+        # e_i, f_j uniform integers in [-30, 30]; Ozaki engine at n^3.
+        n = args.n
+        def spread(row_scaled):
+            u = torch.rand((n, n), generator=gen, device=dev, dtype=torch.float64) * 2 - 1
+            mant = torch.where(u < 0, -1.0, 1.0) * (1 + u.abs())
+            lo = mant * 2.0 ** -53 * (torch.rand((n, n), generator=gen, device=dev, dtype=torch.float64) * 2 - 1)
+            hi = mant + lo
+            lo = lo - (hi - mant)
+            sc = torch.pow(2.0, torch.randint(-30, 31, (n,), generator=gen, device=dev).to(torch.float64))
+            sc = sc[None, :] if row_scaled else sc[:, None]     # storage [column, row]
+            return torch.stack([hi * sc, lo * sc], -1).contiguous()
+        A, B = spread(True), spread(False)
+        C = _dev_dd(torch, (n, n), gen, dev)
+        C0 = C.clone()
+        fn = lambda: lib.mgemm("N", "N", n, n, n, al, A.data_ptr(), n, B.data_ptr(), n, be, C.data_ptr(), n,
+                               engine="ozaki")
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: C.copy_(C0))
+        value, unit, metric = 2.0 * n ** 3 / ms / 1e6, "DD-GFLOP/s", f"DD-GEMM GFLOP/s n={n} exponent-spread stress, Ozaki"
+        cfg = {"workload": f"mgemm_ {n}^3 NN, A rows / B columns scaled by 2^e, e ~ U{{-30..30}}", "engine": "ozaki"}
+        check["moduli"] = int(lib.lib.mwblas_last_ozaki_moduli())
+        if o:
+            C.copy_(C0)
+            fn()
+            rows, cols = rng.integers(0, n, 256), rng.integers(0, n, 256)
+            hA, hB, hC0 = hb(A), hb(B), hb(C0)
+            want = o.qgemm("N", "N", n, n, n, al, hA, n, hB, n, be, hC0, n, rows=rows, cols=cols)
+            got = hb(C)[cols, rows]
+            op = orc.dd_abs(al) * n * orc.dd_absmax(hA) * orc.dd_absmax(hB) + orc.dd_abs(be) * orc.dd_absmax(hC0)
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+            # componentwise view: error relative to |alpha| sum_p |a_ip||b_pj| of the sampled entries
+            check["samples"] = 256
+    elif w == "syrk":
+        n, k = 8192, 2048
+        A = _dev_dd(torch, (k, n), gen, dev)          # n x k, lda = n
+        C = _dev_dd(torch, (n, n), gen, dev)
+        C0 = C.clone()
+        fn = lambda: lib.msyrk("U", "N", n, k, al, A.data_ptr(), n, be, C.data_ptr(), n)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: C.copy_(C0))
+        value, unit = n * (n + 1) * k / ms / 1e6, "DD-GFLOP/s"
+        metric = "DD-SYRK GFLOP/s n=8192 k=2048 upper (n(n+1)k flops)"
+        cfg = {"workload": "msyrk_ U N n=8192 k=2048"}
+        if o:
+            C.copy_(C0)
+            fn()
+            i = rng.integers(0, n, 256)
+            j = rng.integers(0, n, 256)
+            rows, cols = np.minimum(i, j), np.maximum(i, j)
+            hA, hC0 = hb(A), hb(C0)
+            want = o.qgemm("N", "T", n, n, k, al, hA, n, hA, n, be, hC0, n, rows=rows, cols=cols)
+            got = hb(C)[cols, rows]
+            op = orc.dd_abs(al) * k * orc.dd_absmax(hA) ** 2 + orc.dd_abs(be) * orc.dd_absmax(hC0)
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+    elif w == "herk":
+        n, k = 4096, 1024
+        A = _dev_dd(torch, (k, n), gen, dev, cplx_=True)
+        C = _dev_dd(torch, (n, n), gen, dev, cplx_=True)
+        C0 = C.clone()
+        fn = lambda: lib.wherk("U", "N", n, k, al, A.data_ptr(), n, be, C.data_ptr(), n)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: C.copy_(C0))
+        value, unit = 4.0 * n * (n + 1) * k / ms / 1e6, "DD-GFLOP/s"
+        metric = "DD-HERK GFLOP/s n=4096 k=1024 upper (4n(n+1)k real flops)"
+        cfg = {"workload": "wherk_ U N n=4096 k=1024 complex"}
+        if o:
+            C.copy_(C0)
+            fn()
+            i = rng.integers(0, n, 256)
+            j = rng.integers(0, n, 256)
+            rows, cols = np.minimum(i, j), np.maximum(i, j)
+            off = rows != cols
+            rows, cols = rows[off], cols[off]
+            hA, hC0 = hb(A), hb(C0)
+            ca = np.array([al, [0.0, 0.0]])
+            cb = np.array([be, [0.0, 0.0]])
+            want = o.qwgemm("N", "C", n, n, k, ca, hA, n, hA, n, cb, hC0, n, rows=rows, cols=cols)
+            got = hb(C)[cols, rows]
+            op = 2 * (orc.dd_abs(al) * k * orc.dd_absmax(hA) ** 2 + orc.dd_abs(be) * orc.dd_absmax(hC0))
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+    elif w == "trsm":
+        m, nr = 4096, 1024
+        A = _dev_dd(torch, (m, m), gen, dev)
+        A[..., 0] /= m
+        A[..., 1] /= m
+        d = torch.arange(m, device=dev)
+        dg = m * (1 + torch.rand(m, generator=gen, device=dev, dtype=torch.float64))
+        A[d, d, 0] = dg
+        A[d, d, 1] = 0.0
+        B = _dev_dd(torch, (nr, m), gen, dev)
+        B0 = B.clone()
+        fn = lambda: lib.mtrsm("L", "L", "N", "N", m, nr, al, A.data_ptr(), m, B.data_ptr(), m)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: B.copy_(B0))
+        value, unit = float(m) * m * nr / ms / 1e6, "DD-GFLOP/s"
+        metric = "DD-TRSM GFLOP/s LLNN m=4096 nrhs=1024 (m^2 nrhs flops)"
+        cfg = {"workload": "mtrsm_ L L N N m=4096 n=1024, diag U[m,2m], off-diagonal U[-1,1)/m"}
+        if o:
+            B.copy_(B0)
+            fn()
+            cols = rng.choice(nr, 4, replace=False)
+            hA = hb(A)
+            want = np.ascontiguousarray(hb(B0)[cols])
+            o.qtrsm("L", "L", "N", "N", m, len(cols), al, hA, m, want, m)
+            got = hb(B)[cols]
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, orc.dd_abs(al) * orc.dd_absmax(hb(B0)))
+            check["columns_checked"] = len(cols)
+    elif w == "gemv":
+        m = n = 16384
+        A = _dev_dd(torch, (n, m), gen, dev)
+        x = _dev_dd(torch, (n,), gen, dev)
+        y = _dev_dd(torch, (m,), gen, dev)
+        y0 = y.clone()
+        fn = lambda: lib.mgemv("N", m, n, al, A.data_ptr(), m, x.data_ptr(), 1, be, y.data_ptr(), 1)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: y.copy_(y0))
+        nbytes = 16.0 * (m * n + n + 2 * m)
+        value, unit = nbytes / ms / 1e6, "GB/s"
+        metric = "DD-GEMV HBM GB/s m=n=16384 (16(mn+n+2m) bytes)"
+        cfg = {"workload": "mgemv_ N m=n=16384 incx=incy=1"}
+        roof = {"bound": "hbm", "achieved": value, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": value / pk["hbm_gbs"], "peak_kind": pk_kind, "traffic": None}
+        if o:
+            y.copy_(y0)
+            fn()
+            rows = np.sort(rng.choice(m, 64, replace=False))
+            sub = np.ascontiguousarray(hb(A[:, torch.as_tensor(rows, device=dev)]))
+            want = hb(y0)[rows].copy()
+            o.qgemv("N", len(rows), n, al, sub, len(rows), hb(x), 1, be, want, 1)
+            got = hb(y)[rows]
+            amax = float(A[..., 0].abs().max())
+            op = orc.dd_abs(al) * n * amax * orc.dd_absmax(hb(x)) + orc.dd_abs(be) * orc.dd_absmax(hb(y0))
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+    elif w in ("dot", "axpy"):
+        n = 1 << 28
+        x = _dev_dd(torch, (n,), gen, dev)
+        y = _dev_dd(torch, (n,), gen, dev)
+        if w == "dot":
+            out = {}
+            fn = lambda: out.__setitem__("r", lib.mdot(n, x.data_ptr(), 1, y.data_ptr(), 1))
+            ms, clk = _timed(torch, fn, args.steps, args.warmup, stream)
+            nbytes = 32.0 * n
+            metric = "DD-DOT HBM GB/s n=2^28 (32n bytes)"
+            cfg = {"workload": "mdot_ n=2^28 incx=incy=1"}
+            if o:
+                hx, hy = hb(x), hb(y)
+                want = o.qdot(n, hx, 1, hy, 1)
+                got = np.array(out["r"]).reshape(1, 2)
+                check["normwise_err"] = orc.normwise_error(got, np.asarray(want).reshape(1, 2),
+                                                            n * orc.dd_absmax(hx) * orc.dd_absmax(hy))
+        else:
+            y0 = y.clone()
+            fn = lambda: lib.maxpy(n, al, x.data_ptr(), 1, y.data_ptr(), 1)
+            ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: y.copy_(y0))
+            nbytes = 48.0 * n
+            metric = "DD-AXPY HBM GB/s n=2^28 (48n bytes)"
+            cfg = {"workload": "maxpy_ n=2^28 incx=incy=1"}
+            if o:
+                y.copy_(y0)
+                fn()
+                idx = torch.as_tensor(np.sort(rng.choice(n, 4096, replace=False)), device=dev)
+                want = np.ascontiguousarray(hb(y0[idx]))
+                o.qaxpy(len(idx), al, np.ascontiguousarray(hb(x[idx])), want)
+                got = hb(y[idx])
+                check["normwise_err_sampled"] = orc.normwise_error(got, want, orc.dd_abs(al) * orc.dd_absmax(hb(x[idx]))
+                                                                   + orc.dd_absmax(hb(y0[idx])))
+        value, unit = nbytes / ms / 1e6, "GB/s"
+        roof = {"bound": "hbm", "achieved": value, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": value / pk["hbm_gbs"], "peak_kind": pk_kind, "traffic": None}
+    elif w in ("batched_gemm", "batched_trsm"):
+        cnt = 20000 if w == "batched_gemm" else 5000
+        if w == "batched_gemm":
+            dims = np.exp(rng.uniform(np.log(8), np.log(512), (cnt, 3))).round().astype(np.int64)
+            m_, n_, k_ = dims[:, 0], dims[:, 1], dims[:, 2]
+            sizes = np.stack([m_ * k_, k_ * n_, m_ * n_], 1)
+        else:
+            m_ = np.exp(rng.uniform(np.log(16), np.log(256), cnt)).round().astype(np.int64)
+            n_ = rng.integers(1, 65, cnt)
+            sizes = np.stack([m_ * m_, m_ * n_], 1)
+        offs = np.concatenate([[0], np.cumsum(sizes.reshape(-1))])
+        arena = _dev_dd(torch, (int(offs[-1]),), gen, dev)
+        base = arena.data_ptr()
+        ptr = lambda q: [base + 16 * int(v) for v in offs[q:-1:sizes.shape[1]]]
+        if w == "batched_gemm":
+            a_p, b_p, c_p = ptr(0), ptr(1), ptr(2)
+            C0 = arena.clone()
+            ta, tb = ["N"] * cnt, ["N"] * cnt
+            alist, blist = [al] * cnt, [be] * cnt
+            args_g = dict(ta=ta, tb=tb, m=m_, n=n_, k=k_, alpha=alist, a=a_p, lda=m_, b=b_p, ldb=k_, beta=blist,
+                          c=c_p, ldc=m_)
+            rc, chosen = lib.mgemm_grouped_tune(**args_g)
+            assert rc == 0, lib.last_error()
+            garr = lib._grouped_arrays(*[args_g[k] for k in ("ta", "tb", "m", "n", "k", "alpha", "a", "lda", "b",
+                                                            "ldb", "beta", "c", "ldc")])
+            gptrs = [x.ctypes.data for x in garr[1:]]
+            fn = lambda: lib.lib.mgemm_grouped(garr[0], *gptrs)
+            ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: arena.copy_(C0))
+            value, unit = float(np.sum(2.0 * m_ * n_ * k_)) / ms / 1e6, "DD-GFLOP/s"
+            metric = "batched DD-GEMM GFLOP/s, 20000 instances M,N,K log-uniform [8,512]"
+            cfg = {"workload": "mgemm_grouped 20000 x NN, M,N,K ~ logU[8,512]", "split_k_min_chosen": chosen,
+                   "launch": "one persistent kernel from a cached CUDA graph"}
+            if o:
+                arena.copy_(C0)
+                fn()
+                torch.cuda.synchronize()
+                errs = []
+                for t in rng.choice(cnt, 16, replace=False):
+                    mm, nn, kk = int(m_[t]), int(n_[t]), int(k_[t])
+                    seg = lambda q, r, c: hb(C0[int(offs[3 * t + q]):int(offs[3 * t + q]) + r * c]).reshape(c, r, 2)
+                    hA, hB, hC = seg(0, mm, kk), seg(1, kk, nn), seg(2, mm, nn)
+                    want = o.qgemm("N", "N", mm, nn, kk, al, hA, mm, hB, kk, be, hC.copy(), mm)
+                    got = hb(arena[int(offs[3 * t + 2]):int(offs[3 * t + 2]) + mm * nn]).reshape(nn, mm, 2)
+                    op = orc.dd_abs(al) * kk * orc.dd_absmax(hA) * orc.dd_absmax(hB) + orc.dd_abs(be) * orc.dd_absmax(hC)
+                    errs.append(orc.normwise_error(got, want, op) / (max(10, 4 * kk) * orc.EPS_DD))
+                check["max_err_over_tolerance_16_instances"] = float(max(errs))
+        else:
+            a_p, b_p = ptr(0), ptr(1)
+            # lower-triangular, diagonally dominant: off-diagonal / n, diagonal U[n, 2n]
+            for t in range(cnt):
+                nn = int(m_[t])
+                blk = arena[int(offs[2 * t]):int(offs[2 * t]) + nn * nn].view(nn, nn, 2)
+                blk /= nn
+            diag_idx = np.concatenate([offs[2 * t] + np.arange(int(m_[t])) * (int(m_[t]) + 1) for t in range(cnt)])
+            dv = torch.as_tensor(diag_idx, device=dev)
+            mt = torch.as_tensor(np.repeat(m_, m_).astype(np.float64), device=dev)
+            arena[dv, 0] = mt * (1 + torch.rand(len(diag_idx), generator=gen, device=dev, dtype=torch.float64))
+            arena[dv, 1] = 0.0
+            B0 = arena.clone()
+            tarr = [np.ascontiguousarray(m_, dtype=np.int64), np.ascontiguousarray(n_, dtype=np.int64),
+                    np.ascontiguousarray(np.tile(al, (cnt, 1))), np.asarray(a_p, dtype=np.uint64),
+                    np.ascontiguousarray(m_, dtype=np.int64), np.asarray(b_p, dtype=np.uint64),
+                    np.ascontiguousarray(m_, dtype=np.int64)]
+            tptrs = [x.ctypes.data for x in tarr]
+            fn = lambda: lib.lib.mtrsm_grouped(cnt, b"L", b"L", b"N", b"N", *tptrs)
+            ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: arena.copy_(B0))
+            value, unit = float(np.sum(m_.astype(np.float64) ** 2 * n_)) / ms / 1e6, "DD-GFLOP/s"
+            metric = "batched DD-TRSM GFLOP/s, 5000 LLNN systems n logU[16,256], nrhs U[1,64]"
+            cfg = {"workload": "mtrsm_grouped 5000 x L L N N", "launch": "one kernel, warp per 32 right-hand sides"}
+            if o:
+                arena.copy_(B0)
+                fn()
+                torch.cuda.synchronize()
+                errs = []
+                for t in rng.choice(cnt, 16, replace=False):
+                    mm, nn = int(m_[t]), int(n_[t])
+                    hA = hb(B0[int(offs[2 * t]):int(offs[2 * t]) + mm * mm]).reshape(mm, mm, 2)
+                    want = hb(B0[int(offs[2 * t + 1]):int(offs[2 * t + 1]) + mm * nn]).reshape(nn, mm, 2).copy()
+                    o.qtrsm("L", "L", "N", "N", mm, nn, al, hA, mm, want, mm)
+                    got = hb(arena[int(offs[2 * t + 1]):int(offs[2 * t + 1]) + mm * nn]).reshape(nn, mm, 2)
+                    e = orc.normwise_error(got, want, orc.dd_abs(al) * orc.dd_absmax(want))
+                    errs.append(e / (max(20, 8 * mm * mm) * orc.EPS_DD))
+                check["max_err_over_tolerance_16_instances"] = float(max(errs))
+    else:
+        raise SystemExit(f"unknown workload {w}")
+    code, msg = lib.last_error()
+    if code != 0:
+        raise RuntimeError(f"{w}: {code} {msg}")
+    launches = lib.lib.mwblas_launch_count() - l0
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64x2 (double-double)", "data": "synthetic (seeded, on device)",
+            "config": dict(cfg, l2="operands larger than the 129 MB L2" if w not in ("batched_trsm",) else
+                           "arena reset by a device copy between steps"),
+            "gpu_launches": int(launches), "clocks": clk, "check": check}
+    if roof:
+        line["roofline"] = roof
+    print(json.dumps(line))
+    lib.lib.mwblas_set_stream(None)
 
 
 if __name__ == "__main__":

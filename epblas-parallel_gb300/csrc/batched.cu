@@ -1,0 +1,718 @@
+// Batched uneven-size double-double GEMM and TRSM (no reference counterpart:
+// the reference's CPU baseline for this workload is an OpenMP loop over
+// instances calling mgemm_/mtrsm_, whose nested calls run serially,
+// mgemm_parallel.cpp:53-60).
+//
+// mgemm_grouped: one persistent kernel over all instances. The work list is
+// every (instance, 16x16 output tile, K split); CTAs of 64 threads pull items
+// from an atomic counter, so thousands of uneven instances keep all SMs busy.
+// Each item runs the FP64 extraction accumulation of the plain engine
+// (gemm_plain.cu), with sigma taken from an exponent scan of the item's own A
+// rows / B columns over its K range (no pre-pass, no extra scratch). Items of
+// a split instance write partial tiles; the CTA that completes a tile's last
+// split sums the partials in split order (deterministic) and applies
+// alpha/beta. The per-call state (descriptors, work counter, split counters,
+// partial tiles) is uploaded and the kernel launched from a CUDA graph that is
+// captured once per batch layout and replayed.
+//
+// The split-K policy (how many K elements a split must keep, and below how
+// many tiles an instance is split) is chosen by mgemm_grouped_tune, which
+// times the candidates on the caller's batch (writing to scratch copies of C)
+// and caches the winner for batches of the same shape class.
+//
+// mtrsm_grouped: one persistent kernel; a work item is (instance, 32 right-hand
+// sides); a warp solves them by substitution in double-double, one lane per
+// right-hand side, using the double-double reciprocal of the diagonal as the
+// reference does (mtrsm_serial.cpp:144).
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "dd.cuh"
+#include "level3.h"
+#include "runtime.h"
+
+namespace mw {
+
+namespace {
+
+constexpr int kNoExp = -30000;
+constexpr int GT = 16;        // output tile edge
+constexpr int GTHREADS = 64;  // 8 x 8 threads, 2 x 2 outputs each
+constexpr int GBK = 8;        // k-slab
+constexpr int GKB = 8;        // fold interval (k steps)
+
+struct GemmDesc {
+    const double2 *A, *B;
+    double2 *C;
+    int64_t lda, ldb, ldc;
+    int m, n, k;
+    int ta, tb;
+    double2 alpha, beta;
+    int beta_kind;
+    int tiles_m, tiles_n, splitk, klen;
+    int64_t work_begin;   // first work item of this instance
+    int64_t tile_begin;   // first split-tile slot (split instances only)
+};
+
+__device__ __forceinline__ int exp_bound(double x)
+{
+    uint64_t b = (uint64_t)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    if (b == 0) return kNoExp;
+    return (int)(b >> 52) - 1023;
+}
+
+__device__ __forceinline__ double sigma_of(int ea, int eb, int shift)
+{
+    int e = (ea <= kNoExp / 2 || eb <= kNoExp / 2) ? -1000 : ea + eb + shift;
+    e = max(-1000, min(1000, e));
+    return __longlong_as_double((long long)(((uint64_t)(e + 1023) << 52) | (1ull << 51)));
+}
+
+__device__ __forceinline__ double2 opA_at(const GemmDesc &d, int64_t i, int64_t p)
+{
+    return d.ta ? d.A[p + i * d.lda] : d.A[i + p * d.lda];
+}
+__device__ __forceinline__ double2 opB_at(const GemmDesc &d, int64_t p, int64_t j)
+{
+    return d.tb ? d.B[j + p * d.ldb] : d.B[p + j * d.ldb];
+}
+
+__global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__restrict__ descs, int count,
+                                                          int64_t total, unsigned long long *work_counter,
+                                                          int *tile_counters, double2 *partials)
+{
+    __shared__ double2 sA[GBK][GT], sB[GBK][GT];
+    __shared__ int s_ea[GT], s_eb[GT];
+    __shared__ long long s_item;
+    __shared__ int s_last;
+    const int tid = threadIdx.x;
+    const int tx = tid % 8, ty = tid / 8;   // rows tx, tx+8 ; cols ty, ty+8
+    for (;;) {
+        if (tid == 0) s_item = (long long)atomicAdd(work_counter, 1ull);
+        __syncthreads();
+        const long long w = s_item;
+        __syncthreads();
+        if (w >= total) return;
+        // locate the instance (descs sorted by work_begin)
+        int lo = 0, hi = count - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (descs[mid].work_begin <= w) lo = mid;
+            else hi = mid - 1;
+        }
+        const GemmDesc d = descs[lo];
+        const int64_t local = w - d.work_begin;
+        const int split = (int)(local % d.splitk);
+        const int64_t tile = local / d.splitk;
+        const int tm = (int)(tile % d.tiles_m), tn = (int)(tile / d.tiles_m);
+        const int64_t i0 = (int64_t)tm * GT, j0 = (int64_t)tn * GT;
+        const int64_t k0 = (int64_t)split * d.klen, k1 = min((int64_t)d.k, k0 + d.klen);
+
+        // exponent bounds of the tile's rows / columns over [k0, k1)
+        if (tid < GT) {
+            int e = kNoExp;
+            int64_t i = i0 + tid;
+            if (i < d.m)
+                for (int64_t p = k0; p < k1; ++p) e = max(e, exp_bound(opA_at(d, i, p).x));
+            s_ea[tid] = e;
+        } else if (tid < 2 * GT) {
+            int e = kNoExp;
+            int64_t j = j0 + (tid - GT);
+            if (j < d.n)
+                for (int64_t p = k0; p < k1; ++p) e = max(e, exp_bound(opB_at(d, p, j).x));
+            s_eb[tid - GT] = e;
+        }
+        __syncthreads();
+        const int64_t kl = k1 - k0;
+        int terms = (int)(kl < GKB ? kl : GKB);
+        int lg = 0;
+        while ((1 << lg) < terms) ++lg;
+        // sigma binade and second extraction level as in the plain engine
+        // (gemm_plain.cu): shift = lg + 3, X2 for instances with k <= 64.
+        const int shift = lg + 3;
+        const bool comp = d.k <= 64;
+        double X[2][2], X2[2][2], L[2][2], Ah[2][2], Al[2][2];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b) {
+                X[a][b] = sigma_of(s_ea[tx + 8 * a], s_eb[ty + 8 * b], shift);
+                X2[a][b] = sigma_of(s_ea[tx + 8 * a], s_eb[ty + 8 * b], 2 * shift - 54);
+                L[a][b] = Ah[a][b] = Al[a][b] = 0.0;
+            }
+        int since = 0;
+        for (int64_t kk = k0; kk < k1; kk += GBK) {
+            for (int idx = tid; idx < GT * GBK; idx += GTHREADS) {
+                int r = idx % GT, p = idx / GT;
+                int64_t gp = kk + p;
+                double2 va = make_double2(0.0, 0.0), vb = va;
+                if (gp < k1) {
+                    if (i0 + r < d.m) va = opA_at(d, i0 + r, gp);
+                    if (j0 + r < d.n) vb = opB_at(d, gp, j0 + r);
+                }
+                sA[p][r] = va;
+                sB[p][r] = vb;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int p = 0; p < GBK; ++p) {
+                double2 av[2] = {sA[p][tx], sA[p][tx + 8]};
+                double2 bv[2] = {sB[p][ty], sB[p][ty + 8]};
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < 2; ++b) {
+                        double t = __fma_rn(av[a].x, bv[b].x, X[a][b]);
+                        double q = __dsub_rn(X[a][b], t);
+                        double r = __fma_rn(av[a].x, bv[b].x, q);
+                        X[a][b] = t;
+                        if (comp) {
+                            double t2 = __dadd_rn(X2[a][b], r);
+                            double q2 = __dsub_rn(X2[a][b], t2);
+                            r = __dadd_rn(q2, r);
+                            X2[a][b] = t2;
+                        }
+                        double l = __dadd_rn(L[a][b], r);
+                        l = __fma_rn(av[a].x, bv[b].y, l);
+                        L[a][b] = __fma_rn(av[a].y, bv[b].x, l);
+                    }
+            }
+            __syncthreads();
+            since += GBK;
+            if (since == GKB || kk + GBK >= k1) {
+                since = 0;
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < 2; ++b) {
+                        double sg = sigma_of(s_ea[tx + 8 * a], s_eb[ty + 8 * b], shift);
+                        double s = __dsub_rn(X[a][b], sg);
+                        double lsum = L[a][b];
+                        if (comp) {
+                            double sg2 = sigma_of(s_ea[tx + 8 * a], s_eb[ty + 8 * b], 2 * shift - 54);
+                            lsum = __dadd_rn(lsum, __dsub_rn(X2[a][b], sg2));
+                            X2[a][b] = sg2;
+                        }
+                        double h, e;
+                        dd::two_sum(Ah[a][b], s, h, e);
+                        double lo2 = __dadd_rn(Al[a][b], __dadd_rn(e, lsum));
+                        dd::fast_two_sum(h, lo2, Ah[a][b], Al[a][b]);
+                        X[a][b] = sg;
+                        L[a][b] = 0.0;
+                    }
+            }
+        }
+
+        const dd::real alpha = dd::make(d.alpha.x, d.alpha.y), beta = dd::make(d.beta.x, d.beta.y);
+        if (d.splitk > 1) {
+            // write this split's partial tile, then let the last split finish
+            double2 *pt = partials + ((d.tile_begin + tile) * d.splitk + split) * (GT * GT);
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int b = 0; b < 2; ++b) pt[(ty + 8 * b) * GT + tx + 8 * a] = make_double2(Ah[a][b], Al[a][b]);
+            __threadfence();
+            __syncthreads();
+            if (tid == 0) {
+                int old = atomicAdd(&tile_counters[d.tile_begin + tile], 1);
+                s_last = (old == d.splitk - 1);
+            }
+            __syncthreads();
+            if (!s_last) continue;
+            __threadfence();
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int b = 0; b < 2; ++b) {
+                    const double2 *base = partials + (d.tile_begin + tile) * d.splitk * (GT * GT);
+                    // partials written by other CTAs: read through L2
+                    double2 v = __ldcg(base + (ty + 8 * b) * GT + tx + 8 * a);
+                    dd::real acc = dd::make(v.x, v.y);
+                    for (int s2 = 1; s2 < d.splitk; ++s2) {
+                        v = __ldcg(base + (int64_t)s2 * GT * GT + (ty + 8 * b) * GT + tx + 8 * a);
+                        acc = dd::add_fast(acc, dd::make(v.x, v.y));
+                    }
+                    Ah[a][b] = acc.hi;
+                    Al[a][b] = acc.lo;
+                }
+            if (tid == 0) tile_counters[d.tile_begin + tile] = 0;   // ready for the next replay
+        }
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            int64_t j = j0 + ty + 8 * b;
+            if (j >= d.n) continue;
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                int64_t i = i0 + tx + 8 * a;
+                if (i >= d.m) continue;
+                dd::real r = dd::mul_fast(alpha, dd::make(Ah[a][b], Al[a][b]));
+                double2 *pc = d.C + i + j * d.ldc;
+                if (d.beta_kind == 0) {
+                    dd::store(pc, r);
+                } else {
+                    dd::real c0 = dd::load(pc);
+                    if (d.beta_kind == 2) c0 = dd::mul_exact(c0, beta);
+                    dd::store(pc, dd::add_exact(c0, r));
+                }
+            }
+        }
+    }
+}
+
+// ---- grouped TRSM ----------------------------------------------------------------
+
+struct TrsmDesc {
+    const double2 *A;
+    double2 *B;
+    int64_t lda, ldb;
+    int m, n;
+    double2 alpha;
+    int nchunks;          // groups of 32 right-hand sides
+    int64_t work_begin;
+};
+
+__device__ __forceinline__ dd::real dd_recip(dd::real b)
+{
+    // Hida-Li-Bailey accurate division 1 / b
+    double q1 = __ddiv_rn(1.0, b.hi);
+    dd::real r = dd::sub_exact(dd::make(1.0, 0.0), dd::mul_exact(dd::make(q1, 0.0), b));
+    double q2 = __ddiv_rn(r.hi, b.hi);
+    r = dd::sub_exact(r, dd::mul_exact(dd::make(q2, 0.0), b));
+    double q3 = __ddiv_rn(r.hi, b.hi);
+    dd::real q;
+    dd::fast_two_sum(q1, q2, q.hi, q.lo);
+    return dd::add_exact(q, dd::make(q3, 0.0));
+}
+
+// side: 0 left, 1 right; lower: op(A) lower triangular; trans: op = A^T.
+__global__ void __launch_bounds__(128) k_trsm_grouped(const TrsmDesc *__restrict__ descs, int count, int64_t total,
+                                                     int side, int lower, int trans, int unit)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t w = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    if (w >= total) return;
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (descs[mid].work_begin <= w) lo = mid;
+        else hi = mid - 1;
+    }
+    const TrsmDesc d = descs[lo];
+    const int chunk = (int)(w - d.work_begin);
+    const dd::real alpha = dd::make(d.alpha.x, d.alpha.y);
+    const bool alpha1 = (d.alpha.x == 1.0 && d.alpha.y == 0.0);
+#define OPA(i, j) dd::load(trans ? d.A + (j) + (int64_t)(i) * d.lda : d.A + (i) + (int64_t)(j) * d.lda)
+    if (side == 0) {
+        // op(A) X = alpha B, B is m x n; lane handles column chunk*32 + lane
+        const int64_t col = (int64_t)chunk * 32 + lane;
+        if (col >= d.n) return;
+        double2 *b = d.B + col * d.ldb;
+        const int mm = d.m;
+        for (int s = 0; s < mm; ++s) {
+            const int r = lower ? s : mm - 1 - s;
+            dd::real acc = dd::load(b + r);
+            if (!alpha1) acc = dd::mul_fast(acc, alpha);
+            if (lower) {
+                for (int p = 0; p < r; ++p) acc = dd::add_fast(acc, dd::neg(dd::mul_fast(OPA(r, p), dd::load(b + p))));
+            } else {
+                for (int p = r + 1; p < mm; ++p) acc = dd::add_fast(acc, dd::neg(dd::mul_fast(OPA(r, p), dd::load(b + p))));
+            }
+            if (!unit) acc = dd::mul_fast(acc, dd_recip(OPA(r, r)));
+            dd::store(b + r, acc);
+        }
+    } else {
+        // X op(A) = alpha B; lane handles row chunk*32 + lane of B (m x n)
+        const int64_t row = (int64_t)chunk * 32 + lane;
+        if (row >= d.m) return;
+        const int nn = d.n;
+        const bool upper = !lower;
+        for (int s = 0; s < nn; ++s) {
+            const int c = upper ? s : nn - 1 - s;
+            double2 *pb = d.B + row + (int64_t)c * d.ldb;
+            dd::real acc = dd::load(pb);
+            if (!alpha1) acc = dd::mul_fast(acc, alpha);
+            if (upper) {
+                for (int p = 0; p < c; ++p)
+                    acc = dd::add_fast(acc, dd::neg(dd::mul_fast(dd::load(d.B + row + (int64_t)p * d.ldb), OPA(p, c))));
+            } else {
+                for (int p = c + 1; p < nn; ++p)
+                    acc = dd::add_fast(acc, dd::neg(dd::mul_fast(dd::load(d.B + row + (int64_t)p * d.ldb), OPA(p, c))));
+            }
+            if (!unit) acc = dd::mul_fast(acc, dd_recip(OPA(c, c)));
+            dd::store(pb, acc);
+        }
+    }
+#undef OPA
+}
+
+// ---- host: plans, graphs, autotuner ----------------------------------------------
+
+struct Policy {
+    int min_k_per_split = 0;   // 0: never split
+    int max_tiles_split = 4;   // split only instances with at most this many tiles
+};
+
+struct Plan {
+    std::vector<GemmDesc> descs;
+    int64_t total = 0, split_tiles = 0, partial_elems = 0;
+    // device state
+    void *dev = nullptr;
+    size_t dev_bytes = 0;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t key = 0;
+};
+
+std::mutex g_batched_mu;
+std::map<uint64_t, Policy> g_policy_cache;   // shape class -> tuned policy
+Policy g_default_policy{512, 4};
+thread_local Plan t_plan;
+
+uint64_t mix(uint64_t h, uint64_t v)
+{
+    h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+    return h;
+}
+
+// Shape class: count and log-size histogram (the policy depends on shapes, not data).
+uint64_t shape_class(int64_t count, const int64_t *m, const int64_t *n, const int64_t *k)
+{
+    int hist[3][12] = {};
+    for (int64_t i = 0; i < count; ++i) {
+        int64_t v[3] = {m[i], n[i], k[i]};
+        for (int t = 0; t < 3; ++t) {
+            int b = 0;
+            while (b < 11 && ((int64_t)1 << (b + 1)) <= v[t]) ++b;
+            hist[t][b]++;
+        }
+    }
+    uint64_t h = (uint64_t)count;
+    for (int t = 0; t < 3; ++t)
+        for (int b = 0; b < 12; ++b) h = mix(h, (uint64_t)(hist[t][b] * 16 / (count > 0 ? count : 1)));
+    return h;
+}
+
+void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const int64_t *m, const int64_t *n,
+                 const int64_t *k, const mwblas_real64x2 *alpha, const mwblas_real64x2 *const *a, const int64_t *lda,
+                 const mwblas_real64x2 *const *b, const int64_t *ldb, const mwblas_real64x2 *beta,
+                 mwblas_real64x2 *const *c, const int64_t *ldc, const Policy &pol)
+{
+    pl.descs.clear();
+    pl.descs.reserve((size_t)count);
+    int64_t work = 0, stiles = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        if (m[i] <= 0 || n[i] <= 0) continue;
+        GemmDesc d{};
+        d.A = (const double2 *)a[i];
+        d.B = (const double2 *)b[i];
+        d.C = (double2 *)c[i];
+        d.lda = lda[i];
+        d.ldb = ldb[i];
+        d.ldc = ldc[i];
+        d.m = (int)m[i];
+        d.n = (int)n[i];
+        d.k = (int)k[i];
+        char TA = (char)toupper(ta[i]), TB = (char)toupper(tb[i]);
+        d.ta = (TA != 'N');
+        d.tb = (TB != 'N');
+        d.alpha = make_double2(alpha[i].limbs[0], alpha[i].limbs[1]);
+        d.beta = make_double2(beta[i].limbs[0], beta[i].limbs[1]);
+        const bool alpha0 = (d.alpha.x == 0.0 && d.alpha.y == 0.0);
+        d.beta_kind = (d.beta.x == 0.0 && d.beta.y == 0.0) ? 0 : ((d.beta.x == 1.0 && d.beta.y == 0.0) ? 1 : 2);
+        if (alpha0 || d.k == 0) {
+            // only the beta pass: run as a k = 0 product (sigma irrelevant)
+            d.k = 0;
+        }
+        d.tiles_m = (d.m + GT - 1) / GT;
+        d.tiles_n = (d.n + GT - 1) / GT;
+        const int tiles = d.tiles_m * d.tiles_n;
+        d.splitk = 1;
+        if (pol.min_k_per_split > 0 && tiles <= pol.max_tiles_split && d.k >= 2 * pol.min_k_per_split)
+            d.splitk = std::min(16, d.k / pol.min_k_per_split);
+        d.klen = d.splitk > 1 ? ((d.k + d.splitk - 1) / d.splitk + GBK - 1) / GBK * GBK : std::max(d.k, 1);
+        if (d.k == 0) d.klen = 1;
+        d.work_begin = work;
+        d.tile_begin = d.splitk > 1 ? stiles : 0;
+        if (d.splitk > 1) stiles += tiles;
+        work += (int64_t)tiles * d.splitk;
+        pl.descs.push_back(d);
+    }
+    pl.total = work;
+    pl.split_tiles = stiles;
+    int64_t pe = 0;
+    for (auto &d : pl.descs)
+        if (d.splitk > 1) pe += (int64_t)d.tiles_m * d.tiles_n * d.splitk * GT * GT;
+    pl.partial_elems = pe;
+}
+
+uint64_t plan_key(const Plan &pl)
+{
+    // FNV-1a over 64-bit words (GemmDesc is a multiple of 8 bytes)
+    static_assert(sizeof(GemmDesc) % 8 == 0, "descriptor size");
+    uint64_t h = 1469598103934665603ull;
+    const uint64_t *p = (const uint64_t *)pl.descs.data();
+    const size_t nw = pl.descs.size() * sizeof(GemmDesc) / 8;
+    for (size_t i = 0; i < nw; ++i) h = (h ^ p[i]) * 1099511628211ull;
+    return h;
+}
+
+// (Re)creates the device buffers and the graph when the batch layout changed.
+bool prepare_and_launch(Plan &pl, const char *routine)
+{
+    if (pl.descs.empty() || pl.total == 0) return true;
+    const size_t d_bytes = pl.descs.size() * sizeof(GemmDesc);
+    const size_t cnt_bytes = 256 + (size_t)(pl.split_tiles + 1) * sizeof(int);
+    const size_t part_bytes = (size_t)pl.partial_elems * sizeof(double2);
+    const size_t need = d_bytes + cnt_bytes + part_bytes + 512;
+    const uint64_t key = plan_key(pl);
+    cudaStream_t s = stream();
+    if (pl.dev_bytes < need) {
+        if (pl.exec) {
+            cudaGraphExecDestroy(pl.exec);
+            pl.exec = nullptr;
+        }
+        if (pl.dev) cudaFree(pl.dev);
+        pl.dev = nullptr;
+        pl.dev_bytes = 0;
+        if (!cuda_ok(cudaMalloc(&pl.dev, need), routine, "grouped plan buffer")) return false;
+        pl.dev_bytes = need;
+        if (!cuda_ok(cudaMemset(pl.dev, 0, need), routine, "grouped plan clear")) return false;
+    }
+    // layout: [descriptors][work counter (256 B) | tile counters][partials],
+    // each region starting on a 256-byte boundary
+    char *base = (char *)pl.dev;
+    const size_t cnt_off = (d_bytes + 255) / 256 * 256;
+    const size_t part_off = (cnt_off + cnt_bytes + 255) / 256 * 256;
+    GemmDesc *ddesc = (GemmDesc *)base;
+    unsigned long long *counter = (unsigned long long *)(base + cnt_off);
+    int *tile_counters = (int *)(counter + 32);
+    double2 *partials = (double2 *)(base + part_off);
+    const int sms = device_sm_count();
+    const int grid = (int)std::min<int64_t>(pl.total, (int64_t)sms * 16);
+    if (pl.key != key) {
+        // descriptors change only with the batch layout; upload outside the graph
+        if (!cuda_ok(cudaMemcpyAsync(ddesc, pl.descs.data(), d_bytes, cudaMemcpyHostToDevice, s), routine,
+                     "descriptor upload"))
+            return false;
+    }
+    if (!pl.exec || pl.key != key) {
+        if (pl.exec) {
+            cudaGraphExecDestroy(pl.exec);
+            pl.exec = nullptr;
+        }
+        cudaStream_t cap;
+        if (!cuda_ok(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), routine, "capture stream")) return false;
+        cudaGraph_t graph;
+        bool ok = cuda_ok(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), routine, "begin capture");
+        if (ok) {
+            // counters start at zero on every replay
+            cudaMemsetAsync(counter, 0, cnt_bytes, cap);
+            k_gemm_grouped<<<grid, GTHREADS, 0, cap>>>(ddesc, (int)pl.descs.size(), pl.total, counter, tile_counters,
+                                                       partials);
+            ok = cuda_ok(cudaStreamEndCapture(cap, &graph), routine, "end capture");
+        }
+        if (ok) {
+            ok = cuda_ok(cudaGraphInstantiate(&pl.exec, graph, 0), routine, "graph instantiate");
+            cudaGraphDestroy(graph);
+        }
+        cudaStreamDestroy(cap);
+        if (!ok) return false;
+        pl.key = key;
+    }
+    count_launch();
+    return cuda_ok(cudaGraphLaunch(pl.exec, s), routine, "graph launch");
+}
+
+bool grouped_validate(const char *routine, int64_t count, const char *ta, const char *tb, const int64_t *m,
+                      const int64_t *n, const int64_t *k, const mwblas_real64x2 *alpha,
+                      const mwblas_real64x2 *const *a, const int64_t *lda, const mwblas_real64x2 *const *b,
+                      const int64_t *ldb, const mwblas_real64x2 *beta, mwblas_real64x2 *const *c, const int64_t *ldc)
+{
+    if (count < 0) { set_error(routine, 1, "count < 0"); return false; }
+    if (count == 0) return true;
+    if (!ta || !tb || !m || !n || !k || !alpha || !a || !lda || !b || !ldb || !beta || !c || !ldc) {
+        set_error(routine, 2, "null argument array");
+        return false;
+    }
+    for (int64_t i = 0; i < count; ++i) {
+        char TA = (char)toupper(ta[i]), TB = (char)toupper(tb[i]);
+        if (TA != 'N' && TA != 'T' && TA != 'C') { set_error(routine, 2, "invalid transa in instance " + std::to_string(i)); return false; }
+        if (TB != 'N' && TB != 'T' && TB != 'C') { set_error(routine, 3, "invalid transb in instance " + std::to_string(i)); return false; }
+        if (m[i] < 0 || n[i] < 0 || k[i] < 0) { set_error(routine, 4, "negative size in instance " + std::to_string(i)); return false; }
+        if (m[i] > (1 << 30) || n[i] > (1 << 30) || k[i] > (1 << 30)) { set_error(routine, 4, "size too large"); return false; }
+        int64_t nra = (TA == 'N') ? m[i] : k[i], nrb = (TB == 'N') ? k[i] : n[i];
+        if (lda[i] < std::max<int64_t>(1, nra)) { set_error(routine, 9, "lda too small in instance " + std::to_string(i)); return false; }
+        if (ldb[i] < std::max<int64_t>(1, nrb)) { set_error(routine, 11, "ldb too small in instance " + std::to_string(i)); return false; }
+        if (ldc[i] < std::max<int64_t>(1, m[i])) { set_error(routine, 14, "ldc too small in instance " + std::to_string(i)); return false; }
+        if (m[i] > 0 && n[i] > 0 && !is_device_pointer(c[i])) {
+            set_error(routine, 13, "grouped calls take device (or managed) arrays; C of instance " + std::to_string(i));
+            return false;
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+}  // namespace mw
+
+using mw::Plan;
+using mw::Policy;
+
+extern "C" int mgemm_grouped(int64_t count, const char *transa, const char *transb, const int64_t *m,
+                             const int64_t *n, const int64_t *k, const mwblas_real64x2 *alpha,
+                             const mwblas_real64x2 *const *a, const int64_t *lda, const mwblas_real64x2 *const *b,
+                             const int64_t *ldb, const mwblas_real64x2 *beta, mwblas_real64x2 *const *c,
+                             const int64_t *ldc)
+{
+    using namespace mw;
+    const char *routine = "mgemm_grouped";
+    clear_error();
+    if (!grouped_validate(routine, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc))
+        return mwblas_last_error();
+    if (count == 0) return 0;
+    if (!ensure_device(routine)) return mwblas_last_error();
+    Policy pol = g_default_policy;
+    {
+        std::lock_guard<std::mutex> lk(g_batched_mu);
+        auto it = g_policy_cache.find(shape_class(count, m, n, k));
+        if (it != g_policy_cache.end()) pol = it->second;
+    }
+    Plan &pl = t_plan;
+    build_descs(pl, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, pol);
+    if (!prepare_and_launch(pl, routine)) return mwblas_last_error();
+    if (!finish(routine)) return mwblas_last_error();
+    return 0;
+}
+
+// Times the split-K policies on the caller's batch (outputs go to scratch
+// copies of C, the caller's C is not modified) and caches the fastest for
+// batches of the same shape class. Returns 0 and the chosen minimum K per
+// split in *chosen (0 = no split).
+extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char *transb, const int64_t *m,
+                                  const int64_t *n, const int64_t *k, const mwblas_real64x2 *alpha,
+                                  const mwblas_real64x2 *const *a, const int64_t *lda,
+                                  const mwblas_real64x2 *const *b, const int64_t *ldb, const mwblas_real64x2 *beta,
+                                  mwblas_real64x2 *const *c, const int64_t *ldc, int *chosen)
+{
+    using namespace mw;
+    const char *routine = "mgemm_grouped_tune";
+    clear_error();
+    if (!grouped_validate(routine, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc))
+        return mwblas_last_error();
+    if (count == 0) return 0;
+    if (!ensure_device(routine)) return mwblas_last_error();
+    // scratch copies of every C
+    std::vector<int64_t> off((size_t)count);
+    int64_t tot = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        off[(size_t)i] = tot;
+        tot += (m[i] > 0 && n[i] > 0) ? ldc[i] * n[i] : 0;
+    }
+    double2 *scratch = nullptr;
+    if (!cuda_ok(cudaMalloc(&scratch, sizeof(double2) * (size_t)std::max<int64_t>(tot, 1)), routine, "tune scratch"))
+        return mwblas_last_error();
+    std::vector<mwblas_real64x2 *> cs((size_t)count);
+    for (int64_t i = 0; i < count; ++i) {
+        cs[(size_t)i] = (mwblas_real64x2 *)(scratch + off[(size_t)i]);
+        if (m[i] > 0 && n[i] > 0)
+            cudaMemcpyAsync(cs[(size_t)i], c[i], sizeof(double2) * (size_t)(ldc[i] * n[i]), cudaMemcpyDeviceToDevice,
+                            stream());
+    }
+    const int cands[] = {0, 2048, 1024, 512, 256, 128};
+    float best = 1e30f;
+    int best_k = 0;
+    Plan pl;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int cand : cands) {
+        Policy pol{cand, 4};
+        build_descs(pl, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, cs.data(), ldc, pol);
+        if (!prepare_and_launch(pl, routine)) break;   // warm + capture
+        cudaEventRecord(e0, stream());
+        const int reps = 3;
+        for (int r = 0; r < reps; ++r) prepare_and_launch(pl, routine);
+        cudaEventRecord(e1, stream());
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            best_k = cand;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (pl.exec) cudaGraphExecDestroy(pl.exec);
+    if (pl.dev) cudaFree(pl.dev);
+    cudaFree(scratch);
+    {
+        std::lock_guard<std::mutex> lk(g_batched_mu);
+        g_policy_cache[shape_class(count, m, n, k)] = Policy{best_k, 4};
+    }
+    if (chosen) *chosen = best_k;
+    return finish(routine) ? 0 : mwblas_last_error();
+}
+
+extern "C" int mtrsm_grouped(int64_t count, char side, char uplo, char transa, char diag, const int64_t *m,
+                             const int64_t *n, const mwblas_real64x2 *alpha, const mwblas_real64x2 *const *a,
+                             const int64_t *lda, mwblas_real64x2 *const *b, const int64_t *ldb)
+{
+    using namespace mw;
+    const char *routine = "mtrsm_grouped";
+    clear_error();
+    char S = (char)toupper(side), U = (char)toupper(uplo), T = (char)toupper(transa), D = (char)toupper(diag);
+    if (T == 'C') T = 'T';
+    if (count < 0) { set_error(routine, 1, "count < 0"); return 1; }
+    if (S != 'L' && S != 'R') { set_error(routine, 2, "invalid side"); return 2; }
+    if (U != 'U' && U != 'L') { set_error(routine, 3, "invalid uplo"); return 3; }
+    if (T != 'N' && T != 'T') { set_error(routine, 4, "invalid transa"); return 4; }
+    if (D != 'N' && D != 'U') { set_error(routine, 5, "invalid diag"); return 5; }
+    if (count == 0) return 0;
+    if (!m || !n || !alpha || !a || !lda || !b || !ldb) { set_error(routine, 6, "null argument array"); return 6; }
+    std::vector<TrsmDesc> descs;
+    descs.reserve((size_t)count);
+    int64_t work = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        if (m[i] < 0 || n[i] < 0) { set_error(routine, 6, "negative size in instance " + std::to_string(i)); return 6; }
+        if (m[i] == 0 || n[i] == 0) continue;
+        int64_t na = (S == 'L') ? m[i] : n[i];
+        if (lda[i] < std::max<int64_t>(1, na)) { set_error(routine, 10, "lda too small in instance " + std::to_string(i)); return 10; }
+        if (ldb[i] < std::max<int64_t>(1, m[i])) { set_error(routine, 12, "ldb too small in instance " + std::to_string(i)); return 12; }
+        if (!is_device_pointer(b[i])) {
+            set_error(routine, 11, "grouped calls take device (or managed) arrays; B of instance " + std::to_string(i));
+            return 11;
+        }
+        TrsmDesc d{};
+        d.A = (const double2 *)a[i];
+        d.B = (double2 *)b[i];
+        d.lda = lda[i];
+        d.ldb = ldb[i];
+        d.m = (int)m[i];
+        d.n = (int)n[i];
+        d.alpha = make_double2(alpha[i].limbs[0], alpha[i].limbs[1]);
+        const int64_t rhs = (S == 'L') ? n[i] : m[i];
+        d.nchunks = (int)((rhs + 31) / 32);
+        d.work_begin = work;
+        work += d.nchunks;
+        descs.push_back(d);
+    }
+    if (descs.empty()) return 0;
+    if (!ensure_device(routine)) return mwblas_last_error();
+    const size_t bytes = descs.size() * sizeof(TrsmDesc);
+    TrsmDesc *dd_ = (TrsmDesc *)dev_alloc(bytes, routine);
+    if (!dd_) return mwblas_last_error();
+    cudaMemcpyAsync(dd_, descs.data(), bytes, cudaMemcpyHostToDevice, stream());
+    const bool trans = (T != 'N');
+    const bool lower = ((U == 'L') != trans);
+    const int warps = 4;
+    const int64_t blocks = (work + warps - 1) / warps;
+    k_trsm_grouped<<<(unsigned)blocks, warps * 32, 0, stream()>>>(dd_, (int)descs.size(), work, S == 'L' ? 0 : 1,
+                                                                  lower ? 1 : 0, trans ? 1 : 0, D == 'U' ? 1 : 0);
+    count_launch();
+    dev_free(dd_);
+    if (!finish(routine)) return mwblas_last_error();
+    return 0;
+}

@@ -81,16 +81,23 @@ __global__ void k_exp_cols(int64_t rows, int64_t cols, const double2 *M, int64_t
 }
 
 // Exponent offset of sigma above ea + eb: a fold block holds at most
-// min(KB, k) steps of `per_step` products, each below 2^(ea+eb+2); sigma's
-// binade must keep every partial sum below half of 2^E with one more bit of
-// room for the rounding of the extracted high parts.
+// terms = min(KB, k) * per_step products, each below 2^(ea+eb+2), so with
+// 2^lg >= terms and sigma = 1.5 * 2^(ea+eb+lg+3) every partial sum stays below
+// 2^(E-1) and X stays inside (2^E, 2^(E+1)): the fold's X - sigma is exact
+// (Sterbenz) and every extracted remainder is at most ulp(X)/2.
 int sigma_shift(int KB, int64_t k, int per_step)
 {
     int64_t terms = (k < KB ? k : KB) * per_step;
     int lg = 0;
     while (((int64_t)1 << lg) < terms) ++lg;
-    return lg + 4;
+    return lg + 3;
 }
+
+// Products with k at most this use the second extraction level (X2 below):
+// at small k the reference's tolerance, max(10, 4k) * 2^-104 normwise, is
+// tighter than the ~2^(shift-106) * |max product| rounding of the one-level
+// remainder accumulator.
+constexpr int64_t kCompMaxK = 64;
 
 __device__ __forceinline__ double make_sigma(int ea, int eb, int shift)
 {
@@ -104,11 +111,20 @@ __device__ __forceinline__ double make_sigma(int ea, int eb, int shift)
     return __longlong_as_double((long long)bits);
 }
 
+// Second-level sigma for the extracted remainders r (|r| <= 2^(E-53), at most
+// 2^lg = 2^(shift-3) of them per fold): 1.5 * 2^(E - 51 + lg) keeps their
+// running sum inside the binade, so each X2 + r is split exactly (Fast2Sum)
+// and only remainders below ulp(X2)/2 reach L.
+__device__ __forceinline__ double make_sigma2(int ea, int eb, int shift)
+{
+    return make_sigma(ea, eb, 2 * shift - 54);
+}
+
 template <int BM, int BN, int TM, int TN, bool TA, bool TB, int KB>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN))
     k_gemm_plain(int64_t m, int64_t n, int64_t k, dd::real alpha, const double2 *__restrict__ A, int64_t lda,
                  const double2 *__restrict__ B, int64_t ldb, dd::real beta, int beta_kind, double2 *C, int64_t ldc,
-                 const int *__restrict__ ea, const int *__restrict__ eb, int uplo, int SHIFT)
+                 const int *__restrict__ ea, const int *__restrict__ eb, int uplo, int SHIFT, int COMP)
 {
     constexpr int NTX = BM / TM;   // threads along rows
     constexpr int NTY = BN / TN;   // threads along columns
@@ -137,12 +153,13 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
         ebj[b] = (j < n) ? eb[j] : kNoExp;
     }
 
-    double X[TM][TN], L[TM][TN], Ah[TM][TN], Al[TM][TN];
+    double X[TM][TN], X2[TM][TN], L[TM][TN], Ah[TM][TN], Al[TM][TN];
 #pragma unroll
     for (int a = 0; a < TM; ++a)
 #pragma unroll
         for (int b = 0; b < TN; ++b) {
             X[a][b] = make_sigma(eai[a], ebj[b], SHIFT);
+            X2[a][b] = make_sigma2(eai[a], ebj[b], SHIFT);
             L[a][b] = 0.0;
             Ah[a][b] = 0.0;
             Al[a][b] = 0.0;
@@ -186,6 +203,12 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
                     double q = __dsub_rn(X[a][b], t);
                     double r = __fma_rn(av[a].x, bv[b].x, q);
                     X[a][b] = t;
+                    if (COMP) {
+                        double t2 = __dadd_rn(X2[a][b], r);
+                        double q2 = __dsub_rn(X2[a][b], t2);
+                        r = __dadd_rn(q2, r);
+                        X2[a][b] = t2;
+                    }
                     double l = __dadd_rn(L[a][b], r);
                     l = __fma_rn(av[a].x, bv[b].y, l);
                     L[a][b] = __fma_rn(av[a].y, bv[b].x, l);
@@ -202,9 +225,15 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
                 for (int b = 0; b < TN; ++b) {
                     double sg = make_sigma(eai[a], ebj[b], SHIFT);
                     double s = __dsub_rn(X[a][b], sg);   // exact
+                    double lsum = L[a][b];
+                    if (COMP) {
+                        double sg2 = make_sigma2(eai[a], ebj[b], SHIFT);
+                        lsum = __dadd_rn(lsum, __dsub_rn(X2[a][b], sg2));
+                        X2[a][b] = sg2;
+                    }
                     double h, e;
                     dd::two_sum(Ah[a][b], s, h, e);
-                    double lo = __dadd_rn(Al[a][b], __dadd_rn(e, L[a][b]));
+                    double lo = __dadd_rn(Al[a][b], __dadd_rn(e, lsum));
                     dd::fast_two_sum(h, lo, Ah[a][b], Al[a][b]);
                     X[a][b] = sg;
                     L[a][b] = 0.0;
@@ -266,7 +295,7 @@ void dispatch_plain(const GemmArgs &g, const int *ea, const int *eb)
 #define MW_LAUNCH(TA, TB)                                                                                     \
     k_gemm_plain<BM, BN, TM, TN, TA, TB, KB><<<grid, block, 0, stream()>>>(g.m, g.n, g.k, al, A, g.lda, B, g.ldb, \
                                                                           be, g.beta_kind, C, g.ldc, ea, eb, g.uplo, \
-                                                                          sigma_shift(KB, g.k, 1))
+                                                                          sigma_shift(KB, g.k, 1), g.k <= kCompMaxK)
     if (!g.ta && !g.tb) MW_LAUNCH(false, false);
     else if (!g.ta && g.tb) MW_LAUNCH(false, true);
     else if (g.ta && !g.tb) MW_LAUNCH(true, false);
@@ -284,23 +313,36 @@ void dispatch_plain(const GemmArgs &g, const int *ea, const int *eb)
 // negates the imaginary limbs at load, as the reference does at pack time
 // (wgemm_serial.cpp:52-75, :143-157).
 
-__device__ __forceinline__ void xacc(double ah, double al, double bh, double bl, double &X, double &L)
+__device__ __forceinline__ void xacc(double ah, double al, double bh, double bl, double &X, double &X2, double &L,
+                                     int comp)
 {
     double t = __fma_rn(ah, bh, X);
     double q = __dsub_rn(X, t);
     double r = __fma_rn(ah, bh, q);
     X = t;
+    if (comp) {
+        double t2 = __dadd_rn(X2, r);
+        double q2 = __dsub_rn(X2, t2);
+        r = __dadd_rn(q2, r);
+        X2 = t2;
+    }
     double l = __dadd_rn(L, r);
     l = __fma_rn(ah, bl, l);
     L = __fma_rn(al, bh, l);
 }
 
-__device__ __forceinline__ void xfold(double sg, double &X, double &L, double &Ah, double &Al)
+__device__ __forceinline__ void xfold(double sg, double sg2, double &X, double &X2, double &L, double &Ah, double &Al,
+                                      int comp)
 {
     double s = __dsub_rn(X, sg);
+    double lsum = L;
+    if (comp) {
+        lsum = __dadd_rn(lsum, __dsub_rn(X2, sg2));
+        X2 = sg2;
+    }
     double h, e;
     dd::two_sum(Ah, s, h, e);
-    double lo = __dadd_rn(Al, __dadd_rn(e, L));
+    double lo = __dadd_rn(Al, __dadd_rn(e, lsum));
     dd::fast_two_sum(h, lo, Ah, Al);
     X = sg;
     L = 0.0;
@@ -311,7 +353,7 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
     k_gemm_plain_c(int64_t m, int64_t n, int64_t k, dd::cplx alpha, const double2 *__restrict__ A, int64_t lda,
                    const double2 *__restrict__ B, int64_t ldb, dd::cplx beta, int beta_kind, double2 *C,
                    int64_t ldc, const int *__restrict__ ea, const int *__restrict__ eb, int uplo, int herm,
-                   int SHIFT)
+                   int SHIFT, int COMP)
 {
     constexpr int NTX = BM / TM;
     constexpr int NTY = BN / TN;
@@ -338,8 +380,8 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
         ebj[b] = (j < n) ? eb[j] : kNoExp;
     }
 
-    double Xr[TM][TN], Lr[TM][TN], Rh[TM][TN], Rl[TM][TN];
-    double Xi[TM][TN], Li[TM][TN], Ih[TM][TN], Il[TM][TN];
+    double Xr[TM][TN], Lr[TM][TN], Rh[TM][TN], Rl[TM][TN], Xr2[TM][TN];
+    double Xi[TM][TN], Li[TM][TN], Ih[TM][TN], Il[TM][TN], Xi2[TM][TN];
 #pragma unroll
     for (int a = 0; a < TM; ++a)
 #pragma unroll
@@ -347,6 +389,7 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
             double sg = make_sigma(eai[a], ebj[b], SHIFT);
             Xr[a][b] = sg; Lr[a][b] = 0.0; Rh[a][b] = 0.0; Rl[a][b] = 0.0;
             Xi[a][b] = sg; Li[a][b] = 0.0; Ih[a][b] = 0.0; Il[a][b] = 0.0;
+            Xr2[a][b] = Xi2[a][b] = make_sigma2(eai[a], ebj[b], SHIFT);
         }
 
     int since_fold = 0;
@@ -394,10 +437,10 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
             for (int a = 0; a < TM; ++a)
 #pragma unroll
                 for (int b = 0; b < TN; ++b) {
-                    xacc(ar[a].x, ar[a].y, br[b].x, br[b].y, Xr[a][b], Lr[a][b]);
-                    xacc(-ai[a].x, -ai[a].y, bi[b].x, bi[b].y, Xr[a][b], Lr[a][b]);
-                    xacc(ar[a].x, ar[a].y, bi[b].x, bi[b].y, Xi[a][b], Li[a][b]);
-                    xacc(ai[a].x, ai[a].y, br[b].x, br[b].y, Xi[a][b], Li[a][b]);
+                    xacc(ar[a].x, ar[a].y, br[b].x, br[b].y, Xr[a][b], Xr2[a][b], Lr[a][b], COMP);
+                    xacc(-ai[a].x, -ai[a].y, bi[b].x, bi[b].y, Xr[a][b], Xr2[a][b], Lr[a][b], COMP);
+                    xacc(ar[a].x, ar[a].y, bi[b].x, bi[b].y, Xi[a][b], Xi2[a][b], Li[a][b], COMP);
+                    xacc(ai[a].x, ai[a].y, br[b].x, br[b].y, Xi[a][b], Xi2[a][b], Li[a][b], COMP);
                 }
         }
         __syncthreads();
@@ -410,8 +453,9 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 #pragma unroll
                 for (int b = 0; b < TN; ++b) {
                     double sg = make_sigma(eai[a], ebj[b], SHIFT);
-                    xfold(sg, Xr[a][b], Lr[a][b], Rh[a][b], Rl[a][b]);
-                    xfold(sg, Xi[a][b], Li[a][b], Ih[a][b], Il[a][b]);
+                    double sg2 = make_sigma2(eai[a], ebj[b], SHIFT);
+                    xfold(sg, sg2, Xr[a][b], Xr2[a][b], Lr[a][b], Rh[a][b], Rl[a][b], COMP);
+                    xfold(sg, sg2, Xi[a][b], Xi2[a][b], Li[a][b], Ih[a][b], Il[a][b], COMP);
                 }
         }
     }
@@ -481,7 +525,7 @@ void launch_plain_c(const GemmArgs &g, const int *ea, const int *eb)
     be.im = dd::make(g.cbeta.im.hi, g.cbeta.im.lo);
     k_gemm_plain_c<BM, BN, TM, TN, TA, TB, CA, CB, KB><<<grid, block, 0, stream()>>>(
         g.m, g.n, g.k, al, (const double2 *)g.A, g.lda, (const double2 *)g.B, g.ldb, be, g.beta_kind,
-        (double2 *)g.C, g.ldc, ea, eb, g.uplo, g.herm ? 1 : 0, sigma_shift(KB, g.k, 2));
+        (double2 *)g.C, g.ldc, ea, eb, g.uplo, g.herm ? 1 : 0, sigma_shift(KB, g.k, 2), g.k <= kCompMaxK);
     count_launch();
 }
 

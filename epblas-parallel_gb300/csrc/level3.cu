@@ -6,16 +6,15 @@
 // blocks with a diagonal kernel plus a serial GEMM trailing update are a CPU
 // cache strategy; on the GPU the triangle is a single grid.
 //
-// TRSM (mtrsm_parallel.cpp:36-101, mtrsm_serial.cpp:738-822): blocked
-// substitution. B is prescaled by alpha, then for each diagonal block of nb
-// rows (side 'L') or columns (side 'R'), in the order the triangle dictates:
-//   1. a diagonal-block kernel solves the block in double-double, one thread
-//      per right-hand side, multiplying by the double-double reciprocal of
-//      the diagonal (the reference's `inv = one_dd / A(k,k)`,
-//      mtrsm_serial.cpp:144) with the fast multiply;
-//   2. the rest of B is updated with one GEMM (alpha = -1, beta = 1) through
-//      the engine dispatch, so large solves run their O(m^2 n) work on the
-//      same GEMM engines as mgemm_.
+// TRSM (mtrsm_parallel.cpp:36-101, mtrsm_serial.cpp:738-822): B is prescaled
+// by alpha, then the triangle is split in halves recursively: solve one half,
+// update the other half of B with one GEMM (alpha = -1, beta = 1) through the
+// engine dispatch, solve the other half. Blocks of at most 64 rows/columns are
+// solved by substitution in double-double, one thread per right-hand side,
+// multiplying by the double-double reciprocal of the diagonal (the reference's
+// `inv = one_dd / A(k,k)`, mtrsm_serial.cpp:144). The O(m^2 n) update work
+// thus lands in a few large GEMMs (half the triangle at the top level), which
+// is the shape the tensor-core engine needs.
 #include "dd.cuh"
 #include "level3.h"
 #include "runtime.h"
@@ -47,7 +46,8 @@ __device__ __forceinline__ dd::real opA(const double2 *A, int64_t lda, bool tran
 
 // Side 'L': solve op(A)[blk,blk] * X = B[blk, :] in place for a block of nb
 // rows starting at r0. lower: op(A) is lower triangular (forward order).
-// Thread per right-hand-side column.
+// Thread per right-hand-side column; four partial sums break the dependency
+// chain of the dot product.
 __global__ void k_trsm_diag_left(int64_t r0, int nb, int64_t ncols, const double2 *A, int64_t lda, bool trans,
                                  bool lower, bool unit, double2 *B, int64_t ldb)
 {
@@ -57,22 +57,24 @@ __global__ void k_trsm_diag_left(int64_t r0, int nb, int64_t ncols, const double
     for (int s = 0; s < nb; ++s) {
         int r = lower ? s : nb - 1 - s;
         int64_t gr = r0 + r;
-        dd::real acc = dd::load(b + gr);
-        if (lower) {
-            for (int p = 0; p < r; ++p)
-                acc = dd::add_fast(acc, dd::neg(dd::mul_fast(opA(A, lda, trans, gr, r0 + p), dd::load(b + r0 + p))));
-        } else {
-            for (int p = r + 1; p < nb; ++p)
-                acc = dd::add_fast(acc, dd::neg(dd::mul_fast(opA(A, lda, trans, gr, r0 + p), dd::load(b + r0 + p))));
+        int p0 = lower ? 0 : r + 1, p1 = lower ? r : nb;
+        dd::real acc[4] = {dd::load(b + gr), dd::make(0.0, 0.0), dd::make(0.0, 0.0), dd::make(0.0, 0.0)};
+        int p = p0;
+        for (; p + 4 <= p1; p += 4) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                acc[u] = dd::add_fast(acc[u], dd::neg(dd::mul_fast(opA(A, lda, trans, gr, r0 + p + u), dd::load(b + r0 + p + u))));
         }
-        if (!unit) acc = dd::mul_fast(acc, dd_div(dd::make(1.0, 0.0), opA(A, lda, trans, gr, gr)));
-        dd::store(b + gr, acc);
+        for (; p < p1; ++p) acc[0] = dd::add_fast(acc[0], dd::neg(dd::mul_fast(opA(A, lda, trans, gr, r0 + p), dd::load(b + r0 + p))));
+        dd::real v = dd::add_fast(dd::add_fast(acc[0], acc[1]), dd::add_fast(acc[2], acc[3]));
+        if (!unit) v = dd::mul_fast(v, dd_div(dd::make(1.0, 0.0), opA(A, lda, trans, gr, gr)));
+        dd::store(b + gr, v);
     }
 }
 
 // Side 'R': solve X * op(A)[blk,blk] = B[:, blk] for a block of nb columns
 // starting at c0. upper: op(A) is upper triangular (columns in forward order).
-// Thread per row of B.
+// Thread per row of B, four partial sums per dot product.
 __global__ void k_trsm_diag_right(int64_t c0, int nb, int64_t nrows, const double2 *A, int64_t lda, bool trans,
                                   bool upper, bool unit, double2 *B, int64_t ldb)
 {
@@ -81,18 +83,20 @@ __global__ void k_trsm_diag_right(int64_t c0, int nb, int64_t nrows, const doubl
     for (int s = 0; s < nb; ++s) {
         int c = upper ? s : nb - 1 - s;
         int64_t gc = c0 + c;
-        dd::real acc = dd::load(B + row + gc * ldb);
-        if (upper) {
-            for (int p = 0; p < c; ++p)
-                acc = dd::add_fast(acc,
-                                   dd::neg(dd::mul_fast(dd::load(B + row + (c0 + p) * ldb), opA(A, lda, trans, c0 + p, gc))));
-        } else {
-            for (int p = c + 1; p < nb; ++p)
-                acc = dd::add_fast(acc,
-                                   dd::neg(dd::mul_fast(dd::load(B + row + (c0 + p) * ldb), opA(A, lda, trans, c0 + p, gc))));
+        int p0 = upper ? 0 : c + 1, p1 = upper ? c : nb;
+        dd::real acc[4] = {dd::load(B + row + gc * ldb), dd::make(0.0, 0.0), dd::make(0.0, 0.0), dd::make(0.0, 0.0)};
+        int p = p0;
+        for (; p + 4 <= p1; p += 4) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                acc[u] = dd::add_fast(acc[u], dd::neg(dd::mul_fast(dd::load(B + row + (c0 + p + u) * ldb),
+                                                                     opA(A, lda, trans, c0 + p + u, gc))));
         }
-        if (!unit) acc = dd::mul_fast(acc, dd_div(dd::make(1.0, 0.0), opA(A, lda, trans, gc, gc)));
-        dd::store(B + row + gc * ldb, acc);
+        for (; p < p1; ++p)
+            acc[0] = dd::add_fast(acc[0], dd::neg(dd::mul_fast(dd::load(B + row + (c0 + p) * ldb), opA(A, lda, trans, c0 + p, gc))));
+        dd::real v = dd::add_fast(dd::add_fast(acc[0], acc[1]), dd::add_fast(acc[2], acc[3]));
+        if (!unit) v = dd::mul_fast(v, dd_div(dd::make(1.0, 0.0), opA(A, lda, trans, gc, gc)));
+        dd::store(B + row + gc * ldb, v);
     }
 }
 
@@ -156,6 +160,90 @@ bool syrk_device(bool cplx, bool herm, int uplo, bool trans, int64_t n, int64_t 
     return run_gemm(g, cplx, -1, routine);
 }
 
+namespace {
+
+constexpr int64_t kTrsmLeaf = 64;
+
+// B[:, :] -= op(A)-block * X (side L) or X * op(A)-block (side R) through the
+// engine dispatch.
+bool trsm_update(bool left, int64_t m, int64_t n, int64_t k, const void *Ablk, int64_t lda, bool ta,
+                 const void *X, int64_t ldx, void *C, int64_t ldc, const char *routine)
+{
+    GemmArgs g;
+    g.alpha = dd_host{-1.0, 0.0};
+    g.beta = dd_host{1.0, 0.0};
+    g.beta_kind = 1;
+    g.m = m;
+    g.n = n;
+    g.k = k;
+    g.C = C;
+    g.ldc = ldc;
+    if (left) {
+        g.A = Ablk; g.lda = lda; g.ta = ta;
+        g.B = X; g.ldb = ldx; g.tb = false;
+    } else {
+        g.A = X; g.lda = ldx; g.ta = false;
+        g.B = Ablk; g.ldb = lda; g.tb = ta;
+    }
+    return run_gemm(g, false, -1, routine);
+}
+
+// Recursive substitution on the na x na triangle of op(A) starting at (o, o).
+// Side L: B is na x nrhs (rows o..o+na of the caller's B). Side R: B is
+// nrhs x na (columns o..o+na). lower refers to op(A).
+bool trsm_rec(bool left, bool lower, bool trans, bool unit, int64_t o, int64_t na, int64_t nrhs, const void *A,
+              int64_t lda, double2 *B, int64_t ldb, const char *routine)
+{
+    if (na <= kTrsmLeaf) {
+        if (left)
+            k_trsm_diag_left<<<blocks_for(nrhs, 64), 64, 0, stream()>>>(o, (int)na, nrhs, (const double2 *)A, lda,
+                                                                      trans, lower, unit, B, ldb);
+        else
+            k_trsm_diag_right<<<blocks_for(nrhs, 64), 64, 0, stream()>>>(o, (int)na, nrhs, (const double2 *)A, lda,
+                                                                       trans, !lower, unit, B, ldb);
+        count_launch();
+        return true;
+    }
+    int64_t h = (na / 2 + kTrsmLeaf - 1) / kTrsmLeaf * kTrsmLeaf;
+    if (h >= na) h = na - kTrsmLeaf;
+    const int64_t o1 = o, n1 = h, o2 = o + h, n2 = na - h;
+    if (left) {
+        // rows of B: first block B1 = rows o1.., second B2 = rows o2..
+        if (lower) {
+            if (!trsm_rec(true, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, routine)) return false;
+            // B2 -= op(A)[o2:, o1:o1+n1] * X1
+            if (!trsm_update(true, n2, nrhs, n1, op_block(A, lda, trans, o2, o1), lda, trans, B + o1, ldb, B + o2,
+                             ldb, routine))
+                return false;
+            return trsm_rec(true, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, routine);
+        }
+        if (!trsm_rec(true, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, routine)) return false;
+        // B1 -= op(A)[o1:o1+n1, o2:] * X2
+        if (!trsm_update(true, n1, nrhs, n2, op_block(A, lda, trans, o1, o2), lda, trans, B + o2, ldb, B + o1, ldb,
+                         routine))
+            return false;
+        return trsm_rec(true, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, routine);
+    }
+    // side R: columns of B; op(A) upper -> left block first
+    const bool upper = !lower;
+    if (upper) {
+        if (!trsm_rec(false, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, routine)) return false;
+        // B2 -= X1 * op(A)[o1:o1+n1, o2:]
+        if (!trsm_update(false, nrhs, n2, n1, op_block(A, lda, trans, o1, o2), lda, trans, B + o1 * ldb, ldb,
+                         B + o2 * ldb, ldb, routine))
+            return false;
+        return trsm_rec(false, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, routine);
+    }
+    if (!trsm_rec(false, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, routine)) return false;
+    // B1 -= X2 * op(A)[o2:, o1:o1+n1]
+    if (!trsm_update(false, nrhs, n1, n2, op_block(A, lda, trans, o2, o1), lda, trans, B + o2 * ldb, ldb,
+                     B + o1 * ldb, ldb, routine))
+        return false;
+    return trsm_rec(false, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, routine);
+}
+
+}  // namespace
+
 bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_t n, dd_host alpha, const void *A,
                  int64_t lda, void *B, int64_t ldb, const char *routine)
 {
@@ -168,66 +256,8 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
         k_scale_fast<<<blocks_for(m * n, 256), 256, 0, stream()>>>(m, n, dd::make(alpha.hi, alpha.lo), b, ldb);
         count_launch();
     }
-    const int64_t nb = 64;
-    GemmArgs g;
-    g.alpha = dd_host{-1.0, 0.0};
-    g.beta = dd_host{1.0, 0.0};
-    g.beta_kind = 1;
-    if (side == 'L') {
-        int64_t nblk = (m + nb - 1) / nb;
-        for (int64_t s = 0; s < nblk; ++s) {
-            int64_t blk = lower ? s : nblk - 1 - s;
-            int64_t r0 = blk * nb, rb = (m - r0 < nb) ? m - r0 : nb;
-            k_trsm_diag_left<<<blocks_for(n, 128), 128, 0, stream()>>>(r0, (int)rb, n, (const double2 *)A, lda, trans,
-                                                                     lower, unit, b, ldb);
-            count_launch();
-            // trailing rows: lower -> rows below the block, upper -> rows above
-            int64_t t0 = lower ? r0 + rb : 0;
-            int64_t tr = lower ? m - (r0 + rb) : r0;
-            if (tr <= 0) continue;
-            g.m = tr;
-            g.n = n;
-            g.k = rb;
-            g.A = op_block(A, lda, trans, t0, r0);
-            g.lda = lda;
-            g.ta = trans;
-            g.B = b + r0;
-            g.ldb = ldb;
-            g.tb = false;
-            g.C = b + t0;
-            g.ldc = ldb;
-            if (!run_gemm(g, false, -1, routine)) return false;
-        }
-    } else {
-        // X * op(A) = B: op(A) upper -> columns solved left to right.
-        bool upper = !lower;
-        int64_t nblk = (n + nb - 1) / nb;
-        for (int64_t s = 0; s < nblk; ++s) {
-            int64_t blk = upper ? s : nblk - 1 - s;
-            int64_t c0 = blk * nb, cb = (n - c0 < nb) ? n - c0 : nb;
-            k_trsm_diag_right<<<blocks_for(m, 128), 128, 0, stream()>>>(c0, (int)cb, m, (const double2 *)A, lda, trans,
-                                                                      upper, unit, b, ldb);
-            count_launch();
-            // remaining columns: upper -> right of the block, lower -> left
-            int64_t t0 = upper ? c0 + cb : 0;
-            int64_t tc = upper ? n - (c0 + cb) : c0;
-            if (tc <= 0) continue;
-            // B[:, T] -= X[:, blk] * op(A)[blk, T]
-            g.m = m;
-            g.n = tc;
-            g.k = cb;
-            g.A = b + c0 * ldb;
-            g.lda = ldb;
-            g.ta = false;
-            g.B = op_block(A, lda, trans, c0, t0);
-            g.ldb = lda;
-            g.tb = trans;
-            g.C = b + t0 * ldb;
-            g.ldc = ldb;
-            if (!run_gemm(g, false, -1, routine)) return false;
-        }
-    }
-    return true;
+    if (side == 'L') return trsm_rec(true, lower, trans, unit, 0, m, n, A, lda, b, ldb, routine);
+    return trsm_rec(false, lower, trans, unit, 0, n, m, A, lda, b, ldb, routine);
 }
 
 void launch_zero_matrix(int64_t m, int64_t n, void *B, int64_t ldb)

@@ -691,8 +691,19 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, co
         if (ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
             CrtAcc acc;
             acc.reset();
+            // residues of all moduli: issue the loads of 8 planes at a time
+            // so that their latencies overlap
             const uint16_t *rp = R + j * Mp + i;
-            for (int l = 0; l < nmod; ++l) acc.add(sm, l, rp[(int64_t)l * Np * Mp]);
+            const int64_t plane = Np * Mp;
+            int l = 0;
+            for (; l + 8 <= nmod; l += 8) {
+                uint32_t c[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) c[u] = __ldcs(rp + (int64_t)(l + u) * plane);
+#pragma unroll
+                for (int u = 0; u < 8; ++u) acc.add(sm, l + u, c[u]);
+            }
+            for (; l < nmod; ++l) acc.add(sm, l, __ldcs(rp + (int64_t)l * plane));
             v = acc.finish(sm, (bits - 2 - ea[i]) + (bits - 2 - eb[j]));
         }
         if (!alpha_one) v = xf_mul(xa, v);
@@ -740,10 +751,8 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, 
             CrtAcc accr, acci;
             accr.reset();
             acci.reset();
-            for (int l = 0; l < nmod; ++l) {
-                const int64_t o = ((int64_t)l * Np + j) * Mp + i;
+            auto add_l = [&](int l, int p1, int p2, int p3) {
                 const int p = (int)sm.pm[l];
-                const int p1 = R[o], p2 = R[cstride + o], p3 = R[2 * cstride + o];
                 int re = p1 - p2;
                 if (re < 0) re += p;
                 int im = p3 - p1 - p2;
@@ -751,6 +760,22 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, 
                 if (im < 0) im += p;
                 accr.add(sm, l, (uint32_t)re);
                 acci.add(sm, l, (uint32_t)im);
+            };
+            const uint16_t *rp = R + j * Mp + i;
+            const int64_t plane = Np * Mp;
+            int l = 0;
+            for (; l + 4 <= nmod; l += 4) {
+                int c[4][3];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                    for (int z = 0; z < 3; ++z) c[u][z] = __ldcs(rp + z * cstride + (int64_t)(l + u) * plane);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) add_l(l + u, c[u][0], c[u][1], c[u][2]);
+            }
+            for (; l < nmod; ++l) {
+                const uint16_t *q = rp + (int64_t)l * plane;
+                add_l(l, __ldcs(q), __ldcs(q + cstride), __ldcs(q + 2 * cstride));
             }
             const int S2 = (bits - 2 - ea[i]) + (bits - 2 - eb[j]);
             vr = accr.finish(sm, S2);

@@ -126,12 +126,10 @@ class MWBlas:
             self._sig("mwblas_launch_count", _i64, [])
             self._sig("mwblas_version", _ch, [])
             self._sig("mgemv_n_noalloc", _i32, [_i64, _i64, R, _p, _i64, _p, _i64, R, _p, _i64, _p])
-            if hasattr(L, "mgemm_grouped"):
-                self._sig("mgemm_grouped", _i32,
-                          [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p])
-            if hasattr(L, "mtrsm_grouped"):
-                self._sig("mtrsm_grouped", _i32,
-                          [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p])
+            self._sig("mgemm_grouped", _i32, [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p])
+            self._sig("mgemm_grouped_tune", _i32, [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p])
+            self._sig("mtrsm_grouped", _i32, [_i64, C.c_char, C.c_char, C.c_char, C.c_char, _p, _p, _p, _p, _p,
+                                              _p, _p])
 
     def _sig(self, name, res, args):
         f = getattr(self.lib, name, None)
@@ -184,6 +182,37 @@ class MWBlas:
         f = self.lib.mtrsm_64_ if wide else self.lib.mtrsm_
         f(side.encode(), uplo.encode(), transa.encode(), diag.encode(), I(m), I(n), C.byref(real(alpha)), _ptr(a),
           I(lda), _ptr(b), I(ldb))
+
+    # ---- batched (extension) -----------------------------------------------------------
+    @staticmethod
+    def _grouped_arrays(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+        cnt = len(m)
+        arr = lambda v: np.ascontiguousarray(np.asarray(v, dtype=np.int64))
+        ptrs = lambda v: np.ascontiguousarray(np.asarray([_ptr(x) for x in v], dtype=np.uint64))
+        scal = lambda v: np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(cnt, 2))
+        return [cnt, np.frombuffer("".join(ta).encode(), dtype=np.uint8).copy(),
+                np.frombuffer("".join(tb).encode(), dtype=np.uint8).copy(), arr(m), arr(n), arr(k), scal(alpha),
+                ptrs(a), arr(lda), ptrs(b), arr(ldb), scal(beta), ptrs(c), arr(ldc)]
+
+    def mgemm_grouped(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+        """Lists of per-instance flags/sizes/scalars; a, b, c: device pointers."""
+        args = self._grouped_arrays(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc)
+        return int(self.lib.mgemm_grouped(args[0], *[x.ctypes.data for x in args[1:]]))
+
+    def mgemm_grouped_tune(self, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc):
+        args = self._grouped_arrays(ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc)
+        chosen = C.c_int(-1)
+        rc = int(self.lib.mgemm_grouped_tune(args[0], *[x.ctypes.data for x in args[1:]], C.addressof(chosen)))
+        return rc, chosen.value
+
+    def mtrsm_grouped(self, side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb):
+        cnt = len(m)
+        arr = lambda v: np.ascontiguousarray(np.asarray(v, dtype=np.int64))
+        ptrs = lambda v: np.ascontiguousarray(np.asarray([_ptr(x) for x in v], dtype=np.uint64))
+        al = np.ascontiguousarray(np.asarray(alpha, dtype=np.float64).reshape(cnt, 2))
+        keep = [arr(m), arr(n), al, ptrs(a), arr(lda), ptrs(b), arr(ldb)]
+        return int(self.lib.mtrsm_grouped(cnt, side.encode(), uplo.encode(), transa.encode(), diag.encode(),
+                                          *[x.ctypes.data for x in keep]))
 
     # ---- level 2 -----------------------------------------------------------------------
     def mgemv(self, trans, m, n, alpha, a, lda, x, incx, beta, y, incy, wide=True):

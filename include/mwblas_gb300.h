@@ -197,6 +197,30 @@ void mgemm_ozaki_64_(const char *transa, const char *transb, const int64_t *m,
                      const int64_t *ldb, const MWBLAS_R *beta, MWBLAS_R *c,
                      const int64_t *ldc);
 
+/* Batched uneven double-double GEMM (no reference counterpart): for
+ * i < count, C[i] := alpha[i]*op(A[i])*op(B[i]) + beta[i]*C[i], with per-instance
+ * flags transa[i]/transb[i], sizes and leading dimensions. The matrix pointers
+ * must be device (or managed) memory; the per-instance arrays are host arrays.
+ * One persistent kernel runs every instance, launched from a CUDA graph that is
+ * reused while the batch layout is unchanged. Returns 0 or an error code. */
+int mgemm_grouped(int64_t count, const char *transa, const char *transb, const int64_t *m, const int64_t *n,
+                  const int64_t *k, const MWBLAS_R *alpha, const MWBLAS_R *const *a, const int64_t *lda,
+                  const MWBLAS_R *const *b, const int64_t *ldb, const MWBLAS_R *beta, MWBLAS_R *const *c,
+                  const int64_t *ldc);
+/* Autotuner for mgemm_grouped: times the split-K policies on this batch
+ * (results go to scratch copies; C is not modified) and keeps the fastest for
+ * batches of the same shape class. *chosen = minimum K per split (0 = none). */
+int mgemm_grouped_tune(int64_t count, const char *transa, const char *transb, const int64_t *m,
+                       const int64_t *n, const int64_t *k, const MWBLAS_R *alpha, const MWBLAS_R *const *a,
+                       const int64_t *lda, const MWBLAS_R *const *b, const int64_t *ldb, const MWBLAS_R *beta,
+                       MWBLAS_R *const *c, const int64_t *ldc, int *chosen);
+/* Batched triangular solves with shared flags and per-instance sizes: for
+ * i < count, op(A[i]) X = alpha[i] B[i] (side 'L') or X op(A[i]) = alpha[i] B[i]
+ * ('R'); B[i] is overwritten. Device (or managed) matrix pointers. */
+int mtrsm_grouped(int64_t count, char side, char uplo, char transa, char diag, const int64_t *m,
+                  const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *const *a, const int64_t *lda,
+                  MWBLAS_R *const *b, const int64_t *ldb);
+
 /* Ozaki scheme controls.  bits = significant bits kept per scaled operand
  * row/column (0 = automatic from the operands' exponent range); the number
  * of moduli (integer GEMMs) follows from bits and k.  Returns the previous

@@ -9,6 +9,7 @@ from __future__ import annotations
 import importlib.util
 import json
 import os
+import zlib
 import sys
 
 import numpy as np
@@ -81,7 +82,7 @@ def gpu(lib):
 
 @pytest.fixture
 def rng(request):
-    seed = abs(hash(request.node.name)) % (2 ** 31)
+    seed = zlib.crc32(request.node.name.encode())   # stable across processes
     return np.random.default_rng(seed)
 
 

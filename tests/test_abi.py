@@ -37,7 +37,7 @@ def test_lp64_and_ilp64_twins_exported(libpath):
 
 
 def test_reference_symbol_set_covered(libpath):
-    """Every hot-path symbol of the reference's mwblas is exported (SURVEY 8b list)."""
+    """Every hot-path symbol of the reference's mwblas is exported (common/epblas_facade.h pairs)."""
     lib = C.CDLL(libpath)
     for s in ("mgemm_ mgemm_64_ wgemm_ wgemm_64_ msyrk_ msyrk_64_ wherk_ wherk_64_ mtrsm_ mtrsm_64_ mgemv_ "
               "mgemv_64_ mdot_ mdot_64_ maxpy_ maxpy_64_ mscal_ mscal_64_ mcopy_ mcopy_64_ mswap_ mswap_64_ "

@@ -1,0 +1,150 @@
+"""Batched uneven GEMM / TRSM (extensions without a reference counterpart).
+
+Each instance is checked against the binary128 oracle with the same
+tolerances as the single-instance routines; graph replays must reproduce the
+first call bit for bit; the split-K autotuner must leave C untouched and its
+choice must give correct results.
+"""
+import numpy as np
+import pytest
+
+from conftest import mwb, orc
+
+pytestmark = pytest.mark.gpu
+
+
+class DeviceArena:
+    """Places numpy DD arrays in one device buffer and hands out pointers."""
+
+    def __init__(self, arrays):
+        import torch
+        self.offsets, tot = [], 0
+        for a in arrays:
+            self.offsets.append(tot)
+            tot += a.size
+        host = np.zeros(max(tot, 2))
+        for a, o in zip(arrays, self.offsets):
+            host[o:o + a.size] = a.reshape(-1)
+        self.buf = torch.from_numpy(host).cuda()
+        self.shapes = [a.shape for a in arrays]
+
+    def ptr(self, i):
+        return self.buf.data_ptr() + 8 * self.offsets[i]
+
+    def get(self, i):
+        o = self.offsets[i]
+        n = int(np.prod(self.shapes[i]))
+        return self.buf[o:o + n].cpu().numpy().reshape(self.shapes[i])
+
+
+def make_batch(rng, count, maxdim=200, big_k=None):
+    inst = []
+    for t in range(count):
+        m, n, k = (int(x) for x in np.exp(rng.uniform(np.log(1), np.log(maxdim), 3)).round())
+        if t == 3:
+            m = 0
+        if t == 5:
+            k = 0
+        if big_k and t % 7 == 0:
+            m, n, k = 12, 20, big_k
+        ta, tb = rng.choice(["N", "T", "C"]), rng.choice(["N", "T"])
+        lda = (m if ta == "N" else k) + int(rng.integers(0, 3))
+        ldb = (k if tb == "N" else n) + int(rng.integers(0, 3))
+        ldc = m + int(rng.integers(0, 3))
+        A = mwb.dd_matrix(rng, m if ta == "N" else k, k if ta == "N" else m, max(lda, 1))
+        B = mwb.dd_matrix(rng, k if tb == "N" else n, n if tb == "N" else k, max(ldb, 1))
+        Cm = mwb.dd_matrix(rng, m, n, max(ldc, 1))
+        al = mwb.random_dd(rng, ()) if t != 9 else np.zeros(2)
+        be = mwb.random_dd(rng, ()) if t % 3 else np.zeros(2)
+        inst.append(dict(m=m, n=n, k=k, ta=str(ta), tb=str(tb), lda=max(lda, 1), ldb=max(ldb, 1), ldc=max(ldc, 1),
+                         A=A, B=B, C=Cm, alpha=al, beta=be))
+    return inst
+
+
+def run_grouped(gpu, inst, tune=False):
+    arena = DeviceArena([x for d in inst for x in (d["A"], d["B"], d["C"])])
+    args = dict(ta=[d["ta"] for d in inst], tb=[d["tb"] for d in inst], m=[d["m"] for d in inst],
+                n=[d["n"] for d in inst], k=[d["k"] for d in inst], alpha=[d["alpha"] for d in inst],
+                a=[arena.ptr(3 * i) for i in range(len(inst))], lda=[d["lda"] for d in inst],
+                b=[arena.ptr(3 * i + 1) for i in range(len(inst))], ldb=[d["ldb"] for d in inst],
+                beta=[d["beta"] for d in inst], c=[arena.ptr(3 * i + 2) for i in range(len(inst))],
+                ldc=[d["ldc"] for d in inst])
+    chosen = None
+    if tune:
+        rc, chosen = gpu.mgemm_grouped_tune(**args)
+        assert rc == 0, gpu.last_error()
+        for i, d in enumerate(inst):     # tuning must not touch C
+            np.testing.assert_array_equal(arena.get(3 * i + 2), d["C"])
+    rc = gpu.mgemm_grouped(**args)
+    assert rc == 0, gpu.last_error()
+    return arena, args, chosen
+
+
+def check(oracle, inst, arena):
+    for i, d in enumerate(inst):
+        got = arena.get(3 * i + 2)
+        m, n, k = d["m"], d["n"], d["k"]
+        if m == 0 or n == 0:
+            continue
+        want = oracle.qgemm(d["ta"], d["tb"], m, n, k, d["alpha"], d["A"], d["lda"], d["B"], d["ldb"], d["beta"],
+                            d["C"].copy(), d["ldc"])
+        opn = orc.dd_abs(d["alpha"]) * max(k, 1) * orc.dd_absmax(d["A"]) * orc.dd_absmax(d["B"]) \
+            + orc.dd_abs(d["beta"]) * orc.dd_absmax(d["C"])
+        err = orc.normwise_error(got[:, :m], want[:, :m], opn)
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (i, m, n, k, err)
+        if d["ldc"] > m:
+            np.testing.assert_array_equal(got[:, m:], d["C"][:, m:])
+
+
+def test_grouped_gemm_matches_oracle_and_replays(gpu, oracle, rng):
+    inst = make_batch(rng, 60)
+    arena, args, _ = run_grouped(gpu, inst)
+    check(oracle, inst, arena)
+    first = [arena.get(3 * i + 2) for i in range(len(inst))]
+    # replay the cached graph on reset inputs: bit-identical
+    for i, d in enumerate(inst):
+        o = arena.offsets[3 * i + 2]
+        import torch
+        arena.buf[o:o + d["C"].size] = torch.from_numpy(d["C"].reshape(-1)).cuda()
+    assert gpu.mgemm_grouped(**args) == 0
+    for i in range(len(inst)):
+        np.testing.assert_array_equal(arena.get(3 * i + 2), first[i])
+
+
+def test_grouped_gemm_split_k_and_tuner(gpu, oracle, rng):
+    inst = make_batch(rng, 30, maxdim=120, big_k=3000)
+    arena, args, chosen = run_grouped(gpu, inst, tune=True)
+    assert chosen in (0, 2048, 1024, 512, 256, 128)
+    check(oracle, inst, arena)
+
+
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("uplo,trans", [("L", "N"), ("U", "N"), ("L", "T"), ("U", "T")])
+@pytest.mark.parametrize("diag", ["N", "U"])
+def test_grouped_trsm(gpu, oracle, rng, side, uplo, trans, diag):
+    import torch
+    inst = []
+    for t in range(12):
+        na = int(np.exp(rng.uniform(np.log(2), np.log(120))))
+        nrhs = int(rng.integers(1, 70))
+        m, n = (na, nrhs) if side == "L" else (nrhs, na)
+        lda, ldb = na + int(rng.integers(0, 2)), m + int(rng.integers(0, 2))
+        A = mwb.dd_matrix(rng, na, na, lda)
+        A[..., 0] /= na
+        A[..., 1] /= na
+        for d in range(na):
+            A[d, d] = (1.0 + rng.random(), 0.0)
+        B = mwb.dd_matrix(rng, m, n, ldb)
+        inst.append(dict(m=m, n=n, na=na, lda=lda, ldb=ldb, A=A, B=B, alpha=mwb.random_dd(rng, ())))
+    arena = DeviceArena([x for d in inst for x in (d["A"], d["B"])])
+    rc = gpu.mtrsm_grouped(side, uplo, trans, diag, [d["m"] for d in inst], [d["n"] for d in inst],
+                           [d["alpha"] for d in inst], [arena.ptr(2 * i) for i in range(len(inst))],
+                           [d["lda"] for d in inst], [arena.ptr(2 * i + 1) for i in range(len(inst))],
+                           [d["ldb"] for d in inst])
+    assert rc == 0, gpu.last_error()
+    for i, d in enumerate(inst):
+        want = d["B"].copy()
+        oracle.qtrsm(side, uplo, trans, diag, d["m"], d["n"], d["alpha"], d["A"], d["lda"], want, d["ldb"])
+        got = arena.get(2 * i + 1)
+        err = orc.normwise_error(got[:, :d["m"]], want[:, :d["m"]], orc.dd_abs(d["alpha"]) * orc.dd_absmax(d["B"]))
+        assert err <= max(20, 8 * d["na"] ** 2) * orc.EPS_DD, (i, err)
