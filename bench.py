@@ -420,7 +420,8 @@ def tc_traffic_from_profile():
 # workloads, each printed as one JSON line of the same shape as the headline.
 # ---------------------------------------------------------------------------
 
-WORKLOADS = ("gemm", "stress", "syrk", "herk", "trsm", "gemv", "dot", "axpy", "batched_gemm", "batched_trsm")
+WORKLOADS = ("gemm", "stress", "wgemm", "gemm_t", "syrk", "herk", "trsm", "gemv", "dot", "axpy", "batched_gemm",
+             "batched_trsm")
 
 
 def _dev_dd(torch, shape, gen, dev, cplx_=False):
@@ -509,6 +510,42 @@ def run_workload(args):
             check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
             # componentwise view: error relative to |alpha| sum_p |a_ip||b_pj| of the sampled entries
             check["samples"] = 256
+    elif w in ("wgemm", "gemm_t"):
+        # complex GEMM at 4096^3 NN, or the real GEMM at n^3 with both operands transposed
+        cx = w == "wgemm"
+        n = 4096 if cx else args.n
+        A = _dev_dd(torch, (n, n), gen, dev, cplx_=cx)
+        B = _dev_dd(torch, (n, n), gen, dev, cplx_=cx)
+        C = _dev_dd(torch, (n, n), gen, dev, cplx_=cx)
+        C0 = C.clone()
+        ca = np.array([al, be])            # complex alpha = al + i*be
+        cb = np.array([be, al])
+        if cx:
+            fn = lambda: lib.wgemm("N", "N", n, n, n, ca, A.data_ptr(), n, B.data_ptr(), n, cb, C.data_ptr(), n)
+            value_flops = 8.0 * n ** 3
+            metric = "complex DD-GEMM GFLOP/s n=4096 NN (8n^3 real flops)"
+            cfg = {"workload": "wgemm_ 4096^3 NN, complex double-double alpha/beta"}
+        else:
+            fn = lambda: lib.mgemm("T", "T", n, n, n, al, A.data_ptr(), n, B.data_ptr(), n, be, C.data_ptr(), n)
+            value_flops = 2.0 * n ** 3
+            metric = f"DD-GEMM GFLOP/s n={n} TT"
+            cfg = {"workload": f"mgemm_ {n}^3 TT"}
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: C.copy_(C0))
+        value, unit = value_flops / ms / 1e6, "DD-GFLOP/s"
+        if o:
+            C.copy_(C0)
+            fn()
+            rows, cols = rng.integers(0, n, 128), rng.integers(0, n, 128)
+            hA, hB, hC0 = hb(A), hb(B), hb(C0)
+            if cx:
+                want = o.qwgemm("N", "N", n, n, n, ca, hA, n, hB, n, cb, hC0, n, rows=rows, cols=cols)
+                op = (orc.dd_abs(al) + orc.dd_abs(be)) * 2 * n * orc.dd_absmax(hA) * orc.dd_absmax(hB) \
+                    + 2 * (orc.dd_abs(al) + orc.dd_abs(be)) * orc.dd_absmax(hC0)
+            else:
+                want = o.qgemm("T", "T", n, n, n, al, hA, n, hB, n, be, hC0, n, rows=rows, cols=cols)
+                op = orc.dd_abs(al) * n * orc.dd_absmax(hA) * orc.dd_absmax(hB) + orc.dd_abs(be) * orc.dd_absmax(hC0)
+            got = hb(C)[cols, rows]
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
     elif w == "syrk":
         n, k = 8192, 2048
         A = _dev_dd(torch, (k, n), gen, dev)          # n x k, lda = n

@@ -53,7 +53,9 @@ struct GemmDesc {
     int beta_kind;
     int tiles_m, tiles_n, splitk, klen;
     int64_t work_begin;   // first work item of this instance
-    int64_t tile_begin;   // first split-tile slot (split instances only)
+    int64_t tile_begin;   // first tile counter (split instances only)
+    int64_t part_begin;   // first partial-tile slot: earlier split instances
+                          // hold tiles * splitk slots each
 };
 
 __device__ __forceinline__ int exp_bound(double x)
@@ -208,7 +210,7 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__res
         const dd::real alpha = dd::make(d.alpha.x, d.alpha.y), beta = dd::make(d.beta.x, d.beta.y);
         if (d.splitk > 1) {
             // write this split's partial tile, then let the last split finish
-            double2 *pt = partials + ((d.tile_begin + tile) * d.splitk + split) * (GT * GT);
+            double2 *pt = partials + (d.part_begin + tile * d.splitk + split) * (GT * GT);
 #pragma unroll
             for (int a = 0; a < 2; ++a)
 #pragma unroll
@@ -226,7 +228,7 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__res
             for (int a = 0; a < 2; ++a)
 #pragma unroll
                 for (int b = 0; b < 2; ++b) {
-                    const double2 *base = partials + (d.tile_begin + tile) * d.splitk * (GT * GT);
+                    const double2 *base = partials + (d.part_begin + tile * d.splitk) * (GT * GT);
                     // partials written by other CTAs: read through L2
                     double2 v = __ldcg(base + (ty + 8 * b) * GT + tx + 8 * a);
                     dd::real acc = dd::make(v.x, v.y);
@@ -400,7 +402,7 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
 {
     pl.descs.clear();
     pl.descs.reserve((size_t)count);
-    int64_t work = 0, stiles = 0;
+    int64_t work = 0, stiles = 0, pslots = 0;
     for (int64_t i = 0; i < count; ++i) {
         if (m[i] <= 0 || n[i] <= 0) continue;
         GemmDesc d{};
@@ -434,16 +436,17 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
         if (d.k == 0) d.klen = 1;
         d.work_begin = work;
         d.tile_begin = d.splitk > 1 ? stiles : 0;
-        if (d.splitk > 1) stiles += tiles;
+        d.part_begin = d.splitk > 1 ? pslots : 0;
+        if (d.splitk > 1) {
+            stiles += tiles;
+            pslots += (int64_t)tiles * d.splitk;
+        }
         work += (int64_t)tiles * d.splitk;
         pl.descs.push_back(d);
     }
     pl.total = work;
     pl.split_tiles = stiles;
-    int64_t pe = 0;
-    for (auto &d : pl.descs)
-        if (d.splitk > 1) pe += (int64_t)d.tiles_m * d.tiles_n * d.splitk * GT * GT;
-    pl.partial_elems = pe;
+    pl.partial_elems = pslots * GT * GT;
 }
 
 uint64_t plan_key(const Plan &pl)

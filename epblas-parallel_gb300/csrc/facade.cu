@@ -53,6 +53,7 @@ int engine()
         if (e) {
             if (!strcmp(e, "plain")) g_engine = MWBLAS_GEMM_PLAIN;
             else if (!strcmp(e, "ozaki")) g_engine = MWBLAS_GEMM_OZAKI;
+            else if (!strcmp(e, "fixed")) g_engine = MWBLAS_GEMM_FIXED;
         }
     }
     return g_engine;
@@ -83,11 +84,14 @@ bool run_gemm(GemmArgs &g, bool cplx, int force_engine, const char *routine)
     int eng = force_engine >= 0 ? force_engine : engine();
     if (eng == MWBLAS_GEMM_AUTO) {
         // The tensor-core scheme wins once the k-dimension and the output tile
-        // count amortise its operand conversion.
+        // count amortise its operand conversion; below that, real products run
+        // on the integer pipes and complex ones on the FP64 pipe.
         double work = (double)g.m * (double)g.n * (double)g.k;
-        eng = (work >= 64.0 * 64.0 * 64.0 * 8.0 && g.k >= 32) ? MWBLAS_GEMM_OZAKI : MWBLAS_GEMM_PLAIN;
-        if (!ozaki_available()) eng = MWBLAS_GEMM_PLAIN;
+        eng = (work >= 64.0 * 64.0 * 64.0 * 8.0 && g.k >= 32) ? MWBLAS_GEMM_OZAKI : MWBLAS_GEMM_FIXED;
+        if (eng == MWBLAS_GEMM_OZAKI && !ozaki_available()) eng = MWBLAS_GEMM_FIXED;
+        if (eng == MWBLAS_GEMM_FIXED && cplx) eng = MWBLAS_GEMM_PLAIN;
     }
+    if (eng == MWBLAS_GEMM_FIXED && !cplx) return gemm_fixed_real(g, routine);
     if (eng == MWBLAS_GEMM_OZAKI) {
         if (!ozaki_available()) {
             set_error(routine, MWBLAS_ERR_UNSUPPORTED, "tensor-core engine unavailable on this device");
@@ -525,6 +529,14 @@ void mgemm_plain_64_(const char *ta, const char *tb, const int64_t *m, const int
                             c, ldc);
 }
 
+void mgemm_fixed_64_(const char *ta, const char *tb, const int64_t *m, const int64_t *n, const int64_t *k,
+                     const TR *alpha, const TR *a, const int64_t *lda, const TR *b, const int64_t *ldb,
+                     const TR *beta, TR *c, const int64_t *ldc)
+{
+    mw::gemm_entry<int64_t>("mgemm_fixed", false, MWBLAS_GEMM_FIXED, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta,
+                            c, ldc);
+}
+
 void mgemm_ozaki_64_(const char *ta, const char *tb, const int64_t *m, const int64_t *n, const int64_t *k,
                      const TR *alpha, const TR *a, const int64_t *lda, const TR *b, const int64_t *ldb,
                      const TR *beta, TR *c, const int64_t *ldc)
@@ -536,7 +548,7 @@ void mgemm_ozaki_64_(const char *ta, const char *tb, const int64_t *m, const int
 int mwblas_set_gemm_engine(int engine)
 {
     int prev = mw::engine();
-    if (engine >= MWBLAS_GEMM_AUTO && engine <= MWBLAS_GEMM_OZAKI) mw::g_engine = engine;
+    if (engine >= MWBLAS_GEMM_AUTO && engine <= MWBLAS_GEMM_FIXED) mw::g_engine = engine;
     return prev;
 }
 int mwblas_get_gemm_engine(void) { return mw::engine(); }

@@ -28,6 +28,9 @@ struct GemmArgs {
 bool gemm_plain_real(const GemmArgs &g, const char *routine);
 bool gemm_plain_cplx(const GemmArgs &g, const char *routine);
 
+// Fixed-point engine on the integer pipes (real only).
+bool gemm_fixed_real(const GemmArgs &g, const char *routine);
+
 // Integer-exact tensor-core engine (Ozaki scheme II). Returns false with an
 // error recorded on failure.
 bool gemm_ozaki_real(const GemmArgs &g, int bits, const char *routine);

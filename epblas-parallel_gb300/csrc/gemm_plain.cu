@@ -57,6 +57,7 @@ __global__ void k_exp_rows(int64_t rows, int64_t cols, const double2 *M, int64_t
     int64_t j0 = blockIdx.y * cols_per_y;
     int64_t j1 = min(cols, j0 + cols_per_y);
     int e = kNoExp;
+#pragma unroll 8
     for (int64_t j = j0; j < j1; ++j) {
         const double2 *p = M + elem2 * (i + j * ld);
         for (int w = 0; w < elem2; ++w) e = max(e, exp_bound(p[w].x));
@@ -551,9 +552,13 @@ void launch_exp_rows_of_op(const void *X, int64_t rows_x, int64_t cols_x, int64_
 {
     if (!trans) {
         // rows of X: thread per row, column range split over grid.y
-        int64_t per_y = 256;
+        // enough (rows, column-range) blocks to cover the GPU a few times
+        const int64_t rb = (rows_x + 255) / 256;
+        int64_t want_y = (4 * (int64_t)device_sm_count() + rb - 1) / rb;
+        int64_t per_y = (cols_x + want_y - 1) / want_y;
+        if (per_y < 16) per_y = 16;
         if ((cols_x + per_y - 1) / per_y > 65535) per_y = (cols_x + 65534) / 65535;
-        dim3 grid((unsigned)((rows_x + 255) / 256), (unsigned)((cols_x + per_y - 1) / per_y));
+        dim3 grid((unsigned)rb, (unsigned)((cols_x + per_y - 1) / per_y));
         cudaMemsetAsync(out, 0x80, sizeof(int) * rows_x, stream());
         k_exp_rows<<<grid, 256, 0, stream()>>>(rows_x, cols_x, (const double2 *)X, ld, elem2, out, per_y);
     } else {

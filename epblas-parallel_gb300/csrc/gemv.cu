@@ -8,11 +8,20 @@
 // kernel folds them in a fixed order and applies y += alpha*s.
 // Trans: block per column (A's columns are contiguous), warp-shuffle and
 // shared-memory reduction, then y_j += alpha*s (mgemv.cpp:229-233).
-// Products accumulate as TwoProduct + TwoSum into a (sum, error) pair,
-// renormalised every 32 terms, the lo*lo product dropped as in mdot.cpp:60-64.
+// mgemv_ accumulates the products in per-thread integer fixed point
+// (fixacc.cuh): x is first converted once to 128-bit extended floats (it is
+// small and stays in L2), each A(i,j) * x(j) is formed to 2^-126 and added
+// exactly; partial sums combine as extended floats in a fixed order, and
+// y := y + alpha*s is rounded once to double-double. The FP64 pipe, which
+// would bound a double-double multiply-add at a fraction of HBM speed, is
+// not used in the loop.
+// mgemv_n_noalloc keeps the FP64 accumulation (TwoProduct + TwoSum into a
+// (sum, error) pair, renormalised every 32 terms, the lo*lo product dropped as
+// in mdot.cpp:60-64) so that its partial sums fit its fixed scratch array.
 #include <mutex>
 
 #include "dd.cuh"
+#include "fixacc.cuh"
 #include "level3.h"
 #include "runtime.h"
 
@@ -76,37 +85,111 @@ __global__ void k_gemv_n_final(int64_t m, int nchunks, const double2 *part, dd::
     }
 }
 
-__global__ void k_gemv_t(int64_t m, int64_t n, const double2 *A, int64_t lda, const double2 *x, int64_t incx,
-                         dd::real alpha, double2 *y, int64_t incy)
+// ---- fixed-point kernels (mgemv_) ------------------------------------------------------
+
+__global__ void k_xf_convert(int64_t n, const double2 *x, int64_t incx, fx::XFPod *out)
 {
-    __shared__ double2 sh[32];
-    int64_t j = blockIdx.x;
-    const double2 *col = A + j * lda;
-    double s = 0.0, e = 0.0;
-    int cnt = 0;
-    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
-        acc_prod(s, e, col[i], x[vidx(i, m, incx)]);
-        if (++cnt == 32) {
-            dd::fast_two_sum(s, e, s, e);
-            cnt = 0;
-        }
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const double2 v = x[vidx(j, n, incx)];
+        const bool ok = fx::finite_dd(v);
+        xfp::XF f = ok ? xfp::xf_from_dd(v.x, v.y) : xfp::XF{0, 0, false, true};
+        if (ok && v.x == 0.0) f.zero = true;
+        out[j] = fx::to_pod(f, !ok);
     }
-    dd::real v;
-    dd::two_sum(s, e, v.hi, v.lo);
-    for (int off = 16; off > 0; off >>= 1)
-        v = dd::add_fast(v, dd::make(__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)));
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) sh[wid] = make_double2(v.hi, v.lo);
+}
+
+// NoTrans partial sums: row per thread, columns [j0, j1) of chunk blockIdx.y.
+__global__ void __launch_bounds__(256) k_gemv_n_fx(int64_t m, int64_t n, const double2 *__restrict__ A, int64_t lda,
+                                                  const fx::XFPod *__restrict__ xf, int64_t chunk,
+                                                  fx::XFPod *__restrict__ part)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const int64_t j0 = blockIdx.y * chunk, j1 = min(n, j0 + chunk);
+    fx::Acc acc;
+    acc.reset();
+    const double2 *a = A + i;
+    int64_t j = j0;
+    for (; j + 2 <= j1; j += 2) {
+        const double2 a0 = __ldcs(a + j * lda), a1 = __ldcs(a + (j + 1) * lda);
+        const fx::XFPod p0 = xf[j], p1 = xf[j + 1];
+        if (!fx::finite_dd(a0) || !fx::finite_dd(a1) || ((p0.flags | p1.flags) & 4)) acc.bad = true;
+        if (a0.x != 0.0 && !(p0.flags & 2)) acc.add(xfp::xf_mul(xfp::xf_from_dd(a0.x, a0.y), fx::from_pod(p0)));
+        if (a1.x != 0.0 && !(p1.flags & 2)) acc.add(xfp::xf_mul(xfp::xf_from_dd(a1.x, a1.y), fx::from_pod(p1)));
+    }
+    for (; j < j1; ++j) {
+        const double2 a0 = a[j * lda];
+        const fx::XFPod p0 = xf[j];
+        if (!fx::finite_dd(a0) || (p0.flags & 4)) acc.bad = true;
+        if (a0.x != 0.0 && !(p0.flags & 2)) acc.add(xfp::xf_mul(xfp::xf_from_dd(a0.x, a0.y), fx::from_pod(p0)));
+    }
+    part[blockIdx.y * m + i] = fx::to_pod(acc.bad ? xfp::XF{0, 0, false, true} : acc.finish(), acc.bad);
+}
+
+// y(i) := y(i) + alpha * sum_c part(c, i), one rounding to double-double.
+__device__ __forceinline__ void fx_update_y(double2 *py, const xfp::XF &xa, xfp::XF s, bool bad)
+{
+    const double2 y0 = *py;
+    if (bad) {
+        *py = make_double2(__longlong_as_double(0x7ff8000000000000ll), __longlong_as_double(0x7ff8000000000000ll));
+        return;
+    }
+    xfp::XF t = xfp::xf_mul(xa, s);
+    if (!fx::finite_dd(y0)) {
+        double h, l;
+        xfp::xf_to_dd(t, h, l);
+        dd::store(py, dd::add_exact(dd::make(y0.x, y0.y), dd::make(h, l)));
+        return;
+    }
+    t = xfp::xf_add(xfp::xf_from_dd(y0.x, y0.y), t);
+    double h, l;
+    xfp::xf_to_dd(t, h, l);
+    *py = make_double2(h, l);
+}
+
+__global__ void k_gemv_n_fx_final(int64_t m, int nchunks, const fx::XFPod *part, dd::real alpha, double2 *y,
+                                  int64_t incy)
+{
+    const xfp::XF xa = xfp::xf_from_dd(alpha.hi, alpha.lo);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        xfp::XF s;
+        s.zero = true; s.neg = false; s.m = 0; s.e = 0;
+        bool bad = false;
+        for (int c = 0; c < nchunks; ++c) {
+            const fx::XFPod p = part[(int64_t)c * m + i];
+            bad |= (p.flags & 4) != 0;
+            s = xfp::xf_add(s, fx::from_pod(p));
+        }
+        fx_update_y(y + vidx(i, m, incy), xa, s, bad);
+    }
+}
+
+// Trans: block per column j of A (contiguous), threads over rows.
+__global__ void __launch_bounds__(256) k_gemv_t_fx(int64_t m, int64_t n, const double2 *__restrict__ A, int64_t lda,
+                                                  const fx::XFPod *__restrict__ xf, dd::real alpha, double2 *y,
+                                                  int64_t incy)
+{
+    __shared__ fx::XFPod sh[8];
+    const int64_t j = blockIdx.x;
+    const double2 *col = A + j * lda;
+    fx::Acc acc;
+    acc.reset();
+    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const double2 a0 = __ldcs(col + i);
+        const fx::XFPod p0 = xf[i];
+        if (!fx::finite_dd(a0) || (p0.flags & 4)) acc.bad = true;
+        if (a0.x != 0.0 && !(p0.flags & 2)) acc.add(xfp::xf_mul(xfp::xf_from_dd(a0.x, a0.y), fx::from_pod(p0)));
+    }
+    const bool bad = __syncthreads_or(acc.bad ? 1 : 0) != 0;
+    xfp::XF v = fx::xf_warp_sum(acc.bad ? xfp::XF{0, 0, false, true} : acc.finish());
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = fx::to_pod(v, false);
     __syncthreads();
     if (wid == 0) {
-        v = (lane < (int)(blockDim.x >> 5)) ? dd::load(&sh[lane]) : dd::make(0.0, 0.0);
-        for (int off = 16; off > 0; off >>= 1)
-            v = dd::add_fast(v,
-                             dd::make(__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)));
-        if (lane == 0) {
-            double2 *py = y + vidx(j, n, incy);
-            dd::store(py, dd::add_exact(dd::load(py), dd::mul_exact(alpha, v)));
-        }
+        if (lane < (int)(blockDim.x >> 5)) v = fx::from_pod(sh[lane]);
+        else { v.zero = true; v.neg = false; v.m = 0; v.e = 0; }
+        v = fx::xf_warp_sum(v);
+        if (lane == 0) fx_update_y(y + vidx(j, n, incy), xfp::xf_from_dd(alpha.hi, alpha.lo), v, bad);
     }
 }
 
@@ -126,29 +209,40 @@ bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A,
     }
     if (alpha.hi == 0.0 && alpha.lo == 0.0) return true;
     dd::real al = dd::make(alpha.hi, alpha.lo);
+    const int64_t lenx = trans ? m : n;
+    // x as extended floats (lenx * 24 bytes), then the partial sums
+    const size_t xf_bytes = ((size_t)lenx * sizeof(fx::XFPod) + 255) / 256 * 256;
     if (!trans) {
         int64_t rowblocks = (m + 255) / 256;
-        int64_t want = 4 * (int64_t)sms;
+        int64_t want = 8 * (int64_t)sms;
         int64_t nchunks = (want + rowblocks - 1) / rowblocks;
         if (nchunks > n) nchunks = n;
         if (nchunks > 4096) nchunks = 4096;
         if (nchunks < 1) nchunks = 1;
         int64_t chunk = (n + nchunks - 1) / nchunks;
         nchunks = (n + chunk - 1) / chunk;
-        double2 *part = (double2 *)dev_alloc(sizeof(double2) * (size_t)(nchunks * m), routine);
-        if (!part) return false;
+        char *buf = (char *)dev_alloc(xf_bytes + sizeof(fx::XFPod) * (size_t)(nchunks * m), routine);
+        if (!buf) return false;
+        fx::XFPod *xf = (fx::XFPod *)buf, *part = (fx::XFPod *)(buf + xf_bytes);
+        int64_t cb = (n + 255) / 256;
+        if (cb > sms * 8) cb = sms * 8;
+        k_xf_convert<<<(unsigned)cb, 256, 0, stream()>>>(n, (const double2 *)x, incx, xf);
         dim3 grid((unsigned)rowblocks, (unsigned)nchunks);
-        k_gemv_n_partial<<<grid, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, (const double2 *)x, incx, chunk,
-                                                     part);
+        k_gemv_n_fx<<<grid, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, xf, chunk, part);
         int64_t fb = (m + 255) / 256;
         if (fb > sms * 8) fb = sms * 8;
-        k_gemv_n_final<<<(unsigned)fb, 256, 0, stream()>>>(m, (int)nchunks, part, al, (double2 *)y, incy);
-        count_launch(2);
-        dev_free(part);
+        k_gemv_n_fx_final<<<(unsigned)fb, 256, 0, stream()>>>(m, (int)nchunks, part, al, (double2 *)y, incy);
+        count_launch(3);
+        dev_free(buf);
     } else {
-        k_gemv_t<<<(unsigned)n, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, (const double2 *)x, incx, al,
-                                                    (double2 *)y, incy);
-        count_launch();
+        fx::XFPod *xf = (fx::XFPod *)dev_alloc(xf_bytes, routine);
+        if (!xf) return false;
+        int64_t cb = (m + 255) / 256;
+        if (cb > sms * 8) cb = sms * 8;
+        k_xf_convert<<<(unsigned)cb, 256, 0, stream()>>>(m, (const double2 *)x, incx, xf);
+        k_gemv_t_fx<<<(unsigned)n, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, xf, al, (double2 *)y, incy);
+        count_launch(2);
+        dev_free(xf);
     }
     return true;
 }

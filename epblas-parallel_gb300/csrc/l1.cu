@@ -14,6 +14,7 @@
 // (the same element is updated n times in order); those calls run a
 // single-thread kernel that repeats the loop literally.
 #include "dd.cuh"
+#include "fixacc.cuh"
 #include "l1.h"
 #include "runtime.h"
 
@@ -305,62 +306,83 @@ __global__ void k_iamax_final(int nparts, const AmaxKey *part, int64_t *out)
 }
 
 // ---- DOT ---------------------------------------------------------------------
-// Per-thread double-double accumulation (TwoProduct + TwoSum, the lo x lo
-// product dropped as in mdot.cpp:60-64), renormalised every 32 elements; block
-// and grid partials combine with the fast DD add in a fixed order, so the
-// result is deterministic for a given n and device.
+// mdot.cpp:48-87 accumulates TwoProduct + Bailey three-limb sums on the FP64
+// pipe. Here the products are accumulated exactly (to 2^-126 of each product)
+// in per-thread integer fixed point (fixacc.cuh), the thread sums are added
+// as 128-bit extended floats in a fixed order (warp, block, then the grid's
+// block partials), and the result is rounded once to double-double. The
+// result is deterministic for a given n and device and at least as accurate
+// as the reference's.
 
-__device__ __forceinline__ dd::real dd_shfl(dd::real v, int off)
+__device__ fx::XF xf_block_sum(fx::XF v)
 {
-    return dd::make(__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off));
-}
-
-__device__ dd::real dd_block_sum(dd::real v)
-{
-    __shared__ double2 sh[kThreads / 32];
-    for (int off = 16; off > 0; off >>= 1) v = dd::add_fast(v, dd_shfl(v, off));
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) sh[wid] = make_double2(v.hi, v.lo);
+    __shared__ fx::XFPod sh[kThreads / 32];
+    v = fx::xf_warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = fx::to_pod(v, false);
     __syncthreads();
     if (wid == 0) {
-        v = (lane < (int)(blockDim.x >> 5)) ? dd::load(&sh[lane]) : dd::make(0.0, 0.0);
-        for (int off = 16; off > 0; off >>= 1) v = dd::add_fast(v, dd_shfl(v, off));
+        if (lane < (int)(blockDim.x >> 5)) {
+            v = fx::from_pod(sh[lane]);
+        } else {
+            v.zero = true; v.neg = false; v.m = 0; v.e = 0;
+        }
+        v = fx::xf_warp_sum(v);
     }
     return v;
 }
 
-__global__ void k_mdot_partial(int64_t n, const double2 *x, int64_t incx, const double2 *y, int64_t incy,
-                               double2 *part)
+__device__ bool block_any(bool b)
 {
-    double s = 0.0, e = 0.0;
-    int cnt = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        double2 xv = x[vidx(i, n, incx)];
-        double2 yv = y[vidx(i, n, incy)];
-        double p, pe, t;
-        dd::two_prod(xv.x, yv.x, p, pe);
-        e = __fma_rn(xv.x, yv.y, e);
-        e = __fma_rn(xv.y, yv.x, e);
-        e = __dadd_rn(e, pe);
-        dd::two_sum(s, p, s, t);
-        e = __dadd_rn(e, t);
-        if (++cnt == 32) {
-            dd::fast_two_sum(s, e, s, e);
-            cnt = 0;
-        }
-    }
-    dd::real acc;
-    dd::two_sum(s, e, acc.hi, acc.lo);
-    acc = dd_block_sum(acc);
-    if (threadIdx.x == 0) part[blockIdx.x] = make_double2(acc.hi, acc.lo);
+    return __syncthreads_or(b ? 1 : 0) != 0;
 }
 
-__global__ void k_mdot_final(int nparts, const double2 *part, double2 *out)
+__global__ void __launch_bounds__(kThreads) k_mdot_partial(int64_t n, const double2 *__restrict__ x, int64_t incx,
+                                                          const double2 *__restrict__ y, int64_t incy,
+                                                          fx::XFPod *part)
 {
-    dd::real acc = dd::make(0.0, 0.0);
-    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc = dd::add_fast(acc, dd::load(part + i));
-    acc = dd_block_sum(acc);
-    if (threadIdx.x == 0) *out = make_double2(acc.hi, acc.lo);
+    fx::Acc acc;
+    acc.reset();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (incx == 1 && incy == 1) {
+        // two elements in flight per thread
+        for (; i + stride < n; i += 2 * stride) {
+            const double2 x0 = __ldcs(x + i), y0 = __ldcs(y + i);
+            const double2 x1 = __ldcs(x + i + stride), y1 = __ldcs(y + i + stride);
+            if (!fx::finite_dd(x0) || !fx::finite_dd(y0) || !fx::finite_dd(x1) || !fx::finite_dd(y1)) acc.bad = true;
+            acc.add_dd_product(x0.x, x0.y, y0.x, y0.y);
+            acc.add_dd_product(x1.x, x1.y, y1.x, y1.y);
+        }
+    }
+    for (; i < n; i += stride) {
+        const double2 xv = x[vidx(i, n, incx)], yv = y[vidx(i, n, incy)];
+        if (!fx::finite_dd(xv) || !fx::finite_dd(yv)) acc.bad = true;
+        acc.add_dd_product(xv.x, xv.y, yv.x, yv.y);
+    }
+    const bool bad = block_any(acc.bad);
+    fx::XF v = xf_block_sum(acc.bad ? fx::XF{0, 0, false, true} : acc.finish());
+    if (threadIdx.x == 0) part[blockIdx.x] = fx::to_pod(v, bad);
+}
+
+__global__ void __launch_bounds__(kThreads) k_mdot_final(int nparts, const fx::XFPod *part, double2 *out)
+{
+    fx::XF acc;
+    acc.zero = true; acc.neg = false; acc.m = 0; acc.e = 0;
+    bool bad = false;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+        const fx::XFPod p = part[i];
+        bad |= (p.flags & 4) != 0;
+        acc = xfp::xf_add(acc, fx::from_pod(p));
+    }
+    bad = block_any(bad);
+    acc = xf_block_sum(acc);
+    if (threadIdx.x == 0) {
+        double h, l;
+        xfp::xf_to_dd(acc, h, l);
+        if (bad) h = l = __longlong_as_double(0x7ff8000000000000ll);
+        *out = make_double2(h, l);
+    }
 }
 
 }  // namespace
@@ -450,16 +472,18 @@ bool launch_mdot(int64_t n, const void *x, int64_t incx, const void *y, int64_t 
                  const char *routine)
 {
     int g = grid_for(n);
-    size_t bytes = (size_t)(g + 1) * sizeof(double2);
-    double2 *part = (double2 *)dev_alloc(bytes, routine);
-    if (!part) return false;
+    size_t bytes = (size_t)g * sizeof(fx::XFPod) + 256;
+    char *buf = (char *)dev_alloc(bytes, routine);
+    if (!buf) return false;
+    fx::XFPod *part = (fx::XFPod *)buf;
+    double2 *res = (double2 *)(buf + ((size_t)g * sizeof(fx::XFPod) + 15) / 16 * 16);
     k_mdot_partial<<<g, kThreads, 0, stream()>>>(n, (const double2 *)x, incx, (const double2 *)y, incy, part);
-    k_mdot_final<<<1, kThreads, 0, stream()>>>(g, part, part + g);
+    k_mdot_final<<<1, kThreads, 0, stream()>>>(g, part, res);
     count_launch(2);
     double2 r;
-    bool ok = cuda_ok(cudaMemcpyAsync(&r, part + g, sizeof(double2), cudaMemcpyDeviceToHost, stream()), routine,
+    bool ok = cuda_ok(cudaMemcpyAsync(&r, res, sizeof(double2), cudaMemcpyDeviceToHost, stream()), routine,
                       "dot result readback");
-    dev_free(part);
+    dev_free(buf);
     if (!ok) return false;
     if (!cuda_ok(cudaStreamSynchronize(stream()), routine, "dot sync")) return false;
     result_host->hi = r.x;

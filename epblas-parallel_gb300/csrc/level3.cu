@@ -9,13 +9,18 @@
 // TRSM (mtrsm_parallel.cpp:36-101, mtrsm_serial.cpp:738-822): B is prescaled
 // by alpha, then the triangle is split in halves recursively: solve one half,
 // update the other half of B with one GEMM (alpha = -1, beta = 1) through the
-// engine dispatch, solve the other half. Blocks of at most 64 rows/columns are
-// solved by substitution in double-double, one thread per right-hand side,
-// multiplying by the double-double reciprocal of the diagonal (the reference's
-// `inv = one_dd / A(k,k)`, mtrsm_serial.cpp:144). The O(m^2 n) update work
-// thus lands in a few large GEMMs (half the triangle at the top level), which
-// is the shape the tensor-core engine needs.
+// engine dispatch, solve the other half. The O(m^2 n) update work thus lands
+// in a few large GEMMs (half the triangle at the top level), which is the
+// shape the tensor-core engine needs. Blocks of at most 64 rows/columns:
+//  * with many right-hand sides, all 64 x 64 diagonal blocks are inverted in
+//    one launch (substitution with the double-double reciprocal of the
+//    diagonal, the reference's `inv = one_dd / A(k,k)`, mtrsm_serial.cpp:144)
+//    and each block of B is solved as one GEMM with its inverse, as GPU BLAS
+//    libraries do for their TRSM;
+//  * with few, each block is solved by substitution in double-double, one
+//    thread per right-hand side.
 #include "dd.cuh"
+#include "fixacc.cuh"
 #include "level3.h"
 #include "runtime.h"
 
@@ -97,6 +102,74 @@ __global__ void k_trsm_diag_right(int64_t c0, int nb, int64_t nrows, const doubl
         dd::real v = dd::add_fast(dd::add_fast(acc[0], acc[1]), dd::add_fast(acc[2], acc[3]));
         if (!unit) v = dd::mul_fast(v, dd_div(dd::make(1.0, 0.0), opA(A, lda, trans, gc, gc)));
         dd::store(B + row + gc * ldb, v);
+    }
+}
+
+// Inverses of the 64 x 64 diagonal blocks of op(A) (the last block may be
+// shorter), one CTA per block, thread per column c of the inverse: solve
+// op(A)_blk x = e_c by substitution over all rows (x is zero above c for a
+// lower triangle, so every thread walks the same rows and the block entries
+// are shared-memory broadcasts). The sums sum_p L(r,p) x(p) are accumulated
+// in integer fixed point (fixacc.cuh) and rounded once; each row is then
+// multiplied by the double-double reciprocal of the diagonal, as the
+// reference's substitution does (mtrsm_serial.cpp:144).
+// Inv: block b at Inv + b*64*64, column-major with leading dimension 64.
+constexpr int kInvNB = 64;
+
+__global__ void __launch_bounds__(kInvNB) k_trsm_diag_inv(int64_t na, const double2 *__restrict__ A, int64_t lda,
+                                                          bool trans, bool lower, bool unit, double2 *Inv)
+{
+    extern __shared__ fx::XFPod smem_inv[];
+    fx::XFPod *sA = smem_inv;                    // [p][r]: sA[p * 64 + r] = op(A)(o + r, o + p)
+    fx::XFPod *sX = smem_inv + kInvNB * kInvNB;  // [r][c]: x_c(r)
+    __shared__ double2 sInvDiag[kInvNB];
+    const int64_t o = (int64_t)blockIdx.x * kInvNB;
+    const int nb = (int)min((int64_t)kInvNB, na - o);
+    for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+        const int r = idx % nb, c = idx / nb;
+        const dd::real v = opA(A, lda, trans, o + r, o + c);
+        xfp::XF f = xfp::xf_from_dd(v.hi, v.lo);
+        if (v.hi == 0.0) f.zero = true;
+        sA[c * kInvNB + r] = fx::to_pod(f, false);
+    }
+    for (int r = threadIdx.x; r < nb; r += blockDim.x) {
+        const dd::real d = opA(A, lda, trans, o + r, o + r);
+        const dd::real iv = unit ? dd::make(1.0, 0.0) : dd_div(dd::make(1.0, 0.0), d);
+        sInvDiag[r] = make_double2(iv.hi, iv.lo);
+    }
+    __syncthreads();
+    const int c = threadIdx.x;
+    if (c >= nb) return;
+    double2 *out = Inv + (int64_t)blockIdx.x * kInvNB * kInvNB + (int64_t)c * kInvNB;
+    for (int s = 0; s < nb; ++s) {
+        const int r = lower ? s : nb - 1 - s;
+        fx::Acc acc;
+        acc.reset();
+        if (r == c) {
+            xfp::XF one;
+            one.m = (unsigned __int128)1 << 127;
+            one.e = -127;
+            one.neg = false;
+            one.zero = false;
+            acc.add(one);
+        }
+        const int p0 = lower ? 0 : r + 1, p1 = lower ? r : nb;
+        for (int p = p0; p < p1; ++p) {
+            const fx::XFPod xp = sX[p * kInvNB + c];
+            if (xp.flags & 2) continue;
+            const fx::XFPod ap = sA[p * kInvNB + r];
+            if (ap.flags & 2) continue;
+            xfp::XF t = xfp::xf_mul(fx::from_pod(ap), fx::from_pod(xp));
+            t.neg = !t.neg;
+            acc.add(t);
+        }
+        double h, l;
+        xfp::xf_to_dd(acc.finish(), h, l);
+        dd::real v = dd::mul_fast(dd::make(h, l), dd::load(&sInvDiag[r]));
+        xfp::XF f = xfp::xf_from_dd(v.hi, v.lo);
+        if (v.hi == 0.0) f.zero = true;
+        sX[r * kInvNB + c] = fx::to_pod(f, false);
+        out[r] = make_double2(v.hi, v.lo);
     }
 }
 
@@ -191,9 +264,44 @@ bool trsm_update(bool left, int64_t m, int64_t n, int64_t k, const void *Ablk, i
 // Recursive substitution on the na x na triangle of op(A) starting at (o, o).
 // Side L: B is na x nrhs (rows o..o+na of the caller's B). Side R: B is
 // nrhs x na (columns o..o+na). lower refers to op(A).
-bool trsm_rec(bool left, bool lower, bool trans, bool unit, int64_t o, int64_t na, int64_t nrhs, const void *A,
-              int64_t lda, double2 *B, int64_t ldb, const char *routine)
+// Leaf by explicit block inverse: X_blk = Inv_blk * B_blk (side L) or
+// B_blk * Inv_blk (side R) as one GEMM into T, copied back into B.
+struct TrsmInv {
+    const double2 *inv = nullptr;   // diagonal-block inverses (k_trsm_diag_inv)
+    double2 *T = nullptr;           // kTrsmLeaf x nrhs (or nrhs x kTrsmLeaf) scratch
+};
+
+bool trsm_leaf_inv(bool left, int64_t o, int64_t na, int64_t nrhs, const TrsmInv &w, double2 *B, int64_t ldb,
+                   const char *routine)
 {
+    GemmArgs g;
+    g.alpha = dd_host{1.0, 0.0};
+    g.beta = dd_host{0.0, 0.0};
+    g.beta_kind = 0;
+    const double2 *blk = w.inv + (o / kInvNB) * kInvNB * kInvNB;
+    if (left) {
+        g.m = na; g.n = nrhs; g.k = na;
+        g.A = blk; g.lda = kInvNB; g.ta = false;
+        g.B = B + o; g.ldb = ldb; g.tb = false;
+        g.C = w.T; g.ldc = na;
+    } else {
+        g.m = nrhs; g.n = na; g.k = na;
+        g.A = B + o * ldb; g.lda = ldb; g.ta = false;
+        g.B = blk; g.ldb = kInvNB; g.tb = false;
+        g.C = w.T; g.ldc = nrhs;
+    }
+    if (!run_gemm(g, false, -1, routine)) return false;
+    cudaError_t st = left ? cudaMemcpy2DAsync(B + o, ldb * sizeof(double2), w.T, na * sizeof(double2),
+                                              na * sizeof(double2), nrhs, cudaMemcpyDeviceToDevice, stream())
+                          : cudaMemcpy2DAsync(B + o * ldb, ldb * sizeof(double2), w.T, nrhs * sizeof(double2),
+                                              nrhs * sizeof(double2), na, cudaMemcpyDeviceToDevice, stream());
+    return cuda_ok(st, routine, "trsm leaf copy");
+}
+
+bool trsm_rec(bool left, bool lower, bool trans, bool unit, int64_t o, int64_t na, int64_t nrhs, const void *A,
+              int64_t lda, double2 *B, int64_t ldb, const TrsmInv &w, const char *routine)
+{
+    if (na <= kTrsmLeaf && w.inv) return trsm_leaf_inv(left, o, na, nrhs, w, B, ldb, routine);
     if (na <= kTrsmLeaf) {
         if (left)
             k_trsm_diag_left<<<blocks_for(nrhs, 64), 64, 0, stream()>>>(o, (int)na, nrhs, (const double2 *)A, lda,
@@ -210,36 +318,36 @@ bool trsm_rec(bool left, bool lower, bool trans, bool unit, int64_t o, int64_t n
     if (left) {
         // rows of B: first block B1 = rows o1.., second B2 = rows o2..
         if (lower) {
-            if (!trsm_rec(true, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, routine)) return false;
+            if (!trsm_rec(true, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, w, routine)) return false;
             // B2 -= op(A)[o2:, o1:o1+n1] * X1
             if (!trsm_update(true, n2, nrhs, n1, op_block(A, lda, trans, o2, o1), lda, trans, B + o1, ldb, B + o2,
                              ldb, routine))
                 return false;
-            return trsm_rec(true, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, routine);
+            return trsm_rec(true, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, w, routine);
         }
-        if (!trsm_rec(true, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, routine)) return false;
+        if (!trsm_rec(true, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, w, routine)) return false;
         // B1 -= op(A)[o1:o1+n1, o2:] * X2
         if (!trsm_update(true, n1, nrhs, n2, op_block(A, lda, trans, o1, o2), lda, trans, B + o2, ldb, B + o1, ldb,
                          routine))
             return false;
-        return trsm_rec(true, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, routine);
+        return trsm_rec(true, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, w, routine);
     }
     // side R: columns of B; op(A) upper -> left block first
     const bool upper = !lower;
     if (upper) {
-        if (!trsm_rec(false, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, routine)) return false;
+        if (!trsm_rec(false, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, w, routine)) return false;
         // B2 -= X1 * op(A)[o1:o1+n1, o2:]
         if (!trsm_update(false, nrhs, n2, n1, op_block(A, lda, trans, o1, o2), lda, trans, B + o1 * ldb, ldb,
                          B + o2 * ldb, ldb, routine))
             return false;
-        return trsm_rec(false, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, routine);
+        return trsm_rec(false, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, w, routine);
     }
-    if (!trsm_rec(false, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, routine)) return false;
+    if (!trsm_rec(false, lower, trans, unit, o2, n2, nrhs, A, lda, B, ldb, w, routine)) return false;
     // B1 -= X2 * op(A)[o2:, o1:o1+n1]
     if (!trsm_update(false, nrhs, n1, n2, op_block(A, lda, trans, o2, o1), lda, trans, B + o2 * ldb, ldb,
                      B + o1 * ldb, ldb, routine))
         return false;
-    return trsm_rec(false, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, routine);
+    return trsm_rec(false, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, w, routine);
 }
 
 }  // namespace
@@ -256,8 +364,29 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
         k_scale_fast<<<blocks_for(m * n, 256), 256, 0, stream()>>>(m, n, dd::make(alpha.hi, alpha.lo), b, ldb);
         count_launch();
     }
-    if (side == 'L') return trsm_rec(true, lower, trans, unit, 0, m, n, A, lda, b, ldb, routine);
-    return trsm_rec(false, lower, trans, unit, 0, n, m, A, lda, b, ldb, routine);
+    const bool left = (side == 'L');
+    const int64_t na = left ? m : n, nrhs = left ? n : m;
+    // Many right-hand sides: invert the diagonal blocks once (one launch) and
+    // apply them as GEMMs; few: substitute directly.
+    TrsmInv w;
+    void *scratch = nullptr;
+    if (nrhs >= 2 * kTrsmLeaf) {
+        const int64_t nblk = (na + kInvNB - 1) / kInvNB;
+        const size_t inv_bytes = (size_t)nblk * kInvNB * kInvNB * sizeof(double2);
+        const size_t t_bytes = (size_t)kTrsmLeaf * nrhs * sizeof(double2);
+        scratch = dev_alloc(inv_bytes + t_bytes, routine);
+        if (!scratch) return false;
+        w.inv = (const double2 *)scratch;
+        w.T = (double2 *)((char *)scratch + inv_bytes);
+        const size_t smem = 2 * (size_t)kInvNB * kInvNB * sizeof(fx::XFPod);
+        cudaFuncSetAttribute(k_trsm_diag_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_trsm_diag_inv<<<(unsigned)nblk, kInvNB, smem, stream()>>>(na, (const double2 *)A, lda, trans, lower,
+                                                                   unit, (double2 *)scratch);
+        count_launch();
+    }
+    const bool ok = trsm_rec(left, lower, trans, unit, 0, na, nrhs, A, lda, b, ldb, w, routine);
+    if (scratch) dev_free(scratch);
+    return ok;
 }
 
 void launch_zero_matrix(int64_t m, int64_t n, void *B, int64_t ldb)

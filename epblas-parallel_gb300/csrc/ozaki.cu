@@ -46,6 +46,7 @@
 #include "level3.h"
 #include "runtime.h"
 #include "sm100.cuh"
+#include "crt.cuh"
 #include "xfloat.cuh"
 
 namespace mw {
@@ -53,7 +54,6 @@ namespace mw {
 namespace {
 
 constexpr int kMaxMod = 40;
-constexpr int kNL = 9;          // 32-bit limbs of CRT integers
 constexpr int kResLimbs = 11;   // 11-bit limbs of |A'| (bits <= 120)
 constexpr int kNoExp = -30000;
 constexpr int kMaxP = 361;      // largest modulus: residues |r| <= 180 are exact in fp16
@@ -79,42 +79,12 @@ struct OzModParams {
 
 struct OzCrtParams {
     int nmod;
-    uint32_t W[kMaxMod][kNL];
-    float f[kMaxMod];
+    uint32_t F[kMaxMod][crt::kFLPad];   // 160-bit fractions u_l / p_l
     float pm[kMaxMod];
-    uint32_t M[kNL];
+    uint64_t Mhi, Mlo;                  // M = (Mhi:Mlo) * 2^Me, truncated
+    int Me;
 };
 
-// Little-endian multi-limb unsigned integer helpers (host).
-void big_mul_small(uint32_t *x, int nl, uint32_t s)
-{
-    uint64_t carry = 0;
-    for (int i = 0; i < nl; ++i) {
-        uint64_t v = (uint64_t)x[i] * s + carry;
-        x[i] = (uint32_t)v;
-        carry = v >> 32;
-    }
-}
-uint32_t big_divmod_small(uint32_t *x, int nl, uint32_t d)   // x /= d, returns x mod d
-{
-    uint64_t rem = 0;
-    for (int i = nl - 1; i >= 0; --i) {
-        uint64_t cur = (rem << 32) | x[i];
-        x[i] = (uint32_t)(cur / d);
-        rem = cur % d;
-    }
-    return (uint32_t)rem;
-}
-int64_t inv_mod(int64_t a, int64_t m)
-{
-    int64_t g = m, x = 0, x1 = 1, a1 = a % m;
-    while (a1) {
-        int64_t q = g / a1;
-        int64_t t = g - q * a1; g = a1; a1 = t;
-        t = x - q * x1; x = x1; x1 = t;
-    }
-    return ((x % m) + m) % m;
-}
 int gcd(int a, int b) { return b ? gcd(b, a % b) : a; }
 
 // The largest pairwise-coprime moduli <= kMaxP (greedy from the top), enough
@@ -565,8 +535,6 @@ __global__ void __launch_bounds__(256) k_oz_gemm_simt(const __half *__restrict__
 
 // ---- device: CRT reconstruction ----------------------------------------------------------
 
-__device__ __forceinline__ uint32_t limb_at(const uint32_t *x, int idx) { return (idx >= 0 && idx < kNL) ? x[idx] : 0u; }
-
 using xfp::XF;
 using xfp::xf_add;
 using xfp::xf_from_dd;
@@ -579,96 +547,29 @@ __device__ __forceinline__ dd::real xf_dd(const XF &x)
     return r;
 }
 
-// Shared-memory copy of the CRT constants (broadcast reads).
+// Shared-memory copy of the CRT constants (broadcast reads; each row of F is
+// 32 bytes so a modulus' constants are two 16-byte loads).
 struct CrtSmem {
-    uint32_t W[kMaxMod][kNL];
-    float f[kMaxMod];
-    uint32_t pm[kMaxMod];
-    uint32_t M[kNL];
+    alignas(16) uint32_t F[kMaxMod][crt::kFLPad];
+    float pm[kMaxMod];
 };
 
 __device__ __forceinline__ void crt_smem_fill(CrtSmem &sm, const OzCrtParams &K)
 {
-    for (int i = threadIdx.x; i < K.nmod * kNL; i += blockDim.x) sm.W[i / kNL][i % kNL] = K.W[i / kNL][i % kNL];
-    for (int i = threadIdx.x; i < K.nmod; i += blockDim.x) {
-        sm.f[i] = K.f[i];
-        sm.pm[i] = (uint32_t)K.pm[i];
-    }
-    for (int i = threadIdx.x; i < kNL; i += blockDim.x) sm.M[i] = K.M[i];
+    for (int i = threadIdx.x; i < K.nmod * crt::kFLPad; i += blockDim.x)
+        sm.F[i / crt::kFLPad][i % crt::kFLPad] = K.F[i / crt::kFLPad][i % crt::kFLPad];
+    for (int i = threadIdx.x; i < K.nmod; i += blockDim.x) sm.pm[i] = K.pm[i];
 }
 
-// CRT accumulator: X = sum_l c_l W_l - q M, q = round(sum_l c_l u_l / p_l).
-struct CrtAcc {
-    uint64_t S[kNL];
-    float qf;
-    __device__ __forceinline__ void reset()
-    {
-#pragma unroll
-        for (int t = 0; t < kNL; ++t) S[t] = 0;
-        qf = 0.0f;
-    }
-    __device__ __forceinline__ void add(const CrtSmem &K, int l, uint32_t cl)
-    {
-        qf = __fmaf_rn((float)cl, K.f[l], qf);
-#pragma unroll
-        for (int t = 0; t < kNL; ++t) S[t] += (uint64_t)cl * K.W[l][t];
-    }
-    // Top 128 bits of X, as an extended float scaled by 2^-S2.
-    __device__ __forceinline__ XF finish(const CrtSmem &K, int S2) const
-    {
-        uint32_t x[kNL];
-        uint64_t carry = 0;
-#pragma unroll
-        for (int t = 0; t < kNL; ++t) {
-            uint64_t v = S[t] + carry;
-            x[t] = (uint32_t)v;
-            carry = v >> 32;
-        }
-        uint32_t qv = (uint32_t)rintf(qf);
-        uint64_t borrow = 0, mc = 0;
-#pragma unroll
-        for (int t = 0; t < kNL; ++t) {
-            uint64_t prod = (uint64_t)qv * K.M[t] + mc;
-            mc = prod >> 32;
-            uint64_t sub = (uint64_t)(uint32_t)prod + borrow;
-            uint64_t v = (uint64_t)x[t] - sub;
-            x[t] = (uint32_t)v;
-            borrow = (v >> 63) & 1;
-        }
-        const bool neg = (x[kNL - 1] >> 31) != 0;
-        if (neg) {
-            uint64_t cy = 1;
-#pragma unroll
-            for (int t = 0; t < kNL; ++t) {
-                uint64_t v = (uint64_t)(~x[t]) + cy;
-                x[t] = (uint32_t)v;
-                cy = v >> 32;
-            }
-        }
-        int top = -1;
-#pragma unroll
-        for (int t = kNL - 1; t >= 0; --t)
-            if (top < 0 && x[t] != 0) top = t;
-        XF r;
-        if (top < 0) {
-            r.zero = true; r.neg = false; r.m = 0; r.e = 0;
-            return r;
-        }
-        // 128-bit window [P-127, P] below the leading bit P
-        const int z = __clz((int)x[top]);
-        const int P = top * 32 + 31 - z;
-        uint64_t w0 = ((uint64_t)limb_at(x, top) << 32) | limb_at(x, top - 1);
-        uint64_t w1 = ((uint64_t)limb_at(x, top - 2) << 32) | limb_at(x, top - 3);
-        uint64_t w2 = (uint64_t)limb_at(x, top - 4) << 32;
-        unsigned __int128 m = ((unsigned __int128)w0 << 64) | w1;
-        if (z) m = (m << z) | (w2 >> (64 - z));
-        r.neg = neg;
-        r.zero = false;
-        r.m = m;
-        r.e = P - 127 - S2;
-        return r;
-    }
-};
+__device__ __forceinline__ XF crt_m(const OzCrtParams &K)
+{
+    XF m;
+    m.m = ((unsigned __int128)K.Mhi << 64) | K.Mlo;
+    m.e = K.Me;
+    m.neg = false;
+    m.zero = false;
+    return m;
+}
 
 // C(i, j) := alpha * X(i, j) * 2^-S2 + beta * C(i, j), real.
 __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, const uint16_t *__restrict__ R,
@@ -683,13 +584,14 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, co
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= m) return;
     const int nmod = K.nmod;
+    const XF Mx = crt_m(K);
     const XF xa = xf_from_dd(alpha.hi, alpha.lo), xb = xf_from_dd(beta.hi, beta.lo);
     for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
         if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
         XF v;
         v.zero = true; v.neg = false; v.m = 0; v.e = 0;
         if (ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
-            CrtAcc acc;
+            crt::Frac acc;
             acc.reset();
             // residues of all moduli: issue the loads of 8 planes at a time
             // so that their latencies overlap
@@ -701,10 +603,10 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, co
 #pragma unroll
                 for (int u = 0; u < 8; ++u) c[u] = __ldcs(rp + (int64_t)(l + u) * plane);
 #pragma unroll
-                for (int u = 0; u < 8; ++u) acc.add(sm, l + u, c[u]);
+                for (int u = 0; u < 8; ++u) acc.add(sm.F[l + u], c[u]);
             }
-            for (; l < nmod; ++l) acc.add(sm, l, __ldcs(rp + (int64_t)l * plane));
-            v = acc.finish(sm, (bits - 2 - ea[i]) + (bits - 2 - eb[j]));
+            for (; l < nmod; ++l) acc.add(sm.F[l], __ldcs(rp + (int64_t)l * plane));
+            v = acc.finish(Mx, (bits - 2 - ea[i]) + (bits - 2 - eb[j]));
         }
         if (!alpha_one) v = xf_mul(xa, v);
         double2 *pc = C + i + j * ldc;
@@ -741,6 +643,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, 
     if (i >= m) return;
     const int nmod = K.nmod;
     const int64_t cstride = (int64_t)nmod * Np * Mp;
+    const XF Mx = crt_m(K);
     const XF ar = xf_from_dd(alpha.re.hi, alpha.re.lo), ai = xf_from_dd(alpha.im.hi, alpha.im.lo);
     const XF br = xf_from_dd(beta.re.hi, beta.re.lo), bi = xf_from_dd(beta.im.hi, beta.im.lo);
     for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
@@ -748,7 +651,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, 
         XF vr, vi;
         vr.zero = vi.zero = true; vr.neg = vi.neg = false; vr.m = vi.m = 0; vr.e = vi.e = 0;
         if (ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
-            CrtAcc accr, acci;
+            crt::Frac accr, acci;
             accr.reset();
             acci.reset();
             auto add_l = [&](int l, int p1, int p2, int p3) {
@@ -758,8 +661,8 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, 
                 int im = p3 - p1 - p2;
                 if (im < 0) im += p;
                 if (im < 0) im += p;
-                accr.add(sm, l, (uint32_t)re);
-                acci.add(sm, l, (uint32_t)im);
+                accr.add(sm.F[l], (uint32_t)re);
+                acci.add(sm.F[l], (uint32_t)im);
             };
             const uint16_t *rp = R + j * Mp + i;
             const int64_t plane = Np * Mp;
@@ -778,8 +681,8 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, 
                 add_l(l, __ldcs(q), __ldcs(q + cstride), __ldcs(q + 2 * cstride));
             }
             const int S2 = (bits - 2 - ea[i]) + (bits - 2 - eb[j]);
-            vr = accr.finish(sm, S2);
-            vi = acci.finish(sm, S2);
+            vr = accr.finish(Mx, S2);
+            vi = acci.finish(Mx, S2);
         }
         XF rr = vr, ri = vi;
         if (!alpha_one) {
@@ -901,23 +804,12 @@ void fill_res_params(const Moduli &md, OzResParams &rp, OzModParams &mp)
 void fill_crt_params(const Moduli &md, OzCrtParams &cp)
 {
     cp.nmod = md.n;
-    uint32_t Mb[kNL] = {1};
-    for (int t = 1; t < kNL; ++t) Mb[t] = 0;
-    for (int l = 0; l < md.n; ++l) big_mul_small(Mb, kNL, (uint32_t)md.p[l]);
-    memcpy(cp.M, Mb, sizeof(Mb));
-    for (int l = 0; l < md.n; ++l) {
-        uint32_t Ml[kNL];
-        memcpy(Ml, Mb, sizeof(Mb));
-        big_divmod_small(Ml, kNL, (uint32_t)md.p[l]);
-        uint32_t tmp[kNL];
-        memcpy(tmp, Ml, sizeof(Ml));
-        int64_t mlmod = big_divmod_small(tmp, kNL, (uint32_t)md.p[l]);
-        int64_t u = inv_mod(mlmod, md.p[l]);
-        big_mul_small(Ml, kNL, (uint32_t)u);
-        memcpy(cp.W[l], Ml, sizeof(Ml));
-        cp.f[l] = (float)((double)u / (double)md.p[l]);
-        cp.pm[l] = (float)md.p[l];
-    }
+    xfp::XF Mx;
+    crt::constants(md.p, md.n, cp.F, Mx);
+    for (int l = 0; l < md.n; ++l) cp.pm[l] = (float)md.p[l];
+    cp.Mhi = (uint64_t)(Mx.m >> 64);
+    cp.Mlo = (uint64_t)Mx.m;
+    cp.Me = Mx.e;
 }
 
 unsigned blocks_cap(int64_t want)

@@ -108,6 +108,7 @@ class MWBlas:
             PI = C.POINTER(_i64)
             self._sig("mgemm_plain_64_", None, [_ch, _ch, PI, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
             self._sig("mgemm_ozaki_64_", None, [_ch, _ch, PI, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
+            self._sig("mgemm_fixed_64_", None, [_ch, _ch, PI, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
             self._sig("mwblas_set_gemm_engine", _i32, [_i32])
             self._sig("mwblas_get_gemm_engine", _i32, [])
             self._sig("mwblas_set_ozaki_bits", _i32, [_i32])
@@ -154,7 +155,8 @@ class MWBlas:
         if engine is None:
             f = self.lib.mgemm_64_ if wide else self.lib.mgemm_
         else:
-            f = {"plain": self.lib.mgemm_plain_64_, "ozaki": self.lib.mgemm_ozaki_64_}[engine]
+            f = {"plain": self.lib.mgemm_plain_64_, "ozaki": self.lib.mgemm_ozaki_64_,
+                 "fixed": self.lib.mgemm_fixed_64_}[engine]
             I = lambda v: self._I(v, True)
         f(ta.encode(), tb.encode(), I(m), I(n), I(k), C.byref(real(alpha)), _ptr(a), I(lda), _ptr(b), I(ldb),
           C.byref(real(beta)), _ptr(c), I(ldc))

@@ -178,15 +178,21 @@ int64_t iwamax_64_(const int64_t *n, const MWBLAS_C *x, const int64_t *incx);
 
 /* GEMM engine selection for mgemm_/wgemm_ and the level-3 routines built on
  * them.  MWBLAS_GEMM_AUTO picks by size; PLAIN is the FP64 error-free-
- * transform kernel; OZAKI is the integer-exact tensor-core scheme.  The
- * MWBLAS_GEMM environment variable ("auto", "plain", "ozaki") sets the
- * initial value. */
-enum { MWBLAS_GEMM_AUTO = 0, MWBLAS_GEMM_PLAIN = 1, MWBLAS_GEMM_OZAKI = 2 };
+ * transform kernel; OZAKI is the integer-exact tensor-core scheme; FIXED is
+ * the fixed-point kernel on the integer pipes (real routines; complex ones
+ * fall back to PLAIN).  The MWBLAS_GEMM environment variable ("auto",
+ * "plain", "ozaki", "fixed") sets the initial value. */
+enum { MWBLAS_GEMM_AUTO = 0, MWBLAS_GEMM_PLAIN = 1, MWBLAS_GEMM_OZAKI = 2, MWBLAS_GEMM_FIXED = 3 };
 int mwblas_set_gemm_engine(int engine);   /* returns the previous value */
 int mwblas_get_gemm_engine(void);
 
 /* Same arguments as mgemm_64_, forcing one engine. */
 void mgemm_plain_64_(const char *transa, const char *transb, const int64_t *m,
+                     const int64_t *n, const int64_t *k, const MWBLAS_R *alpha,
+                     const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *b,
+                     const int64_t *ldb, const MWBLAS_R *beta, MWBLAS_R *c,
+                     const int64_t *ldc);
+void mgemm_fixed_64_(const char *transa, const char *transb, const int64_t *m,
                      const int64_t *n, const int64_t *k, const MWBLAS_R *alpha,
                      const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *b,
                      const int64_t *ldb, const MWBLAS_R *beta, MWBLAS_R *c,

@@ -46,7 +46,8 @@ def make_batch(rng, count, maxdim=200, big_k=None):
         if t == 5:
             k = 0
         if big_k and t % 7 == 0:
-            m, n, k = 12, 20, big_k
+            # split instances with different split counts share the partial buffer
+            m, n, k = 12, 20, big_k // (1 + (t // 7) % 3)
         ta, tb = rng.choice(["N", "T", "C"]), rng.choice(["N", "T"])
         lda = (m if ta == "N" else k) + int(rng.integers(0, 3))
         ldb = (k if tb == "N" else n) + int(rng.integers(0, 3))

@@ -162,6 +162,34 @@ def test_dot_within_tolerance(gpu, oracle, rng, golden):
             assert orc.normwise_error(got[None], z[k + "_q"][None], op) <= max(10, 4 * c["n"]) * orc.EPS_DD
 
 
+def test_dot_exponent_range_cancellation_and_nonfinite(gpu, oracle, rng):
+    """Products spanning 2^-600..2^600, exact cancellation, and non-finite inputs."""
+    n = 3001
+    x = vec(rng, n, 1)
+    y = vec(rng, n, 1)
+    sc = 2.0 ** rng.integers(-300, 300, n)
+    x *= sc[:, None]
+    y *= (2.0 ** rng.integers(-300, 300, n))[:, None]
+    got = np.array(gpu.mdot(n, x, 1, y, 1))
+    want = oracle.qdot(n, x, 1, y, 1)
+    # normwise against n * max|x| * max|y|, and relative to the largest product
+    op = n * orc.dd_absmax(x) * orc.dd_absmax(y)
+    assert orc.normwise_error(got[None], want[None], op) <= max(10, 4 * n) * orc.EPS_DD
+    pmax = np.max(np.abs(x[:, 0] * y[:, 0]))
+    assert orc.normwise_error(got[None], want[None], pmax) <= 8 * orc.EPS_DD
+    # x . [y, -y] over [x, x] cancels: what is left is far below the largest product
+    xx = np.concatenate([x, x])
+    yy = np.concatenate([y, -y])
+    r = gpu.mdot(2 * n, xx, 1, yy, 1)
+    assert abs(r[0]) <= orc.EPS_DD * pmax, (r, pmax)
+    # a single non-finite element makes the result NaN
+    for bad in (np.inf, -np.inf, np.nan):
+        xb = x.copy()
+        xb[n // 2] = (bad, 0.0)
+        r = gpu.mdot(n, xb, 1, y, 1)
+        assert np.isnan(r[0]), (bad, r)
+
+
 def test_device_pointer_path_matches_host_path(gpu, oracle, rng):
     """Device-resident arrays are used in place (no staging) with the same bits."""
     import torch

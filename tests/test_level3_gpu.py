@@ -17,7 +17,7 @@ from conftest import mwb, orc
 pytestmark = pytest.mark.gpu
 
 SENT = -7.37e18
-ENGINES = ["plain"]
+ENGINES = ["plain", "fixed"]
 
 
 def alpha_beta(rng, cplx_=False):
@@ -60,6 +60,36 @@ def test_mgemm_random(gpu, oracle, rng, engine, ta, tb):
         check_sentinel(got, m)
         err = orc.normwise_error(got[:, :m], want[:, :m], op_norm(al, k, A, B, be, C0[:, :m]))
         assert err <= max(10, 4 * k) * orc.EPS_DD, (m, n, k, err)
+
+
+def test_fixed_engine_long_k_scaled_rows_and_nonfinite(gpu, oracle, rng):
+    """The integer-pipe engine: K beyond one launch's 16384, rows/columns
+    scaled by 2^+-300 (per-row/column scaling keeps them exact), and a
+    non-finite entry turning its row of C into NaN."""
+    m, n, k = 9, 7, 20000
+    A = mwb.dd_matrix(rng, m, k)
+    B = mwb.dd_matrix(rng, k, n)
+    A *= (2.0 ** rng.integers(-300, 300, m))[None, :, None]
+    B *= (2.0 ** rng.integers(-300, 300, n))[:, None, None]
+    C0 = mwb.dd_matrix(rng, m, n)
+    al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+    want = oracle.qgemm("N", "N", m, n, k, al, A, m, B, k, be, C0.copy(), m)
+    got = C0.copy()
+    gpu.mgemm("N", "N", m, n, k, al, A, m, B, k, be, got, m, engine="fixed")
+    assert gpu.last_error()[0] == 0, gpu.last_error()
+    # each entry against its own row/column scale
+    ra = np.max(np.abs(A[..., 0]), axis=0)          # per row of A
+    cb = np.max(np.abs(B[..., 0]), axis=1)          # per column of B
+    scale = orc.dd_abs(al) * k * np.outer(cb, ra) + orc.dd_abs(be) * np.abs(C0[..., 0])
+    err = np.abs((got[..., 0] - want[..., 0]) + (got[..., 1] - want[..., 1]))
+    assert np.all(err <= 4 * k * orc.EPS_DD * scale), np.max(err / scale)
+    A2 = A[:, :, :].copy()
+    A2[k // 2, 3] = (np.inf, 0.0)                   # row 3 of A
+    got = C0.copy()
+    gpu.mgemm("N", "N", m, n, k, al, A2, m, B, k, be, got, m, engine="fixed")
+    assert np.all(np.isnan(got[:, 3, 0])), "row with an infinity must be NaN"
+    rest = [i for i in range(m) if i != 3]
+    assert np.all(np.isfinite(got[:, rest, 0]))
 
 
 def test_mgemm_lp64_and_special_scalars(gpu, oracle, rng):
@@ -160,7 +190,9 @@ def dominant_triangle(rng, na, lda):
 @pytest.mark.parametrize("ta", ["N", "T"])
 @pytest.mark.parametrize("diag", ["N", "U"])
 def test_mtrsm(gpu, oracle, rng, side, uplo, ta, diag):
-    for (m, n) in [(1, 1), (7, 5), (70, 33), (150, 20)]:
+    # (150, 140) and (130, 300): at least 128 right-hand sides take the
+    # block-inverse path (the last diagonal block is partial)
+    for (m, n) in [(1, 1), (7, 5), (70, 33), (150, 20), (150, 140), (130, 300)]:
         if side == "R":
             m, n = n, m
         na = m if side == "L" else n
@@ -193,6 +225,32 @@ def test_mgemv(gpu, oracle, rng, trans):
         opn = orc.dd_abs(al) * lx * orc.dd_absmax(A[:, :m]) * orc.dd_absmax(x) + orc.dd_abs(be) * orc.dd_absmax(y0)
         err = orc.normwise_error(got, want, opn)
         assert err <= max(10, 4 * max(m, n)) * orc.EPS_DD, (m, n, err)
+
+
+@pytest.mark.parametrize("trans", ["N", "T"])
+def test_mgemv_scaled_rows_componentwise(gpu, oracle, rng, trans):
+    """Rows of A scaled by 2^e, e in [-200, 200]: each y(i) is accurate relative
+    to its own |alpha| sum_j |A(i,j) x(j)| + |beta y(i)|, not only normwise."""
+    m, n = 257, 1500
+    A = mwb.dd_matrix(rng, m, n, m)
+    A *= (2.0 ** rng.integers(-200, 200, m))[None, :, None]
+    if trans == "T":
+        A = np.ascontiguousarray(np.transpose(A, (1, 0, 2)))   # n x m, columns scaled
+    rows, cols = (m, n) if trans == "N" else (n, m)
+    lx, ly = (n, m) if trans == "N" else (n, m)
+    x = mwb.random_dd(rng, (lx,))
+    y0 = mwb.random_dd(rng, (ly,))
+    y0 *= (2.0 ** rng.integers(-200, 200, ly))[:, None]
+    al, be = alpha_beta(rng)
+    want = y0.copy(); oracle.qgemv(trans, rows, cols, al, A, rows, x, 1, be, want, 1)
+    got = y0.copy()
+    gpu.mgemv(trans, rows, cols, al, A, rows, x, 1, be, got, 1)
+    Ah = np.abs(A[..., 0])                       # (cols, rows)
+    xs = np.abs(x[:, 0])
+    absum = (Ah.T @ xs) if trans == "N" else (Ah @ xs)
+    bound = orc.dd_abs(al) * absum + orc.dd_abs(be) * np.abs(y0[:, 0])
+    err = np.abs((got[:, 0] - want[:, 0]) + (got[:, 1] - want[:, 1]))
+    assert np.all(err <= 4 * lx * orc.EPS_DD * bound), np.max(err / bound)
 
 
 def test_golden_reference_outputs(gpu, golden):

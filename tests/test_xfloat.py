@@ -97,3 +97,46 @@ def test_alpha_x_plus_beta_c(xf):
         ex = exact(*al) * exact(*x) + exact(*be) * exact(*c)
         scale = abs(exact(*al) * exact(*x)) + abs(exact(*be) * exact(*c))
         assert abs(exact(oh, ol) - ex) <= scale * Fraction(2) ** -104
+
+
+def _moduli(need_bits):
+    """Greedy pairwise-coprime moduli from 361 downwards (as the engine picks them)."""
+    from math import gcd, log2
+    ps, have = [], 0.0
+    for c in range(361, 2, -1):
+        if have >= need_bits:
+            break
+        if all(gcd(c, q) == 1 for q in ps):
+            ps.append(c)
+            have += log2(c)
+    return ps
+
+
+@pytest.mark.parametrize("nmod_bits", [120, 180, 237, 300])
+def test_crt_fraction_reconstruction(xf, nmod_bits):
+    """X from its residues: within M * 2^-140 absolute and 2^-104 relative.
+
+    |X| <= M / 64, the headroom the engine keeps (it asks for 4 bits beyond
+    the product bound plus the sign bit)."""
+    xf.crt_frac.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int,
+                            C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    ps = _moduli(nmod_bits)
+    M = 1
+    for q in ps:
+        M *= q
+    rng = np.random.default_rng(nmod_bits)
+    P = (C.c_int * len(ps))(*ps)
+    xs = [0, 1, -1, M // 64, -(M // 64), 2 ** 106 - 1]
+    for _ in range(300):
+        bits = int(rng.integers(1, M.bit_length() - 7))
+        x = int.from_bytes(rng.bytes(48), "little") % (1 << bits)
+        xs.append(x if rng.random() < 0.5 else -x)
+    for x in xs:
+        cs = (C.c_int * len(ps))(*[x % q for q in ps])
+        S2 = int(rng.integers(-50, 300))
+        h, l = C.c_double(), C.c_double()
+        xf.crt_frac(len(ps), P, cs, S2, C.byref(h), C.byref(l))
+        got = exact(h.value, l.value)
+        want = Fraction(x) / Fraction(2) ** S2
+        tol = (abs(Fraction(x)) * Fraction(2) ** -104 + Fraction(M) * Fraction(2) ** -140) / Fraction(2) ** S2
+        assert abs(got - want) <= tol, (x, S2, float(got), float(want))

@@ -31,3 +31,18 @@ void xf_axpby(double alh, double all, double ah, double al, double beh, double b
 }
 
 }
+
+// CRT reconstruction in fractional fixed point (csrc/crt.cuh): residues c[l]
+// of X modulo p[l] -> X * 2^-S2 as a double-double.
+#include "../epblas-parallel_gb300/csrc/crt.cuh"
+
+extern "C" void crt_frac(int n, const int *p, const int *c, int S2, double *oh, double *ol)
+{
+    uint32_t F[40][crt::kFLPad];
+    xfp::XF Mx;
+    crt::constants(p, n, F, Mx);
+    crt::Frac acc;
+    acc.reset();
+    for (int l = 0; l < n; ++l) acc.add(F[l], (uint32_t)c[l]);
+    xfp::xf_to_dd(acc.finish(Mx, S2), *oh, *ol);
+}
