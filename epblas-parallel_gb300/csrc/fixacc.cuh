@@ -1,21 +1,27 @@
 // Integer fixed-point accumulation of double-double products, for the
-// bandwidth-bound reductions (DOT, GEMV).
+// bandwidth-bound reductions (DOT, GEMV) and the TRSM block inverses.
 //
 // On this part an FP64 instruction issues at ~1/40 of the integer rate, so a
 // double-double multiply-add on the FP64 pipe (12 instructions) cannot keep
-// up with HBM. Here each product is formed exactly enough in integers: both
-// operands become 128-bit mantissas (the exact image of hi + lo), their
-// product keeps its top 128 bits (relative truncation < 2^-126), and it is
-// added, shifted to a per-thread block exponent, into a 192-bit two's
-// complement accumulator. The accumulator keeps 2^-160 of its leading product
-// below the binary point; when a product arrives that would not fit under the
-// 32-bit headroom, the accumulator moves to a higher exponent (a right shift,
-// rare after the first few terms). Sums of these accumulators (warp, block,
-// grid) use the 128-bit extended-float addition, in a fixed order.
+// up with HBM. Here everything is integer work on the bit patterns:
 //
+//  * decode: a double-double (hi, lo) becomes |hi + lo| = (x1:x0) * 2^e with
+//    x1 < 2^54 holding hi's mantissa and x0 the 64 bits below it (lo's
+//    mantissa shifted into place, added or subtracted): the exact value to
+//    2^-117, from shifts and adds only;
+//  * product: Q = floor(|a| |b| / 2^64), three 64 x 64 -> 128-bit products
+//    (the dropped x0*y0 term is below 2^-106 of the product's top), Q < 2^172;
+//  * accumulate: Q is shifted to the accumulator's block exponent and added
+//    into a 192-bit two's complement integer; when a product would reach above
+//    the 12-bit headroom the block exponent moves up (a right shift, rare after
+//    the first terms). At most 4096 products per accumulator (callers size
+//    their grids for it).
+//
+// Sums of accumulators (warp, block, grid) use the 128-bit extended-float
+// addition of xfloat.cuh in a fixed order, so results are deterministic.
 // Non-finite inputs make the double-double operators of the reference return
-// NaN (the TwoProduct error term of an infinity is inf - inf); the
-// accumulator records them and the result is NaN.
+// NaN (the TwoProduct error term of an infinity is inf - inf): they are
+// flagged and the result is NaN.
 #pragma once
 #include "xfloat.cuh"
 
@@ -23,8 +29,69 @@ namespace fx {
 
 using xfp::XF;
 
-constexpr int kHead = 32;    // headroom bits above the largest product so far
-constexpr int kSlack = 12;   // extra room left when the exponent moves up
+constexpr int kMaxAdds = 4096;   // products per accumulator (12-bit headroom)
+
+enum : uint32_t { kNeg = 1, kZero = 2, kBad = 4 };
+
+// |v| = (x1:x0) * 2^e, sign and zero / non-finite flags.
+struct Op {
+    uint64_t x1, x0;
+    int e;
+    uint32_t flags;
+};
+
+__device__ __forceinline__ Op decode(double2 v)
+{
+    Op o;
+    const uint64_t bh = (uint64_t)__double_as_longlong(v.x), bl = (uint64_t)__double_as_longlong(v.y);
+    int eh = (int)((bh >> 52) & 0x7FF), el = (int)((bl >> 52) & 0x7FF);
+    o.flags = (uint32_t)(bh >> 63);
+    if (eh == 0x7FF || el == 0x7FF) {
+        o.flags |= kBad;
+        o.x1 = o.x0 = 0;
+        o.e = 0;
+        return o;
+    }
+    if ((bh << 1) == 0) {   // hi == +-0: a normalised double-double is zero
+        o.flags |= kZero;
+        o.x1 = o.x0 = 0;
+        o.e = 0;
+        return o;
+    }
+    const uint64_t mh = (bh & 0xFFFFFFFFFFFFFull) | (eh ? (1ull << 52) : 0);
+    eh = eh ? eh : 1;
+    o.e = eh - 1075 - 64;
+    o.x1 = mh;
+    o.x0 = 0;
+    if ((bl << 1) != 0) {
+        const uint64_t ml = (bl & 0xFFFFFFFFFFFFFull) | (el ? (1ull << 52) : 0);
+        el = el ? el : 1;
+        const int s = 64 - (eh - el);   // lo's mantissa sits s bits above x0's bit 0
+        uint64_t t1 = 0, t0;
+        if (s >= 64) {
+            // |lo| >= |hi| / 2: not a normalised double-double; keep hi's frame
+            // and fold lo in at 2^64 granularity (the value stays within
+            // 2^-52 of hi + lo relative to lo)
+            const int s1 = s - 64;
+            t1 = s1 < 11 ? (ml << s1) : (ml << 10);
+            t0 = 0;
+        } else if (s >= 0) {
+            t0 = ml << s;
+            t1 = s ? (ml >> (64 - s)) : 0;
+        } else {
+            t0 = (-s < 64) ? (ml >> -s) : 0;
+        }
+        if ((bh ^ bl) >> 63) {   // lo has the opposite sign
+            const uint64_t borrow = t0 != 0;
+            o.x0 = 0 - t0;
+            o.x1 = mh - t1 - borrow;
+        } else {
+            o.x0 = t0;
+            o.x1 = mh + t1;
+        }
+    }
+    return o;
+}
 
 struct Acc {
     uint64_t w0, w1, w2;   // value = W * 2^lsb, W two's complement
@@ -45,7 +112,7 @@ struct Acc {
         // arithmetic shift of the 192-bit W by d >= 1
         const uint64_t sgn = (uint64_t)((int64_t)w2 >> 63);
         if (d >= 192) {
-            w0 = w1 = w2 = 0;   // all previous terms are below the new resolution
+            w0 = w1 = w2 = 0;   // all earlier terms lie below the new resolution
             return;
         }
         while (d >= 64) {
@@ -61,39 +128,36 @@ struct Acc {
         }
     }
 
-    // W += (neg ? -1 : 1) * m * 2^e
-    __device__ __forceinline__ void add(const XF &p)
+    // W += +-(q2:q1:q0) * 2^(eq - lsb), q < 2^172
+    __device__ __forceinline__ void add_q(uint64_t q0, uint64_t q1, uint64_t q2, int eq, bool neg)
     {
-        if (p.zero) return;
-        const int need = p.e + 128 + kHead - 191;   // smallest lsb that keeps the headroom
         if (!init) {
-            lsb = need + kSlack;
+            lsb = eq - 4;
             init = true;
-        } else if (need > lsb) {
-            const int nl = need + kSlack;
-            shift_right(nl - lsb);
-            lsb = nl;
         }
-        const int sh = p.e - lsb;   // position of m's bit 0; <= 63 - kHead
-        const uint64_t m1 = (uint64_t)(p.m >> 64), m0 = (uint64_t)p.m;
+        int s = eq - lsb;
+        if (s > 8) {   // keep Q's top (bit 171 + s) at or below bit 179
+            shift_right(s - 4);
+            lsb += s - 4;
+            s = 4;
+        }
         uint64_t v0, v1, v2;
-        if (sh >= 0) {
-            v0 = m0 << sh;
-            v1 = sh ? ((m1 << sh) | (m0 >> (64 - sh))) : m1;
-            v2 = sh ? (m1 >> (64 - sh)) : 0;
+        if (s >= 0) {
+            v0 = q0 << s;
+            v1 = s ? ((q1 << s) | (q0 >> (64 - s))) : q1;
+            v2 = s ? ((q2 << s) | (q1 >> (64 - s))) : q2;
         } else {
-            const int r = -sh;
-            if (r >= 128) return;
-            if (r >= 64) {
-                v0 = m1 >> (r - 64);
-                v1 = 0;
-            } else {
-                v0 = r ? ((m0 >> r) | (m1 << (64 - r))) : m0;
-                v1 = m1 >> r;
-            }
-            v2 = 0;
+            const int r = -s;
+            if (r >= 172) return;   // below the accumulator's resolution
+            const int ws = r >> 6, b = r & 63;
+            const uint64_t a0 = ws == 0 ? q0 : (ws == 1 ? q1 : q2);
+            const uint64_t a1 = ws == 0 ? q1 : (ws == 1 ? q2 : 0);
+            const uint64_t a2 = ws == 0 ? q2 : 0;
+            v0 = b ? ((a0 >> b) | (a1 << (64 - b))) : a0;
+            v1 = b ? ((a1 >> b) | (a2 << (64 - b))) : a1;
+            v2 = a2 >> b;
         }
-        if (p.neg) {
+        if (neg) {
             asm("sub.cc.u64 %0, %0, %3;\n\t"
                 "subc.cc.u64 %1, %1, %4;\n\t"
                 "subc.u64 %2, %2, %5;"
@@ -108,11 +172,28 @@ struct Acc {
         }
     }
 
-    // double-double product a * b, both finite, added exactly to 2^-126
-    __device__ __forceinline__ void add_dd_product(double ah, double al, double bh, double bl)
+    // += a * b (decoded operands)
+    __device__ __forceinline__ void add_prod(const Op &a, const Op &b)
     {
-        if (ah == 0.0 || bh == 0.0) return;
-        add(xfp::xf_mul(xfp::xf_from_dd(ah, al), xfp::xf_from_dd(bh, bl)));
+        const uint32_t f = a.flags | b.flags;
+        if (f & kBad) {
+            bad = true;
+            return;
+        }
+        if (f & kZero) return;
+        // Q = (a1 b1) 2^64 + a1 b0 + a0 b1 + hi(a0 b0 dropped)
+        const uint64_t p11l = a.x1 * b.x1, p11h = __umul64hi(a.x1, b.x1);
+        const uint64_t p10l = a.x1 * b.x0, p10h = __umul64hi(a.x1, b.x0);
+        const uint64_t p01l = a.x0 * b.x1, p01h = __umul64hi(a.x0, b.x1);
+        uint64_t q0, q1, q2;
+        asm("add.cc.u64 %0, %3, %4;\n\t"
+            "addc.cc.u64 %1, %5, %6;\n\t"
+            "addc.u64 %2, %7, 0;\n\t"
+            "add.cc.u64 %1, %1, %8;\n\t"
+            "addc.u64 %2, %2, 0;"
+            : "=l"(q0), "=l"(q1), "=l"(q2)
+            : "l"(p10l), "l"(p01l), "l"(p11l), "l"(p10h), "l"(p11h), "l"(p01h));
+        add_q(q0, q1, q2, a.e + b.e + 64, ((a.flags ^ b.flags) & kNeg) != 0);
     }
 
     __device__ __forceinline__ XF finish() const
@@ -151,6 +232,18 @@ struct Acc {
         return xfp::xf_norm(neg, m, e);
     }
 };
+
+// An extended float as a decoded operand (for values produced by the CRT or
+// by a previous reduction): |v| = m * 2^e -> (x1:x0) with x1 < 2^54.
+__device__ __forceinline__ Op op_from_xf(const XF &v)
+{
+    Op o;
+    o.flags = (v.neg ? kNeg : 0) | (v.zero ? kZero : 0);
+    o.x1 = (uint64_t)(v.m >> 74);
+    o.x0 = (uint64_t)(v.m >> 10);
+    o.e = v.e + 10;
+    return o;
+}
 
 // Extended-float warp reduction (lane 0 holds the sum; fixed order).
 __device__ __forceinline__ XF xf_shfl_down(const XF &v, int off)
@@ -199,10 +292,35 @@ __device__ __forceinline__ XF from_pod(const XFPod &p)
     return v;
 }
 
+// A decoded operand in the same 24-byte form.
+struct OpPod {
+    unsigned long long x1, x0;
+    int e;
+    unsigned int flags;
+};
+
+__device__ __forceinline__ OpPod to_pod(const Op &o)
+{
+    OpPod p;
+    p.x1 = o.x1;
+    p.x0 = o.x0;
+    p.e = o.e;
+    p.flags = o.flags;
+    return p;
+}
+
+__device__ __forceinline__ Op from_pod(const OpPod &p)
+{
+    Op o;
+    o.x1 = p.x1;
+    o.x0 = p.x0;
+    o.e = p.e;
+    o.flags = p.flags;
+    return o;
+}
+
 __device__ __forceinline__ bool finite_dd(double2 v)
 {
-    // exponent field of hi below 0x7FF (lo is finite whenever hi is, for
-    // any value a double-double operator produces)
     return (((uint64_t)__double_as_longlong(v.x) >> 52) & 0x7FF) != 0x7FF &&
            (((uint64_t)__double_as_longlong(v.y) >> 52) & 0x7FF) != 0x7FF;
 }

@@ -28,6 +28,7 @@
 #include <cmath>
 
 #include "dd.cuh"
+#include "fixacc.cuh"
 #include "gemm.h"
 #include "runtime.h"
 #include "xfloat.cuh"
@@ -44,16 +45,18 @@ constexpr int FX_THREADS = 256;      // 16 x 16 threads, 4 x 4 outputs each
 constexpr int64_t FX_MAX_K = 16384;  // per launch (column-sum headroom)
 constexpr int kNoExpFx = -30000;
 
-// v * 2^sh rounded to an integer (|v * 2^sh| < 2^116), as five balanced 24-bit digits.
+// v * 2^sh rounded to an integer (|v * 2^sh| < 2^116), as five balanced
+// 24-bit digits; bit operations only (fixacc.cuh's decode).
 __device__ __forceinline__ void dd_digits(double2 v, int sh, int d[5])
 {
 #pragma unroll
     for (int t = 0; t < 5; ++t) d[t] = 0;
-    if (v.x == 0.0) return;
-    const XF x = xfp::xf_from_dd(v.x, v.y);
-    const int r = -(x.e + sh);   // N = m * 2^-r; r >= 12 for in-range values
-    if (r >= 128 || r < 1) return;   // below one unit (or a non-finite row, handled by the epilogue)
-    unsigned __int128 N = (x.m >> r) + (unsigned __int128)((x.m >> (r - 1)) & 1);
+    const fx::Op o = fx::decode(v);
+    if (o.flags & (fx::kZero | fx::kBad)) return;   // non-finite rows are handled by the epilogue
+    const int r = -(o.e + sh);   // N = (x1:x0) * 2^-r; r >= 2 for in-range values
+    if (r >= 118 || r < 1) return;
+    const unsigned __int128 X = ((unsigned __int128)o.x1 << 64) | o.x0;
+    unsigned __int128 N = (X >> r) + (unsigned __int128)((X >> (r - 1)) & 1);
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
         int dt = (int)((uint32_t)N & 0xFFFFFFu);
@@ -65,7 +68,7 @@ __device__ __forceinline__ void dd_digits(double2 v, int sh, int d[5])
         d[t] = dt;
     }
     d[4] = (int)(uint32_t)N;
-    if (x.neg) {
+    if (o.flags & fx::kNeg) {
 #pragma unroll
         for (int t = 0; t < 5; ++t) d[t] = -d[t];
     }

@@ -87,20 +87,16 @@ __global__ void k_gemv_n_final(int64_t m, int nchunks, const double2 *part, dd::
 
 // ---- fixed-point kernels (mgemv_) ------------------------------------------------------
 
-__global__ void k_xf_convert(int64_t n, const double2 *x, int64_t incx, fx::XFPod *out)
+__global__ void k_op_convert(int64_t n, const double2 *x, int64_t incx, fx::OpPod *out)
 {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
-        const double2 v = x[vidx(j, n, incx)];
-        const bool ok = fx::finite_dd(v);
-        xfp::XF f = ok ? xfp::xf_from_dd(v.x, v.y) : xfp::XF{0, 0, false, true};
-        if (ok && v.x == 0.0) f.zero = true;
-        out[j] = fx::to_pod(f, !ok);
-    }
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        out[j] = fx::to_pod(fx::decode(x[vidx(j, n, incx)]));
 }
 
-// NoTrans partial sums: row per thread, columns [j0, j1) of chunk blockIdx.y.
+// NoTrans partial sums: row per thread, columns [j0, j1) of chunk blockIdx.y
+// (at most fx::kMaxAdds columns per chunk).
 __global__ void __launch_bounds__(256) k_gemv_n_fx(int64_t m, int64_t n, const double2 *__restrict__ A, int64_t lda,
-                                                  const fx::XFPod *__restrict__ xf, int64_t chunk,
+                                                  const fx::OpPod *__restrict__ xo, int64_t chunk,
                                                   fx::XFPod *__restrict__ part)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -112,18 +108,11 @@ __global__ void __launch_bounds__(256) k_gemv_n_fx(int64_t m, int64_t n, const d
     int64_t j = j0;
     for (; j + 2 <= j1; j += 2) {
         const double2 a0 = __ldcs(a + j * lda), a1 = __ldcs(a + (j + 1) * lda);
-        const fx::XFPod p0 = xf[j], p1 = xf[j + 1];
-        if (!fx::finite_dd(a0) || !fx::finite_dd(a1) || ((p0.flags | p1.flags) & 4)) acc.bad = true;
-        if (a0.x != 0.0 && !(p0.flags & 2)) acc.add(xfp::xf_mul(xfp::xf_from_dd(a0.x, a0.y), fx::from_pod(p0)));
-        if (a1.x != 0.0 && !(p1.flags & 2)) acc.add(xfp::xf_mul(xfp::xf_from_dd(a1.x, a1.y), fx::from_pod(p1)));
+        acc.add_prod(fx::decode(a0), fx::from_pod(xo[j]));
+        acc.add_prod(fx::decode(a1), fx::from_pod(xo[j + 1]));
     }
-    for (; j < j1; ++j) {
-        const double2 a0 = a[j * lda];
-        const fx::XFPod p0 = xf[j];
-        if (!fx::finite_dd(a0) || (p0.flags & 4)) acc.bad = true;
-        if (a0.x != 0.0 && !(p0.flags & 2)) acc.add(xfp::xf_mul(xfp::xf_from_dd(a0.x, a0.y), fx::from_pod(p0)));
-    }
-    part[blockIdx.y * m + i] = fx::to_pod(acc.bad ? xfp::XF{0, 0, false, true} : acc.finish(), acc.bad);
+    for (; j < j1; ++j) acc.add_prod(fx::decode(a[j * lda]), fx::from_pod(xo[j]));
+    part[blockIdx.y * m + i] = fx::to_pod(acc.finish(), acc.bad);
 }
 
 // y(i) := y(i) + alpha * sum_c part(c, i), one rounding to double-double.
@@ -164,9 +153,10 @@ __global__ void k_gemv_n_fx_final(int64_t m, int nchunks, const fx::XFPod *part,
     }
 }
 
-// Trans: block per column j of A (contiguous), threads over rows.
+// Trans: block per column j of A (contiguous), threads over rows; every
+// fx::kMaxAdds products a thread's accumulator is folded into an extended float.
 __global__ void __launch_bounds__(256) k_gemv_t_fx(int64_t m, int64_t n, const double2 *__restrict__ A, int64_t lda,
-                                                  const fx::XFPod *__restrict__ xf, dd::real alpha, double2 *y,
+                                                  const fx::OpPod *__restrict__ xo, dd::real alpha, double2 *y,
                                                   int64_t incy)
 {
     __shared__ fx::XFPod sh[8];
@@ -174,14 +164,23 @@ __global__ void __launch_bounds__(256) k_gemv_t_fx(int64_t m, int64_t n, const d
     const double2 *col = A + j * lda;
     fx::Acc acc;
     acc.reset();
+    xfp::XF total;
+    total.zero = true; total.neg = false; total.m = 0; total.e = 0;
+    bool bad = false;
+    int cnt = 0;
     for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
-        const double2 a0 = __ldcs(col + i);
-        const fx::XFPod p0 = xf[i];
-        if (!fx::finite_dd(a0) || (p0.flags & 4)) acc.bad = true;
-        if (a0.x != 0.0 && !(p0.flags & 2)) acc.add(xfp::xf_mul(xfp::xf_from_dd(a0.x, a0.y), fx::from_pod(p0)));
+        acc.add_prod(fx::decode(__ldcs(col + i)), fx::from_pod(xo[i]));
+        if (++cnt >= fx::kMaxAdds) {
+            bad |= acc.bad;
+            total = xfp::xf_add(total, acc.finish());
+            acc.reset();
+            cnt = 0;
+        }
     }
-    const bool bad = __syncthreads_or(acc.bad ? 1 : 0) != 0;
-    xfp::XF v = fx::xf_warp_sum(acc.bad ? xfp::XF{0, 0, false, true} : acc.finish());
+    bad |= acc.bad;
+    total = xfp::xf_add(total, acc.finish());
+    bad = __syncthreads_or(bad ? 1 : 0) != 0;
+    xfp::XF v = fx::xf_warp_sum(total);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) sh[wid] = fx::to_pod(v, false);
     __syncthreads();
@@ -210,23 +209,28 @@ bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A,
     if (alpha.hi == 0.0 && alpha.lo == 0.0) return true;
     dd::real al = dd::make(alpha.hi, alpha.lo);
     const int64_t lenx = trans ? m : n;
-    // x as extended floats (lenx * 24 bytes), then the partial sums
-    const size_t xf_bytes = ((size_t)lenx * sizeof(fx::XFPod) + 255) / 256 * 256;
+    // x as decoded operands (lenx * 24 bytes), then the partial sums
+    const size_t xf_bytes = ((size_t)lenx * sizeof(fx::OpPod) + 255) / 256 * 256;
     if (!trans) {
         int64_t rowblocks = (m + 255) / 256;
         int64_t want = 8 * (int64_t)sms;
         int64_t nchunks = (want + rowblocks - 1) / rowblocks;
+        if (nchunks < (n + fx::kMaxAdds - 1) / fx::kMaxAdds) nchunks = (n + fx::kMaxAdds - 1) / fx::kMaxAdds;
         if (nchunks > n) nchunks = n;
-        if (nchunks > 4096) nchunks = 4096;
         if (nchunks < 1) nchunks = 1;
         int64_t chunk = (n + nchunks - 1) / nchunks;
         nchunks = (n + chunk - 1) / chunk;
+        if (nchunks > 65535) {
+            set_error(routine, MWBLAS_ERR_UNSUPPORTED, "n too large for the no-transpose GEMV grid");
+            return false;
+        }
         char *buf = (char *)dev_alloc(xf_bytes + sizeof(fx::XFPod) * (size_t)(nchunks * m), routine);
         if (!buf) return false;
-        fx::XFPod *xf = (fx::XFPod *)buf, *part = (fx::XFPod *)(buf + xf_bytes);
+        fx::OpPod *xf = (fx::OpPod *)buf;
+        fx::XFPod *part = (fx::XFPod *)(buf + xf_bytes);
         int64_t cb = (n + 255) / 256;
         if (cb > sms * 8) cb = sms * 8;
-        k_xf_convert<<<(unsigned)cb, 256, 0, stream()>>>(n, (const double2 *)x, incx, xf);
+        k_op_convert<<<(unsigned)cb, 256, 0, stream()>>>(n, (const double2 *)x, incx, xf);
         dim3 grid((unsigned)rowblocks, (unsigned)nchunks);
         k_gemv_n_fx<<<grid, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, xf, chunk, part);
         int64_t fb = (m + 255) / 256;
@@ -235,11 +239,11 @@ bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A,
         count_launch(3);
         dev_free(buf);
     } else {
-        fx::XFPod *xf = (fx::XFPod *)dev_alloc(xf_bytes, routine);
+        fx::OpPod *xf = (fx::OpPod *)dev_alloc(xf_bytes, routine);
         if (!xf) return false;
         int64_t cb = (m + 255) / 256;
         if (cb > sms * 8) cb = sms * 8;
-        k_xf_convert<<<(unsigned)cb, 256, 0, stream()>>>(m, (const double2 *)x, incx, xf);
+        k_op_convert<<<(unsigned)cb, 256, 0, stream()>>>(m, (const double2 *)x, incx, xf);
         k_gemv_t_fx<<<(unsigned)n, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, xf, al, (double2 *)y, incy);
         count_launch(2);
         dev_free(xf);

@@ -343,6 +343,16 @@ __global__ void __launch_bounds__(kThreads) k_mdot_partial(int64_t n, const doub
 {
     fx::Acc acc;
     acc.reset();
+    fx::XF total;   // accumulators are folded in here every kMaxAdds products
+    total.zero = true; total.neg = false; total.m = 0; total.e = 0;
+    bool bad = false;
+    int cnt = 0;
+    auto fold = [&]() {
+        bad |= acc.bad;
+        total = xfp::xf_add(total, acc.finish());
+        acc.reset();
+        cnt = 0;
+    };
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (incx == 1 && incy == 1) {
@@ -350,18 +360,18 @@ __global__ void __launch_bounds__(kThreads) k_mdot_partial(int64_t n, const doub
         for (; i + stride < n; i += 2 * stride) {
             const double2 x0 = __ldcs(x + i), y0 = __ldcs(y + i);
             const double2 x1 = __ldcs(x + i + stride), y1 = __ldcs(y + i + stride);
-            if (!fx::finite_dd(x0) || !fx::finite_dd(y0) || !fx::finite_dd(x1) || !fx::finite_dd(y1)) acc.bad = true;
-            acc.add_dd_product(x0.x, x0.y, y0.x, y0.y);
-            acc.add_dd_product(x1.x, x1.y, y1.x, y1.y);
+            acc.add_prod(fx::decode(x0), fx::decode(y0));
+            acc.add_prod(fx::decode(x1), fx::decode(y1));
+            if ((cnt += 2) >= fx::kMaxAdds) fold();
         }
     }
     for (; i < n; i += stride) {
-        const double2 xv = x[vidx(i, n, incx)], yv = y[vidx(i, n, incy)];
-        if (!fx::finite_dd(xv) || !fx::finite_dd(yv)) acc.bad = true;
-        acc.add_dd_product(xv.x, xv.y, yv.x, yv.y);
+        acc.add_prod(fx::decode(x[vidx(i, n, incx)]), fx::decode(y[vidx(i, n, incy)]));
+        if (++cnt >= fx::kMaxAdds) fold();
     }
-    const bool bad = block_any(acc.bad);
-    fx::XF v = xf_block_sum(acc.bad ? fx::XF{0, 0, false, true} : acc.finish());
+    fold();
+    bad = block_any(bad);
+    fx::XF v = xf_block_sum(total);
     if (threadIdx.x == 0) part[blockIdx.x] = fx::to_pod(v, bad);
 }
 

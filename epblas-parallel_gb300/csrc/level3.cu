@@ -119,18 +119,18 @@ constexpr int kInvNB = 64;
 __global__ void __launch_bounds__(kInvNB) k_trsm_diag_inv(int64_t na, const double2 *__restrict__ A, int64_t lda,
                                                           bool trans, bool lower, bool unit, double2 *Inv)
 {
-    extern __shared__ fx::XFPod smem_inv[];
-    fx::XFPod *sA = smem_inv;                    // [p][r]: sA[p * 64 + r] = op(A)(o + r, o + p)
-    fx::XFPod *sX = smem_inv + kInvNB * kInvNB;  // [r][c]: x_c(r)
+    extern __shared__ fx::OpPod smem_inv[];
+    fx::OpPod *sA = smem_inv;                    // [p][r]: sA[p * 64 + r] = -op(A)(o + r, o + p)
+    fx::OpPod *sX = smem_inv + kInvNB * kInvNB;  // [r][c]: x_c(r)
     __shared__ double2 sInvDiag[kInvNB];
     const int64_t o = (int64_t)blockIdx.x * kInvNB;
     const int nb = (int)min((int64_t)kInvNB, na - o);
     for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
         const int r = idx % nb, c = idx / nb;
         const dd::real v = opA(A, lda, trans, o + r, o + c);
-        xfp::XF f = xfp::xf_from_dd(v.hi, v.lo);
-        if (v.hi == 0.0) f.zero = true;
-        sA[c * kInvNB + r] = fx::to_pod(f, false);
+        fx::Op d = fx::decode(make_double2(v.hi, v.lo));
+        d.flags ^= fx::kNeg;   // the substitution subtracts
+        sA[c * kInvNB + r] = fx::to_pod(d);
     }
     for (int r = threadIdx.x; r < nb; r += blockDim.x) {
         const dd::real d = opA(A, lda, trans, o + r, o + r);
@@ -140,35 +140,19 @@ __global__ void __launch_bounds__(kInvNB) k_trsm_diag_inv(int64_t na, const doub
     __syncthreads();
     const int c = threadIdx.x;
     if (c >= nb) return;
+    const fx::Op one = fx::decode(make_double2(1.0, 0.0));
     double2 *out = Inv + (int64_t)blockIdx.x * kInvNB * kInvNB + (int64_t)c * kInvNB;
     for (int s = 0; s < nb; ++s) {
         const int r = lower ? s : nb - 1 - s;
         fx::Acc acc;
         acc.reset();
-        if (r == c) {
-            xfp::XF one;
-            one.m = (unsigned __int128)1 << 127;
-            one.e = -127;
-            one.neg = false;
-            one.zero = false;
-            acc.add(one);
-        }
+        if (r == c) acc.add_prod(one, one);
         const int p0 = lower ? 0 : r + 1, p1 = lower ? r : nb;
-        for (int p = p0; p < p1; ++p) {
-            const fx::XFPod xp = sX[p * kInvNB + c];
-            if (xp.flags & 2) continue;
-            const fx::XFPod ap = sA[p * kInvNB + r];
-            if (ap.flags & 2) continue;
-            xfp::XF t = xfp::xf_mul(fx::from_pod(ap), fx::from_pod(xp));
-            t.neg = !t.neg;
-            acc.add(t);
-        }
+        for (int p = p0; p < p1; ++p) acc.add_prod(fx::from_pod(sA[p * kInvNB + r]), fx::from_pod(sX[p * kInvNB + c]));
         double h, l;
         xfp::xf_to_dd(acc.finish(), h, l);
-        dd::real v = dd::mul_fast(dd::make(h, l), dd::load(&sInvDiag[r]));
-        xfp::XF f = xfp::xf_from_dd(v.hi, v.lo);
-        if (v.hi == 0.0) f.zero = true;
-        sX[r * kInvNB + c] = fx::to_pod(f, false);
+        const dd::real v = dd::mul_fast(dd::make(h, l), dd::load(&sInvDiag[r]));
+        sX[r * kInvNB + c] = fx::to_pod(fx::decode(make_double2(v.hi, v.lo)));
         out[r] = make_double2(v.hi, v.lo);
     }
 }
@@ -378,7 +362,7 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
         if (!scratch) return false;
         w.inv = (const double2 *)scratch;
         w.T = (double2 *)((char *)scratch + inv_bytes);
-        const size_t smem = 2 * (size_t)kInvNB * kInvNB * sizeof(fx::XFPod);
+        const size_t smem = 2 * (size_t)kInvNB * kInvNB * sizeof(fx::OpPod);
         cudaFuncSetAttribute(k_trsm_diag_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_trsm_diag_inv<<<(unsigned)nblk, kInvNB, smem, stream()>>>(na, (const double2 *)A, lda, trans, lower,
                                                                    unit, (double2 *)scratch);
