@@ -4,14 +4,16 @@
 // mgemm_parallel.cpp:53-60).
 //
 // mgemm_grouped: one persistent kernel over all instances. The work list is
-// every (instance, 16x16 output tile, K split); CTAs of 64 threads pull items
+// every (instance, 32x32 output tile, K split); CTAs of 256 threads pull items
 // from an atomic counter, so thousands of uneven instances keep all SMs busy.
-// Each item runs the FP64 extraction accumulation of the plain engine
-// (gemm_plain.cu), with sigma taken from an exponent scan of the item's own A
-// rows / B columns over its K range (no pre-pass, no extra scratch). Items of
-// a split instance write partial tiles; the CTA that completes a tile's last
-// split sums the partials in split order (deterministic) and applies
-// alpha/beta. The per-call state (descriptors, work counter, split counters,
+// Each item runs the fixed-point arithmetic of the integer-pipe engine
+// (gemm_fixed.cu, fixgemm.cuh): its A rows / B columns are scaled from an
+// exponent scan over the item's own K range (no pre-pass, no extra scratch),
+// converted to balanced 24-bit digits while staged, and multiplied with
+// exact 64-bit column sums. Items of a split instance write partial tiles as
+// extended floats; the CTA that completes a tile's last split sums the
+// partials in split order (deterministic) and applies alpha/beta with one
+// rounding. The per-call state (descriptors, work counter, split counters,
 // partial tiles) is uploaded and the kernel launched from a CUDA graph that is
 // captured once per batch layout and replayed.
 //
@@ -30,6 +32,7 @@
 #include <vector>
 
 #include "dd.cuh"
+#include "fixgemm.cuh"
 #include "level3.h"
 #include "runtime.h"
 
@@ -38,10 +41,9 @@ namespace mw {
 namespace {
 
 constexpr int kNoExp = -30000;
-constexpr int GT = 16;        // output tile edge
-constexpr int GTHREADS = 64;  // 8 x 8 threads, 2 x 2 outputs each
-constexpr int GBK = 8;        // k-slab
-constexpr int GKB = 8;        // fold interval (k steps)
+constexpr int GT = 32;         // output tile edge
+constexpr int GTHREADS = 256;  // 16 x 16 threads, 2 x 2 outputs each
+constexpr int GBK = 8;         // k-slab
 
 struct GemmDesc {
     const double2 *A, *B;
@@ -65,13 +67,6 @@ __device__ __forceinline__ int exp_bound(double x)
     return (int)(b >> 52) - 1023;
 }
 
-__device__ __forceinline__ double sigma_of(int ea, int eb, int shift)
-{
-    int e = (ea <= kNoExp / 2 || eb <= kNoExp / 2) ? -1000 : ea + eb + shift;
-    e = max(-1000, min(1000, e));
-    return __longlong_as_double((long long)(((uint64_t)(e + 1023) << 52) | (1ull << 51)));
-}
-
 __device__ __forceinline__ double2 opA_at(const GemmDesc &d, int64_t i, int64_t p)
 {
     return d.ta ? d.A[p + i * d.lda] : d.A[i + p * d.lda];
@@ -83,14 +78,14 @@ __device__ __forceinline__ double2 opB_at(const GemmDesc &d, int64_t p, int64_t 
 
 __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__restrict__ descs, int count,
                                                           int64_t total, unsigned long long *work_counter,
-                                                          int *tile_counters, double2 *partials)
+                                                          int *tile_counters, fx::XFPod *partials)
 {
-    __shared__ double2 sA[GBK][GT], sB[GBK][GT];
+    __shared__ __align__(16) int sA[GBK][5][GT], sB[GBK][5][GT];
     __shared__ int s_ea[GT], s_eb[GT];
     __shared__ long long s_item;
     __shared__ int s_last;
     const int tid = threadIdx.x;
-    const int tx = tid % 8, ty = tid / 8;   // rows tx, tx+8 ; cols ty, ty+8
+    const int tx = tid & 15, ty = tid >> 4;   // rows 2tx, 2tx+1; columns 2ty, 2ty+1
     for (;;) {
         if (tid == 0) s_item = (long long)atomicAdd(work_counter, 1ull);
         __syncthreads();
@@ -115,106 +110,99 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__res
         // exponent bounds of the tile's rows / columns over [k0, k1)
         if (tid < GT) {
             int e = kNoExp;
-            int64_t i = i0 + tid;
+            const int64_t i = i0 + tid;
             if (i < d.m)
                 for (int64_t p = k0; p < k1; ++p) e = max(e, exp_bound(opA_at(d, i, p).x));
             s_ea[tid] = e;
         } else if (tid < 2 * GT) {
             int e = kNoExp;
-            int64_t j = j0 + (tid - GT);
+            const int64_t j = j0 + (tid - GT);
             if (j < d.n)
                 for (int64_t p = k0; p < k1; ++p) e = max(e, exp_bound(opB_at(d, p, j).x));
             s_eb[tid - GT] = e;
         }
         __syncthreads();
-        const int64_t kl = k1 - k0;
-        int terms = (int)(kl < GKB ? kl : GKB);
-        int lg = 0;
-        while ((1 << lg) < terms) ++lg;
-        // sigma binade and second extraction level as in the plain engine
-        // (gemm_plain.cu): shift = lg + 3, X2 for instances with k <= 64.
-        const int shift = lg + 3;
-        const bool comp = d.k <= 64;
-        double X[2][2], X2[2][2], L[2][2], Ah[2][2], Al[2][2];
+
+        long long acc[2][2][5];
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+                for (int q = 0; q < 5; ++q) acc[a][b][q] = 0;
+
+        for (int64_t kk = k0; kk < k1; kk += GBK) {
+            // stage one element of the A tile and one of the B tile per thread
+            // as digits (GT * GBK == GTHREADS)
+            static_assert(GT * GBK == GTHREADS, "one staged element per thread");
+            {
+                const int idx = tid;
+                int dg[5];
+                {
+                    int r, p;
+                    if (!d.ta) { r = idx % GT; p = idx / GT; }
+                    else       { p = idx % GBK; r = idx / GBK; }
+                    const int64_t gi = i0 + r, gp = kk + p;
+                    const double2 v = (gp < k1 && gi < d.m) ? opA_at(d, gi, gp) : make_double2(0.0, 0.0);
+                    const int e = s_ea[r];
+                    fxg::dd_digits(v, (e <= kNoExp / 2 || e >= 1024) ? -100000 : fxg::FX_S - e, dg);
+#pragma unroll
+                    for (int t = 0; t < 5; ++t) sA[p][t][r] = dg[t];
+                }
+                {
+                    int c, p;
+                    if (!d.tb) { p = idx % GBK; c = idx / GBK; }
+                    else       { c = idx % GT; p = idx / GT; }
+                    const int64_t gj = j0 + c, gp = kk + p;
+                    const double2 v = (gp < k1 && gj < d.n) ? opB_at(d, gp, gj) : make_double2(0.0, 0.0);
+                    const int e = s_eb[c];
+                    fxg::dd_digits(v, (e <= kNoExp / 2 || e >= 1024) ? -100000 : fxg::FX_S - e, dg);
+#pragma unroll
+                    for (int t = 0; t < 5; ++t) sB[p][t][c] = dg[t];
+                }
+            }
+            __syncthreads();
+#pragma unroll 2
+            for (int p = 0; p < GBK; ++p) {
+                int da[2][5], db[2][5];
+#pragma unroll
+                for (int t = 0; t < 5; ++t) {
+                    const int2 va = *reinterpret_cast<const int2 *>(&sA[p][t][2 * tx]);
+                    const int2 vb = *reinterpret_cast<const int2 *>(&sB[p][t][2 * ty]);
+                    da[0][t] = va.x; da[1][t] = va.y;
+                    db[0][t] = vb.x; db[1][t] = vb.y;
+                }
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < 2; ++b) fxg::mac_digits(acc[a][b], da[a], db[b]);
+            }
+            __syncthreads();
+        }
+
+        // the 2 x 2 outputs as extended floats (non-finite rows/columns flagged)
+        xfp::XF v[2][2];
+        bool badv[2][2];
 #pragma unroll
         for (int a = 0; a < 2; ++a)
 #pragma unroll
             for (int b = 0; b < 2; ++b) {
-                X[a][b] = sigma_of(s_ea[tx + 8 * a], s_eb[ty + 8 * b], shift);
-                X2[a][b] = sigma_of(s_ea[tx + 8 * a], s_eb[ty + 8 * b], 2 * shift - 54);
-                L[a][b] = Ah[a][b] = Al[a][b] = 0.0;
-            }
-        int since = 0;
-        for (int64_t kk = k0; kk < k1; kk += GBK) {
-            for (int idx = tid; idx < GT * GBK; idx += GTHREADS) {
-                int r = idx % GT, p = idx / GT;
-                int64_t gp = kk + p;
-                double2 va = make_double2(0.0, 0.0), vb = va;
-                if (gp < k1) {
-                    if (i0 + r < d.m) va = opA_at(d, i0 + r, gp);
-                    if (j0 + r < d.n) vb = opB_at(d, gp, j0 + r);
+                const int ei = s_ea[2 * tx + a], ej = s_eb[2 * ty + b];
+                badv[a][b] = ei >= 1024 || ej >= 1024;
+                if (badv[a][b] || ei <= kNoExp / 2 || ej <= kNoExp / 2) {
+                    v[a][b].zero = true; v[a][b].neg = false; v[a][b].m = 0; v[a][b].e = 0;
+                } else {
+                    v[a][b] = fxg::sums_to_xf(acc[a][b], ei, ej);
                 }
-                sA[p][r] = va;
-                sB[p][r] = vb;
             }
-            __syncthreads();
-#pragma unroll
-            for (int p = 0; p < GBK; ++p) {
-                double2 av[2] = {sA[p][tx], sA[p][tx + 8]};
-                double2 bv[2] = {sB[p][ty], sB[p][ty + 8]};
-#pragma unroll
-                for (int a = 0; a < 2; ++a)
-#pragma unroll
-                    for (int b = 0; b < 2; ++b) {
-                        double t = __fma_rn(av[a].x, bv[b].x, X[a][b]);
-                        double q = __dsub_rn(X[a][b], t);
-                        double r = __fma_rn(av[a].x, bv[b].x, q);
-                        X[a][b] = t;
-                        if (comp) {
-                            double t2 = __dadd_rn(X2[a][b], r);
-                            double q2 = __dsub_rn(X2[a][b], t2);
-                            r = __dadd_rn(q2, r);
-                            X2[a][b] = t2;
-                        }
-                        double l = __dadd_rn(L[a][b], r);
-                        l = __fma_rn(av[a].x, bv[b].y, l);
-                        L[a][b] = __fma_rn(av[a].y, bv[b].x, l);
-                    }
-            }
-            __syncthreads();
-            since += GBK;
-            if (since == GKB || kk + GBK >= k1) {
-                since = 0;
-#pragma unroll
-                for (int a = 0; a < 2; ++a)
-#pragma unroll
-                    for (int b = 0; b < 2; ++b) {
-                        double sg = sigma_of(s_ea[tx + 8 * a], s_eb[ty + 8 * b], shift);
-                        double s = __dsub_rn(X[a][b], sg);
-                        double lsum = L[a][b];
-                        if (comp) {
-                            double sg2 = sigma_of(s_ea[tx + 8 * a], s_eb[ty + 8 * b], 2 * shift - 54);
-                            lsum = __dadd_rn(lsum, __dsub_rn(X2[a][b], sg2));
-                            X2[a][b] = sg2;
-                        }
-                        double h, e;
-                        dd::two_sum(Ah[a][b], s, h, e);
-                        double lo2 = __dadd_rn(Al[a][b], __dadd_rn(e, lsum));
-                        dd::fast_two_sum(h, lo2, Ah[a][b], Al[a][b]);
-                        X[a][b] = sg;
-                        L[a][b] = 0.0;
-                    }
-            }
-        }
 
-        const dd::real alpha = dd::make(d.alpha.x, d.alpha.y), beta = dd::make(d.beta.x, d.beta.y);
         if (d.splitk > 1) {
             // write this split's partial tile, then let the last split finish
-            double2 *pt = partials + (d.part_begin + tile * d.splitk + split) * (GT * GT);
+            fx::XFPod *pt = partials + (d.part_begin + tile * d.splitk + split) * (GT * GT);
 #pragma unroll
             for (int a = 0; a < 2; ++a)
 #pragma unroll
-                for (int b = 0; b < 2; ++b) pt[(ty + 8 * b) * GT + tx + 8 * a] = make_double2(Ah[a][b], Al[a][b]);
+                for (int b = 0; b < 2; ++b) pt[(2 * ty + b) * GT + 2 * tx + a] = fx::to_pod(v[a][b], badv[a][b]);
             __threadfence();
             __syncthreads();
             if (tid == 0) {
@@ -224,40 +212,48 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__res
             __syncthreads();
             if (!s_last) continue;
             __threadfence();
+            const fx::XFPod *base = partials + (d.part_begin + tile * d.splitk) * (GT * GT);
 #pragma unroll
             for (int a = 0; a < 2; ++a)
 #pragma unroll
                 for (int b = 0; b < 2; ++b) {
-                    const double2 *base = partials + (d.part_begin + tile * d.splitk) * (GT * GT);
-                    // partials written by other CTAs: read through L2
-                    double2 v = __ldcg(base + (ty + 8 * b) * GT + tx + 8 * a);
-                    dd::real acc = dd::make(v.x, v.y);
-                    for (int s2 = 1; s2 < d.splitk; ++s2) {
-                        v = __ldcg(base + (int64_t)s2 * GT * GT + (ty + 8 * b) * GT + tx + 8 * a);
-                        acc = dd::add_fast(acc, dd::make(v.x, v.y));
+                    xfp::XF sum;
+                    sum.zero = true; sum.neg = false; sum.m = 0; sum.e = 0;
+                    bool bad = false;
+                    for (int s2 = 0; s2 < d.splitk; ++s2) {
+                        // partials written by other CTAs: read through L2
+                        const fx::XFPod *q = base + (int64_t)s2 * GT * GT + (2 * ty + b) * GT + 2 * tx + a;
+                        fx::XFPod pv;
+                        pv.hi = __ldcg(&q->hi);
+                        pv.lo = __ldcg(&q->lo);
+                        pv.e = __ldcg(&q->e);
+                        pv.flags = __ldcg(&q->flags);
+                        bad |= (pv.flags & 4) != 0;
+                        sum = xfp::xf_add(sum, fx::from_pod(pv));
                     }
-                    Ah[a][b] = acc.hi;
-                    Al[a][b] = acc.lo;
+                    v[a][b] = sum;
+                    badv[a][b] = bad;
                 }
             if (tid == 0) tile_counters[d.tile_begin + tile] = 0;   // ready for the next replay
         }
+        const dd::real beta = dd::make(d.beta.x, d.beta.y);
+        const xfp::XF xa = xfp::xf_from_dd(d.alpha.x, d.alpha.y), xb = xfp::xf_from_dd(d.beta.x, d.beta.y);
+        const bool alpha_one = d.alpha.x == 1.0 && d.alpha.y == 0.0;
 #pragma unroll
         for (int b = 0; b < 2; ++b) {
-            int64_t j = j0 + ty + 8 * b;
+            const int64_t j = j0 + 2 * ty + b;
             if (j >= d.n) continue;
 #pragma unroll
             for (int a = 0; a < 2; ++a) {
-                int64_t i = i0 + tx + 8 * a;
+                const int64_t i = i0 + 2 * tx + a;
                 if (i >= d.m) continue;
-                dd::real r = dd::mul_fast(alpha, dd::make(Ah[a][b], Al[a][b]));
                 double2 *pc = d.C + i + j * d.ldc;
-                if (d.beta_kind == 0) {
-                    dd::store(pc, r);
-                } else {
-                    dd::real c0 = dd::load(pc);
-                    if (d.beta_kind == 2) c0 = dd::mul_exact(c0, beta);
-                    dd::store(pc, dd::add_exact(c0, r));
+                if (badv[a][b]) {
+                    const double qnan = __longlong_as_double(0x7ff8000000000000ll);
+                    *pc = make_double2(qnan, qnan);
+                    continue;
                 }
+                fxg::store_axpby(pc, v[a][b], xa, alpha_one, xb, beta, d.beta_kind);
             }
         }
     }
@@ -432,6 +428,9 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
         d.splitk = 1;
         if (pol.min_k_per_split > 0 && tiles <= pol.max_tiles_split && d.k >= 2 * pol.min_k_per_split)
             d.splitk = std::min(16, d.k / pol.min_k_per_split);
+        // the digit column sums hold at most 16384 multiply-adds per split
+        const int need_splits = (d.k + 16383) / 16384;
+        if (d.splitk < need_splits) d.splitk = need_splits;
         d.klen = d.splitk > 1 ? ((d.k + d.splitk - 1) / d.splitk + GBK - 1) / GBK * GBK : std::max(d.k, 1);
         if (d.k == 0) d.klen = 1;
         d.work_begin = work;
@@ -446,7 +445,7 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
     }
     pl.total = work;
     pl.split_tiles = stiles;
-    pl.partial_elems = pslots * GT * GT;
+    pl.partial_elems = pslots * GT * GT;   // extended-float partials
 }
 
 uint64_t plan_key(const Plan &pl)
@@ -466,7 +465,7 @@ bool prepare_and_launch(Plan &pl, const char *routine)
     if (pl.descs.empty() || pl.total == 0) return true;
     const size_t d_bytes = pl.descs.size() * sizeof(GemmDesc);
     const size_t cnt_bytes = 256 + (size_t)(pl.split_tiles + 1) * sizeof(int);
-    const size_t part_bytes = (size_t)pl.partial_elems * sizeof(double2);
+    const size_t part_bytes = (size_t)pl.partial_elems * sizeof(fx::XFPod);
     const size_t need = d_bytes + cnt_bytes + part_bytes + 512;
     const uint64_t key = plan_key(pl);
     cudaStream_t s = stream();
@@ -490,7 +489,7 @@ bool prepare_and_launch(Plan &pl, const char *routine)
     GemmDesc *ddesc = (GemmDesc *)base;
     unsigned long long *counter = (unsigned long long *)(base + cnt_off);
     int *tile_counters = (int *)(counter + 32);
-    double2 *partials = (double2 *)(base + part_off);
+    fx::XFPod *partials = (fx::XFPod *)(base + part_off);
     const int sms = device_sm_count();
     const int grid = (int)std::min<int64_t>(pl.total, (int64_t)sms * 16);
     if (pl.key != key) {

@@ -3,19 +3,22 @@
 //
 // On this part an FP64 instruction issues at ~1/40 of the integer rate, so a
 // double-double multiply-add on the FP64 pipe (12 instructions) cannot keep
-// up with HBM. Here everything is integer work on the bit patterns:
+// up with HBM. The 64-bit multiply-high (IMAD.HI) also issues at the FP64
+// rate here, so only 32 x 32 -> 64-bit multiply-adds (IMAD.WIDE) are used:
 //
 //  * decode: a double-double (hi, lo) becomes |hi + lo| = (x1:x0) * 2^e with
 //    x1 < 2^54 holding hi's mantissa and x0 the 64 bits below it (lo's
 //    mantissa shifted into place, added or subtracted): the exact value to
 //    2^-117, from shifts and adds only;
-//  * product: Q = floor(|a| |b| / 2^64), three 64 x 64 -> 128-bit products
-//    (the dropped x0*y0 term is below 2^-106 of the product's top), Q < 2^172;
-//  * accumulate: Q is shifted to the accumulator's block exponent and added
-//    into a 192-bit two's complement integer; when a product would reach above
-//    the 12-bit headroom the block exponent moves up (a right shift, rare after
-//    the first terms). At most 4096 products per accumulator (callers size
-//    their grids for it).
+//  * accumulate: each thread keeps a block exponent B. For a product x*y the
+//    integer X is shifted right to the block (X' = X >> (B - ex - ey)) so that
+//    X' * Y lands at 2^B; X' and Y are split into five 24-bit digits and the
+//    19 digit products of weight >= 2^72 are added with IMAD.WIDE into six
+//    64-bit column sums that persist across products (no per-product
+//    alignment of the result). The dropped products are below 2^-130 of the
+//    block. Every 2048 products the column carries are propagated; a product
+//    above the block's headroom moves B up (a right shift of the whole sum,
+//    rare after the first terms).
 //
 // Sums of accumulators (warp, block, grid) use the 128-bit extended-float
 // addition of xfloat.cuh in a fixed order, so results are deterministic.
@@ -29,7 +32,7 @@ namespace fx {
 
 using xfp::XF;
 
-constexpr int kMaxAdds = 4096;   // products per accumulator (12-bit headroom)
+constexpr int kMaxAdds = 1 << 20;   // products per accumulator before it is folded into an extended float
 
 enum : uint32_t { kNeg = 1, kZero = 2, kBad = 4 };
 
@@ -93,108 +96,198 @@ __device__ __forceinline__ Op decode(double2 v)
     return o;
 }
 
+// 256-bit two's complement accumulation of x * 2^s (x signed, s < 128).
+__device__ __forceinline__ void add_shifted(uint64_t W[4], int64_t x, int s)
+{
+    const uint64_t ext = x < 0 ? ~0ull : 0ull;
+    const int b = s & 63;
+    uint64_t v[4];
+    const uint64_t lo = (uint64_t)x << b;
+    const uint64_t hi = b ? (((uint64_t)x >> (64 - b)) | (ext << b)) : ext;
+    if (s < 64) {
+        v[0] = lo; v[1] = hi; v[2] = ext; v[3] = ext;
+    } else {
+        v[0] = 0; v[1] = lo; v[2] = hi; v[3] = ext;
+    }
+    asm("add.cc.u64 %0, %0, %4;\n\t"
+        "addc.cc.u64 %1, %1, %5;\n\t"
+        "addc.cc.u64 %2, %2, %6;\n\t"
+        "addc.u64 %3, %3, %7;"
+        : "+l"(W[0]), "+l"(W[1]), "+l"(W[2]), "+l"(W[3])
+        : "l"(v[0]), "l"(v[1]), "l"(v[2]), "l"(v[3]));
+}
+
+// W * 2^e as an extended float (W two's complement, 256 bits).
+__device__ __forceinline__ XF w256_to_xf(uint64_t W[4], int e)
+{
+    XF r;
+    r.neg = (int64_t)W[3] < 0;
+    if (r.neg) {
+        asm("sub.cc.u64 %0, 0, %0;\n\t"
+            "subc.cc.u64 %1, 0, %1;\n\t"
+            "subc.cc.u64 %2, 0, %2;\n\t"
+            "subc.u64 %3, 0, %3;"
+            : "+l"(W[0]), "+l"(W[1]), "+l"(W[2]), "+l"(W[3]));
+    }
+    int top = 3;
+    while (top > 0 && W[top] == 0) --top;
+    if (W[top] == 0) {
+        r.zero = true; r.neg = false; r.m = 0; r.e = 0;
+        return r;
+    }
+    const int z = xfp::clz64(W[top]);
+    const uint64_t w1 = W[top], w0 = top >= 1 ? W[top - 1] : 0, wm = top >= 2 ? W[top - 2] : 0;
+    unsigned __int128 m = ((unsigned __int128)w1 << 64) | w0;
+    if (z) m = (m << z) | (wm >> (64 - z));
+    r.m = m;
+    r.e = e + 64 * (top - 1) - z;
+    r.zero = false;
+    return r;
+}
+
+// Five unsigned 24-bit digits of a 120-bit integer (x1:x0), least significant first.
+__device__ __forceinline__ void digits24(uint64_t x1, uint64_t x0, int d[5])
+{
+    d[0] = (int)(x0 & 0xFFFFFFu);
+    d[1] = (int)((x0 >> 24) & 0xFFFFFFu);
+    d[2] = (int)(((x0 >> 48) | (x1 << 16)) & 0xFFFFFFu);
+    d[3] = (int)((x1 >> 8) & 0xFFFFFFu);
+    d[4] = (int)((x1 >> 32) & 0xFFFFFFu);
+}
+
+// y pre-split for repeated use (GEMV's x vector): Y's digits, exponent, flags.
+struct Dig {
+    int d[5];
+    int e;
+    uint32_t flags;
+    int pad;
+};
+
+__device__ __forceinline__ Dig to_dig(const Op &o)
+{
+    Dig g;
+    digits24(o.x1, o.x0, g.d);
+    g.e = o.e;
+    g.flags = o.flags;
+    g.pad = 0;
+    return g;
+}
+
 struct Acc {
-    uint64_t w0, w1, w2;   // value = W * 2^lsb, W two's complement
-    int lsb;
+    long long c[6];   // column q has weight 2^(24(q+3) + B)
+    int B;
+    int cnt;
     bool init;
     bool bad;
 
     __device__ __forceinline__ void reset()
     {
-        w0 = w1 = w2 = 0;
-        lsb = 0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) c[q] = 0;
+        B = 0;
+        cnt = 0;
         init = false;
         bad = false;
     }
 
-    __device__ __forceinline__ void shift_right(int d)
+    // carries up: columns 0..4 end in [0, 2^24)
+    __device__ __forceinline__ void normalize()
     {
-        // arithmetic shift of the 192-bit W by d >= 1
-        const uint64_t sgn = (uint64_t)((int64_t)w2 >> 63);
-        if (d >= 192) {
-            w0 = w1 = w2 = 0;   // all earlier terms lie below the new resolution
-            return;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            const long long carry = c[q] >> 24;
+            c[q] -= carry << 24;
+            c[q + 1] += carry;
         }
-        while (d >= 64) {
-            w0 = w1;
-            w1 = w2;
-            w2 = sgn;
-            d -= 64;
-        }
-        if (d) {
-            w0 = (w0 >> d) | (w1 << (64 - d));
-            w1 = (w1 >> d) | (w2 << (64 - d));
-            w2 = (uint64_t)((int64_t)w2 >> d);
-        }
+        cnt = 0;
     }
 
-    // W += +-(q2:q1:q0) * 2^(eq - lsb), q < 2^172
-    __device__ __forceinline__ void add_q(uint64_t q0, uint64_t q1, uint64_t q2, int eq, bool neg)
+    // the sum as a 256-bit integer W with value W * 2^(B + 72)
+    __device__ __forceinline__ void to_w256(uint64_t W[4]) const
     {
-        if (!init) {
-            lsb = eq - 4;
-            init = true;
-        }
-        int s = eq - lsb;
-        if (s > 8) {   // keep Q's top (bit 171 + s) at or below bit 179
-            shift_right(s - 4);
-            lsb += s - 4;
-            s = 4;
-        }
-        uint64_t v0, v1, v2;
-        if (s >= 0) {
-            v0 = q0 << s;
-            v1 = s ? ((q1 << s) | (q0 >> (64 - s))) : q1;
-            v2 = s ? ((q2 << s) | (q1 >> (64 - s))) : q2;
-        } else {
-            const int r = -s;
-            if (r >= 172) return;   // below the accumulator's resolution
-            const int ws = r >> 6, b = r & 63;
-            const uint64_t a0 = ws == 0 ? q0 : (ws == 1 ? q1 : q2);
-            const uint64_t a1 = ws == 0 ? q1 : (ws == 1 ? q2 : 0);
-            const uint64_t a2 = ws == 0 ? q2 : 0;
-            v0 = b ? ((a0 >> b) | (a1 << (64 - b))) : a0;
-            v1 = b ? ((a1 >> b) | (a2 << (64 - b))) : a1;
-            v2 = a2 >> b;
-        }
-        if (neg) {
-            asm("sub.cc.u64 %0, %0, %3;\n\t"
-                "subc.cc.u64 %1, %1, %4;\n\t"
-                "subc.u64 %2, %2, %5;"
-                : "+l"(w0), "+l"(w1), "+l"(w2)
-                : "l"(v0), "l"(v1), "l"(v2));
-        } else {
-            asm("add.cc.u64 %0, %0, %3;\n\t"
-                "addc.cc.u64 %1, %1, %4;\n\t"
-                "addc.u64 %2, %2, %5;"
-                : "+l"(w0), "+l"(w1), "+l"(w2)
-                : "l"(v0), "l"(v1), "l"(v2));
-        }
+        W[0] = W[1] = W[2] = W[3] = 0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) add_shifted(W, c[q], 24 * q);
     }
 
-    // += a * b (decoded operands)
-    __device__ __forceinline__ void add_prod(const Op &a, const Op &b)
+    // move the block exponent up by d >= 1 bits
+    __device__ __forceinline__ void raise(int d)
     {
-        const uint32_t f = a.flags | b.flags;
+        uint64_t W[4];
+        to_w256(W);
+        const uint64_t sgn = (uint64_t)((int64_t)W[3] >> 63);
+        if (d >= 256) {
+            W[0] = W[1] = W[2] = W[3] = 0;
+        } else {
+            while (d >= 64) {
+                W[0] = W[1]; W[1] = W[2]; W[2] = W[3]; W[3] = sgn;
+                d -= 64;
+            }
+            if (d) {
+                W[0] = (W[0] >> d) | (W[1] << (64 - d));
+                W[1] = (W[1] >> d) | (W[2] << (64 - d));
+                W[2] = (W[2] >> d) | (W[3] << (64 - d));
+                W[3] = (uint64_t)((int64_t)W[3] >> d);
+            }
+        }
+        // back to columns: 24-bit chunks, the rest (signed) in the top column
+        c[0] = (long long)(W[0] & 0xFFFFFFu);
+        c[1] = (long long)((W[0] >> 24) & 0xFFFFFFu);
+        c[2] = (long long)(((W[0] >> 48) | (W[1] << 16)) & 0xFFFFFFu);
+        c[3] = (long long)((W[1] >> 8) & 0xFFFFFFu);
+        c[4] = (long long)((W[1] >> 32) & 0xFFFFFFu);
+        c[5] = (long long)((W[1] >> 56) | (W[2] << 8));   // bits 120..183 (the sum stays far below 2^183)
+        cnt = 0;
+    }
+
+    // += x * y, y given as digits
+    __device__ __forceinline__ void add_dig(const Op &x, const Dig &y)
+    {
+        const uint32_t f = x.flags | y.flags;
         if (f & kBad) {
             bad = true;
             return;
         }
         if (f & kZero) return;
-        // Q = (a1 b1) 2^64 + a1 b0 + a0 b1 + hi(a0 b0 dropped)
-        const uint64_t p11l = a.x1 * b.x1, p11h = __umul64hi(a.x1, b.x1);
-        const uint64_t p10l = a.x1 * b.x0, p10h = __umul64hi(a.x1, b.x0);
-        const uint64_t p01l = a.x0 * b.x1, p01h = __umul64hi(a.x0, b.x1);
-        uint64_t q0, q1, q2;
-        asm("add.cc.u64 %0, %3, %4;\n\t"
-            "addc.cc.u64 %1, %5, %6;\n\t"
-            "addc.u64 %2, %7, 0;\n\t"
-            "add.cc.u64 %1, %1, %8;\n\t"
-            "addc.u64 %2, %2, 0;"
-            : "=l"(q0), "=l"(q1), "=l"(q2)
-            : "l"(p10l), "l"(p01l), "l"(p11l), "l"(p10h), "l"(p11h), "l"(p01h));
-        add_q(q0, q1, q2, a.e + b.e + 64, ((a.flags ^ b.flags) & kNeg) != 0);
+        const int ep = x.e + y.e;   // x*y = X*Y*2^ep, X < 2^118, Y < 2^118
+        if (!init) {
+            B = ep + 4;
+            init = true;
+        } else if (ep > B - 2) {
+            const int nb = ep + 4;
+            if (cnt) normalize();
+            raise(nb - B);
+            B = nb;
+        }
+        const int sh = B - ep;   // >= 2: X' = X >> sh < 2^116
+        uint64_t x1 = x.x1, x0 = x.x0;
+        if (sh >= 118) return;
+        if (sh >= 64) {
+            x0 = x1 >> (sh - 64);
+            x1 = 0;
+        } else {
+            x0 = (x0 >> sh) | (x1 << (64 - sh));
+            x1 >>= sh;
+        }
+        int a[5];
+        digits24(x1, x0, a);
+        if ((x.flags ^ y.flags) & kNeg) {
+#pragma unroll
+            for (int t = 0; t < 5; ++t) a[t] = -a[t];
+        }
+        const int *b = y.d;
+        c[0] += (long long)a[0] * b[3] + (long long)a[1] * b[2] + (long long)a[2] * b[1] + (long long)a[3] * b[0];
+        c[1] += (long long)a[0] * b[4] + (long long)a[1] * b[3] + (long long)a[2] * b[2] + (long long)a[3] * b[1] +
+                (long long)a[4] * b[0];
+        c[2] += (long long)a[1] * b[4] + (long long)a[2] * b[3] + (long long)a[3] * b[2] + (long long)a[4] * b[1];
+        c[3] += (long long)a[2] * b[4] + (long long)a[3] * b[3] + (long long)a[4] * b[2];
+        c[4] += (long long)a[3] * b[4] + (long long)a[4] * b[3];
+        c[5] += (long long)a[4] * b[4];
+        if (++cnt >= 2048) normalize();
     }
+
+    // += a * b (decoded operands)
+    __device__ __forceinline__ void add_prod(const Op &a, const Op &b) { add_dig(a, to_dig(b)); }
 
     __device__ __forceinline__ XF finish() const
     {
@@ -204,32 +297,9 @@ struct Acc {
         r.m = 0;
         r.e = 0;
         if (!init) return r;
-        uint64_t a0 = w0, a1 = w1, a2 = w2;
-        const bool neg = (int64_t)a2 < 0;
-        if (neg) {
-            asm("sub.cc.u64 %0, 0, %0;\n\t"
-                "subc.cc.u64 %1, 0, %1;\n\t"
-                "subc.u64 %2, 0, %2;"
-                : "+l"(a0), "+l"(a1), "+l"(a2));
-        }
-        // top 128 bits of the 192-bit magnitude
-        unsigned __int128 m;
-        int e;
-        if (a2) {
-            const int z = xfp::clz64(a2);
-            m = ((unsigned __int128)a2 << 64) | a1;
-            if (z) m = (m << z) | (a0 >> (64 - z));
-            e = lsb + 64 - z;
-        } else if (a1) {
-            m = ((unsigned __int128)a1 << 64) | a0;
-            e = lsb;
-        } else if (a0) {
-            m = a0;
-            e = lsb;
-        } else {
-            return r;
-        }
-        return xfp::xf_norm(neg, m, e);
+        uint64_t W[4];
+        to_w256(W);
+        return w256_to_xf(W, B + 72);
     }
 };
 

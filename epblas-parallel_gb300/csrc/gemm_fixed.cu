@@ -29,6 +29,7 @@
 
 #include "dd.cuh"
 #include "fixacc.cuh"
+#include "fixgemm.cuh"
 #include "gemm.h"
 #include "runtime.h"
 #include "xfloat.cuh"
@@ -38,117 +39,12 @@ namespace mw {
 namespace {
 
 using xfp::XF;
+using namespace fxg;
 
-constexpr int FX_S = 115;
 constexpr int FX_BM = 64, FX_BN = 64, FX_BK = 8;
 constexpr int FX_THREADS = 256;      // 16 x 16 threads, 4 x 4 outputs each
 constexpr int64_t FX_MAX_K = 16384;  // per launch (column-sum headroom)
 constexpr int kNoExpFx = -30000;
-
-// v * 2^sh rounded to an integer (|v * 2^sh| < 2^116), as five balanced
-// 24-bit digits; bit operations only (fixacc.cuh's decode).
-__device__ __forceinline__ void dd_digits(double2 v, int sh, int d[5])
-{
-#pragma unroll
-    for (int t = 0; t < 5; ++t) d[t] = 0;
-    const fx::Op o = fx::decode(v);
-    if (o.flags & (fx::kZero | fx::kBad)) return;   // non-finite rows are handled by the epilogue
-    const int r = -(o.e + sh);   // N = (x1:x0) * 2^-r; r >= 2 for in-range values
-    if (r >= 118 || r < 1) return;
-    const unsigned __int128 X = ((unsigned __int128)o.x1 << 64) | o.x0;
-    unsigned __int128 N = (X >> r) + (unsigned __int128)((X >> (r - 1)) & 1);
-#pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        int dt = (int)((uint32_t)N & 0xFFFFFFu);
-        if (dt >= 0x800000) {
-            dt -= 0x1000000;
-            N += 0x1000000;
-        }
-        N >>= 24;
-        d[t] = dt;
-    }
-    d[4] = (int)(uint32_t)N;
-    if (o.flags & fx::kNeg) {
-#pragma unroll
-        for (int t = 0; t < 5; ++t) d[t] = -d[t];
-    }
-}
-
-// 256-bit two's complement accumulation of x * 2^s (x signed, s < 128).
-__device__ __forceinline__ void add_shifted(uint64_t W[4], int64_t x, int s)
-{
-    const uint64_t ext = x < 0 ? ~0ull : 0ull;
-    const int b = s & 63;
-    uint64_t v[4];
-    const uint64_t lo = (uint64_t)x << b;
-    const uint64_t hi = b ? (((uint64_t)x >> (64 - b)) | (ext << b)) : ext;
-    if (s < 64) {
-        v[0] = lo; v[1] = hi; v[2] = ext; v[3] = ext;
-    } else {
-        v[0] = 0; v[1] = lo; v[2] = hi; v[3] = ext;
-    }
-    asm("add.cc.u64 %0, %0, %4;\n\t"
-        "addc.cc.u64 %1, %1, %5;\n\t"
-        "addc.cc.u64 %2, %2, %6;\n\t"
-        "addc.u64 %3, %3, %7;"
-        : "+l"(W[0]), "+l"(W[1]), "+l"(W[2]), "+l"(W[3])
-        : "l"(v[0]), "l"(v[1]), "l"(v[2]), "l"(v[3]));
-}
-
-// W * 2^e as an extended float.
-__device__ __forceinline__ XF w256_to_xf(uint64_t W[4], int e)
-{
-    XF r;
-    r.neg = (int64_t)W[3] < 0;
-    if (r.neg) {
-        asm("sub.cc.u64 %0, 0, %0;\n\t"
-            "subc.cc.u64 %1, 0, %1;\n\t"
-            "subc.cc.u64 %2, 0, %2;\n\t"
-            "subc.u64 %3, 0, %3;"
-            : "+l"(W[0]), "+l"(W[1]), "+l"(W[2]), "+l"(W[3]));
-    }
-    int top = 3;
-    while (top > 0 && W[top] == 0) --top;
-    if (W[top] == 0) {
-        r.zero = true; r.neg = false; r.m = 0; r.e = 0;
-        return r;
-    }
-    const int z = xfp::clz64(W[top]);
-    const uint64_t w1 = W[top], w0 = top >= 1 ? W[top - 1] : 0, wm = top >= 2 ? W[top - 2] : 0;
-    unsigned __int128 m = ((unsigned __int128)w1 << 64) | w0;
-    if (z) m = (m << z) | (wm >> (64 - z));
-    r.m = m;
-    r.e = e + 64 * (top - 1) - z;
-    r.zero = false;
-    return r;
-}
-
-__device__ __forceinline__ dd::real xf_to_real(const XF &x)
-{
-    dd::real r;
-    xfp::xf_to_dd(x, r.hi, r.lo);
-    return r;
-}
-
-// C := alpha*X + beta*C with one rounding (non-finite C through the DD operators).
-__device__ __forceinline__ void store_axpby(double2 *pc, XF v, const XF &xa, bool alpha_one, const XF &xb,
-                                            dd::real beta, int beta_kind)
-{
-    if (!alpha_one) v = xfp::xf_mul(xa, v);
-    if (beta_kind != 0) {
-        const double2 c0 = *pc;
-        if (!isfinite(c0.x)) {
-            dd::real cv = dd::make(c0.x, c0.y);
-            if (beta_kind == 2) cv = dd::mul_exact(cv, beta);
-            dd::store(pc, dd::add_exact(cv, xf_to_real(v)));
-            return;
-        }
-        XF xc = xfp::xf_from_dd(c0.x, c0.y);
-        if (beta_kind == 2) xc = xfp::xf_mul(xb, xc);
-        v = xfp::xf_add(v, xc);
-    }
-    dd::store(pc, xf_to_real(v));
-}
 
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(FX_THREADS, 1)
@@ -276,10 +172,7 @@ __global__ void __launch_bounds__(FX_THREADS, 1)
             if (ei <= kNoExpFx / 2 || ej <= kNoExpFx / 2) {
                 v.zero = true; v.neg = false; v.m = 0; v.e = 0;
             } else {
-                uint64_t W[4] = {0, 0, 0, 0};
-#pragma unroll
-                for (int w = 0; w < 5; ++w) add_shifted(W, acc[a][b][w], 24 * w);
-                v = w256_to_xf(W, 96 + ei + ej - 2 * FX_S);
+                v = sums_to_xf(acc[a][b], ei, ej);
             }
             store_axpby(pc, v, xa, alpha_one != 0, xb, beta, beta_kind);
         }

@@ -9,12 +9,13 @@
 // Trans: block per column (A's columns are contiguous), warp-shuffle and
 // shared-memory reduction, then y_j += alpha*s (mgemv.cpp:229-233).
 // mgemv_ accumulates the products in per-thread integer fixed point
-// (fixacc.cuh): x is first converted once to 128-bit extended floats (it is
-// small and stays in L2), each A(i,j) * x(j) is formed to 2^-126 and added
-// exactly; partial sums combine as extended floats in a fixed order, and
-// y := y + alpha*s is rounded once to double-double. The FP64 pipe, which
-// would bound a double-double multiply-add at a fraction of HBM speed, is
-// not used in the loop.
+// (fixacc.cuh): x is first split once into 24-bit digit sets (32 bytes per
+// entry; it is small and stays in L2), each A(i,j) is decoded from its bits
+// and its digits multiplied into the thread's exact column sums; partial sums
+// combine as extended floats in a fixed order, and y := y + alpha*s is
+// rounded once to double-double. The FP64 pipe, which would bound a
+// double-double multiply-add at a fraction of HBM speed, is not used in the
+// loop.
 // mgemv_n_noalloc keeps the FP64 accumulation (TwoProduct + TwoSum into a
 // (sum, error) pair, renormalised every 32 terms, the lo*lo product dropped as
 // in mdot.cpp:60-64) so that its partial sums fit its fixed scratch array.
@@ -87,16 +88,16 @@ __global__ void k_gemv_n_final(int64_t m, int nchunks, const double2 *part, dd::
 
 // ---- fixed-point kernels (mgemv_) ------------------------------------------------------
 
-__global__ void k_op_convert(int64_t n, const double2 *x, int64_t incx, fx::OpPod *out)
+__global__ void k_dig_convert(int64_t n, const double2 *x, int64_t incx, fx::Dig *out)
 {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
-        out[j] = fx::to_pod(fx::decode(x[vidx(j, n, incx)]));
+        out[j] = fx::to_dig(fx::decode(x[vidx(j, n, incx)]));
 }
 
 // NoTrans partial sums: row per thread, columns [j0, j1) of chunk blockIdx.y
 // (at most fx::kMaxAdds columns per chunk).
 __global__ void __launch_bounds__(256) k_gemv_n_fx(int64_t m, int64_t n, const double2 *__restrict__ A, int64_t lda,
-                                                  const fx::OpPod *__restrict__ xo, int64_t chunk,
+                                                  const fx::Dig *__restrict__ xo, int64_t chunk,
                                                   fx::XFPod *__restrict__ part)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -108,10 +109,10 @@ __global__ void __launch_bounds__(256) k_gemv_n_fx(int64_t m, int64_t n, const d
     int64_t j = j0;
     for (; j + 2 <= j1; j += 2) {
         const double2 a0 = __ldcs(a + j * lda), a1 = __ldcs(a + (j + 1) * lda);
-        acc.add_prod(fx::decode(a0), fx::from_pod(xo[j]));
-        acc.add_prod(fx::decode(a1), fx::from_pod(xo[j + 1]));
+        acc.add_dig(fx::decode(a0), xo[j]);
+        acc.add_dig(fx::decode(a1), xo[j + 1]);
     }
-    for (; j < j1; ++j) acc.add_prod(fx::decode(a[j * lda]), fx::from_pod(xo[j]));
+    for (; j < j1; ++j) acc.add_dig(fx::decode(a[j * lda]), xo[j]);
     part[blockIdx.y * m + i] = fx::to_pod(acc.finish(), acc.bad);
 }
 
@@ -156,7 +157,7 @@ __global__ void k_gemv_n_fx_final(int64_t m, int nchunks, const fx::XFPod *part,
 // Trans: block per column j of A (contiguous), threads over rows; every
 // fx::kMaxAdds products a thread's accumulator is folded into an extended float.
 __global__ void __launch_bounds__(256) k_gemv_t_fx(int64_t m, int64_t n, const double2 *__restrict__ A, int64_t lda,
-                                                  const fx::OpPod *__restrict__ xo, dd::real alpha, double2 *y,
+                                                  const fx::Dig *__restrict__ xo, dd::real alpha, double2 *y,
                                                   int64_t incy)
 {
     __shared__ fx::XFPod sh[8];
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(256) k_gemv_t_fx(int64_t m, int64_t n, const d
     bool bad = false;
     int cnt = 0;
     for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
-        acc.add_prod(fx::decode(__ldcs(col + i)), fx::from_pod(xo[i]));
+        acc.add_dig(fx::decode(__ldcs(col + i)), xo[i]);
         if (++cnt >= fx::kMaxAdds) {
             bad |= acc.bad;
             total = xfp::xf_add(total, acc.finish());
@@ -209,8 +210,8 @@ bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A,
     if (alpha.hi == 0.0 && alpha.lo == 0.0) return true;
     dd::real al = dd::make(alpha.hi, alpha.lo);
     const int64_t lenx = trans ? m : n;
-    // x as decoded operands (lenx * 24 bytes), then the partial sums
-    const size_t xf_bytes = ((size_t)lenx * sizeof(fx::OpPod) + 255) / 256 * 256;
+    // x as digit sets (lenx * 32 bytes), then the partial sums
+    const size_t xf_bytes = ((size_t)lenx * sizeof(fx::Dig) + 255) / 256 * 256;
     if (!trans) {
         int64_t rowblocks = (m + 255) / 256;
         int64_t want = 8 * (int64_t)sms;
@@ -226,11 +227,11 @@ bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A,
         }
         char *buf = (char *)dev_alloc(xf_bytes + sizeof(fx::XFPod) * (size_t)(nchunks * m), routine);
         if (!buf) return false;
-        fx::OpPod *xf = (fx::OpPod *)buf;
+        fx::Dig *xf = (fx::Dig *)buf;
         fx::XFPod *part = (fx::XFPod *)(buf + xf_bytes);
         int64_t cb = (n + 255) / 256;
         if (cb > sms * 8) cb = sms * 8;
-        k_op_convert<<<(unsigned)cb, 256, 0, stream()>>>(n, (const double2 *)x, incx, xf);
+        k_dig_convert<<<(unsigned)cb, 256, 0, stream()>>>(n, (const double2 *)x, incx, xf);
         dim3 grid((unsigned)rowblocks, (unsigned)nchunks);
         k_gemv_n_fx<<<grid, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, xf, chunk, part);
         int64_t fb = (m + 255) / 256;
@@ -239,11 +240,11 @@ bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A,
         count_launch(3);
         dev_free(buf);
     } else {
-        fx::OpPod *xf = (fx::OpPod *)dev_alloc(xf_bytes, routine);
+        fx::Dig *xf = (fx::Dig *)dev_alloc(xf_bytes, routine);
         if (!xf) return false;
         int64_t cb = (m + 255) / 256;
         if (cb > sms * 8) cb = sms * 8;
-        k_op_convert<<<(unsigned)cb, 256, 0, stream()>>>(m, (const double2 *)x, incx, xf);
+        k_dig_convert<<<(unsigned)cb, 256, 0, stream()>>>(m, (const double2 *)x, incx, xf);
         k_gemv_t_fx<<<(unsigned)n, 256, 0, stream()>>>(m, n, (const double2 *)A, lda, xf, al, (double2 *)y, incy);
         count_launch(2);
         dev_free(xf);

@@ -23,13 +23,28 @@ XF_HD int clz64(uint64_t v)
     return v ? __builtin_clzll(v) : 64;
 #endif
 }
-XF_HD uint64_t mulhi64(uint64_t a, uint64_t b)
+// Full 64 x 64 -> 128-bit product. On the device it is built from four
+// 32 x 32 -> 64-bit multiply-adds: the 64-bit multiply-high instruction
+// issues at the FP64 rate on this part.
+XF_HD void mul64x64(uint64_t a, uint64_t b, uint64_t &hi, uint64_t &lo)
 {
 #ifdef __CUDA_ARCH__
-    return __umul64hi(a, b);
+    const uint32_t al = (uint32_t)a, ah = (uint32_t)(a >> 32), bl = (uint32_t)b, bh = (uint32_t)(b >> 32);
+    const uint64_t ll = (uint64_t)al * bl, lh = (uint64_t)al * bh, hl = (uint64_t)ah * bl, hh = (uint64_t)ah * bh;
+    const uint64_t mid = (ll >> 32) + (uint32_t)lh + (uint32_t)hl;
+    lo = (mid << 32) | (uint32_t)ll;
+    hi = hh + (lh >> 32) + (hl >> 32) + (mid >> 32);
 #else
-    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+    const unsigned __int128 p = (unsigned __int128)a * b;
+    hi = (uint64_t)(p >> 64);
+    lo = (uint64_t)p;
 #endif
+}
+XF_HD uint64_t mulhi64(uint64_t a, uint64_t b)
+{
+    uint64_t hi, lo;
+    mul64x64(a, b, hi, lo);
+    return hi;
 }
 XF_HD uint64_t dbits(double d)
 {
@@ -151,9 +166,13 @@ XF_HD XF xf_mul(const XF &a, const XF &b)
         return z;
     }
     uint64_t a1 = (uint64_t)(a.m >> 64), a0 = (uint64_t)a.m, b1 = (uint64_t)(b.m >> 64), b0 = (uint64_t)b.m;
-    unsigned __int128 p11 = (unsigned __int128)a1 * b1;
-    unsigned __int128 p10 = (unsigned __int128)a1 * b0;
-    unsigned __int128 p01 = (unsigned __int128)a0 * b1;
+    uint64_t h, l;
+    mul64x64(a1, b1, h, l);
+    unsigned __int128 p11 = ((unsigned __int128)h << 64) | l;
+    mul64x64(a1, b0, h, l);
+    unsigned __int128 p10 = ((unsigned __int128)h << 64) | l;
+    mul64x64(a0, b1, h, l);
+    unsigned __int128 p01 = ((unsigned __int128)h << 64) | l;
     uint64_t p00h = mulhi64(a0, b0);
     unsigned __int128 mid = (p10 & 0xFFFFFFFFFFFFFFFFull) + (p01 & 0xFFFFFFFFFFFFFFFFull) + p00h;
     unsigned __int128 hi = p11 + (p10 >> 64) + (p01 >> 64) + (mid >> 64);

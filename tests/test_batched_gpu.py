@@ -149,3 +149,45 @@ def test_grouped_trsm(gpu, oracle, rng, side, uplo, trans, diag):
         got = arena.get(2 * i + 1)
         err = orc.normwise_error(got[:, :d["m"]], want[:, :d["m"]], orc.dd_abs(d["alpha"]) * orc.dd_absmax(d["B"]))
         assert err <= max(20, 8 * d["na"] ** 2) * orc.EPS_DD, (i, err)
+
+
+def test_grouped_gemm_long_k_scaled_and_nonfinite(gpu, oracle, rng):
+    """K beyond one split's 16384 multiply-adds, rows scaled by 2^+-200, and an
+    instance whose A holds an infinity (its rows become NaN, the others are
+    unaffected)."""
+    inst = make_batch(rng, 6, maxdim=40)
+    inst[0].update(m=5, n=3, k=20000, ta="N", tb="N", lda=5, ldb=20000, ldc=5)
+    inst[0]["A"] = mwb.dd_matrix(rng, 5, 20000, 5) * (2.0 ** rng.integers(-200, 200, 5))[None, :, None]
+    inst[0]["B"] = mwb.dd_matrix(rng, 20000, 3, 20000)
+    inst[0]["C"] = mwb.dd_matrix(rng, 5, 3, 5)
+    bad = inst[1]
+    bad.update(ta="N")
+    bad["lda"] = max(bad["m"], 1)
+    bad["A"] = mwb.dd_matrix(rng, bad["m"], bad["k"], bad["lda"])
+    if bad["m"] > 0 and bad["k"] > 0 and bad["n"] > 0:
+        bad["A"][0, 0] = (np.inf, 0.0)
+    arena, args, _ = run_grouped(gpu, inst)
+    # instance 0: entrywise against its own row scale
+    d = inst[0]
+    got = arena.get(2)
+    want = oracle.qgemm("N", "N", 5, 3, 20000, d["alpha"], d["A"], 5, d["B"], 20000, d["beta"], d["C"].copy(), 5)
+    ra = np.max(np.abs(d["A"][..., 0]), axis=0)
+    scale = orc.dd_abs(d["alpha"]) * 20000 * np.outer(np.max(np.abs(d["B"][..., 0]), axis=1), ra) \
+        + orc.dd_abs(d["beta"]) * np.abs(d["C"][..., 0])
+    err = np.abs((got[..., 0] - want[..., 0]) + (got[..., 1] - want[..., 1]))
+    assert np.all(err <= 4 * 20000 * orc.EPS_DD * scale), np.max(err / scale)
+    if bad["m"] > 0 and bad["k"] > 0 and bad["n"] > 0:
+        gb = arena.get(5)
+        assert np.all(np.isnan(gb[:, 0, 0])), "row with an infinity must be NaN"
+    for i in range(2, len(inst)):
+        check(oracle, [inst[i]], _Shift(arena, 3 * i))
+
+
+class _Shift:
+    """View of a DeviceArena whose indices start at instance `base`."""
+
+    def __init__(self, arena, base):
+        self.arena, self.base = arena, base
+
+    def get(self, i):
+        return self.arena.get(self.base + i)
