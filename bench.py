@@ -301,6 +301,9 @@ def main():
     ap.add_argument("--skip-check", action="store_true")
     ap.add_argument("--workload", default="gemm", choices=WORKLOADS,
                     help="gemm: the headline line; the others measure one routine of the level-1/2/3 mix")
+    ap.add_argument("--size", type=int, default=0,
+                    help="problem size of a --workload line (n for dot/axpy, m=n for gemv, m for trsm, "
+                         "n for gemm_fixed/gemm_plain); 0 keeps the default")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.workload != "gemm":
@@ -420,8 +423,8 @@ def tc_traffic_from_profile():
 # workloads, each printed as one JSON line of the same shape as the headline.
 # ---------------------------------------------------------------------------
 
-WORKLOADS = ("gemm", "stress", "wgemm", "gemm_t", "syrk", "herk", "trsm", "gemv", "dot", "axpy", "batched_gemm",
-             "batched_trsm")
+WORKLOADS = ("gemm", "stress", "wgemm", "gemm_t", "gemm_fixed", "gemm_plain", "syrk", "herk", "trsm", "gemv", "dot",
+             "axpy", "batched_gemm", "batched_trsm")
 
 
 def _dev_dd(torch, shape, gen, dev, cplx_=False):
@@ -510,6 +513,28 @@ def run_workload(args):
             check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
             # componentwise view: error relative to |alpha| sum_p |a_ip||b_pj| of the sampled entries
             check["samples"] = 256
+    elif w in ("gemm_fixed", "gemm_plain"):
+        # one engine forced, n^3 NN (default n = 4096)
+        eng = w.split("_")[1]
+        n = args.size or 4096
+        A = _dev_dd(torch, (n, n), gen, dev)
+        B = _dev_dd(torch, (n, n), gen, dev)
+        C = _dev_dd(torch, (n, n), gen, dev)
+        C0 = C.clone()
+        fn = lambda: lib.mgemm("N", "N", n, n, n, al, A.data_ptr(), n, B.data_ptr(), n, be, C.data_ptr(), n,
+                               engine=eng)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: C.copy_(C0))
+        value, unit = 2.0 * n ** 3 / ms / 1e6, "DD-GFLOP/s"
+        metric = f"DD-GEMM GFLOP/s n={n} NN, {eng} engine"
+        cfg = {"workload": f"mgemm_{eng}_64_ {n}^3 NN"}
+        if o:
+            C.copy_(C0)
+            fn()
+            rows, cols = rng.integers(0, n, 128), rng.integers(0, n, 128)
+            hA, hB, hC0 = hb(A), hb(B), hb(C0)
+            want = o.qgemm("N", "N", n, n, n, al, hA, n, hB, n, be, hC0, n, rows=rows, cols=cols)
+            op = orc.dd_abs(al) * n * orc.dd_absmax(hA) * orc.dd_absmax(hB) + orc.dd_abs(be) * orc.dd_absmax(hC0)
+            check["normwise_err_sampled"] = orc.normwise_error(hb(C)[cols, rows], want, op)
     elif w in ("wgemm", "gemm_t"):
         # complex GEMM at 4096^3 NN, or the real GEMM at n^3 with both operands transposed
         cx = w == "wgemm"
@@ -593,7 +618,7 @@ def run_workload(args):
             op = 2 * (orc.dd_abs(al) * k * orc.dd_absmax(hA) ** 2 + orc.dd_abs(be) * orc.dd_absmax(hC0))
             check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
     elif w == "trsm":
-        m, nr = 4096, 1024
+        m, nr = (args.size or 4096), 1024
         A = _dev_dd(torch, (m, m), gen, dev)
         A[..., 0] /= m
         A[..., 1] /= m
@@ -606,8 +631,8 @@ def run_workload(args):
         fn = lambda: lib.mtrsm("L", "L", "N", "N", m, nr, al, A.data_ptr(), m, B.data_ptr(), m)
         ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: B.copy_(B0))
         value, unit = float(m) * m * nr / ms / 1e6, "DD-GFLOP/s"
-        metric = "DD-TRSM GFLOP/s LLNN m=4096 nrhs=1024 (m^2 nrhs flops)"
-        cfg = {"workload": "mtrsm_ L L N N m=4096 n=1024, diag U[m,2m], off-diagonal U[-1,1)/m"}
+        metric = f"DD-TRSM GFLOP/s LLNN m={m} nrhs=1024 (m^2 nrhs flops)"
+        cfg = {"workload": f"mtrsm_ L L N N m={m} n=1024, diag U[m,2m], off-diagonal U[-1,1)/m"}
         if o:
             B.copy_(B0)
             fn()
@@ -619,7 +644,7 @@ def run_workload(args):
             check["normwise_err_sampled"] = orc.normwise_error(got, want, orc.dd_abs(al) * orc.dd_absmax(hb(B0)))
             check["columns_checked"] = len(cols)
     elif w == "gemv":
-        m = n = 16384
+        m = n = args.size or 16384
         A = _dev_dd(torch, (n, m), gen, dev)
         x = _dev_dd(torch, (n,), gen, dev)
         y = _dev_dd(torch, (m,), gen, dev)
@@ -628,8 +653,8 @@ def run_workload(args):
         ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: y.copy_(y0))
         nbytes = 16.0 * (m * n + n + 2 * m)
         value, unit = nbytes / ms / 1e6, "GB/s"
-        metric = "DD-GEMV HBM GB/s m=n=16384 (16(mn+n+2m) bytes)"
-        cfg = {"workload": "mgemv_ N m=n=16384 incx=incy=1"}
+        metric = f"DD-GEMV HBM GB/s m=n={n} (16(mn+n+2m) bytes)"
+        cfg = {"workload": f"mgemv_ N m=n={n} incx=incy=1"}
         roof = {"bound": "hbm", "achieved": value, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": value / pk["hbm_gbs"], "peak_kind": pk_kind, "traffic": None}
         if o:
@@ -644,7 +669,7 @@ def run_workload(args):
             op = orc.dd_abs(al) * n * amax * orc.dd_absmax(hb(x)) + orc.dd_abs(be) * orc.dd_absmax(hb(y0))
             check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
     elif w in ("dot", "axpy"):
-        n = 1 << 28
+        n = args.size or (1 << 28)
         x = _dev_dd(torch, (n,), gen, dev)
         y = _dev_dd(torch, (n,), gen, dev)
         if w == "dot":
@@ -652,8 +677,8 @@ def run_workload(args):
             fn = lambda: out.__setitem__("r", lib.mdot(n, x.data_ptr(), 1, y.data_ptr(), 1))
             ms, clk = _timed(torch, fn, args.steps, args.warmup, stream)
             nbytes = 32.0 * n
-            metric = "DD-DOT HBM GB/s n=2^28 (32n bytes)"
-            cfg = {"workload": "mdot_ n=2^28 incx=incy=1"}
+            metric = f"DD-DOT HBM GB/s n={n} (32n bytes)"
+            cfg = {"workload": f"mdot_ n={n} incx=incy=1"}
             if o:
                 hx, hy = hb(x), hb(y)
                 want = o.qdot(n, hx, 1, hy, 1)
@@ -665,8 +690,8 @@ def run_workload(args):
             fn = lambda: lib.maxpy(n, al, x.data_ptr(), 1, y.data_ptr(), 1)
             ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: y.copy_(y0))
             nbytes = 48.0 * n
-            metric = "DD-AXPY HBM GB/s n=2^28 (48n bytes)"
-            cfg = {"workload": "maxpy_ n=2^28 incx=incy=1"}
+            metric = f"DD-AXPY HBM GB/s n={n} (48n bytes)"
+            cfg = {"workload": f"maxpy_ n={n} incx=incy=1"}
             if o:
                 y.copy_(y0)
                 fn()

@@ -285,12 +285,19 @@ __device__ __forceinline__ dd::real dd_recip(dd::real b)
 }
 
 // side: 0 left, 1 right; lower: op(A) lower triangular; trans: op = A^T.
+// Warp per (instance, 32 right-hand sides), lane per right-hand side. The
+// reciprocals of the diagonal are computed 32 rows at a time, one row per
+// lane, and broadcast with shuffles; each row's sum alpha*b - sum_p A x is
+// accumulated exactly in fixed point (fixacc.cuh) and rounded once before the
+// multiplication by the reciprocal. All lanes stay in the loop (lanes past
+// the last right-hand side do the work on a clamped column and store
+// nothing) so that the shuffles see the whole warp.
 __global__ void __launch_bounds__(128) k_trsm_grouped(const TrsmDesc *__restrict__ descs, int count, int64_t total,
                                                      int side, int lower, int trans, int unit)
 {
     const int lane = threadIdx.x & 31;
     const int64_t w = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-    if (w >= total) return;
+    if (w >= total) return;   // whole warp leaves together
     int lo = 0, hi = count - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
@@ -301,46 +308,59 @@ __global__ void __launch_bounds__(128) k_trsm_grouped(const TrsmDesc *__restrict
     const int chunk = (int)(w - d.work_begin);
     const dd::real alpha = dd::make(d.alpha.x, d.alpha.y);
     const bool alpha1 = (d.alpha.x == 1.0 && d.alpha.y == 0.0);
-#define OPA(i, j) dd::load(trans ? d.A + (j) + (int64_t)(i) * d.lda : d.A + (i) + (int64_t)(j) * d.lda)
-    if (side == 0) {
-        // op(A) X = alpha B, B is m x n; lane handles column chunk*32 + lane
-        const int64_t col = (int64_t)chunk * 32 + lane;
-        if (col >= d.n) return;
-        double2 *b = d.B + col * d.ldb;
-        const int mm = d.m;
-        for (int s = 0; s < mm; ++s) {
-            const int r = lower ? s : mm - 1 - s;
-            dd::real acc = dd::load(b + r);
-            if (!alpha1) acc = dd::mul_fast(acc, alpha);
-            if (lower) {
-                for (int p = 0; p < r; ++p) acc = dd::add_fast(acc, dd::neg(dd::mul_fast(OPA(r, p), dd::load(b + p))));
-            } else {
-                for (int p = r + 1; p < mm; ++p) acc = dd::add_fast(acc, dd::neg(dd::mul_fast(OPA(r, p), dd::load(b + p))));
+    const int na = side == 0 ? d.m : d.n;                 // order of the triangle
+    const int64_t nr = side == 0 ? d.n : d.m;             // right-hand sides
+    const int64_t rhs = (int64_t)chunk * 32 + lane;
+    const bool active = rhs < nr;
+    const int64_t my = active ? rhs : nr - 1;             // clamped: loads stay in bounds
+    // element t of this lane's right-hand side (a column of B for side L, a row for R)
+    auto bptr = [&](int t) -> double2 * {
+        return side == 0 ? d.B + my * d.ldb + t : d.B + my + (int64_t)t * d.ldb;
+    };
+#define OPA(i, j) (trans ? d.A[(j) + (int64_t)(i) * d.lda] : d.A[(i) + (int64_t)(j) * d.lda])
+    // side L: op(A) X = alpha B, forward if op(A) is lower;
+    // side R: X op(A) = alpha B, forward if op(A) is upper.
+    const bool forward = side == 0 ? lower : !lower;
+    fx::Dig one;
+    {
+        const fx::Op o = fx::decode(make_double2(1.0, 0.0));
+        one = fx::to_dig(o);
+    }
+    dd::real inv = dd::make(1.0, 0.0);
+    for (int s = 0; s < na; ++s) {
+        const int r = forward ? s : na - 1 - s;
+        if (!unit && (s & 31) == 0) {
+            // reciprocals of the next 32 diagonal entries, one per lane
+            const int sl = s + lane;
+            if (sl < na) {
+                const int rl = forward ? sl : na - 1 - sl;
+                inv = dd_recip(dd::load(&OPA(rl, rl)));
             }
-            if (!unit) acc = dd::mul_fast(acc, dd_recip(OPA(r, r)));
-            dd::store(b + r, acc);
         }
-    } else {
-        // X op(A) = alpha B; lane handles row chunk*32 + lane of B (m x n)
-        const int64_t row = (int64_t)chunk * 32 + lane;
-        if (row >= d.m) return;
-        const int nn = d.n;
-        const bool upper = !lower;
-        for (int s = 0; s < nn; ++s) {
-            const int c = upper ? s : nn - 1 - s;
-            double2 *pb = d.B + row + (int64_t)c * d.ldb;
-            dd::real acc = dd::load(pb);
-            if (!alpha1) acc = dd::mul_fast(acc, alpha);
-            if (upper) {
-                for (int p = 0; p < c; ++p)
-                    acc = dd::add_fast(acc, dd::neg(dd::mul_fast(dd::load(d.B + row + (int64_t)p * d.ldb), OPA(p, c))));
-            } else {
-                for (int p = c + 1; p < nn; ++p)
-                    acc = dd::add_fast(acc, dd::neg(dd::mul_fast(dd::load(d.B + row + (int64_t)p * d.ldb), OPA(p, c))));
-            }
-            if (!unit) acc = dd::mul_fast(acc, dd_recip(OPA(c, c)));
-            dd::store(pb, acc);
+        fx::Acc acc;
+        acc.reset();
+        dd::real b0 = dd::load(bptr(r));
+        if (!alpha1) b0 = dd::mul_fast(b0, alpha);
+        acc.add_dig(fx::decode(make_double2(b0.hi, b0.lo)), one);
+        const int p0 = forward ? 0 : r + 1, p1 = forward ? r : na;
+        for (int p = p0; p < p1; ++p) {
+            // side L: sum_p op(A)(r, p) x_p; side R: sum_p x_p op(A)(p, r)
+            const double2 av = side == 0 ? OPA(r, p) : OPA(p, r);
+            fx::Op ao = fx::decode(av);
+            ao.flags ^= fx::kNeg;
+            acc.add_dig(ao, fx::to_dig(fx::decode(*bptr(p))));
         }
+        double h, l;
+        xfp::xf_to_dd(acc.finish(), h, l);
+        dd::real v = dd::make(h, l);
+        if (acc.bad) v = dd::make(__longlong_as_double(0x7ff8000000000000ll), 0.0);
+        if (!unit) {
+            const double ih = __shfl_sync(0xffffffffu, inv.hi, s & 31);
+            const double il = __shfl_sync(0xffffffffu, inv.lo, s & 31);
+            v = dd::mul_fast(v, dd::make(ih, il));
+        }
+        if (active) dd::store(bptr(r), v);
+        __syncwarp();
     }
 #undef OPA
 }

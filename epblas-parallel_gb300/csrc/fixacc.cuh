@@ -6,10 +6,11 @@
 // up with HBM. The 64-bit multiply-high (IMAD.HI) also issues at the FP64
 // rate here, so only 32 x 32 -> 64-bit multiply-adds (IMAD.WIDE) are used:
 //
-//  * decode: a double-double (hi, lo) becomes |hi + lo| = (x1:x0) * 2^e with
-//    x1 < 2^54 holding hi's mantissa and x0 the 64 bits below it (lo's
-//    mantissa shifted into place, added or subtracted): the exact value to
-//    2^-117, from shifts and adds only;
+//  * decode: a double-double (hi, lo) becomes |hi + lo| = W * 2^e, W a
+//    118-bit integer in four 32-bit words holding hi's mantissa above 64 bits
+//    of lo's mantissa shifted into place (added or subtracted): the exact
+//    value to 2^-117, from 32-bit shifts and adds only (64-bit shifts issue
+//    at the FP64 rate on this part);
 //  * accumulate: each thread keeps a block exponent B. For a product x*y the
 //    integer X is shifted right to the block (X' = X >> (B - ex - ey)) so that
 //    X' * Y lands at 2^B; X' and Y are split into five 24-bit digits and the
@@ -36,64 +37,103 @@ constexpr int kMaxAdds = 1 << 20;   // products per accumulator before it is fol
 
 enum : uint32_t { kNeg = 1, kZero = 2, kBad = 4 };
 
-// |v| = (x1:x0) * 2^e, sign and zero / non-finite flags.
+// |v| = W * 2^e with W = w[3]:w[2]:w[1]:w[0] (32-bit words, W < 2^118),
+// sign and zero / non-finite flags. Everything here is 32-bit integer work:
+// on this part the 64-bit shifts and multiplies run at the FP64 rate.
 struct Op {
-    uint64_t x1, x0;
+    uint32_t w[4];
     int e;
     uint32_t flags;
 };
 
+// 64-bit mantissa (hi:lo words, < 2^53) shifted left by s (0 <= s < 64) into
+// four words.
+__device__ __forceinline__ void shl53(uint32_t hi, uint32_t lo, int s, uint32_t t[4])
+{
+    const int q = s >> 5, r = s & 31;
+    const uint32_t a0 = lo << r;
+    const uint32_t a1 = __funnelshift_l(lo, hi, r);
+    const uint32_t a2 = r ? (hi >> (32 - r)) : 0u;
+    t[0] = q ? 0u : a0;
+    t[1] = q ? a0 : a1;
+    t[2] = q ? a1 : a2;
+    t[3] = q ? a2 : 0u;
+}
+
 __device__ __forceinline__ Op decode(double2 v)
 {
     Op o;
-    const uint64_t bh = (uint64_t)__double_as_longlong(v.x), bl = (uint64_t)__double_as_longlong(v.y);
-    int eh = (int)((bh >> 52) & 0x7FF), el = (int)((bl >> 52) & 0x7FF);
-    o.flags = (uint32_t)(bh >> 63);
+    const uint32_t hl = (uint32_t)__double2loint(v.x), hh = (uint32_t)__double2hiint(v.x);
+    const uint32_t ll = (uint32_t)__double2loint(v.y), lh = (uint32_t)__double2hiint(v.y);
+    int eh = (int)((hh >> 20) & 0x7FF), el = (int)((lh >> 20) & 0x7FF);
+    o.flags = hh >> 31;
+    o.w[0] = o.w[1] = o.w[2] = o.w[3] = 0;
+    o.e = 0;
     if (eh == 0x7FF || el == 0x7FF) {
         o.flags |= kBad;
-        o.x1 = o.x0 = 0;
-        o.e = 0;
         return o;
     }
-    if ((bh << 1) == 0) {   // hi == +-0: a normalised double-double is zero
+    if (((hh << 1) | hl) == 0) {   // hi == +-0: a normalised double-double is zero
         o.flags |= kZero;
-        o.x1 = o.x0 = 0;
-        o.e = 0;
         return o;
     }
-    const uint64_t mh = (bh & 0xFFFFFFFFFFFFFull) | (eh ? (1ull << 52) : 0);
+    const uint32_t mhh = (hh & 0xFFFFFu) | (eh ? 0x100000u : 0u);
     eh = eh ? eh : 1;
     o.e = eh - 1075 - 64;
-    o.x1 = mh;
-    o.x0 = 0;
-    if ((bl << 1) != 0) {
-        const uint64_t ml = (bl & 0xFFFFFFFFFFFFFull) | (el ? (1ull << 52) : 0);
+    o.w[3] = mhh;
+    o.w[2] = hl;
+    if (((lh << 1) | ll) != 0) {
+        const uint32_t mlh = (lh & 0xFFFFFu) | (el ? 0x100000u : 0u);
         el = el ? el : 1;
-        const int s = 64 - (eh - el);   // lo's mantissa sits s bits above x0's bit 0
-        uint64_t t1 = 0, t0;
+        int s = 64 - (eh - el);   // lo's mantissa sits s bits above bit 0 of W
+        uint32_t t[4];
         if (s >= 64) {
-            // |lo| >= |hi| / 2: not a normalised double-double; keep hi's frame
-            // and fold lo in at 2^64 granularity (the value stays within
-            // 2^-52 of hi + lo relative to lo)
-            const int s1 = s - 64;
-            t1 = s1 < 11 ? (ml << s1) : (ml << 10);
-            t0 = 0;
+            // |lo| >= |hi| / 2: not a normalised double-double; fold lo in at
+            // 2^64 granularity (within 2^-52 of hi + lo relative to lo)
+            const int s1 = s - 64 < 10 ? s - 64 : 10;
+            uint32_t u[4];
+            shl53(mlh, ll, s1, u);
+            t[0] = 0; t[1] = 0; t[2] = u[0]; t[3] = u[1];
         } else if (s >= 0) {
-            t0 = ml << s;
-            t1 = s ? (ml >> (64 - s)) : 0;
+            shl53(mlh, ll, s, t);
         } else {
-            t0 = (-s < 64) ? (ml >> -s) : 0;
+            const int r = -s;   // right shift of the 53-bit mantissa
+            t[2] = t[3] = 0;
+            t[0] = r >= 64 ? 0u : (r >= 32 ? (mlh >> (r - 32)) : __funnelshift_r(ll, mlh, r));
+            t[1] = r >= 32 ? 0u : (mlh >> r);
         }
-        if ((bh ^ bl) >> 63) {   // lo has the opposite sign
-            const uint64_t borrow = t0 != 0;
-            o.x0 = 0 - t0;
-            o.x1 = mh - t1 - borrow;
+        if ((hh ^ lh) >> 31) {   // lo has the opposite sign
+            asm("sub.cc.u32 %0, %0, %4;\n\t"
+                "subc.cc.u32 %1, %1, %5;\n\t"
+                "subc.cc.u32 %2, %2, %6;\n\t"
+                "subc.u32 %3, %3, %7;"
+                : "+r"(o.w[0]), "+r"(o.w[1]), "+r"(o.w[2]), "+r"(o.w[3])
+                : "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]));
         } else {
-            o.x0 = t0;
-            o.x1 = mh + t1;
+            asm("add.cc.u32 %0, %0, %4;\n\t"
+                "addc.cc.u32 %1, %1, %5;\n\t"
+                "addc.cc.u32 %2, %2, %6;\n\t"
+                "addc.u32 %3, %3, %7;"
+                : "+r"(o.w[0]), "+r"(o.w[1]), "+r"(o.w[2]), "+r"(o.w[3])
+                : "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]));
         }
     }
     return o;
+}
+
+// W >> sh (0 <= sh < 128) in four words.
+__device__ __forceinline__ void shr128(const uint32_t w[4], int sh, uint32_t y[4])
+{
+    const int q = sh >> 5, r = sh & 31;
+    // word shift by q
+    const uint32_t a0 = q == 0 ? w[0] : (q == 1 ? w[1] : (q == 2 ? w[2] : w[3]));
+    const uint32_t a1 = q == 0 ? w[1] : (q == 1 ? w[2] : (q == 2 ? w[3] : 0u));
+    const uint32_t a2 = q == 0 ? w[2] : (q == 1 ? w[3] : 0u);
+    const uint32_t a3 = q == 0 ? w[3] : 0u;
+    y[0] = __funnelshift_r(a0, a1, r);
+    y[1] = __funnelshift_r(a1, a2, r);
+    y[2] = __funnelshift_r(a2, a3, r);
+    y[3] = a3 >> r;
 }
 
 // 256-bit two's complement accumulation of x * 2^s (x signed, s < 128).
@@ -145,14 +185,14 @@ __device__ __forceinline__ XF w256_to_xf(uint64_t W[4], int e)
     return r;
 }
 
-// Five unsigned 24-bit digits of a 120-bit integer (x1:x0), least significant first.
-__device__ __forceinline__ void digits24(uint64_t x1, uint64_t x0, int d[5])
+// Five unsigned 24-bit digits of a 120-bit integer in four words, least significant first.
+__device__ __forceinline__ void digits24(const uint32_t w[4], int d[5])
 {
-    d[0] = (int)(x0 & 0xFFFFFFu);
-    d[1] = (int)((x0 >> 24) & 0xFFFFFFu);
-    d[2] = (int)(((x0 >> 48) | (x1 << 16)) & 0xFFFFFFu);
-    d[3] = (int)((x1 >> 8) & 0xFFFFFFu);
-    d[4] = (int)((x1 >> 32) & 0xFFFFFFu);
+    d[0] = (int)(w[0] & 0xFFFFFFu);
+    d[1] = (int)(__funnelshift_r(w[0], w[1], 24) & 0xFFFFFFu);
+    d[2] = (int)(__funnelshift_r(w[1], w[2], 16) & 0xFFFFFFu);
+    d[3] = (int)(w[2] >> 8);
+    d[4] = (int)(w[3] & 0xFFFFFFu);
 }
 
 // y pre-split for repeated use (GEMV's x vector): Y's digits, exponent, flags.
@@ -166,7 +206,7 @@ struct Dig {
 __device__ __forceinline__ Dig to_dig(const Op &o)
 {
     Dig g;
-    digits24(o.x1, o.x0, g.d);
+    digits24(o.w, g.d);
     g.e = o.e;
     g.flags = o.flags;
     g.pad = 0;
@@ -210,7 +250,7 @@ struct Acc {
         for (int q = 0; q < 6; ++q) add_shifted(W, c[q], 24 * q);
     }
 
-    // move the block exponent up by d >= 1 bits
+    // move the block exponent up by d >= 1 bits (rare)
     __device__ __forceinline__ void raise(int d)
     {
         uint64_t W[4];
@@ -260,17 +300,11 @@ struct Acc {
             B = nb;
         }
         const int sh = B - ep;   // >= 2: X' = X >> sh < 2^116
-        uint64_t x1 = x.x1, x0 = x.x0;
         if (sh >= 118) return;
-        if (sh >= 64) {
-            x0 = x1 >> (sh - 64);
-            x1 = 0;
-        } else {
-            x0 = (x0 >> sh) | (x1 << (64 - sh));
-            x1 >>= sh;
-        }
+        uint32_t xs[4];
+        shr128(x.w, sh, xs);
         int a[5];
-        digits24(x1, x0, a);
+        digits24(xs, a);
         if ((x.flags ^ y.flags) & kNeg) {
 #pragma unroll
             for (int t = 0; t < 5; ++t) a[t] = -a[t];
@@ -302,18 +336,6 @@ struct Acc {
         return w256_to_xf(W, B + 72);
     }
 };
-
-// An extended float as a decoded operand (for values produced by the CRT or
-// by a previous reduction): |v| = m * 2^e -> (x1:x0) with x1 < 2^54.
-__device__ __forceinline__ Op op_from_xf(const XF &v)
-{
-    Op o;
-    o.flags = (v.neg ? kNeg : 0) | (v.zero ? kZero : 0);
-    o.x1 = (uint64_t)(v.m >> 74);
-    o.x0 = (uint64_t)(v.m >> 10);
-    o.e = v.e + 10;
-    return o;
-}
 
 // Extended-float warp reduction (lane 0 holds the sum; fixed order).
 __device__ __forceinline__ XF xf_shfl_down(const XF &v, int off)
@@ -362,18 +384,18 @@ __device__ __forceinline__ XF from_pod(const XFPod &p)
     return v;
 }
 
-// A decoded operand in the same 24-byte form.
+// A decoded operand in a 24-byte form.
 struct OpPod {
-    unsigned long long x1, x0;
+    uint32_t w[4];
     int e;
-    unsigned int flags;
+    uint32_t flags;
 };
 
 __device__ __forceinline__ OpPod to_pod(const Op &o)
 {
     OpPod p;
-    p.x1 = o.x1;
-    p.x0 = o.x0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) p.w[t] = o.w[t];
     p.e = o.e;
     p.flags = o.flags;
     return p;
@@ -382,8 +404,8 @@ __device__ __forceinline__ OpPod to_pod(const Op &o)
 __device__ __forceinline__ Op from_pod(const OpPod &p)
 {
     Op o;
-    o.x1 = p.x1;
-    o.x0 = p.x0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) o.w[t] = p.w[t];
     o.e = p.e;
     o.flags = p.flags;
     return o;

@@ -25,21 +25,30 @@ __device__ __forceinline__ void dd_digits(double2 v, int sh, int d[5])
     for (int t = 0; t < 5; ++t) d[t] = 0;
     const fx::Op o = fx::decode(v);
     if (o.flags & (fx::kZero | fx::kBad)) return;   // non-finite rows are handled by the epilogue
-    const int r = -(o.e + sh);   // N = (x1:x0) * 2^-r; r >= 2 for in-range values
+    const int r = -(o.e + sh);   // N = W * 2^-r; r >= 2 for in-range values
     if (r >= 118 || r < 1) return;
-    const unsigned __int128 X = ((unsigned __int128)o.x1 << 64) | o.x0;
-    unsigned __int128 N = (X >> r) + (unsigned __int128)((X >> (r - 1)) & 1);
+    uint32_t y[4], h[4];
+    fx::shr128(o.w, r, y);
+    fx::shr128(o.w, r - 1, h);   // rounding bit
+    const uint32_t rb = h[0] & 1u;
+    asm("add.cc.u32 %0, %0, %4;\n\t"
+        "addc.cc.u32 %1, %1, 0;\n\t"
+        "addc.cc.u32 %2, %2, 0;\n\t"
+        "addc.u32 %3, %3, 0;"
+        : "+r"(y[0]), "+r"(y[1]), "+r"(y[2]), "+r"(y[3])
+        : "r"(rb));
+    int u[5];
+    fx::digits24(y, u);
+    // balanced digits: |d| <= 2^23
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-        int dt = (int)((uint32_t)N & 0xFFFFFFu);
-        if (dt >= 0x800000) {
-            dt -= 0x1000000;
-            N += 0x1000000;
+        if (u[t] >= 0x800000) {
+            u[t] -= 0x1000000;
+            u[t + 1] += 1;
         }
-        N >>= 24;
-        d[t] = dt;
+        d[t] = u[t];
     }
-    d[4] = (int)(uint32_t)N;
+    d[4] = u[4];
     if (o.flags & fx::kNeg) {
 #pragma unroll
         for (int t = 0; t < 5; ++t) d[t] = -d[t];
