@@ -577,6 +577,20 @@ bool grouped_validate(const char *routine, int64_t count, const char *ta, const 
 
 }  // namespace
 
+// Grouped GEMM for the library's own use (device arrays, arguments already
+// valid): its own plan, default split policy, stream-ordered (no sync).
+bool grouped_gemm_device(int64_t count, const char *ta, const char *tb, const int64_t *m, const int64_t *n,
+                         const int64_t *k, const mwblas_real64x2 *alpha, const mwblas_real64x2 *const *a,
+                         const int64_t *lda, const mwblas_real64x2 *const *b, const int64_t *ldb,
+                         const mwblas_real64x2 *beta, mwblas_real64x2 *const *c, const int64_t *ldc,
+                         const char *routine)
+{
+    if (count == 0) return true;
+    static thread_local Plan internal;
+    build_descs(internal, count, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, g_default_policy);
+    return prepare_and_launch(internal, routine);
+}
+
 }  // namespace mw
 
 using mw::Plan;

@@ -19,6 +19,9 @@
 //    libraries do for their TRSM;
 //  * with few, each block is solved by substitution in double-double, one
 //    thread per right-hand side.
+#include <algorithm>
+#include <vector>
+
 #include "dd.cuh"
 #include "fixacc.cuh"
 #include "level3.h"
@@ -251,8 +254,9 @@ bool trsm_update(bool left, int64_t m, int64_t n, int64_t k, const void *Ablk, i
 // Leaf by explicit block inverse: X_blk = Inv_blk * B_blk (side L) or
 // B_blk * Inv_blk (side R) as one GEMM into T, copied back into B.
 struct TrsmInv {
-    const double2 *inv = nullptr;   // diagonal-block inverses (k_trsm_diag_inv)
-    double2 *T = nullptr;           // kTrsmLeaf x nrhs (or nrhs x kTrsmLeaf) scratch
+    const double2 *inv = nullptr;   // inverses of the leaf diagonal blocks, block b at inv + b*nb*nb (ld nb)
+    int64_t nb = kTrsmLeaf;         // leaf (and inverse block) order
+    double2 *T = nullptr;           // nb x nrhs (or nrhs x nb) scratch
 };
 
 bool trsm_leaf_inv(bool left, int64_t o, int64_t na, int64_t nrhs, const TrsmInv &w, double2 *B, int64_t ldb,
@@ -262,16 +266,16 @@ bool trsm_leaf_inv(bool left, int64_t o, int64_t na, int64_t nrhs, const TrsmInv
     g.alpha = dd_host{1.0, 0.0};
     g.beta = dd_host{0.0, 0.0};
     g.beta_kind = 0;
-    const double2 *blk = w.inv + (o / kInvNB) * kInvNB * kInvNB;
+    const double2 *blk = w.inv + (o / w.nb) * w.nb * w.nb;
     if (left) {
         g.m = na; g.n = nrhs; g.k = na;
-        g.A = blk; g.lda = kInvNB; g.ta = false;
+        g.A = blk; g.lda = w.nb; g.ta = false;
         g.B = B + o; g.ldb = ldb; g.tb = false;
         g.C = w.T; g.ldc = na;
     } else {
         g.m = nrhs; g.n = na; g.k = na;
         g.A = B + o * ldb; g.lda = ldb; g.ta = false;
-        g.B = blk; g.ldb = kInvNB; g.tb = false;
+        g.B = blk; g.ldb = w.nb; g.tb = false;
         g.C = w.T; g.ldc = nrhs;
     }
     if (!run_gemm(g, false, -1, routine)) return false;
@@ -285,8 +289,9 @@ bool trsm_leaf_inv(bool left, int64_t o, int64_t na, int64_t nrhs, const TrsmInv
 bool trsm_rec(bool left, bool lower, bool trans, bool unit, int64_t o, int64_t na, int64_t nrhs, const void *A,
               int64_t lda, double2 *B, int64_t ldb, const TrsmInv &w, const char *routine)
 {
-    if (na <= kTrsmLeaf && w.inv) return trsm_leaf_inv(left, o, na, nrhs, w, B, ldb, routine);
-    if (na <= kTrsmLeaf) {
+    const int64_t leaf = w.inv ? w.nb : kTrsmLeaf;
+    if (na <= leaf && w.inv) return trsm_leaf_inv(left, o, na, nrhs, w, B, ldb, routine);
+    if (na <= leaf) {
         if (left)
             k_trsm_diag_left<<<blocks_for(nrhs, 64), 64, 0, stream()>>>(o, (int)na, nrhs, (const double2 *)A, lda,
                                                                       trans, lower, unit, B, ldb);
@@ -296,8 +301,8 @@ bool trsm_rec(bool left, bool lower, bool trans, bool unit, int64_t o, int64_t n
         count_launch();
         return true;
     }
-    int64_t h = (na / 2 + kTrsmLeaf - 1) / kTrsmLeaf * kTrsmLeaf;
-    if (h >= na) h = na - kTrsmLeaf;
+    int64_t h = (na / 2 + leaf - 1) / leaf * leaf;
+    if (h >= na) h = na - leaf;
     const int64_t o1 = o, n1 = h, o2 = o + h, n2 = na - h;
     if (left) {
         // rows of B: first block B1 = rows o1.., second B2 = rows o2..
@@ -334,6 +339,88 @@ bool trsm_rec(bool left, bool lower, bool trans, bool unit, int64_t o, int64_t n
     return trsm_rec(false, lower, trans, unit, o1, n1, nrhs, A, lda, B, ldb, w, routine);
 }
 
+// Copies the two half-block inverses into the diagonal of each merged block
+// and zeroes its off-diagonal triangle (upper right for lower, lower left for
+// upper). One CTA per merged block.
+__global__ void k_inv_merge_copy(int64_t na, int64_t S, const double2 *__restrict__ src, double2 *__restrict__ dst,
+                                 bool lower)
+{
+    const int64_t h = S / 2;
+    const int64_t o = (int64_t)blockIdx.x * S;
+    const int64_t n1 = min(h, na - o), n2 = max((int64_t)0, min(h, na - o - h));
+    const double2 *i1 = src + (2 * blockIdx.x) * h * h;
+    const double2 *i2 = src + (2 * blockIdx.x + 1) * h * h;
+    double2 *d = dst + (int64_t)blockIdx.x * S * S;
+    const int64_t nt = n1 + n2;
+    for (int64_t idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
+        const int64_t r = idx % nt, c = idx / nt;
+        double2 v = make_double2(0.0, 0.0);
+        if (r < n1 && c < n1) v = i1[r + c * h];
+        else if (r >= n1 && c >= n1) v = i2[(r - n1) + (c - n1) * h];
+        d[r + c * S] = v;   // the off-diagonal block is written by the GEMMs (lower: r >= n1, c < n1)
+        (void)lower;
+    }
+}
+
+// Doubles the order of the diagonal-block inverses from h to 2h:
+//   lower: inv [L11 0; L21 L22] = [I1 0; -I2 L21 I1  I2]
+//   upper: inv [U11 U12; 0 U22] = [I1 -I1 U12 I2; 0  I2]
+// with two grouped GEMMs over all merged blocks.
+bool trsm_merge_inverses(int64_t na, int64_t h, const void *A, int64_t lda, bool trans, bool lower,
+                         const double2 *src, double2 *dst, double2 *tmp, const char *routine)
+{
+    const int64_t S = 2 * h;
+    const int64_t nblk = (na + S - 1) / S;
+    k_inv_merge_copy<<<(unsigned)nblk, 256, 0, stream()>>>(na, S, src, dst, lower);
+    count_launch();
+    std::vector<int64_t> m1, n1, k1, lda1, ldb1, ldc1, m2, n2, k2, lda2, ldb2, ldc2;
+    std::vector<const mwblas_real64x2 *> a1, b1, a2, b2;
+    std::vector<mwblas_real64x2 *> c1, c2;
+    std::vector<char> t1a, t1b, t2a, t2b;
+    for (int64_t b = 0; b < nblk; ++b) {
+        const int64_t o = b * S;
+        const int64_t p1 = std::min(h, na - o), p2 = std::max((int64_t)0, std::min(h, na - o - h));
+        if (p2 == 0) continue;
+        const double2 *I1 = src + (2 * b) * h * h, *I2 = src + (2 * b + 1) * h * h;
+        double2 *T = tmp + b * h * h;
+        double2 *D = dst + b * S * S;
+        if (lower) {
+            // T = L21 * I1 (p2 x p1), off = -(I2 * T) into D[p1:, 0:p1]
+            t1a.push_back(trans ? 'T' : 'N'); t1b.push_back('N');
+            m1.push_back(p2); n1.push_back(p1); k1.push_back(p1);
+            a1.push_back((const mwblas_real64x2 *)op_block(A, lda, trans, o + p1, o)); lda1.push_back(lda);
+            b1.push_back((const mwblas_real64x2 *)I1); ldb1.push_back(h);
+            c1.push_back((mwblas_real64x2 *)T); ldc1.push_back(h);
+            t2a.push_back('N'); t2b.push_back('N');
+            m2.push_back(p2); n2.push_back(p1); k2.push_back(p2);
+            a2.push_back((const mwblas_real64x2 *)I2); lda2.push_back(h);
+            b2.push_back((const mwblas_real64x2 *)T); ldb2.push_back(h);
+            c2.push_back((mwblas_real64x2 *)(D + p1)); ldc2.push_back(S);
+        } else {
+            // T = U12 * I2 (p1 x p2), off = -(I1 * T) into D[0:p1, p1:]
+            t1a.push_back(trans ? 'T' : 'N'); t1b.push_back('N');
+            m1.push_back(p1); n1.push_back(p2); k1.push_back(p2);
+            a1.push_back((const mwblas_real64x2 *)op_block(A, lda, trans, o, o + p1)); lda1.push_back(lda);
+            b1.push_back((const mwblas_real64x2 *)I2); ldb1.push_back(h);
+            c1.push_back((mwblas_real64x2 *)T); ldc1.push_back(h);
+            t2a.push_back('N'); t2b.push_back('N');
+            m2.push_back(p1); n2.push_back(p2); k2.push_back(p1);
+            a2.push_back((const mwblas_real64x2 *)I1); lda2.push_back(h);
+            b2.push_back((const mwblas_real64x2 *)T); ldb2.push_back(h);
+            c2.push_back((mwblas_real64x2 *)(D + p1 * S)); ldc2.push_back(S);
+        }
+    }
+    const int64_t cnt = (int64_t)m1.size();
+    if (cnt == 0) return true;
+    std::vector<mwblas_real64x2> one((size_t)cnt, mwblas_real64x2{{1.0, 0.0}}),
+        mone((size_t)cnt, mwblas_real64x2{{-1.0, 0.0}}), zero((size_t)cnt, mwblas_real64x2{{0.0, 0.0}});
+    if (!grouped_gemm_device(cnt, t1a.data(), t1b.data(), m1.data(), n1.data(), k1.data(), one.data(), a1.data(),
+                             lda1.data(), b1.data(), ldb1.data(), zero.data(), c1.data(), ldc1.data(), routine))
+        return false;
+    return grouped_gemm_device(cnt, t2a.data(), t2b.data(), m2.data(), n2.data(), k2.data(), mone.data(), a2.data(),
+                               lda2.data(), b2.data(), ldb2.data(), zero.data(), c2.data(), ldc2.data(), routine);
+}
+
 }  // namespace
 
 bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_t n, dd_host alpha, const void *A,
@@ -354,21 +441,42 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
     // apply them as GEMMs; few: substitute directly.
     TrsmInv w;
     void *scratch = nullptr;
+    bool ok = true;
     if (nrhs >= 2 * kTrsmLeaf) {
-        const int64_t nblk = (na + kInvNB - 1) / kInvNB;
-        const size_t inv_bytes = (size_t)nblk * kInvNB * kInvNB * sizeof(double2);
-        const size_t t_bytes = (size_t)kTrsmLeaf * nrhs * sizeof(double2);
-        scratch = dev_alloc(inv_bytes + t_bytes, routine);
+        // leaf order: 64, doubled (by merging inverses with grouped GEMMs) to
+        // 256 when the right-hand sides make the leaf GEMMs worth it
+        const int64_t nb = (nrhs >= 256 && na >= 1024) ? 256 : kInvNB;
+        const int64_t nblk64 = (na + kInvNB - 1) / kInvNB;
+        const int64_t nblk = (na + nb - 1) / nb;
+        const size_t inv64_bytes = (size_t)nblk64 * kInvNB * kInvNB * sizeof(double2);
+        const size_t inv_bytes = (size_t)nblk * nb * nb * sizeof(double2);
+        const size_t t_bytes = (size_t)nb * nrhs * sizeof(double2);
+        // the merges' products: ceil(na / 2h) blocks of h x h at each level h
+        size_t m_elems = 0;
+        for (int64_t h = kInvNB; h < nb; h *= 2)
+            m_elems = std::max(m_elems, (size_t)((na + 2 * h - 1) / (2 * h)) * h * h);
+        const size_t m_bytes = (m_elems * sizeof(double2) + 255) / 256 * 256;
+        // [inverse buffer A][inverse buffer B][merge products][T]: merges ping-pong between A and B
+        const size_t buf_bytes = (std::max(inv64_bytes, inv_bytes) + 255) / 256 * 256;
+        scratch = dev_alloc(2 * buf_bytes + m_bytes + t_bytes, routine);
         if (!scratch) return false;
-        w.inv = (const double2 *)scratch;
-        w.T = (double2 *)((char *)scratch + inv_bytes);
+        double2 *bufA = (double2 *)scratch, *bufB = (double2 *)((char *)scratch + buf_bytes);
+        double2 *mtmp = (double2 *)((char *)scratch + 2 * buf_bytes);
+        w.T = (double2 *)((char *)scratch + 2 * buf_bytes + m_bytes);
         const size_t smem = 2 * (size_t)kInvNB * kInvNB * sizeof(fx::OpPod);
         cudaFuncSetAttribute(k_trsm_diag_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_trsm_diag_inv<<<(unsigned)nblk, kInvNB, smem, stream()>>>(na, (const double2 *)A, lda, trans, lower,
-                                                                   unit, (double2 *)scratch);
+        k_trsm_diag_inv<<<(unsigned)nblk64, kInvNB, smem, stream()>>>(na, (const double2 *)A, lda, trans, lower,
+                                                                     unit, bufA);
         count_launch();
+        double2 *cur = bufA, *nxt = bufB;
+        for (int64_t h = kInvNB; h < nb && ok; h *= 2) {
+                ok = trsm_merge_inverses(na, h, A, lda, trans, lower, cur, nxt, mtmp, routine);
+            std::swap(cur, nxt);
+        }
+        w.inv = cur;
+        w.nb = nb;
     }
-    const bool ok = trsm_rec(left, lower, trans, unit, 0, na, nrhs, A, lda, b, ldb, w, routine);
+    if (ok) ok = trsm_rec(left, lower, trans, unit, 0, na, nrhs, A, lda, b, ldb, w, routine);
     if (scratch) dev_free(scratch);
     return ok;
 }

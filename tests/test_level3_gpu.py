@@ -209,6 +209,36 @@ def test_mtrsm(gpu, oracle, rng, side, uplo, ta, diag):
         assert err <= max(20, 8 * na * na) * orc.EPS_DD, (m, n, err)
 
 
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("uplo", ["U", "L"])
+@pytest.mark.parametrize("ta", ["N", "T"])
+@pytest.mark.parametrize("diag", ["N", "U"])
+def test_mtrsm_merged_inverse_leaves(gpu, oracle, rng, side, uplo, ta, diag):
+    """order >= 1024 with >= 256 right-hand sides: 256 x 256 leaf inverses
+    built by merging 64 x 64 ones (the last block partial); 4 sampled
+    right-hand sides are checked against the oracle (they are independent)."""
+    na, nr = 1100, 300
+    m, n = (na, nr) if side == "L" else (nr, na)
+    A = dominant_triangle(rng, na, na)
+    B0 = mwb.dd_matrix(rng, m, n, m)
+    al = mwb.random_dd(rng, ())
+    got = B0.copy()
+    gpu.mtrsm(side, uplo, ta, diag, m, n, al, A, na, got, m)
+    assert gpu.last_error()[0] == 0, gpu.last_error()
+    pick = np.sort(rng.choice(nr, 4, replace=False))
+    if side == "L":
+        sub = np.ascontiguousarray(B0[pick])                  # 4 columns, na x 4
+        oracle.qtrsm("L", uplo, ta, diag, na, 4, al, A, na, sub, na)
+        g = got[pick]
+    else:
+        sub = np.ascontiguousarray(B0[:, pick])               # 4 rows: (na, 4) -> 4 x na with ld 4
+        oracle.qtrsm("R", uplo, ta, diag, 4, na, al, A, na, sub, 4)
+        g = got[:, pick]
+    err = orc.normwise_error(g, sub, orc.dd_abs(al) * orc.dd_absmax(B0))
+    assert err <= max(20, 8 * na * na) * orc.EPS_DD, err
+    assert err <= 1e-28, err   # well conditioned: far inside the reference's na^2 bound
+
+
 @pytest.mark.parametrize("trans", ["N", "T"])
 def test_mgemv(gpu, oracle, rng, trans):
     for (m, n, incx, incy) in [(1, 1, 1, 1), (17, 9, 1, 1), (300, 70, 2, -1), (70, 300, -3, 2), (1000, 4000, 1, 1)]:
