@@ -337,7 +337,9 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 2.0 * 4096 * 4096 * 256 / v / 1e6,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64x2 (double-double)",
-                "data": "synthetic", "config": dict(cfg, sample="4096x4096x256 sample of the 8192^3 workload"),
+                "data": "synthetic",
+                "config": dict(cfg, sample="4096x4096x256 sample of the 8192^3 workload",
+                               engine="the reference's mgemm_ on the host cores (OpenMP)"),
                 "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
                                             "d2h_bytes_per_step": 0}}
         print(json.dumps(line))

@@ -108,7 +108,7 @@ __global__ void k_trsm_diag_right(int64_t c0, int nb, int64_t nrows, const doubl
     }
 }
 
-// Inverses of the 64 x 64 diagonal blocks of op(A) (the last block may be
+// Inverses of the 32 x 32 diagonal blocks of op(A) (the last block may be
 // shorter), one CTA per block, thread per column c of the inverse: solve
 // op(A)_blk x = e_c by substitution over all rows (x is zero above c for a
 // lower triangle, so every thread walks the same rows and the block entries
@@ -117,7 +117,7 @@ __global__ void k_trsm_diag_right(int64_t c0, int nb, int64_t nrows, const doubl
 // multiplied by the double-double reciprocal of the diagonal, as the
 // reference's substitution does (mtrsm_serial.cpp:144).
 // Inv: block b at Inv + b*64*64, column-major with leading dimension 64.
-constexpr int kInvNB = 64;
+constexpr int kInvNB = 32;   // order of the directly inverted blocks (merged up to the leaf order)
 
 __global__ void __launch_bounds__(kInvNB) k_trsm_diag_inv(int64_t na, const double2 *__restrict__ A, int64_t lda,
                                                           bool trans, bool lower, bool unit, double2 *Inv)
@@ -351,15 +351,18 @@ __global__ void k_inv_merge_copy(int64_t na, int64_t S, const double2 *__restric
     const double2 *i1 = src + (2 * blockIdx.x) * h * h;
     const double2 *i2 = src + (2 * blockIdx.x + 1) * h * h;
     double2 *d = dst + (int64_t)blockIdx.x * S * S;
-    const int64_t nt = n1 + n2;
-    for (int64_t idx = threadIdx.x; idx < nt * nt; idx += blockDim.x) {
-        const int64_t r = idx % nt, c = idx / nt;
-        double2 v = make_double2(0.0, 0.0);
-        if (r < n1 && c < n1) v = i1[r + c * h];
-        else if (r >= n1 && c >= n1) v = i2[(r - n1) + (c - n1) * h];
-        d[r + c * S] = v;   // the off-diagonal block is written by the GEMMs (lower: r >= n1, c < n1)
-        (void)lower;
+    const int nt = (int)(n1 + n2), n1i = (int)n1, hi = (int)h, Si = (int)S;
+    // column per warp-strided loop, rows across the threads of a warp (coalesced)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int c = wid; c < nt; c += nw) {
+        for (int r = lane; r < nt; r += 32) {
+            double2 v = make_double2(0.0, 0.0);
+            if (r < n1i && c < n1i) v = i1[r + c * hi];
+            else if (r >= n1i && c >= n1i) v = i2[(r - n1i) + (c - n1i) * hi];
+            d[r + c * Si] = v;   // the off-diagonal block is then written by the GEMMs
+        }
     }
+    (void)lower;
 }
 
 // Doubles the order of the diagonal-block inverses from h to 2h:
@@ -443,9 +446,10 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
     void *scratch = nullptr;
     bool ok = true;
     if (nrhs >= 2 * kTrsmLeaf) {
-        // leaf order: 64, doubled (by merging inverses with grouped GEMMs) to
-        // 256 when the right-hand sides make the leaf GEMMs worth it
-        const int64_t nb = (nrhs >= 256 && na >= 1024) ? 256 : kInvNB;
+        // leaf order 64, or 256 when the right-hand sides make the leaf GEMMs
+        // worth it; the 32 x 32 inverses are doubled up to it by merging
+        // with grouped GEMMs
+        const int64_t nb = (nrhs >= 256 && na >= 1024) ? 256 : kTrsmLeaf;
         const int64_t nblk64 = (na + kInvNB - 1) / kInvNB;
         const int64_t nblk = (na + nb - 1) / nb;
         const size_t inv64_bytes = (size_t)nblk64 * kInvNB * kInvNB * sizeof(double2);

@@ -276,6 +276,7 @@ bool finish(const char *routine)
     if (st != cudaSuccess) return cuda_ok(st, routine, "kernel launch");
     if (t_sync || t_stream == nullptr) {
         if (!cuda_ok(cudaStreamSynchronize(stream()), routine, "stream synchronize")) return false;
+        return check_device_status(routine);   // cheap after the sync
     }
     return true;
 }

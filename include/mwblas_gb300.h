@@ -234,10 +234,12 @@ int mtrsm_grouped(int64_t count, char side, char uplo, char transa, char diag, c
 int mwblas_set_ozaki_bits(int bits);
 /* Moduli count used by the most recent Ozaki GEMM on this thread. */
 int mwblas_last_ozaki_moduli(void);
-/* Residue-GEMM unit of the Ozaki engine: 0 = tcgen05 tensor cores (default),
- * 1 = CUDA cores (an independent exact path used to cross-check the tensor
- * cores; the MWBLAS_OZAKI_MMA=simt environment variable selects it too).
- * Both produce bit-identical results. Returns the previous value. */
+/* Residue-GEMM unit of the Ozaki engine: 0 = tcgen05 tensor cores, one CTA
+ * per (modulus, tile) (default), 1 = CUDA cores (an independent exact path
+ * used to cross-check the tensor cores), 2 = tcgen05 in a persistent kernel
+ * (one CTA per SM walking the (modulus, tile) units). The MWBLAS_OZAKI_MMA
+ * environment variable ("simt", "persistent") selects them too. All produce
+ * bit-identical results. Returns the previous value. */
 int mwblas_set_ozaki_mma(int kind);
 
 /* Per-phase device timing of the Ozaki engine (CUDA events on the library

@@ -6,7 +6,8 @@
   e uniform in [-30, 30]);
 * the tcgen05 residue GEMM and the independent CUDA-core residue GEMM give
   bit-identical results (both are exact integer computations);
-* non-finite inputs take the FP64 engine (the integer scheme cannot carry them).
+* non-finite entries of A or B make their output rows/columns NaN, as the FP64
+  engine (and the reference's double-double products of an infinity) do.
 """
 import numpy as np
 import pytest
@@ -49,11 +50,36 @@ def test_tensor_core_and_cuda_core_paths_bit_identical(gpu, rng):
     B = mwb.dd_matrix(rng, k, n)
     al, be = mwb.random_dd(rng, ()), np.zeros(2)
     outs = []
-    for kind in (0, 1):
+    for kind in (0, 1, 2):   # per-tile tcgen05, CUDA cores, persistent tcgen05
         prev = gpu.lib.mwblas_set_ozaki_mma(kind)
         try:
             c = np.zeros((n, m, 2))
             gpu.mgemm("N", "N", m, n, k, al, A, m, B, k, be, c, m, engine="ozaki")
+            assert gpu.last_error()[0] == 0, gpu.last_error()
+            outs.append(c)
+        finally:
+            gpu.lib.mwblas_set_ozaki_mma(prev)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("k", [300, 512, 1024, 1500])
+@pytest.mark.parametrize("uplo", [0, 1])
+def test_persistent_tensor_core_kernel(gpu, rng, k, uplo):
+    """The persistent residue-GEMM kernel gives the per-tile kernel's bits for
+    one, two and more K chunks (512 each), full and triangular outputs."""
+    n = 700
+    A = mwb.dd_matrix(rng, n, k)
+    outs = []
+    for kind in (0, 2):
+        prev = gpu.lib.mwblas_set_ozaki_mma(kind)
+        try:
+            c = np.zeros((n, n, 2))
+            with engine(gpu, OZAKI):
+                if uplo:
+                    gpu.msyrk("U", "N", n, k, 1.0, A, n, 0.0, c, n)
+                else:
+                    gpu.mgemm("N", "T", n, n, k, 1.0, A, n, A, n, 0.0, c, n)
             assert gpu.last_error()[0] == 0, gpu.last_error()
             outs.append(c)
         finally:
@@ -83,7 +109,7 @@ def test_exponent_spread_stress(gpu, oracle, rng):
     assert float(rel.max()) <= 4 * k * orc.EPS_DD * 4
 
 
-def test_nonfinite_inputs_use_fp64_engine(gpu, rng):
+def test_nonfinite_inputs_match_fp64_engine(gpu, rng):
     m, n, k = 40, 30, 50
     A = mwb.dd_matrix(rng, m, k)
     B = mwb.dd_matrix(rng, k, n)
@@ -92,6 +118,12 @@ def test_nonfinite_inputs_use_fp64_engine(gpu, rng):
     gpu.mgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, c1, m, engine="ozaki")
     gpu.mgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, c2, m, engine="plain")
     np.testing.assert_array_equal(np.isfinite(c1), np.isfinite(c2))
+    assert np.all(np.isnan(c1[:, 5])) and np.all(np.isfinite(np.delete(c1, 5, axis=1)))
+    # column 7 of B as well, through the complex-free SYRK-free path with beta != 0
+    B[7, 2] = (np.nan, 0.0)
+    c3 = np.ones((n, m, 2))
+    gpu.mgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.5, c3, m, engine="ozaki")
+    assert np.all(np.isnan(c3[7, :])) and np.all(np.isnan(c3[:, 5]))
 
 
 def test_auto_engine_and_bits_control(gpu, oracle, rng):
