@@ -141,6 +141,20 @@ int mma_kind()
 
 // ---- device: residues -----------------------------------------------------------------------
 
+// rint(y) for |y| < 2^22 with two FP32 adds (round-to-nearest-even on the
+// 1.5 * 2^23 grid), keeping the rounding off the conversion unit.
+__device__ __forceinline__ float rint_small(float y)
+{
+    return __fsub_rn(__fadd_rn(y, 12582912.0f), 12582912.0f);
+}
+
+// The low 16 bits of a float holding an integer 0 <= v < 2^16, without a
+// float-to-int conversion (v + 2^23 puts the integer in the mantissa).
+__device__ __forceinline__ uint32_t small_uint(float v)
+{
+    return __float_as_uint(__fadd_rn(v, 8388608.0f)) & 0xFFFFu;
+}
+
 __device__ __forceinline__ __int128 fixed_round(double x, int s)
 {
     uint64_t b = (uint64_t)__double_as_longlong(x);
@@ -201,7 +215,7 @@ __device__ __forceinline__ float sym_residue4(const float (&fl)[kResLimbs], bool
     x = __fmaf_rn(fl[8], t2.x, x);
     x = __fmaf_rn(fl[9], t2.y, x);
     x = __fmaf_rn(fl[10], t2.z, x);
-    float qq = rintf(__fmul_rn(x, invp));
+    float qq = rint_small(__fmul_rn(x, invp));
     float rr = __fmaf_rn(-qq, p, x);   // in (-p, p)
     float half = 0.5f * p;
     rr = (rr > half) ? __fsub_rn(rr, p) : rr;
@@ -335,7 +349,7 @@ constexpr int TC_SMEM = TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + 1024 /*align*/ +
 
 __device__ __forceinline__ float mod_sym(float x, float p, float invp)
 {
-    float q = rintf(__fmul_rn(x, invp));
+    float q = rint_small(__fmul_rn(x, invp));
     return __fmaf_rn(-q, p, x);   // in (-p, p), exact
 }
 
@@ -469,8 +483,14 @@ __global__ void __launch_bounds__(192, 1)
         }
         if (ok) {
             // Both accumulators now hold reduced partial residues; combine and
-            // store c = (P + Q) mod p in [0, p) as R[l][j][i].
+            // store c = (P + Q) mod p in [0, p) as R[l][j][i] (32-bit index
+            // arithmetic inside the tile: 64-bit compares and multiplies issue
+            // at the FP64 rate on this part).
             const int64_t i = (int64_t)tile_m * TC_BM + row;
+            const int64_t j0 = (int64_t)tile_n * TC_BN;
+            const bool row_ok = i < M;
+            const int jn = (int)min((int64_t)TC_BN, N - j0);
+            uint16_t *q = R + ((int64_t)l * Np + j0) * Mp + i;   // advanced by Mp per column
 #pragma unroll 1
             for (int sl = 0; sl < TC_BN / 32; ++sl) {
                 uint32_t r0[32], r1[32];
@@ -481,12 +501,11 @@ __global__ void __launch_bounds__(192, 1)
                 for (int t = 0; t < 32; ++t) {
                     float v = __uint_as_float(r0[t]);
                     if (nch > 1) v = __fadd_rn(v, __uint_as_float(r1[t]));
-                    float fq = floorf(__fmul_rn(v, invp));
-                    float rr = __fmaf_rn(-fq, p, v);
+                    float fq = rint_small(__fmul_rn(v, invp));
+                    float rr = __fmaf_rn(-fq, p, v);   // in (-p, p)
                     if (rr < 0.0f) rr = __fadd_rn(rr, p);
-                    if (rr >= p) rr = __fsub_rn(rr, p);
-                    const int64_t j = (int64_t)tile_n * TC_BN + sl * 32 + t;
-                    if (i < M && j < N) R[((int64_t)l * Np + j) * Mp + i] = (uint16_t)(int)rr;
+                    if (row_ok && sl * 32 + t < jn) *q = (uint16_t)small_uint(rr);
+                    q += Mp;
                 }
             }
         }
@@ -660,6 +679,10 @@ __global__ void __launch_bounds__(192, 1)
             if (!ok) break;
             // both buffers hold reduced partial residues: c = (P + Q) mod p in [0, p) as R[l][j][i]
             const int64_t i = (int64_t)tm * TC_BM + row;
+            const int64_t j0 = (int64_t)tn * TC_BN;
+            const bool row_ok = i < M;
+            const int jn = (int)min((int64_t)TC_BN, N - j0);
+            uint16_t *q = R + ((int64_t)l * Np + j0) * Mp + i;   // advanced by Mp per column
 #pragma unroll 1
             for (int sl = 0; sl < TC_BN / 32; ++sl) {
                 uint32_t r0[32], r1[32];
@@ -670,12 +693,11 @@ __global__ void __launch_bounds__(192, 1)
                 for (int t = 0; t < 32; ++t) {
                     float v = __uint_as_float(r0[t]);
                     if (nch > 1) v = __fadd_rn(v, __uint_as_float(r1[t]));
-                    float fq = floorf(__fmul_rn(v, invp));
-                    float rr = __fmaf_rn(-fq, p, v);
+                    float fq = rint_small(__fmul_rn(v, invp));
+                    float rr = __fmaf_rn(-fq, p, v);   // in (-p, p)
                     if (rr < 0.0f) rr = __fadd_rn(rr, p);
-                    if (rr >= p) rr = __fsub_rn(rr, p);
-                    const int64_t j = (int64_t)tn * TC_BN + sl * 32 + t;
-                    if (i < M && j < N) R[((int64_t)l * Np + j) * Mp + i] = (uint16_t)(int)rr;
+                    if (row_ok && sl * 32 + t < jn) *q = (uint16_t)small_uint(rr);
+                    q += Mp;
                 }
             }
             // release the buffers of the last two chunks to the next unit
@@ -763,8 +785,16 @@ __device__ __forceinline__ XF crt_m(const OzCrtParams &K)
     return m;
 }
 
-// C(i, j) := alpha * X(i, j) * 2^-S2 + beta * C(i, j), real.
-__global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, const uint16_t *__restrict__ R,
+__device__ __forceinline__ bool finite_hi(double x)
+{
+    return ((__double2hiint(x) >> 20) & 0x7FF) != 0x7FF;   // exponent field test, no FP64 compare
+}
+
+// C(i, j) := alpha * X(i, j) * 2^-S2 + beta * C(i, j), real. Thread per row i,
+// columns j = blockIdx.y, blockIdx.y + gridDim.y, ...; m and n below 2^31
+// (the host routes larger sizes elsewhere), so the per-element index work is
+// 32-bit or pointer increments.
+__global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint16_t *__restrict__ R,
                                                         int64_t Mp, int64_t Np, const int *__restrict__ ea,
                                                         const int *__restrict__ eb, int bits, OzCrtParams K,
                                                         dd::real alpha, int alpha_one, dd::real beta, int beta_kind,
@@ -773,43 +803,52 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, co
     __shared__ CrtSmem sm;
     crt_smem_fill(sm, K);
     __syncthreads();
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const int nmod = K.nmod;
-    const XF Mx = crt_m(K);
-    const XF xa = xf_from_dd(alpha.hi, alpha.lo), xb = xf_from_dd(beta.hi, beta.lo);
-    for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    // alpha folded into M: alpha * X = T * (alpha M)
+    XF Mx = crt_m(K);
+    if (!alpha_one) Mx = xf_mul(xf_from_dd(alpha.hi, alpha.lo), Mx);
+    const XF xb = xf_from_dd(beta.hi, beta.lo);
+    const int eai = ea[i];
+    const int64_t plane = Np * Mp;
+    const int jstep = gridDim.y;
+    const uint16_t *rcol = R + (int64_t)blockIdx.y * Mp + i;
+    double2 *pc = C + i + (int64_t)blockIdx.y * ldc;
+    const int64_t rstep = (int64_t)jstep * Mp, cstep = (int64_t)jstep * ldc;
+    for (int j = blockIdx.y; j < n; j += jstep, rcol += rstep, pc += cstep) {
         if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
-        if (ea[i] >= 1024 || eb[j] >= 1024) {   // a non-finite entry in row i of op(A) or column j of op(B)
+        const int ebj = eb[j];
+        if (eai >= 1024 || ebj >= 1024) {   // a non-finite entry in row i of op(A) or column j of op(B)
             const double qnan = __longlong_as_double(0x7ff8000000000000ll);
-            C[i + j * ldc] = make_double2(qnan, qnan);
+            *pc = make_double2(qnan, qnan);
             continue;
         }
         XF v;
         v.zero = true; v.neg = false; v.m = 0; v.e = 0;
-        if (ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
+        if (eai > kNoExp / 2 && ebj > kNoExp / 2) {
             crt::Frac acc;
             acc.reset();
             // residues of all moduli: issue the loads of 8 planes at a time
             // so that their latencies overlap
-            const uint16_t *rp = R + j * Mp + i;
-            const int64_t plane = Np * Mp;
+            const uint16_t *q = rcol;
             int l = 0;
             for (; l + 8 <= nmod; l += 8) {
                 uint32_t c[8];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) c[u] = __ldcs(rp + (int64_t)(l + u) * plane);
+                for (int u = 0; u < 8; ++u) {
+                    c[u] = __ldcs(q);
+                    q += plane;
+                }
 #pragma unroll
                 for (int u = 0; u < 8; ++u) acc.add(sm.F[l + u], c[u]);
             }
-            for (; l < nmod; ++l) acc.add(sm.F[l], __ldcs(rp + (int64_t)l * plane));
-            v = acc.finish(Mx, (bits - 2 - ea[i]) + (bits - 2 - eb[j]));
+            for (; l < nmod; ++l, q += plane) acc.add(sm.F[l], __ldcs(q));
+            v = acc.finish(Mx, (bits - 2 - eai) + (bits - 2 - ebj));
         }
-        if (!alpha_one) v = xf_mul(xa, v);
-        double2 *pc = C + i + j * ldc;
         if (beta_kind != 0) {
             double2 c0 = *pc;
-            if (!isfinite(c0.x)) {
+            if (!finite_hi(c0.x)) {
                 // non-finite C: the double-double operators propagate it
                 dd::real cv = dd::make(c0.x, c0.y);
                 if (beta_kind == 2) cv = dd::mul_exact(cv, beta);
@@ -826,7 +865,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int64_t m, int64_t n, co
 
 // Complex: R holds the residues of P1 = Ar*Br, P2 = Ai*Bi and
 // P3 = (Ar+Ai)*(Br+Bi) as components 0..2; Re = P1 - P2, Im = P3 - P1 - P2.
-__global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, const uint16_t *__restrict__ R,
+__global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const uint16_t *__restrict__ R,
                                                           int64_t Mp, int64_t Np, const int *__restrict__ ea,
                                                           const int *__restrict__ eb, int bits, OzCrtParams K,
                                                           dd::cplx alpha, int alpha_one, dd::cplx beta,
@@ -836,18 +875,18 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, 
     __shared__ CrtSmem sm;
     crt_smem_fill(sm, K);
     __syncthreads();
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const int nmod = K.nmod;
     const int64_t cstride = (int64_t)nmod * Np * Mp;
     const XF Mx = crt_m(K);
     const XF ar = xf_from_dd(alpha.re.hi, alpha.re.lo), ai = xf_from_dd(alpha.im.hi, alpha.im.lo);
     const XF br = xf_from_dd(beta.re.hi, beta.re.lo), bi = xf_from_dd(beta.im.hi, beta.im.lo);
-    for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    for (int j = blockIdx.y; j < n; j += gridDim.y) {
         if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
         if (ea[i] >= 1024 || eb[j] >= 1024) {
             const double qnan = __longlong_as_double(0x7ff8000000000000ll);
-            double2 *pc = C + 2 * (i + j * ldc);
+            double2 *pc = C + 2 * (i + (int64_t)j * ldc);
             pc[0] = make_double2(qnan, qnan);
             pc[1] = make_double2(qnan, qnan);
             continue;
@@ -868,7 +907,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, 
                 accr.add(sm.F[l], (uint32_t)re);
                 acci.add(sm.F[l], (uint32_t)im);
             };
-            const uint16_t *rp = R + j * Mp + i;
+            const uint16_t *rp = R + (int64_t)j * Mp + i;
             const int64_t plane = Np * Mp;
             int l = 0;
             for (; l + 4 <= nmod; l += 4) {
@@ -895,10 +934,10 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int64_t m, int64_t n, 
             rr = xf_add(xf_mul(ar, vr), t);
             ri = xf_add(xf_mul(ar, vi), xf_mul(ai, vr));
         }
-        double2 *pc = C + 2 * (i + j * ldc);
+        double2 *pc = C + 2 * (i + (int64_t)j * ldc);
         if (beta_kind != 0) {
             double2 c0r = pc[0], c0i = pc[1];
-            if (!isfinite(c0r.x) || !isfinite(c0i.x)) {
+            if (!finite_hi(c0r.x) || !finite_hi(c0i.x)) {
                 dd::cplx c0;
                 c0.re = dd::make(c0r.x, c0r.y);
                 c0.im = dd::make(c0i.x, c0i.y);
@@ -1052,6 +1091,8 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     }
     const GemmArgs &g = g0;
     const int64_t m = g.m, n = g.n, k = g.k;
+    if (m > INT32_MAX || n > INT32_MAX)   // the reconstruction indexes rows and columns in 32 bits
+        return cplx ? gemm_plain_cplx(g, routine) : gemm_fixed_real(g, routine);
     const int nc = cplx ? 3 : 1;
     // Real SYRK (op(B) = op(A)^T on the same array): op(B)'s residue rows are
     // op(A)'s, so one conversion serves both operands; both then use the same
@@ -1171,7 +1212,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         dim3 grid((unsigned)((m + 255) / 256), blocks_cap(n));
         if (!cplx) {
             bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
-            k_oz_reconstruct<<<grid, 256, 0, stream()>>>(m, n, R, Mp, Np, ea, eb, bits, cp,
+            k_oz_reconstruct<<<grid, 256, 0, stream()>>>((int)m, (int)n, R, Mp, Np, ea, eb, bits, cp,
                                                         dd::make(g.alpha.hi, g.alpha.lo), alpha_one ? 1 : 0,
                                                         dd::make(g.beta.hi, g.beta.lo), g.beta_kind, (double2 *)g.C,
                                                         g.ldc, g.uplo);
@@ -1183,7 +1224,8 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
             be.im = dd::make(g.cbeta.im.hi, g.cbeta.im.lo);
             bool alpha_one = (g.calpha.re.hi == 1.0 && g.calpha.re.lo == 0.0 && g.calpha.im.hi == 0.0 &&
                               g.calpha.im.lo == 0.0);
-            k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>(m, n, R, Mp, Np, ea, eb, bits, cp, al, alpha_one ? 1 : 0,
+            k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>((int)m, (int)n, R, Mp, Np, ea, eb, bits, cp, al,
+                                                          alpha_one ? 1 : 0,
                                                           be, g.beta_kind, (double2 *)g.C, g.ldc, g.uplo,
                                                           g.herm ? 1 : 0, g.herm ? 1 : 0);
         }
