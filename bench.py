@@ -431,7 +431,7 @@ def tc_traffic_from_profile():
 # ---------------------------------------------------------------------------
 
 WORKLOADS = ("gemm", "stress", "wgemm", "gemm_t", "gemm_fixed", "gemm_plain", "syrk", "herk", "trsm", "gemv", "dot",
-             "axpy", "batched_gemm", "batched_trsm")
+             "axpy", "scal", "copy", "swap", "iamax", "batched_gemm", "batched_trsm")
 
 
 def _dev_dd(torch, shape, gen, dev, cplx_=False):
@@ -675,6 +675,37 @@ def run_workload(args):
             amax = float(A[..., 0].abs().max())
             op = orc.dd_abs(al) * n * amax * orc.dd_absmax(hb(x)) + orc.dd_abs(be) * orc.dd_absmax(hb(y0))
             check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+    elif w in ("scal", "copy", "swap", "iamax"):
+        # HBM-bound level-1 moves at n = 2^28 (SCAL bit-exact, FP64-bound by its operation sequence)
+        n = args.size or (1 << 28)
+        x = _dev_dd(torch, (n,), gen, dev)
+        y = _dev_dd(torch, (n,), gen, dev) if w in ("copy", "swap") else None
+        x0 = x.clone() if w == "scal" else None
+        if w == "scal":
+            fn = lambda: lib.mscal(n, al, x.data_ptr(), 1)
+            reset, nbytes = (lambda: x.copy_(x0)), 32.0 * n
+        elif w == "copy":
+            fn = lambda: lib.mcopy(n, x.data_ptr(), 1, y.data_ptr(), 1)
+            reset, nbytes = None, 32.0 * n
+        elif w == "swap":
+            fn = lambda: lib.mswap(n, x.data_ptr(), 1, y.data_ptr(), 1)
+            reset, nbytes = None, 64.0 * n
+        else:
+            out = {}
+            fn = lambda: out.__setitem__("i", lib.imamax(n, x.data_ptr(), 1))
+            reset, nbytes = None, 16.0 * n
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=reset)
+        value, unit = nbytes / ms / 1e6, "GB/s"
+        metric = f"DD-{w.upper()} HBM GB/s n={n} ({int(nbytes // n)}n bytes)"
+        cfg = {"workload": f"{'i' if w == 'iamax' else 'm'}{w if w != 'iamax' else 'mamax'}_ n={n} inc=1"}
+        roof = {"bound": "hbm" if w != "scal" else "fp64 (bit-exact operation sequence)", "achieved": value,
+                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": value / pk["hbm_gbs"], "peak_kind": pk_kind,
+                "traffic": None}
+        if w == "iamax" and o is not None:
+            hx = hb(x)
+            mag = np.abs(hx[:, 0])
+            want = int(np.argmax(mag)) + 1
+            check["index_matches_host_argmax_of_hi"] = (out["i"] == want)
     elif w in ("dot", "axpy"):
         n = args.size or (1 << 28)
         x = _dev_dd(torch, (n,), gen, dev)
