@@ -567,8 +567,14 @@ bool grouped_validate(const char *routine, int64_t count, const char *ta, const 
         if (lda[i] < std::max<int64_t>(1, nra)) { set_error(routine, 9, "lda too small in instance " + std::to_string(i)); return false; }
         if (ldb[i] < std::max<int64_t>(1, nrb)) { set_error(routine, 11, "ldb too small in instance " + std::to_string(i)); return false; }
         if (ldc[i] < std::max<int64_t>(1, m[i])) { set_error(routine, 14, "ldc too small in instance " + std::to_string(i)); return false; }
-        if (m[i] > 0 && n[i] > 0 && !is_device_pointer(c[i])) {
-            set_error(routine, 13, "grouped calls take device (or managed) arrays; C of instance " + std::to_string(i));
+        if (m[i] > 0 && n[i] > 0 && !is_dd_device_pointer(c[i])) {
+            set_error(routine, 13, "grouped calls take 16-byte aligned device (or managed) arrays; C of instance " +
+                                       std::to_string(i));
+            return false;
+        }
+        if (m[i] > 0 && n[i] > 0 && k[i] > 0 && !(is_dd_device_pointer(a[i]) && is_dd_device_pointer(b[i]))) {
+            set_error(routine, 8, "grouped calls take 16-byte aligned device (or managed) arrays; A or B of instance " +
+                                      std::to_string(i));
             return false;
         }
     }
@@ -717,9 +723,15 @@ extern "C" int mtrsm_grouped(int64_t count, char side, char uplo, char transa, c
         int64_t na = (S == 'L') ? m[i] : n[i];
         if (lda[i] < std::max<int64_t>(1, na)) { set_error(routine, 10, "lda too small in instance " + std::to_string(i)); return 10; }
         if (ldb[i] < std::max<int64_t>(1, m[i])) { set_error(routine, 12, "ldb too small in instance " + std::to_string(i)); return 12; }
-        if (!is_device_pointer(b[i])) {
-            set_error(routine, 11, "grouped calls take device (or managed) arrays; B of instance " + std::to_string(i));
+        if (!is_dd_device_pointer(b[i])) {
+            set_error(routine, 11, "grouped calls take 16-byte aligned device (or managed) arrays; B of instance " +
+                                       std::to_string(i));
             return 11;
+        }
+        if (!is_dd_device_pointer(a[i])) {
+            set_error(routine, 9, "grouped calls take 16-byte aligned device (or managed) arrays; A of instance " +
+                                      std::to_string(i));
+            return 9;
         }
         TrsmDesc d{};
         d.A = (const double2 *)a[i];

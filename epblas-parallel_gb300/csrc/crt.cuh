@@ -20,6 +20,7 @@
 // __host__ __device__ so the same code is unit-tested on the CPU.
 #pragma once
 #include "xfloat.cuh"
+#include "xword.cuh"
 
 #ifdef __CUDACC__
 #define CRT_HD __host__ __device__ __forceinline__
@@ -28,6 +29,20 @@
 #endif
 
 namespace crt {
+
+// The 128-bit extended float of xfloat.cuh in 32-bit words.
+CRT_HD xw::XW to_xw(const xfp::XF &x)
+{
+    if (x.zero) return xw::zero();
+    xw::XW r;
+    r.w[3] = (uint32_t)(x.m >> 96);
+    r.w[2] = (uint32_t)(x.m >> 64);
+    r.w[1] = (uint32_t)(x.m >> 32);
+    r.w[0] = (uint32_t)x.m;
+    r.e = x.e;
+    r.neg = x.neg ? 1u : 0u;
+    return r;
+}
 
 constexpr int kFL = 5;       // 32-bit limbs of the 160-bit fractions
 constexpr int kFLPad = 8;    // row stride (two 16-byte vectors)
@@ -86,6 +101,50 @@ struct Frac {
         }
         t = xfp::xf_norm(neg, m, e);
         xfp::XF r = xfp::xf_mul(t, Mx);
+        r.e -= S2;
+        return r;
+    }
+    // The same value in 32-bit words: X * 2^-S2 = T * M * 2^-S2 with T the
+    // signed 160-bit fraction; Mx = M (times any folded scale factor).
+    CRT_HD xw::XW finish_xw(const xw::XW &Mx, int S2) const
+    {
+        uint32_t x[kFL];
+        uint32_t carry = 0;
+        for (int t = 0; t < kFL; ++t) {
+            const uint64_t v = S[t] + carry;
+            x[t] = (uint32_t)v;
+            carry = (uint32_t)(v >> 32);
+        }
+        const uint32_t neg = x[kFL - 1] >> 31;
+        if (neg) {
+            uint32_t c = 1;
+            for (int t = 0; t < kFL; ++t) {
+                const uint32_t v = ~x[t] + c;
+                c = c & (x[t] == 0u);
+                x[t] = v;
+            }
+        }
+        // normalise |T| (bit 159 set), keep the top 128 bits
+        int sh = 0;
+        for (int k = 0; k < kFL - 1 && x[kFL - 1] == 0u; ++k) {
+            for (int t = kFL - 1; t > 0; --t) x[t] = x[t - 1];
+            x[0] = 0u;
+            sh += 32;
+        }
+        if (x[kFL - 1] == 0u) return xw::zero();
+        const int z = xw::clz32(x[kFL - 1]);
+        xw::XW r;
+        if (z) {
+            for (int t = kFL - 1; t > 0; --t) x[t] = xw::fshl(x[t - 1], x[t], z);
+            sh += z;
+        }
+        r.w[3] = x[4];
+        r.w[2] = x[3];
+        r.w[1] = x[2];
+        r.w[0] = x[1];
+        r.e = -128 - sh;
+        r.neg = neg;
+        r = xw::mul(r, Mx);
         r.e -= S2;
         return r;
     }

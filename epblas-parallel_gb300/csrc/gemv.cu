@@ -307,8 +307,9 @@ extern "C" int mgemv_n_noalloc(int64_t m, int64_t n, const mwblas_real64x2 *alph
     const bool alpha0 = (al.hi == 0.0 && al.lo == 0.0);
     const int bk = (be.hi == 0.0 && be.lo == 0.0) ? 0 : ((be.hi == 1.0 && be.lo == 0.0) ? 1 : 2);
     if (alpha0 && bk == 1) return 0;
-    if (!y || !is_device_pointer(y) || (!alpha0 && (!a || !x || !is_device_pointer(a) || !is_device_pointer(x)))) {
-        set_error(routine, 9, "A, x and y must be device or managed memory (this entry point stages nothing)");
+    if (!y || !is_dd_device_pointer(y) ||
+        (!alpha0 && (!a || !x || !is_dd_device_pointer(a) || !is_dd_device_pointer(x)))) {
+        set_error(routine, 9, "A, x and y must be 16-byte aligned device or managed memory (this entry point stages nothing)");
         return 9;
     }
     int dev = 0;

@@ -31,24 +31,43 @@ __device__ __forceinline__ int64_t vidx(int64_t i, int64_t n, int64_t inc)
     return inc >= 0 ? i * inc : (n - 1 - i) * (-inc);
 }
 
-// True when element i (0-based, unit stride) falls in the scalar tail of its
-// slice under a T-way blas_part_bound partition of [0, n).
-__device__ __forceinline__ bool in_tail(int64_t i, int64_t n, int64_t T)
-{
-    int64_t base = n / T, rem = n % T;
-    int64_t lo, len;
-    int64_t big = rem * (base + 1);
-    if (i < big) {
-        int64_t t = i / (base + 1);
-        lo = t * (base + 1);
-        len = base + 1;
-    } else {
-        int64_t t = rem + (i - big) / base;
-        lo = t * base + rem;
-        len = base;
+// Position of a thread's elements in the T-way blas_part_bound partition of
+// [0, n) (blas_omp.h:79-84): slice t has base + 1 elements for t < rem and
+// base after that. An element is in the scalar tail when it lies in the last
+// len % 4 elements of its slice. The slice of the thread's first element is
+// found with divisions once; after that the grid-stride walk only advances
+// the slice (the strided index moves forward), so the per-element test is
+// two compares instead of 64-bit divisions.
+struct SliceWalk {
+    int64_t base, rem, t, lo, len, tmax;
+
+    __device__ __forceinline__ void start(int64_t i, int64_t n, int64_t T)
+    {
+        tmax = T - 1;
+        base = n / T;
+        rem = n % T;
+        const int64_t big = rem * (base + 1);
+        if (i < big) {
+            t = i / (base + 1);
+            lo = t * (base + 1);
+            len = base + 1;
+        } else {
+            t = rem + (base ? (i - big) / base : 0);
+            lo = t * base + rem;
+            len = base;
+        }
     }
-    return (i - lo) >= (len & ~(int64_t)3);
-}
+    // i must not decrease between calls
+    __device__ __forceinline__ bool tail(int64_t i)
+    {
+        while (i >= lo + len && t < tmax) {   // every slice before the last is non-empty
+            lo += len;
+            ++t;
+            len = (t < rem) ? base + 1 : base;
+        }
+        return (i - lo) >= (len & ~(int64_t)3);
+    }
+};
 
 int grid_for(int64_t n)
 {
@@ -63,9 +82,12 @@ int grid_for(int64_t n)
 
 __global__ void k_mscal_unit(int64_t n, dd::real alpha, double2 *x, int64_t T)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    SliceWalk sw;
+    if (i0 < n) sw.start(i0, n, T);
+    for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         dd::real v = dd::load(x + i);
-        v = in_tail(i, n, T) ? dd::mul_exact(v, alpha) : dd::mul_fast(v, alpha);
+        v = sw.tail(i) ? dd::mul_exact(v, alpha) : dd::mul_fast(v, alpha);
         dd::store(x + i, v);
     }
 }
@@ -88,9 +110,12 @@ __global__ void k_mscal_strided(int64_t n, dd::real alpha, double2 *x, int64_t i
 
 __global__ void k_wscal_unit(int64_t n, dd::cplx alpha, double2 *x, int64_t T)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    SliceWalk sw;
+    if (i0 < n) sw.start(i0, n, T);
+    for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         dd::cplx v = dd::cload(x + 2 * i);
-        v = in_tail(i, n, T) ? dd::cmul_exact(v, alpha) : dd::cmul_fast(v, alpha);
+        v = sw.tail(i) ? dd::cmul_exact(v, alpha) : dd::cmul_fast(v, alpha);
         dd::cstore(x + 2 * i, v);
     }
 }
@@ -113,9 +138,12 @@ __global__ void k_wscal_strided(int64_t n, dd::cplx alpha, double2 *x, int64_t i
 
 __global__ void k_wmscal_unit(int64_t n, dd::real alpha, double2 *x, int64_t T)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    SliceWalk sw;
+    if (i0 < n) sw.start(i0, n, T);
+    for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         dd::cplx v = dd::cload(x + 2 * i);
-        if (in_tail(i, n, T)) {
+        if (sw.tail(i)) {
             v.re = dd::mul_exact(v.re, alpha);
             v.im = dd::mul_exact(v.im, alpha);
         } else {
@@ -152,10 +180,13 @@ __global__ void k_wmscal_strided(int64_t n, dd::real alpha, double2 *x, int64_t 
 
 __global__ void k_maxpy_unit(int64_t n, dd::real alpha, const double2 *x, double2 *y, int64_t T)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    SliceWalk sw;
+    if (i0 < n) sw.start(i0, n, T);
+    for (int64_t i = i0; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         dd::real xv = dd::load(x + i), yv = dd::load(y + i);
         dd::real r;
-        if (in_tail(i, n, T))
+        if (sw.tail(i))
             r = dd::add_exact(yv, dd::mul_exact(alpha, xv));
         else
             r = dd::add_fast(yv, dd::mul_fast(alpha, xv));
@@ -230,30 +261,91 @@ __global__ void k_swap(int64_t n, double2 *x, int64_t incx, double2 *y, int64_t 
 }
 
 // ---- I*AMAX ------------------------------------------------------------------
-// Key: lexicographic (|hi|, sign-adjusted lo) maximum, lowest index on ties
+// Order: lexicographic (|hi|, sign-adjusted lo) maximum, lowest index on ties
 // (imamax.cpp:43-72, mf_pred.h:60-63). Complex magnitude |re|+|im| uses the
 // scalar-operator add (iwamax.cpp:36-76).
+//
+// The comparison runs on the integer pipe: each magnitude becomes a 128-bit
+// unsigned key whose order is the FP64 order of (|hi|, lo). Word 0..1 hold the
+// bits of |hi| (monotone for non-negative doubles), words 2..3 the usual
+// orderable image of lo (negative: all bits inverted; positive: sign bit set),
+// with -0 mapped to +0 so the two zeros tie as they do under FP64 '=='. A NaN
+// hi gives the all-zero key and a NaN lo the zero low half, so a NaN never
+// beats a number, as with the reference's -inf-seeded vector scan in which
+// 'NaN > best' is false; among all-NaN inputs the lowest index wins.
 
 struct AmaxKey {
-    double h, l;
-    int64_t idx;   // 0-based; -1 = empty
+    uint32_t k[4];   // k[0] most significant
+    int64_t idx;     // 0-based; -1 = empty
 };
 
+__device__ __forceinline__ AmaxKey amax_key(uint4 v, int64_t idx)
+{
+    // v = {hi.lo32, hi.hi32, lo.lo32, lo.hi32}
+    AmaxKey r;
+    const uint32_t ah = v.y & 0x7fffffffu;
+    const bool hnan = ah > 0x7ff00000u || (ah == 0x7ff00000u && v.x != 0u);
+    const uint32_t lh = v.w ^ (v.y & 0x80000000u);   // lo, sign flipped when hi < 0
+    const uint32_t al = lh & 0x7fffffffu;
+    const bool lnan = al > 0x7ff00000u || (al == 0x7ff00000u && v.z != 0u);
+    const bool lzero = (al | v.z) == 0u;
+    const uint32_t m = (uint32_t)((int32_t)lh >> 31);
+    uint32_t k2 = lh ^ (m | 0x80000000u), k3 = v.z ^ m;
+    if (lzero) { k2 = 0x80000000u; k3 = 0u; }
+    if (lnan) { k2 = 0u; k3 = 0u; }
+    r.k[0] = hnan ? 0u : ah;
+    r.k[1] = hnan ? 0u : v.x;
+    r.k[2] = hnan ? 0u : k2;
+    r.k[3] = hnan ? 0u : k3;
+    r.idx = idx;
+    return r;
+}
+
+// a.k > b.k as 128-bit unsigned numbers: the borrow out of b - a.
+__device__ __forceinline__ bool key_gt(const AmaxKey &a, const AmaxKey &b)
+{
+    uint32_t borrow;
+    asm("{\n\t"
+        ".reg .u32 t;\n\t"
+        "sub.cc.u32 t, %4, %8;\n\t"
+        "subc.cc.u32 t, %3, %7;\n\t"
+        "subc.cc.u32 t, %2, %6;\n\t"
+        "subc.cc.u32 t, %1, %5;\n\t"
+        "subc.u32 %0, 0, 0;\n\t"
+        "}"
+        : "=r"(borrow)
+        : "r"(b.k[0]), "r"(b.k[1]), "r"(b.k[2]), "r"(b.k[3]), "r"(a.k[0]), "r"(a.k[1]), "r"(a.k[2]),
+          "r"(a.k[3]));
+    return borrow != 0u;
+}
+
+__device__ __forceinline__ bool key_eq(const AmaxKey &a, const AmaxKey &b)
+{
+    return ((a.k[0] ^ b.k[0]) | (a.k[1] ^ b.k[1]) | (a.k[2] ^ b.k[2]) | (a.k[3] ^ b.k[3])) == 0u;
+}
+
+// Merge order of two partial results (either may be empty).
 __device__ __forceinline__ bool amax_better(const AmaxKey &a, const AmaxKey &b)
 {
     if (a.idx < 0) return false;
     if (b.idx < 0) return true;
-    if (a.h > b.h || (a.h == b.h && a.l > b.l)) return true;
-    if (a.h == b.h && a.l == b.l && a.idx < b.idx) return true;
-    return false;
+    return key_gt(a, b) || (key_eq(a, b) && a.idx < b.idx);
 }
 
 __device__ __forceinline__ AmaxKey amax_shfl(const AmaxKey &k, int off)
 {
     AmaxKey r;
-    r.h = __shfl_down_sync(0xffffffffu, k.h, off);
-    r.l = __shfl_down_sync(0xffffffffu, k.l, off);
+#pragma unroll
+    for (int w = 0; w < 4; ++w) r.k[w] = __shfl_down_sync(0xffffffffu, k.k[w], off);
     r.idx = __shfl_down_sync(0xffffffffu, k.idx, off);
+    return r;
+}
+
+__device__ __forceinline__ AmaxKey amax_empty()
+{
+    AmaxKey r;
+    r.k[0] = r.k[1] = r.k[2] = r.k[3] = 0u;
+    r.idx = -1;
     return r;
 }
 
@@ -268,7 +360,7 @@ __device__ AmaxKey amax_block_reduce(AmaxKey k)
     if (lane == 0) sh[wid] = k;
     __syncthreads();
     if (wid == 0) {
-        k = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : AmaxKey{0.0, 0.0, -1};
+        k = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : amax_empty();
         for (int off = 16; off > 0; off >>= 1) {
             AmaxKey o = amax_shfl(k, off);
             if (amax_better(o, k)) k = o;
@@ -277,20 +369,47 @@ __device__ AmaxKey amax_block_reduce(AmaxKey k)
     return k;
 }
 
+__device__ __forceinline__ uint4 dd_bits(dd::real m)
+{
+    const unsigned long long h = (unsigned long long)__double_as_longlong(m.hi);
+    const unsigned long long l = (unsigned long long)__double_as_longlong(m.lo);
+    return make_uint4((uint32_t)h, (uint32_t)(h >> 32), (uint32_t)l, (uint32_t)(l >> 32));
+}
+
+// Within one thread the candidates arrive in increasing index order, so a
+// strict '>' keeps the lowest index among equal keys.
 template <bool CPLX>
 __global__ void k_iamax_partial(int64_t n, const double2 *x, int64_t inc, AmaxKey *part)
 {
-    AmaxKey best{0.0, 0.0, -1};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        dd::real m;
-        if (CPLX) {
-            const double2 *p = x + 2 * vidx(i, n, inc);
-            m = dd::add_exact(dd::mag(dd::load(p)), dd::mag(dd::load(p + 1)));
-        } else {
-            m = dd::mag(dd::load(x + vidx(i, n, inc)));
+    AmaxKey best = amax_empty();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (!CPLX && inc == 1) {
+        // unit stride: two adjacent elements (32 bytes) per thread and step
+        const uint4 *v = (const uint4 *)x;
+        const int64_t npair = n >> 1;
+        for (int64_t p = i0; p < npair; p += stride) {
+            const uint4 a = __ldcs(v + 2 * p), b = __ldcs(v + 2 * p + 1);
+            const AmaxKey ka = amax_key(a, 2 * p), kb = amax_key(b, 2 * p + 1);
+            if (best.idx < 0 || key_gt(ka, best)) best = ka;
+            if (key_gt(kb, best)) best = kb;
         }
-        AmaxKey c{m.hi, m.lo, i};
-        if (amax_better(c, best)) best = c;
+        if ((n & 1) && i0 == 0) {
+            const AmaxKey kl = amax_key(__ldcs(v + n - 1), n - 1);
+            if (best.idx < 0 || key_gt(kl, best)) best = kl;   // highest index: strict '>'
+        }
+    } else {
+        for (int64_t i = i0; i < n; i += stride) {
+            uint4 bits;
+            if (CPLX) {
+                const double2 *p = x + 2 * vidx(i, n, inc);
+                bits = dd_bits(dd::add_exact(dd::mag(dd::load(p)), dd::mag(dd::load(p + 1))));
+            } else {
+                bits = __ldcs((const uint4 *)(x + vidx(i, n, inc)));
+            }
+            const AmaxKey c = amax_key(bits, i);
+            if (best.idx < 0 || key_gt(c, best)) best = c;
+        }
     }
     best = amax_block_reduce(best);
     if (threadIdx.x == 0) part[blockIdx.x] = best;
@@ -298,7 +417,7 @@ __global__ void k_iamax_partial(int64_t n, const double2 *x, int64_t inc, AmaxKe
 
 __global__ void k_iamax_final(int nparts, const AmaxKey *part, int64_t *out)
 {
-    AmaxKey best{0.0, 0.0, -1};
+    AmaxKey best = amax_empty();
     for (int i = threadIdx.x; i < nparts; i += blockDim.x)
         if (amax_better(part[i], best)) best = part[i];
     best = amax_block_reduce(best);

@@ -47,6 +47,7 @@
 #include "runtime.h"
 #include "sm100.cuh"
 #include "crt.cuh"
+#include "fixacc.cuh"
 #include "xfloat.cuh"
 
 namespace mw {
@@ -69,7 +70,7 @@ struct Moduli {
 struct OzResParams {
     int nmod;
     float p[kMaxMod], invp[kMaxMod];
-    float t[kMaxMod][kResLimbs];   // 2^(11k) mod p
+    float t[kMaxMod][kResLimbs];   // 2^(11k) mod p, symmetric representative
 };
 
 // Per residue-GEMM batch entry z (component * nmod + modulus).
@@ -155,30 +156,6 @@ __device__ __forceinline__ uint32_t small_uint(float v)
     return __float_as_uint(__fadd_rn(v, 8388608.0f)) & 0xFFFFu;
 }
 
-__device__ __forceinline__ __int128 fixed_round(double x, int s)
-{
-    uint64_t b = (uint64_t)__double_as_longlong(x);
-    int ex = (int)((b >> 52) & 0x7FF);
-    uint64_t m = b & 0xFFFFFFFFFFFFFull;
-    if (ex == 0) {
-        if (m == 0) return 0;
-        ex = 1;
-    } else {
-        m |= 1ull << 52;
-    }
-    int sh = ex - 1075 + s;
-    unsigned __int128 mag;
-    if (sh >= 0) {
-        mag = (unsigned __int128)m << sh;
-    } else if (sh > -63) {
-        int r = -sh;
-        mag = (unsigned __int128)((m + (1ull << (r - 1))) >> r);
-    } else {
-        mag = 0;
-    }
-    __int128 v = (__int128)mag;
-    return (b >> 63) ? -v : v;
-}
 
 __device__ __forceinline__ float u11_to_float(uint32_t c)
 {
@@ -192,51 +169,69 @@ __device__ __forceinline__ float u11_to_float(uint32_t c)
 // limbs of |F| (bits <= 120 keeps |F| below 2^121).
 __device__ __forceinline__ void to_limbs(double2 v, int sc, float (&fl)[kResLimbs], bool &neg)
 {
-    __int128 F = fixed_round(v.x, sc) + fixed_round(v.y, sc);
-    neg = F < 0;
-    unsigned __int128 U = (unsigned __int128)(neg ? -F : F);
+    // |v| = W * 2^e exactly (fixacc.cuh's decode, 32-bit words); F = round(|v| * 2^sc) = round(W * 2^-r)
+    const fx::Op o = fx::decode(v);
+    neg = (o.flags & fx::kNeg) != 0;
+    uint32_t y[4] = {0u, 0u, 0u, 0u};
+    const int r = -(o.e + sc);
+    if (!(o.flags & (fx::kZero | fx::kBad)) && r >= 1 && r < 128) {
+        uint32_t h[4];
+        fx::shr128(o.w, r, y);
+        fx::shr128(o.w, r - 1, h);   // rounding bit
+        asm("add.cc.u32 %0, %0, %4;\n\t"
+            "addc.cc.u32 %1, %1, 0;\n\t"
+            "addc.cc.u32 %2, %2, 0;\n\t"
+            "addc.u32 %3, %3, 0;"
+            : "+r"(y[0]), "+r"(y[1]), "+r"(y[2]), "+r"(y[3])
+            : "r"(h[0] & 1u));
+    }
+    // 11-bit limbs: bits [11q, 11q + 11) of the 128-bit F
 #pragma unroll
-    for (int q = 0; q < kResLimbs; ++q) fl[q] = u11_to_float((uint32_t)(U >> (11 * q)) & 0x7FFu);
+    for (int q = 0; q < kResLimbs; ++q) {
+        const int b = 11 * q, w = b >> 5, sh = b & 31;
+        const uint32_t lo = y[w], hi = (w + 1 < 4) ? y[w + 1] : 0u;
+        fl[q] = u11_to_float(__funnelshift_r(lo, hi, sh) & 0x7FFu);
+    }
 }
 
-// Symmetric residue of +-|F| (11-bit limbs) modulo p, exact in fp32: the
-// limb dot product stays below 11 * 2047 * 361 < 2^24.
-__device__ __forceinline__ float sym_residue4(const float (&fl)[kResLimbs], bool neg, float4 t0, float4 t1, float4 t2,
-                                              float p, float invp)
+// Symmetric residues modulo p of two integers F given as signed 11-bit limbs
+// (|limb| <= 2047), with packed FP32 arithmetic (two lanes per instruction).
+// With symmetric constants |t_q| <= p/2 the limb dot product x is an exact
+// fp32 integer, |x| <= 11 * 2047 * p/2 < 2^22. The quotient estimate
+// y = fl(x * fl(1/p)) is within 11258 * 2^-24 + 2^-11 < 0.0012 of x/p; for odd
+// p, x/p is at least 1/(2p) >= 0.0013 away from a half-integer, so rint(y) is
+// the nearest integer to x/p and x - p * rint(y) (exact) lies in [-p/2, p/2].
+// For even p the same holds except at exact half-integers, where either
+// neighbour gives a residue of +-p/2. No correction step is needed.
+__device__ __forceinline__ float2 sym_residue2(const float2 (&fl)[kResLimbs], const float2 (&t)[12], float2 negp,
+                                               float2 invp)
 {
-    float x = __fmul_rn(fl[0], t0.x);
-    x = __fmaf_rn(fl[1], t0.y, x);
-    x = __fmaf_rn(fl[2], t0.z, x);
-    x = __fmaf_rn(fl[3], t0.w, x);
-    x = __fmaf_rn(fl[4], t1.x, x);
-    x = __fmaf_rn(fl[5], t1.y, x);
-    x = __fmaf_rn(fl[6], t1.z, x);
-    x = __fmaf_rn(fl[7], t1.w, x);
-    x = __fmaf_rn(fl[8], t2.x, x);
-    x = __fmaf_rn(fl[9], t2.y, x);
-    x = __fmaf_rn(fl[10], t2.z, x);
-    float qq = rint_small(__fmul_rn(x, invp));
-    float rr = __fmaf_rn(-qq, p, x);   // in (-p, p)
-    float half = 0.5f * p;
-    rr = (rr > half) ? __fsub_rn(rr, p) : rr;
-    rr = (rr < -half) ? __fadd_rn(rr, p) : rr;
-    return neg ? -rr : rr;
+    float2 x = __fmul2_rn(fl[0], t[0]);
+#pragma unroll
+    for (int q = 1; q < kResLimbs; ++q) x = __ffma2_rn(fl[q], t[q], x);
+    float2 y = __fmul2_rn(x, invp);
+    y = __fadd2_rn(y, make_float2(12582912.0f, 12582912.0f));    // rint for |y| < 2^22
+    y = __fadd2_rn(y, make_float2(-12582912.0f, -12582912.0f));
+    return __ffma2_rn(y, negp, x);
 }
 
-__device__ __forceinline__ float sym_wrap(float v, float p)
+// (a + b) wrapped back into [-p/2, p/2] for |a|, |b| <= p/2: the quotient is
+// -1, 0 or 1 and the estimate of (a + b)/p is exact to 2^-22.
+__device__ __forceinline__ float2 sym_wrap2(float2 a, float2 b, float2 negp, float2 invp)
 {
-    float half = 0.5f * p;
-    v = (v > half) ? __fsub_rn(v, p) : v;
-    return (v < -half) ? __fadd_rn(v, p) : v;
+    const float2 x = __fadd2_rn(a, b);
+    float2 y = __fmul2_rn(x, invp);
+    y = __fadd2_rn(y, make_float2(12582912.0f, 12582912.0f));
+    y = __fadd2_rn(y, make_float2(-12582912.0f, -12582912.0f));
+    return __ffma2_rn(y, negp, x);
 }
 
-__device__ __forceinline__ void store4h(__half *dst, const float (&v)[4])
+__device__ __forceinline__ void store4h(__half *dst, float2 a, float2 b)
 {
-    __half2 a = __floats2half2_rn(v[0], v[1]);
-    __half2 b = __floats2half2_rn(v[2], v[3]);
+    const __half2 ha = __floats2half2_rn(a.x, a.y), hb = __floats2half2_rn(b.x, b.y);
     uint2 u;
-    u.x = *reinterpret_cast<uint32_t *>(&a);
-    u.y = *reinterpret_cast<uint32_t *>(&b);
+    u.x = *reinterpret_cast<const uint32_t *>(&ha);
+    u.y = *reinterpret_cast<const uint32_t *>(&hb);
     *reinterpret_cast<uint2 *>(dst) = u;
 }
 
@@ -257,17 +252,16 @@ __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim,
 {
     constexpr int E = CPLX ? 2 : 1;
     __shared__ double2 tile[32][33][E];
-    __shared__ __align__(16) float s_t[kMaxMod][12];
-    __shared__ float s_p[kMaxMod], s_ip[kMaxMod];
+    __shared__ __align__(16) float2 s_t[kMaxMod][12];   // {t, t}
+    __shared__ __align__(16) float4 s_pp[kMaxMod];      // {-p, -p, 1/p, 1/p}
     const int nmod = P.nmod;
     for (int i = threadIdx.x; i < nmod * 12; i += blockDim.x) {
         int l = i / 12, q = i % 12;
-        s_t[l][q] = (q < kResLimbs) ? P.t[l][q] : 0.0f;
+        const float t = (q < kResLimbs) ? P.t[l][q] : 0.0f;
+        s_t[l][q] = make_float2(t, t);
     }
-    for (int i = threadIdx.x; i < nmod; i += blockDim.x) {
-        s_p[i] = P.p[i];
-        s_ip[i] = P.invp[i];
-    }
+    for (int i = threadIdx.x; i < nmod; i += blockDim.x)
+        s_pp[i] = make_float4(-P.p[i], -P.p[i], P.invp[i], P.invp[i]);
     const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
     {
         const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -296,45 +290,56 @@ __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim,
     const int e = (r < rows) ? rexp[r] : kNoExp;
     const bool live = e > kNoExp / 2;
     const int sc = bits - 2 - e;
-    float fr[4][kResLimbs], fi[CPLX ? 4 : 1][kResLimbs];
-    bool nr[4], ni[4];
+    // signed limbs of elements (cg, cg+1) and (cg+2, cg+3) in the two lanes
+    float2 fr[2][kResLimbs], fi[CPLX ? 2 : 1][kResLimbs];
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-        nr[v] = ni[v] = false;
+        float f[kResLimbs];
+        bool ng = false;
         if (live) {
-            to_limbs(tile[s][cg + v][0], sc, fr[v], nr[v]);
-            if (CPLX) {
-                to_limbs(tile[s][cg + v][E - 1], sc, fi[CPLX ? v : 0], ni[v]);
-                if (conj) ni[v] = !ni[v];
-            }
+            to_limbs(tile[s][cg + v][0], sc, f, ng);
         } else {
 #pragma unroll
+            for (int q = 0; q < kResLimbs; ++q) f[q] = 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < kResLimbs; ++q) {
+            const float sv = ng ? -f[q] : f[q];
+            if (v & 1) fr[v >> 1][q].y = sv;
+            else fr[v >> 1][q].x = sv;
+        }
+        if (CPLX) {
+            bool ngi = false;
+            if (live) {
+                to_limbs(tile[s][cg + v][E - 1], sc, f, ngi);
+                if (conj) ngi = !ngi;
+            }
+#pragma unroll
             for (int q = 0; q < kResLimbs; ++q) {
-                fr[v][q] = 0.0f;
-                if (CPLX) fi[CPLX ? v : 0][q] = 0.0f;
+                const float sv = ngi ? -f[q] : f[q];
+                if (v & 1) fi[CPLX ? v >> 1 : 0][q].y = sv;
+                else fi[CPLX ? v >> 1 : 0][q].x = sv;
             }
         }
     }
     const int64_t cstride = (int64_t)nmod * rows_pad * kpad;
     __half *o = out + (r * kpad + cb);
     for (int l = 0; l < nmod; ++l) {
-        const float4 t0 = *reinterpret_cast<const float4 *>(&s_t[l][0]);
-        const float4 t1 = *reinterpret_cast<const float4 *>(&s_t[l][4]);
-        const float4 t2 = *reinterpret_cast<const float4 *>(&s_t[l][8]);
-        const float p = s_p[l], ip = s_ip[l];
-        float rr[4];
+        float2 t[12];
 #pragma unroll
-        for (int v = 0; v < 4; ++v) rr[v] = sym_residue4(fr[v], nr[v], t0, t1, t2, p, ip);
-        store4h(o, rr);
+        for (int q = 0; q < 12; q += 2) {
+            const float4 u = *reinterpret_cast<const float4 *>(&s_t[l][q]);
+            t[q] = make_float2(u.x, u.y);
+            t[q + 1] = make_float2(u.z, u.w);
+        }
+        const float4 pp = s_pp[l];
+        const float2 negp = make_float2(pp.x, pp.y), invp = make_float2(pp.z, pp.w);
+        const float2 ra = sym_residue2(fr[0], t, negp, invp), rb = sym_residue2(fr[1], t, negp, invp);
+        store4h(o, ra, rb);
         if (CPLX) {
-            float ii[4], ss[4];
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                ii[v] = sym_residue4(fi[CPLX ? v : 0], ni[v], t0, t1, t2, p, ip);
-                ss[v] = sym_wrap(__fadd_rn(rr[v], ii[v]), p);
-            }
-            store4h(o + cstride, ii);
-            store4h(o + 2 * cstride, ss);
+            const float2 ia = sym_residue2(fi[0], t, negp, invp), ib = sym_residue2(fi[CPLX ? 1 : 0], t, negp, invp);
+            store4h(o + cstride, ia, ib);
+            store4h(o + 2 * cstride, sym_wrap2(ra, ia, negp, invp), sym_wrap2(rb, ib, negp, invp));
         }
         o += rows_pad * kpad;
     }
@@ -467,6 +472,7 @@ __global__ void __launch_bounds__(192, 1)
             // warp-uniform outcome before the .sync.aligned TMEM accesses
             if (!__all_sync(0xffffffffu, sm100::mbar_wait(&accf[b], (c >> 1) & 1, status, 4))) { ok = false; break; }
             sm100::tc_fence_after();
+            if (c >= nch - 2) continue;   // the last chunk of each buffer is reduced in the combine
 #pragma unroll 1
             for (int sl = 0; sl < TC_BN / 32; ++sl) {
                 uint32_t r[32];
@@ -482,10 +488,11 @@ __global__ void __launch_bounds__(192, 1)
             sm100::mbar_arrive(&acce[b]);
         }
         if (ok) {
-            // Both accumulators now hold reduced partial residues; combine and
-            // store c = (P + Q) mod p in [0, p) as R[l][j][i] (32-bit index
-            // arithmetic inside the tile: 64-bit compares and multiplies issue
-            // at the FP64 rate on this part).
+            // Both accumulators hold their last chunk's sums (below 2^24,
+            // exact); reduce each, combine and store c = (P + Q) mod p in
+            // [0, p) as R[l][j][i] (32-bit index arithmetic inside the tile:
+            // 64-bit compares and multiplies issue at the FP64 rate on this
+            // part).
             const int64_t i = (int64_t)tile_m * TC_BM + row;
             const int64_t j0 = (int64_t)tile_n * TC_BN;
             const bool row_ok = i < M;
@@ -499,8 +506,8 @@ __global__ void __launch_bounds__(192, 1)
                 sm100::tmem_wait_ld();
 #pragma unroll
                 for (int t = 0; t < 32; ++t) {
-                    float v = __uint_as_float(r0[t]);
-                    if (nch > 1) v = __fadd_rn(v, __uint_as_float(r1[t]));
+                    float v = mod_sym(__uint_as_float(r0[t]), p, invp);
+                    if (nch > 1) v = __fadd_rn(v, mod_sym(__uint_as_float(r1[t]), p, invp));
                     float fq = rint_small(__fmul_rn(v, invp));
                     float rr = __fmaf_rn(-fq, p, v);   // in (-p, p)
                     if (rr < 0.0f) rr = __fadd_rn(rr, p);
@@ -660,6 +667,7 @@ __global__ void __launch_bounds__(192, 1)
                 if (!__all_sync(0xffffffffu, sm100::mbar_wait(&accf[b], fcnt[b] & 1, status, 4))) { ok = false; break; }
                 ++fcnt[b];
                 sm100::tc_fence_after();
+                if (c >= nch - 2) continue;   // reduced in the combine
 #pragma unroll 1
                 for (int sl = 0; sl < TC_BN / 32; ++sl) {
                     uint32_t r[32];
@@ -671,13 +679,11 @@ __global__ void __launch_bounds__(192, 1)
                     sm100::tmem_st32(ta, r);
                 }
                 sm100::tmem_wait_st();
-                if (c < nch - 2) {   // chunk c + 2 of this unit accumulates onto it
-                    sm100::tc_fence_before();
-                    sm100::mbar_arrive(&acce[b]);
-                }
+                sm100::tc_fence_before();   // chunk c + 2 of this unit accumulates onto it
+                sm100::mbar_arrive(&acce[b]);
             }
             if (!ok) break;
-            // both buffers hold reduced partial residues: c = (P + Q) mod p in [0, p) as R[l][j][i]
+            // both buffers hold their last chunk's sums: c = (P + Q) mod p in [0, p) as R[l][j][i]
             const int64_t i = (int64_t)tm * TC_BM + row;
             const int64_t j0 = (int64_t)tn * TC_BN;
             const bool row_ok = i < M;
@@ -691,8 +697,8 @@ __global__ void __launch_bounds__(192, 1)
                 sm100::tmem_wait_ld();
 #pragma unroll
                 for (int t = 0; t < 32; ++t) {
-                    float v = __uint_as_float(r0[t]);
-                    if (nch > 1) v = __fadd_rn(v, __uint_as_float(r1[t]));
+                    float v = mod_sym(__uint_as_float(r0[t]), p, invp);
+                    if (nch > 1) v = __fadd_rn(v, mod_sym(__uint_as_float(r1[t]), p, invp));
                     float fq = rint_small(__fmul_rn(v, invp));
                     float rr = __fmaf_rn(-fq, p, v);   // in (-p, p)
                     if (rr < 0.0f) rr = __fadd_rn(rr, p);
@@ -754,13 +760,6 @@ using xfp::xf_add;
 using xfp::xf_from_dd;
 using xfp::xf_mul;
 
-__device__ __forceinline__ dd::real xf_dd(const XF &x)
-{
-    dd::real r;
-    xfp::xf_to_dd(x, r.hi, r.lo);
-    return r;
-}
-
 // Shared-memory copy of the CRT constants (broadcast reads; each row of F is
 // 32 bytes so a modulus' constants are two 16-byte loads).
 struct CrtSmem {
@@ -785,6 +784,15 @@ __device__ __forceinline__ XF crt_m(const OzCrtParams &K)
     return m;
 }
 
+__device__ __forceinline__ xw::XW crt_mw(const OzCrtParams &K) { return crt::to_xw(crt_m(K)); }
+
+__device__ __forceinline__ dd::real xw_dd(const xw::XW &x)
+{
+    dd::real r;
+    xw::to_dd(x, r.hi, r.lo);
+    return r;
+}
+
 __device__ __forceinline__ bool finite_hi(double x)
 {
     return ((__double2hiint(x) >> 20) & 0x7FF) != 0x7FF;   // exponent field test, no FP64 compare
@@ -807,9 +815,9 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
     if (i >= m) return;
     const int nmod = K.nmod;
     // alpha folded into M: alpha * X = T * (alpha M)
-    XF Mx = crt_m(K);
-    if (!alpha_one) Mx = xf_mul(xf_from_dd(alpha.hi, alpha.lo), Mx);
-    const XF xb = xf_from_dd(beta.hi, beta.lo);
+    xw::XW Mx = crt_mw(K);
+    if (!alpha_one) Mx = xw::mul(xw::from_dd(alpha.hi, alpha.lo), Mx);
+    const xw::XW xb = xw::from_dd(beta.hi, beta.lo);
     const int eai = ea[i];
     const int64_t plane = Np * Mp;
     const int jstep = gridDim.y;
@@ -824,8 +832,8 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
             *pc = make_double2(qnan, qnan);
             continue;
         }
-        XF v;
-        v.zero = true; v.neg = false; v.m = 0; v.e = 0;
+        xw::XW v;
+        v = xw::zero();
         if (eai > kNoExp / 2 && ebj > kNoExp / 2) {
             crt::Frac acc;
             acc.reset();
@@ -844,7 +852,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
                 for (int u = 0; u < 8; ++u) acc.add(sm.F[l + u], c[u]);
             }
             for (; l < nmod; ++l, q += plane) acc.add(sm.F[l], __ldcs(q));
-            v = acc.finish(Mx, (bits - 2 - eai) + (bits - 2 - ebj));
+            v = acc.finish_xw(Mx, (bits - 2 - eai) + (bits - 2 - ebj));
         }
         if (beta_kind != 0) {
             double2 c0 = *pc;
@@ -852,14 +860,14 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
                 // non-finite C: the double-double operators propagate it
                 dd::real cv = dd::make(c0.x, c0.y);
                 if (beta_kind == 2) cv = dd::mul_exact(cv, beta);
-                dd::store(pc, dd::add_exact(cv, xf_dd(v)));
+                dd::store(pc, dd::add_exact(cv, xw_dd(v)));
                 continue;
             }
-            XF xc = xf_from_dd(c0.x, c0.y);
-            if (beta_kind == 2) xc = xf_mul(xb, xc);
-            v = xf_add(v, xc);
+            xw::XW xc = xw::from_dd(c0.x, c0.y);
+            if (beta_kind == 2) xc = xw::mul(xb, xc);
+            v = xw::add(v, xc);
         }
-        dd::store(pc, xf_dd(v));
+        dd::store(pc, xw_dd(v));
     }
 }
 
@@ -879,9 +887,9 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
     if (i >= m) return;
     const int nmod = K.nmod;
     const int64_t cstride = (int64_t)nmod * Np * Mp;
-    const XF Mx = crt_m(K);
-    const XF ar = xf_from_dd(alpha.re.hi, alpha.re.lo), ai = xf_from_dd(alpha.im.hi, alpha.im.lo);
-    const XF br = xf_from_dd(beta.re.hi, beta.re.lo), bi = xf_from_dd(beta.im.hi, beta.im.lo);
+    const xw::XW Mx = crt_mw(K);
+    const xw::XW ar = xw::from_dd(alpha.re.hi, alpha.re.lo), ai = xw::from_dd(alpha.im.hi, alpha.im.lo);
+    const xw::XW br = xw::from_dd(beta.re.hi, beta.re.lo), bi = xw::from_dd(beta.im.hi, beta.im.lo);
     for (int j = blockIdx.y; j < n; j += gridDim.y) {
         if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
         if (ea[i] >= 1024 || eb[j] >= 1024) {
@@ -891,8 +899,8 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
             pc[1] = make_double2(qnan, qnan);
             continue;
         }
-        XF vr, vi;
-        vr.zero = vi.zero = true; vr.neg = vi.neg = false; vr.m = vi.m = 0; vr.e = vi.e = 0;
+        xw::XW vr, vi;
+        vr = vi = xw::zero();
         if (ea[i] > kNoExp / 2 && eb[j] > kNoExp / 2) {
             crt::Frac accr, acci;
             accr.reset();
@@ -924,15 +932,15 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
                 add_l(l, __ldcs(q), __ldcs(q + cstride), __ldcs(q + 2 * cstride));
             }
             const int S2 = (bits - 2 - ea[i]) + (bits - 2 - eb[j]);
-            vr = accr.finish(Mx, S2);
-            vi = acci.finish(Mx, S2);
+            vr = accr.finish_xw(Mx, S2);
+            vi = acci.finish_xw(Mx, S2);
         }
-        XF rr = vr, ri = vi;
+        xw::XW rr = vr, ri = vi;
         if (!alpha_one) {
-            XF t = xf_mul(ai, vi);
-            t.neg = !t.neg;
-            rr = xf_add(xf_mul(ar, vr), t);
-            ri = xf_add(xf_mul(ar, vi), xf_mul(ai, vr));
+            xw::XW t = xw::mul(ai, vi);
+            t.neg ^= 1u;
+            rr = xw::add(xw::mul(ar, vr), t);
+            ri = xw::add(xw::mul(ar, vi), xw::mul(ai, vr));
         }
         double2 *pc = C + 2 * (i + (int64_t)j * ldc);
         if (beta_kind != 0) {
@@ -950,32 +958,32 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
                     }
                 }
                 dd::cplx out;
-                out.re = dd::add_exact(c0.re, xf_dd(rr));
-                out.im = dd::add_exact(c0.im, xf_dd(ri));
+                out.re = dd::add_exact(c0.re, xw_dd(rr));
+                out.im = dd::add_exact(c0.im, xw_dd(ri));
                 if (herm && i == j) out.im = dd::make(0.0, 0.0);
                 dd::cstore(pc, out);
                 continue;
             }
-            XF cr = xf_from_dd(c0r.x, c0r.y), ci = xf_from_dd(c0i.x, c0i.y);
+            xw::XW cr = xw::from_dd(c0r.x, c0r.y), ci = xw::from_dd(c0i.x, c0i.y);
             if (beta_kind == 2) {
                 if (real_beta) {
-                    cr = xf_mul(br, cr);
-                    ci = xf_mul(br, ci);
+                    cr = xw::mul(br, cr);
+                    ci = xw::mul(br, ci);
                 } else {
-                    XF t = xf_mul(bi, ci);
-                    t.neg = !t.neg;
-                    XF nr = xf_add(xf_mul(br, cr), t);
-                    XF ni = xf_add(xf_mul(br, ci), xf_mul(bi, cr));
+                    xw::XW t = xw::mul(bi, ci);
+                    t.neg ^= 1u;
+                    xw::XW nr = xw::add(xw::mul(br, cr), t);
+                    xw::XW ni = xw::add(xw::mul(br, ci), xw::mul(bi, cr));
                     cr = nr;
                     ci = ni;
                 }
             }
-            rr = xf_add(rr, cr);
-            ri = xf_add(ri, ci);
+            rr = xw::add(rr, cr);
+            ri = xw::add(ri, ci);
         }
         dd::cplx out;
-        out.re = xf_dd(rr);
-        out.im = (herm && i == j) ? dd::make(0.0, 0.0) : xf_dd(ri);
+        out.re = xw_dd(rr);
+        out.im = (herm && i == j) ? dd::make(0.0, 0.0) : xw_dd(ri);
         dd::cstore(pc, out);
     }
 }
@@ -1028,7 +1036,7 @@ void fill_res_params(const Moduli &md, OzResParams &rp, OzModParams &mp)
         }
         int64_t t = 1;
         for (int q = 0; q < kResLimbs; ++q) {
-            rp.t[l][q] = (float)t;
+            rp.t[l][q] = (float)(t > p / 2 ? t - p : t);   // symmetric: |t| <= p/2
             t = (t * 2048) % p;
         }
     }

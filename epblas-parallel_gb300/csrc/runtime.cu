@@ -178,6 +178,10 @@ bool is_device_pointer(const void *p)
     return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
 }
 
+bool is_aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+bool is_dd_device_pointer(const void *p) { return is_aligned16(p) && is_device_pointer(p); }
+
 bool stage_matrix(Staged &s, const void *host, int64_t rows, int64_t cols, int64_t ld, size_t elem,
                   bool copy_in, const char *routine)
 {
@@ -188,7 +192,7 @@ bool stage_matrix(Staged &s, const void *host, int64_t rows, int64_t cols, int64
     s.ld = ld;
     s.elem = elem;
     if (rows <= 0 || cols <= 0) return true;
-    if (is_device_pointer(host)) {
+    if (is_dd_device_pointer(host)) {   // used in place; anything else is copied
         s.dev = const_cast<void *>(host);
         return true;
     }
@@ -198,7 +202,7 @@ bool stage_matrix(Staged &s, const void *host, int64_t rows, int64_t cols, int64
     s.owned = true;
     if (copy_in) {
         if (!cuda_ok(cudaMemcpy2DAsync(s.dev, (size_t)ld * elem, host, (size_t)ld * elem, (size_t)rows * elem,
-                                       (size_t)cols, cudaMemcpyHostToDevice, stream()),
+                                       (size_t)cols, cudaMemcpyDefault, stream()),
                      routine, "copy matrix to device"))
             return false;
     }
@@ -210,7 +214,7 @@ bool unstage_matrix(Staged &s, const char *routine)
     if (!s.owned || s.rows <= 0 || s.cols <= 0) return true;
     return cuda_ok(cudaMemcpy2DAsync(const_cast<void *>(s.host), (size_t)s.ld * s.elem, s.dev,
                                      (size_t)s.ld * s.elem, (size_t)s.rows * s.elem, (size_t)s.cols,
-                                     cudaMemcpyDeviceToHost, stream()),
+                                     cudaMemcpyDefault, stream()),
                    routine, "copy matrix to host");
 }
 
@@ -225,7 +229,7 @@ bool stage_vector(Staged &s, const void *host, int64_t n, int64_t inc, size_t el
     s.is_vector = true;
     dev_inc = inc;
     if (n <= 0) return true;
-    if (is_device_pointer(host)) {
+    if (is_dd_device_pointer(host)) {   // used in place; anything else is copied
         s.dev = const_cast<void *>(host);
         return true;
     }
@@ -238,11 +242,11 @@ bool stage_vector(Staged &s, const void *host, int64_t n, int64_t inc, size_t el
     if (copy_in) {
         bool ok;
         if (ainc <= 1)
-            ok = cuda_ok(cudaMemcpyAsync(s.dev, host, (size_t)cnt * elem, cudaMemcpyHostToDevice, stream()),
+            ok = cuda_ok(cudaMemcpyAsync(s.dev, host, (size_t)cnt * elem, cudaMemcpyDefault, stream()),
                          routine, "copy vector to device");
         else
             ok = cuda_ok(cudaMemcpy2DAsync(s.dev, elem, host, (size_t)ainc * elem, elem, (size_t)cnt,
-                                           cudaMemcpyHostToDevice, stream()),
+                                           cudaMemcpyDefault, stream()),
                          routine, "copy strided vector to device");
         if (!ok) return false;
     }
@@ -256,10 +260,10 @@ bool unstage_vector(Staged &s, const char *routine)
     int64_t cnt = (s.inc == 0) ? 1 : s.n;
     if (ainc <= 1)
         return cuda_ok(cudaMemcpyAsync(const_cast<void *>(s.host), s.dev, (size_t)cnt * s.elem,
-                                       cudaMemcpyDeviceToHost, stream()),
+                                       cudaMemcpyDefault, stream()),
                        routine, "copy vector to host");
     return cuda_ok(cudaMemcpy2DAsync(const_cast<void *>(s.host), (size_t)ainc * s.elem, s.dev, s.elem, s.elem,
-                                     (size_t)cnt, cudaMemcpyDeviceToHost, stream()),
+                                     (size_t)cnt, cudaMemcpyDefault, stream()),
                    routine, "copy strided vector to host");
 }
 

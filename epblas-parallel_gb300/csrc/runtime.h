@@ -52,6 +52,10 @@ void dev_free(void *p);
 
 // True when the pointer is device or managed memory that kernels may use.
 bool is_device_pointer(const void *p);
+bool is_aligned16(const void *p);
+// Device (or managed) memory at a 16-byte boundary: an array of double-double
+// elements that the kernels may read in place with 16-byte loads.
+bool is_dd_device_pointer(const void *p);
 
 // A device view of a caller array. If the caller's pointer is already device
 // memory it is used in place; otherwise a scratch copy is made.

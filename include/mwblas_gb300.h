@@ -206,7 +206,8 @@ void mgemm_ozaki_64_(const char *transa, const char *transb, const int64_t *m,
 /* Batched uneven double-double GEMM (no reference counterpart): for
  * i < count, C[i] := alpha[i]*op(A[i])*op(B[i]) + beta[i]*C[i], with per-instance
  * flags transa[i]/transb[i], sizes and leading dimensions. The matrix pointers
- * must be device (or managed) memory; the per-instance arrays are host arrays.
+ * must be 16-byte aligned device (or managed) memory; the per-instance arrays
+ * are host arrays.
  * One persistent kernel runs every instance, launched from a CUDA graph that is
  * reused while the batch layout is unchanged. Returns 0 or an error code. */
 int mgemm_grouped(int64_t count, const char *transa, const char *transb, const int64_t *m, const int64_t *n,

@@ -122,6 +122,65 @@ def test_amax_exact_index(gpu, oracle, rng):
             assert gpu.imamax(n, cx, inc, cplx_=True) == oracle.iwamax(n, cx, inc)
 
 
+def test_amax_special_values(gpu, oracle, rng):
+    """Signed zeros tie, infinities and the lo limb order as FP64 '>' does, and
+    a NaN never beats a number (the reference's -inf-seeded vector scan,
+    imamax.cpp:88-131, used for unit stride and n >= 8)."""
+    for n in [64, 4099, 100003]:
+        x = vec(rng, n, 1)
+        p = np.sort(rng.choice(n, size=6, replace=False))
+        x[p[0]] = (7.0, -0.0)
+        x[p[1]] = (-7.0, 0.0)          # magnitude (7, -0): ties with p[0]
+        assert gpu.imamax(n, x, 1) == oracle.imamax(n, x, 1) == p[0] + 1
+        x[p[2]] = (-7.0, -2.0 ** -60)  # magnitude (7, +2^-60) wins
+        assert gpu.imamax(n, x, 1) == oracle.imamax(n, x, 1) == p[2] + 1
+        x[p[3]] = (-np.inf, 0.0)
+        x[p[4]] = (np.inf, 0.0)
+        assert gpu.imamax(n, x, 1) == oracle.imamax(n, x, 1) == p[3] + 1
+        y = vec(rng, n, 1)
+        y[0] = (np.nan, 0.0)
+        y[p[5]] = (np.nan, np.nan)
+        clean = y.copy()
+        clean[0] = clean[p[5]] = (0.0, 0.0)
+        assert gpu.imamax(n, y, 1) == oracle.imamax(n, clean, 1)
+        allnan = np.full((n, 2), np.nan)
+        assert gpu.imamax(n, allnan, 1) == 1
+
+
+def test_misaligned_device_operands_are_staged(gpu, oracle, rng):
+    """A device array that is only 8-byte aligned is copied to an aligned
+    buffer (and back when written) instead of being read with 16-byte loads."""
+    import torch
+    n = 3001
+    x = mwb.random_dd(rng, (n,))
+    y = mwb.random_dd(rng, (n,))
+    a = mwb.random_dd(rng, ())
+    buf = torch.zeros(4 * n + 8, dtype=torch.float64, device="cuda")
+    xd = buf[1:1 + 2 * n]
+    yd = buf[2 * n + 3:2 * n + 3 + 2 * n]
+    assert xd.data_ptr() % 16 == 8 and yd.data_ptr() % 16 == 8
+    xd.copy_(torch.from_numpy(x.reshape(-1)))
+    yd.copy_(torch.from_numpy(y.reshape(-1)))
+    want = y.copy(); oracle.maxpy(n, a, x, 1, want, 1, team=1)
+    gpu.lib.mwblas_set_l1_partition(1)
+    try:
+        gpu.maxpy(n, a, xd.data_ptr(), 1, yd.data_ptr(), 1)
+    finally:
+        gpu.lib.mwblas_set_l1_partition(0)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(yd.cpu().numpy().reshape(n, 2), want)
+    assert gpu.imamax(n, xd.data_ptr(), 1) == oracle.imamax(n, x, 1)
+    m = k = 40
+    A = mwb.random_dd(rng, (k, m))
+    B = mwb.random_dd(rng, (k, m))
+    Ad = torch.zeros(2 * m * k + 1, dtype=torch.float64, device="cuda")[1:]
+    Ad.copy_(torch.from_numpy(A.reshape(-1)))
+    C1 = np.zeros((m, m, 2)); C2 = np.zeros((m, m, 2))
+    gpu.mgemm("N", "N", m, m, k, (1.0, 0.0), A, m, B, k, (0.0, 0.0), C1, m)
+    gpu.mgemm("N", "N", m, m, k, (1.0, 0.0), Ad.data_ptr(), m, B, k, (0.0, 0.0), C2, m)
+    np.testing.assert_array_equal(C1, C2)
+
+
 def test_golden_amax_and_level1(gpu, golden):
     """The reference's own outputs from the golden fixtures, team 1."""
     z, meta = golden
