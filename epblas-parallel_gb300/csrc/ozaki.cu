@@ -105,7 +105,7 @@ Moduli choose_moduli(double need_bits)
 }
 
 int g_last_moduli = 0;
-int g_mma_kind = -1;   // 0 tcgen05, 1 SIMT cross-check
+int g_mma_kind = -1;   // 0 tcgen05 per tile, 1 SIMT cross-check, 2 tcgen05 persistent (default)
 
 // Optional per-phase timing with CUDA events on the library stream.
 enum { PH_EXP = 0, PH_RES, PH_GEMM, PH_REC, PH_N };
@@ -135,7 +135,7 @@ int mma_kind()
 {
     if (g_mma_kind < 0) {
         const char *e = getenv("MWBLAS_OZAKI_MMA");
-        g_mma_kind = (e && !strcmp(e, "simt")) ? 1 : ((e && !strcmp(e, "persistent")) ? 2 : 0);
+        g_mma_kind = (e && !strcmp(e, "simt")) ? 1 : ((e && !strcmp(e, "pertile")) ? 0 : 2);
     }
     return g_mma_kind;
 }
@@ -175,15 +175,16 @@ __device__ __forceinline__ void to_limbs(double2 v, int sc, float (&fl)[kResLimb
     uint32_t y[4] = {0u, 0u, 0u, 0u};
     const int r = -(o.e + sc);
     if (!(o.flags & (fx::kZero | fx::kBad)) && r >= 1 && r < 128) {
-        uint32_t h[4];
         fx::shr128(o.w, r, y);
-        fx::shr128(o.w, r - 1, h);   // rounding bit
+        // rounding bit: bit r - 1 of W
+        const int rb = r - 1, wq = rb >> 5;
+        const uint32_t word = wq == 0 ? o.w[0] : (wq == 1 ? o.w[1] : (wq == 2 ? o.w[2] : o.w[3]));
         asm("add.cc.u32 %0, %0, %4;\n\t"
             "addc.cc.u32 %1, %1, 0;\n\t"
             "addc.cc.u32 %2, %2, 0;\n\t"
             "addc.u32 %3, %3, 0;"
             : "+r"(y[0]), "+r"(y[1]), "+r"(y[2]), "+r"(y[3])
-            : "r"(h[0] & 1u));
+            : "r"((word >> (rb & 31)) & 1u));
     }
     // 11-bit limbs: bits [11q, 11q + 11) of the 128-bit F
 #pragma unroll
@@ -244,6 +245,20 @@ __device__ __forceinline__ void store4h(__half *dst, float2 a, float2 b)
 // complex multiply. A block converts a 32 x 32 tile; each thread converts four
 // consecutive elements of one row, so every modulus constant read from shared
 // memory serves four elements and the four residues leave as one 8-byte store.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes)
+{
+    const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+template <bool CPLX>
+constexpr size_t residue_smem_bytes()
+{
+    return 2 * 32 * 33 * (CPLX ? 2 : 1) * sizeof(double2);
+}
+
 template <bool ROWC, bool CPLX>
 __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim, const double2 *__restrict__ X,
                                                      int64_t ld, const int *__restrict__ rexp, int bits,
@@ -251,7 +266,9 @@ __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim,
                                                      int64_t kpad, int conj)
 {
     constexpr int E = CPLX ? 2 : 1;
-    __shared__ double2 tile[32][33][E];
+    extern __shared__ __align__(16) unsigned char res_smem[];
+    typedef double2 Tile[32][33][E];
+    Tile *tiles = reinterpret_cast<Tile *>(res_smem);   // two buffers
     __shared__ __align__(16) float2 s_t[kMaxMod][12];   // {t, t}
     __shared__ __align__(16) float4 s_pp[kMaxMod];      // {-p, -p, 1/p, 1/p}
     const int nmod = P.nmod;
@@ -262,87 +279,118 @@ __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim,
     }
     for (int i = threadIdx.x; i < nmod; i += blockDim.x)
         s_pp[i] = make_float4(-P.p[i], -P.p[i], P.invp[i], P.invp[i]);
-    const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
-    {
-        const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int ntc = (int)(kpad / 32);
+    const int ntiles = ntc * (int)(rows_pad / 32);
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    // Tile loads go through cp.async into the other buffer while this tile is
+    // converted (zero fill outside op(X)).
+    auto issue = [&](int tile, int buf) {
+        const int64_t r0 = (int64_t)(tile / ntc) * 32, c0 = (int64_t)(tile % ntc) * 32;
         for (int s = ty; s < 32; s += 8) {
-            int64_t r = ROWC ? r0 + tx : r0 + s;
-            int64_t c = ROWC ? c0 + s : c0 + tx;
-            double2 v[E];
+            const int64_t r = ROWC ? r0 + tx : r0 + s;
+            const int64_t c = ROWC ? c0 + s : c0 + tx;
+            const bool ok = r < rows && c < kdim;
+            const double2 *src = ok ? X + E * (ROWC ? r + c * ld : c + r * ld) : X;
 #pragma unroll
-            for (int w = 0; w < E; ++w) v[w] = make_double2(0.0, 0.0);
-            if (r < rows && c < kdim) {
-                const double2 *src = X + E * (ROWC ? r + c * ld : c + r * ld);
-#pragma unroll
-                for (int w = 0; w < E; ++w) v[w] = src[w];
-            }
-#pragma unroll
-            for (int w = 0; w < E; ++w) {
-                if (ROWC) tile[tx][s][w] = v[w];
-                else tile[s][tx][w] = v[w];
-            }
+            for (int w = 0; w < E; ++w)
+                cp_async16(ROWC ? &tiles[buf][tx][s][w] : &tiles[buf][s][tx][w], src + (ok ? w : 0), ok ? 16 : 0);
         }
-    }
-    __syncthreads();
+    };
+    int tile = blockIdx.x, buf = 0;
+    if (tile < ntiles) issue(tile, 0);
+    cp_async_commit();
     const int s = threadIdx.x >> 3, cg = (threadIdx.x & 7) * 4;
-    const int64_t r = r0 + s, cb = c0 + cg;
-    if (r >= rows_pad || cb >= kpad) return;
-    const int e = (r < rows) ? rexp[r] : kNoExp;
-    const bool live = e > kNoExp / 2;
-    const int sc = bits - 2 - e;
-    // signed limbs of elements (cg, cg+1) and (cg+2, cg+3) in the two lanes
-    float2 fr[2][kResLimbs], fi[CPLX ? 2 : 1][kResLimbs];
+    for (; tile < ntiles; tile += gridDim.x, buf ^= 1) {
+        const int next = tile + gridDim.x;
+        if (next < ntiles) issue(next, buf ^ 1);
+        cp_async_commit();
+        cp_async_wait1();   // this tile's group has landed
+        __syncthreads();
+        const int64_t r = (int64_t)(tile / ntc) * 32 + s, cb = (int64_t)(tile % ntc) * 32 + cg;
+        const int e = (r < rows) ? rexp[r] : kNoExp;
+        const bool live = e > kNoExp / 2;
+        const int sc = bits - 2 - e;
+        // signed limbs of elements (cg, cg+1) and (cg+2, cg+3) in the two lanes
+        float2 fr[2][kResLimbs], fi[CPLX ? 2 : 1][kResLimbs];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-        float f[kResLimbs];
-        bool ng = false;
-        if (live) {
-            to_limbs(tile[s][cg + v][0], sc, f, ng);
-        } else {
-#pragma unroll
-            for (int q = 0; q < kResLimbs; ++q) f[q] = 0.0f;
-        }
-#pragma unroll
-        for (int q = 0; q < kResLimbs; ++q) {
-            const float sv = ng ? -f[q] : f[q];
-            if (v & 1) fr[v >> 1][q].y = sv;
-            else fr[v >> 1][q].x = sv;
-        }
-        if (CPLX) {
-            bool ngi = false;
+        for (int v = 0; v < 4; ++v) {
+            float f[kResLimbs];
+            bool ng = false;
             if (live) {
-                to_limbs(tile[s][cg + v][E - 1], sc, f, ngi);
-                if (conj) ngi = !ngi;
+                to_limbs(tiles[buf][s][cg + v][0], sc, f, ng);
+            } else {
+#pragma unroll
+                for (int q = 0; q < kResLimbs; ++q) f[q] = 0.0f;
             }
 #pragma unroll
             for (int q = 0; q < kResLimbs; ++q) {
-                const float sv = ngi ? -f[q] : f[q];
-                if (v & 1) fi[CPLX ? v >> 1 : 0][q].y = sv;
-                else fi[CPLX ? v >> 1 : 0][q].x = sv;
+                const float sv = ng ? -f[q] : f[q];
+                if (v & 1) fr[v >> 1][q].y = sv;
+                else fr[v >> 1][q].x = sv;
+            }
+            if (CPLX) {
+                bool ngi = false;
+                if (live) {
+                    to_limbs(tiles[buf][s][cg + v][E - 1], sc, f, ngi);
+                    if (conj) ngi = !ngi;
+                }
+#pragma unroll
+                for (int q = 0; q < kResLimbs; ++q) {
+                    const float sv = ngi ? -f[q] : f[q];
+                    if (v & 1) fi[CPLX ? v >> 1 : 0][q].y = sv;
+                    else fi[CPLX ? v >> 1 : 0][q].x = sv;
+                }
             }
         }
-    }
-    const int64_t cstride = (int64_t)nmod * rows_pad * kpad;
-    __half *o = out + (r * kpad + cb);
-    for (int l = 0; l < nmod; ++l) {
-        float2 t[12];
+        __syncthreads();   // the buffer is refilled two iterations on; the limbs are in registers
+        const int64_t cstride = (int64_t)nmod * rows_pad * kpad;
+        __half *o = out + (r * kpad + cb);
+        for (int l = 0; l < nmod; ++l) {
+            float2 t[12];
 #pragma unroll
-        for (int q = 0; q < 12; q += 2) {
-            const float4 u = *reinterpret_cast<const float4 *>(&s_t[l][q]);
-            t[q] = make_float2(u.x, u.y);
-            t[q + 1] = make_float2(u.z, u.w);
+            for (int q = 0; q < 12; q += 2) {
+                const float4 u = *reinterpret_cast<const float4 *>(&s_t[l][q]);
+                t[q] = make_float2(u.x, u.y);
+                t[q + 1] = make_float2(u.z, u.w);
+            }
+            const float4 pp = s_pp[l];
+            const float2 negp = make_float2(pp.x, pp.y), invp = make_float2(pp.z, pp.w);
+            const float2 ra = sym_residue2(fr[0], t, negp, invp), rb = sym_residue2(fr[1], t, negp, invp);
+            store4h(o, ra, rb);
+            if (CPLX) {
+                const float2 ia = sym_residue2(fi[0], t, negp, invp), ib = sym_residue2(fi[CPLX ? 1 : 0], t, negp, invp);
+                store4h(o + cstride, ia, ib);
+                store4h(o + 2 * cstride, sym_wrap2(ra, ia, negp, invp), sym_wrap2(rb, ib, negp, invp));
+            }
+            o += rows_pad * kpad;
         }
-        const float4 pp = s_pp[l];
-        const float2 negp = make_float2(pp.x, pp.y), invp = make_float2(pp.z, pp.w);
-        const float2 ra = sym_residue2(fr[0], t, negp, invp), rb = sym_residue2(fr[1], t, negp, invp);
-        store4h(o, ra, rb);
-        if (CPLX) {
-            const float2 ia = sym_residue2(fi[0], t, negp, invp), ib = sym_residue2(fi[CPLX ? 1 : 0], t, negp, invp);
-            store4h(o + cstride, ia, ib);
-            store4h(o + 2 * cstride, sym_wrap2(ra, ia, negp, invp), sym_wrap2(rb, ib, negp, invp));
-        }
-        o += rows_pad * kpad;
     }
+}
+
+// One block per SM slot (as many as fit), each walking tiles with the next
+// tile's load in flight.
+template <bool ROWC, bool CPLX>
+void launch_residues(int64_t rows, int64_t kdim, const double2 *X, int64_t ld, const int *rexp, int bits,
+                     const OzResParams &rp, __half *out, int64_t rows_pad, int64_t kpad, int conj)
+{
+    static int per_sm[64];   // resident blocks per SM, per device (0 = not queried yet)
+    const size_t smem = residue_smem_bytes<CPLX>();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaFuncSetAttribute(k_oz_residues<ROWC, CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int &b = per_sm[dev & 63];
+    if (b <= 0) {
+        int q = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, k_oz_residues<ROWC, CPLX>, 256, smem);
+        b = q > 0 ? q : 1;
+    }
+    const int64_t ntiles = (kpad / 32) * (rows_pad / 32);
+    int64_t grid = (int64_t)b * device_sm_count();
+    if (grid > ntiles) grid = ntiles;
+    if (grid < 1) grid = 1;
+    k_oz_residues<ROWC, CPLX><<<(unsigned)grid, 256, smem, stream()>>>(rows, kdim, X, ld, rexp, bits, rp, out, rows_pad,
+                                                                        kpad, conj);
+    count_launch();
 }
 
 // ---- device: residue GEMM, tensor cores ---------------------------------------------------
@@ -529,12 +577,19 @@ __global__ void __launch_bounds__(192, 1)
 
 // Persistent form of k_oz_gemm_tc: one CTA per SM walks the (modulus, tile)
 // units u = blockIdx.x, blockIdx.x + gridDim.x, ... (tiles along N fastest,
-// then M, then the modulus, the order of the per-tile grid). Barriers, TMEM
-// and the tensor-map prefetch are set up once per CTA; the TMA producer runs
-// ahead into the next unit while the epilogue combines the previous one, and
-// every TMEM buffer is handed back and forth with one release per MMA chunk
-// written into it, so the phases continue across units.
-__global__ void __launch_bounds__(192, 1)
+// then M, then the modulus, the order of the per-tile grid), two units at a
+// time. Unit A of a pair accumulates in TMEM buffer 0 and unit B in buffer 1,
+// and the MMA warp interleaves their K chunks (A.c0, B.c0, A.c1, B.c1, ...):
+// while it fills one buffer, the epilogue reduces the other in place (chunk
+// c + 1 accumulates onto the reduced chunk c, 512 * 180^2 + 361 < 2^24, so
+// every fp32 sum stays exact) or, after a unit's last chunk, reduces it and
+// stores the residues. The final store of one unit therefore overlaps the
+// other unit's MMAs instead of stalling the tensor pipe. Eight epilogue warps,
+// two per TMEM lane quadrant, each take half of the 256 columns.
+constexpr int TCP_EPI_WARPS = 8;
+constexpr int TCP_THREADS = 64 + 32 * TCP_EPI_WARPS;
+
+__global__ void __launch_bounds__(TCP_THREADS, 1)
     k_oz_gemm_tc_p(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t Mp,
                    int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint16_t *__restrict__ R, int *status,
                    int uplo, int tiles_m, int tiles_n, int nz)
@@ -564,6 +619,12 @@ __global__ void __launch_bounds__(192, 1)
         const int64_t i0 = (int64_t)tm * TC_BM, j0 = (int64_t)tn * TC_BN;
         return !((uplo == 1 && i0 > j0 + TC_BN - 1) || (uplo == 2 && i0 + TC_BM - 1 < j0));
     };
+    // the next unit of this CTA at or after u that has work (units if none)
+    auto next_unit = [&](int64_t u) -> int64_t {
+        int tn, tm, l;
+        while (u < units && !unit_at(u, tn, tm, l)) u += gridDim.x;
+        return u < units ? u : units;
+    };
 
     if (warp == 0 && lane == 0) {
         for (int s = 0; s < TC_STAGES; ++s) {
@@ -572,7 +633,7 @@ __global__ void __launch_bounds__(192, 1)
         }
         for (int b = 0; b < 2; ++b) {
             sm100::mbar_init(&accf[b], 1);
-            sm100::mbar_init(&acce[b], 128);
+            sm100::mbar_init(&acce[b], 32 * TCP_EPI_WARPS);
         }
         sm100::mbar_init(drain, 1);
         sm100::fence_mbar_init();
@@ -592,20 +653,31 @@ __global__ void __launch_bounds__(192, 1)
             sm100::tma_prefetch_desc(&tmB);
             uint32_t gs = 0;   // k-steps issued by this CTA
             bool ok = true;
-            for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
-                int tn, tm, l;
-                if (!unit_at(u, tn, tm, l)) continue;
-                const int32_t ya = (int32_t)(l * Mp + (int64_t)tm * TC_BM);
-                const int32_t yb = (int32_t)(l * Np + (int64_t)tn * TC_BN);
-                for (int step = 0; step < nsteps; ++step) {
-                    const int s = gs % TC_STAGES;
-                    const uint32_t ph = gs / TC_STAGES;
-                    if (ph > 0 && !sm100::mbar_wait(&empty[s], (ph - 1) & 1, status, 1)) { ok = false; break; }
-                    sm100::mbar_arrive_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
-                    sm100::tma_load_2d(sA + s * TC_A_BYTES, &tmA, &full[s], step * TC_BK, ya);
-                    sm100::tma_load_2d(sB + s * TC_B_BYTES, &tmB, &full[s], step * TC_BK, yb);
-                    ++gs;
+            for (int64_t ua = next_unit(blockIdx.x); ua < units && ok;) {
+                const int64_t ub = next_unit(ua + gridDim.x);
+                const int nu = ub < units ? 2 : 1;
+                int32_t ya[2], yb[2];
+                for (int v = 0; v < nu; ++v) {
+                    int tn, tm, l;
+                    unit_at(v ? ub : ua, tn, tm, l);
+                    ya[v] = (int32_t)(l * Mp + (int64_t)tm * TC_BM);
+                    yb[v] = (int32_t)(l * Np + (int64_t)tn * TC_BN);
                 }
+                for (int c = 0; c < nch && ok; ++c) {
+                    const int s0 = c * kcs, s1 = min(nsteps, s0 + kcs);
+                    for (int v = 0; v < nu && ok; ++v) {
+                        for (int step = s0; step < s1; ++step) {
+                            const int s = gs % TC_STAGES;
+                            const uint32_t ph = gs / TC_STAGES;
+                            if (ph > 0 && !sm100::mbar_wait(&empty[s], (ph - 1) & 1, status, 1)) { ok = false; break; }
+                            sm100::mbar_arrive_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
+                            sm100::tma_load_2d(sA + s * TC_A_BYTES, &tmA, &full[s], step * TC_BK, ya[v]);
+                            sm100::tma_load_2d(sB + s * TC_B_BYTES, &tmB, &full[s], step * TC_BK, yb[v]);
+                            ++gs;
+                        }
+                    }
+                }
+                ua = nu == 2 ? next_unit(ub + gridDim.x) : units;
             }
             // never leave with copies in flight: wait (bounded) for the last use of every stage
             for (uint32_t t = (gs > TC_STAGES ? gs - TC_STAGES : 0); t < gs; ++t)
@@ -617,98 +689,103 @@ __global__ void __launch_bounds__(192, 1)
             uint32_t gs = 0;
             uint32_t uses[2] = {0, 0};   // chunks written into each buffer so far
             bool ok = true;
-            for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
-                int tn, tm, l;
-                if (!unit_at(u, tn, tm, l)) continue;
+            for (int64_t ua = next_unit(blockIdx.x); ua < units && ok;) {
+                const int64_t ub = next_unit(ua + gridDim.x);
+                const int nu = ub < units ? 2 : 1;
                 for (int c = 0; c < nch && ok; ++c) {
-                    const int b = c & 1;
-                    if (uses[b] > 0) {   // the previous chunk in this buffer has been released
-                        if (!sm100::mbar_wait(&acce[b], (uses[b] - 1) & 1, status, 2)) { ok = false; break; }
-                        sm100::tc_fence_after();
-                    }
                     const int s0 = c * kcs, s1 = min(nsteps, s0 + kcs);
-                    for (int step = s0; step < s1; ++step) {
-                        const int s = gs % TC_STAGES;
-                        if (!sm100::mbar_wait(&full[s], (gs / TC_STAGES) & 1, status, 3)) { ok = false; break; }
-                        sm100::tc_fence_after();
-                        const uint64_t ad = sm100::smem_desc_sw128(sm100::smem_u32(sA + s * TC_A_BYTES));
-                        const uint64_t bd = sm100::smem_desc_sw128(sm100::smem_u32(sB + s * TC_B_BYTES));
-#pragma unroll
-                        for (int kk = 0; kk < TC_BK / 16; ++kk) {
-                            const uint32_t acc = (c >= 2 || step > s0 || kk > 0) ? 1u : 0u;
-                            sm100::mma_f16(tmem + b * TC_BN, ad + 2 * kk, bd + 2 * kk, idesc, acc);
+                    for (int b = 0; b < nu && ok; ++b) {
+                        if (uses[b] > 0) {   // the previous chunk in this buffer has been released
+                            if (!sm100::mbar_wait(&acce[b], (uses[b] - 1) & 1, status, 2)) { ok = false; break; }
+                            sm100::tc_fence_after();
                         }
-                        sm100::mma_commit(&empty[s]);
-                        ++gs;
+                        for (int step = s0; step < s1; ++step) {
+                            const int s = gs % TC_STAGES;
+                            if (!sm100::mbar_wait(&full[s], (gs / TC_STAGES) & 1, status, 3)) { ok = false; break; }
+                            sm100::tc_fence_after();
+                            const uint64_t ad = sm100::smem_desc_sw128(sm100::smem_u32(sA + s * TC_A_BYTES));
+                            const uint64_t bd = sm100::smem_desc_sw128(sm100::smem_u32(sB + s * TC_B_BYTES));
+#pragma unroll
+                            for (int kk = 0; kk < TC_BK / 16; ++kk) {
+                                const uint32_t acc = (c > 0 || step > s0 || kk > 0) ? 1u : 0u;
+                                sm100::mma_f16(tmem + b * TC_BN, ad + 2 * kk, bd + 2 * kk, idesc, acc);
+                            }
+                            sm100::mma_commit(&empty[s]);
+                            ++gs;
+                        }
+                        if (!ok) break;
+                        sm100::mma_commit(&accf[b]);
+                        ++uses[b];
                     }
-                    if (!ok) break;
-                    sm100::mma_commit(&accf[b]);
-                    ++uses[b];
                 }
+                ua = nu == 2 ? next_unit(ub + gridDim.x) : units;
             }
             // no MMA may still be writing TMEM when it is freed
             sm100::mma_commit(drain);
             sm100::mbar_wait(drain, 0, nullptr, 0);
         }
     } else {
-        // ---- epilogue: 128 threads, one TMEM lane (tile row) each
+        // ---- epilogue: warps 2..9, TMEM lane quadrant warp % 4, column half (warp - 2) / 4
         const int q = warp & 3;
+        const int half = (warp - 2) >> 2;
         const int row = q * 32 + lane;
-        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + half * (TC_BN / 2);
         uint32_t fcnt[2] = {0, 0};   // chunk completions consumed per buffer
         bool ok = true;
-        for (int64_t u = blockIdx.x; u < units && ok; u += gridDim.x) {
-            int tn, tm, l;
-            if (!unit_at(u, tn, tm, l)) continue;
-            const float p = P.p[l], invp = P.invp[l];
-            for (int c = 0; c < nch; ++c) {
-                const int b = c & 1;
-                // warp-uniform outcome before the .sync.aligned TMEM accesses
-                if (!__all_sync(0xffffffffu, sm100::mbar_wait(&accf[b], fcnt[b] & 1, status, 4))) { ok = false; break; }
-                ++fcnt[b];
-                sm100::tc_fence_after();
-                if (c >= nch - 2) continue;   // reduced in the combine
+        for (int64_t ua = next_unit(blockIdx.x); ua < units && ok;) {
+            const int64_t ub = next_unit(ua + gridDim.x);
+            const int nu = ub < units ? 2 : 1;
+            for (int c = 0; c < nch && ok; ++c) {
+                for (int b = 0; b < nu; ++b) {
+                    int tn, tm, l;
+                    unit_at(b ? ub : ua, tn, tm, l);
+                    const float p = P.p[l], invp = P.invp[l];
+                    // warp-uniform outcome before the .sync.aligned TMEM accesses
+                    if (!__all_sync(0xffffffffu, sm100::mbar_wait(&accf[b], fcnt[b] & 1, status, 4))) {
+                        ok = false;
+                        break;
+                    }
+                    ++fcnt[b];
+                    sm100::tc_fence_after();
+                    const uint32_t tb = lane_base + b * TC_BN;
+                    if (c < nch - 1) {
+                        // reduce in place; the next chunk accumulates onto it
 #pragma unroll 1
-                for (int sl = 0; sl < TC_BN / 32; ++sl) {
-                    uint32_t r[32];
-                    const uint32_t ta = lane_base + b * TC_BN + sl * 32;
-                    sm100::tmem_ld32(ta, r);
-                    sm100::tmem_wait_ld();
+                        for (int sl = 0; sl < TC_BN / 64; ++sl) {
+                            uint32_t r[32];
+                            sm100::tmem_ld32(tb + sl * 32, r);
+                            sm100::tmem_wait_ld();
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) r[i] = __float_as_uint(mod_sym(__uint_as_float(r[i]), p, invp));
-                    sm100::tmem_st32(ta, r);
-                }
-                sm100::tmem_wait_st();
-                sm100::tc_fence_before();   // chunk c + 2 of this unit accumulates onto it
-                sm100::mbar_arrive(&acce[b]);
-            }
-            if (!ok) break;
-            // both buffers hold their last chunk's sums: c = (P + Q) mod p in [0, p) as R[l][j][i]
-            const int64_t i = (int64_t)tm * TC_BM + row;
-            const int64_t j0 = (int64_t)tn * TC_BN;
-            const bool row_ok = i < M;
-            const int jn = (int)min((int64_t)TC_BN, N - j0);
-            uint16_t *q = R + ((int64_t)l * Np + j0) * Mp + i;   // advanced by Mp per column
+                            for (int t = 0; t < 32; ++t) r[t] = __float_as_uint(mod_sym(__uint_as_float(r[t]), p, invp));
+                            sm100::tmem_st32(tb + sl * 32, r);
+                        }
+                        sm100::tmem_wait_st();
+                    } else {
+                        // last chunk: c = sum mod p in [0, p) as R[l][j][i]
+                        const int64_t i = (int64_t)tm * TC_BM + row;
+                        const int64_t j0 = (int64_t)tn * TC_BN + half * (TC_BN / 2);
+                        const bool row_ok = i < M;
+                        const int jn = (int)max((int64_t)0, min((int64_t)(TC_BN / 2), N - j0));
+                        uint16_t *o = R + ((int64_t)l * Np + j0) * Mp + i;   // advanced by Mp per column
 #pragma unroll 1
-            for (int sl = 0; sl < TC_BN / 32; ++sl) {
-                uint32_t r0[32], r1[32];
-                sm100::tmem_ld32(lane_base + sl * 32, r0);
-                if (nch > 1) sm100::tmem_ld32(lane_base + TC_BN + sl * 32, r1);
-                sm100::tmem_wait_ld();
+                        for (int sl = 0; sl < TC_BN / 64; ++sl) {
+                            uint32_t r[32];
+                            sm100::tmem_ld32(tb + sl * 32, r);
+                            sm100::tmem_wait_ld();
 #pragma unroll
-                for (int t = 0; t < 32; ++t) {
-                    float v = mod_sym(__uint_as_float(r0[t]), p, invp);
-                    if (nch > 1) v = __fadd_rn(v, mod_sym(__uint_as_float(r1[t]), p, invp));
-                    float fq = rint_small(__fmul_rn(v, invp));
-                    float rr = __fmaf_rn(-fq, p, v);   // in (-p, p)
-                    if (rr < 0.0f) rr = __fadd_rn(rr, p);
-                    if (row_ok && sl * 32 + t < jn) *q = (uint16_t)small_uint(rr);
-                    q += Mp;
+                            for (int t = 0; t < 32; ++t) {
+                                float rr = mod_sym(__uint_as_float(r[t]), p, invp);   // in [-p/2, p/2]
+                                if (rr < 0.0f) rr = __fadd_rn(rr, p);
+                                if (row_ok && sl * 32 + t < jn) *o = (uint16_t)small_uint(rr);
+                                o += Mp;
+                            }
+                        }
+                    }
+                    sm100::tc_fence_before();
+                    sm100::mbar_arrive(&acce[b]);
                 }
             }
-            // release the buffers of the last two chunks to the next unit
-            sm100::tc_fence_before();
-            for (int c = (nch > 2 ? nch - 2 : 0); c < nch; ++c) sm100::mbar_arrive(&acce[c & 1]);
+            ua = nu == 2 ? next_unit(ub + gridDim.x) : units;
         }
     }
 
@@ -774,18 +851,6 @@ __device__ __forceinline__ void crt_smem_fill(CrtSmem &sm, const OzCrtParams &K)
     for (int i = threadIdx.x; i < K.nmod; i += blockDim.x) sm.pm[i] = K.pm[i];
 }
 
-__device__ __forceinline__ XF crt_m(const OzCrtParams &K)
-{
-    XF m;
-    m.m = ((unsigned __int128)K.Mhi << 64) | K.Mlo;
-    m.e = K.Me;
-    m.neg = false;
-    m.zero = false;
-    return m;
-}
-
-__device__ __forceinline__ xw::XW crt_mw(const OzCrtParams &K) { return crt::to_xw(crt_m(K)); }
-
 __device__ __forceinline__ dd::real xw_dd(const xw::XW &x)
 {
     dd::real r;
@@ -798,76 +863,92 @@ __device__ __forceinline__ bool finite_hi(double x)
     return ((__double2hiint(x) >> 20) & 0x7FF) != 0x7FF;   // exponent field test, no FP64 compare
 }
 
-// C(i, j) := alpha * X(i, j) * 2^-S2 + beta * C(i, j), real. Thread per row i,
-// columns j = blockIdx.y, blockIdx.y + gridDim.y, ...; m and n below 2^31
+// C(i, j) := alpha * X(i, j) * 2^-S2 + beta * C(i, j), real. Thread per pair
+// of rows, columns j = blockIdx.y, blockIdx.y + gridDim.y, ...; m and n below 2^31
 // (the host routes larger sizes elsewhere), so the per-element index work is
 // 32-bit or pointer increments.
 __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint16_t *__restrict__ R,
                                                         int64_t Mp, int64_t Np, const int *__restrict__ ea,
                                                         const int *__restrict__ eb, int bits, OzCrtParams K,
-                                                        dd::real alpha, int alpha_one, dd::real beta, int beta_kind,
+                                                        xw::XW Mx, xw::XW xb, dd::real beta, int beta_kind,
                                                         double2 *C, int64_t ldc, int uplo)
 {
+    // Mx = alpha * M and xb = beta as extended floats (formed on the host).
+    // A thread takes rows i0, i0 + 1 (one 32-bit load per modulus serves both).
     __shared__ CrtSmem sm;
     crt_smem_fill(sm, K);
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m) return;
+    const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (i0 >= m) return;
     const int nmod = K.nmod;
-    // alpha folded into M: alpha * X = T * (alpha M)
-    xw::XW Mx = crt_mw(K);
-    if (!alpha_one) Mx = xw::mul(xw::from_dd(alpha.hi, alpha.lo), Mx);
-    const xw::XW xb = xw::from_dd(beta.hi, beta.lo);
-    const int eai = ea[i];
+    const bool two = i0 + 1 < m;
+    const int ea0 = ea[i0], ea1 = two ? ea[i0 + 1] : kNoExp;
     const int64_t plane = Np * Mp;
     const int jstep = gridDim.y;
-    const uint16_t *rcol = R + (int64_t)blockIdx.y * Mp + i;
-    double2 *pc = C + i + (int64_t)blockIdx.y * ldc;
+    const uint16_t *rcol = R + (int64_t)blockIdx.y * Mp + i0;
+    double2 *pc = C + i0 + (int64_t)blockIdx.y * ldc;
     const int64_t rstep = (int64_t)jstep * Mp, cstep = (int64_t)jstep * ldc;
     for (int j = blockIdx.y; j < n; j += jstep, rcol += rstep, pc += cstep) {
-        if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
         const int ebj = eb[j];
-        if (eai >= 1024 || ebj >= 1024) {   // a non-finite entry in row i of op(A) or column j of op(B)
-            const double qnan = __longlong_as_double(0x7ff8000000000000ll);
-            *pc = make_double2(qnan, qnan);
-            continue;
-        }
-        xw::XW v;
-        v = xw::zero();
-        if (eai > kNoExp / 2 && ebj > kNoExp / 2) {
-            crt::Frac acc;
-            acc.reset();
-            // residues of all moduli: issue the loads of 8 planes at a time
-            // so that their latencies overlap
-            const uint16_t *q = rcol;
+        crt::Frac acc0, acc1;
+        acc0.reset();
+        acc1.reset();
+        const bool live0 = ea0 > kNoExp / 2 && ea0 < 1024 && ebj > kNoExp / 2 && ebj < 1024;
+        const bool live1 = two && ea1 > kNoExp / 2 && ea1 < 1024 && ebj > kNoExp / 2 && ebj < 1024;
+        if (live0 || live1) {
+            // residues of all moduli for both rows: the loads of 8 planes are
+            // issued together so that their latencies overlap
+            const uint32_t *q = reinterpret_cast<const uint32_t *>(rcol);
+            const int64_t qstep = plane / 2;
             int l = 0;
             for (; l + 8 <= nmod; l += 8) {
                 uint32_t c[8];
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
                     c[u] = __ldcs(q);
-                    q += plane;
+                    q += qstep;
                 }
 #pragma unroll
-                for (int u = 0; u < 8; ++u) acc.add(sm.F[l + u], c[u]);
+                for (int u = 0; u < 8; ++u) {
+                    acc0.add(sm.F[l + u], c[u] & 0xFFFFu);
+                    acc1.add(sm.F[l + u], c[u] >> 16);
+                }
             }
-            for (; l < nmod; ++l, q += plane) acc.add(sm.F[l], __ldcs(q));
-            v = acc.finish_xw(Mx, (bits - 2 - eai) + (bits - 2 - ebj));
+            for (; l < nmod; ++l, q += qstep) {
+                const uint32_t c = __ldcs(q);
+                acc0.add(sm.F[l], c & 0xFFFFu);
+                acc1.add(sm.F[l], c >> 16);
+            }
         }
-        if (beta_kind != 0) {
-            double2 c0 = *pc;
-            if (!finite_hi(c0.x)) {
-                // non-finite C: the double-double operators propagate it
-                dd::real cv = dd::make(c0.x, c0.y);
-                if (beta_kind == 2) cv = dd::mul_exact(cv, beta);
-                dd::store(pc, dd::add_exact(cv, xw_dd(v)));
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = i0 + h;
+            if (h == 1 && !two) break;
+            if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
+            const int eai = h ? ea1 : ea0;
+            double2 *pe = pc + h;
+            if (eai >= 1024 || ebj >= 1024) {   // a non-finite entry in row i of op(A) or column j of op(B)
+                const double qnan = __longlong_as_double(0x7ff8000000000000ll);
+                *pe = make_double2(qnan, qnan);
                 continue;
             }
-            xw::XW xc = xw::from_dd(c0.x, c0.y);
-            if (beta_kind == 2) xc = xw::mul(xb, xc);
-            v = xw::add(v, xc);
+            xw::XW v = xw::zero();
+            if (h ? live1 : live0) v = (h ? acc1 : acc0).finish_xw(Mx, (bits - 2 - eai) + (bits - 2 - ebj));
+            if (beta_kind != 0) {
+                const double2 c0 = *pe;
+                if (!finite_hi(c0.x)) {
+                    // non-finite C: the double-double operators propagate it
+                    dd::real cv = dd::make(c0.x, c0.y);
+                    if (beta_kind == 2) cv = dd::mul_exact(cv, beta);
+                    dd::store(pe, dd::add_exact(cv, xw_dd(v)));
+                    continue;
+                }
+                xw::XW xc = xw::from_dd(c0.x, c0.y);
+                if (beta_kind == 2) xc = xw::mul(xb, xc);
+                v = xw::add(v, xc);
+            }
+            dd::store(pe, xw_dd(v));
         }
-        dd::store(pc, xw_dd(v));
     }
 }
 
@@ -876,10 +957,11 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
 __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const uint16_t *__restrict__ R,
                                                           int64_t Mp, int64_t Np, const int *__restrict__ ea,
                                                           const int *__restrict__ eb, int bits, OzCrtParams K,
-                                                          dd::cplx alpha, int alpha_one, dd::cplx beta,
-                                                          int beta_kind, double2 *C, int64_t ldc, int uplo, int herm,
-                                                          int real_beta)
+                                                          xw::XW Mx, xw::XW ar, xw::XW ai, int alpha_one,
+                                                          dd::cplx beta, xw::XW br, xw::XW bi, int beta_kind,
+                                                          double2 *C, int64_t ldc, int uplo, int herm, int real_beta)
 {
+    // Mx = M, (ar, ai) = alpha and (br, bi) = beta as extended floats (formed on the host)
     __shared__ CrtSmem sm;
     crt_smem_fill(sm, K);
     __syncthreads();
@@ -887,9 +969,6 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
     if (i >= m) return;
     const int nmod = K.nmod;
     const int64_t cstride = (int64_t)nmod * Np * Mp;
-    const xw::XW Mx = crt_mw(K);
-    const xw::XW ar = xw::from_dd(alpha.re.hi, alpha.re.lo), ai = xw::from_dd(alpha.im.hi, alpha.im.lo);
-    const xw::XW br = xw::from_dd(beta.re.hi, beta.re.lo), bi = xw::from_dd(beta.im.hi, beta.im.lo);
     for (int j = blockIdx.y; j < n; j += gridDim.y) {
         if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
         if (ea[i] >= 1024 || eb[j] >= 1024) {
@@ -1160,26 +1239,22 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     {
         // op(A) = A: A[i + p*lda] is contiguous along rows; op(A) = A^T along k.
         // op(B)(p, j) = B[p + j*ldb] is contiguous along k; op(B) = B^T along rows j.
-        dim3 grid((unsigned)(Kp / 32), (unsigned)(Mp / 32));
         const double2 *Ad = (const double2 *)g.A, *Bd = (const double2 *)g.B;
         if (cplx) {
-            if (!g.ta) k_oz_residues<true, true><<<grid, 256, 0, stream()>>>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
-            else k_oz_residues<false, true><<<grid, 256, 0, stream()>>>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
+            if (!g.ta) launch_residues<true, true>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
+            else launch_residues<false, true>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
         } else {
-            if (!g.ta) k_oz_residues<true, false><<<grid, 256, 0, stream()>>>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
-            else k_oz_residues<false, false><<<grid, 256, 0, stream()>>>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
+            if (!g.ta) launch_residues<true, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
+            else launch_residues<false, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
         }
-        count_launch();
         if (!shared_ops) {
-            dim3 gridb((unsigned)(Kp / 32), (unsigned)(Np / 32));
             if (cplx) {
-                if (!g.tb) k_oz_residues<false, true><<<gridb, 256, 0, stream()>>>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, g.cb);
-                else k_oz_residues<true, true><<<gridb, 256, 0, stream()>>>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, g.cb);
+                if (!g.tb) launch_residues<false, true>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, g.cb);
+                else launch_residues<true, true>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, g.cb);
             } else {
-                if (!g.tb) k_oz_residues<false, false><<<gridb, 256, 0, stream()>>>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, 0);
-                else k_oz_residues<true, false><<<gridb, 256, 0, stream()>>>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, 0);
+                if (!g.tb) launch_residues<false, false>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, 0);
+                else launch_residues<true, false>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, 0);
             }
-            count_launch();
         }
     }
 
@@ -1198,8 +1273,9 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
                 const int64_t units = (int64_t)nz * tiles_m * tiles_n;
                 const int64_t sms = device_sm_count();
                 const unsigned grid = (unsigned)(units < sms ? units : sms);
-                k_oz_gemm_tc_p<<<grid, 192, TC_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R, device_status_word(),
-                                                                 g.uplo, tiles_m, tiles_n, nz);
+                k_oz_gemm_tc_p<<<grid, TCP_THREADS, TC_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R,
+                                                                         device_status_word(), g.uplo, tiles_m,
+                                                                         tiles_n, nz);
             } else {
                 cudaFuncSetAttribute(k_oz_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
                 dim3 grid((unsigned)(Np / TC_BN), (unsigned)(Mp / TC_BM), (unsigned)nz);
@@ -1217,11 +1293,23 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     // 5. reconstruction + alpha/beta
     phase_mark(PH_REC);
     if (ok) {
-        dim3 grid((unsigned)((m + 255) / 256), blocks_cap(n));
+        // a thread per row and several columns: about 16 blocks per SM in all
+        const unsigned gx = (unsigned)((m + (cplx ? 255 : 511)) / (cplx ? 256 : 512));
+        const int64_t want_y = ((int64_t)device_sm_count() * 16 + gx - 1) / gx;
+        dim3 grid(gx, blocks_cap(want_y < n ? want_y : n));
+        xw::XW Mx;
+        Mx.w[3] = (uint32_t)(cp.Mhi >> 32);
+        Mx.w[2] = (uint32_t)cp.Mhi;
+        Mx.w[1] = (uint32_t)(cp.Mlo >> 32);
+        Mx.w[0] = (uint32_t)cp.Mlo;
+        Mx.e = cp.Me;
+        Mx.neg = 0u;
         if (!cplx) {
             bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
-            k_oz_reconstruct<<<grid, 256, 0, stream()>>>((int)m, (int)n, R, Mp, Np, ea, eb, bits, cp,
-                                                        dd::make(g.alpha.hi, g.alpha.lo), alpha_one ? 1 : 0,
+            // alpha folded into M: alpha * X = T * (alpha M)
+            const xw::XW aM = alpha_one ? Mx : xw::mul(xw::from_dd(g.alpha.hi, g.alpha.lo), Mx);
+            k_oz_reconstruct<<<grid, 256, 0, stream()>>>((int)m, (int)n, R, Mp, Np, ea, eb, bits, cp, aM,
+                                                        xw::from_dd(g.beta.hi, g.beta.lo),
                                                         dd::make(g.beta.hi, g.beta.lo), g.beta_kind, (double2 *)g.C,
                                                         g.ldc, g.uplo);
         } else {
@@ -1232,10 +1320,11 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
             be.im = dd::make(g.cbeta.im.hi, g.cbeta.im.lo);
             bool alpha_one = (g.calpha.re.hi == 1.0 && g.calpha.re.lo == 0.0 && g.calpha.im.hi == 0.0 &&
                               g.calpha.im.lo == 0.0);
-            k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>((int)m, (int)n, R, Mp, Np, ea, eb, bits, cp, al,
-                                                          alpha_one ? 1 : 0,
-                                                          be, g.beta_kind, (double2 *)g.C, g.ldc, g.uplo,
-                                                          g.herm ? 1 : 0, g.herm ? 1 : 0);
+            k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>(
+                (int)m, (int)n, R, Mp, Np, ea, eb, bits, cp, Mx, xw::from_dd(al.re.hi, al.re.lo),
+                xw::from_dd(al.im.hi, al.im.lo), alpha_one ? 1 : 0, be, xw::from_dd(be.re.hi, be.re.lo),
+                xw::from_dd(be.im.hi, be.im.lo), g.beta_kind, (double2 *)g.C, g.ldc, g.uplo, g.herm ? 1 : 0,
+                g.herm ? 1 : 0);
         }
         count_launch();
     }
@@ -1271,6 +1360,6 @@ extern "C" float mwblas_last_phase_ms(int phase)
 extern "C" int mwblas_set_ozaki_mma(int kind)
 {
     int prev = mw::mma_kind();
-    mw::g_mma_kind = (kind >= 0 && kind <= 2) ? kind : 0;
+    mw::g_mma_kind = (kind >= 0 && kind <= 2) ? kind : 2;
     return prev;
 }

@@ -228,13 +228,74 @@ XW_HD XW from_dd(double hi, double lo)
     return r;
 }
 
-// Top 128 bits of the product of two normalised mantissas (partial products
-// below 2^96 of the 256-bit product are dropped: relative error < 2^-122).
+// Top 128 bits of the product of two normalised mantissas (the partial
+// products of columns 0..2 of the 256-bit product are dropped: relative error
+// < 2^-122). The host and device forms sum the same partial products.
 XW_HD XW mul(const XW &a, const XW &b)
 {
     if (a.w[3] == 0u || b.w[3] == 0u) return zero();
     const uint32_t a0 = a.w[0], a1 = a.w[1], a2 = a.w[2], a3 = a.w[3];
     const uint32_t b0 = b.w[0], b1 = b.w[1], b2 = b.w[2], b3 = b.w[3];
+#ifdef __CUDA_ARCH__
+    // Row by row (b3, b2, b1, b0) with 32-bit multiply-add carry chains into
+    // the columns 3..7 of the 256-bit product.
+    uint32_t c3, c4, c5, c6, c7;
+    asm("mul.lo.u32 %0, %5, %9;\n\t"
+        "mul.lo.u32 %1, %6, %9;\n\t"
+        "mul.lo.u32 %2, %7, %9;\n\t"
+        "mul.lo.u32 %3, %8, %9;\n\t"
+        "mad.hi.cc.u32 %1, %5, %9, %1;\n\t"
+        "madc.hi.cc.u32 %2, %6, %9, %2;\n\t"
+        "madc.hi.cc.u32 %3, %7, %9, %3;\n\t"
+        "madc.hi.u32 %4, %8, %9, 0;\n\t"
+        // b2: a1, a2, a3 at columns 3, 4, 5
+        "mad.lo.cc.u32 %0, %6, %10, %0;\n\t"
+        "madc.lo.cc.u32 %1, %7, %10, %1;\n\t"
+        "madc.lo.cc.u32 %2, %8, %10, %2;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.hi.cc.u32 %1, %6, %10, %1;\n\t"
+        "madc.hi.cc.u32 %2, %7, %10, %2;\n\t"
+        "madc.hi.cc.u32 %3, %8, %10, %3;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        // b1: a2, a3 at columns 3, 4
+        "mad.lo.cc.u32 %0, %7, %11, %0;\n\t"
+        "madc.lo.cc.u32 %1, %8, %11, %1;\n\t"
+        "addc.cc.u32 %2, %2, 0;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.hi.cc.u32 %1, %7, %11, %1;\n\t"
+        "madc.hi.cc.u32 %2, %8, %11, %2;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        // b0: a3 at column 3
+        "mad.lo.cc.u32 %0, %8, %12, %0;\n\t"
+        "addc.cc.u32 %1, %1, 0;\n\t"
+        "addc.cc.u32 %2, %2, 0;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.hi.cc.u32 %1, %8, %12, %1;\n\t"
+        "addc.cc.u32 %2, %2, 0;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;"
+        : "=&r"(c3), "=&r"(c4), "=&r"(c5), "=&r"(c6), "=&r"(c7)
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b3), "r"(b2), "r"(b1), "r"(b0));
+    XW r;
+    r.neg = a.neg ^ b.neg;
+    r.e = a.e + b.e + 128;
+    r.w[3] = c7;
+    r.w[2] = c6;
+    r.w[1] = c5;
+    r.w[0] = c4;
+    if (!(c7 >> 31)) {   // product below 2^255: one more bit from column 3
+        r.w[3] = fshl(c6, c7, 1);
+        r.w[2] = fshl(c5, c6, 1);
+        r.w[1] = fshl(c4, c5, 1);
+        r.w[0] = fshl(c3, c4, 1);
+        r.e -= 1;
+    }
+    return r;
+#else
     const uint64_t p03 = (uint64_t)a0 * b3, p12 = (uint64_t)a1 * b2, p21 = (uint64_t)a2 * b1, p30 = (uint64_t)a3 * b0;
     const uint64_t p13 = (uint64_t)a1 * b3, p22 = (uint64_t)a2 * b2, p31 = (uint64_t)a3 * b1;
     const uint64_t p23 = (uint64_t)a2 * b3, p32 = (uint64_t)a3 * b2;
@@ -260,6 +321,7 @@ XW_HD XW mul(const XW &a, const XW &b)
         r.e -= 1;
     }
     return r;
+#endif
 }
 
 // a + b, truncating the smaller operand's bits below 2^-128 of the larger.

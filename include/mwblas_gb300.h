@@ -236,11 +236,13 @@ int mwblas_set_ozaki_bits(int bits);
 /* Moduli count used by the most recent Ozaki GEMM on this thread. */
 int mwblas_last_ozaki_moduli(void);
 /* Residue-GEMM unit of the Ozaki engine: 0 = tcgen05 tensor cores, one CTA
- * per (modulus, tile) (default), 1 = CUDA cores (an independent exact path
- * used to cross-check the tensor cores), 2 = tcgen05 in a persistent kernel
- * (one CTA per SM walking the (modulus, tile) units). The MWBLAS_OZAKI_MMA
- * environment variable ("simt", "persistent") selects them too. All produce
- * bit-identical results. Returns the previous value. */
+ * per (modulus, tile), 1 = CUDA cores (an independent exact path used to
+ * cross-check the tensor cores), 2 = tcgen05 in a persistent kernel (one CTA
+ * per SM walking the (modulus, tile) units two at a time, so that one unit's
+ * final reduction overlaps the other's MMAs; the default). The
+ * MWBLAS_OZAKI_MMA environment variable ("pertile", "simt", "persistent")
+ * selects them too. All produce bit-identical results. Returns the previous
+ * value. */
 int mwblas_set_ozaki_mma(int kind);
 
 /* Per-phase device timing of the Ozaki engine (CUDA events on the library

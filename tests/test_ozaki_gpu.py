@@ -63,11 +63,13 @@ def test_tensor_core_and_cuda_core_paths_bit_identical(gpu, rng):
     np.testing.assert_array_equal(outs[0], outs[2])
 
 
-@pytest.mark.parametrize("k", [300, 512, 1024, 1500])
+@pytest.mark.parametrize("k", [300, 512, 1024, 1500, 2600])
 @pytest.mark.parametrize("uplo", [0, 1])
 def test_persistent_tensor_core_kernel(gpu, rng, k, uplo):
-    """The persistent residue-GEMM kernel gives the per-tile kernel's bits for
-    one, two and more K chunks (512 each), full and triangular outputs."""
+    """The persistent residue-GEMM kernel (units taken two at a time, their K
+    chunks interleaved) gives the per-tile kernel's bits for one, two and more
+    K chunks (512 each), full and triangular outputs, and CTAs left with an
+    odd unit at the end."""
     n = 700
     A = mwb.dd_matrix(rng, n, k)
     outs = []
@@ -187,7 +189,7 @@ def test_ozaki_complex_tc_equals_cuda_core(gpu, rng):
     A = mwb.dd_matrix(rng, m, k, cplx_=True)
     B = mwb.dd_matrix(rng, k, n, cplx_=True)
     outs = []
-    for kind in (0, 1):
+    for kind in (0, 1, 2):
         prev = gpu.lib.mwblas_set_ozaki_mma(kind)
         try:
             c = np.zeros((n, m, 2, 2))
@@ -197,6 +199,7 @@ def test_ozaki_complex_tc_equals_cuda_core(gpu, rng):
         finally:
             gpu.lib.mwblas_set_ozaki_mma(prev)
     np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
 
 
 @pytest.mark.parametrize("uplo", ["U", "L"])
