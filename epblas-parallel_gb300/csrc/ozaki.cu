@@ -748,39 +748,52 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
                     ++fcnt[b];
                     sm100::tc_fence_after();
                     const uint32_t tb = lane_base + b * TC_BN;
-                    if (c < nch - 1) {
-                        // reduce in place; the next chunk accumulates onto it
+                    // this warp's 128 columns, 64 at a time (two loads in flight per wait)
+                    const float2 negp2 = make_float2(-p, -p), invp2 = make_float2(invp, invp);
+                    const int64_t i = (int64_t)tm * TC_BM + row;
+                    const int64_t j0 = (int64_t)tn * TC_BN + half * (TC_BN / 2);
+                    const bool row_ok = i < M;
+                    const int jn = (int)max((int64_t)0, min((int64_t)(TC_BN / 2), N - j0));
+                    uint16_t *o = R + ((int64_t)l * Np + j0) * Mp + i;   // advanced by Mp per column
 #pragma unroll 1
-                        for (int sl = 0; sl < TC_BN / 64; ++sl) {
-                            uint32_t r[32];
-                            sm100::tmem_ld32(tb + sl * 32, r);
-                            sm100::tmem_wait_ld();
+                    for (int hh = 0; hh < 2; ++hh) {
+                        uint32_t r[2][32];
+                        sm100::tmem_ld32(tb + hh * 64, r[0]);
+                        sm100::tmem_ld32(tb + hh * 64 + 32, r[1]);
+                        sm100::tmem_wait_ld();
+                        // x - p * rint(x / p), two columns per packed instruction (in (-p, p), exact)
 #pragma unroll
-                            for (int t = 0; t < 32; ++t) r[t] = __float_as_uint(mod_sym(__uint_as_float(r[t]), p, invp));
-                            sm100::tmem_st32(tb + sl * 32, r);
+                        for (int sl = 0; sl < 2; ++sl) {
+#pragma unroll
+                            for (int t = 0; t < 32; t += 2) {
+                                float2 x = make_float2(__uint_as_float(r[sl][t]), __uint_as_float(r[sl][t + 1]));
+                                float2 y = __fmul2_rn(x, invp2);
+                                y = __fadd2_rn(y, make_float2(12582912.0f, 12582912.0f));
+                                y = __fadd2_rn(y, make_float2(-12582912.0f, -12582912.0f));
+                                x = __ffma2_rn(y, negp2, x);
+                                r[sl][t] = __float_as_uint(x.x);
+                                r[sl][t + 1] = __float_as_uint(x.y);
+                            }
                         }
-                        sm100::tmem_wait_st();
-                    } else {
-                        // last chunk: c = sum mod p in [0, p) as R[l][j][i]
-                        const int64_t i = (int64_t)tm * TC_BM + row;
-                        const int64_t j0 = (int64_t)tn * TC_BN + half * (TC_BN / 2);
-                        const bool row_ok = i < M;
-                        const int jn = (int)max((int64_t)0, min((int64_t)(TC_BN / 2), N - j0));
-                        uint16_t *o = R + ((int64_t)l * Np + j0) * Mp + i;   // advanced by Mp per column
-#pragma unroll 1
-                        for (int sl = 0; sl < TC_BN / 64; ++sl) {
-                            uint32_t r[32];
-                            sm100::tmem_ld32(tb + sl * 32, r);
-                            sm100::tmem_wait_ld();
+                        if (c < nch - 1) {
+                            // reduce in place; the next chunk accumulates onto it
+                            sm100::tmem_st32(tb + hh * 64, r[0]);
+                            sm100::tmem_st32(tb + hh * 64 + 32, r[1]);
+                        } else {
+                            // last chunk: c = sum mod p in [0, p) as R[l][j][i]
 #pragma unroll
-                            for (int t = 0; t < 32; ++t) {
-                                float rr = mod_sym(__uint_as_float(r[t]), p, invp);   // in [-p/2, p/2]
-                                if (rr < 0.0f) rr = __fadd_rn(rr, p);
-                                if (row_ok && sl * 32 + t < jn) *o = (uint16_t)small_uint(rr);
-                                o += Mp;
+                            for (int sl = 0; sl < 2; ++sl) {
+#pragma unroll
+                                for (int t = 0; t < 32; ++t) {
+                                    float rr = __uint_as_float(r[sl][t]);
+                                    if (rr < 0.0f) rr = __fadd_rn(rr, p);
+                                    if (row_ok && hh * 64 + sl * 32 + t < jn) *o = (uint16_t)small_uint(rr);
+                                    o += Mp;
+                                }
                             }
                         }
                     }
+                    if (c < nch - 1) sm100::tmem_wait_st();
                     sm100::tc_fence_before();
                     sm100::mbar_arrive(&acce[b]);
                 }
