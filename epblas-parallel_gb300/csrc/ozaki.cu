@@ -105,7 +105,7 @@ Moduli choose_moduli(double need_bits)
 }
 
 int g_last_moduli = 0;
-int g_mma_kind = -1;   // 0 tcgen05 per tile, 1 SIMT cross-check, 2 tcgen05 persistent (default)
+int g_mma_kind = -1;   // 0 tcgen05 per tile, 1 SIMT cross-check, 2 tcgen05 persistent, 3 CTA pairs (default)
 
 // Optional per-phase timing with CUDA events on the library stream.
 enum { PH_EXP = 0, PH_RES, PH_GEMM, PH_REC, PH_N };
@@ -135,7 +135,10 @@ int mma_kind()
 {
     if (g_mma_kind < 0) {
         const char *e = getenv("MWBLAS_OZAKI_MMA");
-        g_mma_kind = (e && !strcmp(e, "simt")) ? 1 : ((e && !strcmp(e, "pertile")) ? 0 : 2);
+        g_mma_kind = (e && !strcmp(e, "simt"))         ? 1
+                     : (e && !strcmp(e, "pertile"))    ? 0
+                     : (e && !strcmp(e, "persistent")) ? 2
+                                                       : 3;
     }
     return g_mma_kind;
 }
@@ -811,6 +814,255 @@ __global__ void __launch_bounds__(TCP_THREADS, 1)
     }
 }
 
+// Pair form of k_oz_gemm_tc_p: clusters of two CTAs on two SMs compute 256 x 256
+// tiles with tcgen05.mma.cta_group::2 (M = 256 across the pair, N = 256). Each
+// CTA stages its 128 rows of A and 128 of the 256 rows of B per K-step, so a
+// K-step moves 32 KB into each SM instead of 48 KB and six stages fit in shared
+// memory; each CTA's TMEM holds its 128 rows of the tile. Units are
+// (modulus, 256-row tile, 256-column tile), walked two at a time per cluster
+// with interleaved K chunks as in k_oz_gemm_tc_p. The MMAs are issued by the
+// even CTA; stage and accumulator barriers of both CTAs are released by its
+// multicast commits; both CTAs' loads complete on the even CTA's stage barrier
+// and both CTAs' epilogue warps release accumulators on the even CTA's barrier.
+constexpr int T2_STAGES = 6;
+constexpr int T2_A_BYTES = 128 * TC_BK * 2;   // 16 KB
+constexpr int T2_B_BYTES = 128 * TC_BK * 2;   // 16 KB (half of the 256-row B tile)
+constexpr int T2_SMEM = T2_STAGES * (T2_A_BYTES + T2_B_BYTES) + 1024 + 256;
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TCP_THREADS, 1)
+    k_oz_gemm_tc_2sm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t Mp,
+                     int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint16_t *__restrict__ R,
+                     int *status, int uplo, int tiles_m2, int tiles_n, int nz)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + T2_STAGES * T2_A_BYTES;
+    uint64_t *bars = (uint64_t *)(smem + T2_STAGES * (T2_A_BYTES + T2_B_BYTES));
+    uint64_t *full = bars;                  // [T2_STAGES] even CTA: both CTAs' loads landed
+    uint64_t *empty = bars + T2_STAGES;     // [T2_STAGES] each CTA: stage free again
+    uint64_t *accf = bars + 2 * T2_STAGES;  // [2] each CTA: chunk committed into buffer b
+    uint64_t *acce = accf + 2;              // [2] even CTA: buffer b released by both epilogues
+    uint64_t *drain = acce + 2;             // [1] even CTA: all MMAs retired
+    uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t rank = sm100::cluster_ctarank();
+    const bool lead = rank == 0;
+    const int cid = (int)(blockIdx.x >> 1), ncl = (int)(gridDim.x >> 1);
+    const int nsteps = (int)(Kp / TC_BK);
+    const int kcs = kChunk / TC_BK;
+    const int nch = (nsteps + kcs - 1) / kcs;
+    const int64_t units = (int64_t)nz * tiles_m2 * tiles_n;
+    auto unit_at = [&](int64_t u, int &tn, int &tm2, int &l) -> bool {
+        tn = (int)(u % tiles_n);
+        tm2 = (int)((u / tiles_n) % tiles_m2);
+        l = (int)(u / ((int64_t)tiles_n * tiles_m2));
+        const int64_t i0 = (int64_t)tm2 * 256, j0 = (int64_t)tn * TC_BN;
+        return !((uplo == 1 && i0 > j0 + TC_BN - 1) || (uplo == 2 && i0 + 255 < j0));
+    };
+    auto next_unit = [&](int64_t u) -> int64_t {
+        int tn, tm2, l;
+        while (u < units && !unit_at(u, tn, tm2, l)) u += ncl;
+        return u < units ? u : units;
+    };
+
+    if (warp == 0 && lane == 0) {
+        for (int st = 0; st < T2_STAGES; ++st) {
+            sm100::mbar_init(&full[st], 1);
+            sm100::mbar_init(&empty[st], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            sm100::mbar_init(&accf[b], 1);
+            sm100::mbar_init(&acce[b], 2 * TCP_EPI_WARPS);
+        }
+        sm100::mbar_init(drain, 1);
+        sm100::fence_mbar_init();
+    }
+    if (warp == 1) {
+        sm100::tmem_alloc_pair(tmem_slot, 512);
+        sm100::tmem_relinquish_pair();
+    }
+    sm100::tc_fence_before();
+    __syncthreads();
+    sm100::cluster_sync();   // both CTAs' barriers initialised, TMEM allocated
+    sm100::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            sm100::tma_prefetch_desc(&tmA);
+            sm100::tma_prefetch_desc(&tmB);
+            uint32_t gs = 0;
+            bool ok = true;
+            for (int64_t ua = next_unit(cid); ua < units && ok;) {
+                const int64_t ub = next_unit(ua + ncl);
+                const int nu = ub < units ? 2 : 1;
+                int32_t ya[2], yb[2];
+                for (int v = 0; v < nu; ++v) {
+                    int tn, tm2, l;
+                    unit_at(v ? ub : ua, tn, tm2, l);
+                    ya[v] = (int32_t)(l * Mp + (int64_t)tm2 * 256 + rank * 128);
+                    yb[v] = (int32_t)(l * Np + (int64_t)tn * TC_BN + rank * 128);
+                }
+                for (int c = 0; c < nch && ok; ++c) {
+                    const int s0 = c * kcs, s1 = min(nsteps, s0 + kcs);
+                    for (int v = 0; v < nu && ok; ++v) {
+                        for (int step = s0; step < s1; ++step) {
+                            const int st = gs % T2_STAGES;
+                            const uint32_t ph = gs / T2_STAGES;
+                            if (ph > 0 && !sm100::mbar_wait(&empty[st], (ph - 1) & 1, status, 1)) { ok = false; break; }
+                            if (lead) sm100::mbar_arrive_expect_tx(&full[st], 2 * (T2_A_BYTES + T2_B_BYTES));
+                            const uint32_t fb = sm100::mapa(&full[st], 0);
+                            sm100::tma_load_2d_pair(sA + st * T2_A_BYTES, &tmA, fb, step * TC_BK, ya[v]);
+                            sm100::tma_load_2d_pair(sB + st * T2_B_BYTES, &tmB, fb, step * TC_BK, yb[v]);
+                            ++gs;
+                        }
+                    }
+                }
+                ua = nu == 2 ? next_unit(ub + ncl) : units;
+            }
+            // Never leave with copies in flight. A stage is released (empty, in
+            // both CTAs) only after the MMAs that read it retired, i.e. after
+            // both CTAs' loads into it landed; after a failure, give loads
+            // still in flight time to land.
+            if (ok) {
+                for (uint32_t t = (gs > T2_STAGES ? gs - T2_STAGES : 0); t < gs; ++t)
+                    if (!sm100::mbar_wait(&empty[t % T2_STAGES], (t / T2_STAGES) & 1, status, 1)) { ok = false; break; }
+            }
+            if (!ok) {
+                const uint64_t t0 = sm100::globaltimer_ns();
+                while (sm100::globaltimer_ns() - t0 < 2000000ull) __nanosleep(1000);
+            }
+        }
+    } else if (warp == 1) {
+        if (lead && lane == 0) {
+            const uint32_t idesc = sm100::idesc_f16_f32(256, TC_BN);
+            uint32_t gs = 0;
+            uint32_t uses[2] = {0, 0};
+            bool ok = true;
+            for (int64_t ua = next_unit(cid); ua < units && ok;) {
+                const int64_t ub = next_unit(ua + ncl);
+                const int nu = ub < units ? 2 : 1;
+                for (int c = 0; c < nch && ok; ++c) {
+                    const int s0 = c * kcs, s1 = min(nsteps, s0 + kcs);
+                    for (int b = 0; b < nu && ok; ++b) {
+                        if (uses[b] > 0) {   // both CTAs' epilogues released the previous chunk in this buffer
+                            if (!sm100::mbar_wait_cluster(&acce[b], (uses[b] - 1) & 1, status, 2)) { ok = false; break; }
+                            sm100::tc_fence_after();
+                        }
+                        for (int step = s0; step < s1; ++step) {
+                            const int st = gs % T2_STAGES;
+                            if (!sm100::mbar_wait_cluster(&full[st], (gs / T2_STAGES) & 1, status, 3)) { ok = false; break; }
+                            sm100::tc_fence_after();
+                            const uint64_t ad = sm100::smem_desc_sw128(sm100::smem_u32(sA + st * T2_A_BYTES));
+                            const uint64_t bd = sm100::smem_desc_sw128(sm100::smem_u32(sB + st * T2_B_BYTES));
+#pragma unroll
+                            for (int kk = 0; kk < TC_BK / 16; ++kk) {
+                                const uint32_t acc = (c > 0 || step > s0 || kk > 0) ? 1u : 0u;
+                                sm100::mma_f16_pair(tmem + b * TC_BN, ad + 2 * kk, bd + 2 * kk, idesc, acc);
+                            }
+                            sm100::mma_commit_pair(&empty[st], 3);
+                            ++gs;
+                        }
+                        if (!ok) break;
+                        sm100::mma_commit_pair(&accf[b], 3);
+                        ++uses[b];
+                    }
+                }
+                ua = nu == 2 ? next_unit(ub + ncl) : units;
+            }
+            sm100::mma_commit_pair(drain, 1);
+            sm100::mbar_wait(drain, 0, nullptr, 0);
+        }
+    } else {
+        // ---- epilogue: warps 2..9 of each CTA on its 128 rows (TMEM lane quadrant
+        // warp % 4, column half (warp - 2) / 4)
+        const int q = warp & 3;
+        const int half = (warp - 2) >> 2;
+        const int row = q * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + half * (TC_BN / 2);
+        const uint32_t acce_lead[2] = {sm100::mapa(&acce[0], 0), sm100::mapa(&acce[1], 0)};
+        uint32_t fcnt[2] = {0, 0};
+        bool ok = true;
+        for (int64_t ua = next_unit(cid); ua < units && ok;) {
+            const int64_t ub = next_unit(ua + ncl);
+            const int nu = ub < units ? 2 : 1;
+            for (int c = 0; c < nch && ok; ++c) {
+                for (int b = 0; b < nu; ++b) {
+                    int tn, tm2, l;
+                    unit_at(b ? ub : ua, tn, tm2, l);
+                    const float p = P.p[l], invp = P.invp[l];
+                    if (!__all_sync(0xffffffffu, sm100::mbar_wait(&accf[b], fcnt[b] & 1, status, 4))) {
+                        ok = false;
+                        break;
+                    }
+                    ++fcnt[b];
+                    sm100::tc_fence_after();
+                    const uint32_t tb = lane_base + b * TC_BN;
+                    const float2 negp2 = make_float2(-p, -p), invp2 = make_float2(invp, invp);
+                    const int64_t i = (int64_t)tm2 * 256 + rank * 128 + row;
+                    const int64_t j0 = (int64_t)tn * TC_BN + half * (TC_BN / 2);
+                    const bool row_ok = i < M;
+                    const int jn = (int)max((int64_t)0, min((int64_t)(TC_BN / 2), N - j0));
+                    uint16_t *o = R + ((int64_t)l * Np + j0) * Mp + i;   // advanced by Mp per column
+#pragma unroll 1
+                    for (int hh = 0; hh < 2; ++hh) {
+                        uint32_t r[2][32];
+                        sm100::tmem_ld32(tb + hh * 64, r[0]);
+                        sm100::tmem_ld32(tb + hh * 64 + 32, r[1]);
+                        sm100::tmem_wait_ld();
+#pragma unroll
+                        for (int sl = 0; sl < 2; ++sl) {
+#pragma unroll
+                            for (int t = 0; t < 32; t += 2) {
+                                float2 x = make_float2(__uint_as_float(r[sl][t]), __uint_as_float(r[sl][t + 1]));
+                                float2 y = __fmul2_rn(x, invp2);
+                                y = __fadd2_rn(y, make_float2(12582912.0f, 12582912.0f));
+                                y = __fadd2_rn(y, make_float2(-12582912.0f, -12582912.0f));
+                                x = __ffma2_rn(y, negp2, x);
+                                r[sl][t] = __float_as_uint(x.x);
+                                r[sl][t + 1] = __float_as_uint(x.y);
+                            }
+                        }
+                        if (c < nch - 1) {
+                            sm100::tmem_st32(tb + hh * 64, r[0]);
+                            sm100::tmem_st32(tb + hh * 64 + 32, r[1]);
+                        } else {
+#pragma unroll
+                            for (int sl = 0; sl < 2; ++sl) {
+#pragma unroll
+                                for (int t = 0; t < 32; ++t) {
+                                    float rr = __uint_as_float(r[sl][t]);
+                                    if (rr < 0.0f) rr = __fadd_rn(rr, p);
+                                    if (row_ok && hh * 64 + sl * 32 + t < jn) *o = (uint16_t)small_uint(rr);
+                                    o += Mp;
+                                }
+                            }
+                        }
+                    }
+                    if (c < nch - 1) sm100::tmem_wait_st();
+                    sm100::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) sm100::mbar_arrive_cluster(acce_lead[b]);
+                }
+            }
+            ua = nu == 2 ? next_unit(ub + ncl) : units;
+        }
+    }
+
+    // Both CTAs stay resident until every role of both is done: the even CTA's
+    // MMAs write the odd CTA's TMEM and read its shared memory, and the odd
+    // CTA's epilogue arrives on the even CTA's barriers.
+    sm100::tc_fence_before();
+    __syncthreads();
+    sm100::cluster_sync();
+    if (warp == 1) {
+        sm100::tc_fence_after();
+        sm100::tmem_dealloc_pair(tmem, 512);
+    }
+}
+
 // ---- device: residue GEMM, CUDA cores (cross-check engine) ---------------------------------
 
 __global__ void __launch_bounds__(256) k_oz_gemm_simt(const __half *__restrict__ A, const __half *__restrict__ B,
@@ -1199,7 +1451,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     // per-modulus row padding.
     const bool shared_ops = !cplx && g.uplo != 0 && g.A == g.B && g.lda == g.ldb && g.ta != g.tb && m == n;
     const int64_t Np = (n + TC_BN - 1) / TC_BN * TC_BN;
-    const int64_t Mp = shared_ops ? Np : (m + TC_BM - 1) / TC_BM * TC_BM;
+    const int64_t Mp = shared_ops ? Np : (m + 255) / 256 * 256;   // the pair kernel's 256-row tiles
     const int64_t Kp = (k + TC_BK - 1) / TC_BK * TC_BK;
 
     // 1. exponent bounds of the rows of op(A) / columns of op(B)
@@ -1275,12 +1527,21 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     phase_mark(PH_GEMM);
     bool ok = true;
     const int nz = nc * md.n;
-    if (mma_kind() == 0 || mma_kind() == 2) {
+    if (mma_kind() == 0 || mma_kind() == 2 || mma_kind() == 3) {
         CUtensorMap ma, mb;
         ok = make_map(&ma, Ares, (uint64_t)Kp, (uint64_t)(nz * Mp), TC_BM, routine) &&
-             make_map(&mb, Bres, (uint64_t)Kp, (uint64_t)(nz * Np), TC_BN, routine);
+             make_map(&mb, Bres, (uint64_t)Kp, (uint64_t)(nz * Np), mma_kind() == 3 ? 128 : TC_BN, routine);
         if (ok) {
-            if (mma_kind() == 2) {
+            if (mma_kind() == 3) {
+                cudaFuncSetAttribute(k_oz_gemm_tc_2sm, cudaFuncAttributeMaxDynamicSharedMemorySize, T2_SMEM);
+                const int tiles_m2 = (int)(Mp / 256), tiles_n = (int)(Np / TC_BN);
+                const int64_t units = (int64_t)nz * tiles_m2 * tiles_n;
+                const int64_t pairs = device_sm_count() / 2;
+                const unsigned grid = 2u * (unsigned)(units < pairs ? units : pairs);
+                k_oz_gemm_tc_2sm<<<grid, TCP_THREADS, T2_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R,
+                                                                           device_status_word(), g.uplo, tiles_m2,
+                                                                           tiles_n, nz);
+            } else if (mma_kind() == 2) {
                 cudaFuncSetAttribute(k_oz_gemm_tc_p, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
                 const int tiles_m = (int)(Mp / TC_BM), tiles_n = (int)(Np / TC_BN);
                 const int64_t units = (int64_t)nz * tiles_m * tiles_n;
@@ -1373,6 +1634,6 @@ extern "C" float mwblas_last_phase_ms(int phase)
 extern "C" int mwblas_set_ozaki_mma(int kind)
 {
     int prev = mw::mma_kind();
-    mw::g_mma_kind = (kind >= 0 && kind <= 2) ? kind : 2;
+    mw::g_mma_kind = (kind >= 0 && kind <= 3) ? kind : 3;
     return prev;
 }

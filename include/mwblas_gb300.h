@@ -239,10 +239,11 @@ int mwblas_last_ozaki_moduli(void);
  * per (modulus, tile), 1 = CUDA cores (an independent exact path used to
  * cross-check the tensor cores), 2 = tcgen05 in a persistent kernel (one CTA
  * per SM walking the (modulus, tile) units two at a time, so that one unit's
- * final reduction overlaps the other's MMAs; the default). The
- * MWBLAS_OZAKI_MMA environment variable ("pertile", "simt", "persistent")
- * selects them too. All produce bit-identical results. Returns the previous
- * value. */
+ * final reduction overlaps the other's MMAs), 3 = as 2 with pairs of CTAs on
+ * two SMs computing 256 x 256 tiles with cta_group::2 MMAs (the default). The
+ * MWBLAS_OZAKI_MMA environment variable ("pertile", "simt", "persistent",
+ * "pair") selects them too. All produce bit-identical results. Returns the
+ * previous value. */
 int mwblas_set_ozaki_mma(int kind);
 
 /* Per-phase device timing of the Ozaki engine (CUDA events on the library

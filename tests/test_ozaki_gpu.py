@@ -50,7 +50,7 @@ def test_tensor_core_and_cuda_core_paths_bit_identical(gpu, rng):
     B = mwb.dd_matrix(rng, k, n)
     al, be = mwb.random_dd(rng, ()), np.zeros(2)
     outs = []
-    for kind in (0, 1, 2):   # per-tile tcgen05, CUDA cores, persistent tcgen05
+    for kind in (0, 1, 2, 3):   # per-tile tcgen05, CUDA cores, persistent tcgen05, CTA pairs
         prev = gpu.lib.mwblas_set_ozaki_mma(kind)
         try:
             c = np.zeros((n, m, 2))
@@ -61,6 +61,7 @@ def test_tensor_core_and_cuda_core_paths_bit_identical(gpu, rng):
             gpu.lib.mwblas_set_ozaki_mma(prev)
     np.testing.assert_array_equal(outs[0], outs[1])
     np.testing.assert_array_equal(outs[0], outs[2])
+    np.testing.assert_array_equal(outs[0], outs[3])
 
 
 @pytest.mark.parametrize("k", [300, 512, 1024, 1500, 2600])
@@ -73,7 +74,7 @@ def test_persistent_tensor_core_kernel(gpu, rng, k, uplo):
     n = 700
     A = mwb.dd_matrix(rng, n, k)
     outs = []
-    for kind in (0, 2):
+    for kind in (0, 2, 3):
         prev = gpu.lib.mwblas_set_ozaki_mma(kind)
         try:
             c = np.zeros((n, n, 2))
@@ -87,6 +88,7 @@ def test_persistent_tensor_core_kernel(gpu, rng, k, uplo):
         finally:
             gpu.lib.mwblas_set_ozaki_mma(prev)
     np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
 
 
 def test_exponent_spread_stress(gpu, oracle, rng):
@@ -189,7 +191,7 @@ def test_ozaki_complex_tc_equals_cuda_core(gpu, rng):
     A = mwb.dd_matrix(rng, m, k, cplx_=True)
     B = mwb.dd_matrix(rng, k, n, cplx_=True)
     outs = []
-    for kind in (0, 1, 2):
+    for kind in (0, 1, 2, 3):
         prev = gpu.lib.mwblas_set_ozaki_mma(kind)
         try:
             c = np.zeros((n, m, 2, 2))
@@ -200,6 +202,7 @@ def test_ozaki_complex_tc_equals_cuda_core(gpu, rng):
             gpu.lib.mwblas_set_ozaki_mma(prev)
     np.testing.assert_array_equal(outs[0], outs[1])
     np.testing.assert_array_equal(outs[0], outs[2])
+    np.testing.assert_array_equal(outs[0], outs[3])
 
 
 @pytest.mark.parametrize("uplo", ["U", "L"])
