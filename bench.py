@@ -382,14 +382,16 @@ def main():
 
     pk, pk_kind = res["peaks"], res["peaks_kind"]
     n = args.n
-    # Roofline of the dominant kernel (the tcgen05 residue GEMM, one launch
+    # Roofline of the dominant kernel (the tcgen05 residue GEMM on CTA pairs, one launch
     # per step): algorithmic fp16 tensor flops per launch = moduli * 2*m*n*k
     # (the padded tile work is not counted), over its CUDA-event duration.
     tc_ms = res["phase_ms"][2]
     tc_flops = res["moduli"] * 2.0 * n * n * n
     peak_tf = pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
     achieved = tc_flops / (tc_ms * 1e-3) / 1e12 if tc_ms > 0 else None
-    roof = {"bound": "tensor", "kernel": "k_oz_gemm_tc (tcgen05.mma kind::f16, fp32 accumulate in TMEM)",
+    roof = {"bound": "tensor",
+            "kernel": "k_oz_gemm_tc_2sm (tcgen05.mma.cta_group::2 kind::f16, 256x256 tiles on SM pairs, "
+                      "fp32 accumulate in TMEM)",
             "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
             "frac": (achieved / peak_tf) if achieved else None,
             "peak_kind": f"{pk_kind} bf16 dense, sustained figure (MEASURED_PEAKS.json)",
@@ -416,7 +418,7 @@ def main():
 
 
 def tc_traffic_from_profile():
-    p = os.path.join(ROOT, "profiles", "k_oz_gemm_tc_4096_ncu.txt")
+    p = os.path.join(ROOT, "profiles", "k_oz_gemm_tc_2sm_4096_ncu.txt")
     if not os.path.exists(p):
         return None
     for line in open(p):
