@@ -119,6 +119,21 @@ __device__ __forceinline__ real neg(real a) { return make(-a.hi, -a.lo); }
 __device__ __forceinline__ real sub_exact(real x, real y) { return add_exact(x, neg(y)); }
 __device__ __forceinline__ real sub_fast(real x, real y) { return add_fast(x, neg(y)); }
 
+// Double-double division a / b (Hida, Li, Bailey 2001, "accurate" DD
+// division): three quotient digits from the hi limbs, the remainder
+// recomputed in double-double after each.
+__device__ __forceinline__ real div(real a, real b)
+{
+    double q1 = __ddiv_rn(a.hi, b.hi);
+    real r = sub_exact(a, mul_exact(make(q1, 0.0), b));
+    double q2 = __ddiv_rn(r.hi, b.hi);
+    r = sub_exact(r, mul_exact(make(q2, 0.0), b));
+    double q3 = __ddiv_rn(r.hi, b.hi);
+    real q;
+    fast_two_sum(q1, q2, q.hi, q.lo);
+    return add_exact(q, make(q3, 0.0));
+}
+
 // ---- complex (mf_simd_fast.h:119-144 and mf_kernels.h:43-53) -------------
 
 // fast complex multiply: re = a.re*b.re - a.im*b.im ; im = a.re*b.im + a.im*b.re

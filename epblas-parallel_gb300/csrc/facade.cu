@@ -14,6 +14,7 @@
 #include "gemm.h"
 #include "l1.h"
 #include "level3.h"
+#include "level3x.h"
 #include "runtime.h"
 
 namespace mw {
@@ -454,6 +455,275 @@ mwblas_real64x2 dot_entry(const char *routine, const INT *n, const void *x, cons
     return r;
 }
 
+// ---- mgemmtr / wgemmtr (mgemmtr_parallel.cpp:35-80) -------------------------------------
+
+GemmArgs scalars(bool cplx, const void *alpha, const void *beta)
+{
+    GemmArgs g;
+    if (cplx) {
+        g.calpha = cd((const mwblas_complex64x2 *)alpha);
+        g.cbeta = cd((const mwblas_complex64x2 *)beta);
+        g.beta_kind = beta_kind(g.cbeta);
+    } else {
+        g.alpha = rd((const mwblas_real64x2 *)alpha);
+        g.beta = rd((const mwblas_real64x2 *)beta);
+        g.beta_kind = beta_kind(g.beta);
+    }
+    return g;
+}
+
+bool is_zero(bool cplx, const void *v)
+{
+    return cplx ? ceq0(cd((const mwblas_complex64x2 *)v)) : eq0(rd((const mwblas_real64x2 *)v));
+}
+bool is_one(bool cplx, const void *v)
+{
+    return cplx ? ceq1(cd((const mwblas_complex64x2 *)v)) : eq1(rd((const mwblas_real64x2 *)v));
+}
+
+template <typename INT>
+void gemmtr_entry(const char *routine, bool cplx, const char *uplo, const char *transa, const char *transb,
+                  const INT *n, const INT *k, const void *alpha, const void *a, const INT *lda, const void *b,
+                  const INT *ldb, const void *beta, void *c, const INT *ldc)
+{
+    Scope sc(routine);
+    if (!uplo || !transa || !transb || !n || !k || !alpha || !beta || !lda || !ldb || !ldc) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char U = up(uplo);
+    char TA = cplx ? up(transa) : trans_real(transa);
+    char TB = cplx ? up(transb) : trans_real(transb);
+    if (U != 'U' && U != 'L') { set_error(routine, 1, "invalid uplo"); return; }
+    if (!(TA == 'N' || TA == 'T' || TA == 'C')) { set_error(routine, 2, "invalid transa"); return; }
+    if (!(TB == 'N' || TB == 'T' || TB == 'C')) { set_error(routine, 3, "invalid transb"); return; }
+    int64_t N = *n, K = *k;
+    if (N <= 0) return;   // mgemmtr_parallel.cpp:56
+    if (K < 0) K = 0;
+    int64_t nrowa = (TA == 'N') ? N : K, nrowb = (TB == 'N') ? K : N;
+    if (*lda < (nrowa > 1 ? nrowa : 1)) { set_error(routine, 8, "lda too small"); return; }
+    if (*ldb < (nrowb > 1 ? nrowb : 1)) { set_error(routine, 10, "ldb too small"); return; }
+    if (*ldc < (N > 1 ? N : 1)) { set_error(routine, 13, "ldc too small"); return; }
+    if (!c) { set_error(routine, 12, "null C"); return; }
+    const bool compute = !(is_zero(cplx, alpha) || K == 0);
+    if (!compute && is_one(cplx, beta)) return;   // mgemmtr_parallel.cpp:58-59
+    if (compute && (!a || !b)) { set_error(routine, a ? 9 : 7, "null A or B"); return; }
+    if (!ensure_device(routine)) return;
+    const size_t es = cplx ? 32 : 16;
+    const int ul = U == 'U' ? 1 : 2;
+    Staged SA, SB, SC;
+    sc.add(SA); sc.add(SB); sc.add(SC);
+    if (!stage_matrix(SC, c, N, N, *ldc, es, true, routine)) return;   // the other triangle is written back as read
+    const GemmArgs g = scalars(cplx, alpha, beta);
+    if (!compute) {
+        if (cplx) launch_scale_matrix_c(N, N, g.cbeta, g.beta_kind, SC.dev, *ldc, ul);
+        else launch_scale_matrix(N, N, g.beta, g.beta_kind, SC.dev, *ldc, ul);
+    } else {
+        if (!stage_matrix(SA, a, nrowa, TA == 'N' ? K : N, *lda, es, true, routine)) return;
+        if (!stage_matrix(SB, b, nrowb, TB == 'N' ? N : K, *ldb, es, true, routine)) return;
+        if (!gemmtr_device(cplx, ul, TA != 'N', TA == 'C', TB != 'N', TB == 'C', N, K, g, SA.dev, *lda, SB.dev,
+                           *ldb, SC.dev, *ldc, routine))
+            return;
+    }
+    if (!unstage_matrix(SC, routine)) return;
+    finish(routine);
+}
+
+// ---- msymm / wsymm / whemm (msymm_parallel.cpp:37-102) -------------------------------------
+
+template <typename INT>
+void symm_entry(const char *routine, bool cplx, bool herm, const char *side, const char *uplo, const INT *m,
+                const INT *n, const void *alpha, const void *a, const INT *lda, const void *b, const INT *ldb,
+                const void *beta, void *c, const INT *ldc)
+{
+    Scope sc(routine);
+    if (!side || !uplo || !m || !n || !alpha || !beta || !lda || !ldb || !ldc) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char S = up(side), U = up(uplo);
+    if (S != 'L' && S != 'R') { set_error(routine, 1, "invalid side"); return; }
+    if (U != 'U' && U != 'L') { set_error(routine, 2, "invalid uplo"); return; }
+    int64_t M = *m, N = *n;
+    if (M < 0) { set_error(routine, 3, "m < 0"); return; }
+    if (N < 0) { set_error(routine, 4, "n < 0"); return; }
+    if (M == 0 || N == 0) return;   // msymm_parallel.cpp:58
+    int64_t na = S == 'L' ? M : N;
+    if (*lda < (na > 1 ? na : 1)) { set_error(routine, 7, "lda too small"); return; }
+    if (*ldb < (M > 1 ? M : 1)) { set_error(routine, 9, "ldb too small"); return; }
+    if (*ldc < (M > 1 ? M : 1)) { set_error(routine, 12, "ldc too small"); return; }
+    if (!c) { set_error(routine, 11, "null C"); return; }
+    const bool alpha0 = is_zero(cplx, alpha);
+    if (alpha0 && is_one(cplx, beta)) return;   // msymm_parallel.cpp:60-61
+    if (!alpha0 && (!a || !b)) { set_error(routine, a ? 8 : 6, "null A or B"); return; }
+    if (!ensure_device(routine)) return;
+    const size_t es = cplx ? 32 : 16;
+    GemmArgs g = scalars(cplx, alpha, beta);
+    Staged SA, SB, SC;
+    sc.add(SA); sc.add(SB); sc.add(SC);
+    if (!stage_matrix(SC, c, M, N, *ldc, es, g.beta_kind != 0, routine)) return;
+    if (alpha0) {
+        if (cplx) launch_scale_matrix_c(M, N, g.cbeta, g.beta_kind, SC.dev, *ldc);
+        else launch_scale_matrix(M, N, g.beta, g.beta_kind, SC.dev, *ldc);
+    } else {
+        if (!stage_matrix(SA, a, na, na, *lda, es, true, routine)) return;
+        if (!stage_matrix(SB, b, M, N, *ldb, es, true, routine)) return;
+        if (!symm_device(cplx, herm, S, U, M, N, g, SA.dev, *lda, SB.dev, *ldb, SC.dev, *ldc, routine)) return;
+    }
+    if (!unstage_matrix(SC, routine)) return;
+    finish(routine);
+}
+
+// ---- msyr2k / wsyr2k / wher2k (msyr2k_parallel.cpp:38-83, wher2k_parallel.cpp) ------------
+// beta is real for HER2K (beta_cplx=false), alpha always of the matrix type.
+
+template <typename INT>
+void syr2k_entry(const char *routine, bool cplx, bool herm, const char *uplo, const char *trans, const INT *n,
+                 const INT *k, const void *alpha, const void *a, const INT *lda, const void *b, const INT *ldb,
+                 const void *beta, void *c, const INT *ldc)
+{
+    Scope sc(routine);
+    if (!uplo || !trans || !n || !k || !alpha || !beta || !lda || !ldb || !ldc) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char U = up(uplo), T = up(trans);
+    if (!herm && T == 'C') T = 'T';   // msyr2k / wsyr2k_parallel.cpp:58
+    if (herm && T == 'T') T = 'C';
+    if (U != 'U' && U != 'L') { set_error(routine, 1, "invalid uplo"); return; }
+    if (T != 'N' && T != (herm ? 'C' : 'T')) { set_error(routine, 2, "invalid trans"); return; }
+    int64_t N = *n, K = *k;
+    if (N < 0) { set_error(routine, 3, "n < 0"); return; }
+    if (K < 0) { set_error(routine, 4, "k < 0"); return; }
+    if (N == 0) return;
+    int64_t nrow = (T == 'N') ? N : K;
+    if (*lda < (nrow > 1 ? nrow : 1)) { set_error(routine, 7, "lda too small"); return; }
+    if (*ldb < (nrow > 1 ? nrow : 1)) { set_error(routine, 9, "ldb too small"); return; }
+    if (*ldc < (N > 1 ? N : 1)) { set_error(routine, 12, "ldc too small"); return; }
+    if (!c) { set_error(routine, 11, "null C"); return; }
+    // scalars: HER2K has a complex alpha and a real beta
+    GemmArgs g;
+    if (cplx) {
+        g.calpha = cd((const mwblas_complex64x2 *)alpha);
+        g.cbeta = herm ? cdd_host{rd((const mwblas_real64x2 *)beta), {0.0, 0.0}} : cd((const mwblas_complex64x2 *)beta);
+        g.beta_kind = beta_kind(g.cbeta);
+    } else {
+        g.alpha = rd((const mwblas_real64x2 *)alpha);
+        g.beta = rd((const mwblas_real64x2 *)beta);
+        g.beta_kind = beta_kind(g.beta);
+    }
+    const bool compute = !(is_zero(cplx, alpha) || K == 0);
+    if (!compute && g.beta_kind == 1 && !herm) return;   // msyr2k_parallel.cpp:62-63
+    if (compute && (!a || !b)) { set_error(routine, a ? 8 : 6, "null A or B"); return; }
+    if (!ensure_device(routine)) return;
+    const size_t es = cplx ? 32 : 16;
+    const int ul = U == 'U' ? 1 : 2;
+    Staged SA, SB, SC;
+    sc.add(SA); sc.add(SB); sc.add(SC);
+    if (!stage_matrix(SC, c, N, N, *ldc, es, true, routine)) return;
+    if (!compute) {
+        // wher2k_parallel.cpp:65-75: beta == 1 still zeroes Im(diag)
+        if (cplx) launch_scale_matrix_c(N, N, g.cbeta, g.beta_kind, SC.dev, *ldc, ul, herm);
+        else launch_scale_matrix(N, N, g.beta, g.beta_kind, SC.dev, *ldc, ul);
+    } else {
+        if (!stage_matrix(SA, a, nrow, T == 'N' ? K : N, *lda, es, true, routine)) return;
+        if (!stage_matrix(SB, b, nrow, T == 'N' ? K : N, *ldb, es, true, routine)) return;
+        if (!syr2k_device(cplx, herm, ul, T != 'N', N, K, g, SA.dev, *lda, SB.dev, *ldb, SC.dev, *ldc, routine))
+            return;
+    }
+    if (!unstage_matrix(SC, routine)) return;
+    finish(routine);
+}
+
+// ---- wsyrk (wsyrk_parallel.cpp): complex symmetric rank-k, complex alpha/beta -----------
+
+template <typename INT>
+void csyrk_entry(const char *routine, const char *uplo, const char *trans, const INT *n, const INT *k,
+                 const mwblas_complex64x2 *alpha, const void *a, const INT *lda, const mwblas_complex64x2 *beta,
+                 void *c, const INT *ldc)
+{
+    Scope sc(routine);
+    if (!uplo || !trans || !n || !k || !alpha || !beta || !lda || !ldc) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char U = up(uplo), T = up(trans);
+    if (T == 'C') T = 'T';
+    if (U != 'U' && U != 'L') { set_error(routine, 1, "invalid uplo"); return; }
+    if (T != 'N' && T != 'T') { set_error(routine, 2, "invalid trans"); return; }
+    int64_t N = *n, K = *k;
+    if (N < 0) { set_error(routine, 3, "n < 0"); return; }
+    if (K < 0) { set_error(routine, 4, "k < 0"); return; }
+    if (N == 0) return;   // wsyrk_parallel.cpp:55
+    int64_t nrowa = (T == 'N') ? N : K;
+    if (*lda < (nrowa > 1 ? nrowa : 1)) { set_error(routine, 7, "lda too small"); return; }
+    if (*ldc < (N > 1 ? N : 1)) { set_error(routine, 10, "ldc too small"); return; }
+    if (!c) { set_error(routine, 9, "null C"); return; }
+    GemmArgs g = scalars(true, alpha, beta);
+    const bool compute = !(ceq0(g.calpha) || K == 0);
+    if (!compute && g.beta_kind == 1) return;   // wsyrk_parallel.cpp:57-58
+    if (compute && !a) { set_error(routine, 6, "null A"); return; }
+    if (!ensure_device(routine)) return;
+    const int ul = U == 'U' ? 1 : 2;
+    Staged SA, SC;
+    sc.add(SA); sc.add(SC);
+    if (!stage_matrix(SC, c, N, N, *ldc, 32, true, routine)) return;
+    if (!compute) {
+        launch_scale_matrix_c(N, N, g.cbeta, g.beta_kind, SC.dev, *ldc, ul);
+    } else {
+        if (!stage_matrix(SA, a, nrowa, T == 'N' ? K : N, *lda, 32, true, routine)) return;
+        if (!syrk_device(true, false, ul, T != 'N', N, K, SA.dev, *lda, g, SC.dev, *ldc, routine)) return;
+    }
+    if (!unstage_matrix(SC, routine)) return;
+    finish(routine);
+}
+
+// ---- mtrmm / wtrmm (mtrmm_parallel.cpp:37-106) and wtrsm (wtrsm_parallel.cpp) ------------
+
+template <typename INT>
+void trxm_entry(const char *routine, bool cplx, bool solve, const char *side, const char *uplo, const char *transa,
+                const char *diag, const INT *m, const INT *n, const void *alpha, const void *a, const INT *lda,
+                void *b, const INT *ldb)
+{
+    Scope sc(routine);
+    if (!side || !uplo || !transa || !diag || !m || !n || !alpha || !lda || !ldb) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char S = up(side), U = up(uplo), T = cplx ? up(transa) : trans_real(transa), D = up(diag);
+    if (S != 'L' && S != 'R') { set_error(routine, 1, "invalid side"); return; }
+    if (U != 'U' && U != 'L') { set_error(routine, 2, "invalid uplo"); return; }
+    if (T != 'N' && T != 'T' && T != 'C') { set_error(routine, 3, "invalid transa"); return; }
+    if (D != 'U' && D != 'N') { set_error(routine, 4, "invalid diag"); return; }
+    int64_t M = *m, N = *n;
+    if (M < 0) { set_error(routine, 5, "m < 0"); return; }
+    if (N < 0) { set_error(routine, 6, "n < 0"); return; }
+    if (M == 0 || N == 0) return;   // mtrmm_parallel.cpp:58, wtrsm_parallel.cpp:58
+    int64_t na = (S == 'L') ? M : N;
+    if (*lda < (na > 1 ? na : 1)) { set_error(routine, 9, "lda too small"); return; }
+    if (*ldb < (M > 1 ? M : 1)) { set_error(routine, 11, "ldb too small"); return; }
+    if (!b) { set_error(routine, 10, "null B"); return; }
+    const bool zero = is_zero(cplx, alpha);   // mtrmm_parallel.cpp:60: alpha == 0 zeroes B
+    if (!zero && !a) { set_error(routine, 8, "null A"); return; }
+    if (!ensure_device(routine)) return;
+    const size_t es = cplx ? 32 : 16;
+    Staged SA, SB;
+    sc.add(SA); sc.add(SB);
+    if (!stage_matrix(SB, b, M, N, *ldb, es, !zero, routine)) return;
+    if (zero) {
+        if (cplx) launch_scale_matrix_c(M, N, cdd_host{{0.0, 0.0}, {0.0, 0.0}}, 0, SB.dev, *ldb);
+        else launch_zero_matrix(M, N, SB.dev, *ldb);
+    } else {
+        if (!stage_matrix(SA, a, na, na, *lda, es, true, routine)) return;
+        GemmArgs g = scalars(cplx, alpha, alpha);
+        bool ok = solve ? ctrsm_device(S, U, T, D, M, N, g.calpha, SA.dev, *lda, SB.dev, *ldb, routine)
+                        : trmm_device(cplx, S, U, T, D, M, N, g, SA.dev, *lda, SB.dev, *ldb, routine);
+        if (!ok) return;
+    }
+    if (!unstage_matrix(SB, routine)) return;
+    finish(routine);
+}
+
 }  // namespace
 }  // namespace mw
 
@@ -507,6 +777,83 @@ void mtrsm_64_(const char *side, const char *uplo, const char *transa, const cha
 {
     mw::trsm_entry<int64_t>("mtrsm", side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb);
 }
+
+#define MW_GEMMTR_PAIR(NAME, T, CPLX)                                                                             \
+    void NAME##_(const char *uplo, const char *ta, const char *tb, const int *n, const int *k, const T *alpha,  \
+                 const T *a, const int *lda, const T *b, const int *ldb, const T *beta, T *c, const int *ldc)   \
+    {                                                                                                           \
+        mw::gemmtr_entry<int>(#NAME, CPLX, uplo, ta, tb, n, k, alpha, a, lda, b, ldb, beta, c, ldc);            \
+    }                                                                                                           \
+    void NAME##_64_(const char *uplo, const char *ta, const char *tb, const int64_t *n, const int64_t *k,      \
+                    const T *alpha, const T *a, const int64_t *lda, const T *b, const int64_t *ldb,             \
+                    const T *beta, T *c, const int64_t *ldc)                                                    \
+    {                                                                                                           \
+        mw::gemmtr_entry<int64_t>(#NAME, CPLX, uplo, ta, tb, n, k, alpha, a, lda, b, ldb, beta, c, ldc);        \
+    }
+MW_GEMMTR_PAIR(mgemmtr, TR, false)
+MW_GEMMTR_PAIR(wgemmtr, TC, true)
+#undef MW_GEMMTR_PAIR
+
+#define MW_SYMM_PAIR(NAME, T, CPLX, HERM)                                                                         \
+    void NAME##_(const char *side, const char *uplo, const int *m, const int *n, const T *alpha, const T *a,    \
+                 const int *lda, const T *b, const int *ldb, const T *beta, T *c, const int *ldc)               \
+    {                                                                                                           \
+        mw::symm_entry<int>(#NAME, CPLX, HERM, side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc);          \
+    }                                                                                                           \
+    void NAME##_64_(const char *side, const char *uplo, const int64_t *m, const int64_t *n, const T *alpha,     \
+                    const T *a, const int64_t *lda, const T *b, const int64_t *ldb, const T *beta, T *c,        \
+                    const int64_t *ldc)                                                                         \
+    {                                                                                                           \
+        mw::symm_entry<int64_t>(#NAME, CPLX, HERM, side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc);      \
+    }
+MW_SYMM_PAIR(msymm, TR, false, false)
+MW_SYMM_PAIR(wsymm, TC, true, false)
+MW_SYMM_PAIR(whemm, TC, true, true)
+#undef MW_SYMM_PAIR
+
+#define MW_SYR2K_PAIR(NAME, SA, SB, VT, CPLX, HERM)                                                                \
+    void NAME##_(const char *uplo, const char *trans, const int *n, const int *k, const SA *alpha, const VT *a,  \
+                 const int *lda, const VT *b, const int *ldb, const SB *beta, VT *c, const int *ldc)             \
+    {                                                                                                            \
+        mw::syr2k_entry<int>(#NAME, CPLX, HERM, uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc);         \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const char *trans, const int64_t *n, const int64_t *k, const SA *alpha,   \
+                    const VT *a, const int64_t *lda, const VT *b, const int64_t *ldb, const SB *beta, VT *c,     \
+                    const int64_t *ldc)                                                                          \
+    {                                                                                                            \
+        mw::syr2k_entry<int64_t>(#NAME, CPLX, HERM, uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc);     \
+    }
+MW_SYR2K_PAIR(msyr2k, TR, TR, TR, false, false)
+MW_SYR2K_PAIR(wsyr2k, TC, TC, TC, true, false)
+MW_SYR2K_PAIR(wher2k, TC, TR, TC, true, true)
+#undef MW_SYR2K_PAIR
+
+void wsyrk_(const char *uplo, const char *trans, const int *n, const int *k, const TC *alpha, const TC *a,
+            const int *lda, const TC *beta, TC *c, const int *ldc)
+{
+    mw::csyrk_entry<int>("wsyrk", uplo, trans, n, k, alpha, a, lda, beta, c, ldc);
+}
+void wsyrk_64_(const char *uplo, const char *trans, const int64_t *n, const int64_t *k, const TC *alpha, const TC *a,
+               const int64_t *lda, const TC *beta, TC *c, const int64_t *ldc)
+{
+    mw::csyrk_entry<int64_t>("wsyrk", uplo, trans, n, k, alpha, a, lda, beta, c, ldc);
+}
+
+#define MW_TRXM_PAIR(NAME, T, CPLX, SOLVE)                                                                          \
+    void NAME##_(const char *side, const char *uplo, const char *transa, const char *diag, const int *m,          \
+                 const int *n, const T *alpha, const T *a, const int *lda, T *b, const int *ldb)                  \
+    {                                                                                                             \
+        mw::trxm_entry<int>(#NAME, CPLX, SOLVE, side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb);           \
+    }                                                                                                             \
+    void NAME##_64_(const char *side, const char *uplo, const char *transa, const char *diag, const int64_t *m,   \
+                    const int64_t *n, const T *alpha, const T *a, const int64_t *lda, T *b, const int64_t *ldb)   \
+    {                                                                                                             \
+        mw::trxm_entry<int64_t>(#NAME, CPLX, SOLVE, side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb);       \
+    }
+MW_TRXM_PAIR(mtrmm, TR, false, false)
+MW_TRXM_PAIR(wtrmm, TC, true, false)
+MW_TRXM_PAIR(wtrsm, TC, true, true)
+#undef MW_TRXM_PAIR
 
 // ---- level 2 -----------------------------------------------------------------------------
 

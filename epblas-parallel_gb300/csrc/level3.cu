@@ -31,20 +31,7 @@ namespace mw {
 
 namespace {
 
-// Double-double division a / b (Hida, Li, Bailey 2001, "accurate" DD
-// division): three quotient digits from the hi limbs, the remainder
-// recomputed in double-double after each.
-__device__ __forceinline__ dd::real dd_div(dd::real a, dd::real b)
-{
-    double q1 = __ddiv_rn(a.hi, b.hi);
-    dd::real r = dd::sub_exact(a, dd::mul_exact(dd::make(q1, 0.0), b));
-    double q2 = __ddiv_rn(r.hi, b.hi);
-    r = dd::sub_exact(r, dd::mul_exact(dd::make(q2, 0.0), b));
-    double q3 = __ddiv_rn(r.hi, b.hi);
-    dd::real q;
-    dd::fast_two_sum(q1, q2, q.hi, q.lo);
-    return dd::add_exact(q, dd::make(q3, 0.0));
-}
+__device__ __forceinline__ dd::real dd_div(dd::real a, dd::real b) { return dd::div(a, b); }
 
 // op(A)(i, j) for a column-major A with optional transpose.
 __device__ __forceinline__ dd::real opA(const double2 *A, int64_t lda, bool trans, int64_t i, int64_t j)

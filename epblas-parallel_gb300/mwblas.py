@@ -91,6 +91,18 @@ class MWBlas:
             self._sig("msyrk" + suf, None, [_ch, _ch, PI, PI, R, _p, PI, R, _p, PI])
             self._sig("wherk" + suf, None, [_ch, _ch, PI, PI, R, _p, PI, R, _p, PI])
             self._sig("mtrsm" + suf, None, [_ch, _ch, _ch, _ch, PI, PI, R, _p, PI, _p, PI])
+            self._sig("mgemmtr" + suf, None, [_ch, _ch, _ch, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
+            self._sig("wgemmtr" + suf, None, [_ch, _ch, _ch, PI, PI, Cx, _p, PI, _p, PI, Cx, _p, PI])
+            self._sig("msymm" + suf, None, [_ch, _ch, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
+            self._sig("wsymm" + suf, None, [_ch, _ch, PI, PI, Cx, _p, PI, _p, PI, Cx, _p, PI])
+            self._sig("whemm" + suf, None, [_ch, _ch, PI, PI, Cx, _p, PI, _p, PI, Cx, _p, PI])
+            self._sig("msyr2k" + suf, None, [_ch, _ch, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
+            self._sig("wsyr2k" + suf, None, [_ch, _ch, PI, PI, Cx, _p, PI, _p, PI, Cx, _p, PI])
+            self._sig("wher2k" + suf, None, [_ch, _ch, PI, PI, Cx, _p, PI, _p, PI, R, _p, PI])
+            self._sig("wsyrk" + suf, None, [_ch, _ch, PI, PI, Cx, _p, PI, Cx, _p, PI])
+            self._sig("mtrmm" + suf, None, [_ch, _ch, _ch, _ch, PI, PI, R, _p, PI, _p, PI])
+            self._sig("wtrmm" + suf, None, [_ch, _ch, _ch, _ch, PI, PI, Cx, _p, PI, _p, PI])
+            self._sig("wtrsm" + suf, None, [_ch, _ch, _ch, _ch, PI, PI, Cx, _p, PI, _p, PI])
             self._sig("mgemv" + suf, None, [_ch, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
             self._sig("mdot" + suf, Real64x2, [PI, _p, PI, _p, PI])
             self._sig("maxpy" + suf, None, [PI, R, _p, PI, _p, PI])
@@ -184,6 +196,44 @@ class MWBlas:
         f = self.lib.mtrsm_64_ if wide else self.lib.mtrsm_
         f(side.encode(), uplo.encode(), transa.encode(), diag.encode(), I(m), I(n), C.byref(real(alpha)), _ptr(a),
           I(lda), _ptr(b), I(ldb))
+
+    def _scal(self, cplx_, v):
+        return C.byref(cplx(v)) if cplx_ else C.byref(real(v))
+
+    def gemmtr(self, uplo, ta, tb, n, k, alpha, a, lda, b, ldb, beta, c, ldc, cplx_=False, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = getattr(self.lib, ("wgemmtr" if cplx_ else "mgemmtr") + ("_64_" if wide else "_"))
+        f(uplo.encode(), ta.encode(), tb.encode(), I(n), I(k), self._scal(cplx_, alpha), _ptr(a), I(lda), _ptr(b),
+          I(ldb), self._scal(cplx_, beta), _ptr(c), I(ldc))
+
+    def symm(self, name, side, uplo, m, n, alpha, a, lda, b, ldb, beta, c, ldc, wide=True):
+        """name in msymm, wsymm, whemm."""
+        I = lambda v: self._I(v, wide)
+        cp = name != "msymm"
+        getattr(self.lib, name + ("_64_" if wide else "_"))(
+            side.encode(), uplo.encode(), I(m), I(n), self._scal(cp, alpha), _ptr(a), I(lda), _ptr(b), I(ldb),
+            self._scal(cp, beta), _ptr(c), I(ldc))
+
+    def syr2k(self, name, uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc, wide=True):
+        """name in msyr2k, wsyr2k, wher2k (real beta)."""
+        I = lambda v: self._I(v, wide)
+        cp = name != "msyr2k"
+        getattr(self.lib, name + ("_64_" if wide else "_"))(
+            uplo.encode(), trans.encode(), I(n), I(k), self._scal(cp, alpha), _ptr(a), I(lda), _ptr(b), I(ldb),
+            self._scal(name == "wsyr2k", beta), _ptr(c), I(ldc))
+
+    def wsyrk(self, uplo, trans, n, k, alpha, a, lda, beta, c, ldc, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = self.lib.wsyrk_64_ if wide else self.lib.wsyrk_
+        f(uplo.encode(), trans.encode(), I(n), I(k), C.byref(cplx(alpha)), _ptr(a), I(lda), C.byref(cplx(beta)),
+          _ptr(c), I(ldc))
+
+    def trxm(self, name, side, uplo, transa, diag, m, n, alpha, a, lda, b, ldb, wide=True):
+        """name in mtrmm, wtrmm, wtrsm."""
+        I = lambda v: self._I(v, wide)
+        getattr(self.lib, name + ("_64_" if wide else "_"))(
+            side.encode(), uplo.encode(), transa.encode(), diag.encode(), I(m), I(n),
+            self._scal(name != "mtrmm", alpha), _ptr(a), I(lda), _ptr(b), I(ldb))
 
     # ---- batched (extension) -----------------------------------------------------------
     @staticmethod

@@ -91,6 +91,108 @@ void wherk_64_(const char *uplo, const char *trans, const int64_t *n,
                const int64_t *lda, const MWBLAS_R *beta, MWBLAS_C *c,
                const int64_t *ldc);
 
+/* C := alpha*op(A)*op(B) + beta*C on the uplo triangle of the n x n C.
+ * Replaces mgemmtr_/mgemmtr_64_ and wgemmtr_/wgemmtr_64_
+ * (multifloats/mgemmtr_parallel.cpp:35-82, wgemmtr_parallel.cpp:40-85,
+ * facade epblas_facade.h:242-247). */
+void mgemmtr_(const char *uplo, const char *transa, const char *transb, const int *n, const int *k,
+              const MWBLAS_R *alpha, const MWBLAS_R *a, const int *lda, const MWBLAS_R *b, const int *ldb,
+              const MWBLAS_R *beta, MWBLAS_R *c, const int *ldc);
+void mgemmtr_64_(const char *uplo, const char *transa, const char *transb, const int64_t *n, const int64_t *k,
+                 const MWBLAS_R *alpha, const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *b,
+                 const int64_t *ldb, const MWBLAS_R *beta, MWBLAS_R *c, const int64_t *ldc);
+void wgemmtr_(const char *uplo, const char *transa, const char *transb, const int *n, const int *k,
+              const MWBLAS_C *alpha, const MWBLAS_C *a, const int *lda, const MWBLAS_C *b, const int *ldb,
+              const MWBLAS_C *beta, MWBLAS_C *c, const int *ldc);
+void wgemmtr_64_(const char *uplo, const char *transa, const char *transb, const int64_t *n, const int64_t *k,
+                 const MWBLAS_C *alpha, const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *b,
+                 const int64_t *ldb, const MWBLAS_C *beta, MWBLAS_C *c, const int64_t *ldc);
+
+/* C := alpha*A*B + beta*C (side='L') or alpha*B*A + beta*C (side='R'), A
+ * symmetric (msymm_, wsymm_) or Hermitian with a real diagonal (whemm_),
+ * read from its uplo triangle.  Replaces msymm_/wsymm_/whemm_ and the _64_
+ * twins (multifloats/msymm_parallel.cpp:37-104, wsymm_parallel.cpp:40-105,
+ * whemm_parallel.cpp:40-104, whemm_serial.cpp:11-12, facade
+ * epblas_facade.h:250-255). */
+void msymm_(const char *side, const char *uplo, const int *m, const int *n, const MWBLAS_R *alpha,
+            const MWBLAS_R *a, const int *lda, const MWBLAS_R *b, const int *ldb, const MWBLAS_R *beta,
+            MWBLAS_R *c, const int *ldc);
+void msymm_64_(const char *side, const char *uplo, const int64_t *m, const int64_t *n, const MWBLAS_R *alpha,
+               const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *b, const int64_t *ldb,
+               const MWBLAS_R *beta, MWBLAS_R *c, const int64_t *ldc);
+void wsymm_(const char *side, const char *uplo, const int *m, const int *n, const MWBLAS_C *alpha,
+            const MWBLAS_C *a, const int *lda, const MWBLAS_C *b, const int *ldb, const MWBLAS_C *beta,
+            MWBLAS_C *c, const int *ldc);
+void wsymm_64_(const char *side, const char *uplo, const int64_t *m, const int64_t *n, const MWBLAS_C *alpha,
+               const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *b, const int64_t *ldb,
+               const MWBLAS_C *beta, MWBLAS_C *c, const int64_t *ldc);
+void whemm_(const char *side, const char *uplo, const int *m, const int *n, const MWBLAS_C *alpha,
+            const MWBLAS_C *a, const int *lda, const MWBLAS_C *b, const int *ldb, const MWBLAS_C *beta,
+            MWBLAS_C *c, const int *ldc);
+void whemm_64_(const char *side, const char *uplo, const int64_t *m, const int64_t *n, const MWBLAS_C *alpha,
+               const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *b, const int64_t *ldb,
+               const MWBLAS_C *beta, MWBLAS_C *c, const int64_t *ldc);
+
+/* Rank-2k updates on the uplo triangle: C := alpha*A*B**T + alpha*B*A**T +
+ * beta*C (trans='N') or alpha*A**T*B + alpha*B**T*A + beta*C (msyr2k_,
+ * wsyr2k_); wher2k_ uses A**H, conj(alpha) on the second product, a real beta
+ * and keeps the diagonal real.  Replaces msyr2k_/wsyr2k_/wher2k_ and the
+ * _64_ twins (multifloats/msyr2k_parallel.cpp:38-85,
+ * wsyr2k_parallel.cpp:40-86, wher2k_parallel.cpp:40-91, facade
+ * epblas_facade.h:268-273). */
+void msyr2k_(const char *uplo, const char *trans, const int *n, const int *k, const MWBLAS_R *alpha,
+             const MWBLAS_R *a, const int *lda, const MWBLAS_R *b, const int *ldb, const MWBLAS_R *beta,
+             MWBLAS_R *c, const int *ldc);
+void msyr2k_64_(const char *uplo, const char *trans, const int64_t *n, const int64_t *k, const MWBLAS_R *alpha,
+                const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *b, const int64_t *ldb,
+                const MWBLAS_R *beta, MWBLAS_R *c, const int64_t *ldc);
+void wsyr2k_(const char *uplo, const char *trans, const int *n, const int *k, const MWBLAS_C *alpha,
+             const MWBLAS_C *a, const int *lda, const MWBLAS_C *b, const int *ldb, const MWBLAS_C *beta,
+             MWBLAS_C *c, const int *ldc);
+void wsyr2k_64_(const char *uplo, const char *trans, const int64_t *n, const int64_t *k, const MWBLAS_C *alpha,
+                const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *b, const int64_t *ldb,
+                const MWBLAS_C *beta, MWBLAS_C *c, const int64_t *ldc);
+void wher2k_(const char *uplo, const char *trans, const int *n, const int *k, const MWBLAS_C *alpha,
+             const MWBLAS_C *a, const int *lda, const MWBLAS_C *b, const int *ldb, const MWBLAS_R *beta,
+             MWBLAS_C *c, const int *ldc);
+void wher2k_64_(const char *uplo, const char *trans, const int64_t *n, const int64_t *k, const MWBLAS_C *alpha,
+                const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *b, const int64_t *ldb,
+                const MWBLAS_R *beta, MWBLAS_C *c, const int64_t *ldc);
+
+/* Complex symmetric (not Hermitian) rank-k update with complex alpha/beta:
+ * C := alpha*A*A**T + beta*C (trans='N') or alpha*A**T*A + beta*C, uplo
+ * triangle.  Replaces wsyrk_/wsyrk_64_ (multifloats/wsyrk_parallel.cpp:40-86,
+ * facade epblas_facade.h:259-265). */
+void wsyrk_(const char *uplo, const char *trans, const int *n, const int *k, const MWBLAS_C *alpha,
+            const MWBLAS_C *a, const int *lda, const MWBLAS_C *beta, MWBLAS_C *c, const int *ldc);
+void wsyrk_64_(const char *uplo, const char *trans, const int64_t *n, const int64_t *k, const MWBLAS_C *alpha,
+               const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *beta, MWBLAS_C *c, const int64_t *ldc);
+
+/* Triangular multiply B := alpha*op(A)*B (side='L') or alpha*B*op(A)
+ * (side='R'), B overwritten.  Replaces mtrmm_/wtrmm_ and the _64_ twins
+ * (multifloats/mtrmm_parallel.cpp:37-108, wtrmm_parallel.cpp:40-110, facade
+ * epblas_facade.h:276-282). */
+void mtrmm_(const char *side, const char *uplo, const char *transa, const char *diag, const int *m, const int *n,
+            const MWBLAS_R *alpha, const MWBLAS_R *a, const int *lda, MWBLAS_R *b, const int *ldb);
+void mtrmm_64_(const char *side, const char *uplo, const char *transa, const char *diag, const int64_t *m,
+               const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *a, const int64_t *lda, MWBLAS_R *b,
+               const int64_t *ldb);
+void wtrmm_(const char *side, const char *uplo, const char *transa, const char *diag, const int *m, const int *n,
+            const MWBLAS_C *alpha, const MWBLAS_C *a, const int *lda, MWBLAS_C *b, const int *ldb);
+void wtrmm_64_(const char *side, const char *uplo, const char *transa, const char *diag, const int64_t *m,
+               const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *a, const int64_t *lda, MWBLAS_C *b,
+               const int64_t *ldb);
+
+/* Complex triangular solve op(A)*X = alpha*B (side='L') or X*op(A) = alpha*B
+ * (side='R'), op in {N, T, C}; B is overwritten by X.  Replaces
+ * wtrsm_/wtrsm_64_ (multifloats/wtrsm_parallel.cpp:39-105, facade
+ * epblas_facade.h:276-282). */
+void wtrsm_(const char *side, const char *uplo, const char *transa, const char *diag, const int *m, const int *n,
+            const MWBLAS_C *alpha, const MWBLAS_C *a, const int *lda, MWBLAS_C *b, const int *ldb);
+void wtrsm_64_(const char *side, const char *uplo, const char *transa, const char *diag, const int64_t *m,
+               const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *a, const int64_t *lda, MWBLAS_C *b,
+               const int64_t *ldb);
+
 /* Triangular solve op(A)*X = alpha*B (side='L') or X*op(A) = alpha*B
  * (side='R'); B is overwritten by X.  Replaces mtrsm_/mtrsm_64_
  * (multifloats/mtrsm_parallel.cpp:36-105, facade epblas_facade.h:276-282). */
