@@ -433,7 +433,8 @@ def tc_traffic_from_profile():
 # ---------------------------------------------------------------------------
 
 WORKLOADS = ("gemm", "stress", "wgemm", "gemm_t", "gemm_fixed", "gemm_plain", "syrk", "herk", "trsm", "gemv", "dot",
-             "axpy", "scal", "copy", "swap", "iamax", "batched_gemm", "batched_trsm")
+             "axpy", "scal", "copy", "swap", "iamax", "batched_gemm", "batched_trsm", "gemmtr", "symm", "syr2k",
+             "trmm", "wtrsm")
 
 
 def _dev_dd(torch, shape, gen, dev, cplx_=False):
@@ -652,6 +653,133 @@ def run_workload(args):
             got = hb(B)[cols]
             check["normwise_err_sampled"] = orc.normwise_error(got, want, orc.dd_abs(al) * orc.dd_absmax(hb(B0)))
             check["columns_checked"] = len(cols)
+    elif w == "gemmtr":
+        n, k = 8192, 2048
+        A = _dev_dd(torch, (k, n), gen, dev)           # n x k
+        B = _dev_dd(torch, (n, k), gen, dev)           # k x n
+        C = _dev_dd(torch, (n, n), gen, dev)
+        C0 = C.clone()
+        fn = lambda: lib.gemmtr("U", "N", "N", n, k, al, A.data_ptr(), n, B.data_ptr(), k, be, C.data_ptr(), n)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: C.copy_(C0))
+        value, unit = n * (n + 1) * k / ms / 1e6, "DD-GFLOP/s"
+        metric = "DD-GEMMTR GFLOP/s n=8192 k=2048 upper (n(n+1)k flops)"
+        cfg = {"workload": "mgemmtr_ U N N n=8192 k=2048"}
+        if o:
+            C.copy_(C0)
+            fn()
+            i, j = rng.integers(0, n, 256), rng.integers(0, n, 256)
+            rows, cols = np.minimum(i, j), np.maximum(i, j)
+            hA, hB, hC0 = hb(A), hb(B), hb(C0)
+            want = o.qgemm("N", "N", n, n, k, al, hA, n, hB, k, be, hC0, n, rows=rows, cols=cols)
+            got = hb(C)[cols, rows]
+            op = orc.dd_abs(al) * k * orc.dd_absmax(hA) * orc.dd_absmax(hB) + orc.dd_abs(be) * orc.dd_absmax(hC0)
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+    elif w == "symm":
+        m = n = 8192
+        A = _dev_dd(torch, (m, m), gen, dev)           # symmetric, upper triangle used
+        B = _dev_dd(torch, (n, m), gen, dev)
+        C = _dev_dd(torch, (n, m), gen, dev)
+        C0 = C.clone()
+        fn = lambda: lib.symm("msymm", "L", "U", m, n, al, A.data_ptr(), m, B.data_ptr(), m, be, C.data_ptr(), m)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: C.copy_(C0))
+        value, unit = 2.0 * m * m * n / ms / 1e6, "DD-GFLOP/s"
+        metric = "DD-SYMM GFLOP/s m=n=8192 side L upper (2m^2n flops)"
+        cfg = {"workload": "msymm_ L U m=n=8192"}
+        if o:
+            C.copy_(C0)
+            fn()
+            hA = hb(A)
+            iu = np.triu_indices(m)   # array [col, row]: row <= col is the stored upper triangle
+            full = np.empty_like(hA)
+            full[iu[1], iu[0]] = hA[iu[1], iu[0]]
+            full[iu[0], iu[1]] = hA[iu[1], iu[0]]
+            rows, cols = rng.integers(0, m, 256), rng.integers(0, n, 256)
+            hB, hC0 = hb(B), hb(C0)
+            want = o.qgemm("N", "N", m, n, m, al, full, m, hB, m, be, hC0, m, rows=rows, cols=cols)
+            got = hb(C)[cols, rows]
+            op = orc.dd_abs(al) * m * orc.dd_absmax(hA) * orc.dd_absmax(hB) + orc.dd_abs(be) * orc.dd_absmax(hC0)
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+    elif w == "syr2k":
+        n, k = 8192, 2048
+        A = _dev_dd(torch, (k, n), gen, dev)
+        B = _dev_dd(torch, (k, n), gen, dev)
+        C = _dev_dd(torch, (n, n), gen, dev)
+        C0 = C.clone()
+        fn = lambda: lib.syr2k("msyr2k", "U", "N", n, k, al, A.data_ptr(), n, B.data_ptr(), n, be, C.data_ptr(), n)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: C.copy_(C0))
+        value, unit = 2.0 * n * (n + 1) * k / ms / 1e6, "DD-GFLOP/s"
+        metric = "DD-SYR2K GFLOP/s n=8192 k=2048 upper (2n(n+1)k flops)"
+        cfg = {"workload": "msyr2k_ U N n=8192 k=2048"}
+        if o:
+            C.copy_(C0)
+            fn()
+            i, j = rng.integers(0, n, 256), rng.integers(0, n, 256)
+            rows, cols = np.minimum(i, j), np.maximum(i, j)
+            hA, hB, hC0 = hb(A), hb(B), hb(C0)
+            # both products in one binary128 sum: [A B] [B A]^T
+            AB = np.ascontiguousarray(np.concatenate([hA, hB], axis=0))
+            BA = np.ascontiguousarray(np.concatenate([hB, hA], axis=0))
+            want = o.qgemm("N", "T", n, n, 2 * k, al, AB, n, BA, n, be, hC0, n, rows=rows, cols=cols)
+            got = hb(C)[cols, rows]
+            op = 2 * orc.dd_abs(al) * k * orc.dd_absmax(hA) * orc.dd_absmax(hB) + orc.dd_abs(be) * orc.dd_absmax(hC0)
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+    elif w == "trmm":
+        m, n = 8192, 4096
+        A = _dev_dd(torch, (m, m), gen, dev)           # upper triangle used, non-unit
+        B = _dev_dd(torch, (n, m), gen, dev)
+        B0 = B.clone()
+        fn = lambda: lib.trxm("mtrmm", "L", "U", "N", "N", m, n, al, A.data_ptr(), m, B.data_ptr(), m)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: B.copy_(B0))
+        value, unit = float(m) * m * n / ms / 1e6, "DD-GFLOP/s"
+        metric = "DD-TRMM GFLOP/s m=8192 n=4096 LUNN (m^2 n flops)"
+        cfg = {"workload": "mtrmm_ L U N N m=8192 n=4096"}
+        if o:
+            B.copy_(B0)
+            fn()
+            hA = hb(A)
+            tri = np.zeros_like(hA)
+            iu = np.triu_indices(m)
+            tri[iu[1], iu[0]] = hA[iu[1], iu[0]]
+            rows, cols = rng.integers(0, m, 256), rng.integers(0, n, 256)
+            hB0 = hb(B0)
+            want = o.qgemm("N", "N", m, n, m, al, tri, m, hB0, m, np.zeros(2), np.zeros_like(hB0), m,
+                           rows=rows, cols=cols)
+            got = hb(B)[cols, rows]
+            op = orc.dd_abs(al) * m * orc.dd_absmax(hA) * orc.dd_absmax(hB0)
+            check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+    elif w == "wtrsm":
+        m, nr = (args.size or 4096), 1024
+        A = _dev_dd(torch, (m, m), gen, dev, cplx_=True) / m
+        d = torch.arange(m, device=dev)
+        A[d, d, 0, 0] = 1 + torch.rand(m, generator=gen, device=dev, dtype=torch.float64)
+        A[d, d, 0, 1] = 0.0
+        B = _dev_dd(torch, (nr, m), gen, dev, cplx_=True)
+        B0 = B.clone()
+        ca = np.array([al, [0.5, 0.0]])
+        fn = lambda: lib.trxm("wtrsm", "L", "L", "N", "N", m, nr, ca, A.data_ptr(), m, B.data_ptr(), m)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: B.copy_(B0))
+        value, unit = 4.0 * m * m * nr / ms / 1e6, "DD-GFLOP/s"
+        metric = f"complex DD-TRSM GFLOP/s LLNN m={m} nrhs=1024 (4 m^2 nrhs real flops)"
+        cfg = {"workload": f"wtrsm_ L L N N m={m} n=1024, diag U[1,2), off-diagonal U[-1,1)/m"}
+        if o:
+            B.copy_(B0)
+            fn()
+            # residual op(A) X - alpha B at 256 sampled entries, in binary128
+            hA, X, hB0 = hb(A), hb(B), hb(B0)
+            tri = np.zeros_like(hA)
+            il = np.tril_indices(m)
+            tri[il[1], il[0]] = hA[il[1], il[0]]
+            rows, cols = rng.integers(0, m, 256), rng.integers(0, nr, 256)
+            one, zero = np.array([[1.0, 0.0], [0.0, 0.0]]), np.zeros((2, 2))
+            AX = o.qwgemm("N", "N", m, nr, m, one, tri, m, X, m, zero, np.zeros_like(X), m, rows=rows, cols=cols)
+            # alpha * B0 at the same entries: a k = 1 product with a 1 x 1 one
+            eye1 = np.ascontiguousarray(one.reshape(1, 1, 2, 2))
+            rhs = np.stack([o.qwgemm("N", "N", m, 1, 1, ca, np.ascontiguousarray(hB0[c:c + 1]), m, eye1, 1, zero,
+                                     np.zeros((1, m, 2, 2)), m, rows=np.array([r]), cols=np.array([0]))[0]
+                            for r, c in zip(rows, cols)])
+            scale = m * orc.dd_absmax(tri) * orc.dd_absmax(X) + orc.dd_abs(ca) * orc.dd_absmax(hB0)
+            check["normwise_residual_sampled"] = orc.normwise_error(AX, rhs, scale)
+            check["entries_checked"] = 256
     elif w == "gemv":
         m = n = args.size or 16384
         A = _dev_dd(torch, (n, m), gen, dev)

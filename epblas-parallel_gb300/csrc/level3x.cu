@@ -126,39 +126,56 @@ __device__ __forceinline__ dd::cplx opAc(const double2 *A, int64_t lda, bool tra
     return v;
 }
 
-// Complex left solve of op(A)[r0:r0+nb, r0:r0+nb] * X = B[r0:r0+nb, :] in place,
-// thread per right-hand-side column. lower: op(A) lower triangular (forward).
-// The diagonal divisor is applied as conj(d) / |d|^2 (a DD division of the
-// squared modulus).
+__device__ __forceinline__ dd::cplx cshfl_down(const dd::cplx &v, int off)
+{
+    dd::cplx r;
+    r.re.hi = __shfl_down_sync(0xffffffffu, v.re.hi, off);
+    r.re.lo = __shfl_down_sync(0xffffffffu, v.re.lo, off);
+    r.im.hi = __shfl_down_sync(0xffffffffu, v.im.hi, off);
+    r.im.lo = __shfl_down_sync(0xffffffffu, v.im.lo, off);
+    return r;
+}
+
+// Complex left solve of op(A)[r0:r0+nb, r0:r0+nb] * X = B[r0:r0+nb, :] in place
+// (nb <= 32), a warp per right-hand-side column with lane l holding row l.
+// Row i is finished by lane i after a warp reduction of the solved lanes'
+// products; lower: op(A) lower triangular (forward order). The diagonal
+// divisor is applied as conj(d) / |d|^2 (a DD division of the squared
+// modulus).
 __global__ void k_ctrsm_diag(int64_t r0, int nb, int64_t ncols, const double2 *__restrict__ A, int64_t lda,
                              bool trans, bool conj, bool lower, bool unit, double2 *__restrict__ B, int64_t ldb)
 {
-    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (j >= ncols) return;
+    const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (j >= ncols) return;   // whole warps leave together
     double2 *b = B + 2 * (r0 + j * ldb);
+    const dd::real z = dd::make(0.0, 0.0);
+    dd::cplx x = lane < nb ? dd::cload(b + 2 * lane) : dd::cplx{z, z};
     for (int s = 0; s < nb; ++s) {
         const int i = lower ? s : nb - 1 - s;
-        dd::cplx acc = dd::cload(b + 2 * i);
-        if (lower) {
-            for (int q = 0; q < i; ++q) {
-                const dd::cplx a = opAc(A, lda, trans, conj, r0 + i, r0 + q);
-                acc = dd::cadd_exact(acc, dd::cmul_exact(dd::cplx{dd::neg(a.re), dd::neg(a.im)}, dd::cload(b + 2 * q)));
+        const bool solved = lower ? (lane < i) : (lane > i && lane < nb);
+        dd::cplx t{z, z};
+        if (solved) t = dd::cmul_exact(opAc(A, lda, trans, conj, r0 + i, r0 + lane), x);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) t = dd::cadd_exact(t, cshfl_down(t, off));
+        dd::cplx tot;
+        tot.re.hi = __shfl_sync(0xffffffffu, t.re.hi, 0);
+        tot.re.lo = __shfl_sync(0xffffffffu, t.re.lo, 0);
+        tot.im.hi = __shfl_sync(0xffffffffu, t.im.hi, 0);
+        tot.im.lo = __shfl_sync(0xffffffffu, t.im.lo, 0);
+        if (lane == i) {
+            dd::cplx acc = dd::cadd_exact(x, dd::cplx{dd::neg(tot.re), dd::neg(tot.im)});
+            if (!unit) {
+                const dd::cplx d = opAc(A, lda, trans, conj, r0 + i, r0 + i);
+                const dd::real m2 = dd::add_exact(dd::mul_exact(d.re, d.re), dd::mul_exact(d.im, d.im));
+                const dd::real inv = dd::div(dd::make(1.0, 0.0), m2);
+                const dd::cplx dc{dd::mul_exact(d.re, inv), dd::neg(dd::mul_exact(d.im, inv))};
+                acc = dd::cmul_exact(acc, dc);
             }
-        } else {
-            for (int q = i + 1; q < nb; ++q) {
-                const dd::cplx a = opAc(A, lda, trans, conj, r0 + i, r0 + q);
-                acc = dd::cadd_exact(acc, dd::cmul_exact(dd::cplx{dd::neg(a.re), dd::neg(a.im)}, dd::cload(b + 2 * q)));
-            }
+            x = acc;
         }
-        if (!unit) {
-            const dd::cplx d = opAc(A, lda, trans, conj, r0 + i, r0 + i);
-            const dd::real m2 = dd::add_exact(dd::mul_exact(d.re, d.re), dd::mul_exact(d.im, d.im));
-            const dd::real inv = dd::div(dd::make(1.0, 0.0), m2);
-            const dd::cplx dc{dd::mul_exact(d.re, inv), dd::neg(dd::mul_exact(d.im, inv))};
-            acc = dd::cmul_exact(acc, dc);
-        }
-        dd::cstore(b + 2 * i, acc);
     }
+    if (lane < nb) dd::cstore(b + 2 * lane, x);
 }
 
 // Scratch allocation released on scope exit.
@@ -176,8 +193,8 @@ bool ctrsm_left_rec(int64_t r0, int64_t n, int64_t nrhs, const double2 *A, int64
                     bool lower, bool unit, double2 *B, int64_t ldb, const char *routine)
 {
     if (n <= kCtrsmLeaf) {
-        k_ctrsm_diag<<<blocks_for(nrhs), kThreads, 0, stream()>>>(r0, (int)n, nrhs, A, lda, trans, conj, lower,
-                                                                   unit, B, ldb);
+        const unsigned nbk = (unsigned)((nrhs * 32 + kThreads - 1) / kThreads);
+        k_ctrsm_diag<<<nbk, kThreads, 0, stream()>>>(r0, (int)n, nrhs, A, lda, trans, conj, lower, unit, B, ldb);
         count_launch();
         return true;
     }
