@@ -13,6 +13,7 @@
 
 #include "gemm.h"
 #include "l1.h"
+#include "l1x.h"
 #include "level3.h"
 #include "level3x.h"
 #include "runtime.h"
@@ -724,6 +725,124 @@ void trxm_entry(const char *routine, bool cplx, bool solve, const char *side, co
     finish(routine);
 }
 
+// ---- wdotu / wdotc / masum / mwasum / mnrm2 / mwnrm2 -------------------------------------
+
+// mode as launch_reduce; returns (re, im) (im zero for the real results).
+template <typename INT>
+void reduce_entry(const char *routine, int mode, const INT *n, const void *x, const INT *incx, const void *y,
+                  const INT *incy, double2 out[2])
+{
+    Scope sc(routine);
+    out[0] = make_double2(0.0, 0.0);
+    out[1] = make_double2(0.0, 0.0);
+    const bool dot = mode <= 1;
+    if (!n || !incx || (dot && !incy)) { set_error(routine, 1, "null argument pointer"); return; }
+    int64_t N = *n, ix = *incx, iy = dot ? *incy : 0;
+    if (N <= 0) return;                 // wdotc.cpp:127, masum.cpp:119
+    if (!dot && ix < 1) return;         // masum.cpp:119, mnrm2.cpp:182
+    if (!x || (dot && !y)) { set_error(routine, 2, "null vector"); return; }
+    const size_t es = (mode == 2 || mode == 4) ? 16 : 32;
+    if (mode == 4 && N == 1) {
+        // mnrm2.cpp:183: |x(1)| exactly
+        const mwblas_real64x2 *p = (const mwblas_real64x2 *)x;
+        mwblas_real64x2 v;
+        if (!ensure_device(routine)) return;
+        if (is_device_pointer(x)) {
+            if (!cuda_ok(cudaMemcpy(&v, p, 16, cudaMemcpyDefault), routine, "read x(1)")) return;
+        } else {
+            v = *p;
+        }
+        const bool neg = v.limbs[0] < 0.0 || (v.limbs[0] == 0.0 && v.limbs[1] < 0.0);
+        out[0] = neg ? make_double2(-v.limbs[0], -v.limbs[1]) : make_double2(v.limbs[0], v.limbs[1]);
+        return;
+    }
+    if (!ensure_device(routine)) return;
+    Staged SX, SY;
+    sc.add(SX); sc.add(SY);
+    int64_t dix, diy = 0;
+    if (!stage_vector(SX, x, N, ix, es, true, dix, routine)) return;
+    if (dot && !stage_vector(SY, y, N, iy, es, true, diy, routine)) return;
+    if (!launch_reduce(mode, N, SX.dev, dix, dot ? SY.dev : nullptr, diy, out, routine)) return;
+}
+
+// ---- waxpy (waxpy.cpp:101) --------------------------------------------------------------
+
+template <typename INT>
+void waxpy_entry(const INT *n, const mwblas_complex64x2 *alpha, const void *x, const INT *incx, void *y,
+                 const INT *incy)
+{
+    const char *routine = "waxpy";
+    Scope sc(routine);
+    if (!n || !alpha || !incx || !incy) { set_error(routine, 1, "null argument pointer"); return; }
+    int64_t N = *n;
+    const cdd_host a = cd(alpha);
+    if (N <= 0 || ceq0(a)) return;
+    if (!x || !y) { set_error(routine, 3, "null vector"); return; }
+    if (!ensure_device(routine)) return;
+    Staged SX, SY;
+    sc.add(SX); sc.add(SY);
+    int64_t dix, diy;
+    if (!stage_vector(SX, x, N, *incx, 32, true, dix, routine)) return;
+    if (!stage_vector(SY, y, N, *incy, 32, true, diy, routine)) return;
+    launch_waxpy(N, a, SX.dev, dix, SY.dev, diy);
+    if (!unstage_vector(SY, routine)) return;
+    finish(routine);
+}
+
+// ---- mrot / wmrot / mrotm (mrot.cpp:106, mrotm.cpp:200) ---------------------------------
+
+template <typename INT>
+void rot_entry(const char *routine, int e2, const INT *n, void *x, const INT *incx, void *y, const INT *incy,
+               const dd_host h[4])
+{
+    Scope sc(routine);
+    int64_t N = *n;
+    if (N <= 0) return;
+    if (!x || !y) { set_error(routine, 2, "null vector"); return; }
+    if (!ensure_device(routine)) return;
+    Staged SX, SY;
+    sc.add(SX); sc.add(SY);
+    int64_t dix, diy;
+    if (!stage_vector(SX, x, N, *incx, 16 * e2, true, dix, routine)) return;
+    if (!stage_vector(SY, y, N, *incy, 16 * e2, true, diy, routine)) return;
+    launch_rot(N, SX.dev, dix, SY.dev, diy, e2, h);
+    if (!unstage_vector(SX, routine)) return;
+    if (!unstage_vector(SY, routine)) return;
+    finish(routine);
+}
+
+template <typename INT>
+void rotcs_entry(const char *routine, int e2, const INT *n, void *x, const INT *incx, void *y, const INT *incy,
+                 const mwblas_real64x2 *c, const mwblas_real64x2 *s)
+{
+    if (!n || !incx || !incy || !c || !s) { set_error(routine, 1, "null argument pointer"); return; }
+    const dd_host cc = rd(c), ss = rd(s);
+    const dd_host h[4] = {cc, ss, {-ss.hi, -ss.lo}, cc};
+    rot_entry(routine, e2, n, x, incx, y, incy, h);
+}
+
+template <typename INT>
+void rotm_entry(const INT *n, void *x, const INT *incx, void *y, const INT *incy, const mwblas_real64x2 *param)
+{
+    const char *routine = "mrotm";
+    if (!n || !incx || !incy || !param) { set_error(routine, 1, "null argument pointer"); return; }
+    const dd_host flag = rd(param);
+    // mrotm.cpp:200: flag == -2 is the identity; otherwise H from dparam(2:5)
+    // = (h11, h21, h12, h22) with the implied entries of flags 0 and 1
+    if (flag.hi == -2.0 && flag.lo == 0.0) return;
+    const dd_host one{1.0, 0.0}, mone{-1.0, 0.0};
+    dd_host h11 = rd(param + 1), h21 = rd(param + 2), h12 = rd(param + 3), h22 = rd(param + 4);
+    if (flag.hi == 0.0 && flag.lo == 0.0) {
+        h11 = one;
+        h22 = one;
+    } else if (flag.hi == 1.0 && flag.lo == 0.0) {
+        h12 = one;
+        h21 = mone;
+    }
+    const dd_host h[4] = {h11, h12, h21, h22};
+    rot_entry(routine, 1, n, x, incx, y, incy, h);
+}
+
 }  // namespace
 }  // namespace mw
 
@@ -854,6 +973,76 @@ MW_TRXM_PAIR(mtrmm, TR, false, false)
 MW_TRXM_PAIR(wtrmm, TC, true, false)
 MW_TRXM_PAIR(wtrsm, TC, true, true)
 #undef MW_TRXM_PAIR
+
+// ---- further level 1 -----------------------------------------------------------------------
+
+#define MW_CDOT_PAIR(NAME, MODE)                                                                                \
+    TC NAME##_(const int *n, const TC *x, const int *incx, const TC *y, const int *incy)                       \
+    {                                                                                                          \
+        double2 o[2];                                                                                          \
+        mw::reduce_entry<int>(#NAME, MODE, n, x, incx, y, incy, o);                                            \
+        return TC{{{o[0].x, o[0].y}}, {{o[1].x, o[1].y}}};                                                     \
+    }                                                                                                          \
+    TC NAME##_64_(const int64_t *n, const TC *x, const int64_t *incx, const TC *y, const int64_t *incy)        \
+    {                                                                                                          \
+        double2 o[2];                                                                                          \
+        mw::reduce_entry<int64_t>(#NAME, MODE, n, x, incx, y, incy, o);                                        \
+        return TC{{{o[0].x, o[0].y}}, {{o[1].x, o[1].y}}};                                                     \
+    }
+MW_CDOT_PAIR(wdotu, 0)
+MW_CDOT_PAIR(wdotc, 1)
+#undef MW_CDOT_PAIR
+
+#define MW_ASUM_PAIR(NAME, VT, MODE)                                                                           \
+    TR NAME##_(const int *n, const VT *x, const int *incx)                                                    \
+    {                                                                                                          \
+        double2 o[2];                                                                                          \
+        mw::reduce_entry<int>(#NAME, MODE, n, x, incx, (const VT *)nullptr, (const int *)nullptr, o);          \
+        return TR{{o[0].x, o[0].y}};                                                                           \
+    }                                                                                                          \
+    TR NAME##_64_(const int64_t *n, const VT *x, const int64_t *incx)                                         \
+    {                                                                                                          \
+        double2 o[2];                                                                                          \
+        mw::reduce_entry<int64_t>(#NAME, MODE, n, x, incx, (const VT *)nullptr, (const int64_t *)nullptr, o);  \
+        return TR{{o[0].x, o[0].y}};                                                                           \
+    }
+MW_ASUM_PAIR(masum, TR, 2)
+MW_ASUM_PAIR(mwasum, TC, 3)
+MW_ASUM_PAIR(mnrm2, TR, 4)
+MW_ASUM_PAIR(mwnrm2, TC, 5)
+#undef MW_ASUM_PAIR
+
+void waxpy_(const int *n, const TC *alpha, const TC *x, const int *incx, TC *y, const int *incy)
+{
+    mw::waxpy_entry<int>(n, alpha, x, incx, y, incy);
+}
+void waxpy_64_(const int64_t *n, const TC *alpha, const TC *x, const int64_t *incx, TC *y, const int64_t *incy)
+{
+    mw::waxpy_entry<int64_t>(n, alpha, x, incx, y, incy);
+}
+
+#define MW_ROT_PAIR(NAME, VT, E2)                                                                               \
+    void NAME##_(const int *n, VT *x, const int *incx, VT *y, const int *incy, const TR *c, const TR *s)        \
+    {                                                                                                          \
+        mw::rotcs_entry<int>(#NAME, E2, n, x, incx, y, incy, c, s);                                            \
+    }                                                                                                          \
+    void NAME##_64_(const int64_t *n, VT *x, const int64_t *incx, VT *y, const int64_t *incy, const TR *c,     \
+                    const TR *s)                                                                               \
+    {                                                                                                          \
+        mw::rotcs_entry<int64_t>(#NAME, E2, n, x, incx, y, incy, c, s);                                        \
+    }
+MW_ROT_PAIR(mrot, TR, 1)
+MW_ROT_PAIR(wmrot, TC, 2)
+#undef MW_ROT_PAIR
+
+void mrotm_(const int *n, TR *x, const int *incx, TR *y, const int *incy, const TR *dparam)
+{
+    mw::rotm_entry<int>(n, x, incx, y, incy, dparam);
+}
+void mrotm_64_(const int64_t *n, TR *x, const int64_t *incx, TR *y, const int64_t *incy, const TR *dparam)
+{
+    mw::rotm_entry<int64_t>(n, x, incx, y, incy, dparam);
+}
 
 // ---- level 2 -----------------------------------------------------------------------------
 

@@ -103,6 +103,14 @@ class MWBlas:
             self._sig("mtrmm" + suf, None, [_ch, _ch, _ch, _ch, PI, PI, R, _p, PI, _p, PI])
             self._sig("wtrmm" + suf, None, [_ch, _ch, _ch, _ch, PI, PI, Cx, _p, PI, _p, PI])
             self._sig("wtrsm" + suf, None, [_ch, _ch, _ch, _ch, PI, PI, Cx, _p, PI, _p, PI])
+            self._sig("wdotu" + suf, Complex64x2, [PI, _p, PI, _p, PI])
+            self._sig("wdotc" + suf, Complex64x2, [PI, _p, PI, _p, PI])
+            for nm in ("masum", "mwasum", "mnrm2", "mwnrm2"):
+                self._sig(nm + suf, Real64x2, [PI, _p, PI])
+            self._sig("waxpy" + suf, None, [PI, Cx, _p, PI, _p, PI])
+            self._sig("mrot" + suf, None, [PI, _p, PI, _p, PI, R, R])
+            self._sig("wmrot" + suf, None, [PI, _p, PI, _p, PI, R, R])
+            self._sig("mrotm" + suf, None, [PI, _p, PI, _p, PI, _p])
             self._sig("mgemv" + suf, None, [_ch, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
             self._sig("mdot" + suf, Real64x2, [PI, _p, PI, _p, PI])
             self._sig("maxpy" + suf, None, [PI, R, _p, PI, _p, PI])
@@ -234,6 +242,34 @@ class MWBlas:
         getattr(self.lib, name + ("_64_" if wide else "_"))(
             side.encode(), uplo.encode(), transa.encode(), diag.encode(), I(m), I(n),
             self._scal(name != "mtrmm", alpha), _ptr(a), I(lda), _ptr(b), I(ldb))
+
+    def cdot(self, name, n, x, incx, y, incy, wide=True):
+        """wdotu / wdotc -> numpy (2, 2) [re, im] double-doubles."""
+        I = lambda v: self._I(v, wide)
+        r = getattr(self.lib, name + ("_64_" if wide else "_"))(I(n), _ptr(x), I(incx), _ptr(y), I(incy))
+        return np.array([[r.re.limbs[0], r.re.limbs[1]], [r.im.limbs[0], r.im.limbs[1]]])
+
+    def vnorm(self, name, n, x, incx, wide=True):
+        """masum / mwasum / mnrm2 / mwnrm2 -> numpy (2,) double-double."""
+        I = lambda v: self._I(v, wide)
+        r = getattr(self.lib, name + ("_64_" if wide else "_"))(I(n), _ptr(x), I(incx))
+        return np.array([r.limbs[0], r.limbs[1]])
+
+    def waxpy(self, n, alpha, x, incx, y, incy, wide=True):
+        I = lambda v: self._I(v, wide)
+        f = self.lib.waxpy_64_ if wide else self.lib.waxpy_
+        f(I(n), C.byref(cplx(alpha)), _ptr(x), I(incx), _ptr(y), I(incy))
+
+    def rot(self, name, n, x, incx, y, incy, c, s, wide=True):
+        """mrot / wmrot."""
+        I = lambda v: self._I(v, wide)
+        getattr(self.lib, name + ("_64_" if wide else "_"))(I(n), _ptr(x), I(incx), _ptr(y), I(incy),
+                                                             C.byref(real(c)), C.byref(real(s)))
+
+    def rotm(self, n, x, incx, y, incy, param, wide=True):
+        I = lambda v: self._I(v, wide)
+        p = np.ascontiguousarray(np.asarray(param, dtype=np.float64).reshape(5, 2))
+        (self.lib.mrotm_64_ if wide else self.lib.mrotm_)(I(n), _ptr(x), I(incx), _ptr(y), I(incy), _ptr(p))
 
     # ---- batched (extension) -----------------------------------------------------------
     @staticmethod

@@ -218,6 +218,54 @@ void mgemv_64_(const char *trans, const int64_t *m, const int64_t *n,
 
 /* ======================= Level 1 ======================================= */
 
+/* Complex dots sum x(i)*y(i) (wdotu_) and sum conj(x(i))*y(i) (wdotc_), the
+ * complex result returned by value.  Replaces wdotu_/wdotc_ and the _64_
+ * twins (multifloats/wdotu.cpp:121-140, wdotc.cpp:121-140, facade
+ * epblas_facade.h:102-107). */
+MWBLAS_C wdotu_(const int *n, const MWBLAS_C *x, const int *incx, const MWBLAS_C *y, const int *incy);
+MWBLAS_C wdotu_64_(const int64_t *n, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *y,
+                   const int64_t *incy);
+MWBLAS_C wdotc_(const int *n, const MWBLAS_C *x, const int *incx, const MWBLAS_C *y, const int *incy);
+MWBLAS_C wdotc_64_(const int64_t *n, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *y,
+                   const int64_t *incy);
+
+/* sum |x(i)| (masum_), sum |Re x(i)| + |Im x(i)| (mwasum_), and the Euclidean
+ * norms (mnrm2_, mwnrm2_); 0 for n < 1 or incx < 1.  Replaces masum_,
+ * mwasum_, mnrm2_, mwnrm2_ and the _64_ twins (multifloats/masum.cpp:115-127,
+ * mwasum.cpp:116-128, mnrm2.cpp:178-195, mwnrm2.cpp:176-192, facade
+ * epblas_facade.h:76-79). */
+MWBLAS_R masum_(const int *n, const MWBLAS_R *x, const int *incx);
+MWBLAS_R masum_64_(const int64_t *n, const MWBLAS_R *x, const int64_t *incx);
+MWBLAS_R mwasum_(const int *n, const MWBLAS_C *x, const int *incx);
+MWBLAS_R mwasum_64_(const int64_t *n, const MWBLAS_C *x, const int64_t *incx);
+MWBLAS_R mnrm2_(const int *n, const MWBLAS_R *x, const int *incx);
+MWBLAS_R mnrm2_64_(const int64_t *n, const MWBLAS_R *x, const int64_t *incx);
+MWBLAS_R mwnrm2_(const int *n, const MWBLAS_C *x, const int *incx);
+MWBLAS_R mwnrm2_64_(const int64_t *n, const MWBLAS_C *x, const int64_t *incx);
+
+/* y := alpha*x + y, complex.  Replaces waxpy_/waxpy_64_
+ * (multifloats/waxpy.cpp:97-110, facade epblas_facade.h:81-86). */
+void waxpy_(const int *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int *incx, MWBLAS_C *y, const int *incy);
+void waxpy_64_(const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int64_t *incx, MWBLAS_C *y,
+               const int64_t *incy);
+
+/* Plane rotation (x, y) := (c*x + s*y, c*y - s*x) with real c, s, for real
+ * (mrot_) and complex (wmrot_) vectors; mrotm_ applies the modified-Givens
+ * matrix of dparam (flag, h11, h21, h12, h22).  Replaces mrot_, wmrot_,
+ * mrotm_ and the _64_ twins (multifloats/mrot.cpp:102-115,
+ * wmrot.cpp:119-132, mrotm.cpp:196-215, facade epblas_facade.h:109-121). */
+void mrot_(const int *n, MWBLAS_R *x, const int *incx, MWBLAS_R *y, const int *incy, const MWBLAS_R *c,
+           const MWBLAS_R *s);
+void mrot_64_(const int64_t *n, MWBLAS_R *x, const int64_t *incx, MWBLAS_R *y, const int64_t *incy,
+              const MWBLAS_R *c, const MWBLAS_R *s);
+void wmrot_(const int *n, MWBLAS_C *x, const int *incx, MWBLAS_C *y, const int *incy, const MWBLAS_R *c,
+            const MWBLAS_R *s);
+void wmrot_64_(const int64_t *n, MWBLAS_C *x, const int64_t *incx, MWBLAS_C *y, const int64_t *incy,
+               const MWBLAS_R *c, const MWBLAS_R *s);
+void mrotm_(const int *n, MWBLAS_R *x, const int *incx, MWBLAS_R *y, const int *incy, const MWBLAS_R *dparam);
+void mrotm_64_(const int64_t *n, MWBLAS_R *x, const int64_t *incx, MWBLAS_R *y, const int64_t *incy,
+               const MWBLAS_R *dparam);
+
 /* sum x(i)*y(i).  Replaces mdot_/mdot_64_ (multifloats/mdot.cpp:127-148). */
 MWBLAS_R mdot_(const int *n, const MWBLAS_R *x, const int *incx, const MWBLAS_R *y,
                const int *incy);
