@@ -16,6 +16,7 @@
 #include "l1x.h"
 #include "level3.h"
 #include "level3x.h"
+#include "level2x.h"
 #include "runtime.h"
 
 namespace mw {
@@ -843,6 +844,323 @@ void rotm_entry(const INT *n, void *x, const INT *incx, void *y, const INT *incy
     rot_entry(routine, 1, n, x, incx, y, incy, h);
 }
 
+// ---- level 2 beyond real GEMV (gbmv, symv/hemv/sbmv/hbmv/spmv/hpmv, trmv/tbmv/tpmv,
+//      trsv/tbsv/tpsv, ger/geru/gerc, syr/her/spr/hpr, syr2/her2/spr2/hpr2) ------------
+// Matrix formats: 0 dense (lda), 1 band (ldab, k or kl/ku), 2 packed (n(n+1)/2).
+
+void set_scalars(bool cplx, const void *alpha, const void *beta, dd_host &a, dd_host &b, cdd_host &ca, cdd_host &cb,
+                 int &bk)
+{
+    if (cplx) {
+        ca = cd((const mwblas_complex64x2 *)alpha);
+        cb = beta ? cd((const mwblas_complex64x2 *)beta) : cdd_host{{0.0, 0.0}, {0.0, 0.0}};
+        bk = beta_kind(cb);
+    } else {
+        a = rd((const mwblas_real64x2 *)alpha);
+        b = beta ? rd((const mwblas_real64x2 *)beta) : dd_host{0.0, 0.0};
+        bk = beta_kind(b);
+    }
+}
+
+// GEMV (complex) and GBMV: y := alpha*op(A)*x + beta*y (mgbmv.cpp, wgemv.cpp)
+template <typename INT>
+void gemv2_entry(const char *routine, bool cplx, bool band, const char *trans, const INT *m, const INT *n,
+                 const INT *kl, const INT *ku, const void *alpha, const void *a, const INT *lda, const void *x,
+                 const INT *incx, const void *beta, void *y, const INT *incy)
+{
+    Scope sc(routine);
+    if (!trans || !m || !n || !alpha || !lda || !incx || !beta || !incy || (band && (!kl || !ku))) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char T = cplx ? up(trans) : trans_real(trans);
+    if (T != 'N' && T != 'T' && T != 'C') { set_error(routine, 1, "invalid trans"); return; }
+    int64_t M = *m, N = *n, KL = band ? *kl : 0, KU = band ? *ku : 0;
+    if (M < 0 || N < 0 || KL < 0 || KU < 0) { set_error(routine, 2, "negative size"); return; }
+    const int64_t ldmin = band ? KL + KU + 1 : (M > 1 ? M : 1);
+    if (*lda < ldmin) { set_error(routine, band ? 8 : 6, "lda too small"); return; }
+    if (*incx == 0 || *incy == 0) { set_error(routine, *incx == 0 ? 10 : 13, "zero increment"); return; }
+    if (M == 0 || N == 0) return;
+    MvArgs v;
+    v.cplx = cplx;
+    v.trans = T;
+    set_scalars(cplx, alpha, beta, v.alpha, v.beta, v.calpha, v.cbeta, v.beta_kind);
+    const bool alpha0 = is_zero(cplx, alpha);
+    if (alpha0 && v.beta_kind == 1) return;
+    if (!y || (!alpha0 && (!a || !x))) { set_error(routine, 3, "null array"); return; }
+    if (!ensure_device(routine)) return;
+    const int e2 = cplx ? 2 : 1;
+    const size_t es = 16 * (size_t)e2;
+    v.lenx = (T == 'N') ? N : M;
+    v.leny = (T == 'N') ? M : N;
+    Staged SA, SX, SY;
+    sc.add(SA); sc.add(SX); sc.add(SY);
+    int64_t dix = 1, diy;
+    if (!stage_vector(SY, y, v.leny, *incy, es, v.beta_kind != 0, diy, routine)) return;
+    void *dense = nullptr;
+    v.alpha_zero = alpha0;
+    if (!alpha0) {
+        if (!stage_vector(SX, x, v.lenx, *incx, es, true, dix, routine)) return;
+        if (!stage_matrix(SA, a, band ? (KL + KU + 1) : M, N, *lda, es, true, routine)) return;
+        if (band) {
+            dense = dev_alloc((size_t)M * N * es, routine);
+            if (!dense) return;
+            band_expand(M, N, KL, KU, SA.dev, *lda, e2, 0, false, false, dense);
+        }
+    }
+    v.A = band ? dense : SA.dev;
+    v.lda = band ? M : *lda;
+    v.x = SX.dev;
+    v.incx = dix;
+    v.y = SY.dev;
+    v.incy = diy;
+    const bool ok = mv_device(v, routine);
+    if (dense) dev_free(dense);
+    if (!ok) return;
+    if (!unstage_vector(SY, routine)) return;
+    finish(routine);
+}
+
+// SYMV/HEMV (dense), SBMV/HBMV (band, k), SPMV/HPMV (packed)
+template <typename INT>
+void symv_entry(const char *routine, bool cplx, bool herm, int fmt, const char *uplo, const INT *n, const INT *k,
+                const void *alpha, const void *a, const INT *lda, const void *x, const INT *incx, const void *beta,
+                void *y, const INT *incy)
+{
+    Scope sc(routine);
+    if (!uplo || !n || !alpha || !incx || !beta || !incy || (fmt != 2 && !lda) || (fmt == 1 && !k)) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char U = up(uplo);
+    if (U != 'U' && U != 'L') { set_error(routine, 1, "invalid uplo"); return; }
+    int64_t N = *n, K = fmt == 1 ? *k : 0;
+    if (N < 0 || K < 0) { set_error(routine, 2, "negative size"); return; }
+    if (fmt == 0 && *lda < (N > 1 ? N : 1)) { set_error(routine, 5, "lda too small"); return; }
+    if (fmt == 1 && *lda < K + 1) { set_error(routine, 6, "lda too small"); return; }
+    if (*incx == 0 || *incy == 0) { set_error(routine, 7, "zero increment"); return; }
+    if (N == 0) return;
+    MvArgs v;
+    v.cplx = cplx;
+    set_scalars(cplx, alpha, beta, v.alpha, v.beta, v.calpha, v.cbeta, v.beta_kind);
+    const bool alpha0 = is_zero(cplx, alpha);
+    if (alpha0 && v.beta_kind == 1) return;
+    if (!y || (!alpha0 && (!a || !x))) { set_error(routine, 3, "null array"); return; }
+    if (!ensure_device(routine)) return;
+    const int e2 = cplx ? 2 : 1;
+    const size_t es = 16 * (size_t)e2;
+    Staged SA, SX, SY;
+    sc.add(SA); sc.add(SX); sc.add(SY);
+    int64_t dix = 1, diy;
+    if (!stage_vector(SY, y, N, *incy, es, v.beta_kind != 0, diy, routine)) return;
+    if (alpha0) {
+        v.alpha_zero = true;
+        v.lenx = N;
+        v.leny = N;
+        v.y = SY.dev;
+        v.incy = diy;
+        if (!mv_device(v, routine)) return;
+    } else {
+        if (!stage_vector(SX, x, N, *incx, es, true, dix, routine)) return;
+        void *dense = nullptr;
+        if (fmt == 0) {
+            if (!stage_matrix(SA, a, N, N, *lda, es, true, routine)) return;
+        } else {
+            const int64_t len = fmt == 1 ? 0 : N * (N + 1) / 2;
+            if (fmt == 1) {
+                if (!stage_matrix(SA, a, K + 1, N, *lda, es, true, routine)) return;
+            } else {
+                if (!stage_matrix(SA, a, len, 1, len, es, true, routine)) return;
+            }
+            dense = dev_alloc((size_t)N * N * es, routine);
+            if (!dense) return;
+            if (fmt == 1) band_expand(N, N, U == 'L' ? K : 0, U == 'U' ? K : 0, SA.dev, *lda, e2, herm ? 2 : 1,
+                                      U == 'U', false, dense);
+            else pack_move(N, SA.dev, e2, U == 'U', dense, true);
+        }
+        v.shape = (fmt == 1) ? MV_GENERAL : (herm ? MV_HERMITIAN : MV_SYMMETRIC);
+        v.trans = 'N';
+        v.uplo = U;
+        v.lenx = N;
+        v.leny = N;
+        v.A = fmt == 0 ? SA.dev : dense;
+        v.lda = fmt == 0 ? *lda : N;
+        v.x = SX.dev;
+        v.incx = dix;
+        v.y = SY.dev;
+        v.incy = diy;
+        const bool ok = mv_device(v, routine);
+        if (dense) dev_free(dense);
+        if (!ok) return;
+    }
+    if (!unstage_vector(SY, routine)) return;
+    finish(routine);
+}
+
+// TRMV/TBMV/TPMV (solve=false), TRSV/TBSV/TPSV (solve=true)
+template <typename INT>
+void trv_entry(const char *routine, bool cplx, bool solve, int fmt, const char *uplo, const char *trans,
+               const char *diag, const INT *n, const INT *k, const void *a, const INT *lda, void *x, const INT *incx)
+{
+    Scope sc(routine);
+    if (!uplo || !trans || !diag || !n || !incx || (fmt != 2 && !lda) || (fmt == 1 && !k)) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char U = up(uplo), T = cplx ? up(trans) : trans_real(trans), D = up(diag);
+    if (U != 'U' && U != 'L') { set_error(routine, 1, "invalid uplo"); return; }
+    if (T != 'N' && T != 'T' && T != 'C') { set_error(routine, 2, "invalid trans"); return; }
+    if (D != 'U' && D != 'N') { set_error(routine, 3, "invalid diag"); return; }
+    int64_t N = *n, K = fmt == 1 ? *k : 0;
+    if (N < 0 || K < 0) { set_error(routine, 4, "negative size"); return; }
+    if (fmt == 0 && *lda < (N > 1 ? N : 1)) { set_error(routine, 6, "lda too small"); return; }
+    if (fmt == 1 && *lda < K + 1) { set_error(routine, 7, "lda too small"); return; }
+    if (*incx == 0) { set_error(routine, 8, "zero increment"); return; }
+    if (N == 0) return;
+    if (!a || !x) { set_error(routine, 5, "null array"); return; }
+    if (!ensure_device(routine)) return;
+    const int e2 = cplx ? 2 : 1;
+    const size_t es = 16 * (size_t)e2;
+    Staged SA, SX;
+    sc.add(SA); sc.add(SX);
+    int64_t dix;
+    if (!stage_vector(SX, x, N, *incx, es, true, dix, routine)) return;
+    void *dense = nullptr;
+    char Dd = D;
+    if (fmt == 0) {
+        if (!stage_matrix(SA, a, N, N, *lda, es, true, routine)) return;
+    } else {
+        const int64_t len = N * (N + 1) / 2;
+        if (fmt == 1) {
+            if (!stage_matrix(SA, a, K + 1, N, *lda, es, true, routine)) return;
+        } else {
+            if (!stage_matrix(SA, a, len, 1, len, es, true, routine)) return;
+        }
+        dense = dev_alloc((size_t)N * N * es, routine);
+        if (!dense) return;
+        if (fmt == 1) {
+            band_expand(N, N, U == 'L' ? K : 0, U == 'U' ? K : 0, SA.dev, *lda, e2, 3, U == 'U', D == 'U', dense);
+            Dd = 'N';   // the unit diagonal is in the dense copy
+        } else {
+            pack_move(N, SA.dev, e2, U == 'U', dense, true);
+        }
+    }
+    const bool ok = trv_device(cplx, solve, U, T, Dd, N, fmt == 0 ? SA.dev : dense, fmt == 0 ? *lda : N, SX.dev, dix,
+                               routine);
+    if (dense) dev_free(dense);
+    if (!ok) return;
+    if (!unstage_vector(SX, routine)) return;
+    finish(routine);
+}
+
+// GER / GERU / GERC: A := alpha*x*y^T (y^H for GERC) + A
+template <typename INT>
+void ger_entry(const char *routine, bool cplx, bool conj, const INT *m, const INT *n, const void *alpha, const void *x,
+               const INT *incx, const void *y, const INT *incy, void *a, const INT *lda)
+{
+    Scope sc(routine);
+    if (!m || !n || !alpha || !incx || !incy || !lda) { set_error(routine, 1, "null argument pointer"); return; }
+    int64_t M = *m, N = *n;
+    if (M < 0 || N < 0) { set_error(routine, 1, "negative size"); return; }
+    if (*incx == 0 || *incy == 0) { set_error(routine, 5, "zero increment"); return; }
+    if (*lda < (M > 1 ? M : 1)) { set_error(routine, 9, "lda too small"); return; }
+    if (M == 0 || N == 0 || is_zero(cplx, alpha)) return;
+    if (!a || !x || !y) { set_error(routine, 4, "null array"); return; }
+    if (!ensure_device(routine)) return;
+    const size_t es = cplx ? 32 : 16;
+    Staged SA, SX, SY;
+    sc.add(SA); sc.add(SX); sc.add(SY);
+    int64_t dix, diy;
+    if (!stage_vector(SX, x, M, *incx, es, true, dix, routine)) return;
+    if (!stage_vector(SY, y, N, *incy, es, true, diy, routine)) return;
+    if (!stage_matrix(SA, a, M, N, *lda, es, true, routine)) return;
+    RankArgs r;
+    r.cplx = cplx;
+    r.conj = conj;
+    r.uplo = 0;
+    r.m = M;
+    r.n = N;
+    r.x = SX.dev;
+    r.incx = dix;
+    r.y = SY.dev;
+    r.incy = diy;
+    r.A = SA.dev;
+    r.lda = *lda;
+    dd_host b;
+    cdd_host cb;
+    int bk;
+    set_scalars(cplx, alpha, nullptr, r.alpha, b, r.calpha, cb, bk);
+    if (!rank_update_device(r, routine)) return;
+    if (!unstage_matrix(SA, routine)) return;
+    finish(routine);
+}
+
+// SYR/HER (two=false) and SYR2/HER2 (two=true), dense or packed; HER/HPR take
+// a real alpha (the Hermitian forms keep the diagonal real).
+template <typename INT>
+void syr_entry(const char *routine, bool cplx, bool herm, bool packed, bool two, const char *uplo, const INT *n,
+               const void *alpha, const void *x, const INT *incx, const void *y, const INT *incy, void *a,
+               const INT *lda)
+{
+    Scope sc(routine);
+    if (!uplo || !n || !alpha || !incx || (two && !incy) || (!packed && !lda)) {
+        set_error(routine, 1, "null argument pointer");
+        return;
+    }
+    char U = up(uplo);
+    if (U != 'U' && U != 'L') { set_error(routine, 1, "invalid uplo"); return; }
+    int64_t N = *n;
+    if (N < 0) { set_error(routine, 2, "n < 0"); return; }
+    if (*incx == 0 || (two && *incy == 0)) { set_error(routine, 5, "zero increment"); return; }
+    if (!packed && *lda < (N > 1 ? N : 1)) { set_error(routine, two ? 9 : 7, "lda too small"); return; }
+    // real alpha for HER / HPR; complex for HER2 / HPR2
+    const bool alpha_real = !cplx || (herm && !two);
+    if (N == 0 || is_zero(!alpha_real, alpha)) return;
+    if (!a || !x || (two && !y)) { set_error(routine, 4, "null array"); return; }
+    if (!ensure_device(routine)) return;
+    const int e2 = cplx ? 2 : 1;
+    const size_t es = 16 * (size_t)e2;
+    Staged SA, SX, SY;
+    sc.add(SA); sc.add(SX); sc.add(SY);
+    int64_t dix, diy = 1;
+    if (!stage_vector(SX, x, N, *incx, es, true, dix, routine)) return;
+    if (two && !stage_vector(SY, y, N, *incy, es, true, diy, routine)) return;
+    const int64_t len = N * (N + 1) / 2;
+    void *dense = nullptr;
+    if (packed) {
+        if (!stage_matrix(SA, a, len, 1, len, es, true, routine)) return;
+        dense = dev_alloc((size_t)N * N * es, routine);
+        if (!dense) return;
+        pack_move(N, SA.dev, e2, U == 'U', dense, true);
+    } else {
+        if (!stage_matrix(SA, a, N, N, *lda, es, true, routine)) return;
+    }
+    RankArgs r;
+    r.cplx = cplx;
+    r.conj = herm;
+    r.uplo = U == 'U' ? 1 : 2;
+    r.m = N;
+    r.n = N;
+    r.x = SX.dev;
+    r.incx = dix;
+    r.y = two ? SY.dev : nullptr;
+    r.incy = diy;
+    r.A = packed ? dense : SA.dev;
+    r.lda = packed ? N : *lda;
+    if (alpha_real) {
+        r.alpha = rd((const mwblas_real64x2 *)alpha);
+        r.calpha = cdd_host{r.alpha, {0.0, 0.0}};
+    } else {
+        r.calpha = cd((const mwblas_complex64x2 *)alpha);
+    }
+    bool ok = rank_update_device(r, routine);
+    if (ok && packed) pack_move(N, SA.dev, e2, U == 'U', dense, false);
+    if (dense) dev_free(dense);
+    if (!ok) return;
+    if (!unstage_matrix(SA, routine)) return;
+    finish(routine);
+}
+
 }  // namespace
 }  // namespace mw
 
@@ -1043,6 +1361,222 @@ void mrotm_64_(const int64_t *n, TR *x, const int64_t *incx, TR *y, const int64_
 {
     mw::rotm_entry<int64_t>(n, x, incx, y, incy, dparam);
 }
+
+// ---- level 2 beyond real GEMV -------------------------------------------------------------
+
+void wgemv_(const char *trans, const int *m, const int *n, const TC *alpha, const TC *a, const int *lda, const TC *x,
+            const int *incx, const TC *beta, TC *y, const int *incy)
+{
+    mw::gemv2_entry<int>("wgemv", true, false, trans, m, n, (const int *)nullptr, (const int *)nullptr, alpha, a, lda,
+                         x, incx, beta, y, incy);
+}
+void wgemv_64_(const char *trans, const int64_t *m, const int64_t *n, const TC *alpha, const TC *a, const int64_t *lda,
+               const TC *x, const int64_t *incx, const TC *beta, TC *y, const int64_t *incy)
+{
+    mw::gemv2_entry<int64_t>("wgemv", true, false, trans, m, n, (const int64_t *)nullptr, (const int64_t *)nullptr,
+                             alpha, a, lda, x, incx, beta, y, incy);
+}
+
+#define MW_GBMV_PAIR(NAME, T, CPLX)                                                                              \
+    void NAME##_(const char *trans, const int *m, const int *n, const int *kl, const int *ku, const T *alpha,   \
+                 const T *a, const int *lda, const T *x, const int *incx, const T *beta, T *y, const int *incy) \
+    {                                                                                                          \
+        mw::gemv2_entry<int>(#NAME, CPLX, true, trans, m, n, kl, ku, alpha, a, lda, x, incx, beta, y, incy);   \
+    }                                                                                                          \
+    void NAME##_64_(const char *trans, const int64_t *m, const int64_t *n, const int64_t *kl, const int64_t *ku, \
+                    const T *alpha, const T *a, const int64_t *lda, const T *x, const int64_t *incx,            \
+                    const T *beta, T *y, const int64_t *incy)                                                   \
+    {                                                                                                          \
+        mw::gemv2_entry<int64_t>(#NAME, CPLX, true, trans, m, n, kl, ku, alpha, a, lda, x, incx, beta, y,      \
+                                 incy);                                                                         \
+    }
+MW_GBMV_PAIR(mgbmv, TR, false)
+MW_GBMV_PAIR(wgbmv, TC, true)
+#undef MW_GBMV_PAIR
+
+#define MW_SYMV_PAIR(NAME, T, CPLX, HERM)                                                                          \
+    void NAME##_(const char *uplo, const int *n, const T *alpha, const T *a, const int *lda, const T *x,          \
+                 const int *incx, const T *beta, T *y, const int *incy)                                           \
+    {                                                                                                            \
+        mw::symv_entry<int>(#NAME, CPLX, HERM, 0, uplo, n, (const int *)nullptr, alpha, a, lda, x, incx, beta, y, \
+                            incy);                                                                                \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const int64_t *n, const T *alpha, const T *a, const int64_t *lda,           \
+                    const T *x, const int64_t *incx, const T *beta, T *y, const int64_t *incy)                    \
+    {                                                                                                            \
+        mw::symv_entry<int64_t>(#NAME, CPLX, HERM, 0, uplo, n, (const int64_t *)nullptr, alpha, a, lda, x, incx,  \
+                                beta, y, incy);                                                                   \
+    }
+MW_SYMV_PAIR(msymv, TR, false, false)
+MW_SYMV_PAIR(whemv, TC, true, true)
+#undef MW_SYMV_PAIR
+
+#define MW_SBMV_PAIR(NAME, T, CPLX, HERM)                                                                          \
+    void NAME##_(const char *uplo, const int *n, const int *k, const T *alpha, const T *a, const int *lda,        \
+                 const T *x, const int *incx, const T *beta, T *y, const int *incy)                               \
+    {                                                                                                            \
+        mw::symv_entry<int>(#NAME, CPLX, HERM, 1, uplo, n, k, alpha, a, lda, x, incx, beta, y, incy);            \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const int64_t *n, const int64_t *k, const T *alpha, const T *a,             \
+                    const int64_t *lda, const T *x, const int64_t *incx, const T *beta, T *y, const int64_t *incy) \
+    {                                                                                                            \
+        mw::symv_entry<int64_t>(#NAME, CPLX, HERM, 1, uplo, n, k, alpha, a, lda, x, incx, beta, y, incy);        \
+    }
+MW_SBMV_PAIR(msbmv, TR, false, false)
+MW_SBMV_PAIR(whbmv, TC, true, true)
+#undef MW_SBMV_PAIR
+
+#define MW_SPMV_PAIR(NAME, T, CPLX, HERM)                                                                          \
+    void NAME##_(const char *uplo, const int *n, const T *alpha, const T *ap, const T *x, const int *incx,        \
+                 const T *beta, T *y, const int *incy)                                                            \
+    {                                                                                                            \
+        mw::symv_entry<int>(#NAME, CPLX, HERM, 2, uplo, n, (const int *)nullptr, alpha, ap, (const int *)nullptr, \
+                            x, incx, beta, y, incy);                                                              \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const int64_t *n, const T *alpha, const T *ap, const T *x,                  \
+                    const int64_t *incx, const T *beta, T *y, const int64_t *incy)                                \
+    {                                                                                                            \
+        mw::symv_entry<int64_t>(#NAME, CPLX, HERM, 2, uplo, n, (const int64_t *)nullptr, alpha, ap,               \
+                                (const int64_t *)nullptr, x, incx, beta, y, incy);                                \
+    }
+MW_SPMV_PAIR(mspmv, TR, false, false)
+MW_SPMV_PAIR(whpmv, TC, true, true)
+#undef MW_SPMV_PAIR
+
+#define MW_TRV_PAIR(NAME, T, CPLX, SOLVE)                                                                          \
+    void NAME##_(const char *uplo, const char *trans, const char *diag, const int *n, const T *a, const int *lda, \
+                 T *x, const int *incx)                                                                           \
+    {                                                                                                            \
+        mw::trv_entry<int>(#NAME, CPLX, SOLVE, 0, uplo, trans, diag, n, (const int *)nullptr, a, lda, x, incx);  \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const T *a,          \
+                    const int64_t *lda, T *x, const int64_t *incx)                                                \
+    {                                                                                                            \
+        mw::trv_entry<int64_t>(#NAME, CPLX, SOLVE, 0, uplo, trans, diag, n, (const int64_t *)nullptr, a, lda, x, \
+                               incx);                                                                             \
+    }
+MW_TRV_PAIR(mtrmv, TR, false, false)
+MW_TRV_PAIR(wtrmv, TC, true, false)
+MW_TRV_PAIR(mtrsv, TR, false, true)
+MW_TRV_PAIR(wtrsv, TC, true, true)
+#undef MW_TRV_PAIR
+
+#define MW_TBV_PAIR(NAME, T, CPLX, SOLVE)                                                                          \
+    void NAME##_(const char *uplo, const char *trans, const char *diag, const int *n, const int *k, const T *a,  \
+                 const int *lda, T *x, const int *incx)                                                           \
+    {                                                                                                            \
+        mw::trv_entry<int>(#NAME, CPLX, SOLVE, 1, uplo, trans, diag, n, k, a, lda, x, incx);                      \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const int64_t *k,    \
+                    const T *a, const int64_t *lda, T *x, const int64_t *incx)                                    \
+    {                                                                                                            \
+        mw::trv_entry<int64_t>(#NAME, CPLX, SOLVE, 1, uplo, trans, diag, n, k, a, lda, x, incx);                  \
+    }
+MW_TBV_PAIR(mtbmv, TR, false, false)
+MW_TBV_PAIR(wtbmv, TC, true, false)
+MW_TBV_PAIR(mtbsv, TR, false, true)
+MW_TBV_PAIR(wtbsv, TC, true, true)
+#undef MW_TBV_PAIR
+
+#define MW_TPV_PAIR(NAME, T, CPLX, SOLVE)                                                                          \
+    void NAME##_(const char *uplo, const char *trans, const char *diag, const int *n, const T *ap, T *x,          \
+                 const int *incx)                                                                                 \
+    {                                                                                                            \
+        mw::trv_entry<int>(#NAME, CPLX, SOLVE, 2, uplo, trans, diag, n, (const int *)nullptr, ap,                 \
+                           (const int *)nullptr, x, incx);                                                        \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const T *ap, T *x,   \
+                    const int64_t *incx)                                                                          \
+    {                                                                                                            \
+        mw::trv_entry<int64_t>(#NAME, CPLX, SOLVE, 2, uplo, trans, diag, n, (const int64_t *)nullptr, ap,         \
+                               (const int64_t *)nullptr, x, incx);                                                \
+    }
+MW_TPV_PAIR(mtpmv, TR, false, false)
+MW_TPV_PAIR(wtpmv, TC, true, false)
+MW_TPV_PAIR(mtpsv, TR, false, true)
+MW_TPV_PAIR(wtpsv, TC, true, true)
+#undef MW_TPV_PAIR
+
+#define MW_GER_PAIR(NAME, T, CPLX, CONJ)                                                                           \
+    void NAME##_(const int *m, const int *n, const T *alpha, const T *x, const int *incx, const T *y,            \
+                 const int *incy, T *a, const int *lda)                                                           \
+    {                                                                                                            \
+        mw::ger_entry<int>(#NAME, CPLX, CONJ, m, n, alpha, x, incx, y, incy, a, lda);                            \
+    }                                                                                                            \
+    void NAME##_64_(const int64_t *m, const int64_t *n, const T *alpha, const T *x, const int64_t *incx,          \
+                    const T *y, const int64_t *incy, T *a, const int64_t *lda)                                    \
+    {                                                                                                            \
+        mw::ger_entry<int64_t>(#NAME, CPLX, CONJ, m, n, alpha, x, incx, y, incy, a, lda);                        \
+    }
+MW_GER_PAIR(mger, TR, false, false)
+MW_GER_PAIR(wgeru, TC, true, false)
+MW_GER_PAIR(wgerc, TC, true, true)
+#undef MW_GER_PAIR
+
+#define MW_SYR_PAIR(NAME, ST, VT, CPLX, HERM)                                                                      \
+    void NAME##_(const char *uplo, const int *n, const ST *alpha, const VT *x, const int *incx, VT *a,           \
+                 const int *lda)                                                                                  \
+    {                                                                                                            \
+        mw::syr_entry<int>(#NAME, CPLX, HERM, false, false, uplo, n, alpha, x, incx, (const VT *)nullptr,         \
+                           (const int *)nullptr, a, lda);                                                         \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const int64_t *n, const ST *alpha, const VT *x, const int64_t *incx, VT *a, \
+                    const int64_t *lda)                                                                           \
+    {                                                                                                            \
+        mw::syr_entry<int64_t>(#NAME, CPLX, HERM, false, false, uplo, n, alpha, x, incx, (const VT *)nullptr,     \
+                               (const int64_t *)nullptr, a, lda);                                                 \
+    }
+MW_SYR_PAIR(msyr, TR, TR, false, false)
+MW_SYR_PAIR(wher, TR, TC, true, true)
+#undef MW_SYR_PAIR
+
+#define MW_SPR_PAIR(NAME, ST, VT, CPLX, HERM)                                                                      \
+    void NAME##_(const char *uplo, const int *n, const ST *alpha, const VT *x, const int *incx, VT *ap)          \
+    {                                                                                                            \
+        mw::syr_entry<int>(#NAME, CPLX, HERM, true, false, uplo, n, alpha, x, incx, (const VT *)nullptr,          \
+                           (const int *)nullptr, ap, (const int *)nullptr);                                       \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const int64_t *n, const ST *alpha, const VT *x, const int64_t *incx,        \
+                    VT *ap)                                                                                       \
+    {                                                                                                            \
+        mw::syr_entry<int64_t>(#NAME, CPLX, HERM, true, false, uplo, n, alpha, x, incx, (const VT *)nullptr,      \
+                               (const int64_t *)nullptr, ap, (const int64_t *)nullptr);                           \
+    }
+MW_SPR_PAIR(mspr, TR, TR, false, false)
+MW_SPR_PAIR(whpr, TR, TC, true, true)
+#undef MW_SPR_PAIR
+
+#define MW_SYR2_PAIR(NAME, T, CPLX, HERM, PACKED)                                                                 \
+    void NAME##_(const char *uplo, const int *n, const T *alpha, const T *x, const int *incx, const T *y,       \
+                 const int *incy, T *a, const int *lda)                                                          \
+    {                                                                                                           \
+        mw::syr_entry<int>(#NAME, CPLX, HERM, PACKED, true, uplo, n, alpha, x, incx, y, incy, a, lda);          \
+    }                                                                                                           \
+    void NAME##_64_(const char *uplo, const int64_t *n, const T *alpha, const T *x, const int64_t *incx,         \
+                    const T *y, const int64_t *incy, T *a, const int64_t *lda)                                   \
+    {                                                                                                           \
+        mw::syr_entry<int64_t>(#NAME, CPLX, HERM, PACKED, true, uplo, n, alpha, x, incx, y, incy, a, lda);      \
+    }
+MW_SYR2_PAIR(msyr2, TR, false, false, false)
+MW_SYR2_PAIR(wher2, TC, true, true, false)
+#undef MW_SYR2_PAIR
+
+#define MW_SPR2_PAIR(NAME, T, CPLX, HERM)                                                                          \
+    void NAME##_(const char *uplo, const int *n, const T *alpha, const T *x, const int *incx, const T *y,        \
+                 const int *incy, T *ap)                                                                          \
+    {                                                                                                            \
+        mw::syr_entry<int>(#NAME, CPLX, HERM, true, true, uplo, n, alpha, x, incx, y, incy, ap,                  \
+                           (const int *)nullptr);                                                                 \
+    }                                                                                                            \
+    void NAME##_64_(const char *uplo, const int64_t *n, const T *alpha, const T *x, const int64_t *incx,          \
+                    const T *y, const int64_t *incy, T *ap)                                                       \
+    {                                                                                                            \
+        mw::syr_entry<int64_t>(#NAME, CPLX, HERM, true, true, uplo, n, alpha, x, incx, y, incy, ap,              \
+                               (const int64_t *)nullptr);                                                         \
+    }
+MW_SPR2_PAIR(mspr2, TR, false, false)
+MW_SPR2_PAIR(whpr2, TC, true, true)
+#undef MW_SPR2_PAIR
 
 // ---- level 2 -----------------------------------------------------------------------------
 

@@ -111,6 +111,14 @@ class MWBlas:
             self._sig("mrot" + suf, None, [PI, _p, PI, _p, PI, R, R])
             self._sig("wmrot" + suf, None, [PI, _p, PI, _p, PI, R, R])
             self._sig("mrotm" + suf, None, [PI, _p, PI, _p, PI, _p])
+            # level 2 beyond mgemv (all scalars and arrays passed as pointers)
+            for nm, na in (("wgemv", 11), ("mgbmv", 13), ("wgbmv", 13), ("msymv", 10), ("whemv", 10),
+                           ("msbmv", 11), ("whbmv", 11), ("mspmv", 9), ("whpmv", 9), ("mtrmv", 8), ("wtrmv", 8),
+                           ("mtrsv", 8), ("wtrsv", 8), ("mtbmv", 9), ("wtbmv", 9), ("mtbsv", 9), ("wtbsv", 9),
+                           ("mtpmv", 7), ("wtpmv", 7), ("mtpsv", 7), ("wtpsv", 7), ("mger", 9), ("wgeru", 9),
+                           ("wgerc", 9), ("msyr", 7), ("wher", 7), ("mspr", 6), ("whpr", 6), ("msyr2", 9),
+                           ("wher2", 9), ("mspr2", 8), ("whpr2", 8)):
+                self._sig(nm + suf, None, [_p] * na)
             self._sig("mgemv" + suf, None, [_ch, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
             self._sig("mdot" + suf, Real64x2, [PI, _p, PI, _p, PI])
             self._sig("maxpy" + suf, None, [PI, R, _p, PI, _p, PI])
@@ -270,6 +278,29 @@ class MWBlas:
         I = lambda v: self._I(v, wide)
         p = np.ascontiguousarray(np.asarray(param, dtype=np.float64).reshape(5, 2))
         (self.lib.mrotm_64_ if wide else self.lib.mrotm_)(I(n), _ptr(x), I(incx), _ptr(y), I(incy), _ptr(p))
+
+    def l2(self, name, *args, wide=True):
+        """Level-2 routines beyond mgemv: arguments in the Fortran order; str
+        for flags, int for sizes/increments, numpy arrays or device pointers
+        for arrays, array-likes for scalars (real (2,) or complex (2, 2))."""
+        conv, keep = [], []
+        IT = _i64 if wide else _i32
+        for a in args:
+            if isinstance(a, str):
+                b = C.c_char_p(a.encode())
+                keep.append(b)
+                conv.append(C.cast(b, C.c_void_p))
+            elif isinstance(a, (int, np.integer)):
+                b = IT(int(a))
+                keep.append(b)
+                conv.append(C.cast(C.pointer(b), C.c_void_p))
+            elif isinstance(a, tuple) and len(a) == 1:     # (device pointer,)
+                conv.append(C.c_void_p(a[0]))
+            else:
+                arr = np.ascontiguousarray(np.asarray(a, dtype=np.float64)) if not isinstance(a, np.ndarray) else a
+                keep.append(arr)
+                conv.append(C.c_void_p(arr.ctypes.data))
+        getattr(self.lib, name + ("_64_" if wide else "_"))(*conv)
 
     # ---- batched (extension) -----------------------------------------------------------
     @staticmethod

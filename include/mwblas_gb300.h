@@ -216,6 +216,92 @@ void mgemv_64_(const char *trans, const int64_t *m, const int64_t *n,
                const MWBLAS_R *x, const int64_t *incx, const MWBLAS_R *beta,
                MWBLAS_R *y, const int64_t *incy);
 
+/* ======================= Level 2 (beyond mgemv_) ========================
+ * Matrix-vector products, solves and rank updates with dense, band (LAPACK
+ * band layout) or packed operands, real and complex; vectors take any
+ * non-zero increment.  Replace the reference's routines of the same names and
+ * their _64_ twins (facade epblas_facade.h:132-223). */
+
+/* y := alpha*op(A)*x + beta*y, complex A (multifloats/wgemv.cpp), banded A
+ * (mgbmv.cpp, wgbmv.cpp). */
+void wgemv_(const char *trans, const int *m, const int *n, const MWBLAS_C *alpha, const MWBLAS_C *a, const int *lda, const MWBLAS_C *x, const int *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int *incy);
+void wgemv_64_(const char *trans, const int64_t *m, const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int64_t *incy);
+void mgbmv_(const char *trans, const int *m, const int *n, const int *kl, const int *ku, const MWBLAS_R *alpha, const MWBLAS_R *a, const int *lda, const MWBLAS_R *x, const int *incx, const MWBLAS_R *beta, MWBLAS_R *y, const int *incy);
+void mgbmv_64_(const char *trans, const int64_t *m, const int64_t *n, const int64_t *kl, const int64_t *ku, const MWBLAS_R *alpha, const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *x, const int64_t *incx, const MWBLAS_R *beta, MWBLAS_R *y, const int64_t *incy);
+void wgbmv_(const char *trans, const int *m, const int *n, const int *kl, const int *ku, const MWBLAS_C *alpha, const MWBLAS_C *a, const int *lda, const MWBLAS_C *x, const int *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int *incy);
+void wgbmv_64_(const char *trans, const int64_t *m, const int64_t *n, const int64_t *kl, const int64_t *ku, const MWBLAS_C *alpha, const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int64_t *incy);
+
+/* y := alpha*A*x + beta*y with A symmetric / Hermitian: dense (msymv.cpp,
+ * whemv.cpp), band (msbmv.cpp, whbmv.cpp), packed (mspmv.cpp, whpmv.cpp). */
+void msymv_(const char *uplo, const int *n, const MWBLAS_R *alpha, const MWBLAS_R *a, const int *lda, const MWBLAS_R *x, const int *incx, const MWBLAS_R *beta, MWBLAS_R *y, const int *incy);
+void msymv_64_(const char *uplo, const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *x, const int64_t *incx, const MWBLAS_R *beta, MWBLAS_R *y, const int64_t *incy);
+void whemv_(const char *uplo, const int *n, const MWBLAS_C *alpha, const MWBLAS_C *a, const int *lda, const MWBLAS_C *x, const int *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int *incy);
+void whemv_64_(const char *uplo, const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int64_t *incy);
+void msbmv_(const char *uplo, const int *n, const int *k, const MWBLAS_R *alpha, const MWBLAS_R *a, const int *lda, const MWBLAS_R *x, const int *incx, const MWBLAS_R *beta, MWBLAS_R *y, const int *incy);
+void msbmv_64_(const char *uplo, const int64_t *n, const int64_t *k, const MWBLAS_R *alpha, const MWBLAS_R *a, const int64_t *lda, const MWBLAS_R *x, const int64_t *incx, const MWBLAS_R *beta, MWBLAS_R *y, const int64_t *incy);
+void whbmv_(const char *uplo, const int *n, const int *k, const MWBLAS_C *alpha, const MWBLAS_C *a, const int *lda, const MWBLAS_C *x, const int *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int *incy);
+void whbmv_64_(const char *uplo, const int64_t *n, const int64_t *k, const MWBLAS_C *alpha, const MWBLAS_C *a, const int64_t *lda, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int64_t *incy);
+void mspmv_(const char *uplo, const int *n, const MWBLAS_R *alpha, const MWBLAS_R *ap, const MWBLAS_R *x, const int *incx, const MWBLAS_R *beta, MWBLAS_R *y, const int *incy);
+void mspmv_64_(const char *uplo, const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *ap, const MWBLAS_R *x, const int64_t *incx, const MWBLAS_R *beta, MWBLAS_R *y, const int64_t *incy);
+void whpmv_(const char *uplo, const int *n, const MWBLAS_C *alpha, const MWBLAS_C *ap, const MWBLAS_C *x, const int *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int *incy);
+void whpmv_64_(const char *uplo, const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *ap, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *beta, MWBLAS_C *y, const int64_t *incy);
+
+/* x := op(A)*x and x := op(A)^-1*x with A triangular: dense (mtrmv.cpp,
+ * mtrsv.cpp, wtrmv.cpp, wtrsv.cpp), band (mtbmv.cpp, mtbsv.cpp, ...), packed
+ * (mtpmv.cpp, mtpsv.cpp, ...). */
+void mtrmv_(const char *uplo, const char *trans, const char *diag, const int *n, const MWBLAS_R *a, const int *lda, MWBLAS_R *x, const int *incx);
+void mtrmv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const MWBLAS_R *a, const int64_t *lda, MWBLAS_R *x, const int64_t *incx);
+void wtrmv_(const char *uplo, const char *trans, const char *diag, const int *n, const MWBLAS_C *a, const int *lda, MWBLAS_C *x, const int *incx);
+void wtrmv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const MWBLAS_C *a, const int64_t *lda, MWBLAS_C *x, const int64_t *incx);
+void mtrsv_(const char *uplo, const char *trans, const char *diag, const int *n, const MWBLAS_R *a, const int *lda, MWBLAS_R *x, const int *incx);
+void mtrsv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const MWBLAS_R *a, const int64_t *lda, MWBLAS_R *x, const int64_t *incx);
+void wtrsv_(const char *uplo, const char *trans, const char *diag, const int *n, const MWBLAS_C *a, const int *lda, MWBLAS_C *x, const int *incx);
+void wtrsv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const MWBLAS_C *a, const int64_t *lda, MWBLAS_C *x, const int64_t *incx);
+void mtbmv_(const char *uplo, const char *trans, const char *diag, const int *n, const int *k, const MWBLAS_R *a, const int *lda, MWBLAS_R *x, const int *incx);
+void mtbmv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const int64_t *k, const MWBLAS_R *a, const int64_t *lda, MWBLAS_R *x, const int64_t *incx);
+void wtbmv_(const char *uplo, const char *trans, const char *diag, const int *n, const int *k, const MWBLAS_C *a, const int *lda, MWBLAS_C *x, const int *incx);
+void wtbmv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const int64_t *k, const MWBLAS_C *a, const int64_t *lda, MWBLAS_C *x, const int64_t *incx);
+void mtbsv_(const char *uplo, const char *trans, const char *diag, const int *n, const int *k, const MWBLAS_R *a, const int *lda, MWBLAS_R *x, const int *incx);
+void mtbsv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const int64_t *k, const MWBLAS_R *a, const int64_t *lda, MWBLAS_R *x, const int64_t *incx);
+void wtbsv_(const char *uplo, const char *trans, const char *diag, const int *n, const int *k, const MWBLAS_C *a, const int *lda, MWBLAS_C *x, const int *incx);
+void wtbsv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const int64_t *k, const MWBLAS_C *a, const int64_t *lda, MWBLAS_C *x, const int64_t *incx);
+void mtpmv_(const char *uplo, const char *trans, const char *diag, const int *n, const MWBLAS_R *ap, MWBLAS_R *x, const int *incx);
+void mtpmv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const MWBLAS_R *ap, MWBLAS_R *x, const int64_t *incx);
+void wtpmv_(const char *uplo, const char *trans, const char *diag, const int *n, const MWBLAS_C *ap, MWBLAS_C *x, const int *incx);
+void wtpmv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const MWBLAS_C *ap, MWBLAS_C *x, const int64_t *incx);
+void mtpsv_(const char *uplo, const char *trans, const char *diag, const int *n, const MWBLAS_R *ap, MWBLAS_R *x, const int *incx);
+void mtpsv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const MWBLAS_R *ap, MWBLAS_R *x, const int64_t *incx);
+void wtpsv_(const char *uplo, const char *trans, const char *diag, const int *n, const MWBLAS_C *ap, MWBLAS_C *x, const int *incx);
+void wtpsv_64_(const char *uplo, const char *trans, const char *diag, const int64_t *n, const MWBLAS_C *ap, MWBLAS_C *x, const int64_t *incx);
+
+/* Rank-1/2 updates: A := alpha*x*y**T (+A) (mger.cpp; wgeru.cpp, wgerc.cpp
+ * with y**H), A := alpha*x*x**T(**H) + A on a triangle (msyr.cpp, wher.cpp
+ * with real alpha; packed mspr.cpp, whpr.cpp), A := alpha*x*y**T +
+ * alpha*y*x**T + A (msyr2.cpp; wher2.cpp with conj(alpha); packed mspr2.cpp,
+ * whpr2.cpp). */
+void mger_(const int *m, const int *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int *incx, const MWBLAS_R *y, const int *incy, MWBLAS_R *a, const int *lda);
+void mger_64_(const int64_t *m, const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int64_t *incx, const MWBLAS_R *y, const int64_t *incy, MWBLAS_R *a, const int64_t *lda);
+void wgeru_(const int *m, const int *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int *incx, const MWBLAS_C *y, const int *incy, MWBLAS_C *a, const int *lda);
+void wgeru_64_(const int64_t *m, const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *y, const int64_t *incy, MWBLAS_C *a, const int64_t *lda);
+void wgerc_(const int *m, const int *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int *incx, const MWBLAS_C *y, const int *incy, MWBLAS_C *a, const int *lda);
+void wgerc_64_(const int64_t *m, const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *y, const int64_t *incy, MWBLAS_C *a, const int64_t *lda);
+void msyr_(const char *uplo, const int *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int *incx, MWBLAS_R *a, const int *lda);
+void msyr_64_(const char *uplo, const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int64_t *incx, MWBLAS_R *a, const int64_t *lda);
+void wher_(const char *uplo, const int *n, const MWBLAS_R *alpha, const MWBLAS_C *x, const int *incx, MWBLAS_C *a, const int *lda);
+void wher_64_(const char *uplo, const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_C *x, const int64_t *incx, MWBLAS_C *a, const int64_t *lda);
+void mspr_(const char *uplo, const int *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int *incx, MWBLAS_R *ap);
+void mspr_64_(const char *uplo, const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int64_t *incx, MWBLAS_R *ap);
+void whpr_(const char *uplo, const int *n, const MWBLAS_R *alpha, const MWBLAS_C *x, const int *incx, MWBLAS_C *ap);
+void whpr_64_(const char *uplo, const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_C *x, const int64_t *incx, MWBLAS_C *ap);
+void msyr2_(const char *uplo, const int *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int *incx, const MWBLAS_R *y, const int *incy, MWBLAS_R *a, const int *lda);
+void msyr2_64_(const char *uplo, const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int64_t *incx, const MWBLAS_R *y, const int64_t *incy, MWBLAS_R *a, const int64_t *lda);
+void wher2_(const char *uplo, const int *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int *incx, const MWBLAS_C *y, const int *incy, MWBLAS_C *a, const int *lda);
+void wher2_64_(const char *uplo, const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *y, const int64_t *incy, MWBLAS_C *a, const int64_t *lda);
+void mspr2_(const char *uplo, const int *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int *incx, const MWBLAS_R *y, const int *incy, MWBLAS_R *ap);
+void mspr2_64_(const char *uplo, const int64_t *n, const MWBLAS_R *alpha, const MWBLAS_R *x, const int64_t *incx, const MWBLAS_R *y, const int64_t *incy, MWBLAS_R *ap);
+void whpr2_(const char *uplo, const int *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int *incx, const MWBLAS_C *y, const int *incy, MWBLAS_C *ap);
+void whpr2_64_(const char *uplo, const int64_t *n, const MWBLAS_C *alpha, const MWBLAS_C *x, const int64_t *incx, const MWBLAS_C *y, const int64_t *incy, MWBLAS_C *ap);
+
 /* ======================= Level 1 ======================================= */
 
 /* Complex dots sum x(i)*y(i) (wdotu_) and sum conj(x(i))*y(i) (wdotc_), the
