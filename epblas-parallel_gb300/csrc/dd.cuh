@@ -134,6 +134,22 @@ __device__ __forceinline__ real div(real a, real b)
     return add_exact(q, make(q3, 0.0));
 }
 
+// Double-double square root (Karp and Markstein 1997: one correction of the
+// FP64 root s by the exact residual, s + (v - s^2) / (2s)). v <= 0 gives 0
+// (v == 0) or NaN.
+__device__ __forceinline__ real sqrt(real v)
+{
+    if (v.hi <= 0.0) return make(v.hi == 0.0 ? 0.0 : __longlong_as_double(0x7ff8000000000000ll), 0.0);
+    const double s = __dsqrt_rn(v.hi);
+    double p, e;
+    two_prod(s, s, p, e);
+    const real r = sub_exact(v, make(p, e));
+    const double t = __ddiv_rn(r.hi, __dmul_rn(2.0, s));
+    real out;
+    fast_two_sum(s, t, out.hi, out.lo);
+    return out;
+}
+
 // ---- complex (mf_simd_fast.h:119-144 and mf_kernels.h:43-53) -------------
 
 // fast complex multiply: re = a.re*b.re - a.im*b.im ; im = a.re*b.im + a.im*b.re
@@ -194,6 +210,13 @@ __device__ __forceinline__ bool gt(real a, real b)
 {
     return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo);
 }
+__device__ __forceinline__ bool lt(real a, real b) { return gt(b, a); }
+__device__ __forceinline__ bool eq0(real a) { return a.hi == 0.0 && a.lo == 0.0; }
+__device__ __forceinline__ bool lt0(real a) { return a.hi < 0.0 || (a.hi == 0.0 && a.lo < 0.0); }
+__device__ __forceinline__ bool gt0(real a) { return a.hi > 0.0 || (a.hi == 0.0 && a.lo > 0.0); }
+
+// a < 0 ? -a : a with the limb-lexicographic sign (mf_pred.h:70).
+__device__ __forceinline__ real absv(real a) { return lt0(a) ? neg(a) : a; }
 
 // Branch-free magnitude used by the reference's vector argmax
 // (imamax.cpp:60-72): (|hi|, lo with its sign flipped when hi is negative).

@@ -844,6 +844,76 @@ void rotm_entry(const INT *n, void *x, const INT *incx, void *y, const INT *incy
     rot_entry(routine, 1, n, x, incx, y, incy, h);
 }
 
+// ---- mcabs1 / mrotg / mrotmg / wrotg (mcabs1.cpp:20, mrotg.cpp:21, mrotmg.cpp:25, wrotg.cpp:27) ----
+// Scalar arguments are host variables, as in the reference's signatures.
+
+bool gen_run(const char *routine, int op, const double2 *in, int nin, GenResult &r)
+{
+    Scope sc(routine);
+    if (!ensure_device(routine)) return false;
+    GenInput gi;
+    for (int i = 0; i < 4; ++i) gi.v[i] = i < nin ? in[i] : make_double2(0.0, 0.0);
+    if (!launch_generator(op, gi, &r, routine)) return false;
+    return true;
+}
+
+inline double2 d2(const mwblas_real64x2 *p) { return make_double2(p->limbs[0], p->limbs[1]); }
+inline void put(mwblas_real64x2 *p, const GenResult &r, int i)
+{
+    if (r.mask & (1u << i)) {
+        p->limbs[0] = r.v[i].x;
+        p->limbs[1] = r.v[i].y;
+    }
+}
+
+mwblas_real64x2 cabs1_entry(const mwblas_complex64x2 *z)
+{
+    mwblas_real64x2 out{{0.0, 0.0}};
+    if (!z) { set_error("mcabs1", 1, "null argument pointer"); return out; }
+    const double2 in[2] = {d2(&z->re), d2(&z->im)};
+    GenResult r;
+    if (gen_run("mcabs1", GEN_CABS1, in, 2, r)) put(&out, r, 0);
+    return out;
+}
+
+void rotg_entry(mwblas_real64x2 *a, mwblas_real64x2 *b, mwblas_real64x2 *c, mwblas_real64x2 *s)
+{
+    if (!a || !b || !c || !s) { set_error("mrotg", 1, "null argument pointer"); return; }
+    const double2 in[2] = {d2(a), d2(b)};
+    GenResult r;
+    if (!gen_run("mrotg", GEN_ROTG, in, 2, r)) return;
+    put(a, r, 0);
+    put(b, r, 1);
+    put(c, r, 2);
+    put(s, r, 3);
+}
+
+void rotmg_entry(mwblas_real64x2 *d1, mwblas_real64x2 *d2_, mwblas_real64x2 *x1, const mwblas_real64x2 *y1,
+                 mwblas_real64x2 *param)
+{
+    if (!d1 || !d2_ || !x1 || !y1 || !param) { set_error("mrotmg", 1, "null argument pointer"); return; }
+    const double2 in[4] = {d2(d1), d2(d2_), d2(x1), d2(y1)};
+    GenResult r;
+    if (!gen_run("mrotmg", GEN_ROTMG, in, 4, r)) return;
+    put(d1, r, 0);
+    put(d2_, r, 1);
+    put(x1, r, 2);
+    for (int i = 0; i < 5; ++i) put(param + i, r, 3 + i);
+}
+
+void wrotg_entry(mwblas_complex64x2 *a, const mwblas_complex64x2 *b, mwblas_real64x2 *c, mwblas_complex64x2 *s)
+{
+    if (!a || !b || !c || !s) { set_error("wrotg", 1, "null argument pointer"); return; }
+    const double2 in[4] = {d2(&a->re), d2(&a->im), d2(&b->re), d2(&b->im)};
+    GenResult r;
+    if (!gen_run("wrotg", GEN_WROTG, in, 4, r)) return;
+    put(&a->re, r, 0);
+    put(&a->im, r, 1);
+    put(c, r, 2);
+    put(&s->re, r, 3);
+    put(&s->im, r, 4);
+}
+
 // ---- level 2 beyond real GEMV (gbmv, symv/hemv/sbmv/hbmv/spmv/hpmv, trmv/tbmv/tpmv,
 //      trsv/tbsv/tpsv, ger/geru/gerc, syr/her/spr/hpr, syr2/her2/spr2/hpr2) ------------
 // Matrix formats: 0 dense (lda), 1 band (ldab, k or kl/ku), 2 packed (n(n+1)/2).
@@ -1361,6 +1431,15 @@ void mrotm_64_(const int64_t *n, TR *x, const int64_t *incx, TR *y, const int64_
 {
     mw::rotm_entry<int64_t>(n, x, incx, y, incy, dparam);
 }
+
+TR mcabs1_(const TC *z) { return mw::cabs1_entry(z); }
+TR mcabs1_64_(const TC *z) { return mw::cabs1_entry(z); }
+void mrotg_(TR *a, TR *b, TR *c, TR *s) { mw::rotg_entry(a, b, c, s); }
+void mrotg_64_(TR *a, TR *b, TR *c, TR *s) { mw::rotg_entry(a, b, c, s); }
+void mrotmg_(TR *d1, TR *d2, TR *x1, const TR *y1, TR *dparam) { mw::rotmg_entry(d1, d2, x1, y1, dparam); }
+void mrotmg_64_(TR *d1, TR *d2, TR *x1, const TR *y1, TR *dparam) { mw::rotmg_entry(d1, d2, x1, y1, dparam); }
+void wrotg_(TC *a, const TC *b, TR *c, TC *s) { mw::wrotg_entry(a, b, c, s); }
+void wrotg_64_(TC *a, const TC *b, TR *c, TC *s) { mw::wrotg_entry(a, b, c, s); }
 
 // ---- level 2 beyond real GEMV -------------------------------------------------------------
 

@@ -139,14 +139,7 @@ __global__ void __launch_bounds__(kThreads) k_reduce(int64_t n, const double2 *_
 // step in double-double, then scaled by 2^k.
 __device__ dd::real dd_sqrt_scaled(dd::real v, int k)
 {
-    if (v.hi <= 0.0) return dd::make(v.hi == 0.0 ? 0.0 : __longlong_as_double(0x7ff8000000000000ll), 0.0);
-    const double s = __dsqrt_rn(v.hi);
-    double p, e;
-    dd::two_prod(s, s, p, e);
-    const dd::real r = dd::sub_exact(v, dd::make(p, e));   // v - s^2
-    const double t = __ddiv_rn(r.hi, 2.0 * s);
-    dd::real out;
-    dd::fast_two_sum(s, t, out.hi, out.lo);
+    const dd::real out = dd::sqrt(v);
     const double f = ldexp(1.0, k);
     return dd::make(out.hi * f, out.lo * f);
 }
@@ -218,7 +211,236 @@ __global__ void k_rot(int64_t n, double2 *x, int64_t incx, double2 *y, int64_t i
     }
 }
 
+// ---- scalar generators: one thread, scalar-operator double-double arithmetic ----------
+// out->v holds the results in the order documented at launch_generator; bit i
+// of out->mask says whether result i is written back (the reference leaves
+// the others untouched).
+
+__device__ __forceinline__ void gput(GenResult *out, int i, dd::real v)
+{
+    out->v[i] = make_double2(v.hi, v.lo);
+    out->mask |= 1u << i;
+}
+
+// mcabs1.cpp:20-24: |Re z| + |Im z|.
+__device__ void gen_cabs1(const double2 *in, GenResult *out)
+{
+    gput(out, 0, dd::add_exact(dd::absv(dd::load(in)), dd::absv(dd::load(in + 1))));
+}
+
+// mrotg.cpp:21-34: (a, b) -> (r, z), c, s with [c s; -s c](a; b) = (r; 0),
+// r = sign(a) sqrt(a^2 + b^2), z = s when |a| > |b| else 1/c.
+// Results: 0 a, 1 b, 2 c, 3 s.
+__device__ void gen_rotg(const double2 *in, GenResult *out)
+{
+    const dd::real zero = dd::make(0.0, 0.0), one = dd::make(1.0, 0.0);
+    const dd::real a = dd::load(in), b = dd::load(in + 1);
+    const dd::real an = dd::absv(a), bn = dd::absv(b);
+    if (dd::eq0(bn)) {
+        gput(out, 2, one);
+        gput(out, 3, zero);
+        gput(out, 1, zero);
+        return;
+    }
+    if (dd::eq0(an)) {
+        gput(out, 2, zero);
+        gput(out, 3, one);
+        gput(out, 0, b);
+        gput(out, 1, one);
+        return;
+    }
+    dd::real r = dd::sqrt(dd::add_exact(dd::mul_exact(an, an), dd::mul_exact(bn, bn)));
+    if (dd::lt(a, zero)) r = dd::neg(r);
+    const dd::real c = dd::div(a, r), s = dd::div(b, r);
+    gput(out, 2, c);
+    gput(out, 3, s);
+    gput(out, 0, r);
+    gput(out, 1, dd::gt(an, bn) ? s : dd::div(one, c));
+}
+
+// mrotmg.cpp:25-106 (the DROTMG algorithm): modified Givens for
+// (sqrt(d1) x1, sqrt(d2) y1). Inputs d1, d2, x1, y1. Results: 0 d1, 1 d2,
+// 2 x1, 3..7 dparam(1..5).
+__device__ void gen_rotmg(const double2 *in, GenResult *out)
+{
+    const dd::real zero = dd::make(0.0, 0.0), one = dd::make(1.0, 0.0), mone = dd::make(-1.0, 0.0);
+    const dd::real gam = dd::make(4096.0, 0.0), gamsq = dd::make(16777216.0, 0.0);
+    const dd::real rgamsq = dd::make(5.9604645e-8, 0.0);   // the reference's literal, not 2^-24
+    dd::real d1 = dd::load(in), d2 = dd::load(in + 1), x1 = dd::load(in + 2);
+    const dd::real y1 = dd::load(in + 3);
+    dd::real flag, h11 = zero, h12 = zero, h21 = zero, h22 = zero;
+    if (dd::lt0(d1)) {
+        flag = mone;
+        d1 = d2 = x1 = zero;
+    } else {
+        const dd::real p2 = dd::mul_exact(d2, y1);
+        if (dd::eq0(p2)) {
+            gput(out, 3, dd::make(-2.0, 0.0));
+            return;
+        }
+        const dd::real p1 = dd::mul_exact(d1, x1);
+        const dd::real q2 = dd::mul_exact(p2, y1);
+        const dd::real q1 = dd::mul_exact(p1, x1);
+        if (dd::gt(dd::absv(q1), dd::absv(q2))) {
+            h21 = dd::div(dd::neg(y1), x1);
+            h12 = dd::div(p2, p1);
+            const dd::real u = dd::sub_exact(one, dd::mul_exact(h12, h21));
+            if (dd::gt0(u)) {
+                flag = zero;
+                d1 = dd::div(d1, u);
+                d2 = dd::div(d2, u);
+                x1 = dd::mul_exact(x1, u);
+            } else {
+                flag = mone;
+                h11 = h12 = h21 = h22 = zero;
+                d1 = d2 = x1 = zero;
+            }
+        } else if (dd::lt0(q2)) {
+            flag = mone;
+            h11 = h12 = h21 = h22 = zero;
+            d1 = d2 = x1 = zero;
+        } else {
+            flag = one;
+            h11 = dd::div(p1, p2);
+            h22 = dd::div(x1, y1);
+            const dd::real u = dd::add_exact(one, dd::mul_exact(h11, h22));
+            const dd::real t = dd::div(d2, u);
+            d2 = dd::div(d1, u);
+            d1 = t;
+            x1 = dd::mul_exact(y1, u);
+        }
+        // Rescale by gam = 2^12 until rgamsq < d < gamsq. Each pass moves the
+        // exponent by 24, so a finite d leaves the loop within 90 passes; the
+        // cap only guards non-finite values.
+        if (!dd::eq0(d1)) {
+            for (int it = 0; it < 200 && (!dd::gt(d1, rgamsq) || !dd::lt(d1, gamsq)); ++it) {
+                if (dd::eq0(flag)) {
+                    h11 = one;
+                    h22 = one;
+                } else {
+                    h21 = mone;
+                    h12 = one;
+                }
+                flag = mone;
+                if (!dd::gt(d1, rgamsq)) {
+                    d1 = dd::mul_exact(dd::mul_exact(d1, gam), gam);
+                    x1 = dd::div(x1, gam);
+                    h11 = dd::div(h11, gam);
+                    h12 = dd::div(h12, gam);
+                } else {
+                    d1 = dd::div(d1, dd::mul_exact(gam, gam));
+                    x1 = dd::mul_exact(x1, gam);
+                    h11 = dd::mul_exact(h11, gam);
+                    h12 = dd::mul_exact(h12, gam);
+                }
+            }
+        }
+        if (!dd::eq0(d2)) {
+            dd::real ad2 = dd::absv(d2);
+            for (int it = 0; it < 200 && (!dd::gt(ad2, rgamsq) || !dd::lt(ad2, gamsq)); ++it) {
+                if (dd::eq0(flag)) {
+                    h11 = one;
+                    h22 = one;
+                } else {
+                    h21 = mone;
+                    h12 = one;
+                }
+                flag = mone;
+                if (!dd::gt(ad2, rgamsq)) {
+                    d2 = dd::mul_exact(dd::mul_exact(d2, gam), gam);
+                    h21 = dd::div(h21, gam);
+                    h22 = dd::div(h22, gam);
+                } else {
+                    d2 = dd::div(d2, dd::mul_exact(gam, gam));
+                    h21 = dd::mul_exact(h21, gam);
+                    h22 = dd::mul_exact(h22, gam);
+                }
+                ad2 = dd::absv(d2);
+            }
+        }
+    }
+    gput(out, 3, flag);
+    if (dd::lt0(flag)) {
+        gput(out, 4, h11);
+        gput(out, 5, h21);
+        gput(out, 6, h12);
+        gput(out, 7, h22);
+    } else if (dd::eq0(flag)) {
+        gput(out, 6, h12);
+        gput(out, 5, h21);
+    } else {
+        gput(out, 4, h11);
+        gput(out, 7, h22);
+    }
+    gput(out, 0, d1);
+    gput(out, 1, d2);
+    gput(out, 2, x1);
+}
+
+// wrotg.cpp:27-48 (ZROTG analogue): c = |a|/sqrt(|a|^2+|b|^2),
+// s = conj(b) a / sqrt(|a|^2 (|a|^2+|b|^2)), a := a/c. Inputs a, b (complex).
+// Results: 0/1 a (re, im), 2 c, 3/4 s (re, im).
+__device__ void gen_wrotg(const double2 *in, GenResult *out)
+{
+    const dd::real zero = dd::make(0.0, 0.0);
+    const dd::cplx a = dd::cload(in), b = dd::cload(in + 2);
+    const dd::real g2 = dd::add_exact(dd::mul_exact(b.re, b.re), dd::mul_exact(b.im, b.im));
+    if (dd::eq0(g2)) {
+        gput(out, 2, dd::make(1.0, 0.0));
+        gput(out, 3, zero);
+        gput(out, 4, zero);
+        return;
+    }
+    const dd::real f2 = dd::add_exact(dd::mul_exact(a.re, a.re), dd::mul_exact(a.im, a.im));
+    if (dd::eq0(f2)) {
+        gput(out, 2, zero);
+        const dd::real d = dd::sqrt(g2);
+        gput(out, 3, dd::div(b.re, d));
+        gput(out, 4, dd::div(dd::neg(b.im), d));
+        gput(out, 0, d);
+        gput(out, 1, zero);
+        return;
+    }
+    const dd::real h2 = dd::add_exact(f2, g2);
+    const dd::real c = dd::sqrt(dd::div(f2, h2));
+    gput(out, 2, c);
+    gput(out, 0, dd::div(a.re, c));
+    gput(out, 1, dd::div(a.im, c));
+    const dd::real d = dd::sqrt(dd::mul_exact(f2, h2));
+    dd::cplx bc;
+    bc.re = b.re;
+    bc.im = dd::neg(b.im);
+    const dd::cplx p = dd::cmul_exact(bc, a);
+    gput(out, 3, dd::div(p.re, d));
+    gput(out, 4, dd::div(p.im, d));
+}
+
+__global__ void k_generator(int op, GenInput in, GenResult *out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    out->mask = 0;
+    switch (op) {
+    case GEN_CABS1: gen_cabs1(in.v, out); break;
+    case GEN_ROTG: gen_rotg(in.v, out); break;
+    case GEN_ROTMG: gen_rotmg(in.v, out); break;
+    default: gen_wrotg(in.v, out); break;
+    }
+}
+
 }  // namespace
+
+bool launch_generator(int op, const GenInput &in, GenResult *result_host, const char *routine)
+{
+    GenResult *d = (GenResult *)dev_alloc(sizeof(GenResult), routine);
+    if (!d) return false;
+    k_generator<<<1, 32, 0, stream()>>>(op, in, d);
+    count_launch();
+    bool ok = cuda_ok(cudaMemcpyAsync(result_host, d, sizeof(GenResult), cudaMemcpyDeviceToHost, stream()), routine,
+                      "generator result readback");
+    ok = ok && cuda_ok(cudaStreamSynchronize(stream()), routine, "generator sync");
+    dev_free(d);
+    return ok;
+}
 
 bool launch_reduce(int mode, int64_t n, const void *x, int64_t incx, const void *y, int64_t incy,
                    double2 *result_host, const char *routine)

@@ -111,6 +111,10 @@ class MWBlas:
             self._sig("mrot" + suf, None, [PI, _p, PI, _p, PI, R, R])
             self._sig("wmrot" + suf, None, [PI, _p, PI, _p, PI, R, R])
             self._sig("mrotm" + suf, None, [PI, _p, PI, _p, PI, _p])
+            self._sig("mcabs1" + suf, Real64x2, [_p])
+            self._sig("mrotg" + suf, None, [_p] * 4)
+            self._sig("mrotmg" + suf, None, [_p] * 5)
+            self._sig("wrotg" + suf, None, [_p] * 4)
             # level 2 beyond mgemv (all scalars and arrays passed as pointers)
             for nm, na in (("wgemv", 11), ("mgbmv", 13), ("wgbmv", 13), ("msymv", 10), ("whemv", 10),
                            ("msbmv", 11), ("whbmv", 11), ("mspmv", 9), ("whpmv", 9), ("mtrmv", 8), ("wtrmv", 8),
@@ -278,6 +282,13 @@ class MWBlas:
         I = lambda v: self._I(v, wide)
         p = np.ascontiguousarray(np.asarray(param, dtype=np.float64).reshape(5, 2))
         (self.lib.mrotm_64_ if wide else self.lib.mrotm_)(I(n), _ptr(x), I(incx), _ptr(y), I(incy), _ptr(p))
+
+    def generator(self, name, *bufs, wide=True):
+        """mcabs1 / mrotg / mrotmg / wrotg on float64 arrays, in the reference's
+        argument order (modified in place); mcabs1 returns its (2,) value."""
+        f = getattr(self.lib, name + ("_64_" if wide else "_"))
+        r = f(*[_ptr(b) for b in bufs])
+        return np.array([r.limbs[0], r.limbs[1]]) if name == "mcabs1" else None
 
     def l2(self, name, *args, wide=True):
         """Level-2 routines beyond mgemv: arguments in the Fortran order; str

@@ -352,6 +352,24 @@ void mrotm_(const int *n, MWBLAS_R *x, const int *incx, MWBLAS_R *y, const int *
 void mrotm_64_(const int64_t *n, MWBLAS_R *x, const int64_t *incx, MWBLAS_R *y, const int64_t *incy,
                const MWBLAS_R *dparam);
 
+/* Scalar generators, computed by one device thread in double-double.
+ * mcabs1_: |Re z| + |Im z| (multifloats/mcabs1.cpp:20-25).
+ * mrotg_: Givens rotation of (a, b); on return a = r, b = z
+ *   (multifloats/mrotg.cpp:21-35).
+ * mrotmg_: modified Givens (DROTMG); updates d1, d2, x1 and the dparam
+ *   entries the flag uses (multifloats/mrotmg.cpp:25-110).
+ * wrotg_: complex Givens; a := r, real c, complex s (multifloats/wrotg.cpp:27-52).
+ * The arguments are host variables.  No integer arguments, so each _64_ twin
+ * has the same signature. */
+MWBLAS_R mcabs1_(const MWBLAS_C *z);
+MWBLAS_R mcabs1_64_(const MWBLAS_C *z);
+void mrotg_(MWBLAS_R *a, MWBLAS_R *b, MWBLAS_R *c, MWBLAS_R *s);
+void mrotg_64_(MWBLAS_R *a, MWBLAS_R *b, MWBLAS_R *c, MWBLAS_R *s);
+void mrotmg_(MWBLAS_R *d1, MWBLAS_R *d2, MWBLAS_R *x1, const MWBLAS_R *y1, MWBLAS_R *dparam);
+void mrotmg_64_(MWBLAS_R *d1, MWBLAS_R *d2, MWBLAS_R *x1, const MWBLAS_R *y1, MWBLAS_R *dparam);
+void wrotg_(MWBLAS_C *a, const MWBLAS_C *b, MWBLAS_R *c, MWBLAS_C *s);
+void wrotg_64_(MWBLAS_C *a, const MWBLAS_C *b, MWBLAS_R *c, MWBLAS_C *s);
+
 /* sum x(i)*y(i).  Replaces mdot_/mdot_64_ (multifloats/mdot.cpp:127-148). */
 MWBLAS_R mdot_(const int *n, const MWBLAS_R *x, const int *incx, const MWBLAS_R *y,
                const int *incy);

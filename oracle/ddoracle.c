@@ -341,6 +341,165 @@ int64_t or_iwamax(int64_t n, const cdd *x, int64_t incx)
     return best;
 }
 
+/* ====================== scalar generators ================================== */
+/* Double-double division and square root, step for step as the shim's
+ * operator/ and sqrtdd (Hida, Li and Bailey 2001 accurate division; Karp and
+ * Markstein 1997 square root); the reference does not describe either. */
+static inline dd dd_div(dd a, dd b)
+{
+    double q1 = a.hi / b.hi;
+    dd t = {q1, 0.0};
+    dd r = sub_exact(a, mul_exact(t, b));
+    double q2 = r.hi / b.hi;
+    t.hi = q2;
+    r = sub_exact(r, mul_exact(t, b));
+    double q3 = r.hi / b.hi;
+    dd q;
+    fast_two_sum(q1, q2, &q.hi, &q.lo);
+    dd q3d = {q3, 0.0};
+    return add_exact(q, q3d);
+}
+
+static inline dd dd_sqrt(dd v)
+{
+    dd out = {0.0, 0.0};
+    if (v.hi <= 0.0) { out.hi = v.hi == 0.0 ? 0.0 : NAN; return out; }
+    double s = sqrt(v.hi), p, e;
+    two_prod(s, s, &p, &e);
+    dd pe = {p, e};
+    dd r = sub_exact(v, pe);
+    double t = r.hi / (2.0 * s);
+    fast_two_sum(s, t, &out.hi, &out.lo);
+    return out;
+}
+
+/* mf_pred.h:54-70 */
+static inline int dlt0(dd x) { return x.hi < 0.0 || (x.hi == 0.0 && x.lo < 0.0); }
+static inline int dgt0(dd x) { return x.hi > 0.0 || (x.hi == 0.0 && x.lo > 0.0); }
+static inline dd dmag(dd a) { return dlt0(a) ? dneg(a) : a; }
+static inline dd dmk(double h) { dd r = {h, 0.0}; return r; }
+
+/* mcabs1.cpp:20-24 */
+dd or_mcabs1(const cdd *z) { return add_exact(dmag(z->re), dmag(z->im)); }
+
+/* mrotg.cpp:21-34 (fabsdd is the limb-negating magnitude) */
+void or_mrotg(dd *a, dd *b, dd *c, dd *s)
+{
+    dd an = a->hi < 0.0 ? dneg(*a) : *a, bn = b->hi < 0.0 ? dneg(*b) : *b;
+    if (eq0(bn)) { *c = dmk(1.0); *s = dmk(0.0); *b = dmk(0.0); return; }
+    if (eq0(an)) { *c = dmk(0.0); *s = dmk(1.0); *a = *b; *b = dmk(1.0); return; }
+    dd r = dd_sqrt(add_exact(mul_exact(an, an), mul_exact(bn, bn)));
+    if (dgt(dmk(0.0), *a)) r = dneg(r);
+    *c = dd_div(*a, r);
+    *s = dd_div(*b, r);
+    dd z = dgt(an, bn) ? *s : dd_div(dmk(1.0), *c);
+    *a = r;
+    *b = z;
+}
+
+/* mrotmg.cpp:25-106 (DROTMG) */
+void or_mrotmg(dd *d1p, dd *d2p, dd *x1p, const dd *y1p, dd *dparam)
+{
+    const dd zero = dmk(0.0), one = dmk(1.0), mone = dmk(-1.0);
+    const dd gam = dmk(4096.0), gamsq = dmk(16777216.0), rgamsq = dmk(5.9604645e-8);
+    dd d1 = *d1p, d2 = *d2p, x1 = *x1p, y1 = *y1p;
+    dd flag, h11 = zero, h12 = zero, h21 = zero, h22 = zero;
+    if (dlt0(d1)) {
+        flag = mone;
+        d1 = d2 = x1 = zero;
+    } else {
+        dd p2 = mul_exact(d2, y1);
+        if (eq0(p2)) { dparam[0] = dmk(-2.0); return; }
+        dd p1 = mul_exact(d1, x1), q2 = mul_exact(p2, y1), q1 = mul_exact(p1, x1);
+        if (dgt(dmag(q1), dmag(q2))) {
+            h21 = dd_div(dneg(y1), x1);
+            h12 = dd_div(p2, p1);
+            dd u = sub_exact(one, mul_exact(h12, h21));
+            if (dgt0(u)) {
+                flag = zero;
+                d1 = dd_div(d1, u); d2 = dd_div(d2, u); x1 = mul_exact(x1, u);
+            } else {
+                flag = mone;
+                h11 = h12 = h21 = h22 = zero;
+                d1 = d2 = x1 = zero;
+            }
+        } else if (dlt0(q2)) {
+            flag = mone;
+            h11 = h12 = h21 = h22 = zero;
+            d1 = d2 = x1 = zero;
+        } else {
+            flag = one;
+            h11 = dd_div(p1, p2);
+            h22 = dd_div(x1, y1);
+            dd u = add_exact(one, mul_exact(h11, h22));
+            dd t = dd_div(d2, u);
+            d2 = dd_div(d1, u);
+            d1 = t;
+            x1 = mul_exact(y1, u);
+        }
+        if (!eq0(d1)) {
+            while (!dgt(d1, rgamsq) || !dgt(gamsq, d1)) {
+                if (eq0(flag)) { h11 = one; h22 = one; } else { h21 = mone; h12 = one; }
+                flag = mone;
+                if (!dgt(d1, rgamsq)) {
+                    d1 = mul_exact(mul_exact(d1, gam), gam);
+                    x1 = dd_div(x1, gam); h11 = dd_div(h11, gam); h12 = dd_div(h12, gam);
+                } else {
+                    d1 = dd_div(d1, mul_exact(gam, gam));
+                    x1 = mul_exact(x1, gam); h11 = mul_exact(h11, gam); h12 = mul_exact(h12, gam);
+                }
+            }
+        }
+        if (!eq0(d2)) {
+            dd ad2 = dmag(d2);
+            while (!dgt(ad2, rgamsq) || !dgt(gamsq, ad2)) {
+                if (eq0(flag)) { h11 = one; h22 = one; } else { h21 = mone; h12 = one; }
+                flag = mone;
+                if (!dgt(ad2, rgamsq)) {
+                    d2 = mul_exact(mul_exact(d2, gam), gam);
+                    h21 = dd_div(h21, gam); h22 = dd_div(h22, gam);
+                } else {
+                    d2 = dd_div(d2, mul_exact(gam, gam));
+                    h21 = mul_exact(h21, gam); h22 = mul_exact(h22, gam);
+                }
+                ad2 = dmag(d2);
+            }
+        }
+    }
+    dparam[0] = flag;
+    if (dlt0(flag)) { dparam[1] = h11; dparam[2] = h21; dparam[3] = h12; dparam[4] = h22; }
+    else if (eq0(flag)) { dparam[3] = h12; dparam[2] = h21; }
+    else { dparam[1] = h11; dparam[4] = h22; }
+    *d1p = d1; *d2p = d2; *x1p = x1;
+}
+
+/* wrotg.cpp:27-48 */
+void or_wrotg(cdd *a, const cdd *b, dd *c, cdd *s)
+{
+    dd g2 = add_exact(mul_exact(b->re, b->re), mul_exact(b->im, b->im));
+    if (eq0(g2)) { *c = dmk(1.0); s->re = s->im = dmk(0.0); return; }
+    dd f2 = add_exact(mul_exact(a->re, a->re), mul_exact(a->im, a->im));
+    if (eq0(f2)) {
+        *c = dmk(0.0);
+        dd d = dd_sqrt(g2);
+        s->re = dd_div(b->re, d);
+        s->im = dd_div(dneg(b->im), d);
+        a->re = d;
+        a->im = dmk(0.0);
+        return;
+    }
+    dd h2 = add_exact(f2, g2);
+    *c = dd_sqrt(dd_div(f2, h2));
+    cdd av = *a;
+    a->re = dd_div(av.re, *c);
+    a->im = dd_div(av.im, *c);
+    dd d = dd_sqrt(mul_exact(f2, h2));
+    cdd bc = {b->re, dneg(b->im)};
+    cdd p = cmul_exact(bc, av);
+    s->re = dd_div(p.re, d);
+    s->im = dd_div(p.im, d);
+}
+
 /* ====================== binary128 helpers ================================= */
 static inline qreal q_of(dd a) { return (qreal)a.hi + (qreal)a.lo; }
 static inline dd dd_of(qreal q)

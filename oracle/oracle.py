@@ -40,6 +40,15 @@ def _ptr(a):
     return a.ctypes.data
 
 
+class DD2(C.Structure):
+    """A double-double returned by value (two doubles, hi first)."""
+    _fields_ = [("hi", C.c_double), ("lo", C.c_double)]
+
+
+# generator -> number of pointer arguments
+GENERATORS = {"mcabs1": 1, "mrotg": 4, "mrotmg": 5, "wrotg": 4}
+
+
 class Oracle:
     def __init__(self, path: str = LIB):
         if not os.path.exists(path):
@@ -79,6 +88,16 @@ class Oracle:
             f.argtypes = [_i64, _p, _i64]
             f.restype = _i64
         L.or_max_threads.restype = C.c_int
+        for name, nargs in GENERATORS.items():
+            f = getattr(L, "or_" + name)
+            f.argtypes = [_p] * nargs
+            f.restype = DD2 if name == "mcabs1" else None
+
+    # scalar generators (mcabs1.cpp, mrotg.cpp, mrotmg.cpp, wrotg.cpp), with the
+    # reference's argument order; float64 arrays are modified in place
+    def generator(self, name, *bufs):
+        r = getattr(self.lib, "or_" + name)(*[_ptr(b) for b in bufs])
+        return np.array([r.hi, r.lo]) if name == "mcabs1" else None
 
     # bit-exact level 1 (arrays modified in place)
     def mscal(self, n, alpha, x, incx, team=1):

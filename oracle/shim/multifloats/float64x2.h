@@ -151,4 +151,26 @@ static inline bool operator!=(const float64x2 &a, double b) { return a != float6
 
 static inline float64x2 abs(const float64x2 &a) { return (a.limbs[0] < 0.0) ? -a : a; }
 
+/* fabsdd / sqrtdd (used by the Givens generators mrotg.cpp, wrotg.cpp).
+ * Neither is described in the reference. fabsdd is the limb-negating
+ * magnitude above. sqrtdd is written from Karp and Markstein (1997, "High
+ * precision division and square root"): the FP64 root s of the hi limb,
+ * corrected once by the exactly formed residual, s + (v - s*s) / (2s).
+ * Its last bits are therefore unpinned against upstream. */
+static inline float64x2 fabsdd(const float64x2 &a) { return abs(a); }
+
+static inline float64x2 sqrtdd(const float64x2 &v)
+{
+    using namespace shim_detail;
+    if (v.limbs[0] <= 0.0) return float64x2{{v.limbs[0] == 0.0 ? 0.0 : std::nan(""), 0.0}};
+    double s = std::sqrt(v.limbs[0]);
+    double p, e;
+    two_prod(s, s, p, e);
+    float64x2 r = v - float64x2{{p, e}};
+    double t = r.limbs[0] / (2.0 * s);
+    float64x2 out;
+    fast_two_sum(s, t, out.limbs[0], out.limbs[1]);
+    return out;
+}
+
 }  // namespace multifloats

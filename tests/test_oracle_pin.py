@@ -144,3 +144,76 @@ def test_live_reference_bitexact_random(oracle):
         oracle.mscal(n, a, r2, 1, team=1)
         np.testing.assert_array_equal(r1, r2)
         assert ref.imamax(n, xv, 1) == oracle.imamax(n, xv, 1)
+
+
+# ---- scalar generators (mcabs1, mrotg, mrotmg, wrotg) ------------------------------------
+
+def _generators():
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "make_generators.py")
+    spec = importlib.util.spec_from_file_location("make_generators", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod, np.load(path.replace("make_generators.py", "ref_generators.npz"))
+
+
+@pytest.mark.parametrize("name", ["mcabs1", "mrotg", "mrotmg", "wrotg"])
+def test_generators_match_reference(oracle, name):
+    """The oracle's restatements reproduce the reference's generators bit for
+    bit, including which outputs each branch leaves untouched."""
+    mg, z = _generators()
+    got = mg.run(lambda n: getattr(oracle.lib, "or_" + n), name, z[name + "_in"])
+    np.testing.assert_array_equal(got.view(np.uint64), z[name + "_out"].view(np.uint64))
+
+
+def _exact_generator(name, x):
+    """The same algorithms in 80-digit decimal arithmetic (an output the branch
+    does not write keeps its input value)."""
+    from decimal import Decimal, getcontext
+    getcontext().prec = 80
+    D = lambda v: Decimal(float(v[0])) + Decimal(float(v[1]))
+    if name == "mcabs1":
+        return [abs(D(x[0])) + abs(D(x[1]))]
+    if name == "mrotg":
+        a, b = D(x[0]), D(x[1])
+        if b == 0:
+            return [a, Decimal(0), Decimal(1), Decimal(0)]
+        if a == 0:
+            return [b, Decimal(1), Decimal(0), Decimal(1)]
+        r = (a * a + b * b).sqrt()
+        r = -r if a < 0 else r
+        c, s = a / r, b / r
+        return [r, s if abs(a) > abs(b) else 1 / c, c, s]
+    if name == "wrotg":
+        ar, ai, br, bi = D(x[0, 0]), D(x[0, 1]), D(x[1, 0]), D(x[1, 1])
+        g2 = br * br + bi * bi
+        if g2 == 0:
+            return [ar, ai, Decimal(1), Decimal(0), Decimal(0)]
+        f2 = ar * ar + ai * ai
+        if f2 == 0:
+            d = g2.sqrt()
+            return [d, Decimal(0), Decimal(0), br / d, -bi / d]
+        h2 = f2 + g2
+        c = (f2 / h2).sqrt()
+        d = (f2 * h2).sqrt()
+        return [ar / c, ai / c, c, (br * ar + bi * ai) / d, (br * ai - bi * ar) / d]
+    raise ValueError(name)
+
+
+@pytest.mark.parametrize("name", ["mcabs1", "mrotg", "wrotg"])
+def test_generators_accuracy(oracle, name):
+    """Against the exact formulas: relative error within the reference's
+    consistency tolerance (100 eps, fuzz_mrotg.fypp:34, fuzz_wrotg.fypp:39;
+    10 eps for mcabs1, fuzz_mcabs1.fypp:34), so the unpinned division and
+    square root are accurate ones."""
+    from decimal import Decimal
+    mg, z = _generators()
+    got = mg.run(lambda n: getattr(oracle.lib, "or_" + n), name, z[name + "_in"])
+    tol = (10 if name == "mcabs1" else 100) * orc.EPS_DD
+    for x, g in zip(z[name + "_in"], got):
+        want = _exact_generator(name, x)
+        for w, gv in zip(want, g):
+            d = abs(Decimal(float(gv[0])) + Decimal(float(gv[1])) - w)
+            scale = abs(w) if w != 0 else Decimal(1)
+            assert float(d / scale) <= tol, (name, x, gv, w)
