@@ -434,7 +434,7 @@ def tc_traffic_from_profile():
 
 WORKLOADS = ("gemm", "stress", "wgemm", "gemm_t", "gemm_fixed", "gemm_plain", "syrk", "herk", "trsm", "gemv", "dot",
              "axpy", "scal", "copy", "swap", "iamax", "batched_gemm", "batched_trsm", "gemmtr", "symm", "syr2k",
-             "trmm", "wtrsm")
+             "trmm", "wtrsm", "sbmv", "spmv")
 
 
 def _dev_dd(torch, shape, gen, dev, cplx_=False):
@@ -805,6 +805,54 @@ def run_workload(args):
             amax = float(A[..., 0].abs().max())
             op = orc.dd_abs(al) * n * amax * orc.dd_absmax(hb(x)) + orc.dd_abs(be) * orc.dd_absmax(hb(y0))
             check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
+    elif w in ("sbmv", "spmv"):
+        # symmetric band (k = 16, n = 2^22) / packed (n = 16384) matrix-vector
+        # products, A read in place from its band or packed storage
+        band = w == "sbmv"
+        n = args.size or ((1 << 22) if band else 16384)
+        k = 16
+        nst = n * (k + 1) if band else n * (n + 1) // 2
+        A = _dev_dd(torch, (n, k + 1) if band else (nst,), gen, dev)
+        x = _dev_dd(torch, (n,), gen, dev)
+        y = _dev_dd(torch, (n,), gen, dev)
+        y0 = y.clone()
+        if band:
+            fn = lambda: lib.l2("msbmv", "U", n, k, al, (A.data_ptr(),), k + 1, (x.data_ptr(),), 1, be,
+                                (y.data_ptr(),), 1)
+        else:
+            fn = lambda: lib.l2("mspmv", "U", n, al, (A.data_ptr(),), (x.data_ptr(),), 1, be, (y.data_ptr(),), 1)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: y.copy_(y0))
+        nbytes = 16.0 * (nst + 3 * n)
+        value, unit = nbytes / ms / 1e6, "GB/s"
+        metric = (f"DD-{'SBMV' if band else 'SPMV'} HBM GB/s n={n}" + (f" k={k}" if band else "")
+                  + " (16(stored + 3n) bytes)")
+        cfg = {"workload": f"m{w}_ U n={n}" + (f" k={k}" if band else "") + " incx=incy=1"}
+        roof = {"bound": "hbm", "achieved": value, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": value / pk["hbm_gbs"], "peak_kind": pk_kind, "traffic": None}
+        if o:
+            y.copy_(y0)
+            fn()
+            rows = np.sort(rng.choice(n, 32, replace=False))
+            hx, hy0, hy = hb(x), hb(y0), hb(y)
+            got, want = [], []
+            for r in rows:
+                c0, c1 = (max(0, r - k), min(n - 1, r + k)) if band else (0, n - 1)
+                cs = np.arange(c0, c1 + 1)
+                i, j = np.minimum(cs, r), np.maximum(cs, r)           # stored upper entry (i <= j)
+                if band:
+                    idx = torch.as_tensor(j * (k + 1) + (k + i - j), device=dev)
+                    row = A.reshape(-1, 2)[idx]
+                else:
+                    row = A[torch.as_tensor(i + j * (j + 1) // 2, device=dev)]
+                rv = np.ascontiguousarray(hb(row)[:, None, :])           # 1 x len, lda 1
+                yr = hy0[r:r + 1].copy()
+                o.qgemv("N", 1, len(cs), al, rv, 1, np.ascontiguousarray(hx[c0:c1 + 1]), 1, be, yr, 1)
+                want.append(yr[0])
+                got.append(hy[r])
+            op = orc.dd_abs(al) * (2 * k + 1 if band else n) * orc.dd_absmax(hb(A[:1 << 20])) * orc.dd_absmax(hx) \
+                + orc.dd_abs(be) * orc.dd_absmax(hy0)
+            check["normwise_err_sampled"] = orc.normwise_error(np.array(got), np.array(want), op)
+            check["rows_checked"] = len(rows)
     elif w in ("scal", "copy", "swap", "iamax"):
         # HBM-bound level-1 moves at n = 2^28 (SCAL bit-exact, FP64-bound by its operation sequence)
         n = args.size or (1 << 28)

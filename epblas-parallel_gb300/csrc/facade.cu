@@ -967,25 +967,43 @@ void gemv2_entry(const char *routine, bool cplx, bool band, const char *trans, c
     sc.add(SA); sc.add(SX); sc.add(SY);
     int64_t dix = 1, diy;
     if (!stage_vector(SY, y, v.leny, *incy, es, v.beta_kind != 0, diy, routine)) return;
-    void *dense = nullptr;
     v.alpha_zero = alpha0;
     if (!alpha0) {
         if (!stage_vector(SX, x, v.lenx, *incx, es, true, dix, routine)) return;
         if (!stage_matrix(SA, a, band ? (KL + KU + 1) : M, N, *lda, es, true, routine)) return;
-        if (band) {
-            dense = dev_alloc((size_t)M * N * es, routine);
-            if (!dense) return;
-            band_expand(M, N, KL, KU, SA.dev, *lda, e2, 0, false, false, dense);
-        }
     }
-    v.A = band ? dense : SA.dev;
-    v.lda = band ? M : *lda;
-    v.x = SX.dev;
-    v.incx = dix;
-    v.y = SY.dev;
-    v.incy = diy;
-    const bool ok = mv_device(v, routine);
-    if (dense) dev_free(dense);
+    bool ok;
+    if (band && !alpha0) {
+        SmvArgs b;
+        b.cplx = cplx;
+        b.fmt = 1;
+        b.kind = 0;
+        b.trans = T;
+        b.rows = v.leny;
+        b.cols = v.lenx;
+        b.kl = KL;
+        b.ku = KU;
+        b.ldab = *lda;
+        b.A = SA.dev;
+        b.x = SX.dev;
+        b.incx = dix;
+        b.y = SY.dev;
+        b.incy = diy;
+        b.alpha = v.alpha;
+        b.beta = v.beta;
+        b.calpha = v.calpha;
+        b.cbeta = v.cbeta;
+        b.beta_kind = v.beta_kind;
+        ok = smv_device(b, routine);
+    } else {
+        v.A = SA.dev;
+        v.lda = *lda;
+        v.x = SX.dev;
+        v.incx = dix;
+        v.y = SY.dev;
+        v.incy = diy;
+        ok = mv_device(v, routine);
+    }
     if (!ok) return;
     if (!unstage_vector(SY, routine)) return;
     finish(routine);
@@ -1032,35 +1050,49 @@ void symv_entry(const char *routine, bool cplx, bool herm, int fmt, const char *
         if (!mv_device(v, routine)) return;
     } else {
         if (!stage_vector(SX, x, N, *incx, es, true, dix, routine)) return;
-        void *dense = nullptr;
+        bool ok;
         if (fmt == 0) {
             if (!stage_matrix(SA, a, N, N, *lda, es, true, routine)) return;
+            v.shape = herm ? MV_HERMITIAN : MV_SYMMETRIC;
+            v.trans = 'N';
+            v.uplo = U;
+            v.lenx = N;
+            v.leny = N;
+            v.A = SA.dev;
+            v.lda = *lda;
+            v.x = SX.dev;
+            v.incx = dix;
+            v.y = SY.dev;
+            v.incy = diy;
+            ok = mv_device(v, routine);
         } else {
-            const int64_t len = fmt == 1 ? 0 : N * (N + 1) / 2;
+            const int64_t len = N * (N + 1) / 2;
             if (fmt == 1) {
                 if (!stage_matrix(SA, a, K + 1, N, *lda, es, true, routine)) return;
             } else {
                 if (!stage_matrix(SA, a, len, 1, len, es, true, routine)) return;
             }
-            dense = dev_alloc((size_t)N * N * es, routine);
-            if (!dense) return;
-            if (fmt == 1) band_expand(N, N, U == 'L' ? K : 0, U == 'U' ? K : 0, SA.dev, *lda, e2, herm ? 2 : 1,
-                                      U == 'U', false, dense);
-            else pack_move(N, SA.dev, e2, U == 'U', dense, true);
+            SmvArgs b;
+            b.cplx = cplx;
+            b.fmt = fmt;
+            b.kind = herm ? 2 : 1;
+            b.upper = U == 'U';
+            b.rows = b.cols = b.n = N;
+            b.kl = U == 'L' ? K : 0;
+            b.ku = U == 'U' ? K : 0;
+            b.ldab = fmt == 1 ? *lda : 1;
+            b.A = SA.dev;
+            b.x = SX.dev;
+            b.incx = dix;
+            b.y = SY.dev;
+            b.incy = diy;
+            b.alpha = v.alpha;
+            b.beta = v.beta;
+            b.calpha = v.calpha;
+            b.cbeta = v.cbeta;
+            b.beta_kind = v.beta_kind;
+            ok = smv_device(b, routine);
         }
-        v.shape = (fmt == 1) ? MV_GENERAL : (herm ? MV_HERMITIAN : MV_SYMMETRIC);
-        v.trans = 'N';
-        v.uplo = U;
-        v.lenx = N;
-        v.leny = N;
-        v.A = fmt == 0 ? SA.dev : dense;
-        v.lda = fmt == 0 ? *lda : N;
-        v.x = SX.dev;
-        v.incx = dix;
-        v.y = SY.dev;
-        v.incy = diy;
-        const bool ok = mv_device(v, routine);
-        if (dense) dev_free(dense);
         if (!ok) return;
     }
     if (!unstage_vector(SY, routine)) return;
@@ -1097,6 +1129,35 @@ void trv_entry(const char *routine, bool cplx, bool solve, int fmt, const char *
     if (!stage_vector(SX, x, N, *incx, es, true, dix, routine)) return;
     void *dense = nullptr;
     char Dd = D;
+    if (fmt != 0 && !solve) {
+        // x := op(A) x with A read in place from its band or packed storage
+        const int64_t len = N * (N + 1) / 2;
+        if (fmt == 1) {
+            if (!stage_matrix(SA, a, K + 1, N, *lda, es, true, routine)) return;
+        } else {
+            if (!stage_matrix(SA, a, len, 1, len, es, true, routine)) return;
+        }
+        SmvArgs b;
+        b.cplx = cplx;
+        b.fmt = fmt;
+        b.kind = 3;
+        b.trans = T;
+        b.upper = U == 'U';
+        b.unit = D == 'U';
+        b.rows = b.cols = b.n = N;
+        b.kl = U == 'L' ? K : 0;
+        b.ku = U == 'U' ? K : 0;
+        b.ldab = fmt == 1 ? *lda : 1;
+        b.A = SA.dev;
+        b.x = SX.dev;
+        b.incx = dix;
+        b.y = SX.dev;   // x is gathered before y is written
+        b.incy = dix;
+        if (!smv_device(b, routine)) return;
+        if (!unstage_vector(SX, routine)) return;
+        finish(routine);
+        return;
+    }
     if (fmt == 0) {
         if (!stage_matrix(SA, a, N, N, *lda, es, true, routine)) return;
     } else {

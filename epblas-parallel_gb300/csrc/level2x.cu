@@ -14,6 +14,7 @@
 // (exact fixed point or tensor-core residues) and the error bounds are the
 // level-3 ones.
 #include "dd.cuh"
+#include "fixacc.cuh"
 #include "level2x.h"
 #include "level3.h"
 #include "level3x.h"
@@ -121,6 +122,197 @@ __global__ void k_pack(int64_t n, double2 *AP, int e2, bool upper, double2 *dens
     }
 }
 
+// ---- band and packed matrix-vector products, read in place ---------------------------
+// Row r of op(A) has its stored entries in the columns [r - lo, r + hi]; each
+// is decoded into the fixed point of fixacc.cuh and multiplied with x exactly
+// (as DOT and GEMV), one thread (T = 1) or one warp (T = 32, lanes over the
+// columns, partial sums combined in a fixed order) per output element, then
+// y := beta*y + alpha*s with one rounding. Traffic is the stored entries and
+// the vectors, O(n k) for a band, instead of the O(n^2) of a dense copy.
+
+// Kernel parameters of smv_device (vectors contiguous).
+struct SmvParams {
+    int64_t rows, cols, n, kl, ku, ldab;
+    const double2 *A;
+    int fmt, kind, op;   // op 0 'N', 1 'T', 2 'C'
+    bool upper, unit;
+    const double2 *x;
+    double2 *y;
+    dd::real ar, ai, br, bi;
+    int beta_kind;
+};
+
+__device__ __forceinline__ void smv_range(const SmvParams &p, int64_t r, int64_t &c0, int64_t &c1)
+{
+    int64_t lo, hi;
+    if (p.kind == 0) {
+        lo = p.op == 0 ? p.kl : p.ku;
+        hi = p.op == 0 ? p.ku : p.kl;
+    } else {
+        const int64_t k = p.fmt == 2 ? p.n - 1 : (p.upper ? p.ku : p.kl);
+        if (p.kind != 3) {
+            lo = hi = k;
+        } else {
+            const bool right = p.upper == (p.op == 0);   // stored entries right of the diagonal
+            lo = right ? 0 : k;
+            hi = right ? k : 0;
+        }
+    }
+    c0 = r - lo < 0 ? 0 : r - lo;
+    c1 = r + hi > p.cols - 1 ? p.cols - 1 : r + hi;
+}
+
+// Position of stored entry (i, j): packed upper i + j(j+1)/2, packed lower
+// i + j(2n-j-1)/2, band AB(ku + i - j, j) (ku = 0 for a lower triangle).
+__device__ __forceinline__ int64_t smv_addr(const SmvParams &p, int64_t i, int64_t j)
+{
+    if (p.fmt == 2) return p.upper ? i + j * (j + 1) / 2 : i + j * (2 * p.n - j - 1) / 2;
+    return (p.ku + i - j) + j * p.ldab;
+}
+
+template <bool CX>
+__device__ __forceinline__ void smv_elem(const SmvParams &p, int64_t r, int64_t c, fx::Op &er, fx::Op &ei)
+{
+    int64_t i, j;
+    bool cj, realdiag = false;
+    if (p.kind == 1 || p.kind == 2) {
+        const bool stored = p.upper ? r <= c : r >= c;
+        i = stored ? r : c;
+        j = stored ? c : r;
+        cj = !stored && p.kind == 2;
+        realdiag = p.kind == 2 && r == c;
+    } else {
+        i = p.op == 0 ? r : c;
+        j = p.op == 0 ? c : r;
+        cj = p.op == 2;
+        if (p.kind == 3 && p.unit && i == j) {
+            er = fx::decode(make_double2(1.0, 0.0));
+            ei = fx::decode(make_double2(0.0, 0.0));
+            return;
+        }
+    }
+    const double2 *a = p.A + (CX ? 2 : 1) * smv_addr(p, i, j);
+    er = fx::decode(a[0]);
+    if (CX) {
+        ei = fx::decode(realdiag ? make_double2(0.0, 0.0) : a[1]);
+        if (cj) ei.flags ^= fx::kNeg;
+    }
+}
+
+__device__ __forceinline__ xfp::XF xneg(xfp::XF v)
+{
+    if (!v.zero) v.neg = !v.neg;
+    return v;
+}
+
+__device__ __forceinline__ xfp::XF xzero()
+{
+    xfp::XF z;
+    z.zero = true;
+    z.neg = false;
+    z.m = 0;
+    z.e = 0;
+    return z;
+}
+
+// y := b + t, one rounding (b = beta*y as a double-double; non-finite b is
+// added in double-double as the reference's operator+ would).
+__device__ __forceinline__ double2 smv_round(dd::real b, bool have_b, xfp::XF t)
+{
+    double h, l;
+    if (have_b && !fx::finite_dd(make_double2(b.hi, b.lo))) {
+        xfp::xf_to_dd(t, h, l);
+        const dd::real s = dd::add_exact(b, dd::make(h, l));
+        return make_double2(s.hi, s.lo);
+    }
+    if (have_b) t = xfp::xf_add(xfp::xf_from_dd(b.hi, b.lo), t);
+    xfp::xf_to_dd(t, h, l);
+    return make_double2(h, l);
+}
+
+template <bool CX, int T>
+__global__ void __launch_bounds__(256) k_smv(SmvParams p)
+{
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
+    const int lane = T == 1 ? 0 : (threadIdx.x & 31);
+    const int64_t teams = (int64_t)gridDim.x * blockDim.x / T;
+    for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / T; r < p.rows; r += teams) {
+        int64_t c0, c1;
+        smv_range(p, r, c0, c1);
+        fx::Acc acc[CX ? 2 : 1];
+        xfp::XF tot[CX ? 2 : 1];
+        bool bad = false;
+        for (int w = 0; w < (CX ? 2 : 1); ++w) {
+            acc[w].reset();
+            tot[w] = xzero();
+        }
+        int cnt = 0;
+        for (int64_t c = c0 + lane; c <= c1; c += T) {
+            fx::Op er, ei;
+            smv_elem<CX>(p, r, c, er, ei);
+            if (CX) {
+                const fx::Op xr = fx::decode(p.x[2 * c]), xi = fx::decode(p.x[2 * c + 1]);
+                fx::Op nei = ei;
+                nei.flags ^= fx::kNeg;
+                acc[0].add_prod(er, xr);
+                acc[0].add_prod(nei, xi);
+                acc[1].add_prod(er, xi);
+                acc[1].add_prod(ei, xr);
+                cnt += 2;
+            } else {
+                acc[0].add_prod(er, fx::decode(p.x[c]));
+                ++cnt;
+            }
+            if (cnt >= fx::kMaxAdds - 2) {
+                for (int w = 0; w < (CX ? 2 : 1); ++w) {
+                    bad |= acc[w].bad;
+                    tot[w] = xfp::xf_add(tot[w], acc[w].finish());
+                    acc[w].reset();
+                }
+                cnt = 0;
+            }
+        }
+        for (int w = 0; w < (CX ? 2 : 1); ++w) {
+            bad |= acc[w].bad;
+            tot[w] = xfp::xf_add(tot[w], acc[w].finish());
+            if (T == 32) tot[w] = fx::xf_warp_sum(tot[w]);
+        }
+        if (T == 32) bad = __any_sync(0xffffffffu, bad);
+        if (lane != 0) continue;
+        double2 *py = p.y + (CX ? 2 : 1) * r;
+        if (bad) {
+            py[0] = make_double2(nan, nan);
+            if (CX) py[1] = make_double2(nan, nan);
+            continue;
+        }
+        const xfp::XF xar = xfp::xf_from_dd(p.ar.hi, p.ar.lo);
+        if (!CX) {
+            dd::real b = dd::make(0.0, 0.0);
+            if (p.beta_kind == 1) b = dd::load(py);
+            else if (p.beta_kind == 2) b = dd::mul_exact(p.br, dd::load(py));
+            py[0] = smv_round(b, p.beta_kind != 0, xfp::xf_mul(xar, tot[0]));
+        } else {
+            const xfp::XF xai = xfp::xf_from_dd(p.ai.hi, p.ai.lo);
+            const xfp::XF tr = xfp::xf_add(xfp::xf_mul(xar, tot[0]), xneg(xfp::xf_mul(xai, tot[1])));
+            const xfp::XF ti = xfp::xf_add(xfp::xf_mul(xar, tot[1]), xfp::xf_mul(xai, tot[0]));
+            dd::cplx b;
+            b.re = b.im = dd::make(0.0, 0.0);
+            if (p.beta_kind == 1) {
+                b = dd::cload(py);
+            } else if (p.beta_kind == 2) {
+                dd::cplx be;
+                be.re = p.br;
+                be.im = p.bi;
+                b = dd::cmul_exact(be, dd::cload(py));
+            }
+            const double2 yr = smv_round(b.re, p.beta_kind != 0, tr);
+            const double2 yi = smv_round(b.im, p.beta_kind != 0, ti);
+            py[0] = yr;
+            py[1] = yi;
+        }
+    }
+}
+
 struct Buf {
     void *p = nullptr;
     Buf(size_t bytes, const char *routine) { p = dev_alloc(bytes, routine); }
@@ -148,6 +340,64 @@ void pack_move(int64_t n, void *AP, int e2, bool upper, void *dense, bool unpack
 {
     k_pack<<<blocks_for(n * n), kThreads, 0, stream()>>>(n, (double2 *)AP, e2, upper, (double2 *)dense, unpack);
     count_launch();
+}
+
+bool smv_device(const SmvArgs &a, const char *routine)
+{
+    const int e2 = a.cplx ? 2 : 1;
+    const size_t es = 16 * (size_t)e2;
+    Buf xb((size_t)(a.cols > 0 ? a.cols : 1) * es, routine), yb((size_t)(a.rows > 0 ? a.rows : 1) * es, routine);
+    if (!xb.p || !yb.p) return false;
+    vgather(a.cols, a.x, a.incx, e2, xb.p, true);
+    if (a.beta_kind != 0) vgather(a.rows, a.y, a.incy, e2, yb.p, true);
+    SmvParams p;
+    p.rows = a.rows;
+    p.cols = a.cols;
+    p.n = a.n;
+    p.kl = a.kl;
+    p.ku = a.ku;
+    p.ldab = a.ldab;
+    p.A = (const double2 *)a.A;
+    p.fmt = a.fmt;
+    p.kind = a.kind;
+    p.op = a.trans == 'N' ? 0 : (a.trans == 'T' ? 1 : 2);
+    p.upper = a.upper;
+    p.unit = a.unit;
+    p.x = (const double2 *)xb.p;
+    p.y = (double2 *)yb.p;
+    if (a.cplx) {
+        p.ar = dd::make(a.calpha.re.hi, a.calpha.re.lo);
+        p.ai = dd::make(a.calpha.im.hi, a.calpha.im.lo);
+        p.br = dd::make(a.cbeta.re.hi, a.cbeta.re.lo);
+        p.bi = dd::make(a.cbeta.im.hi, a.cbeta.im.lo);
+    } else {
+        p.ar = dd::make(a.alpha.hi, a.alpha.lo);
+        p.ai = dd::make(0.0, 0.0);
+        p.br = dd::make(a.beta.hi, a.beta.lo);
+        p.bi = dd::make(0.0, 0.0);
+    }
+    p.beta_kind = a.beta_kind;
+    // average stored entries per row: a warp per row once rows are long
+    int64_t len;
+    if (a.fmt == 2) len = a.kind == 3 ? (a.n + 1) / 2 : a.n;
+    else if (a.kind == 0) len = a.kl + a.ku + 1;
+    else len = (a.kind == 3 ? 1 : 2) * (a.kl > a.ku ? a.kl : a.ku) + 1;
+    const bool warp = len >= 48;
+    const int64_t threads = a.rows * (warp ? 32 : 1);
+    int64_t blocks = (threads + 255) / 256;
+    const int64_t cap = (int64_t)device_sm_count() * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    if (a.cplx) {
+        if (warp) k_smv<true, 32><<<(unsigned)blocks, 256, 0, stream()>>>(p);
+        else k_smv<true, 1><<<(unsigned)blocks, 256, 0, stream()>>>(p);
+    } else {
+        if (warp) k_smv<false, 32><<<(unsigned)blocks, 256, 0, stream()>>>(p);
+        else k_smv<false, 1><<<(unsigned)blocks, 256, 0, stream()>>>(p);
+    }
+    count_launch();
+    vgather(a.rows, a.y, a.incy, e2, yb.p, false);
+    return true;
 }
 
 bool mv_device(const MvArgs &a, const char *routine)

@@ -33,6 +33,30 @@ bool mv_device(const MvArgs &a, const char *routine);
 bool trv_device(bool cplx, bool solve, char uplo, char trans, char diag, int64_t n, const void *A, int64_t lda,
                 void *x, int64_t incx, const char *routine);
 
+// Band (fmt 1, LAPACK layout, leading dimension ldab) or packed (fmt 2)
+// operand, read in place: y := alpha*op(A)*x + beta*y with op(A) rows x cols.
+// kind 0 general band (kl, ku); 1 symmetric, 2 Hermitian, 3 triangular
+// (unit diagonal when `unit`), the stored triangle given by `upper` with,
+// for a band, kl = 0, ku = k (upper) or kl = k, ku = 0 (lower); n is the
+// order of a packed matrix. x and y have any increment; they may be the same
+// vector when beta_kind == 0 (x is gathered before y is written).
+struct SmvArgs {
+    bool cplx = false;
+    int fmt = 1, kind = 0;
+    char trans = 'N';
+    bool upper = true, unit = false;
+    int64_t rows = 0, cols = 0, n = 0, kl = 0, ku = 0, ldab = 1;
+    const void *A = nullptr;
+    const void *x = nullptr;
+    int64_t incx = 1;
+    void *y = nullptr;
+    int64_t incy = 1;
+    dd_host alpha{1.0, 0.0}, beta{0.0, 0.0};
+    cdd_host calpha{{1.0, 0.0}, {0.0, 0.0}}, cbeta{{0.0, 0.0}, {0.0, 0.0}};
+    int beta_kind = 0;
+};
+bool smv_device(const SmvArgs &a, const char *routine);
+
 // Rank updates: uplo 0: GER (A m x n += alpha x op(y), conj for GERC);
 // uplo 1/2 (upper/lower triangle of the n = m square A): SYR/HER (y null),
 // SYR2/HER2; conj selects the Hermitian forms.
