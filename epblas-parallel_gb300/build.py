@@ -1,7 +1,8 @@
-"""Builds libmwblas_gb300.so from csrc/ with nvcc for sm_103a.
+"""Builds libmwblas_gb300.so (and the static libmwblas_gb300.a) from csrc/
+with nvcc for sm_103a.
 
 Each .cu translation unit is compiled in parallel into _build/, then linked
-into a shared library next to this file. A unit is recompiled only when it or
+into a shared library next to this file and archived beside it. A unit is recompiled only when it or
 any header in csrc/ or include/ is newer than its object.
 
 Usage:  python build.py            (or call build() from Python)
@@ -19,6 +20,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmwblas_gb300.so")
+ARCHIVE = os.path.join(HERE, "libmwblas_gb300.a")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -89,6 +91,16 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+    if not os.path.exists(ARCHIVE) or os.path.getmtime(ARCHIVE) < max(os.path.getmtime(o) for o in objs):
+        # the same objects as a static archive; a program links it with the
+        # static CUDA runtime: -lmwblas_gb300 -lcudart_static -lstdc++ -lpthread -ldl -lrt
+        tmp = ARCHIVE + ".tmp"
+        if os.path.exists(tmp):
+            os.remove(tmp)
+        r = subprocess.run(["ar", "rcs", tmp, *objs], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"archive failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, ARCHIVE)
     return LIB
 
 
