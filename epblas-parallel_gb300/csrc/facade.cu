@@ -82,7 +82,8 @@ struct Scope {
 
 // ---- GEMM dispatch shared by mgemm_/wgemm_ and the level-3 routines ---------------
 
-bool run_gemm(GemmArgs &g, bool cplx, int force_engine, const char *routine)
+// The engine a product of this shape runs on.
+int pick_engine(const GemmArgs &g, bool cplx, int force_engine)
 {
     int eng = force_engine >= 0 ? force_engine : engine();
     if (eng == MWBLAS_GEMM_AUTO) {
@@ -94,6 +95,13 @@ bool run_gemm(GemmArgs &g, bool cplx, int force_engine, const char *routine)
         if (eng == MWBLAS_GEMM_OZAKI && !ozaki_available()) eng = MWBLAS_GEMM_FIXED;
         if (eng == MWBLAS_GEMM_FIXED && cplx) eng = MWBLAS_GEMM_PLAIN;
     }
+    return eng;
+}
+
+bool run_gemm(GemmArgs &g, bool cplx, int force_engine, const char *routine)
+{
+    const int eng = pick_engine(g, cplx, force_engine);
+    if (g.hs && eng != MWBLAS_GEMM_OZAKI && !g.hs->wait_all(routine)) return false;
     if (eng == MWBLAS_GEMM_FIXED && !cplx) return gemm_fixed_real(g, routine);
     if (eng == MWBLAS_GEMM_OZAKI) {
         if (!ozaki_available()) {
@@ -156,6 +164,36 @@ void gemm_entry(const char *routine, bool cplx, int force_engine, const char *tr
 
     Staged SA, SB, SC;
     sc.add(SA); sc.add(SB); sc.add(SC);
+    // Large products on host arrays for the tensor-core engine: the three
+    // uploads run on the copy stream in the order the engine needs them and
+    // C comes back in chunks behind the reconstruction.
+    const double host_bytes = (double)es * ((double)nrowa * (TA == 'N' ? K : M) + (double)nrowb * (TB == 'N' ? N : K) +
+                                            (double)M * N);
+    if (compute && K <= 65536 && M <= INT32_MAX && N <= INT32_MAX && host_bytes >= 64.0 * 1048576.0 &&
+        pick_engine(g, cplx, force_engine) == MWBLAS_GEMM_OZAKI && ozaki_available() && !is_dd_device_pointer(a) &&
+        !is_dd_device_pointer(b) && !is_dd_device_pointer(c)) {
+        HostStage hs;
+        // on every exit: stream(), which frees the buffers, waits for the copies
+        struct JoinCopies {
+            const char *r;
+            ~JoinCopies() { join_copy_stream(r); }
+        } join_guard{routine};
+        if (!stage_matrix_async(SA, a, nrowa, TA == 'N' ? K : M, *lda, es, true, hs.a_ready, routine)) return;
+        if (!stage_matrix_async(SB, b, nrowb, TB == 'N' ? N : K, *ldb, es, true, hs.b_ready, routine)) return;
+        if (!stage_matrix_async(SC, c, M, N, *ldc, es, g.beta_kind != 0, hs.c_ready, routine)) return;
+        hs.c = &SC;
+        g.A = SA.dev; g.lda = *lda;
+        g.B = SB.dev; g.ldb = *ldb;
+        g.C = SC.dev; g.ldc = *ldc;
+        g.hs = &hs;
+        const bool ok = run_gemm(g, cplx, force_engine, routine);
+        // whatever happened, nothing may be freed before the copies are done
+        const bool joined = hs.wait_all(routine) && join_copy_stream(routine);
+        if (!ok || !joined) return;
+        if (!hs.c_written && !unstage_matrix(SC, routine)) return;
+        finish(routine);
+        return;
+    }
     // C is read unless beta == 0.
     if (!stage_matrix(SC, c, M, N, *ldc, es, g.beta_kind != 0, routine)) return;
     g.C = SC.dev; g.ldc = *ldc;

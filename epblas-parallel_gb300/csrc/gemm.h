@@ -6,6 +6,8 @@
 
 namespace mw {
 
+struct HostStage;
+
 struct GemmArgs {
     int64_t m = 0, n = 0, k = 0;
     bool ta = false, tb = false;   // op(X) is a transpose
@@ -22,6 +24,7 @@ struct GemmArgs {
     int64_t ldc = 0;
     int uplo = 0;                  // output triangle: 0 full, 1 upper (i <= j), 2 lower (i >= j)
     bool herm = false;             // complex: force a real diagonal (HERK)
+    HostStage *hs = nullptr;       // operands still being uploaded (Ozaki engine only)
 };
 
 // Plain FP64 error-free-transform engine.

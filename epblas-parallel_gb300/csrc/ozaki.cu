@@ -1443,8 +1443,10 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     }
     const GemmArgs &g = g0;
     const int64_t m = g.m, n = g.n, k = g.k;
-    if (m > INT32_MAX || n > INT32_MAX)   // the reconstruction indexes rows and columns in 32 bits
+    if (m > INT32_MAX || n > INT32_MAX) {   // the reconstruction indexes rows and columns in 32 bits
+        if (g.hs && !g.hs->wait_all(routine)) return false;
         return cplx ? gemm_plain_cplx(g, routine) : gemm_fixed_real(g, routine);
+    }
     const int nc = cplx ? 3 : 1;
     // Real SYRK (op(B) = op(A)^T on the same array): op(B)'s residue rows are
     // op(A)'s, so one conversion serves both operands; both then use the same
@@ -1462,6 +1464,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     if (scal_nonfinite) {
         // Inf/NaN alpha or beta: the FP64 engine propagates them as the
         // reference's operators do.
+        if (g.hs && !g.hs->wait_all(routine)) return false;
         return cplx ? gemm_plain_cplx(g, routine) : gemm_plain_real(g, routine);
     }
     // Inf/NaN entries of A or B need no host round trip: their rows/columns
@@ -1471,9 +1474,17 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     int *ex = (int *)dev_alloc(sizeof(int) * (size_t)(m + n + 2), routine);
     if (!ex) return false;
     int *ea = ex, *eb = ex + m;
+    // Operands still arriving from the host: A's exponents and residues are
+    // computed while B is copied, and C is waited for only by the
+    // reconstruction, so its copy runs under the residue GEMMs.
+    HostStage *hs = g.hs;
     phase_mark(PH_EXP);
+    if (hs && !wait_event(hs->a_ready, routine)) {
+        dev_free(ex);
+        return false;
+    }
     launch_exp_rows_of_op(g.A, g.ta ? k : m, g.ta ? m : k, g.lda, g.ta, E, ea);
-    launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, E, eb);
+    if (!hs) launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, E, eb);
 
     // 2. precision and moduli (complex: |Re|, |Im| <= 2k * 2^(2bits-2))
     int bits = bits_req > 0 ? bits_req : 106;
@@ -1511,6 +1522,10 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         } else {
             if (!g.ta) launch_residues<true, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
             else launch_residues<false, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
+        }
+        if (hs) {
+            wait_event(hs->b_ready, routine);
+            launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, E, eb);
         }
         if (!shared_ops) {
             if (cplx) {
@@ -1566,11 +1581,15 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
 
     // 5. reconstruction + alpha/beta
     phase_mark(PH_REC);
+    if (ok && hs) ok = wait_event(hs->c_ready, routine);
     if (ok) {
+        // C going back to the host: the reconstruction runs in column chunks,
+        // each copied back while the next one is computed
+        const bool chunked = hs && hs->c && g.uplo == 0 && !g.herm;
+        const int64_t cw = chunked ? (n + 7) / 8 : n;
         // a thread per row and several columns: about 16 blocks per SM in all
         const unsigned gx = (unsigned)((m + (cplx ? 255 : 511)) / (cplx ? 256 : 512));
         const int64_t want_y = ((int64_t)device_sm_count() * 16 + gx - 1) / gx;
-        dim3 grid(gx, blocks_cap(want_y < n ? want_y : n));
         xw::XW Mx;
         Mx.w[3] = (uint32_t)(cp.Mhi >> 32);
         Mx.w[2] = (uint32_t)cp.Mhi;
@@ -1578,29 +1597,41 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         Mx.w[0] = (uint32_t)cp.Mlo;
         Mx.e = cp.Me;
         Mx.neg = 0u;
-        if (!cplx) {
-            bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
-            // alpha folded into M: alpha * X = T * (alpha M)
-            const xw::XW aM = alpha_one ? Mx : xw::mul(xw::from_dd(g.alpha.hi, g.alpha.lo), Mx);
-            k_oz_reconstruct<<<grid, 256, 0, stream()>>>((int)m, (int)n, R, Mp, Np, ea, eb, bits, cp, aM,
-                                                        xw::from_dd(g.beta.hi, g.beta.lo),
-                                                        dd::make(g.beta.hi, g.beta.lo), g.beta_kind, (double2 *)g.C,
-                                                        g.ldc, g.uplo);
-        } else {
-            dd::cplx al, be;
-            al.re = dd::make(g.calpha.re.hi, g.calpha.re.lo);
-            al.im = dd::make(g.calpha.im.hi, g.calpha.im.lo);
-            be.re = dd::make(g.cbeta.re.hi, g.cbeta.re.lo);
-            be.im = dd::make(g.cbeta.im.hi, g.cbeta.im.lo);
-            bool alpha_one = (g.calpha.re.hi == 1.0 && g.calpha.re.lo == 0.0 && g.calpha.im.hi == 0.0 &&
-                              g.calpha.im.lo == 0.0);
-            k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>(
-                (int)m, (int)n, R, Mp, Np, ea, eb, bits, cp, Mx, xw::from_dd(al.re.hi, al.re.lo),
-                xw::from_dd(al.im.hi, al.im.lo), alpha_one ? 1 : 0, be, xw::from_dd(be.re.hi, be.re.lo),
-                xw::from_dd(be.im.hi, be.im.lo), g.beta_kind, (double2 *)g.C, g.ldc, g.uplo, g.herm ? 1 : 0,
-                g.herm ? 1 : 0);
+        for (int64_t j0 = 0; ok && j0 < n; j0 += cw) {
+            const int64_t nn = (n - j0 < cw) ? n - j0 : cw;
+            dim3 grid(gx, blocks_cap(want_y < nn ? want_y : nn));
+            const uint16_t *Rj = R + j0 * Mp;     // column j0 of every residue plane
+            double2 *Cj = (double2 *)g.C + (int64_t)E * j0 * g.ldc;
+            if (!cplx) {
+                bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
+                // alpha folded into M: alpha * X = T * (alpha M)
+                const xw::XW aM = alpha_one ? Mx : xw::mul(xw::from_dd(g.alpha.hi, g.alpha.lo), Mx);
+                k_oz_reconstruct<<<grid, 256, 0, stream()>>>((int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits, cp, aM,
+                                                            xw::from_dd(g.beta.hi, g.beta.lo),
+                                                            dd::make(g.beta.hi, g.beta.lo), g.beta_kind, Cj, g.ldc,
+                                                            g.uplo);
+            } else {
+                dd::cplx al, be;
+                al.re = dd::make(g.calpha.re.hi, g.calpha.re.lo);
+                al.im = dd::make(g.calpha.im.hi, g.calpha.im.lo);
+                be.re = dd::make(g.cbeta.re.hi, g.cbeta.re.lo);
+                be.im = dd::make(g.cbeta.im.hi, g.cbeta.im.lo);
+                bool alpha_one = (g.calpha.re.hi == 1.0 && g.calpha.re.lo == 0.0 && g.calpha.im.hi == 0.0 &&
+                                  g.calpha.im.lo == 0.0);
+                k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>(
+                    (int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits, cp, Mx, xw::from_dd(al.re.hi, al.re.lo),
+                    xw::from_dd(al.im.hi, al.im.lo), alpha_one ? 1 : 0, be, xw::from_dd(be.re.hi, be.re.lo),
+                    xw::from_dd(be.im.hi, be.im.lo), g.beta_kind, Cj, g.ldc, g.uplo, g.herm ? 1 : 0,
+                    g.herm ? 1 : 0);
+            }
+            count_launch();
+            if (chunked) ok = unstage_columns_async(*hs->c, j0, j0 + nn, routine);
         }
-        count_launch();
+        if (ok && chunked) {
+            // the buffers are freed on stream(): order that after the copies
+            ok = join_copy_stream(routine);
+            hs->c_written = ok;
+        }
     }
     phase_mark(PH_N);
     dev_free(work);

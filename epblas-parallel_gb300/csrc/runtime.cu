@@ -218,6 +218,90 @@ bool unstage_matrix(Staged &s, const char *routine)
                    routine, "copy matrix to host");
 }
 
+namespace {
+
+// Per-thread copy streams, destroyed with the thread.
+struct CopyStreams {
+    cudaStream_t s[64] = {};
+    ~CopyStreams()
+    {
+        for (cudaStream_t &x : s)
+            if (x) cudaStreamDestroy(x);
+    }
+};
+thread_local CopyStreams t_copy;
+
+// stream `after` waits for the work queued so far on stream `before`
+bool order(cudaStream_t before, cudaStream_t after, const char *routine)
+{
+    cudaEvent_t e;
+    if (!cuda_ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), routine, "event create")) return false;
+    bool ok = cuda_ok(cudaEventRecord(e, before), routine, "event record") &&
+              cuda_ok(cudaStreamWaitEvent(after, e, 0), routine, "stream wait");
+    cudaEventDestroy(e);
+    return ok;
+}
+
+}  // namespace
+
+cudaStream_t copy_stream()
+{
+    int d = 0;
+    cudaGetDevice(&d);
+    if (d < 0 || d >= 64) d = 0;
+    if (!t_copy.s[d]) cudaStreamCreateWithFlags(&t_copy.s[d], cudaStreamNonBlocking);
+    return t_copy.s[d];
+}
+
+bool stage_matrix_async(Staged &s, const void *host, int64_t rows, int64_t cols, int64_t ld, size_t elem,
+                        bool copy_in, cudaEvent_t &ready, const char *routine)
+{
+    ready = nullptr;
+    if (!copy_in || rows <= 0 || cols <= 0 || is_dd_device_pointer(host))
+        return stage_matrix(s, host, rows, cols, ld, elem, copy_in, routine);
+    if (!stage_matrix(s, host, rows, cols, ld, elem, false, routine)) return false;   // allocation only
+    cudaStream_t cs = copy_stream();
+    if (!cs) {
+        set_error(routine, MWBLAS_ERR_CUDA, "copy stream unavailable");
+        return false;
+    }
+    if (!order(stream(), cs, routine)) return false;
+    if (!cuda_ok(cudaMemcpy2DAsync(s.dev, (size_t)ld * elem, host, (size_t)ld * elem, (size_t)rows * elem,
+                                   (size_t)cols, cudaMemcpyDefault, cs),
+                 routine, "copy matrix to device"))
+        return false;
+    if (!cuda_ok(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), routine, "event create")) {
+        ready = nullptr;
+        return false;
+    }
+    return cuda_ok(cudaEventRecord(ready, cs), routine, "event record");
+}
+
+bool unstage_columns_async(Staged &s, int64_t j0, int64_t j1, const char *routine)
+{
+    if (!s.owned || s.rows <= 0 || j1 <= j0) return true;
+    cudaStream_t cs = copy_stream();
+    if (!order(stream(), cs, routine)) return false;
+    const size_t pitch = (size_t)s.ld * s.elem;
+    return cuda_ok(cudaMemcpy2DAsync((char *)const_cast<void *>(s.host) + (size_t)j0 * pitch, pitch,
+                                     (char *)s.dev + (size_t)j0 * pitch, pitch, (size_t)s.rows * s.elem,
+                                     (size_t)(j1 - j0), cudaMemcpyDefault, cs),
+                   routine, "copy matrix columns to host");
+}
+
+bool wait_event(cudaEvent_t e, const char *routine)
+{
+    return !e || cuda_ok(cudaStreamWaitEvent(stream(), e, 0), routine, "stream wait");
+}
+
+bool join_copy_stream(const char *routine) { return order(copy_stream(), stream(), routine); }
+
+HostStage::~HostStage()
+{
+    for (cudaEvent_t e : {a_ready, b_ready, c_ready})
+        if (e) cudaEventDestroy(e);
+}
+
 bool stage_vector(Staged &s, const void *host, int64_t n, int64_t inc, size_t elem, bool copy_in,
                   int64_t &dev_inc, const char *routine)
 {

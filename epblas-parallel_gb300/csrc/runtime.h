@@ -77,6 +77,37 @@ bool stage_matrix(Staged &s, const void *host, int64_t rows, int64_t cols, int64
 // caller's array are never written).
 bool unstage_matrix(Staged &s, const char *routine);
 
+// ---- copies that overlap the kernels -------------------------------------------
+// A second stream of the calling thread for host<->device copies (one per
+// device, created on first use).
+cudaStream_t copy_stream();
+// stage_matrix with the copy to the device queued on copy_stream() (after the
+// allocation on stream()); `ready`, recorded on copy_stream(), marks its end.
+// Device memory used in place, copy_in=false or an empty matrix give no event.
+bool stage_matrix_async(Staged &s, const void *host, int64_t rows, int64_t cols, int64_t ld, size_t elem,
+                        bool copy_in, cudaEvent_t &ready, const char *routine);
+// Queues the copy of columns [j0, j1) of a staged matrix back to the caller's
+// array on copy_stream(), after the work queued so far on stream().
+bool unstage_columns_async(Staged &s, int64_t j0, int64_t j1, const char *routine);
+// stream() waits for `e` (nullptr: nothing to wait for).
+bool wait_event(cudaEvent_t e, const char *routine);
+// stream() waits for everything queued so far on copy_stream().
+bool join_copy_stream(const char *routine);
+
+// Host operands of one call whose uploads run on copy_stream(). An engine that
+// understands it waits on each event just before it first reads that operand,
+// and may write C back itself in column chunks behind its own kernels.
+struct HostStage {
+    cudaEvent_t a_ready = nullptr, b_ready = nullptr, c_ready = nullptr;
+    Staged *c = nullptr;       // the staged C (target of the write-back)
+    bool c_written = false;    // the engine has queued C's copy back and joined
+    bool wait_all(const char *routine) const
+    {
+        return wait_event(a_ready, routine) && wait_event(b_ready, routine) && wait_event(c_ready, routine);
+    }
+    ~HostStage();
+};
+
 // Vector of n logical elements with increment inc (BLAS convention: a
 // negative increment starts at the far end). A staged host vector is
 // compacted; the device increment is returned in `dev_inc` (+1, -1 or 0).

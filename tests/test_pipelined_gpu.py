@@ -1,0 +1,68 @@
+"""GEMMs on host arrays large enough (>= 64 MB of operands) for the pipelined
+path of the tensor-core engine: the uploads run on a copy stream that the
+kernels wait on operand by operand, and C comes back in column chunks behind
+the reconstruction. The result must be bit-identical to the same call on
+device-resident operands (same kernels, same order of every sum), for
+pageable and pinned host memory, real and complex, beta zero or not, and with
+a column count that leaves a short last chunk; sampled entries are checked
+against binary128 at the reference's tolerance (max(10, 4k) * 2^-104).
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import mwb, orc
+
+pytestmark = pytest.mark.gpu
+
+
+def _host(x, pinned):
+    if not pinned:
+        return x, x.ctypes.data
+    t = torch.from_numpy(x).pin_memory()
+    return t, t.data_ptr()
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+@pytest.mark.parametrize("ta,tb,beta0", [("N", "N", False), ("T", "N", True), ("N", "T", False)])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_host_pipeline_matches_device(gpu, oracle, rng, cplx, ta, tb, beta0, pinned):
+    m, n, k = (1031, 997, 900) if cplx else (1531, 1283, 1100)
+    rnd = mwb.random_cdd if cplx else mwb.random_dd
+    A = rnd(rng, (k, m) if ta == "N" else (m, k))        # storage [column][row]: lda = rows of A
+    B = rnd(rng, (n, k) if tb == "N" else (k, n))
+    C0 = rnd(rng, (n, m))
+    lda, ldb = (m if ta == "N" else k), (k if tb == "N" else n)
+    if cplx:
+        al, be = mwb.random_cdd(rng, ()), (np.zeros((2, 2)) if beta0 else mwb.random_cdd(rng, ()))
+    else:
+        al, be = mwb.random_dd(rng, ()), (np.zeros(2) if beta0 else mwb.random_dd(rng, ()))
+
+    def call(pa, pb, pc):
+        if cplx:
+            gpu.wgemm(ta, tb, m, n, k, al, pa, lda, pb, ldb, be, pc, m)
+        else:
+            gpu.mgemm(ta, tb, m, n, k, al, pa, lda, pb, ldb, be, pc, m, engine="ozaki")
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+
+    dev = torch.device("cuda", 0)
+    dA, dB = torch.from_numpy(A).to(dev), torch.from_numpy(B).to(dev)
+    dC = torch.from_numpy(C0).to(dev)
+    call(dA.data_ptr(), dB.data_ptr(), dC.data_ptr())
+    want_dev = dC.cpu().numpy()
+
+    hA, pa = _host(A, pinned)
+    hB, pb = _host(B, pinned)
+    hC, pc = _host(C0.copy(), pinned)
+    call(pa, pb, pc)
+    got = hC.numpy() if pinned else hC
+    assert np.array_equal(got.view(np.uint64), want_dev.view(np.uint64))
+
+    rows, cols = rng.integers(0, m, 48), rng.integers(0, n, 48)
+    if cplx:
+        want = oracle.qwgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0, m, rows=rows, cols=cols)
+    else:
+        want = oracle.qgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0, m, rows=rows, cols=cols)
+    scale = orc.dd_abs(al) * k * orc.dd_absmax(A) * orc.dd_absmax(B) + orc.dd_abs(be) * orc.dd_absmax(C0)
+    err = float(np.max(orc.dd_diff_abs(got[cols, rows], want))) / scale
+    assert err <= max(10, 4 * k) * orc.EPS_DD, err
