@@ -179,8 +179,29 @@ void gemm_entry(const char *routine, bool cplx, int force_engine, const char *tr
             ~JoinCopies() { join_copy_stream(r); }
         } join_guard{routine};
         if (!stage_matrix_async(SA, a, nrowa, TA == 'N' ? K : M, *lda, es, true, hs.a_ready, routine)) return;
-        if (!stage_matrix_async(SB, b, nrowb, TB == 'N' ? N : K, *ldb, es, true, hs.b_ready, routine)) return;
-        if (!stage_matrix_async(SC, c, M, N, *ldc, es, g.beta_kind != 0, hs.c_ready, routine)) return;
+        // op(B) and C in about eight blocks of whole 256-column tiles, queued
+        // as (B block, C block) pairs in the order the engine uses them
+        int64_t w = ((N + 7) / 8 + 255) / 256 * 256;
+        if (w < 512) w = 512;
+        if (w < N) {
+            hs.block_cols = w;
+            if (!stage_matrix(SB, b, nrowb, TB == 'N' ? N : K, *ldb, es, false, routine)) return;
+            if (!stage_matrix(SC, c, M, N, *ldc, es, false, routine)) return;
+            for (int64_t j0 = 0; j0 < N; j0 += w) {
+                const int64_t j1 = (N - j0 < w) ? N : j0 + w;
+                cudaEvent_t eb = nullptr, ec = nullptr;
+                const bool okb = TB == 'N' ? upload_block_async(SB, 0, K, j0, j1, eb, routine)
+                                           : upload_block_async(SB, j0, j1, 0, K, eb, routine);
+                hs.b_block.push_back(eb);
+                if (!okb) return;
+                const bool okc = g.beta_kind == 0 || upload_block_async(SC, 0, M, j0, j1, ec, routine);
+                hs.c_block.push_back(ec);
+                if (!okc) return;
+            }
+        } else {
+            if (!stage_matrix_async(SB, b, nrowb, TB == 'N' ? N : K, *ldb, es, true, hs.b_ready, routine)) return;
+            if (!stage_matrix_async(SC, c, M, N, *ldc, es, g.beta_kind != 0, hs.c_ready, routine)) return;
+        }
         hs.c = &SC;
         g.A = SA.dev; g.lda = *lda;
         g.B = SB.dev; g.ldb = *ldb;

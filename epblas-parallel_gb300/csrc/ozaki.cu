@@ -266,7 +266,7 @@ template <bool ROWC, bool CPLX>
 __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim, const double2 *__restrict__ X,
                                                      int64_t ld, const int *__restrict__ rexp, int bits,
                                                      OzResParams P, __half *__restrict__ out, int64_t rows_pad,
-                                                     int64_t kpad, int conj)
+                                                     int64_t kpad, int conj, int64_t plane_rows)
 {
     constexpr int E = CPLX ? 2 : 1;
     extern __shared__ __align__(16) unsigned char res_smem[];
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim,
             }
         }
         __syncthreads();   // the buffer is refilled two iterations on; the limbs are in registers
-        const int64_t cstride = (int64_t)nmod * rows_pad * kpad;
+        const int64_t cstride = (int64_t)nmod * plane_rows * kpad;
         __half *o = out + (r * kpad + cb);
         for (int l = 0; l < nmod; ++l) {
             float2 t[12];
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim,
                 store4h(o + cstride, ia, ib);
                 store4h(o + 2 * cstride, sym_wrap2(ra, ia, negp, invp), sym_wrap2(rb, ib, negp, invp));
             }
-            o += rows_pad * kpad;
+            o += plane_rows * kpad;
         }
     }
 }
@@ -374,8 +374,10 @@ __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim,
 // tile's load in flight.
 template <bool ROWC, bool CPLX>
 void launch_residues(int64_t rows, int64_t kdim, const double2 *X, int64_t ld, const int *rexp, int bits,
-                     const OzResParams &rp, __half *out, int64_t rows_pad, int64_t kpad, int conj)
+                     const OzResParams &rp, __half *out, int64_t rows_pad, int64_t kpad, int conj,
+                     int64_t plane_rows = -1)
 {
+    if (plane_rows < 0) plane_rows = rows_pad;
     static int per_sm[64];   // resident blocks per SM, per device (0 = not queried yet)
     const size_t smem = residue_smem_bytes<CPLX>();
     int dev = 0;
@@ -392,7 +394,7 @@ void launch_residues(int64_t rows, int64_t kdim, const double2 *X, int64_t ld, c
     if (grid > ntiles) grid = ntiles;
     if (grid < 1) grid = 1;
     k_oz_residues<ROWC, CPLX><<<(unsigned)grid, 256, smem, stream()>>>(rows, kdim, X, ld, rexp, bits, rp, out, rows_pad,
-                                                                        kpad, conj);
+                                                                        kpad, conj, plane_rows);
     count_launch();
 }
 
@@ -832,7 +834,7 @@ constexpr int T2_SMEM = T2_STAGES * (T2_A_BYTES + T2_B_BYTES) + 1024 + 256;
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TCP_THREADS, 1)
     k_oz_gemm_tc_2sm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t Mp,
                      int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint16_t *__restrict__ R,
-                     int *status, int uplo, int tiles_m2, int tiles_n, int nz)
+                     int *status, int uplo, int tiles_m2, int tiles_n, int nz, int tn0)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -855,7 +857,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TCP_THREADS, 1)
     const int nch = (nsteps + kcs - 1) / kcs;
     const int64_t units = (int64_t)nz * tiles_m2 * tiles_n;
     auto unit_at = [&](int64_t u, int &tn, int &tm2, int &l) -> bool {
-        tn = (int)(u % tiles_n);
+        tn = tn0 + (int)(u % tiles_n);   // column tiles [tn0, tn0 + tiles_n) of the product
         tm2 = (int)((u / tiles_n) % tiles_m2);
         l = (int)(u / ((int64_t)tiles_n * tiles_m2));
         const int64_t i0 = (int64_t)tm2 * 256, j0 = (int64_t)tn * TC_BN;
@@ -1512,50 +1514,72 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     __half *Bres = shared_ops ? Ares : (__half *)(work + a_bytes);
     uint16_t *R = (uint16_t *)(work + a_bytes + b_bytes);
     phase_mark(PH_RES);
-    {
-        // op(A) = A: A[i + p*lda] is contiguous along rows; op(A) = A^T along k.
-        // op(B)(p, j) = B[p + j*ldb] is contiguous along k; op(B) = B^T along rows j.
-        const double2 *Ad = (const double2 *)g.A, *Bd = (const double2 *)g.B;
+    // op(B) and C arriving in column blocks (pair kernel, full output): the
+    // columns of block j are converted, multiplied, reconstructed and copied
+    // back while later blocks are still being uploaded.
+    const bool blocked = hs && hs->block_cols > 0 && mma_kind() == 3 && !shared_ops && g.uplo == 0 && !g.herm;
+    const bool ok_pre = !(hs && hs->block_cols > 0 && !blocked) || hs->wait_all(routine);
+    const double2 *Ad = (const double2 *)g.A;
+    // op(A) = A: A[i + p*lda] is contiguous along rows; op(A) = A^T along k.
+    if (cplx) {
+        if (!g.ta) launch_residues<true, true>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
+        else launch_residues<false, true>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
+    } else {
+        if (!g.ta) launch_residues<true, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
+        else launch_residues<false, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
+    }
+    // op(B)(p, j) = B[p + j*ldb] is contiguous along k; op(B) = B^T along the
+    // columns j. Columns [j0, j0 + nn) of op(B), and their exponent bounds,
+    // go to residue rows [j0, j0 + rpad) of every plane (zeros past n).
+    auto b_cols = [&](int64_t j0) { return (const double2 *)g.B + (int64_t)E * (g.tb ? j0 : j0 * g.ldb); };
+    auto exp_B = [&](int64_t j0, int64_t nn) {
+        launch_exp_cols_of_op(b_cols(j0), g.tb ? nn : k, g.tb ? k : nn, g.ldb, g.tb, E, eb + j0);
+    };
+    auto convert_B = [&](int64_t j0, int64_t nn, int64_t rpad) {
+        const double2 *Bj = b_cols(j0);
+        __half *Bo = Bres + j0 * Kp;
         if (cplx) {
-            if (!g.ta) launch_residues<true, true>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
-            else launch_residues<false, true>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
+            if (!g.tb) launch_residues<false, true>(nn, k, Bj, g.ldb, eb + j0, bits, rp, Bo, rpad, Kp, g.cb, Np);
+            else launch_residues<true, true>(nn, k, Bj, g.ldb, eb + j0, bits, rp, Bo, rpad, Kp, g.cb, Np);
         } else {
-            if (!g.ta) launch_residues<true, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
-            else launch_residues<false, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
+            if (!g.tb) launch_residues<false, false>(nn, k, Bj, g.ldb, eb + j0, bits, rp, Bo, rpad, Kp, 0, Np);
+            else launch_residues<true, false>(nn, k, Bj, g.ldb, eb + j0, bits, rp, Bo, rpad, Kp, 0, Np);
         }
+    };
+    if (!blocked) {
         if (hs) {
             wait_event(hs->b_ready, routine);
-            launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, E, eb);
+            exp_B(0, n);
         }
-        if (!shared_ops) {
-            if (cplx) {
-                if (!g.tb) launch_residues<false, true>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, g.cb);
-                else launch_residues<true, true>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, g.cb);
-            } else {
-                if (!g.tb) launch_residues<false, false>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, 0);
-                else launch_residues<true, false>(n, k, Bd, g.ldb, eb, bits, rp, Bres, Np, Kp, 0);
-            }
-        }
+        if (!shared_ops) convert_B(0, n, Np);
     }
 
     // 4. residue GEMMs, one batch entry per (component, modulus)
     phase_mark(PH_GEMM);
-    bool ok = true;
+    bool ok = ok_pre;
     const int nz = nc * md.n;
-    if (mma_kind() == 0 || mma_kind() == 2 || mma_kind() == 3) {
-        CUtensorMap ma, mb;
-        ok = make_map(&ma, Ares, (uint64_t)Kp, (uint64_t)(nz * Mp), TC_BM, routine) &&
+    CUtensorMap ma, mb;
+    // CTA-pair kernel over the column tiles [tn0, tn0 + ntn) of the product
+    auto pair_gemm = [&](int tn0, int ntn) {
+        cudaFuncSetAttribute(k_oz_gemm_tc_2sm, cudaFuncAttributeMaxDynamicSharedMemorySize, T2_SMEM);
+        const int tiles_m2 = (int)(Mp / 256);
+        const int64_t units = (int64_t)nz * tiles_m2 * ntn;
+        const int64_t pairs = device_sm_count() / 2;
+        const unsigned grid = 2u * (unsigned)(units < pairs ? units : pairs);
+        k_oz_gemm_tc_2sm<<<grid, TCP_THREADS, T2_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R,
+                                                                   device_status_word(), g.uplo, tiles_m2, ntn, nz,
+                                                                   tn0);
+    };
+    if (blocked) {
+        // launched block by block with the reconstruction below
+        ok = ok && make_map(&ma, Ares, (uint64_t)Kp, (uint64_t)(nz * Mp), TC_BM, routine) &&
+             make_map(&mb, Bres, (uint64_t)Kp, (uint64_t)(nz * Np), 128, routine);
+    } else if (mma_kind() == 0 || mma_kind() == 2 || mma_kind() == 3) {
+        ok = ok && make_map(&ma, Ares, (uint64_t)Kp, (uint64_t)(nz * Mp), TC_BM, routine) &&
              make_map(&mb, Bres, (uint64_t)Kp, (uint64_t)(nz * Np), mma_kind() == 3 ? 128 : TC_BN, routine);
         if (ok) {
             if (mma_kind() == 3) {
-                cudaFuncSetAttribute(k_oz_gemm_tc_2sm, cudaFuncAttributeMaxDynamicSharedMemorySize, T2_SMEM);
-                const int tiles_m2 = (int)(Mp / 256), tiles_n = (int)(Np / TC_BN);
-                const int64_t units = (int64_t)nz * tiles_m2 * tiles_n;
-                const int64_t pairs = device_sm_count() / 2;
-                const unsigned grid = 2u * (unsigned)(units < pairs ? units : pairs);
-                k_oz_gemm_tc_2sm<<<grid, TCP_THREADS, T2_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R,
-                                                                           device_status_word(), g.uplo, tiles_m2,
-                                                                           tiles_n, nz);
+                pair_gemm(0, (int)(Np / TC_BN));
             } else if (mma_kind() == 2) {
                 cudaFuncSetAttribute(k_oz_gemm_tc_p, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
                 const int tiles_m = (int)(Mp / TC_BM), tiles_n = (int)(Np / TC_BN);
@@ -1579,56 +1603,82 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         count_launch();
     }
 
+
     // 5. reconstruction + alpha/beta
     phase_mark(PH_REC);
-    if (ok && hs) ok = wait_event(hs->c_ready, routine);
-    if (ok) {
+    // a thread per row and several columns: about 16 blocks per SM in all
+    const unsigned gx = (unsigned)((m + (cplx ? 255 : 511)) / (cplx ? 256 : 512));
+    const int64_t want_y = ((int64_t)device_sm_count() * 16 + gx - 1) / gx;
+    xw::XW Mx;
+    Mx.w[3] = (uint32_t)(cp.Mhi >> 32);
+    Mx.w[2] = (uint32_t)cp.Mhi;
+    Mx.w[1] = (uint32_t)(cp.Mlo >> 32);
+    Mx.w[0] = (uint32_t)cp.Mlo;
+    Mx.e = cp.Me;
+    Mx.neg = 0u;
+    // columns [j0, j0 + nn) of C
+    auto reconstruct_cols = [&](int64_t j0, int64_t nn) {
+        dim3 grid(gx, blocks_cap(want_y < nn ? want_y : nn));
+        const uint16_t *Rj = R + j0 * Mp;     // column j0 of every residue plane
+        double2 *Cj = (double2 *)g.C + (int64_t)E * j0 * g.ldc;
+        if (!cplx) {
+            bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
+            // alpha folded into M: alpha * X = T * (alpha M)
+            const xw::XW aM = alpha_one ? Mx : xw::mul(xw::from_dd(g.alpha.hi, g.alpha.lo), Mx);
+            k_oz_reconstruct<<<grid, 256, 0, stream()>>>((int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits, cp, aM,
+                                                        xw::from_dd(g.beta.hi, g.beta.lo),
+                                                        dd::make(g.beta.hi, g.beta.lo), g.beta_kind, Cj, g.ldc,
+                                                        g.uplo);
+        } else {
+            dd::cplx al, be;
+            al.re = dd::make(g.calpha.re.hi, g.calpha.re.lo);
+            al.im = dd::make(g.calpha.im.hi, g.calpha.im.lo);
+            be.re = dd::make(g.cbeta.re.hi, g.cbeta.re.lo);
+            be.im = dd::make(g.cbeta.im.hi, g.cbeta.im.lo);
+            bool alpha_one = (g.calpha.re.hi == 1.0 && g.calpha.re.lo == 0.0 && g.calpha.im.hi == 0.0 &&
+                              g.calpha.im.lo == 0.0);
+            k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>(
+                (int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits, cp, Mx, xw::from_dd(al.re.hi, al.re.lo),
+                xw::from_dd(al.im.hi, al.im.lo), alpha_one ? 1 : 0, be, xw::from_dd(be.re.hi, be.re.lo),
+                xw::from_dd(be.im.hi, be.im.lo), g.beta_kind, Cj, g.ldc, g.uplo, g.herm ? 1 : 0, g.herm ? 1 : 0);
+        }
+        count_launch();
+    };
+    if (ok && blocked) {
+        // block j: its columns of op(B) in, converted, multiplied, reconstructed
+        // and copied back; the uploads of later blocks run meanwhile
+        const int64_t w = hs->block_cols;
+        for (int64_t j0 = 0, jb = 0; ok && j0 < n; j0 += w, ++jb) {
+            const int64_t nn = (n - j0 < w) ? n - j0 : w;
+            const bool last = j0 + w >= n;
+            ok = wait_event(jb < (int64_t)hs->b_block.size() ? hs->b_block[jb] : nullptr, routine);
+            if (!ok) break;
+            exp_B(j0, nn);
+            convert_B(j0, nn, last ? Np - j0 : nn);
+            pair_gemm((int)(j0 / TC_BN), (int)((last ? Np - j0 : nn) / TC_BN));
+            count_launch();
+            ok = wait_event(jb < (int64_t)hs->c_block.size() ? hs->c_block[jb] : nullptr, routine);
+            if (!ok) break;
+            reconstruct_cols(j0, nn);
+            ok = unstage_columns_async(*hs->c, j0, j0 + nn, routine);
+        }
+        if (ok) {
+            // the buffers are freed on stream(): order that after the copies
+            ok = join_copy_stream(routine);
+            hs->c_written = ok;
+        }
+    } else if (ok) {
+        if (hs) ok = wait_event(hs->c_ready, routine);
         // C going back to the host: the reconstruction runs in column chunks,
         // each copied back while the next one is computed
         const bool chunked = hs && hs->c && g.uplo == 0 && !g.herm;
         const int64_t cw = chunked ? (n + 7) / 8 : n;
-        // a thread per row and several columns: about 16 blocks per SM in all
-        const unsigned gx = (unsigned)((m + (cplx ? 255 : 511)) / (cplx ? 256 : 512));
-        const int64_t want_y = ((int64_t)device_sm_count() * 16 + gx - 1) / gx;
-        xw::XW Mx;
-        Mx.w[3] = (uint32_t)(cp.Mhi >> 32);
-        Mx.w[2] = (uint32_t)cp.Mhi;
-        Mx.w[1] = (uint32_t)(cp.Mlo >> 32);
-        Mx.w[0] = (uint32_t)cp.Mlo;
-        Mx.e = cp.Me;
-        Mx.neg = 0u;
         for (int64_t j0 = 0; ok && j0 < n; j0 += cw) {
             const int64_t nn = (n - j0 < cw) ? n - j0 : cw;
-            dim3 grid(gx, blocks_cap(want_y < nn ? want_y : nn));
-            const uint16_t *Rj = R + j0 * Mp;     // column j0 of every residue plane
-            double2 *Cj = (double2 *)g.C + (int64_t)E * j0 * g.ldc;
-            if (!cplx) {
-                bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
-                // alpha folded into M: alpha * X = T * (alpha M)
-                const xw::XW aM = alpha_one ? Mx : xw::mul(xw::from_dd(g.alpha.hi, g.alpha.lo), Mx);
-                k_oz_reconstruct<<<grid, 256, 0, stream()>>>((int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits, cp, aM,
-                                                            xw::from_dd(g.beta.hi, g.beta.lo),
-                                                            dd::make(g.beta.hi, g.beta.lo), g.beta_kind, Cj, g.ldc,
-                                                            g.uplo);
-            } else {
-                dd::cplx al, be;
-                al.re = dd::make(g.calpha.re.hi, g.calpha.re.lo);
-                al.im = dd::make(g.calpha.im.hi, g.calpha.im.lo);
-                be.re = dd::make(g.cbeta.re.hi, g.cbeta.re.lo);
-                be.im = dd::make(g.cbeta.im.hi, g.cbeta.im.lo);
-                bool alpha_one = (g.calpha.re.hi == 1.0 && g.calpha.re.lo == 0.0 && g.calpha.im.hi == 0.0 &&
-                                  g.calpha.im.lo == 0.0);
-                k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>(
-                    (int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits, cp, Mx, xw::from_dd(al.re.hi, al.re.lo),
-                    xw::from_dd(al.im.hi, al.im.lo), alpha_one ? 1 : 0, be, xw::from_dd(be.re.hi, be.re.lo),
-                    xw::from_dd(be.im.hi, be.im.lo), g.beta_kind, Cj, g.ldc, g.uplo, g.herm ? 1 : 0,
-                    g.herm ? 1 : 0);
-            }
-            count_launch();
+            reconstruct_cols(j0, nn);
             if (chunked) ok = unstage_columns_async(*hs->c, j0, j0 + nn, routine);
         }
         if (ok && chunked) {
-            // the buffers are freed on stream(): order that after the copies
             ok = join_copy_stream(routine);
             hs->c_written = ok;
         }

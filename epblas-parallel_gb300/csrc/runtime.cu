@@ -300,6 +300,29 @@ HostStage::~HostStage()
 {
     for (cudaEvent_t e : {a_ready, b_ready, c_ready})
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : b_block)
+        if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : c_block)
+        if (e) cudaEventDestroy(e);
+}
+
+bool upload_block_async(Staged &s, int64_t r0, int64_t r1, int64_t c0, int64_t c1, cudaEvent_t &ready,
+                        const char *routine)
+{
+    ready = nullptr;
+    if (!s.owned || r1 <= r0 || c1 <= c0) return true;
+    cudaStream_t cs = copy_stream();
+    if (!order(stream(), cs, routine)) return false;
+    const size_t pitch = (size_t)s.ld * s.elem, off = (size_t)c0 * pitch + (size_t)r0 * s.elem;
+    if (!cuda_ok(cudaMemcpy2DAsync((char *)s.dev + off, pitch, (const char *)s.host + off, pitch,
+                                   (size_t)(r1 - r0) * s.elem, (size_t)(c1 - c0), cudaMemcpyDefault, cs),
+                 routine, "copy matrix block to device"))
+        return false;
+    if (!cuda_ok(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), routine, "event create")) {
+        ready = nullptr;
+        return false;
+    }
+    return cuda_ok(cudaEventRecord(ready, cs), routine, "event record");
 }
 
 bool stage_vector(Staged &s, const void *host, int64_t n, int64_t inc, size_t elem, bool copy_in,

@@ -97,16 +97,28 @@ bool join_copy_stream(const char *routine);
 // Host operands of one call whose uploads run on copy_stream(). An engine that
 // understands it waits on each event just before it first reads that operand,
 // and may write C back itself in column chunks behind its own kernels.
+// With block_cols > 0, op(B) and C arrive instead in blocks of that many
+// columns (block j: columns [j * block_cols, ...)), one event per block, so
+// that the product of block j can start when its columns are in.
 struct HostStage {
     cudaEvent_t a_ready = nullptr, b_ready = nullptr, c_ready = nullptr;
+    int64_t block_cols = 0;
+    std::vector<cudaEvent_t> b_block, c_block;
     Staged *c = nullptr;       // the staged C (target of the write-back)
     bool c_written = false;    // the engine has queued C's copy back and joined
     bool wait_all(const char *routine) const
     {
-        return wait_event(a_ready, routine) && wait_event(b_ready, routine) && wait_event(c_ready, routine);
+        bool ok = wait_event(a_ready, routine) && wait_event(b_ready, routine) && wait_event(c_ready, routine);
+        for (cudaEvent_t e : b_block) ok = ok && wait_event(e, routine);
+        for (cudaEvent_t e : c_block) ok = ok && wait_event(e, routine);
+        return ok;
     }
     ~HostStage();
 };
+// Queues the copy of rows [r0, r1) x columns [c0, c1) of the caller's matrix
+// into a staged (allocated) matrix on copy_stream(); `ready` marks its end.
+bool upload_block_async(Staged &s, int64_t r0, int64_t r1, int64_t c0, int64_t c1, cudaEvent_t &ready,
+                        const char *routine);
 
 // Vector of n logical elements with increment inc (BLAS convention: a
 // negative increment starts at the far end). A staged host vector is
