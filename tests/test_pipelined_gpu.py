@@ -26,14 +26,14 @@ def _host(x, pinned):
 @pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("ta,tb,beta0", [("N", "N", False), ("T", "N", True), ("N", "T", False)])
 @pytest.mark.parametrize("cplx", [False, True])
-@pytest.mark.parametrize("wide", [True, False])
-def test_host_pipeline_matches_device(gpu, oracle, rng, cplx, ta, tb, beta0, pinned, wide):
-    """wide: n large enough for column blocks (B and C uploaded block by
-    block, blocks of 512 columns and a short last one); otherwise one block."""
-    if wide:
-        m, n, k = (1031, 997, 900) if cplx else (1531, 1283, 1100)
-    else:
-        m, n, k = (1500, 300, 1200) if cplx else (2000, 400, 1800)
+@pytest.mark.parametrize("shape", ["blocks", "one_column_block", "one_row_block"])
+def test_host_pipeline_matches_device(gpu, oracle, rng, cplx, ta, tb, beta0, pinned, shape):
+    """op(B) and C above 512 columns arrive in column blocks of 512 (short
+    last blocks included); at most 512 columns come as one block. A is
+    uploaded whole."""
+    m, n, k = {"blocks": ((1031, 997, 900), (1531, 1283, 1100)),
+               "one_column_block": ((1500, 300, 1200), (2000, 400, 1800)),
+               "one_row_block": ((300, 1500, 1200), (400, 1800, 2000))}[shape][0 if cplx else 1]
     rnd = mwb.random_cdd if cplx else mwb.random_dd
     A = rnd(rng, (k, m) if ta == "N" else (m, k))        # storage [column][row]: lda = rows of A
     B = rnd(rng, (n, k) if tb == "N" else (k, n))
