@@ -136,11 +136,21 @@ struct SmvParams {
     const double2 *A;
     int fmt, kind, op;   // op 0 'N', 1 'T', 2 'C'
     bool upper, unit;
-    const double2 *x;
+    const fx::Dig *xd;   // x decoded and split into digits once (complex: re, im)
     double2 *y;
     dd::real ar, ai, br, bi;
     int beta_kind;
 };
+
+// x (any increment, BLAS order) decoded and split for the products.
+__global__ void k_vdig(int64_t n, const double2 *x, int64_t inc, int e2, fx::Dig *out)
+{
+    const int64_t total = n * e2;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t / e2, w = t % e2;
+        out[t] = fx::to_dig(fx::decode(x[e2 * vpos(i, n, inc) + w]));
+    }
+}
 
 __device__ __forceinline__ void smv_range(const SmvParams &p, int64_t r, int64_t &c0, int64_t &c1)
 {
@@ -251,16 +261,16 @@ __global__ void __launch_bounds__(256) k_smv(SmvParams p)
             fx::Op er, ei;
             smv_elem<CX>(p, r, c, er, ei);
             if (CX) {
-                const fx::Op xr = fx::decode(p.x[2 * c]), xi = fx::decode(p.x[2 * c + 1]);
+                const fx::Dig xr = p.xd[2 * c], xi = p.xd[2 * c + 1];
                 fx::Op nei = ei;
                 nei.flags ^= fx::kNeg;
-                acc[0].add_prod(er, xr);
-                acc[0].add_prod(nei, xi);
-                acc[1].add_prod(er, xi);
-                acc[1].add_prod(ei, xr);
+                acc[0].add_dig(er, xr);
+                acc[0].add_dig(nei, xi);
+                acc[1].add_dig(er, xi);
+                acc[1].add_dig(ei, xr);
                 cnt += 2;
             } else {
-                acc[0].add_prod(er, fx::decode(p.x[c]));
+                acc[0].add_dig(er, p.xd[c]);
                 ++cnt;
             }
             if (cnt >= fx::kMaxAdds - 2) {
@@ -346,9 +356,12 @@ bool smv_device(const SmvArgs &a, const char *routine)
 {
     const int e2 = a.cplx ? 2 : 1;
     const size_t es = 16 * (size_t)e2;
-    Buf xb((size_t)(a.cols > 0 ? a.cols : 1) * es, routine), yb((size_t)(a.rows > 0 ? a.rows : 1) * es, routine);
+    Buf xb((size_t)(a.cols > 0 ? a.cols : 1) * e2 * sizeof(fx::Dig), routine),
+        yb((size_t)(a.rows > 0 ? a.rows : 1) * es, routine);
     if (!xb.p || !yb.p) return false;
-    vgather(a.cols, a.x, a.incx, e2, xb.p, true);
+    k_vdig<<<blocks_for(a.cols * e2), kThreads, 0, stream()>>>(a.cols, (const double2 *)a.x, a.incx, e2,
+                                                              (fx::Dig *)xb.p);
+    count_launch();
     if (a.beta_kind != 0) vgather(a.rows, a.y, a.incy, e2, yb.p, true);
     SmvParams p;
     p.rows = a.rows;
@@ -363,7 +376,7 @@ bool smv_device(const SmvArgs &a, const char *routine)
     p.op = a.trans == 'N' ? 0 : (a.trans == 'T' ? 1 : 2);
     p.upper = a.upper;
     p.unit = a.unit;
-    p.x = (const double2 *)xb.p;
+    p.xd = (const fx::Dig *)xb.p;
     p.y = (double2 *)yb.p;
     if (a.cplx) {
         p.ar = dd::make(a.calpha.re.hi, a.calpha.re.lo);
