@@ -18,9 +18,10 @@
 // scratch matrix by a bandwidth-bound kernel and the product runs through
 // the engine dispatch (tensor cores for large sizes), in place of the
 // reference's diagonal-block kernels plus GEMM wings. SYR2K/HER2K are two
-// triangular GEMMs into C. The complex TRSM halves the triangle recursively
-// with complex GEMM updates and solves 32-row diagonal blocks by
-// substitution in double-double arithmetic.
+// triangular GEMMs into C. The complex TRSM scales each row of op(A) by its
+// inverse diagonal and solves the resulting unit triangle, written as a real
+// triangle of twice the order over interleaved (re, im) unknowns, with the
+// real blocked TRSM in place in B.
 #include <cstring>
 
 #include "dd.cuh"
@@ -126,56 +127,79 @@ __device__ __forceinline__ dd::cplx opAc(const double2 *A, int64_t lda, bool tra
     return v;
 }
 
-__device__ __forceinline__ dd::cplx cshfl_down(const dd::cplx &v, int off)
+// ---- complex triangular solve through the real one --------------------------------------
+// Row i of op(A) X = B scaled by s_i = 1/op(A)(i, i) gives a unit-diagonal
+// complex triangle A'. Written as 2 x 2 real blocks [[re, -im], [im, re]]
+// over interleaved (re, im) unknowns, A' is a unit-diagonal REAL triangle of
+// order 2m, and a column-major complex B (ldb) read as real IS the interleaved
+// right-hand side (2m rows, leading dimension 2 ldb). So the complex solve is
+// the real blocked TRSM on that 2m x 2m matrix, in place in B.
+
+// inv[i] = 1 / op(A)(i, i) and s[i] = alpha * inv[i] (inv = 1 on a unit diagonal).
+__global__ void k_cdiag_inv(int64_t n, const double2 *__restrict__ A, int64_t lda, bool trans, bool conj, bool unit,
+                            dd::cplx alpha, double2 *__restrict__ inv, double2 *__restrict__ s)
 {
-    dd::cplx r;
-    r.re.hi = __shfl_down_sync(0xffffffffu, v.re.hi, off);
-    r.re.lo = __shfl_down_sync(0xffffffffu, v.re.lo, off);
-    r.im.hi = __shfl_down_sync(0xffffffffu, v.im.hi, off);
-    r.im.lo = __shfl_down_sync(0xffffffffu, v.im.lo, off);
-    return r;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        dd::cplx r;
+        r.re = dd::make(1.0, 0.0);
+        r.im = dd::make(0.0, 0.0);
+        if (!unit) {
+            const dd::cplx d = opAc(A, lda, trans, conj, i, i);
+            const dd::real m2 = dd::add_exact(dd::mul_exact(d.re, d.re), dd::mul_exact(d.im, d.im));
+            const dd::real q = dd::div(dd::make(1.0, 0.0), m2);
+            r.re = dd::mul_exact(d.re, q);
+            r.im = dd::neg(dd::mul_exact(d.im, q));
+        }
+        dd::cstore(inv + 2 * i, r);
+        dd::cstore(s + 2 * i, dd::cmul_exact(alpha, r));
+    }
 }
 
-// Complex left solve of op(A)[r0:r0+nb, r0:r0+nb] * X = B[r0:r0+nb, :] in place
-// (nb <= 32), a warp per right-hand-side column with lane l holding row l.
-// Row i is finished by lane i after a warp reduction of the solved lanes'
-// products; lower: op(A) lower triangular (forward order). The diagonal
-// divisor is applied as conj(d) / |d|^2 (a DD division of the squared
-// modulus).
-__global__ void k_ctrsm_diag(int64_t r0, int nb, int64_t ncols, const double2 *__restrict__ A, int64_t lda,
-                             bool trans, bool conj, bool lower, bool unit, double2 *__restrict__ B, int64_t ldb)
+// L (2n x 2n real, ld 2n): the 2 x 2 block (i, j) is [[v.re, -v.im], [v.im,
+// v.re]] with v = inv[i] * op(A)(i, j) inside the triangle, the identity on
+// the diagonal and zero outside.
+__global__ void k_ctri_to_real(int64_t n, const double2 *__restrict__ A, int64_t lda, bool trans, bool conj,
+                               bool lower, bool unit, const double2 *__restrict__ inv, double2 *__restrict__ L)
 {
-    const int64_t j = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (j >= ncols) return;   // whole warps leave together
-    double2 *b = B + 2 * (r0 + j * ldb);
-    const dd::real z = dd::make(0.0, 0.0);
-    dd::cplx x = lane < nb ? dd::cload(b + 2 * lane) : dd::cplx{z, z};
-    for (int s = 0; s < nb; ++s) {
-        const int i = lower ? s : nb - 1 - s;
-        const bool solved = lower ? (lane < i) : (lane > i && lane < nb);
-        dd::cplx t{z, z};
-        if (solved) t = dd::cmul_exact(opAc(A, lda, trans, conj, r0 + i, r0 + lane), x);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) t = dd::cadd_exact(t, cshfl_down(t, off));
-        dd::cplx tot;
-        tot.re.hi = __shfl_sync(0xffffffffu, t.re.hi, 0);
-        tot.re.lo = __shfl_sync(0xffffffffu, t.re.lo, 0);
-        tot.im.hi = __shfl_sync(0xffffffffu, t.im.hi, 0);
-        tot.im.lo = __shfl_sync(0xffffffffu, t.im.lo, 0);
-        if (lane == i) {
-            dd::cplx acc = dd::cadd_exact(x, dd::cplx{dd::neg(tot.re), dd::neg(tot.im)});
-            if (!unit) {
-                const dd::cplx d = opAc(A, lda, trans, conj, r0 + i, r0 + i);
-                const dd::real m2 = dd::add_exact(dd::mul_exact(d.re, d.re), dd::mul_exact(d.im, d.im));
-                const dd::real inv = dd::div(dd::make(1.0, 0.0), m2);
-                const dd::cplx dc{dd::mul_exact(d.re, inv), dd::neg(dd::mul_exact(d.im, inv))};
-                acc = dd::cmul_exact(acc, dc);
-            }
-            x = acc;
+    const int64_t ld = 2 * n;
+    const double2 zero = make_double2(0.0, 0.0);
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t % n, j = t / n;
+        double2 v00 = zero, v10 = zero, v01 = zero, v11 = zero;
+        if (i == j) {
+            v00 = v11 = make_double2(1.0, 0.0);
+        } else if (lower ? i > j : i < j) {
+            dd::cplx v = opAc(A, lda, trans, conj, i, j);
+            if (!unit) v = dd::cmul_exact(dd::cload(inv + 2 * i), v);
+            v00 = v11 = make_double2(v.re.hi, v.re.lo);
+            v10 = make_double2(v.im.hi, v.im.lo);
+            v01 = make_double2(-v.im.hi, -v.im.lo);
         }
+        double2 *c0 = L + 2 * j * ld + 2 * i;   // column 2j, rows 2i and 2i + 1
+        c0[0] = v00;
+        c0[1] = v10;
+        c0[ld] = v01;
+        c0[ld + 1] = v11;
     }
-    if (lane < nb) dd::cstore(b + 2 * lane, x);
+}
+
+// B(i, :) := s[i] * B(i, :)
+__global__ void k_crow_scale(int64_t n, int64_t nrhs, const double2 *__restrict__ s, double2 *B, int64_t ldb)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * nrhs;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t % n, j = t / n;
+        double2 *p = B + 2 * (i + j * ldb);
+        dd::cstore(p, dd::cmul_exact(dd::cload(s + 2 * i), dd::cload(p)));
+    }
+}
+
+unsigned grid_cap(int64_t work)
+{
+    int64_t b = (work + kThreads - 1) / kThreads;
+    const int64_t cap = (int64_t)device_sm_count() * 16;
+    if (b > cap) b = cap;
+    return (unsigned)(b < 1 ? 1 : b);
 }
 
 // Scratch allocation released on scope exit.
@@ -185,48 +209,23 @@ struct Scratch {
     ~Scratch() { dev_free(p); }
 };
 
-constexpr int kCtrsmLeaf = 32;
-
-// Recursive complex left solve over rows [r0, r0 + n) of op(A) (stored A with
-// trans/conj flags), all right-hand sides.
-bool ctrsm_left_rec(int64_t r0, int64_t n, int64_t nrhs, const double2 *A, int64_t lda, bool trans, bool conj,
-                    bool lower, bool unit, double2 *B, int64_t ldb, const char *routine)
+// op(A) X = alpha B for all nrhs columns of B (stored A with trans/conj
+// flags; `lower`: op(A) is lower triangular), through the real solve above.
+bool ctrsm_left_real(int64_t n, int64_t nrhs, const double2 *A, int64_t lda, bool trans, bool conj, bool lower,
+                     bool unit, cdd_host alpha, double2 *B, int64_t ldb, const char *routine)
 {
-    if (n <= kCtrsmLeaf) {
-        const unsigned nbk = (unsigned)((nrhs * 32 + kThreads - 1) / kThreads);
-        k_ctrsm_diag<<<nbk, kThreads, 0, stream()>>>(r0, (int)n, nrhs, A, lda, trans, conj, lower, unit, B, ldb);
-        count_launch();
-        return true;
-    }
-    const int64_t n1 = ((n / 2 + kCtrsmLeaf - 1) / kCtrsmLeaf) * kCtrsmLeaf, n2 = n - n1;
-    // op(A) block (rows ra.., cols ca..) as a GEMM operand of the stored A
-    auto update = [&](int64_t rows_at, int64_t nrows, int64_t cols_at, int64_t ncols, int64_t xr0) -> bool {
-        // B[rows_at : +nrows, :] -= op(A)[rows_at.., cols_at..] * X[xr0 : +ncols, :]
-        GemmArgs g;
-        g.calpha = cdd_host{{-1.0, 0.0}, {0.0, 0.0}};
-        g.cbeta = cdd_host{{1.0, 0.0}, {0.0, 0.0}};
-        g.beta_kind = 1;
-        g.m = nrows;
-        g.n = nrhs;
-        g.k = ncols;
-        g.ta = trans;
-        g.ca = conj;
-        g.A = A + 2 * (trans ? (cols_at + rows_at * lda) : (rows_at + cols_at * lda));
-        g.lda = lda;
-        g.B = B + 2 * xr0;
-        g.ldb = ldb;
-        g.C = B + 2 * rows_at;
-        g.ldc = ldb;
-        return run_gemm(g, true, -1, routine);
-    };
-    if (lower) {
-        if (!ctrsm_left_rec(r0, n1, nrhs, A, lda, trans, conj, lower, unit, B, ldb, routine)) return false;
-        if (!update(r0 + n1, n2, r0, n1, r0)) return false;
-        return ctrsm_left_rec(r0 + n1, n2, nrhs, A, lda, trans, conj, lower, unit, B, ldb, routine);
-    }
-    if (!ctrsm_left_rec(r0 + n1, n2, nrhs, A, lda, trans, conj, lower, unit, B, ldb, routine)) return false;
-    if (!update(r0, n1, r0 + n1, n2, r0 + n1)) return false;
-    return ctrsm_left_rec(r0, n1, nrhs, A, lda, trans, conj, lower, unit, B, ldb, routine);
+    Scratch sc((size_t)n * 64 + (size_t)4 * n * n * 16, routine);
+    if (!sc.p) return false;
+    double2 *inv = (double2 *)sc.p, *sv = inv + 2 * n, *L = sv + 2 * n;
+    dd::cplx al;
+    al.re = dd::make(alpha.re.hi, alpha.re.lo);
+    al.im = dd::make(alpha.im.hi, alpha.im.lo);
+    k_cdiag_inv<<<grid_cap(n), kThreads, 0, stream()>>>(n, A, lda, trans, conj, unit, al, inv, sv);
+    k_ctri_to_real<<<grid_cap(n * n), kThreads, 0, stream()>>>(n, A, lda, trans, conj, lower, unit, inv, L);
+    k_crow_scale<<<grid_cap(n * nrhs), kThreads, 0, stream()>>>(n, nrhs, sv, B, ldb);
+    count_launch(3);
+    return trsm_device('L', lower ? 'L' : 'U', 'N', 'U', 2 * n, nrhs, dd_host{1.0, 0.0}, L, 2 * n, B, 2 * ldb,
+                       routine);
 }
 
 }  // namespace
@@ -363,13 +362,10 @@ bool ctrsm_device(char side, char uplo, char transa, char diag, int64_t m, int64
                   int64_t lda, void *B, int64_t ldb, const char *routine)
 {
     const bool unit = diag == 'U';
-    // B := alpha * B first (the solve is linear in B)
-    const bool alpha1 = alpha.re.hi == 1.0 && alpha.re.lo == 0.0 && alpha.im.hi == 0.0 && alpha.im.lo == 0.0;
-    if (!alpha1) launch_scale_matrix_c(m, n, alpha, 2, B, ldb);
     bool t = transa != 'N', c = transa == 'C';
     if (side == 'L') {
         const bool lower = (uplo == 'L') != t;
-        return ctrsm_left_rec(0, m, n, (const double2 *)A, lda, t, c, lower, unit, (double2 *)B, ldb, routine);
+        return ctrsm_left_real(m, n, (const double2 *)A, lda, t, c, lower, unit, alpha, (double2 *)B, ldb, routine);
     }
     // X * op(A) = B  <=>  op(A)^T * X^T = B^T, with op(A)^T = A (N -> T),
     // A (T -> N) or conj(A) (C -> conjugate, no transpose)
@@ -380,7 +376,7 @@ bool ctrsm_device(char side, char uplo, char transa, char diag, int64_t m, int64
     count_launch();
     const bool t2 = !t;
     const bool lower = (uplo == 'L') != t2;
-    if (!ctrsm_left_rec(0, n, m, (const double2 *)A, lda, t2, c, lower, unit, (double2 *)bt.p, n, routine))
+    if (!ctrsm_left_real(n, m, (const double2 *)A, lda, t2, c, lower, unit, alpha, (double2 *)bt.p, n, routine))
         return false;
     dim3 gb((unsigned)((n + 31) / 32), (unsigned)((m + 31) / 32));
     k_transpose<<<gb, kThreads, 0, stream()>>>(n, m, (const double2 *)bt.p, n, 2, (double2 *)B, ldb);
