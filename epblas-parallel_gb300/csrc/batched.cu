@@ -269,7 +269,10 @@ struct TrsmDesc {
     double2 alpha;
     int nchunks;          // groups of 32 right-hand sides
     int64_t work_begin;
+    int64_t xop_begin;    // this instance's decoded solutions in the scratch array (na * 32 per chunk)
 };
+
+constexpr int kTrsmTile = 256;   // entries of a row of op(A) split into digits at a time
 
 __device__ __forceinline__ dd::real dd_recip(dd::real b)
 {
@@ -293,8 +296,12 @@ __device__ __forceinline__ dd::real dd_recip(dd::real b)
 // the last right-hand side do the work on a clamped column and store
 // nothing) so that the shuffles see the whole warp.
 __global__ void __launch_bounds__(128) k_trsm_grouped(const TrsmDesc *__restrict__ descs, int count, int64_t total,
-                                                     int side, int lower, int trans, int unit)
+                                                     int side, int lower, int trans, int unit, fx::Op *xops)
 {
+    // per warp: a tile of the current row of op(A), split into digits once
+    // for all 32 right-hand sides
+    __shared__ fx::Dig s_arow[4][kTrsmTile];
+    fx::Dig *arow = s_arow[(threadIdx.x >> 5) & 3];
     const int lane = threadIdx.x & 31;
     const int64_t w = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
     if (w >= total) return;   // whole warp leaves together
@@ -312,6 +319,7 @@ __global__ void __launch_bounds__(128) k_trsm_grouped(const TrsmDesc *__restrict
     const int64_t nr = side == 0 ? d.n : d.m;             // right-hand sides
     const int64_t rhs = (int64_t)chunk * 32 + lane;
     const bool active = rhs < nr;
+    fx::Op *xw = xops + d.xop_begin + (int64_t)chunk * na * 32;   // [row][lane]
     const int64_t my = active ? rhs : nr - 1;             // clamped: loads stay in bounds
     // element t of this lane's right-hand side (a column of B for side L, a row for R)
     auto bptr = [&](int t) -> double2 * {
@@ -343,12 +351,21 @@ __global__ void __launch_bounds__(128) k_trsm_grouped(const TrsmDesc *__restrict
         if (!alpha1) b0 = dd::mul_fast(b0, alpha);
         acc.add_dig(fx::decode(make_double2(b0.hi, b0.lo)), one);
         const int p0 = forward ? 0 : r + 1, p1 = forward ? r : na;
-        for (int p = p0; p < p1; ++p) {
+        for (int t0 = p0; t0 < p1; t0 += kTrsmTile) {
+            const int tl = min(kTrsmTile, p1 - t0);
             // side L: sum_p op(A)(r, p) x_p; side R: sum_p x_p op(A)(p, r)
-            const double2 av = side == 0 ? OPA(r, p) : OPA(p, r);
-            fx::Op ao = fx::decode(av);
-            ao.flags ^= fx::kNeg;
-            acc.add_dig(ao, fx::to_dig(fx::decode(*bptr(p))));
+            for (int q = lane; q < tl; q += 32) {
+                const int p = t0 + q;
+                arow[q] = fx::to_dig(fx::decode(side == 0 ? OPA(r, p) : OPA(p, r)));
+            }
+            __syncwarp();
+            const fx::Op *xp = xw + (int64_t)t0 * 32 + lane;
+            for (int q = 0; q < tl; ++q, xp += 32) {
+                fx::Op xo = *xp;
+                xo.flags ^= fx::kNeg;
+                acc.add_dig(xo, arow[q]);
+            }
+            __syncwarp();
         }
         double h, l;
         xfp::xf_to_dd(acc.finish(), h, l);
@@ -360,6 +377,7 @@ __global__ void __launch_bounds__(128) k_trsm_grouped(const TrsmDesc *__restrict
             v = dd::mul_fast(v, dd::make(ih, il));
         }
         if (active) dd::store(bptr(r), v);
+        xw[(int64_t)r * 32 + lane] = fx::decode(make_double2(v.hi, v.lo));
         __syncwarp();
     }
 #undef OPA
@@ -743,22 +761,33 @@ extern "C" int mtrsm_grouped(int64_t count, char side, char uplo, char transa, c
         d.alpha = make_double2(alpha[i].limbs[0], alpha[i].limbs[1]);
         const int64_t rhs = (S == 'L') ? n[i] : m[i];
         d.nchunks = (int)((rhs + 31) / 32);
-        d.work_begin = work;
-        work += d.nchunks;
         descs.push_back(d);
     }
     if (descs.empty()) return 0;
+    // the longest triangles first, so that they do not form the tail
+    std::stable_sort(descs.begin(), descs.end(), [S](const TrsmDesc &x, const TrsmDesc &y) {
+        return (S == 'L' ? x.m : x.n) > (S == 'L' ? y.m : y.n);
+    });
+    int64_t xop_elems = 0;
+    for (TrsmDesc &d : descs) {
+        d.work_begin = work;
+        work += d.nchunks;
+        d.xop_begin = xop_elems;
+        xop_elems += (int64_t)d.nchunks * (S == 'L' ? d.m : d.n) * 32;
+    }
     if (!ensure_device(routine)) return mwblas_last_error();
-    const size_t bytes = descs.size() * sizeof(TrsmDesc);
-    TrsmDesc *dd_ = (TrsmDesc *)dev_alloc(bytes, routine);
+    const size_t bytes = (descs.size() * sizeof(TrsmDesc) + 255) / 256 * 256;
+    TrsmDesc *dd_ = (TrsmDesc *)dev_alloc(bytes + (size_t)xop_elems * sizeof(fx::Op), routine);
     if (!dd_) return mwblas_last_error();
-    cudaMemcpyAsync(dd_, descs.data(), bytes, cudaMemcpyHostToDevice, stream());
+    fx::Op *xops = (fx::Op *)((char *)dd_ + bytes);
+    cudaMemcpyAsync(dd_, descs.data(), descs.size() * sizeof(TrsmDesc), cudaMemcpyHostToDevice, stream());
     const bool trans = (T != 'N');
     const bool lower = ((U == 'L') != trans);
     const int warps = 4;
     const int64_t blocks = (work + warps - 1) / warps;
     k_trsm_grouped<<<(unsigned)blocks, warps * 32, 0, stream()>>>(dd_, (int)descs.size(), work, S == 'L' ? 0 : 1,
-                                                                  lower ? 1 : 0, trans ? 1 : 0, D == 'U' ? 1 : 0);
+                                                                  lower ? 1 : 0, trans ? 1 : 0, D == 'U' ? 1 : 0,
+                                                                  xops);
     count_launch();
     dev_free(dd_);
     if (!finish(routine)) return mwblas_last_error();
