@@ -295,7 +295,7 @@ __device__ __forceinline__ dd::real dd_recip(dd::real b)
 // multiplication by the reciprocal. All lanes stay in the loop (lanes past
 // the last right-hand side do the work on a clamped column and store
 // nothing) so that the shuffles see the whole warp.
-__global__ void __launch_bounds__(128) k_trsm_grouped(const TrsmDesc *__restrict__ descs, int count, int64_t total,
+__global__ void __launch_bounds__(128, 4) k_trsm_grouped(const TrsmDesc *__restrict__ descs, int count, int64_t total,
                                                      int side, int lower, int trans, int unit, fx::Op *xops)
 {
     // per warp: a tile of the current row of op(A), split into digits once
@@ -360,7 +360,19 @@ __global__ void __launch_bounds__(128) k_trsm_grouped(const TrsmDesc *__restrict
             }
             __syncwarp();
             const fx::Op *xp = xw + (int64_t)t0 * 32 + lane;
-            for (int q = 0; q < tl; ++q, xp += 32) {
+            int q = 0;
+            // four solutions loaded ahead of their products, so the loads overlap
+            for (; q + 4 <= tl; q += 4, xp += 128) {
+                fx::Op xo[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) xo[u] = xp[32 * u];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    xo[u].flags ^= fx::kNeg;
+                    acc.add_dig(xo[u], arow[q + u]);
+                }
+            }
+            for (; q < tl; ++q, xp += 32) {
                 fx::Op xo = *xp;
                 xo.flags ^= fx::kNeg;
                 acc.add_dig(xo, arow[q]);
