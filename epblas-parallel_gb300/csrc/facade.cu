@@ -178,12 +178,30 @@ void gemm_entry(const char *routine, bool cplx, int force_engine, const char *tr
             const char *r;
             ~JoinCopies() { join_copy_stream(r); }
         } join_guard{routine};
-        if (!stage_matrix_async(SA, a, nrowa, TA == 'N' ? K : M, *lda, es, true, hs.a_ready, routine)) return;
-        // op(B) and C in about eight blocks of whole 256-column tiles, queued
-        // as (B block, C block) pairs in the order the engine uses them
+        // op(B) and C in about eight blocks of whole 256-column tiles; with
+        // them, op(A) in about four blocks of whole 256-row tiles. Queued in
+        // the order the engine uses them: A0, B0, A1.., C0, B1, C1, ...
         int64_t w = ((N + 7) / 8 + 255) / 256 * 256;
         if (w < 512) w = 512;
-        if (w < N) {
+        int64_t h = ((M + 3) / 4 + 255) / 256 * 256;
+        if (h < 512) h = 512;
+        const bool colblocks = w < N, rowblocks = colblocks && h < M;
+        auto upload_a = [&](int64_t i0) -> bool {
+            const int64_t i1 = (M - i0 < h) ? M : i0 + h;
+            cudaEvent_t e = nullptr;
+            const bool ok = TA == 'N' ? upload_block_async(SA, i0, i1, 0, K, e, routine)
+                                      : upload_block_async(SA, 0, K, i0, i1, e, routine);
+            hs.a_block.push_back(e);
+            return ok;
+        };
+        if (rowblocks) {
+            hs.a_rows = h;
+            if (!stage_matrix(SA, a, nrowa, TA == 'N' ? K : M, *lda, es, false, routine)) return;
+            if (!upload_a(0)) return;
+        } else if (!stage_matrix_async(SA, a, nrowa, TA == 'N' ? K : M, *lda, es, true, hs.a_ready, routine)) {
+            return;
+        }
+        if (colblocks) {
             hs.block_cols = w;
             if (!stage_matrix(SB, b, nrowb, TB == 'N' ? N : K, *ldb, es, false, routine)) return;
             if (!stage_matrix(SC, c, M, N, *ldc, es, false, routine)) return;
@@ -194,6 +212,9 @@ void gemm_entry(const char *routine, bool cplx, int force_engine, const char *tr
                                            : upload_block_async(SB, j0, j1, 0, K, eb, routine);
                 hs.b_block.push_back(eb);
                 if (!okb) return;
+                if (j0 == 0 && rowblocks)
+                    for (int64_t i0 = h; i0 < M; i0 += h)
+                        if (!upload_a(i0)) return;
                 const bool okc = g.beta_kind == 0 || upload_block_async(SC, 0, M, j0, j1, ec, routine);
                 hs.c_block.push_back(ec);
                 if (!okc) return;

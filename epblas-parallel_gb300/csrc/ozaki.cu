@@ -834,7 +834,7 @@ constexpr int T2_SMEM = T2_STAGES * (T2_A_BYTES + T2_B_BYTES) + 1024 + 256;
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TCP_THREADS, 1)
     k_oz_gemm_tc_2sm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t Mp,
                      int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint16_t *__restrict__ R,
-                     int *status, int uplo, int tiles_m2, int tiles_n, int nz, int tn0)
+                     int *status, int uplo, int tiles_m2, int tiles_n, int nz, int tn0, int tm0)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -857,8 +857,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TCP_THREADS, 1)
     const int nch = (nsteps + kcs - 1) / kcs;
     const int64_t units = (int64_t)nz * tiles_m2 * tiles_n;
     auto unit_at = [&](int64_t u, int &tn, int &tm2, int &l) -> bool {
-        tn = tn0 + (int)(u % tiles_n);   // column tiles [tn0, tn0 + tiles_n) of the product
-        tm2 = (int)((u / tiles_n) % tiles_m2);
+        tn = tn0 + (int)(u % tiles_n);             // column tiles [tn0, tn0 + tiles_n)
+        tm2 = tm0 + (int)((u / tiles_n) % tiles_m2);   // row tile pairs [tm0, tm0 + tiles_m2)
         l = (int)(u / ((int64_t)tiles_n * tiles_m2));
         const int64_t i0 = (int64_t)tm2 * 256, j0 = (int64_t)tn * TC_BN;
         return !((uplo == 1 && i0 > j0 + TC_BN - 1) || (uplo == 2 && i0 + 255 < j0));
@@ -1481,11 +1481,12 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     // reconstruction, so its copy runs under the residue GEMMs.
     HostStage *hs = g.hs;
     phase_mark(PH_EXP);
+    const bool a_blocks = hs && hs->a_rows > 0;   // op(A) scanned and converted block by block below
     if (hs && !wait_event(hs->a_ready, routine)) {
         dev_free(ex);
         return false;
     }
-    launch_exp_rows_of_op(g.A, g.ta ? k : m, g.ta ? m : k, g.lda, g.ta, E, ea);
+    if (!a_blocks) launch_exp_rows_of_op(g.A, g.ta ? k : m, g.ta ? m : k, g.lda, g.ta, E, ea);
     if (!hs) launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, E, eb);
 
     // 2. precision and moduli (complex: |Re|, |Im| <= 2k * 2^(2bits-2))
@@ -1519,14 +1520,33 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     // back while later blocks are still being uploaded.
     const bool blocked = hs && hs->block_cols > 0 && mma_kind() == 3 && !shared_ops && g.uplo == 0 && !g.herm;
     const bool ok_pre = !(hs && hs->block_cols > 0 && !blocked) || hs->wait_all(routine);
-    const double2 *Ad = (const double2 *)g.A;
     // op(A) = A: A[i + p*lda] is contiguous along rows; op(A) = A^T along k.
-    if (cplx) {
-        if (!g.ta) launch_residues<true, true>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
-        else launch_residues<false, true>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, g.ca);
-    } else {
-        if (!g.ta) launch_residues<true, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
-        else launch_residues<false, false>(m, k, Ad, g.lda, ea, bits, rp, Ares, Mp, Kp, 0);
+    // Rows [i0, i0 + ni) of op(A), with their exponent bounds, go to residue
+    // rows [i0, i0 + rpad) of every plane (zeros past m).
+    auto a_rows_at = [&](int64_t i0) { return (const double2 *)g.A + (int64_t)E * (g.ta ? i0 * g.lda : i0); };
+    auto convert_A = [&](int64_t i0, int64_t ni, int64_t rpad) {
+        const double2 *Ai = a_rows_at(i0);
+        __half *Ao = Ares + i0 * Kp;
+        if (cplx) {
+            if (!g.ta) launch_residues<true, true>(ni, k, Ai, g.lda, ea + i0, bits, rp, Ao, rpad, Kp, g.ca, Mp);
+            else launch_residues<false, true>(ni, k, Ai, g.lda, ea + i0, bits, rp, Ao, rpad, Kp, g.ca, Mp);
+        } else {
+            if (!g.ta) launch_residues<true, false>(ni, k, Ai, g.lda, ea + i0, bits, rp, Ao, rpad, Kp, 0, Mp);
+            else launch_residues<false, false>(ni, k, Ai, g.lda, ea + i0, bits, rp, Ao, rpad, Kp, 0, Mp);
+        }
+    };
+    // row block ib of op(A): wait for it, scan its exponents, convert it
+    auto a_block = [&](int64_t ib) {
+        const int64_t h = hs->a_rows, i0 = ib * h, ni = (m - i0 < h) ? m - i0 : h;
+        wait_event(ib < (int64_t)hs->a_block.size() ? hs->a_block[ib] : nullptr, routine);
+        launch_exp_rows_of_op(a_rows_at(i0), g.ta ? k : ni, g.ta ? ni : k, g.lda, g.ta, E, ea + i0);
+        convert_A(i0, ni, i0 + h >= m ? Mp - i0 : ni);
+    };
+    const int64_t n_ablocks = a_blocks ? (m + hs->a_rows - 1) / hs->a_rows : 0;
+    if (!a_blocks) {
+        convert_A(0, m, Mp);
+    } else if (!blocked) {
+        for (int64_t ib = 0; ib < n_ablocks; ++ib) a_block(ib);
     }
     // op(B)(p, j) = B[p + j*ldb] is contiguous along k; op(B) = B^T along the
     // columns j. Columns [j0, j0 + nn) of op(B), and their exponent bounds,
@@ -1559,16 +1579,17 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     bool ok = ok_pre;
     const int nz = nc * md.n;
     CUtensorMap ma, mb;
-    // CTA-pair kernel over the column tiles [tn0, tn0 + ntn) of the product
-    auto pair_gemm = [&](int tn0, int ntn) {
+    // CTA-pair kernel over the column tiles [tn0, tn0 + ntn) and the 256-row
+    // tile pairs [tm0, tm0 + ntm) of the product (ntm = 0: all of them)
+    auto pair_gemm = [&](int tn0, int ntn, int tm0 = 0, int ntm = 0) {
         cudaFuncSetAttribute(k_oz_gemm_tc_2sm, cudaFuncAttributeMaxDynamicSharedMemorySize, T2_SMEM);
-        const int tiles_m2 = (int)(Mp / 256);
+        const int tiles_m2 = ntm > 0 ? ntm : (int)(Mp / 256);
         const int64_t units = (int64_t)nz * tiles_m2 * ntn;
         const int64_t pairs = device_sm_count() / 2;
         const unsigned grid = 2u * (unsigned)(units < pairs ? units : pairs);
         k_oz_gemm_tc_2sm<<<grid, TCP_THREADS, T2_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R,
                                                                    device_status_word(), g.uplo, tiles_m2, ntn, nz,
-                                                                   tn0);
+                                                                   tn0, tm0);
     };
     if (blocked) {
         // launched block by block with the reconstruction below
@@ -1651,12 +1672,31 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         for (int64_t j0 = 0, jb = 0; ok && j0 < n; j0 += w, ++jb) {
             const int64_t nn = (n - j0 < w) ? n - j0 : w;
             const bool last = j0 + w >= n;
-            ok = wait_event(jb < (int64_t)hs->b_block.size() ? hs->b_block[jb] : nullptr, routine);
-            if (!ok) break;
-            exp_B(j0, nn);
-            convert_B(j0, nn, last ? Np - j0 : nn);
-            pair_gemm((int)(j0 / TC_BN), (int)((last ? Np - j0 : nn) / TC_BN));
-            count_launch();
+            const int ntn = (int)((last ? Np - j0 : nn) / TC_BN);
+            if (jb == 0 && a_blocks) {
+                // the first column block row block by row block, as A arrives
+                for (int64_t ib = 0; ib < n_ablocks; ++ib) {
+                    a_block(ib);
+                    if (ib == 0) {
+                        ok = wait_event(hs->b_block.empty() ? nullptr : hs->b_block[0], routine);
+                        if (!ok) break;
+                        exp_B(j0, nn);
+                        convert_B(j0, nn, last ? Np - j0 : nn);
+                    }
+                    const int64_t i0 = ib * hs->a_rows;
+                    const int64_t rows = (i0 + hs->a_rows >= m) ? Mp - i0 : hs->a_rows;
+                    pair_gemm(0, ntn, (int)(i0 / 256), (int)(rows / 256));
+                    count_launch();
+                }
+                if (!ok) break;
+            } else {
+                ok = wait_event(jb < (int64_t)hs->b_block.size() ? hs->b_block[jb] : nullptr, routine);
+                if (!ok) break;
+                exp_B(j0, nn);
+                convert_B(j0, nn, last ? Np - j0 : nn);
+                pair_gemm((int)(j0 / TC_BN), ntn);
+                count_launch();
+            }
             ok = wait_event(jb < (int64_t)hs->c_block.size() ? hs->c_block[jb] : nullptr, routine);
             if (!ok) break;
             reconstruct_cols(j0, nn);

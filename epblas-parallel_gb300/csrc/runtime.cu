@@ -300,6 +300,8 @@ HostStage::~HostStage()
 {
     for (cudaEvent_t e : {a_ready, b_ready, c_ready})
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : a_block)
+        if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : b_block)
         if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : c_block)

@@ -99,16 +99,20 @@ bool join_copy_stream(const char *routine);
 // and may write C back itself in column chunks behind its own kernels.
 // With block_cols > 0, op(B) and C arrive instead in blocks of that many
 // columns (block j: columns [j * block_cols, ...)), one event per block, so
-// that the product of block j can start when its columns are in.
+// that the product of block j can start when its columns are in; with
+// a_rows > 0 (only together with column blocks), op(A) arrives in blocks of
+// that many rows, and the first column block is multiplied row block by row
+// block while the rest of A is still on its way.
 struct HostStage {
     cudaEvent_t a_ready = nullptr, b_ready = nullptr, c_ready = nullptr;
-    int64_t block_cols = 0;
-    std::vector<cudaEvent_t> b_block, c_block;
+    int64_t block_cols = 0, a_rows = 0;
+    std::vector<cudaEvent_t> a_block, b_block, c_block;
     Staged *c = nullptr;       // the staged C (target of the write-back)
     bool c_written = false;    // the engine has queued C's copy back and joined
     bool wait_all(const char *routine) const
     {
         bool ok = wait_event(a_ready, routine) && wait_event(b_ready, routine) && wait_event(c_ready, routine);
+        for (cudaEvent_t e : a_block) ok = ok && wait_event(e, routine);
         for (cudaEvent_t e : b_block) ok = ok && wait_event(e, routine);
         for (cudaEvent_t e : c_block) ok = ok && wait_event(e, routine);
         return ok;
