@@ -180,7 +180,9 @@ void gemm_entry(const char *routine, bool cplx, int force_engine, const char *tr
         } join_guard{routine};
         // op(B) and C in about eight blocks of whole 256-column tiles; with
         // them, op(A) in about four blocks of whole 256-row tiles. Queued in
-        // the order the engine uses them: A0, B0, A1.., C0, B1, C1, ...
+        // the order the engine uses them: A0, B0, B1, A1.., C0, C1, B2, C2, ...
+        // (two column blocks are multiplied while A arrives: about the work
+        // that keeps pace with the copies)
         int64_t w = ((N + 7) / 8 + 255) / 256 * 256;
         if (w < 512) w = 512;
         int64_t h = ((M + 3) / 4 + 255) / 256 * 256;
@@ -203,22 +205,31 @@ void gemm_entry(const char *routine, bool cplx, int force_engine, const char *tr
         }
         if (colblocks) {
             hs.block_cols = w;
+            const int64_t nblocks = (N + w - 1) / w;
+            const int64_t early = rowblocks ? (nblocks < 2 ? nblocks : 2) : 0;
+            hs.early_blocks = early;
             if (!stage_matrix(SB, b, nrowb, TB == 'N' ? N : K, *ldb, es, false, routine)) return;
             if (!stage_matrix(SC, c, M, N, *ldc, es, false, routine)) return;
-            for (int64_t j0 = 0; j0 < N; j0 += w) {
-                const int64_t j1 = (N - j0 < w) ? N : j0 + w;
-                cudaEvent_t eb = nullptr, ec = nullptr;
-                const bool okb = TB == 'N' ? upload_block_async(SB, 0, K, j0, j1, eb, routine)
-                                           : upload_block_async(SB, j0, j1, 0, K, eb, routine);
-                hs.b_block.push_back(eb);
-                if (!okb) return;
-                if (j0 == 0 && rowblocks)
-                    for (int64_t i0 = h; i0 < M; i0 += h)
-                        if (!upload_a(i0)) return;
-                const bool okc = g.beta_kind == 0 || upload_block_async(SC, 0, M, j0, j1, ec, routine);
-                hs.c_block.push_back(ec);
-                if (!okc) return;
-            }
+            hs.b_block.assign((size_t)nblocks, nullptr);
+            hs.c_block.assign((size_t)nblocks, nullptr);
+            auto upload_b = [&](int64_t jb) -> bool {
+                const int64_t j0 = jb * w, j1 = (N - j0 < w) ? N : j0 + w;
+                return TB == 'N' ? upload_block_async(SB, 0, K, j0, j1, hs.b_block[jb], routine)
+                                 : upload_block_async(SB, j0, j1, 0, K, hs.b_block[jb], routine);
+            };
+            auto upload_c = [&](int64_t jb) -> bool {
+                const int64_t j0 = jb * w, j1 = (N - j0 < w) ? N : j0 + w;
+                return g.beta_kind == 0 || upload_block_async(SC, 0, M, j0, j1, hs.c_block[jb], routine);
+            };
+            for (int64_t jb = 0; jb < early; ++jb)
+                if (!upload_b(jb)) return;
+            if (rowblocks)
+                for (int64_t i0 = h; i0 < M; i0 += h)
+                    if (!upload_a(i0)) return;
+            for (int64_t jb = 0; jb < early; ++jb)
+                if (!upload_c(jb)) return;
+            for (int64_t jb = early; jb < nblocks; ++jb)
+                if (!upload_b(jb) || !upload_c(jb)) return;
         } else {
             if (!stage_matrix_async(SB, b, nrowb, TB == 'N' ? N : K, *ldb, es, true, hs.b_ready, routine)) return;
             if (!stage_matrix_async(SC, c, M, N, *ldc, es, g.beta_kind != 0, hs.c_ready, routine)) return;

@@ -1669,34 +1669,48 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         // block j: its columns of op(B) in, converted, multiplied, reconstructed
         // and copied back; the uploads of later blocks run meanwhile
         const int64_t w = hs->block_cols;
-        for (int64_t j0 = 0, jb = 0; ok && j0 < n; j0 += w, ++jb) {
+        auto ev = [&](const std::vector<cudaEvent_t> &v, int64_t i) -> cudaEvent_t {
+            return i < (int64_t)v.size() ? v[i] : nullptr;
+        };
+        int64_t first = 0;   // column blocks done in the row-blocked phase
+        if (a_blocks && hs->early_blocks > 0) {
+            // the first early_blocks column blocks row block by row block, as A arrives
+            first = hs->early_blocks;
+            const int64_t jend = (first * w < n) ? first * w : n;
+            const int ntn = (int)(((jend >= n) ? Np : jend) / TC_BN);
+            for (int64_t ib = 0; ok && ib < n_ablocks; ++ib) {
+                a_block(ib);
+                for (int64_t jb = 0; ok && ib == 0 && jb < first; ++jb) {
+                    const int64_t j0 = jb * w, nn = (n - j0 < w) ? n - j0 : w;
+                    ok = wait_event(ev(hs->b_block, jb), routine);
+                    if (!ok) break;
+                    exp_B(j0, nn);
+                    convert_B(j0, nn, (j0 + w >= n) ? Np - j0 : nn);
+                }
+                if (!ok) break;
+                const int64_t i0 = ib * hs->a_rows;
+                const int64_t rows = (i0 + hs->a_rows >= m) ? Mp - i0 : hs->a_rows;
+                pair_gemm(0, ntn, (int)(i0 / 256), (int)(rows / 256));
+                count_launch();
+            }
+            for (int64_t jb = 0; ok && jb < first; ++jb) {
+                const int64_t j0 = jb * w, nn = (n - j0 < w) ? n - j0 : w;
+                ok = wait_event(ev(hs->c_block, jb), routine);
+                if (!ok) break;
+                reconstruct_cols(j0, nn);
+                ok = unstage_columns_async(*hs->c, j0, j0 + nn, routine);
+            }
+        }
+        for (int64_t j0 = first * w, jb = first; ok && j0 < n; j0 += w, ++jb) {
             const int64_t nn = (n - j0 < w) ? n - j0 : w;
             const bool last = j0 + w >= n;
             const int ntn = (int)((last ? Np - j0 : nn) / TC_BN);
-            if (jb == 0 && a_blocks) {
-                // the first column block row block by row block, as A arrives
-                for (int64_t ib = 0; ib < n_ablocks; ++ib) {
-                    a_block(ib);
-                    if (ib == 0) {
-                        ok = wait_event(hs->b_block.empty() ? nullptr : hs->b_block[0], routine);
-                        if (!ok) break;
-                        exp_B(j0, nn);
-                        convert_B(j0, nn, last ? Np - j0 : nn);
-                    }
-                    const int64_t i0 = ib * hs->a_rows;
-                    const int64_t rows = (i0 + hs->a_rows >= m) ? Mp - i0 : hs->a_rows;
-                    pair_gemm(0, ntn, (int)(i0 / 256), (int)(rows / 256));
-                    count_launch();
-                }
-                if (!ok) break;
-            } else {
-                ok = wait_event(jb < (int64_t)hs->b_block.size() ? hs->b_block[jb] : nullptr, routine);
-                if (!ok) break;
-                exp_B(j0, nn);
-                convert_B(j0, nn, last ? Np - j0 : nn);
-                pair_gemm((int)(j0 / TC_BN), ntn);
-                count_launch();
-            }
+            ok = wait_event(ev(hs->b_block, jb), routine);
+            if (!ok) break;
+            exp_B(j0, nn);
+            convert_B(j0, nn, last ? Np - j0 : nn);
+            pair_gemm((int)(j0 / TC_BN), ntn);
+            count_launch();
             ok = wait_event(jb < (int64_t)hs->c_block.size() ? hs->c_block[jb] : nullptr, routine);
             if (!ok) break;
             reconstruct_cols(j0, nn);

@@ -101,11 +101,12 @@ bool join_copy_stream(const char *routine);
 // columns (block j: columns [j * block_cols, ...)), one event per block, so
 // that the product of block j can start when its columns are in; with
 // a_rows > 0 (only together with column blocks), op(A) arrives in blocks of
-// that many rows, and the first column block is multiplied row block by row
-// block while the rest of A is still on its way.
+// that many rows, and the first `early_blocks` column blocks (uploaded right
+// after A's first row block) are multiplied row block by row block while the
+// rest of A is still on its way.
 struct HostStage {
     cudaEvent_t a_ready = nullptr, b_ready = nullptr, c_ready = nullptr;
-    int64_t block_cols = 0, a_rows = 0;
+    int64_t block_cols = 0, a_rows = 0, early_blocks = 0;
     std::vector<cudaEvent_t> a_block, b_block, c_block;
     Staged *c = nullptr;       // the staged C (target of the write-back)
     bool c_written = false;    // the engine has queued C's copy back and joined
