@@ -1156,6 +1156,8 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
     double2 *pc = C + i0 + (int64_t)blockIdx.y * ldc;
     const int64_t rstep = (int64_t)jstep * Mp, cstep = (int64_t)jstep * ldc;
     for (int j = blockIdx.y; j < n; j += jstep, rcol += rstep, pc += cstep) {
+        // both rows outside the stored triangle: nothing to compute
+        if ((uplo == 1 && i0 > j) || (uplo == 2 && i0 + 1 < j)) continue;
         const int ebj = eb[j];
         crt::Frac acc0, acc1;
         acc0.reset();
