@@ -434,7 +434,7 @@ def tc_traffic_from_profile():
 
 WORKLOADS = ("gemm", "stress", "wgemm", "gemm_t", "gemm_fixed", "gemm_plain", "syrk", "herk", "trsm", "gemv", "dot",
              "axpy", "scal", "copy", "swap", "iamax", "batched_gemm", "batched_trsm", "gemmtr", "symm", "syr2k",
-             "trmm", "wtrsm", "sbmv", "spmv")
+             "trmm", "wtrsm", "sbmv", "spmv", "tbsv")
 
 
 def _dev_dd(torch, shape, gen, dev, cplx_=False):
@@ -852,6 +852,41 @@ def run_workload(args):
             op = orc.dd_abs(al) * (2 * k + 1 if band else n) * orc.dd_absmax(hb(A[:1 << 20])) * orc.dd_absmax(hx) \
                 + orc.dd_abs(be) * orc.dd_absmax(hy0)
             check["normwise_err_sampled"] = orc.normwise_error(np.array(got), np.array(want), op)
+            check["rows_checked"] = len(rows)
+    elif w == "tbsv":
+        # lower band triangular solve, n = 2^20, k = 16, A read in place from its band
+        n = args.size or (1 << 20)
+        k = 16
+        A = _dev_dd(torch, (n, k + 1), gen, dev)                  # band storage: row 0 is the diagonal
+        A[:, 1:] /= 4 * k
+        A[:, 0, 0] = 1.0 + torch.rand(n, generator=gen, device=dev, dtype=torch.float64)
+        A[:, 0, 1] = 0.0
+        x = _dev_dd(torch, (n,), gen, dev)
+        x0 = x.clone()
+        fn = lambda: lib.l2("mtbsv", "L", "N", "N", n, k, (A.data_ptr(),), k + 1, (x.data_ptr(),), 1)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: x.copy_(x0))
+        nbytes = 16.0 * (n * (k + 1) + 2 * n)
+        value, unit = nbytes / ms / 1e6, "GB/s"
+        metric = f"DD-TBSV GB/s n={n} k={k} lower (16(n(k+1) + 2n) bytes; one warp, sequential in n)"
+        cfg = {"workload": f"mtbsv_ L N N n={n} k={k} incx=1, diagonal U[1,2), off-diagonal U[-1,1)/(4k)"}
+        if o:
+            x.copy_(x0)
+            fn()
+            hA, hx, hbv = hb(A), hb(x), hb(x0)
+            rows = np.sort(rng.choice(n, 32, replace=False))
+            got, want = [], []
+            for r in rows:
+                c0 = max(0, r - k)
+                cs = np.arange(c0, r + 1)
+                row = hA[cs, r - cs]                                   # A(r, c) = AB(r - c, c)
+                rv = np.ascontiguousarray(row[:, None, :])
+                res = np.zeros((1, 2))
+                o.qgemv("N", 1, len(cs), np.array([1.0, 0.0]), rv, 1, np.ascontiguousarray(hx[c0:r + 1]), 1,
+                        np.array([0.0, 0.0]), res, 1)
+                got.append(res[0])
+                want.append(hbv[r])
+            scale = (k + 1) * orc.dd_absmax(hA[:4096]) * orc.dd_absmax(hx)
+            check["normwise_residual_sampled"] = orc.normwise_error(np.array(got), np.array(want), scale)
             check["rows_checked"] = len(rows)
     elif w in ("scal", "copy", "swap", "iamax"):
         # HBM-bound level-1 moves at n = 2^28 (SCAL bit-exact, FP64-bound by its operation sequence)

@@ -8,6 +8,7 @@
 // values follow the reference's *_core functions line for line; the checks
 // the reference does not have (leading dimensions, flag letters, null
 // pointers) record an error and leave the outputs untouched.
+#include <atomic>
 #include <cctype>
 #include <cstring>
 
@@ -112,6 +113,8 @@ bool run_gemm(GemmArgs &g, bool cplx, int force_engine, const char *routine)
     }
     return cplx ? gemm_plain_cplx(g, routine) : gemm_plain_real(g, routine);
 }
+
+std::atomic<int> g_band_solve{MWBLAS_BAND_SOLVE_AUTO};
 
 namespace {
 
@@ -1220,6 +1223,17 @@ void trv_entry(const char *routine, bool cplx, bool solve, int fmt, const char *
     if (!stage_vector(SX, x, N, *incx, es, true, dix, routine)) return;
     void *dense = nullptr;
     char Dd = D;
+    const int band_mode = g_band_solve.load();
+    if (fmt == 1 && solve &&
+        (band_mode == MWBLAS_BAND_SOLVE_IN_PLACE ||
+         (band_mode == MWBLAS_BAND_SOLVE_AUTO && (double)N * (double)N * (double)es > 268435456.0))) {
+        // solved in place from the band (a dense copy would be too large, or asked for)
+        if (!stage_matrix(SA, a, K + 1, N, *lda, es, true, routine)) return;
+        if (!tbsv_device(cplx, U, T, D, N, K, SA.dev, *lda, SX.dev, dix, routine)) return;
+        if (!unstage_vector(SX, routine)) return;
+        finish(routine);
+        return;
+    }
     if (fmt != 0 && !solve) {
         // x := op(A) x with A read in place from its band or packed storage
         const int64_t len = N * (N + 1) / 2;
@@ -1853,6 +1867,12 @@ int mwblas_set_gemm_engine(int engine)
     return prev;
 }
 int mwblas_get_gemm_engine(void) { return mw::engine(); }
+int mwblas_set_band_solve(int mode)
+{
+    int prev = mw::g_band_solve.load();
+    if (mode >= MWBLAS_BAND_SOLVE_AUTO && mode <= MWBLAS_BAND_SOLVE_DENSE) mw::g_band_solve = mode;
+    return prev;
+}
 int mwblas_set_ozaki_bits(int bits)
 {
     int prev = mw::g_ozaki_bits;

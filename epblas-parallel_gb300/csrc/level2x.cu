@@ -323,6 +323,116 @@ __global__ void __launch_bounds__(256) k_smv(SmvParams p)
     }
 }
 
+// ---- triangular band solve, read in place ----------------------------------------------
+// op(A) x = b for a band triangle of bandwidth k, by one warp: rows are taken
+// 32 at a time in solve order (lane l owns the l-th row of the tile). Each
+// lane first sums its row's band entries against the solutions of earlier
+// tiles (independent across lanes); then 32 steps finish one row each: the
+// owner forms x_r = (b_r - s_r) * (1 / a_rr), broadcasts it, and the later
+// rows of the tile add their entry times x_r. The sums are double-double
+// (scalar operators): with a single warp, finishing a fixed-point sum per row
+// (a 256-bit conversion on one lane) costs more than the products. Work
+// O(n k), memory the band itself.
+struct TbsvParams {
+    int64_t n, k, ldab;
+    const double2 *AB;
+    int op;             // 0 'N', 1 'T', 2 'C'
+    bool upper, unit;   // stored triangle, unit diagonal
+    double2 *x;         // contiguous, b on entry
+};
+
+template <bool CX>
+__device__ __forceinline__ dd::cplx tbsv_entry(const TbsvParams &p, int64_t r, int64_t c)
+{
+    const int64_t i = p.op == 0 ? r : c, j = p.op == 0 ? c : r;
+    const double2 *a = p.AB + (CX ? 2 : 1) * ((p.upper ? p.k : 0) + i - j + j * p.ldab);
+    dd::cplx v;
+    v.re = dd::load(a);
+    v.im = CX ? dd::load(a + 1) : dd::make(0.0, 0.0);
+    if (CX && p.op == 2) v.im = dd::neg(v.im);
+    return v;
+}
+
+// s += a * x in double-double (scalar operators; complex: re = ar xr - ai xi,
+// im = ar xi + ai xr)
+template <bool CX>
+__device__ __forceinline__ void tbsv_add(dd::cplx &s, const dd::cplx &a, const dd::cplx &x)
+{
+    if (CX) {
+        s = dd::cadd_exact(s, dd::cmul_exact(a, x));
+    } else {
+        s.re = dd::add_exact(s.re, dd::mul_exact(a.re, x.re));
+    }
+}
+
+template <bool CX>
+__global__ void __launch_bounds__(32) k_tbsv(TbsvParams p)
+{
+    const int lane = threadIdx.x & 31;
+    const bool forward = p.upper == (p.op != 0);   // op(A) lower: rows in increasing order
+    auto row_of = [&](int64_t s) { return forward ? s : p.n - 1 - s; };
+    const dd::real zero = dd::make(0.0, 0.0);
+    for (int64_t t0 = 0; t0 < p.n; t0 += 32) {
+        const int64_t s = t0 + lane;
+        const bool live = s < p.n;
+        const int64_t r = live ? row_of(s) : row_of(p.n - 1);
+        dd::cplx acc{zero, zero};
+        dd::cplx b;
+        if (CX) {
+            b = dd::cload(p.x + 2 * r);
+        } else {
+            b.re = dd::load(p.x + r);
+            b.im = zero;
+        }
+        // 1/a_rr (complex: conj(d) / |d|^2)
+        dd::cplx inv{dd::make(1.0, 0.0), zero};
+        if (!p.unit) {
+            const dd::cplx d = tbsv_entry<CX>(p, r, r);
+            if (CX) {
+                const dd::real m2 = dd::add_exact(dd::mul_exact(d.re, d.re), dd::mul_exact(d.im, d.im));
+                const dd::real q = dd::div(dd::make(1.0, 0.0), m2);
+                inv.re = dd::mul_exact(d.re, q);
+                inv.im = dd::neg(dd::mul_exact(d.im, q));
+            } else {
+                inv.re = dd::div(dd::make(1.0, 0.0), d.re);
+            }
+        }
+        // solutions of earlier tiles within the band
+        if (live) {
+            for (int64_t s2 = (s - p.k > 0 ? s - p.k : 0); s2 < t0; ++s2) {
+                const int64_t c = row_of(s2);
+                dd::cplx xc;
+                xc.re = dd::load(p.x + (CX ? 2 * c : c));
+                xc.im = CX ? dd::load(p.x + 2 * c + 1) : zero;
+                tbsv_add<CX>(acc, tbsv_entry<CX>(p, r, c), xc);
+            }
+        }
+        // the tile, one row per step
+        const int steps = (p.n - t0 < 32) ? (int)(p.n - t0) : 32;
+        for (int u = 0; u < steps; ++u) {
+            dd::cplx v{zero, zero};
+            if (lane == u) {
+                v.re = dd::sub_exact(b.re, acc.re);
+                v.im = CX ? dd::sub_exact(b.im, acc.im) : zero;
+                if (!p.unit) {
+                    if (CX) v = dd::cmul_exact(v, inv);
+                    else v.re = dd::mul_exact(v.re, inv.re);
+                }
+                if (CX) dd::cstore(p.x + 2 * r, v);
+                else dd::store(p.x + r, v.re);
+            }
+            v.re.hi = __shfl_sync(0xffffffffu, v.re.hi, u);
+            v.re.lo = __shfl_sync(0xffffffffu, v.re.lo, u);
+            if (CX) {
+                v.im.hi = __shfl_sync(0xffffffffu, v.im.hi, u);
+                v.im.lo = __shfl_sync(0xffffffffu, v.im.lo, u);
+            }
+            if (live && lane > u && lane - u <= p.k) tbsv_add<CX>(acc, tbsv_entry<CX>(p, r, row_of(t0 + u)), v);
+        }
+        __syncwarp();
+    }
+}
+
 struct Buf {
     void *p = nullptr;
     Buf(size_t bytes, const char *routine) { p = dev_alloc(bytes, routine); }
@@ -464,6 +574,29 @@ bool mv_device(const MvArgs &a, const char *routine)
     }
     if (!ok) return false;
     vgather(ly, a.y, a.incy, e2, yb.p, false);
+    return true;
+}
+
+bool tbsv_device(bool cplx, char uplo, char trans, char diag, int64_t n, int64_t k, const void *AB, int64_t ldab,
+                 void *x, int64_t incx, const char *routine)
+{
+    const int e2 = cplx ? 2 : 1;
+    Buf xb((size_t)n * 16 * e2, routine);
+    if (!xb.p) return false;
+    vgather(n, x, incx, e2, xb.p, true);
+    TbsvParams p;
+    p.n = n;
+    p.k = k;
+    p.ldab = ldab;
+    p.AB = (const double2 *)AB;
+    p.op = trans == 'N' ? 0 : (trans == 'T' ? 1 : 2);
+    p.upper = uplo == 'U';
+    p.unit = diag == 'U';
+    p.x = (double2 *)xb.p;
+    if (cplx) k_tbsv<true><<<1, 32, 0, stream()>>>(p);
+    else k_tbsv<false><<<1, 32, 0, stream()>>>(p);
+    count_launch();
+    vgather(n, x, incx, e2, xb.p, false);
     return true;
 }
 

@@ -57,6 +57,12 @@ struct SmvArgs {
 };
 bool smv_device(const SmvArgs &a, const char *routine);
 
+// op(A) x = b with A a band triangle (LAPACK band storage, bandwidth k,
+// leading dimension ldab) read in place: one warp, 32-row tiles,
+// double-double row sums. x has any increment.
+bool tbsv_device(bool cplx, char uplo, char trans, char diag, int64_t n, int64_t k, const void *AB, int64_t ldab,
+                 void *x, int64_t incx, const char *routine);
+
 // Rank updates: uplo 0: GER (A m x n += alpha x op(y), conj for GERC);
 // uplo 1/2 (upper/lower triangle of the n = m square A): SYR/HER (y null),
 // SYR2/HER2; conj selects the Hermitian forms.

@@ -142,6 +142,7 @@ class MWBlas:
             self._sig("mgemm_ozaki_64_", None, [_ch, _ch, PI, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
             self._sig("mgemm_fixed_64_", None, [_ch, _ch, PI, PI, PI, R, _p, PI, _p, PI, R, _p, PI])
             self._sig("mwblas_set_gemm_engine", _i32, [_i32])
+            self._sig("mwblas_set_band_solve", _i32, [_i32])
             self._sig("mwblas_get_gemm_engine", _i32, [])
             self._sig("mwblas_set_ozaki_bits", _i32, [_i32])
             self._sig("mwblas_last_ozaki_moduli", _i32, [])

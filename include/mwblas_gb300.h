@@ -440,6 +440,13 @@ enum { MWBLAS_GEMM_AUTO = 0, MWBLAS_GEMM_PLAIN = 1, MWBLAS_GEMM_OZAKI = 2, MWBLA
 int mwblas_set_gemm_engine(int engine);   /* returns the previous value */
 int mwblas_get_gemm_engine(void);
 
+/* Triangular band solves (mtbsv_/wtbsv_): MWBLAS_BAND_SOLVE_AUTO solves in
+ * place from the band (one warp, O(n k) memory) when a dense copy of the
+ * triangle would exceed 256 MB, and through a dense copy and the blocked TRSM
+ * otherwise (faster at those sizes); the other two values force one way. */
+enum { MWBLAS_BAND_SOLVE_AUTO = 0, MWBLAS_BAND_SOLVE_IN_PLACE = 1, MWBLAS_BAND_SOLVE_DENSE = 2 };
+int mwblas_set_band_solve(int mode);   /* returns the previous value */
+
 /* Same arguments as mgemm_64_, forcing one engine. */
 void mgemm_plain_64_(const char *transa, const char *transb, const int64_t *m,
                      const int64_t *n, const int64_t *k, const MWBLAS_R *alpha,

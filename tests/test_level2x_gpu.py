@@ -182,7 +182,7 @@ def test_triangular_mv_and_solve(gpu, oracle, rng, kind, c, uplo, trans, diag):
     if trans == "C" and not c:
         pytest.skip("real 'C' folds to 'T'")
     p = "w" if c else "m"
-    for n, k in [(1, 0), (60, 7)]:
+    for n, k in [(1, 0), (60, 7), (200, 45), (150, 70)]:
         A = dense(rng, n, n, c) / n
         d = np.arange(n)
         A[d, d] = ONE[c] * 0 + (np.array([[1.5, 0.0], [0.0, 0.0]]) if c else np.array([1.5, 0.0]))
@@ -210,16 +210,20 @@ def test_triangular_mv_and_solve(gpu, oracle, rng, kind, c, uplo, trans, diag):
         assert err_ok(gather(got, n, inc), want, scale, max(10, 4 * n) * orc.EPS_DD), (n, "mv")
         # solve: residual op(T) x - b in binary128
         b = vecs(rng, n, inc, c)
-        sol = b.copy()
-        args = (uplo, trans, diag, n) + ((k,) if kind == "tb" else ()) + (Tin,) + \
-            (() if kind == "tp" else ((k + 1) if kind == "tb" else n,)) + (sol, inc)
-        gpu.l2(p + kind + "sv", *args)
-        assert gpu.last_error()[0] == 0, gpu.last_error()
-        xs = gather(sol, n, inc)
-        r = matvec(oracle, c, trans if c else ("T" if trans != "N" else "N"), T, n, n, xs, ONE[c], ZERO[c],
-                   np.zeros_like(xs))
-        scale = n * orc.dd_absmax(T) * orc.dd_absmax(xs) + orc.dd_absmax(b)
-        assert err_ok(r, gather(b, n, inc), scale, max(20, 8 * n) * orc.EPS_DD), (n, "sv")
+        # band solves both in place from the band (1) and through a dense copy (2)
+        for mode in ((1, 2) if kind == "tb" else (0,)):
+            prev = gpu.lib.mwblas_set_band_solve(mode)
+            sol = b.copy()
+            args = (uplo, trans, diag, n) + ((k,) if kind == "tb" else ()) + (Tin,) + \
+                (() if kind == "tp" else ((k + 1) if kind == "tb" else n,)) + (sol, inc)
+            gpu.l2(p + kind + "sv", *args)
+            gpu.lib.mwblas_set_band_solve(prev)
+            assert gpu.last_error()[0] == 0, gpu.last_error()
+            xs = gather(sol, n, inc)
+            r = matvec(oracle, c, trans if c else ("T" if trans != "N" else "N"), T, n, n, xs, ONE[c], ZERO[c],
+                       np.zeros_like(xs))
+            scale = n * orc.dd_absmax(T) * orc.dd_absmax(xs) + orc.dd_absmax(b)
+            assert err_ok(r, gather(b, n, inc), scale, max(20, 8 * n) * orc.EPS_DD), (n, "sv", mode)
 
 
 @pytest.mark.parametrize("name", ["mger", "wgeru", "wgerc"])
