@@ -113,11 +113,28 @@ bool g_timing = false;
 thread_local cudaEvent_t t_ev[PH_N + 1] = {};
 thread_local float t_phase_ms[PH_N] = {};
 
+// Residue GEMM launches of a blocked product, timed one by one (their sum is
+// the GEMM phase; the rest of the block loop is reported as reconstruction).
+constexpr int kTimedGemms = 64;
+thread_local cudaEvent_t t_gev[2 * kTimedGemms] = {};
+thread_local int t_gemm_n = 0;
+
 void phase_mark(int i)
 {
     if (!g_timing) return;
+    if (i == PH_EXP) t_gemm_n = 0;
     if (!t_ev[i]) cudaEventCreate(&t_ev[i]);
     cudaEventRecord(t_ev[i], stream());
+}
+
+void gemm_mark(bool begin)
+{
+    if (!g_timing) return;
+    const int i = 2 * t_gemm_n + (begin ? 0 : 1);
+    if (i >= 2 * kTimedGemms) return;
+    if (!t_gev[i]) cudaEventCreate(&t_gev[i]);
+    cudaEventRecord(t_gev[i], stream());
+    if (!begin) ++t_gemm_n;
 }
 
 void phase_collect()
@@ -128,6 +145,17 @@ void phase_collect()
         float ms = 0.0f;
         if (t_ev[i] && t_ev[i + 1]) cudaEventElapsedTime(&ms, t_ev[i], t_ev[i + 1]);
         t_phase_ms[i] = ms;
+    }
+    if (t_gemm_n > 0) {
+        float sum = 0.0f;
+        for (int i = 0; i < t_gemm_n && i < kTimedGemms; ++i) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, t_gev[2 * i], t_gev[2 * i + 1]);
+            sum += ms;
+        }
+        const float span = t_phase_ms[PH_GEMM] + t_phase_ms[PH_REC];
+        t_phase_ms[PH_GEMM] = sum;
+        t_phase_ms[PH_REC] = span > sum ? span - sum : 0.0f;
     }
 }
 
@@ -1520,7 +1548,12 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     // op(B) and C arriving in column blocks (pair kernel, full output): the
     // columns of block j are converted, multiplied, reconstructed and copied
     // back while later blocks are still being uploaded.
-    const bool blocked = hs && hs->block_cols > 0 && mma_kind() == 3 && !shared_ops && g.uplo == 0 && !g.herm;
+    // (Device operands are not blocked: a reconstruction running beside the
+    // residue GEMM slows it by about as much as it hides, 8192^3: 17.2 ->
+    // 19.3 ms for 2.1 ms of reconstruction.)
+    const int64_t block_w = hs ? hs->block_cols : 0;
+    const bool blocked = block_w > 0 && block_w < n + TC_BN && mma_kind() == 3 && !shared_ops && g.uplo == 0 &&
+                         !g.herm;
     const bool ok_pre = !(hs && hs->block_cols > 0 && !blocked) || hs->wait_all(routine);
     // op(A) = A: A[i + p*lda] is contiguous along rows; op(A) = A^T along k.
     // Rows [i0, i0 + ni) of op(A), with their exponent bounds, go to residue
@@ -1668,11 +1701,23 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         count_launch();
     };
     if (ok && blocked) {
-        // block j: its columns of op(B) in, converted, multiplied, reconstructed
-        // and copied back; the uploads of later blocks run meanwhile
-        const int64_t w = hs->block_cols;
+        // block j: its columns of op(B) converted and multiplied on this stream;
+        // its reconstruction (and, for host arrays, write-back) on the side
+        // stream, where it runs beside the next blocks' residue GEMMs (the
+        // pair kernel leaves registers and shared memory for it on every SM)
+        const int64_t w = block_w;
+        static const std::vector<cudaEvent_t> none;
+        const std::vector<cudaEvent_t> &bev = hs ? hs->b_block : none, &cev = hs ? hs->c_block : none;
         auto ev = [&](const std::vector<cudaEvent_t> &v, int64_t i) -> cudaEvent_t {
             return i < (int64_t)v.size() ? v[i] : nullptr;
+        };
+        const cudaStream_t main_s = stream(), side = side_stream();
+        auto finish_block = [&](int64_t jb, int64_t j0, int64_t nn) -> bool {
+            if (!order_streams(main_s, side, routine)) return false;
+            StreamOverride so(side);
+            if (!wait_event(ev(cev, jb), routine)) return false;
+            reconstruct_cols(j0, nn);
+            return !hs || unstage_columns_async(*hs->c, j0, j0 + nn, routine);
         };
         int64_t first = 0;   // column blocks done in the row-blocked phase
         if (a_blocks && hs->early_blocks > 0) {
@@ -1684,7 +1729,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
                 a_block(ib);
                 for (int64_t jb = 0; ok && ib == 0 && jb < first; ++jb) {
                     const int64_t j0 = jb * w, nn = (n - j0 < w) ? n - j0 : w;
-                    ok = wait_event(ev(hs->b_block, jb), routine);
+                    ok = wait_event(ev(bev, jb), routine);
                     if (!ok) break;
                     exp_B(j0, nn);
                     convert_B(j0, nn, (j0 + w >= n) ? Np - j0 : nn);
@@ -1692,34 +1737,34 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
                 if (!ok) break;
                 const int64_t i0 = ib * hs->a_rows;
                 const int64_t rows = (i0 + hs->a_rows >= m) ? Mp - i0 : hs->a_rows;
+                gemm_mark(true);
                 pair_gemm(0, ntn, (int)(i0 / 256), (int)(rows / 256));
+                gemm_mark(false);
                 count_launch();
             }
             for (int64_t jb = 0; ok && jb < first; ++jb) {
                 const int64_t j0 = jb * w, nn = (n - j0 < w) ? n - j0 : w;
-                ok = wait_event(ev(hs->c_block, jb), routine);
-                if (!ok) break;
-                reconstruct_cols(j0, nn);
-                ok = unstage_columns_async(*hs->c, j0, j0 + nn, routine);
+                ok = finish_block(jb, j0, nn);
             }
         }
         for (int64_t j0 = first * w, jb = first; ok && j0 < n; j0 += w, ++jb) {
             const int64_t nn = (n - j0 < w) ? n - j0 : w;
             const bool last = j0 + w >= n;
             const int ntn = (int)((last ? Np - j0 : nn) / TC_BN);
-            ok = wait_event(ev(hs->b_block, jb), routine);
+            ok = wait_event(ev(bev, jb), routine);
             if (!ok) break;
             exp_B(j0, nn);
             convert_B(j0, nn, last ? Np - j0 : nn);
+            gemm_mark(true);
             pair_gemm((int)(j0 / TC_BN), ntn);
+            gemm_mark(false);
             count_launch();
-            ok = wait_event(jb < (int64_t)hs->c_block.size() ? hs->c_block[jb] : nullptr, routine);
-            if (!ok) break;
-            reconstruct_cols(j0, nn);
-            ok = unstage_columns_async(*hs->c, j0, j0 + nn, routine);
+            ok = finish_block(jb, j0, nn);
         }
-        if (ok) {
-            // the buffers are freed on stream(): order that after the copies
+        // the buffers are freed on this stream: order that after the side
+        // stream's kernels and the copies back
+        if (!order_streams(side, main_s, routine)) ok = false;
+        if (ok && hs) {
             ok = join_copy_stream(routine);
             hs->c_written = ok;
         }

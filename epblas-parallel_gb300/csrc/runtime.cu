@@ -229,7 +229,7 @@ struct CopyStreams {
             if (x) cudaStreamDestroy(x);
     }
 };
-thread_local CopyStreams t_copy;
+thread_local CopyStreams t_copy, t_side;
 
 // stream `after` waits for the work queued so far on stream `before`
 bool order(cudaStream_t before, cudaStream_t after, const char *routine)
@@ -243,6 +243,23 @@ bool order(cudaStream_t before, cudaStream_t after, const char *routine)
 }
 
 }  // namespace
+
+cudaStream_t side_stream()
+{
+    int d = 0;
+    cudaGetDevice(&d);
+    if (d < 0 || d >= 64) d = 0;
+    if (!t_side.s[d]) cudaStreamCreateWithFlags(&t_side.s[d], cudaStreamNonBlocking);
+    return t_side.s[d];
+}
+
+StreamOverride::StreamOverride(cudaStream_t s) : prev(t_stream) { t_stream = s; }
+StreamOverride::~StreamOverride() { t_stream = prev; }
+
+bool order_streams(cudaStream_t before, cudaStream_t after, const char *routine)
+{
+    return order(before, after, routine);
+}
 
 cudaStream_t copy_stream()
 {

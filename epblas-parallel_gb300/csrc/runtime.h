@@ -89,6 +89,17 @@ bool stage_matrix_async(Staged &s, const void *host, int64_t rows, int64_t cols,
 // Queues the copy of columns [j0, j1) of a staged matrix back to the caller's
 // array on copy_stream(), after the work queued so far on stream().
 bool unstage_columns_async(Staged &s, int64_t j0, int64_t j1, const char *routine);
+// A third per-thread stream, for kernels that run beside those of stream()
+// (created on first use, per device).
+cudaStream_t side_stream();
+// Makes stream() return `s` on this thread until the scope ends.
+struct StreamOverride {
+    cudaStream_t prev;
+    explicit StreamOverride(cudaStream_t s);
+    ~StreamOverride();
+};
+// stream `after` waits for the work queued so far on stream `before`.
+bool order_streams(cudaStream_t before, cudaStream_t after, const char *routine);
 // stream() waits for `e` (nullptr: nothing to wait for).
 bool wait_event(cudaEvent_t e, const char *routine);
 // stream() waits for everything queued so far on copy_stream().

@@ -265,3 +265,33 @@ def test_ozaki_trsm_trailing_updates(gpu, oracle, rng):
         assert gpu.last_error()[0] == 0
         err = orc.normwise_error(got, want, orc.dd_abs(al) * orc.dd_absmax(B0))
         assert err <= max(20, 8 * m * m) * orc.EPS_DD
+
+
+@pytest.mark.parametrize("cplx_", [False, True])
+def test_pair_kernel_large_device_product_bit_identical(gpu, rng, cplx_):
+    """A device-resident product above 2048 x 2048 (a short last 256-column
+    tile, beta != 0): the CTA-pair kernel gives the single-SM persistent
+    kernel's bits."""
+    import torch
+    m, n, k = 2100, 2300, 300
+    dev = torch.device("cuda", 0)
+    A = torch.from_numpy(mwb.dd_matrix(rng, m, k, cplx_=cplx_)).to(dev)
+    B = torch.from_numpy(mwb.dd_matrix(rng, k, n, cplx_=cplx_)).to(dev)
+    C0 = torch.from_numpy(mwb.dd_matrix(rng, m, n, cplx_=cplx_)).to(dev)
+    al = mwb.random_cdd(rng, ()) if cplx_ else mwb.random_dd(rng, ())
+    be = mwb.random_cdd(rng, ()) if cplx_ else mwb.random_dd(rng, ())
+    outs = []
+    for kind in (3, 2):
+        prev = gpu.lib.mwblas_set_ozaki_mma(kind)
+        try:
+            C = C0.clone()
+            with engine(gpu, OZAKI):
+                if cplx_:
+                    gpu.wgemm("N", "N", m, n, k, al, A.data_ptr(), m, B.data_ptr(), k, be, C.data_ptr(), m)
+                else:
+                    gpu.mgemm("N", "N", m, n, k, al, A.data_ptr(), m, B.data_ptr(), k, be, C.data_ptr(), m)
+            assert gpu.last_error()[0] == 0, gpu.last_error()
+            outs.append(C.cpu().numpy())
+        finally:
+            gpu.lib.mwblas_set_ozaki_mma(prev)
+    assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
