@@ -72,3 +72,33 @@ def test_host_pipeline_matches_device(gpu, oracle, rng, cplx, ta, tb, beta0, pin
     scale = orc.dd_abs(al) * k * orc.dd_absmax(A) * orc.dd_absmax(B) + orc.dd_abs(be) * orc.dd_absmax(C0)
     err = float(np.max(orc.dd_diff_abs(got[cols, rows], want))) / scale
     assert err <= max(10, 4 * k) * orc.EPS_DD, err
+
+
+@pytest.mark.parametrize("fail_at", [0, 1, 2, 3, 4])
+def test_host_pipeline_allocation_failure(gpu, rng, fail_at):
+    """A device allocation that fails at any point of the pipelined host path
+    (the staged operands, the engine's scratch) is reported as an error, no
+    copy is left writing into freed memory, and the next call succeeds with
+    the right result."""
+    m, n, k = 1531, 1283, 1100
+    A = mwb.random_dd(rng, (k, m))
+    B = mwb.random_dd(rng, (n, k))
+    C0 = mwb.random_dd(rng, (n, m))
+    al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+    dev = torch.device("cuda", 0)
+    dC = torch.from_numpy(C0).to(dev)
+    gpu.mgemm("N", "N", m, n, k, al, torch.from_numpy(A).to(dev).data_ptr(), m,
+              torch.from_numpy(B).to(dev).data_ptr(), k, be, dC.data_ptr(), m, engine="ozaki")
+    want = dC.cpu().numpy()
+    C = C0.copy()
+    gpu.lib.mwblas_debug_fail_alloc_after(fail_at)
+    try:
+        gpu.mgemm("N", "N", m, n, k, al, A, m, B, k, be, C, m, engine="ozaki")
+        err = gpu.last_error()[0]
+    finally:
+        gpu.lib.mwblas_debug_fail_alloc_after(-1)
+    assert err != 0
+    C = C0.copy()
+    gpu.mgemm("N", "N", m, n, k, al, A, m, B, k, be, C, m, engine="ozaki")
+    assert gpu.last_error()[0] == 0, gpu.last_error()
+    assert np.array_equal(C.view(np.uint64), want.view(np.uint64))
