@@ -86,9 +86,8 @@ def test_host_pipeline_allocation_failure(gpu, rng, fail_at):
     C0 = mwb.random_dd(rng, (n, m))
     al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
     dev = torch.device("cuda", 0)
-    dC = torch.from_numpy(C0).to(dev)
-    gpu.mgemm("N", "N", m, n, k, al, torch.from_numpy(A).to(dev).data_ptr(), m,
-              torch.from_numpy(B).to(dev).data_ptr(), k, be, dC.data_ptr(), m, engine="ozaki")
+    dA, dB, dC = (torch.from_numpy(x).to(dev) for x in (A, B, C0))   # kept alive through the call
+    gpu.mgemm("N", "N", m, n, k, al, dA.data_ptr(), m, dB.data_ptr(), k, be, dC.data_ptr(), m, engine="ozaki")
     want = dC.cpu().numpy()
     C = C0.copy()
     gpu.lib.mwblas_debug_fail_alloc_after(fail_at)
