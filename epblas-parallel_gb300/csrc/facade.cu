@@ -1226,8 +1226,9 @@ void trv_entry(const char *routine, bool cplx, bool solve, int fmt, const char *
     const int band_mode = g_band_solve.load();
     if (fmt == 1 && solve &&
         (band_mode == MWBLAS_BAND_SOLVE_IN_PLACE ||
-         (band_mode == MWBLAS_BAND_SOLVE_AUTO && (double)N * (double)N * (double)es > 268435456.0))) {
-        // solved in place from the band (a dense copy would be too large, or asked for)
+         (band_mode == MWBLAS_BAND_SOLVE_AUTO && (K <= 31 || (double)N * (double)N * (double)es > 268435456.0)))) {
+        // solved in place from the band: a narrow band (partitioned solve), a
+        // dense copy too large, or asked for
         if (!stage_matrix(SA, a, K + 1, N, *lda, es, true, routine)) return;
         if (!tbsv_device(cplx, U, T, D, N, K, SA.dev, *lda, SX.dev, dix, routine)) return;
         if (!unstage_vector(SX, routine)) return;

@@ -433,6 +433,170 @@ __global__ void __launch_bounds__(32) k_tbsv(TbsvParams p)
     }
 }
 
+// ---- partitioned band solve (k <= 31) ----------------------------------------------
+// The rows, in solve order, are cut into P chunks of L >= 2k. With the
+// incoming solutions of the previous chunk's last k rows t_{c-1}, chunk c
+// satisfies T_c x_c = b_c - E_c t_{c-1} (E_c: the band entries reaching back
+// into chunk c-1). So x_c = y_c - V_c t_{c-1} with T_c y_c = b_c and
+// T_c V_c = E_c, all chunks solved independently (lane 0: y, lane 1 + j:
+// column j of V); then one warp carries t_c = tail(y_c) - tail(V_c) t_{c-1}
+// across the chunks, and every row is corrected in parallel. Work (k + 1)
+// times the serial solve's, in parallel over P chunks; memory O(n k).
+struct SpikeParams {
+    TbsvParams t;
+    int64_t L, P;
+    double2 *invd;   // n entries: 1 / op(A)(r, r) by solve position (complex: 2 per entry)
+    double2 *Y;      // n: local solutions for b
+    double2 *V;      // n * k: local solutions for the coupling columns, [s][j]
+    double2 *T;      // P * k: t_c
+};
+
+template <bool CX>
+__device__ __forceinline__ dd::cplx sp_load(const double2 *p, int64_t i)
+{
+    dd::cplx v;
+    if (CX) {
+        v = dd::cload(p + 2 * i);
+    } else {
+        v.re = dd::load(p + i);
+        v.im = dd::make(0.0, 0.0);
+    }
+    return v;
+}
+
+template <bool CX>
+__device__ __forceinline__ void sp_store(double2 *p, int64_t i, const dd::cplx &v)
+{
+    if (CX) dd::cstore(p + 2 * i, v);
+    else dd::store(p + i, v.re);
+}
+
+__device__ __forceinline__ int64_t sp_row(const TbsvParams &p, bool forward, int64_t s)
+{
+    return forward ? s : p.n - 1 - s;
+}
+
+template <bool CX>
+__global__ void k_spike_invdiag(SpikeParams q)
+{
+    const TbsvParams &p = q.t;
+    const bool forward = p.upper == (p.op != 0);
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < p.n; s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = sp_row(p, forward, s);
+        dd::cplx inv{dd::make(1.0, 0.0), dd::make(0.0, 0.0)};
+        if (!p.unit) {
+            const dd::cplx d = tbsv_entry<CX>(p, r, r);
+            if (CX) {
+                const dd::real m2 = dd::add_exact(dd::mul_exact(d.re, d.re), dd::mul_exact(d.im, d.im));
+                const dd::real qq = dd::div(dd::make(1.0, 0.0), m2);
+                inv.re = dd::mul_exact(d.re, qq);
+                inv.im = dd::neg(dd::mul_exact(d.im, qq));
+            } else {
+                inv.re = dd::div(dd::make(1.0, 0.0), d.re);
+            }
+        }
+        sp_store<CX>(q.invd, s, inv);
+    }
+}
+
+// one warp per chunk: lane 0 solves for b, lane 1 + j for coupling column j
+template <bool CX>
+__global__ void __launch_bounds__(128) k_spike_local(SpikeParams q)
+{
+    const TbsvParams &p = q.t;
+    const bool forward = p.upper == (p.op != 0);
+    const int lane = threadIdx.x & 31;
+    const int64_t c = blockIdx.x * (int64_t)(blockDim.x / 32) + (threadIdx.x >> 5);
+    if (c >= q.P) return;
+    const int k = (int)p.k;
+    if (lane > k || (c == 0 && lane > 0)) return;   // chunk 0 has no incoming coupling
+    const int64_t s0 = c * q.L, s1 = (s0 + q.L < p.n) ? s0 + q.L : p.n;
+    const int j = lane - 1;
+    const int64_t sj = s0 - k + j;   // the previous chunk's row that coupling column j stands for
+    const dd::real zero = dd::make(0.0, 0.0);
+    for (int64_t s = s0; s < s1; ++s) {
+        const int64_t r = sp_row(p, forward, s);
+        dd::cplx rhs{zero, zero};
+        if (lane == 0) rhs = sp_load<CX>(p.x, r);
+        else if (s - sj <= k) rhs = tbsv_entry<CX>(p, r, sp_row(p, forward, sj));
+        dd::cplx acc{zero, zero};
+        for (int64_t s2 = (s - k > s0 ? s - k : s0); s2 < s; ++s2) {
+            const dd::cplx xv = lane == 0 ? sp_load<CX>(q.Y, s2) : sp_load<CX>(q.V, s2 * k + j);
+            tbsv_add<CX>(acc, tbsv_entry<CX>(p, r, sp_row(p, forward, s2)), xv);
+        }
+        dd::cplx v;
+        v.re = dd::sub_exact(rhs.re, acc.re);
+        v.im = CX ? dd::sub_exact(rhs.im, acc.im) : zero;
+        if (!p.unit) {
+            const dd::cplx inv = sp_load<CX>(q.invd, s);
+            if (CX) v = dd::cmul_exact(v, inv);
+            else v.re = dd::mul_exact(v.re, inv.re);
+        }
+        if (lane == 0) sp_store<CX>(q.Y, s, v);
+        else sp_store<CX>(q.V, s * k + j, v);
+    }
+}
+
+// one warp, chunk after chunk: t_c[i] = Y[s_i] - sum_j V[s_i][j] t_{c-1}[j]
+// for the last k rows s_i of chunk c (t_0 = the tail of Y in chunk 0)
+template <bool CX>
+__global__ void __launch_bounds__(32) k_spike_carry(SpikeParams q)
+{
+    const TbsvParams &p = q.t;
+    const int lane = threadIdx.x & 31;
+    const int k = (int)p.k;
+    const dd::real zero = dd::make(0.0, 0.0);
+    const unsigned mk = (1u << k) - 1u;   // lanes 0 .. k-1 (1 <= k <= 31)
+    dd::cplx t{zero, zero};   // lane i < k: t_{c-1}[i]
+    for (int64_t c = 0; c + 1 < q.P; ++c) {
+        const int64_t si = (c + 1) * q.L - k + lane;
+        dd::cplx v{zero, zero};
+        if (lane < k) {
+            v = sp_load<CX>(q.Y, si);
+            if (c > 0) {
+                dd::cplx acc{zero, zero};
+                for (int jj = 0; jj < k; ++jj) {
+                    dd::cplx tj;
+                    tj.re.hi = __shfl_sync(mk, t.re.hi, jj);
+                    tj.re.lo = __shfl_sync(mk, t.re.lo, jj);
+                    tj.im = zero;
+                    if (CX) {
+                        tj.im.hi = __shfl_sync(mk, t.im.hi, jj);
+                        tj.im.lo = __shfl_sync(mk, t.im.lo, jj);
+                    }
+                    tbsv_add<CX>(acc, sp_load<CX>(q.V, si * k + jj), tj);
+                }
+                v.re = dd::sub_exact(v.re, acc.re);
+                if (CX) v.im = dd::sub_exact(v.im, acc.im);
+            }
+            sp_store<CX>(q.T, c * k + lane, v);
+        }
+        t = v;
+        __syncwarp();
+    }
+}
+
+// x(row of s) = Y[s] - sum_j V[s][j] t_{c-1}[j] for s in chunk c >= 1; Y[s] in chunk 0
+template <bool CX>
+__global__ void k_spike_correct(SpikeParams q)
+{
+    const TbsvParams &p = q.t;
+    const bool forward = p.upper == (p.op != 0);
+    const int k = (int)p.k;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < p.n; s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = s / q.L;
+        dd::cplx v = sp_load<CX>(q.Y, s);
+        if (c > 0) {
+            dd::cplx acc{dd::make(0.0, 0.0), dd::make(0.0, 0.0)};
+            for (int jj = 0; jj < k; ++jj)
+                tbsv_add<CX>(acc, sp_load<CX>(q.V, s * k + jj), sp_load<CX>(q.T, (c - 1) * k + jj));
+            v.re = dd::sub_exact(v.re, acc.re);
+            if (CX) v.im = dd::sub_exact(v.im, acc.im);
+        }
+        sp_store<CX>(p.x, sp_row(p, forward, s), v);
+    }
+}
+
 struct Buf {
     void *p = nullptr;
     Buf(size_t bytes, const char *routine) { p = dev_alloc(bytes, routine); }
@@ -593,9 +757,41 @@ bool tbsv_device(bool cplx, char uplo, char trans, char diag, int64_t n, int64_t
     p.upper = uplo == 'U';
     p.unit = diag == 'U';
     p.x = (double2 *)xb.p;
-    if (cplx) k_tbsv<true><<<1, 32, 0, stream()>>>(p);
-    else k_tbsv<false><<<1, 32, 0, stream()>>>(p);
-    count_launch();
+    // chunks of L >= 2k rows, about a thousand of them
+    int64_t L = (n + 1023) / 1024;
+    if (L < 2 * k) L = 2 * k;
+    if (L < 64) L = 64;
+    const int64_t P = (n + L - 1) / L;
+    if (k >= 1 && k <= 31 && P >= 2) {
+        SpikeParams q;
+        q.t = p;
+        q.L = L;
+        q.P = P;
+        const size_t es = (size_t)16 * e2;
+        Buf sb(es * ((size_t)n * (2 + (size_t)k) + (size_t)P * k), routine);
+        if (!sb.p) return false;
+        q.invd = (double2 *)sb.p;
+        q.Y = q.invd + (size_t)n * e2;
+        q.V = q.Y + (size_t)n * e2;
+        q.T = q.V + (size_t)n * k * e2;
+        const unsigned gl = (unsigned)((P + 3) / 4);
+        if (cplx) {
+            k_spike_invdiag<true><<<blocks_for(n), kThreads, 0, stream()>>>(q);
+            k_spike_local<true><<<gl, 128, 0, stream()>>>(q);
+            k_spike_carry<true><<<1, 32, 0, stream()>>>(q);
+            k_spike_correct<true><<<blocks_for(n), kThreads, 0, stream()>>>(q);
+        } else {
+            k_spike_invdiag<false><<<blocks_for(n), kThreads, 0, stream()>>>(q);
+            k_spike_local<false><<<gl, 128, 0, stream()>>>(q);
+            k_spike_carry<false><<<1, 32, 0, stream()>>>(q);
+            k_spike_correct<false><<<blocks_for(n), kThreads, 0, stream()>>>(q);
+        }
+        count_launch(4);
+    } else {
+        if (cplx) k_tbsv<true><<<1, 32, 0, stream()>>>(p);
+        else k_tbsv<false><<<1, 32, 0, stream()>>>(p);
+        count_launch();
+    }
     vgather(n, x, incx, e2, xb.p, false);
     return true;
 }

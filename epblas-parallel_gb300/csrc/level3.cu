@@ -427,16 +427,18 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
     }
     const bool left = (side == 'L');
     const int64_t na = left ? m : n, nrhs = left ? n : m;
-    // Many right-hand sides: invert the diagonal blocks once (one launch) and
-    // apply them as GEMMs; few: substitute directly.
+    // Many right-hand sides, or a large triangle: invert the diagonal blocks
+    // once (one launch) and apply them as GEMMs; otherwise substitute
+    // directly (a substitution leaf runs a thread per right-hand side, so
+    // with few of them it is latency-bound: TRSV at n = 1024 took 27 ms).
     TrsmInv w;
     void *scratch = nullptr;
     bool ok = true;
-    if (nrhs >= 2 * kTrsmLeaf) {
+    if (nrhs >= 2 * kTrsmLeaf || na >= 128) {
         // leaf order 64, or 256 when the right-hand sides make the leaf GEMMs
-        // worth it; the 32 x 32 inverses are doubled up to it by merging
-        // with grouped GEMMs
-        const int64_t nb = (nrhs >= 256 && na >= 1024) ? 256 : kTrsmLeaf;
+        // worth it or there are only a few of them; the 32 x 32 inverses are
+        // doubled up to it by merging with grouped GEMMs
+        const int64_t nb = (na >= 1024 && (nrhs >= 256 || nrhs < 2 * kTrsmLeaf)) ? 256 : kTrsmLeaf;
         const int64_t nblk64 = (na + kInvNB - 1) / kInvNB;
         const int64_t nblk = (na + nb - 1) / nb;
         const size_t inv64_bytes = (size_t)nblk64 * kInvNB * kInvNB * sizeof(double2);

@@ -441,9 +441,11 @@ int mwblas_set_gemm_engine(int engine);   /* returns the previous value */
 int mwblas_get_gemm_engine(void);
 
 /* Triangular band solves (mtbsv_/wtbsv_): MWBLAS_BAND_SOLVE_AUTO solves in
- * place from the band (one warp, O(n k) memory) when a dense copy of the
- * triangle would exceed 256 MB, and through a dense copy and the blocked TRSM
- * otherwise (faster at those sizes); the other two values force one way. */
+ * place from the band (O(n k) memory; bandwidth k <= 31: the rows cut into
+ * chunks solved in parallel and joined by a k x k carry, wider bands: one
+ * warp) when k <= 31 or a dense copy of the triangle would exceed 256 MB, and
+ * through a dense copy and the blocked TRSM otherwise; the other two values
+ * force one way. */
 enum { MWBLAS_BAND_SOLVE_AUTO = 0, MWBLAS_BAND_SOLVE_IN_PLACE = 1, MWBLAS_BAND_SOLVE_DENSE = 2 };
 int mwblas_set_band_solve(int mode);   /* returns the previous value */
 

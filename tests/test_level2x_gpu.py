@@ -182,7 +182,7 @@ def test_triangular_mv_and_solve(gpu, oracle, rng, kind, c, uplo, trans, diag):
     if trans == "C" and not c:
         pytest.skip("real 'C' folds to 'T'")
     p = "w" if c else "m"
-    for n, k in [(1, 0), (60, 7), (200, 45), (150, 70)]:
+    for n, k in [(1, 0), (60, 7), (200, 45), (150, 70), (300, 7), (1000, 31)]:   # k <= 31, n > 64: partitioned
         A = dense(rng, n, n, c) / n
         d = np.arange(n)
         A[d, d] = ONE[c] * 0 + (np.array([[1.5, 0.0], [0.0, 0.0]]) if c else np.array([1.5, 0.0]))
