@@ -101,6 +101,12 @@ int pick_engine(const GemmArgs &g, bool cplx, int force_engine)
 
 bool run_gemm(GemmArgs &g, bool cplx, int force_engine, const char *routine)
 {
+    if (!cplx && g.n == 1 && g.uplo == 0 && !g.hs && force_engine < 0 && engine() == MWBLAS_GEMM_AUTO) {
+        // a real matrix-vector product (the updates and leaf solves of TRSV,
+        // for instance): the fixed-point GEMV kernels, three launches
+        return gemv_device(g.ta, g.ta ? g.k : g.m, g.ta ? g.m : g.k, g.alpha, g.A, g.lda, g.B, g.tb ? g.ldb : 1,
+                           g.beta, g.beta_kind, g.C, 1, routine);
+    }
     const int eng = pick_engine(g, cplx, force_engine);
     if (g.hs && eng != MWBLAS_GEMM_OZAKI && !g.hs->wait_all(routine)) return false;
     if (eng == MWBLAS_GEMM_FIXED && !cplx) return gemm_fixed_real(g, routine);
