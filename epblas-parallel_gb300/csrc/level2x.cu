@@ -597,6 +597,53 @@ __global__ void k_spike_correct(SpikeParams q)
     }
 }
 
+// ---- rank-1 / rank-2 updates, elementwise -------------------------------------------
+// A(i, j) += u_i v_j (+ u2_i v2_j) over the whole matrix (uplo 0) or one
+// triangle (1 upper, 2 lower), with u = x, v_j = alpha op(y_j) and, for the
+// rank-2 forms, u2 = y, v2_j = alpha x_j (symmetric) or conj(alpha x_j)
+// (Hermitian): the reference BLAS association (temp = alpha * y(j);
+// a(i, j) += x(i) * temp). Hermitian updates leave the diagonal real.
+
+// v[j] = a * op(w[j]) with op = conj when `conj`; conj_after: v = conj(a w)
+template <bool CX>
+__global__ void k_rank_prep(int64_t n, const double2 *w, dd::cplx a, bool conj, bool conj_after, double2 *v)
+{
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        if (CX) {
+            dd::cplx wj = dd::cload(w + 2 * j);
+            if (conj) wj.im = dd::neg(wj.im);
+            dd::cplx r = dd::cmul_exact(a, wj);
+            if (conj_after) r.im = dd::neg(r.im);
+            dd::cstore(v + 2 * j, r);
+        } else {
+            dd::store(v + j, dd::mul_exact(a.re, dd::load(w + j)));
+        }
+    }
+}
+
+template <bool CX, bool TWO>
+__global__ void k_rank_update(int64_t m, int64_t n, const double2 *__restrict__ u, const double2 *__restrict__ v,
+                              const double2 *__restrict__ u2, const double2 *__restrict__ v2, int uplo, bool herm,
+                              double2 *A, int64_t lda)
+{
+    const int64_t total = m * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t % m, j = t / m;
+        if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
+        double2 *pa = A + (CX ? 2 : 1) * (i + j * lda);
+        if (CX) {
+            dd::cplx acc = dd::cadd_exact(dd::cload(pa), dd::cmul_exact(dd::cload(u + 2 * i), dd::cload(v + 2 * j)));
+            if (TWO) acc = dd::cadd_exact(acc, dd::cmul_exact(dd::cload(u2 + 2 * i), dd::cload(v2 + 2 * j)));
+            if (herm && i == j) acc.im = dd::make(0.0, 0.0);
+            dd::cstore(pa, acc);
+        } else {
+            dd::real acc = dd::add_exact(dd::load(pa), dd::mul_exact(dd::load(u + i), dd::load(v + j)));
+            if (TWO) acc = dd::add_exact(acc, dd::mul_exact(dd::load(u2 + i), dd::load(v2 + j)));
+            dd::store(pa, acc);
+        }
+    }
+}
+
 struct Buf {
     void *p = nullptr;
     Buf(size_t bytes, const char *routine) { p = dev_alloc(bytes, routine); }
@@ -823,35 +870,50 @@ bool trv_device(bool cplx, bool solve, char uplo, char trans, char diag, int64_t
 bool rank_update_device(const RankArgs &r, const char *routine)
 {
     const int e2 = r.cplx ? 2 : 1;
-    Buf xb((size_t)r.m * 16 * e2, routine), yb((size_t)(r.y ? r.n : 1) * 16 * e2, routine);
-    if (!xb.p || !yb.p) return false;
+    const bool two = r.y && r.uplo != 0;           // SYR2 / HER2
+    const bool herm = r.cplx && r.conj && r.uplo != 0;
+    const int64_t ny = r.uplo == 0 ? r.n : r.m;    // length of y (GER) or of x (SYR/HER)
+    // u = x, v = alpha op(y) (GER) or alpha op(x) (SYR/HER); for rank 2: u2 = y, v2 = alpha x or conj(alpha x)
+    Buf xb((size_t)r.m * 16 * e2, routine), yb((size_t)ny * 16 * e2, routine), vb((size_t)ny * 16 * e2, routine),
+        v2b((size_t)(two ? r.m : 1) * 16 * e2, routine);
+    if (!xb.p || !yb.p || !vb.p || !v2b.p) return false;
     vgather(r.m, r.x, r.incx, e2, xb.p, true);
-    if (r.y) vgather(r.n, r.y, r.incy, e2, yb.p, true);
-    GemmArgs g;
-    g.alpha = r.alpha;
-    g.calpha = r.calpha;
-    g.beta = dd_host{1.0, 0.0};
-    g.cbeta = cdd_host{{1.0, 0.0}, {0.0, 0.0}};
-    g.beta_kind = 1;
-    if (r.uplo == 0) {
-        // GER: A += alpha * x * op(y) with op = transpose (conjugated for GERC)
-        g.m = r.m;
-        g.n = r.n;
-        g.k = 1;
-        g.A = xb.p;
-        g.lda = r.m;
-        g.B = yb.p;
-        g.ldb = r.n;
-        g.tb = true;
-        g.cb = r.conj;
-        g.C = r.A;
-        g.ldc = r.lda;
-        return run_gemm(g, r.cplx, -1, routine);
+    if (r.y) vgather(ny, r.y, r.incy, e2, yb.p, true);
+    dd::cplx a;
+    if (r.cplx) {
+        a.re = dd::make(r.calpha.re.hi, r.calpha.re.lo);
+        a.im = dd::make(r.calpha.im.hi, r.calpha.im.lo);
+    } else {
+        a.re = dd::make(r.alpha.hi, r.alpha.lo);
+        a.im = dd::make(0.0, 0.0);
     }
-    if (!r.y)   // SYR / HER: A += alpha * x * x^T (x^H), triangle
-        return syrk_device(r.cplx, r.conj, r.uplo, false, r.m, 1, xb.p, r.m, g, r.A, r.lda, routine);
-    // SYR2 / HER2
-    return syr2k_device(r.cplx, r.conj, r.uplo, false, r.m, 1, g, xb.p, r.m, yb.p, r.m, r.A, r.lda, routine);
+    if (herm && !two) a.im = dd::make(0.0, 0.0);   // HER: alpha real
+    const double2 *ysrc = (const double2 *)(r.y ? yb.p : xb.p);
+    const double2 *u = (const double2 *)xb.p, *v = (const double2 *)vb.p;
+    const double2 *u2 = two ? (const double2 *)yb.p : nullptr, *v2 = two ? (const double2 *)v2b.p : nullptr;
+    if (r.cplx) {
+        k_rank_prep<true><<<blocks_for(ny), kThreads, 0, stream()>>>(ny, ysrc, a, r.conj, false, (double2 *)vb.p);
+        if (two)
+            k_rank_prep<true><<<blocks_for(r.m), kThreads, 0, stream()>>>(r.m, (const double2 *)xb.p, a, false, herm,
+                                                                        (double2 *)v2b.p);
+    } else {
+        k_rank_prep<false><<<blocks_for(ny), kThreads, 0, stream()>>>(ny, ysrc, a, false, false, (double2 *)vb.p);
+        if (two)
+            k_rank_prep<false><<<blocks_for(r.m), kThreads, 0, stream()>>>(r.m, (const double2 *)xb.p, a, false, false,
+                                                                         (double2 *)v2b.p);
+    }
+    const int64_t cols = r.uplo == 0 ? r.n : r.m;
+    const unsigned g = blocks_for(r.m * cols);
+    double2 *A = (double2 *)r.A;
+    if (r.cplx) {
+        if (two) k_rank_update<true, true><<<g, kThreads, 0, stream()>>>(r.m, cols, u, v, u2, v2, r.uplo, herm, A, r.lda);
+        else k_rank_update<true, false><<<g, kThreads, 0, stream()>>>(r.m, cols, u, v, u2, v2, r.uplo, herm, A, r.lda);
+    } else {
+        if (two) k_rank_update<false, true><<<g, kThreads, 0, stream()>>>(r.m, cols, u, v, u2, v2, r.uplo, false, A, r.lda);
+        else k_rank_update<false, false><<<g, kThreads, 0, stream()>>>(r.m, cols, u, v, u2, v2, r.uplo, false, A, r.lda);
+    }
+    count_launch(two ? 3 : 2);
+    return true;
 }
 
 }  // namespace mw
