@@ -107,6 +107,28 @@ bool run_gemm(GemmArgs &g, bool cplx, int force_engine, const char *routine)
         return gemv_device(g.ta, g.ta ? g.k : g.m, g.ta ? g.m : g.k, g.alpha, g.A, g.lda, g.B, g.tb ? g.ldb : 1,
                            g.beta, g.beta_kind, g.C, 1, routine);
     }
+    if (cplx && g.n == 1 && !g.tb && g.uplo == 0 && !g.herm && !g.hs && force_engine < 0 &&
+        engine() == MWBLAS_GEMM_AUTO) {
+        // a complex matrix-vector product: the fixed-point matrix-vector
+        // kernel reading the dense operand in place
+        SmvArgs v;
+        v.cplx = true;
+        v.fmt = 0;
+        v.kind = 0;
+        v.trans = g.ta ? (g.ca ? 'C' : 'T') : 'N';
+        v.rows = g.m;
+        v.cols = g.k;
+        v.ldab = g.lda;
+        v.A = g.A;
+        v.x = g.B;
+        v.incx = 1;
+        v.y = g.C;
+        v.incy = 1;
+        v.calpha = g.calpha;
+        v.cbeta = g.cbeta;
+        v.beta_kind = g.beta_kind;
+        return smv_device(v, routine);
+    }
     const int eng = pick_engine(g, cplx, force_engine);
     if (g.hs && eng != MWBLAS_GEMM_OZAKI && !g.hs->wait_all(routine)) return false;
     if (eng == MWBLAS_GEMM_FIXED && !cplx) return gemm_fixed_real(g, routine);

@@ -154,6 +154,11 @@ __global__ void k_vdig(int64_t n, const double2 *x, int64_t inc, int e2, fx::Dig
 
 __device__ __forceinline__ void smv_range(const SmvParams &p, int64_t r, int64_t &c0, int64_t &c1)
 {
+    if (p.fmt == 0) {   // dense general: every column
+        c0 = 0;
+        c1 = p.cols - 1;
+        return;
+    }
     int64_t lo, hi;
     if (p.kind == 0) {
         lo = p.op == 0 ? p.kl : p.ku;
@@ -176,6 +181,7 @@ __device__ __forceinline__ void smv_range(const SmvParams &p, int64_t r, int64_t
 // i + j(2n-j-1)/2, band AB(ku + i - j, j) (ku = 0 for a lower triangle).
 __device__ __forceinline__ int64_t smv_addr(const SmvParams &p, int64_t i, int64_t j)
 {
+    if (p.fmt == 0) return i + j * p.ldab;
     if (p.fmt == 2) return p.upper ? i + j * (j + 1) / 2 : i + j * (2 * p.n - j - 1) / 2;
     return (p.ku + i - j) + j * p.ldab;
 }
@@ -713,7 +719,8 @@ bool smv_device(const SmvArgs &a, const char *routine)
     p.beta_kind = a.beta_kind;
     // average stored entries per row: a warp per row once rows are long
     int64_t len;
-    if (a.fmt == 2) len = a.kind == 3 ? (a.n + 1) / 2 : a.n;
+    if (a.fmt == 0) len = a.cols;
+    else if (a.fmt == 2) len = a.kind == 3 ? (a.n + 1) / 2 : a.n;
     else if (a.kind == 0) len = a.kl + a.ku + 1;
     else len = (a.kind == 3 ? 1 : 2) * (a.kl > a.ku ? a.kl : a.ku) + 1;
     const bool warp = len >= 48;

@@ -33,8 +33,9 @@ bool mv_device(const MvArgs &a, const char *routine);
 bool trv_device(bool cplx, bool solve, char uplo, char trans, char diag, int64_t n, const void *A, int64_t lda,
                 void *x, int64_t incx, const char *routine);
 
-// Band (fmt 1, LAPACK layout, leading dimension ldab) or packed (fmt 2)
-// operand, read in place: y := alpha*op(A)*x + beta*y with op(A) rows x cols.
+// Dense general (fmt 0, kind 0, leading dimension ldab), band (fmt 1, LAPACK
+// layout, leading dimension ldab) or packed (fmt 2) operand, read in place:
+// y := alpha*op(A)*x + beta*y with op(A) rows x cols.
 // kind 0 general band (kl, ku); 1 symmetric, 2 Hermitian, 3 triangular
 // (unit diagonal when `unit`), the stored triangle given by `upper` with,
 // for a band, kl = 0, ku = k (upper) or kl = k, ku = 0 (lower); n is the
