@@ -1391,12 +1391,9 @@ void syr_entry(const char *routine, bool cplx, bool herm, bool packed, bool two,
     if (!stage_vector(SX, x, N, *incx, es, true, dix, routine)) return;
     if (two && !stage_vector(SY, y, N, *incy, es, true, diy, routine)) return;
     const int64_t len = N * (N + 1) / 2;
-    void *dense = nullptr;
     if (packed) {
+        // updated in place in the packed triangle
         if (!stage_matrix(SA, a, len, 1, len, es, true, routine)) return;
-        dense = dev_alloc((size_t)N * N * es, routine);
-        if (!dense) return;
-        pack_move(N, SA.dev, e2, U == 'U', dense, true);
     } else {
         if (!stage_matrix(SA, a, N, N, *lda, es, true, routine)) return;
     }
@@ -1410,18 +1407,15 @@ void syr_entry(const char *routine, bool cplx, bool herm, bool packed, bool two,
     r.incx = dix;
     r.y = two ? SY.dev : nullptr;
     r.incy = diy;
-    r.A = packed ? dense : SA.dev;
-    r.lda = packed ? N : *lda;
+    r.A = SA.dev;
+    r.lda = packed ? -1 : *lda;
     if (alpha_real) {
         r.alpha = rd((const mwblas_real64x2 *)alpha);
         r.calpha = cdd_host{r.alpha, {0.0, 0.0}};
     } else {
         r.calpha = cd((const mwblas_complex64x2 *)alpha);
     }
-    bool ok = rank_update_device(r, routine);
-    if (ok && packed) pack_move(N, SA.dev, e2, U == 'U', dense, false);
-    if (dense) dev_free(dense);
-    if (!ok) return;
+    if (!rank_update_device(r, routine)) return;
     if (!unstage_matrix(SA, routine)) return;
     finish(routine);
 }

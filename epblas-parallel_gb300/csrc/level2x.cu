@@ -627,6 +627,7 @@ __global__ void k_rank_prep(int64_t n, const double2 *w, dd::cplx a, bool conj, 
     }
 }
 
+// lda < 0: A is the packed triangle (upper: i + j(j+1)/2, lower: i + j(2m-j-1)/2)
 template <bool CX, bool TWO>
 __global__ void k_rank_update(int64_t m, int64_t n, const double2 *__restrict__ u, const double2 *__restrict__ v,
                               const double2 *__restrict__ u2, const double2 *__restrict__ v2, int uplo, bool herm,
@@ -636,7 +637,8 @@ __global__ void k_rank_update(int64_t m, int64_t n, const double2 *__restrict__ 
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = t % m, j = t / m;
         if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
-        double2 *pa = A + (CX ? 2 : 1) * (i + j * lda);
+        const int64_t pos = lda >= 0 ? i + j * lda : (uplo == 1 ? i + j * (j + 1) / 2 : i + j * (2 * m - j - 1) / 2);
+        double2 *pa = A + (CX ? 2 : 1) * pos;
         if (CX) {
             dd::cplx acc = dd::cadd_exact(dd::cload(pa), dd::cmul_exact(dd::cload(u + 2 * i), dd::cload(v + 2 * j)));
             if (TWO) acc = dd::cadd_exact(acc, dd::cmul_exact(dd::cload(u2 + 2 * i), dd::cload(v2 + 2 * j)));

@@ -76,7 +76,7 @@ struct RankArgs {
     const void *y = nullptr;
     int64_t incy = 1;
     void *A = nullptr;
-    int64_t lda = 0;
+    int64_t lda = 0;   // < 0 (SYR/HER forms only): A is the packed triangle
     dd_host alpha{1.0, 0.0};
     cdd_host calpha{{1.0, 0.0}, {0.0, 0.0}};
 };
