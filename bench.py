@@ -7,11 +7,14 @@ the plain FP64 error-free-transform engine on the same GPU, work counted as
 
 A step is one C := alpha*A*B + beta*C at 8192^3 (alpha, beta random
 double-double of magnitude 0.5..2, A/B/C with hi ~ U[-1,1), lo = hi*2^-53*U),
-through the library's C ABI (mgemm_ozaki_64_).
+through the drop-in symbol a caller of the reference links (mgemm_64_), whose
+automatic engine choice takes the tensor-core engine at this size.
   value : device-resident operands (1 GiB each, larger than L2), CUDA events
           around K steps on the library's stream, max over ranks.
   e2e   : the same call with pinned HOST buffers, so every step includes the
-          host->device copies of A, B, C and the device->host copy of C.
+          host->device copies of A, B, C and the device->host copy of C;
+          e2e_pageable: the same with ordinary (pageable) host arrays, as a
+          Fortran or C caller hands them over.
 Multi-GPU (torchrun): every rank runs its own independent GEMM (replicas; the
 path needs no collective), value = total flops of all ranks / max time.
 
@@ -142,7 +145,9 @@ def run_ours(args, rank, world, local_rank):
     stream = torch.cuda.current_stream(dev)
     lib.lib.mwblas_set_stream(stream.cuda_stream)
 
-    def step(engine="ozaki", c=dC):
+    lib.lib.mwblas_set_gemm_engine(0)   # AUTO: the drop-in call's own engine choice
+
+    def step(engine=None, c=dC):
         lib.mgemm("N", "N", n, n, n, alpha, dA.data_ptr(), n, dB.data_ptr(), n, beta, c.data_ptr(), n, engine=engine)
 
     dist = None
@@ -159,8 +164,10 @@ def run_ours(args, rank, world, local_rank):
         step()
     code, msg = lib.last_error()
     if code != 0:
-        raise RuntimeError(f"mgemm_ozaki_64_ failed: {code} {msg}")
+        raise RuntimeError(f"mgemm_64_ failed: {code} {msg}")
     moduli = int(lib.lib.mwblas_last_ozaki_moduli())
+    if moduli <= 0:
+        raise RuntimeError("mgemm_64_ did not take the tensor-core engine")
 
     # ---- timed region: K steps, device-resident operands (each 1 GiB > L2).
     # The library records CUDA events around each engine phase on its stream,
@@ -190,25 +197,41 @@ def run_ours(args, rank, world, local_rank):
     hA = torch.from_numpy(A).pin_memory()
     hB = torch.from_numpy(B).pin_memory()
     hC = torch.from_numpy(C0).pin_memory()
-    for _ in range(max(3, args.warmup)):   # warm-up calls, as for the device-timed steps
-        lib.mgemm("N", "N", n, n, n, alpha, hA.data_ptr(), n, hB.data_ptr(), n, beta, hC.data_ptr(), n,
-                  engine="ozaki")
-    barrier()
-    # each call timed on the host clock (the call returns with C back in host
-    # memory); the median of five, as the host link is shared with other jobs
+    def host_calls(a_, b_, c_, calls):
+        for _ in range(max(3, args.warmup)):   # warm-up calls, as for the device-timed steps
+            lib.mgemm("N", "N", n, n, n, alpha, a_, n, b_, n, beta, c_, n)
+        barrier()
+        # each call timed on the host clock (the call returns with C back in host
+        # memory); the median, as the host link is shared with other jobs
+        per = []
+        for _ in range(calls):
+            t0 = time.perf_counter()
+            lib.mgemm("N", "N", n, n, n, alpha, a_, n, b_, n, beta, c_, n)
+            per.append((time.perf_counter() - t0) * 1e3)
+        barrier()
+        code_, msg_ = lib.last_error()
+        if code_ != 0:
+            raise RuntimeError(f"mgemm_64_ on host arrays failed: {code_} {msg_}")
+        return per
+
     e_steps = max(1, min(args.steps, 5))
-    per_call = []
-    for _ in range(e_steps):
-        t0 = time.perf_counter()
-        lib.mgemm("N", "N", n, n, n, alpha, hA.data_ptr(), n, hB.data_ptr(), n, beta, hC.data_ptr(), n,
-                  engine="ozaki")
-        per_call.append((time.perf_counter() - t0) * 1e3)
-    barrier()
+    per_call = host_calls(hA.data_ptr(), hB.data_ptr(), hC.data_ptr(), e_steps)
     e_val, e_ms = job_throughput(float(np.median(per_call)), flops, world, dist, dev)
     e2e = {"value": e_val / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": 3 * n * n * 16, "d2h_bytes_per_step": n * n * 16,
            "ms_per_step": e_ms, "stat": f"median of {e_steps} calls",
-           "per_call_ms": [round(x, 2) for x in per_call], "api": "mgemm_ozaki_64_ on pinned host arrays"}
+           "per_call_ms": [round(x, 2) for x in per_call], "api": "mgemm_64_ on pinned host arrays"}
+    del hA, hB, hC
+    # the same call on ordinary pageable numpy arrays
+    pA, pB, pC = A.copy(), B.copy(), C0.copy()
+    p_steps = max(1, min(args.steps, 3))
+    per_call_p = host_calls(pA, pB, pC, p_steps)
+    p_val, p_ms = job_throughput(float(np.median(per_call_p)), flops, world, dist, dev)
+    e2e_pageable = {"value": p_val / 1e9, "unit": UNIT,
+                    "h2d_bytes_per_step": 3 * n * n * 16, "d2h_bytes_per_step": n * n * 16,
+                    "ms_per_step": p_ms, "stat": f"median of {p_steps} calls",
+                    "per_call_ms": [round(x, 2) for x in per_call_p], "api": "mgemm_64_ on pageable host arrays"}
+    del pA, pB, pC
 
     # ---- the plain FP64-EFT engine on the same GPU (one timed call)
     plain = None
@@ -227,7 +250,8 @@ def run_ours(args, rank, world, local_rank):
                  "fp64_inst_per_s": fp64_inst / (pms * 1e-3),
                  "note": "FP64 pipe issue-bound; the probe measured 1.58 DFMA/clk/SM on this GPU"}
 
-    res = dict(value=value, ms=ms, launches=launches, moduli=moduli, phase_ms=phase.tolist(), e2e=e2e, plain=plain, clocks=clk.summary(),
+    res = dict(value=value, ms=ms, launches=launches, moduli=moduli, phase_ms=phase.tolist(), e2e=e2e,
+               e2e_pageable=e2e_pageable, plain=plain, clocks=clk.summary(),
                flops=flops, peaks=pk, peaks_kind=pk_kind, alpha=alpha, beta=beta, A=A, B=B, C0=C0,
                C=dC.cpu().numpy() if (rank == 0 and not args.skip_check) else None)
     lib.lib.mwblas_set_stream(None)
@@ -332,7 +356,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     cfg = {"workload": f"mgemm_ {args.n}x{args.n}x{args.n} NN, random double-double alpha/beta (|.| in [0.5,2]), "
                        "A,B,C hi~U[-1,1) lo=hi*2^-53*U[-1,1)",
-           "m": args.n, "n": args.n, "k": args.n, "engine": "ozaki-II CRT, tcgen05 kind::f16 residue GEMMs",
+           "m": args.n, "n": args.n, "k": args.n, "api": "mgemm_64_ (engine chosen by the library: AUTO)",
+           "engine": "ozaki-II CRT, tcgen05 kind::f16 residue GEMMs",
            "l2": "operands 1 GiB each, larger than the 129 MB L2", "parallelism": f"replicas x{world}"}
 
     if args.impl == "reference":
@@ -380,8 +405,7 @@ def main():
         dB = torch.from_numpy(res["B"]).cuda()
         dC = torch.from_numpy(res["C0"]).cuda()
         n = args.n
-        lib.mgemm("N", "N", n, n, n, res["alpha"], dA.data_ptr(), n, dB.data_ptr(), n, res["beta"], dC.data_ptr(), n,
-                  engine="ozaki")
+        lib.mgemm("N", "N", n, n, n, res["alpha"], dA.data_ptr(), n, dB.data_ptr(), n, res["beta"], dC.data_ptr(), n)
         torch.cuda.synchronize()
         res["C_check"] = dC.cpu().numpy()
         del dA, dB, dC
@@ -410,7 +434,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64x2 (double-double); residue GEMMs fp16 x fp16 -> fp32 exact",
             "data": "synthetic (seeded, reference value distribution)", "config": cfg,
-            "e2e": res["e2e"], "gpu_launches": int(res["launches"]), "clocks": res["clocks"],
+            "e2e": res["e2e"], "e2e_pageable": res["e2e_pageable"], "gpu_launches": int(res["launches"]),
+            "clocks": res["clocks"],
             "roofline": roof, "ozaki": {"moduli": res["moduli"], "bits": 106},
             "plain_fp64_eft": res["plain"]}
     if cpu:

@@ -107,10 +107,11 @@ bool run_gemm(GemmArgs &g, bool cplx, int force_engine, const char *routine)
         return gemv_device(g.ta, g.ta ? g.k : g.m, g.ta ? g.m : g.k, g.alpha, g.A, g.lda, g.B, g.tb ? g.ldb : 1,
                            g.beta, g.beta_kind, g.C, 1, routine);
     }
-    if (cplx && g.n == 1 && !g.tb && g.uplo == 0 && !g.herm && !g.hs && force_engine < 0 &&
-        engine() == MWBLAS_GEMM_AUTO) {
+    if (cplx && g.n == 1 && !g.tb && !g.cb && !(g.ca && !g.ta) && g.uplo == 0 && !g.herm && !g.hs &&
+        force_engine < 0 && engine() == MWBLAS_GEMM_AUTO) {
         // a complex matrix-vector product: the fixed-point matrix-vector
-        // kernel reading the dense operand in place
+        // kernel reading the dense operand in place (a conjugate without a
+        // transpose, which the kernel cannot express, takes the general engine)
         SmvArgs v;
         v.cplx = true;
         v.fmt = 0;

@@ -271,7 +271,10 @@ bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A,
 // needs to start at zero: every entry a call reads was written earlier by the
 // same call. The host learns its device address once per device, with that
 // device current, on the first call made on that device; that first call
-// should therefore come before any stream capture.
+// should therefore come before any stream capture. The address is cached
+// together with the CUDA context it was looked up in and looked up again
+// when the calling thread's current context differs (after cudaDeviceReset,
+// or on a context other than the device's primary one).
 
 namespace mw {
 namespace {
@@ -281,6 +284,24 @@ static __device__ __align__(256) double2 g_gemv_noalloc_scratch[kNoAllocScratch]
 
 std::mutex g_noalloc_mu;
 double2 *g_noalloc_addr[64] = {};
+void *g_noalloc_ctx[64] = {};
+
+// The calling thread's current CUDA context (driver entry point, looked up once).
+void *current_context()
+{
+    using Fn = int (*)(void **);
+    static Fn fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return (Fn)f;
+    }();
+    void *ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
 
 }  // namespace
 }  // namespace mw
@@ -317,15 +338,20 @@ extern "C" int mgemv_n_noalloc(int64_t m, int64_t n, const mwblas_real64x2 *alph
     if (dev < 0 || dev >= 64) { set_error(routine, MWBLAS_ERR_DEVICE, "device ordinal out of range"); return MWBLAS_ERR_DEVICE; }
     double2 *scratch;
     {
+        // null before the runtime has initialised a context on this thread; the
+        // lookup below initialises it, and the context is read again after it
+        void *ctx = current_context();
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
+        if (!g_noalloc_addr[dev] || g_noalloc_ctx[dev] != ctx) {
             void *p = nullptr;
             cudaError_t st = cudaGetSymbolAddress(&p, g_gemv_noalloc_scratch);
             if (st != cudaSuccess) {
+                g_noalloc_addr[dev] = nullptr;
                 cuda_ok(st, routine, "cudaGetSymbolAddress(scratch)");
                 return MWBLAS_ERR_CUDA;
             }
             g_noalloc_addr[dev] = (double2 *)p;
+            g_noalloc_ctx[dev] = current_context();
         }
         scratch = g_noalloc_addr[dev];
     }

@@ -878,6 +878,12 @@ bool trv_device(bool cplx, bool solve, char uplo, char trans, char diag, int64_t
 
 bool rank_update_device(const RankArgs &r, const char *routine)
 {
+    if (r.lda < 0 && r.uplo == 0) {
+        // lda < 0 marks a packed triangle, which only SPR/HPR/SPR2/HPR2 (uplo
+        // set) hand over; a general rank update never has one
+        set_error(routine, MWBLAS_ERR_UNSUPPORTED, "packed storage without a triangle");
+        return false;
+    }
     const int e2 = r.cplx ? 2 : 1;
     const bool two = r.y && r.uplo != 0;           // SYR2 / HER2
     const bool herm = r.cplx && r.conj && r.uplo != 0;

@@ -36,6 +36,7 @@
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -106,6 +107,17 @@ Moduli choose_moduli(double need_bits)
 
 int g_last_moduli = 0;
 int g_mma_kind = -1;   // 0 tcgen05 per tile, 1 SIMT cross-check, 2 tcgen05 persistent, 3 CTA pairs (default)
+
+// Failure injection for the bounded-wait path: the next g_lose_loads launches
+// of the CTA-pair residue GEMM issue no operand loads (see k_oz_gemm_tc_2sm).
+std::atomic<int> g_lose_loads{0};
+int take_lost_load_injection()
+{
+    int v = g_lose_loads.load();
+    while (v > 0 && !g_lose_loads.compare_exchange_weak(v, v - 1)) {
+    }
+    return v > 0 ? 1 : 0;
+}
 
 // Optional per-phase timing with CUDA events on the library stream.
 enum { PH_EXP = 0, PH_RES, PH_GEMM, PH_REC, PH_N };
@@ -862,7 +874,7 @@ constexpr int T2_SMEM = T2_STAGES * (T2_A_BYTES + T2_B_BYTES) + 1024 + 256;
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TCP_THREADS, 1)
     k_oz_gemm_tc_2sm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t Mp,
                      int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint16_t *__restrict__ R,
-                     int *status, int uplo, int tiles_m2, int tiles_n, int nz, int tn0, int tm0)
+                     int *status, int uplo, int tiles_m2, int tiles_n, int nz, int tn0, int tm0, int lose_loads)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -925,7 +937,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TCP_THREADS, 1)
             sm100::tma_prefetch_desc(&tmB);
             uint32_t gs = 0;
             bool ok = true;
-            for (int64_t ua = next_unit(cid); ua < units && ok;) {
+            // lose_loads (a failure-injection hook): issue no operand load at
+            // all, so that the MMA issuer's first wait for a landed stage runs
+            // out with nothing in flight anywhere in the pair
+            for (int64_t ua = lose_loads ? units : next_unit(cid); ua < units && ok;) {
                 const int64_t ub = next_unit(ua + ncl);
                 const int nu = ub < units ? 2 : 1;
                 int32_t ya[2], yb[2];
@@ -1624,7 +1639,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         const unsigned grid = 2u * (unsigned)(units < pairs ? units : pairs);
         k_oz_gemm_tc_2sm<<<grid, TCP_THREADS, T2_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R,
                                                                    device_status_word(), g.uplo, tiles_m2, ntn, nz,
-                                                                   tn0, tm0);
+                                                                   tn0, tm0, take_lost_load_injection());
     };
     if (blocked) {
         // launched block by block with the reconstruction below
@@ -1812,6 +1827,21 @@ extern "C" float mwblas_last_phase_ms(int phase)
 {
     return (phase >= 0 && phase < mw::PH_N) ? mw::t_phase_ms[phase] : -1.0f;
 }
+
+extern "C" uint64_t mwblas_set_wait_limit_ns(uint64_t ns)
+{
+    static std::atomic<uint64_t> current{sm100::kWaitLimitNs};
+    const uint64_t v = ns == 0 ? sm100::kWaitLimitNs : (ns < 1000000ull ? 1000000ull : ns);
+    mw::clear_error();
+    const cudaError_t st = cudaMemcpyToSymbol(sm100::g_wait_limit_ns, &v, sizeof(v));
+    if (st != cudaSuccess) {
+        mw::cuda_ok(st, "mwblas_set_wait_limit_ns", "cudaMemcpyToSymbol");
+        return current.load();
+    }
+    return current.exchange(v);
+}
+
+extern "C" void mwblas_debug_lose_operand_loads(int count) { mw::g_lose_loads.store(count > 0 ? count : 0); }
 
 extern "C" int mwblas_set_ozaki_mma(int kind)
 {

@@ -11,7 +11,18 @@
 
 namespace sm100 {
 
-constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s: far above any legitimate wait
+__host__ __device__ constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s: far above any legitimate wait
+
+// The limit of the waits that report into a status word (set from the host by
+// mwblas_set_wait_limit_ns, never below 1 ms). The drain waits a kernel makes
+// after a failure, which report nothing, keep the fixed kWaitLimitNs, so a
+// short limit can never cut a drain short.
+static __device__ uint64_t g_wait_limit_ns = kWaitLimitNs;
+
+__device__ __forceinline__ uint64_t wait_limit_ns(const int *status)
+{
+    return status ? *(volatile uint64_t *)&g_wait_limit_ns : kWaitLimitNs;
+}
 
 __device__ __forceinline__ uint64_t globaltimer_ns()
 {
@@ -62,18 +73,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 }
 
 // Bounded wait for the phase with the given parity to complete. Gives up
-// after kWaitLimitNs, or as soon as another role has recorded a failure in
+// after the wait limit (above), or as soon as another role has recorded a failure in
 // *status; on its own timeout writes `code` to *status (first writer wins).
 // Returns false when it gave up.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status, int code)
 {
     if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = globaltimer_ns();
+    const uint64_t t0 = globaltimer_ns(), limit = wait_limit_ns(status);
     while (true) {
         for (int i = 0; i < 32; ++i)
             if (mbar_try_wait(bar, parity)) return true;
         if (status && *(volatile int *)status != 0) return false;
-        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+        if (globaltimer_ns() - t0 > limit) {
             if (status) atomicCAS(status, 0, code);
             return false;
         }
@@ -248,12 +259,12 @@ __device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t *bar, uint32_t pa
 __device__ __forceinline__ bool mbar_wait_cluster(uint64_t *bar, uint32_t parity, int *status, int code)
 {
     if (mbar_try_wait_cluster(bar, parity)) return true;
-    const uint64_t t0 = globaltimer_ns();
+    const uint64_t t0 = globaltimer_ns(), limit = wait_limit_ns(status);
     while (true) {
         for (int i = 0; i < 32; ++i)
             if (mbar_try_wait_cluster(bar, parity)) return true;
         if (status && *(volatile int *)status != 0) return false;
-        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+        if (globaltimer_ns() - t0 > limit) {
             if (status) atomicCAS(status, 0, code);
             return false;
         }

@@ -2,8 +2,8 @@
 
 The binding is written against the Fortran-style symbols, so the same class
 drives any library that exports them: libmwblas_gb300.so (the GB300 library),
-or a build of the reference epblas-parallel mwblas. This is the binding a
-Python caller of the reference would write; INTEGRATION.md shows it.
+or a build of the reference epblas-parallel mwblas. It is the binding a
+Python caller of the reference would write.
 
 Double-double arrays are numpy float64 arrays whose last axis holds the two
 limbs (hi, lo). A column-major m x n matrix with leading dimension ld is a
@@ -157,6 +157,8 @@ class MWBlas:
             self._sig("mwblas_last_error_routine", _ch, [])
             self._sig("mwblas_clear_error", None, [])
             self._sig("mwblas_debug_fail_alloc_after", None, [_i64])
+            self._sig("mwblas_set_wait_limit_ns", C.c_uint64, [C.c_uint64])
+            self._sig("mwblas_debug_lose_operand_loads", None, [_i32])
             self._sig("mwblas_launch_count", _i64, [])
             self._sig("mwblas_version", _ch, [])
             self._sig("mgemv_n_noalloc", _i32, [_i64, _i64, R, _p, _i64, _p, _i64, R, _p, _i64, _p])

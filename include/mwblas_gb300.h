@@ -554,6 +554,20 @@ void mwblas_clear_error(void);
  * GPU fault. */
 void mwblas_debug_fail_alloc_after(int64_t count);
 
+/* Limit of the bounded device waits of the tensor-core kernels, in
+ * nanoseconds, on the current device (0 restores the default of 2 s; values
+ * below 1 ms are raised to 1 ms). A wait that runs out makes the kernel drain
+ * its own copies and MMAs, free its tensor memory and return; the routine then
+ * reports MWBLAS_ERR_TIMEOUT and the contents of its output are unspecified.
+ * Returns the previous limit. No counterpart in the reference. */
+uint64_t mwblas_set_wait_limit_ns(uint64_t ns);
+
+/* Test hook: the next `count` launches of the CTA-pair residue GEMM issue no
+ * operand loads, so their first wait for a landed operand stage runs out (with
+ * nothing in flight) and the call reports MWBLAS_ERR_TIMEOUT. Exercises the
+ * timeout path without a GPU fault. */
+void mwblas_debug_lose_operand_loads(int count);
+
 /* Number of kernels this library has launched in the process. */
 int64_t mwblas_launch_count(void);
 

@@ -748,17 +748,30 @@ void or_qgemv(char trans, int64_t m, int64_t n, const dd *alpha, const dd *A, in
     }
 }
 
-/* DOT in binary128 */
+/* DOT in binary128. Long vectors are summed in 64 contiguous slices in
+ * parallel, the slice sums added in slice order (deterministic); the binary128
+ * rounding of either order is far below the double-double tolerance. */
 void or_qdot(int64_t n, const dd *x, int64_t incx, const dd *y, int64_t incy, dd *out)
 {
-    qreal acc = 0;
-    int64_t ix = (incx < 0) ? (-n + 1) * incx : 0;
-    int64_t iy = (incy < 0) ? (-n + 1) * incy : 0;
-    for (int64_t i = 0; i < n; ++i) {
-        acc += q_of(x[ix]) * q_of(y[iy]);
-        ix += incx;
-        iy += incy;
+    const int64_t ix0 = (incx < 0) ? (-n + 1) * incx : 0;
+    const int64_t iy0 = (incy < 0) ? (-n + 1) * incy : 0;
+    enum { SLICES = 64 };
+    qreal part[SLICES];
+    const int64_t ns = n >= (1 << 20) ? SLICES : 1;
+#pragma omp parallel for schedule(dynamic, 1) if (ns > 1)
+    for (int64_t s = 0; s < ns; ++s) {
+        const int64_t i0 = n * s / ns, i1 = n * (s + 1) / ns;
+        qreal acc = 0;
+        int64_t ix = ix0 + i0 * incx, iy = iy0 + i0 * incy;
+        for (int64_t i = i0; i < i1; ++i) {
+            acc += q_of(x[ix]) * q_of(y[iy]);
+            ix += incx;
+            iy += incy;
+        }
+        part[s] = acc;
     }
+    qreal acc = 0;
+    for (int64_t s = 0; s < ns; ++s) acc += part[s];
     *out = dd_of(acc);
 }
 

@@ -26,10 +26,17 @@ _p = C.c_void_p
 _c = C.c_char
 
 
-def build(ref: bool = False) -> None:
-    """Builds liboracle.so (and the reference libraries when `ref`)."""
+def build(ref: bool = False, ref_dir: str | None = None) -> None:
+    """Builds liboracle.so (and, when `ref`, the reference libraries from the
+    reference checkout at `ref_dir`, else at $EPBLAS_REFERENCE_DIR)."""
     targets = ["all"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}", *targets], check=True)
+    extra = []
+    if ref:
+        d = ref_dir or os.environ.get("EPBLAS_REFERENCE_DIR", "")
+        if not d:
+            raise RuntimeError("building the reference needs EPBLAS_REFERENCE_DIR (a checkout of the reference)")
+        extra = [f"REF={d}"]
+    subprocess.run(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}", *targets, *extra], check=True)
 
 
 def _ptr(a):
