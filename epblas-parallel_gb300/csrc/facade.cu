@@ -1904,6 +1904,7 @@ int mwblas_set_ozaki_bits(int bits)
     return prev;
 }
 int mwblas_last_ozaki_moduli(void) { return mw::ozaki_last_moduli(); }
+int mwblas_last_ozaki_bits(int operand) { return mw::ozaki_last_bits(operand); }
 
 // ---- level 1 -----------------------------------------------------------------------------
 

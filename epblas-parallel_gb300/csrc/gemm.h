@@ -39,6 +39,7 @@ bool gemm_fixed_real(const GemmArgs &g, const char *routine);
 bool gemm_ozaki_real(const GemmArgs &g, int bits, const char *routine);
 bool gemm_ozaki_cplx(const GemmArgs &g, int bits, const char *routine);
 int ozaki_last_moduli();
+int ozaki_last_bits(int operand);   // 0: op(A), 1: op(B)
 
 // C := beta*C over an m x n block (beta_kind 0 writes zeros, 1 is a no-op).
 // uplo restricts the update to a triangle (0 full, 1 upper, 2 lower); herm
@@ -49,10 +50,12 @@ void launch_scale_matrix_c(int64_t m, int64_t n, cdd_host beta, int beta_kind, v
                            bool herm = false);
 
 // Exponent bounds of the rows / columns of op(X) (X column-major
-// rows_x x cols_x; elem2 = 1 real, 2 complex).
+// rows_x x cols_x; elem2 = 1 real, 2 complex); with `low`, also the binary
+// exponent of the lowest set bit in each row / column (0x3f3f3f3f when it
+// holds no nonzero finite entry).
 void launch_exp_rows_of_op(const void *X, int64_t rows_x, int64_t cols_x, int64_t ld, bool trans, int elem2,
-                           int *out);
+                           int *out, int *low = nullptr);
 void launch_exp_cols_of_op(const void *X, int64_t rows_x, int64_t cols_x, int64_t ld, bool trans, int elem2,
-                           int *out);
+                           int *out, int *low = nullptr);
 
 }  // namespace mw

@@ -46,39 +46,79 @@ __device__ __forceinline__ int exp_bound(double x)
     return (int)(b >> 52) - 1023;
 }
 
+// Binary exponent of the lowest set bit of the double-double value hi + lo
+// (kLowNone for zero). With |lo| <= ulp(hi)/2, lo's lowest bit lies below
+// hi's, so it is lo's when lo != 0. Non-finite values give kLowNone too (their
+// rows are NaN in the output whatever the width).
+constexpr int kLowNone = 0x3f3f3f3f;   // also the byte-wise memset value below
+__device__ __forceinline__ int low_bit(double2 v)
+{
+    const uint64_t bl = (uint64_t)__double_as_longlong(v.y) & 0x7fffffffffffffffull;
+    const uint64_t b = bl ? bl : ((uint64_t)__double_as_longlong(v.x) & 0x7fffffffffffffffull);
+    const uint32_t bx = (uint32_t)(b >> 52);
+    if (b == 0 || bx == 0x7ff) return kLowNone;
+    const uint64_t sig = bx ? ((b & 0xfffffffffffffull) | (1ull << 52)) : b;
+    return (bx ? (int)bx : 1) - 1075 + (__ffsll((long long)sig) - 1);
+}
+
 // Row exponent bound of a column-major matrix M (rows x cols, ld): out[i] =
-// max over j of exp_bound(M[i + j*ld].hi). Thread per row, grid.y splits the
-// columns; combined with atomicMax.
+// max over j of exp_bound(M[i + j*ld].hi); with `low`, also low[i] = min over
+// j of low_bit(M[i + j*ld]). Thread per row, grid.y splits the columns;
+// combined with atomicMax / atomicMin.
 __global__ void k_exp_rows(int64_t rows, int64_t cols, const double2 *M, int64_t ld, int elem2, int *out,
-                           int64_t cols_per_y)
+                           int64_t cols_per_y, int *low)
 {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= rows) return;
     int64_t j0 = blockIdx.y * cols_per_y;
     int64_t j1 = min(cols, j0 + cols_per_y);
-    int e = kNoExp;
+    int e = kNoExp, lb = kLowNone;
+    if (low) {
+#pragma unroll 4
+        for (int64_t j = j0; j < j1; ++j) {
+            const double2 *p = M + elem2 * (i + j * ld);
+            for (int w = 0; w < elem2; ++w) {
+                const double2 v = p[w];
+                e = max(e, exp_bound(v.x));
+                lb = min(lb, low_bit(v));
+            }
+        }
+        atomicMin(low + i, lb);
+    } else {
 #pragma unroll 8
-    for (int64_t j = j0; j < j1; ++j) {
-        const double2 *p = M + elem2 * (i + j * ld);
-        for (int w = 0; w < elem2; ++w) e = max(e, exp_bound(p[w].x));
+        for (int64_t j = j0; j < j1; ++j) {
+            const double2 *p = M + elem2 * (i + j * ld);
+            for (int w = 0; w < elem2; ++w) e = max(e, exp_bound(p[w].x));
+        }
     }
     atomicMax(out + i, e);
 }
 
-// Column exponent bound: out[j] = max over i of exp_bound(M[i + j*ld].hi).
-// Warp per column, lanes stride down the contiguous column.
-__global__ void k_exp_cols(int64_t rows, int64_t cols, const double2 *M, int64_t ld, int elem2, int *out)
+// Column exponent bound: out[j] = max over i of exp_bound(M[i + j*ld].hi)
+// (and low[j] = min of low_bit). Warp per column, lanes stride down the
+// contiguous column.
+__global__ void k_exp_cols(int64_t rows, int64_t cols, const double2 *M, int64_t ld, int elem2, int *out, int *low)
 {
     int64_t j = blockIdx.x * (int64_t)(blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
     if (j >= cols) return;
-    int e = kNoExp;
+    int e = kNoExp, lb = kLowNone;
     for (int64_t i = lane; i < rows; i += 32) {
         const double2 *p = M + elem2 * (i + j * ld);
-        for (int w = 0; w < elem2; ++w) e = max(e, exp_bound(p[w].x));
+        for (int w = 0; w < elem2; ++w) {
+            const double2 v = p[w];
+            e = max(e, exp_bound(v.x));
+            if (low) lb = min(lb, low_bit(v));
+        }
     }
-    for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_down_sync(0xffffffffu, e, off));
-    if (lane == 0) out[j] = e;
+    for (int off = 16; off > 0; off >>= 1) {
+        e = max(e, __shfl_down_sync(0xffffffffu, e, off));
+        lb = min(lb, __shfl_down_sync(0xffffffffu, lb, off));
+    }
+    if (lane == 0) {
+        out[j] = e;
+        if (low) low[j] = lb;
+    }
 }
 
 // Exponent offset of sigma above ea + eb: a fold block holds at most
@@ -546,9 +586,9 @@ void launch_plain_c_conj(const GemmArgs &g, const int *ea, const int *eb)
 
 // Row exponents of op(X) where X is stored column-major (rows_x x cols_x) and
 // op(X) = X (trans=false) or X^T (trans=true). Produces one int per row of
-// op(X).
+// op(X), and with `low` the exponent of the lowest set bit in that row.
 void launch_exp_rows_of_op(const void *X, int64_t rows_x, int64_t cols_x, int64_t ld, bool trans, int elem2,
-                           int *out)
+                           int *out, int *low)
 {
     if (!trans) {
         // rows of X: thread per row, column range split over grid.y
@@ -560,20 +600,21 @@ void launch_exp_rows_of_op(const void *X, int64_t rows_x, int64_t cols_x, int64_
         if ((cols_x + per_y - 1) / per_y > 65535) per_y = (cols_x + 65534) / 65535;
         dim3 grid((unsigned)rb, (unsigned)((cols_x + per_y - 1) / per_y));
         cudaMemsetAsync(out, 0x80, sizeof(int) * rows_x, stream());
-        k_exp_rows<<<grid, 256, 0, stream()>>>(rows_x, cols_x, (const double2 *)X, ld, elem2, out, per_y);
+        if (low) cudaMemsetAsync(low, 0x3f, sizeof(int) * rows_x, stream());   // kLowNone
+        k_exp_rows<<<grid, 256, 0, stream()>>>(rows_x, cols_x, (const double2 *)X, ld, elem2, out, per_y, low);
     } else {
         // rows of X^T = columns of X
         dim3 grid((unsigned)((cols_x + 7) / 8));
-        k_exp_cols<<<grid, 256, 0, stream()>>>(rows_x, cols_x, (const double2 *)X, ld, elem2, out);
+        k_exp_cols<<<grid, 256, 0, stream()>>>(rows_x, cols_x, (const double2 *)X, ld, elem2, out, low);
     }
     count_launch();
 }
 
 // Column exponents of op(X): columns of X^T are rows of X and vice versa.
 void launch_exp_cols_of_op(const void *X, int64_t rows_x, int64_t cols_x, int64_t ld, bool trans, int elem2,
-                           int *out)
+                           int *out, int *low)
 {
-    launch_exp_rows_of_op(X, rows_x, cols_x, ld, !trans, elem2, out);
+    launch_exp_rows_of_op(X, rows_x, cols_x, ld, !trans, elem2, out, low);
 }
 
 void launch_scale_matrix(int64_t m, int64_t n, dd_host beta, int beta_kind, void *C, int64_t ldc, int uplo)

@@ -106,6 +106,7 @@ Moduli choose_moduli(double need_bits)
 }
 
 int g_last_moduli = 0;
+int g_last_bits[2] = {0, 0};   // bits of op(A), op(B) in the most recent call
 int g_mma_kind = -1;   // 0 tcgen05 per tile, 1 SIMT cross-check, 2 tcgen05 persistent, 3 CTA pairs (default)
 
 // Failure injection for the bounded-wait path: the next g_lose_loads launches
@@ -1179,7 +1180,7 @@ __device__ __forceinline__ bool finite_hi(double x)
 // 32-bit or pointer increments.
 __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint16_t *__restrict__ R,
                                                         int64_t Mp, int64_t Np, const int *__restrict__ ea,
-                                                        const int *__restrict__ eb, int bits, OzCrtParams K,
+                                                        const int *__restrict__ eb, int bsum, OzCrtParams K,
                                                         xw::XW Mx, xw::XW xb, dd::real beta, int beta_kind,
                                                         double2 *C, int64_t ldc, int uplo)
 {
@@ -1245,7 +1246,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
                 continue;
             }
             xw::XW v = xw::zero();
-            if (h ? live1 : live0) v = (h ? acc1 : acc0).finish_xw(Mx, (bits - 2 - eai) + (bits - 2 - ebj));
+            if (h ? live1 : live0) v = (h ? acc1 : acc0).finish_xw(Mx, bsum - 4 - eai - ebj);
             if (beta_kind != 0) {
                 const double2 c0 = *pe;
                 if (!finite_hi(c0.x)) {
@@ -1268,7 +1269,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
 // P3 = (Ar+Ai)*(Br+Bi) as components 0..2; Re = P1 - P2, Im = P3 - P1 - P2.
 __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const uint16_t *__restrict__ R,
                                                           int64_t Mp, int64_t Np, const int *__restrict__ ea,
-                                                          const int *__restrict__ eb, int bits, OzCrtParams K,
+                                                          const int *__restrict__ eb, int bsum, OzCrtParams K,
                                                           xw::XW Mx, xw::XW ar, xw::XW ai, int alpha_one,
                                                           dd::cplx beta, xw::XW br, xw::XW bi, int beta_kind,
                                                           double2 *C, int64_t ldc, int uplo, int herm, int real_beta)
@@ -1322,7 +1323,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
                 const uint16_t *q = rp + (int64_t)l * plane;
                 add_l(l, __ldcs(q), __ldcs(q + cstride), __ldcs(q + 2 * cstride));
             }
-            const int S2 = (bits - 2 - ea[i]) + (bits - 2 - eb[j]);
+            const int S2 = bsum - 4 - ea[i] - eb[j];
             vr = accr.finish_xw(Mx, S2);
             vi = acci.finish_xw(Mx, S2);
         }
@@ -1465,8 +1466,58 @@ bool ozaki_available()
 }
 
 int ozaki_last_moduli() { return g_last_moduli; }
+int ozaki_last_bits(int operand) { return (operand == 0 || operand == 1) ? g_last_bits[operand] : 0; }
 
 namespace {
+
+// Significant width of op(X)'s rows (or op(B)'s columns): the largest
+// e_i - low_i + 2 over rows that hold a nonzero finite entry, where e_i bounds
+// the row's binary exponents and low_i is the exponent of its lowest set bit.
+// Scaled to that many bits (A'_ip = a_ip * 2^(bits - 2 - e_i)), every entry of
+// such a row is an exact integer below 2^(bits - 1).
+constexpr int kLowNone = 0x3f3f3f3f;   // no nonzero finite entry (the scan's fill value)
+__global__ void k_width(int64_t rows, const int *__restrict__ e, const int *__restrict__ low, int *out)
+{
+    int w = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ei = e[i], li = low[i];
+        if (ei > kNoExp / 2 && ei < 1024 && li != kLowNone) w = max(w, ei - li + 2);
+    }
+    for (int off = 16; off > 0; off >>= 1) w = max(w, __shfl_down_sync(0xffffffffu, w, off));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, w);
+}
+
+
+// Products at least this large (m n k) on device-resident operands size their
+// moduli from the operands' significant width; the readback of the two widths
+// costs one stream synchronisation (~20 us).
+constexpr double kWidthMinWork = 512.0 * 512.0 * 512.0;
+
+// The significant widths of op(A)'s rows and op(B)'s columns, read back to the
+// host; false when they could not be (the caller then keeps the full width).
+bool read_widths(int64_t m, int64_t n, const int *ea, const int *eb, const int *la, const int *lb, int *w,
+                 int &wa, int &wb)
+{
+    thread_local int *host = nullptr;
+    if (!host && cudaHostAlloc((void **)&host, 2 * sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        host = nullptr;
+        return false;
+    }
+    cudaMemsetAsync(w, 0, 2 * sizeof(int), stream());
+    const int ga = (int)std::min<int64_t>((m + 255) / 256, 4 * (int64_t)device_sm_count());
+    const int gb = (int)std::min<int64_t>((n + 255) / 256, 4 * (int64_t)device_sm_count());
+    k_width<<<ga, 256, 0, stream()>>>(m, ea, la, w);
+    k_width<<<gb, 256, 0, stream()>>>(n, eb, lb, w + 1);
+    count_launch(2);
+    if (cudaMemcpyAsync(host, w, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream()) != cudaSuccess ||
+        cudaStreamSynchronize(stream()) != cudaSuccess) {
+        return false;   // the routine's own synchronisation reports the error
+    }
+    wa = host[0];
+    wb = host[1];
+    return true;
+}
 
 bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine)
 {
@@ -1518,9 +1569,20 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     // carry exponent bound 1024, the residues there are don't-care values,
     // and the reconstruction writes NaN to every output they reach (the
     // reference's double-double product of an infinity is NaN).
-    int *ex = (int *)dev_alloc(sizeof(int) * (size_t)(m + n + 2), routine);
+    // The moduli count follows from the operands' significant width where the
+    // operands are on the device and the call may wait for the exponent scan
+    // (not while a stream is being captured); otherwise from the full width.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream(), &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusActive;
+    }
+    const bool detect = bits_req <= 0 && !g.hs && cap == cudaStreamCaptureStatusNone &&
+                        (double)m * (double)n * (double)k >= kWidthMinWork;
+    int *ex = (int *)dev_alloc(sizeof(int) * (size_t)(detect ? 2 * (m + n) + 4 : m + n + 2), routine);
     if (!ex) return false;
     int *ea = ex, *eb = ex + m;
+    int *la = detect ? ex + m + n : nullptr, *lb = detect ? la + m : nullptr, *wbuf = detect ? lb + n : nullptr;
     // Operands still arriving from the host: A's exponents and residues are
     // computed while B is copied, and C is waited for only by the
     // reconstruction, so its copy runs under the residue GEMMs.
@@ -1531,16 +1593,31 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         dev_free(ex);
         return false;
     }
-    if (!a_blocks) launch_exp_rows_of_op(g.A, g.ta ? k : m, g.ta ? m : k, g.lda, g.ta, E, ea);
-    if (!hs) launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, E, eb);
+    if (!a_blocks) launch_exp_rows_of_op(g.A, g.ta ? k : m, g.ta ? m : k, g.lda, g.ta, E, ea, la);
+    if (!hs) launch_exp_cols_of_op(g.B, g.tb ? n : k, g.tb ? k : n, g.ldb, g.tb, E, eb, lb);
 
-    // 2. precision and moduli (complex: |Re|, |Im| <= 2k * 2^(2bits-2))
+    // 2. precision and moduli. Rows of op(A) are scaled to bits_a bits and
+    // columns of op(B) to bits_b: by default the 106 bits of a double-double,
+    // fewer where every entry is an exact integer at fewer bits (double values
+    // with lo = 0 over a limited exponent range, say), which loses nothing.
+    // |A'B'| <= k 2^(bits_a + bits_b - 2) (complex: |Re|, |Im| twice that).
     int bits = bits_req > 0 ? bits_req : 106;
     if (bits < 40) bits = 40;
     if (bits > 120) bits = 120;
-    double need = 2.0 * (bits - 1) + std::log2((double)(k > 1 ? k : 1)) + 1.0 + 4.0 + (cplx ? 1.0 : 0.0);
+    int bits_a = bits, bits_b = bits;
+    if (detect) {
+        int wa = 0, wb = 0;
+        if (read_widths(m, n, ea, eb, la, lb, wbuf, wa, wb)) {
+            bits_a = std::max(8, std::min(bits, wa));
+            bits_b = std::max(8, std::min(bits, wb));
+        }
+    }
+    if (shared_ops) bits_a = bits_b = std::max(bits_a, bits_b);   // one conversion serves both operands
+    const double need = (bits_a - 1) + (bits_b - 1) + std::log2((double)(k > 1 ? k : 1)) + 1.0 + 4.0 + (cplx ? 1.0 : 0.0);
     Moduli md = choose_moduli(need);
     g_last_moduli = md.n;
+    g_last_bits[0] = bits_a;
+    g_last_bits[1] = bits_b;
     OzResParams rp;
     OzModParams mp;
     OzCrtParams cp;
@@ -1578,11 +1655,11 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         const double2 *Ai = a_rows_at(i0);
         __half *Ao = Ares + i0 * Kp;
         if (cplx) {
-            if (!g.ta) launch_residues<true, true>(ni, k, Ai, g.lda, ea + i0, bits, rp, Ao, rpad, Kp, g.ca, Mp);
-            else launch_residues<false, true>(ni, k, Ai, g.lda, ea + i0, bits, rp, Ao, rpad, Kp, g.ca, Mp);
+            if (!g.ta) launch_residues<true, true>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, g.ca, Mp);
+            else launch_residues<false, true>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, g.ca, Mp);
         } else {
-            if (!g.ta) launch_residues<true, false>(ni, k, Ai, g.lda, ea + i0, bits, rp, Ao, rpad, Kp, 0, Mp);
-            else launch_residues<false, false>(ni, k, Ai, g.lda, ea + i0, bits, rp, Ao, rpad, Kp, 0, Mp);
+            if (!g.ta) launch_residues<true, false>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, 0, Mp);
+            else launch_residues<false, false>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, 0, Mp);
         }
     };
     // row block ib of op(A): wait for it, scan its exponents, convert it
@@ -1609,11 +1686,11 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         const double2 *Bj = b_cols(j0);
         __half *Bo = Bres + j0 * Kp;
         if (cplx) {
-            if (!g.tb) launch_residues<false, true>(nn, k, Bj, g.ldb, eb + j0, bits, rp, Bo, rpad, Kp, g.cb, Np);
-            else launch_residues<true, true>(nn, k, Bj, g.ldb, eb + j0, bits, rp, Bo, rpad, Kp, g.cb, Np);
+            if (!g.tb) launch_residues<false, true>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, g.cb, Np);
+            else launch_residues<true, true>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, g.cb, Np);
         } else {
-            if (!g.tb) launch_residues<false, false>(nn, k, Bj, g.ldb, eb + j0, bits, rp, Bo, rpad, Kp, 0, Np);
-            else launch_residues<true, false>(nn, k, Bj, g.ldb, eb + j0, bits, rp, Bo, rpad, Kp, 0, Np);
+            if (!g.tb) launch_residues<false, false>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, 0, Np);
+            else launch_residues<true, false>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, 0, Np);
         }
     };
     if (!blocked) {
@@ -1696,7 +1773,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
             bool alpha_one = (g.alpha.hi == 1.0 && g.alpha.lo == 0.0);
             // alpha folded into M: alpha * X = T * (alpha M)
             const xw::XW aM = alpha_one ? Mx : xw::mul(xw::from_dd(g.alpha.hi, g.alpha.lo), Mx);
-            k_oz_reconstruct<<<grid, 256, 0, stream()>>>((int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits, cp, aM,
+            k_oz_reconstruct<<<grid, 256, 0, stream()>>>((int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits_a + bits_b, cp, aM,
                                                         xw::from_dd(g.beta.hi, g.beta.lo),
                                                         dd::make(g.beta.hi, g.beta.lo), g.beta_kind, Cj, g.ldc,
                                                         g.uplo);
@@ -1709,7 +1786,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
             bool alpha_one = (g.calpha.re.hi == 1.0 && g.calpha.re.lo == 0.0 && g.calpha.im.hi == 0.0 &&
                               g.calpha.im.lo == 0.0);
             k_oz_reconstruct_c<<<grid, 256, 0, stream()>>>(
-                (int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits, cp, Mx, xw::from_dd(al.re.hi, al.re.lo),
+                (int)m, (int)nn, Rj, Mp, Np, ea, eb + j0, bits_a + bits_b, cp, Mx, xw::from_dd(al.re.hi, al.re.lo),
                 xw::from_dd(al.im.hi, al.im.lo), alpha_one ? 1 : 0, be, xw::from_dd(be.re.hi, be.re.lo),
                 xw::from_dd(be.im.hi, be.im.lo), g.beta_kind, Cj, g.ldc, g.uplo, g.herm ? 1 : 0, g.herm ? 1 : 0);
         }

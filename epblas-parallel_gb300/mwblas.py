@@ -146,6 +146,7 @@ class MWBlas:
             self._sig("mwblas_get_gemm_engine", _i32, [])
             self._sig("mwblas_set_ozaki_bits", _i32, [_i32])
             self._sig("mwblas_last_ozaki_moduli", _i32, [])
+            self._sig("mwblas_last_ozaki_bits", _i32, [_i32])
             self._sig("mwblas_set_ozaki_mma", _i32, [_i32])
             self._sig("mwblas_set_kernel_timing", _i32, [_i32])
             self._sig("mwblas_last_phase_ms", C.c_float, [_i32])

@@ -492,12 +492,23 @@ int mtrsm_grouped(int64_t count, char side, char uplo, char transa, char diag, c
                   MWBLAS_R *const *b, const int64_t *ldb);
 
 /* Ozaki scheme controls.  bits = significant bits kept per scaled operand
- * row/column (0 = automatic from the operands' exponent range); the number
- * of moduli (integer GEMMs) follows from bits and k.  Returns the previous
- * value. */
+ * row/column, 40..120.  0 (the default) = automatic: 106 bits (a
+ * double-double's), reduced per operand to its significant width when every
+ * entry of op(A) (or op(B)) is an exact integer at fewer bits after its
+ * row's (column's) power-of-two scaling -- FP64 values with lo = 0 over a
+ * limited exponent range, for instance; the result is then unchanged in
+ * accuracy and computed with fewer moduli.  The width is measured on
+ * device-resident operands of products with m*n*k >= 512^3 and costs one
+ * stream synchronisation after the exponent scan; it is skipped while the
+ * library's stream is being captured and for host arrays that are uploaded
+ * block by block.  The number of moduli (integer GEMMs) follows from the two
+ * widths and k.  Returns the previous value. */
 int mwblas_set_ozaki_bits(int bits);
-/* Moduli count used by the most recent Ozaki GEMM on this thread. */
+/* Moduli count used by the most recent Ozaki GEMM (process-wide). */
 int mwblas_last_ozaki_moduli(void);
+/* Bits the most recent Ozaki GEMM scaled op(A) (operand 0) or op(B)
+ * (operand 1) to. */
+int mwblas_last_ozaki_bits(int operand);
 /* Residue-GEMM unit of the Ozaki engine: 0 = tcgen05 tensor cores, one CTA
  * per (modulus, tile), 1 = CUDA cores (an independent exact path used to
  * cross-check the tensor cores), 2 = tcgen05 in a persistent kernel (one CTA

@@ -295,3 +295,160 @@ def test_pair_kernel_large_device_product_bit_identical(gpu, rng, cplx_):
         finally:
             gpu.lib.mwblas_set_ozaki_mma(prev)
     assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
+
+
+# ---- moduli count from the operands' significant width ---------------------------------------
+
+def _lo0(rng, rows, cols):
+    """FP64 values (lo = 0), hi ~ U[-1, 1): the reference fuzz's real64x2(2u - 1)."""
+    a = mwb.dd_matrix(rng, rows, cols)
+    a[..., 1] = 0.0
+    return a
+
+
+def _dev(torch, a):
+    return torch.from_numpy(a).cuda()
+
+
+def _ozaki_dev(gpu, torch, ta, tb, m, n, k, al, dA, lda, dB, ldb, be, C0, bits=0):
+    """One tensor-core GEMM on device arrays at a given bits setting; returns
+    the output, the moduli count and the bits of op(A), op(B)."""
+    dC = _dev(torch, C0)
+    prev = gpu.lib.mwblas_set_ozaki_bits(bits)
+    try:
+        gpu.mgemm(ta, tb, m, n, k, al, dA.data_ptr(), lda, dB.data_ptr(), ldb, be, dC.data_ptr(), m,
+                  engine="ozaki")
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+    finally:
+        gpu.lib.mwblas_set_ozaki_bits(prev)
+    return (dC.cpu().numpy(), gpu.lib.mwblas_last_ozaki_moduli(),
+            (gpu.lib.mwblas_last_ozaki_bits(0), gpu.lib.mwblas_last_ozaki_bits(1)))
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("T", "N"), ("N", "T")])
+def test_fp64_inputs_take_fewer_moduli_with_identical_results(gpu, oracle, rng, ta, tb):
+    """lo = 0 operands are exact integers at about 60-70 bits after the row /
+    column scaling, so the automatic width cuts the moduli count; the exact
+    integer product, hence the rounded result, is the same as at 106 bits."""
+    import torch
+    m, n, k = 512, 640, 1024
+    A = _lo0(rng, m if ta == "N" else k, k if ta == "N" else m)
+    B = _lo0(rng, k if tb == "N" else n, n if tb == "N" else k)
+    C0 = mwb.dd_matrix(rng, m, n)
+    al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+    lda, ldb = A.shape[1], B.shape[1]
+    dA, dB = _dev(torch, A), _dev(torch, B)
+    auto, md_auto, (ba, bb) = _ozaki_dev(gpu, torch, ta, tb, m, n, k, al, dA, lda, dB, ldb, be, C0, 0)
+    full, md_full, bw_full = _ozaki_dev(gpu, torch, ta, tb, m, n, k, al, dA, lda, dB, ldb, be, C0, 106)
+    assert bw_full == (106, 106)
+    assert 50 <= ba < 106 and 50 <= bb < 106, (ba, bb)
+    assert md_auto <= md_full - 7, (md_auto, md_full)
+    np.testing.assert_array_equal(auto, full)
+    want = oracle.qgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0.copy(), m)
+    err = orc.normwise_error(auto, want, op_norm(al, k, A, B, be, C0))
+    assert err <= max(10, 4 * k) * orc.EPS_DD, err
+
+
+def test_width_is_full_for_double_double_inputs(gpu, rng):
+    import torch
+    m = n = k = 512
+    A, B = mwb.dd_matrix(rng, m, k), mwb.dd_matrix(rng, k, n)
+    C0 = np.zeros((n, m, 2))
+    dA, dB = _dev(torch, A), _dev(torch, B)
+    _, _, bw = _ozaki_dev(gpu, torch, "N", "N", m, n, k, np.array([1.0, 0.0]), dA, m, dB, k, np.zeros(2), C0)
+    assert bw == (106, 106)
+
+
+def test_small_integer_inputs_use_few_moduli_and_are_exact(gpu, rng):
+    """Entries in {-3..3}: a few bits per operand, a handful of moduli, and the
+    product of integers is exact."""
+    import torch
+    m, n, k = 600, 520, 700
+    A = np.zeros((k, m, 2)); A[..., 0] = rng.integers(-3, 4, (k, m))
+    B = np.zeros((n, k, 2)); B[..., 0] = rng.integers(-3, 4, (n, k))
+    dA, dB = _dev(torch, A), _dev(torch, B)
+    dC = torch.zeros((n, m, 2), dtype=torch.float64, device="cuda")
+    gpu.mgemm("N", "N", m, n, k, np.array([1.0, 0.0]), dA.data_ptr(), m, dB.data_ptr(), k, np.zeros(2),
+              dC.data_ptr(), m, engine="ozaki")
+    assert gpu.last_error()[0] == 0
+    md = gpu.lib.mwblas_last_ozaki_moduli()
+    assert gpu.lib.mwblas_last_ozaki_bits(0) <= 8 and md <= 5, md
+    exact = (A[..., 0].T @ B[..., 0].T)          # m x n, exact in float64 here
+    got = dC.cpu().numpy()
+    np.testing.assert_array_equal(got[..., 0], exact.T)
+    assert np.all(got[..., 1] == 0)
+
+
+def test_width_ignores_nonfinite_and_zero_rows(gpu, rng):
+    """A row of op(A) holding an Inf (its outputs become NaN) and an all-zero
+    row do not widen the operand; the other outputs equal the full-width
+    ones. One entry far below the rest of its row does widen it (to the full
+    106 bits, as exactness would need ~950)."""
+    import torch
+    m, n, k = 512, 512, 600
+    A = _lo0(rng, m, k)
+    B = _lo0(rng, k, n)
+    A[:, 5, 0] = 0.0                             # row 5 all zero
+    A[17, 9, 0] = np.inf                         # row 9 holds an Inf
+    C0 = np.zeros((n, m, 2))
+    one, zero = np.array([1.0, 0.0]), np.zeros(2)
+    dA, dB = _dev(torch, A), _dev(torch, B)
+    auto, md_auto, (ba, _) = _ozaki_dev(gpu, torch, "N", "N", m, n, k, one, dA, m, dB, k, zero, C0, 0)
+    full, md_full, _ = _ozaki_dev(gpu, torch, "N", "N", m, n, k, one, dA, m, dB, k, zero, C0, 106)
+    assert ba < 106 and md_auto < md_full
+    assert np.all(np.isnan(auto[:, 9, 0])) and np.all(np.isnan(full[:, 9, 0]))
+    np.testing.assert_array_equal(np.delete(auto, 9, axis=1), np.delete(full, 9, axis=1))
+    assert np.all(auto[:, 5] == 0)
+    A[3, 11, 0] = 2.0 ** -900                    # row 11: one entry far below the others
+    dA = _dev(torch, A)
+    _, _, (ba, _) = _ozaki_dev(gpu, torch, "N", "N", m, n, k, one, dA, m, dB, k, zero, C0, 0)
+    assert ba == 106
+
+
+def test_fp64_inputs_complex_and_syrk(gpu, oracle, rng):
+    """The width also sizes complex products (real and imaginary parts
+    together) and SYRK, where one conversion serves both operands."""
+    import torch
+    n, k = 520, 600
+    A = _lo0(rng, n, k)
+    dA = _dev(torch, A)
+    al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+    C0 = mwb.dd_matrix(rng, n, n)
+    got = []
+    for bits in (0, 106):
+        dC = _dev(torch, C0)
+        prev = gpu.lib.mwblas_set_ozaki_bits(bits)
+        prev_e = gpu.lib.mwblas_set_gemm_engine(2)
+        try:
+            gpu.msyrk("U", "N", n, k, al, dA.data_ptr(), n, be, dC.data_ptr(), n)
+            assert gpu.last_error()[0] == 0
+            got.append((dC.cpu().numpy(), gpu.lib.mwblas_last_ozaki_moduli()))
+        finally:
+            gpu.lib.mwblas_set_ozaki_bits(prev)
+            gpu.lib.mwblas_set_gemm_engine(prev_e)
+    assert got[0][1] < got[1][1]
+    np.testing.assert_array_equal(got[0][0], got[1][0])
+    # complex, conjugate-transposed B
+    m, n, k = 512, 512, 520
+    Ac = mwb.dd_matrix(rng, m, k, cplx_=True); Ac[..., 1] = 0.0
+    Bc = mwb.dd_matrix(rng, n, k, cplx_=True); Bc[..., 1] = 0.0
+    cal, cbe = mwb.random_cdd(rng, ()), mwb.random_cdd(rng, ())
+    Cc = mwb.dd_matrix(rng, m, n, cplx_=True)
+    dAc, dBc = _dev(torch, Ac), _dev(torch, Bc)
+    outs = []
+    for bits in (0, 106):
+        dC = _dev(torch, Cc)
+        prev = gpu.lib.mwblas_set_ozaki_bits(bits)
+        prev_e = gpu.lib.mwblas_set_gemm_engine(2)
+        try:
+            gpu.wgemm("N", "C", m, n, k, cal, dAc.data_ptr(), m, dBc.data_ptr(), n, cbe, dC.data_ptr(), m)
+            assert gpu.last_error()[0] == 0
+            outs.append((dC.cpu().numpy(), gpu.lib.mwblas_last_ozaki_moduli()))
+        finally:
+            gpu.lib.mwblas_set_ozaki_bits(prev)
+            gpu.lib.mwblas_set_gemm_engine(prev_e)
+    assert outs[0][1] < outs[1][1]
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    want = oracle.qwgemm("N", "C", m, n, k, cal, Ac, m, Bc, n, cbe, Cc.copy(), m)
+    op = orc.dd_abs(cal) * k * orc.dd_absmax(Ac) * orc.dd_absmax(Bc) + orc.dd_abs(cbe) * orc.dd_absmax(Cc)
+    assert orc.normwise_error(outs[0][0], want, op) <= max(10, 4 * k) * orc.EPS_DD
