@@ -464,7 +464,7 @@ def tc_traffic_from_profile():
 # workloads, each printed as one JSON line of the same shape as the headline.
 # ---------------------------------------------------------------------------
 
-WORKLOADS = ("gemm", "stress", "wgemm", "gemm_t", "gemm_fixed", "gemm_plain", "syrk", "herk", "trsm", "gemv", "dot",
+WORKLOADS = ("gemm", "stress", "gemm_fp64", "wgemm", "gemm_t", "gemm_fixed", "gemm_plain", "syrk", "herk", "trsm", "gemv", "dot",
              "axpy", "scal", "copy", "swap", "iamax", "batched_gemm", "batched_trsm", "gemmtr", "symm", "syr2k",
              "trmm", "wtrsm", "sbmv", "spmv", "tbsv")
 
@@ -554,6 +554,33 @@ def run_workload(args):
             op = orc.dd_abs(al) * n * orc.dd_absmax(hA) * orc.dd_absmax(hB) + orc.dd_abs(be) * orc.dd_absmax(hC0)
             check["normwise_err_sampled"] = orc.normwise_error(got, want, op)
             # componentwise view: error relative to |alpha| sum_p |a_ip||b_pj| of the sampled entries
+            check["samples"] = 256
+    elif w == "gemm_fp64":
+        # FP64 operands (lo = 0, hi ~ U[-1,1): the reference fuzz's real64x2(2u-1)) through the
+        # drop-in mgemm_64_ at n^3: the moduli count follows from their significant width
+        n = args.n
+        A = _dev_dd(torch, (n, n), gen, dev)
+        B = _dev_dd(torch, (n, n), gen, dev)
+        A[..., 1] = 0.0
+        B[..., 1] = 0.0
+        C = _dev_dd(torch, (n, n), gen, dev)
+        C0 = C.clone()
+        lib.lib.mwblas_set_gemm_engine(0)
+        fn = lambda: lib.mgemm("N", "N", n, n, n, al, A.data_ptr(), n, B.data_ptr(), n, be, C.data_ptr(), n)
+        ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: C.copy_(C0))
+        value, unit = 2.0 * n ** 3 / ms / 1e6, "DD-GFLOP/s"
+        metric = f"DD-GEMM GFLOP/s n={n} NN, FP64 operands (lo = 0), moduli from the operands' width"
+        cfg = {"workload": f"mgemm_64_ {n}^3 NN, A and B with lo = 0, hi ~ U[-1,1)", "engine": "AUTO"}
+        check["moduli"] = int(lib.lib.mwblas_last_ozaki_moduli())
+        check["bits"] = [int(lib.lib.mwblas_last_ozaki_bits(0)), int(lib.lib.mwblas_last_ozaki_bits(1))]
+        if o:
+            C.copy_(C0)
+            fn()
+            rows, cols = rng.integers(0, n, 256), rng.integers(0, n, 256)
+            hA, hB, hC0 = hb(A), hb(B), hb(C0)
+            want = o.qgemm("N", "N", n, n, n, al, hA, n, hB, n, be, hC0, n, rows=rows, cols=cols)
+            op = orc.dd_abs(al) * n * orc.dd_absmax(hA) * orc.dd_absmax(hB) + orc.dd_abs(be) * orc.dd_absmax(hC0)
+            check["normwise_err_sampled"] = orc.normwise_error(hb(C)[cols, rows], want, op)
             check["samples"] = 256
     elif w in ("gemm_fixed", "gemm_plain"):
         # one engine forced, n^3 NN (default n = 4096)

@@ -5,10 +5,13 @@ of its kind16 binary128 routines on seeded inputs (tests/golden/make_golden.py).
 The oracle's bit-exact restatements must reproduce the former bit for bit; its
 binary128 routines must agree with the latter to binary128 rounding level.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
-from conftest import orc, ref_library
+from conftest import ROOT, orc, ref_library
 
 
 def l1_case(z, meta, ci):
@@ -125,6 +128,23 @@ def test_gemm_port_is_bitexact_to_reference_simd_path(oracle, golden):
         oracle.port_mgemm(c["ta"], c["tb"], c["m"], c["n"], c["k"], z[k + "_alpha"], z[k + "_A"], c["lda"],
                           z[k + "_B"], c["ldb"], z[k + "_beta"], out, c["ldc"], simd_order=1)
         np.testing.assert_array_equal(out[:, :c["m"]], z[k + "_ref"][:, :c["m"]], err_msg=k)
+
+
+def test_gemm_port_is_bitexact_to_reference_scalar_path(oracle):
+    """or_port_mgemm(simd_order=0) -- the CPU baseline timed on aarch64 hosts --
+    reproduces the reference's GEMM built without its SIMD block (the scalar
+    micro-kernel, mgemm_serial.cpp:355-407) bit for bit, across the MC/KC/NC
+    block edges and every transpose pair (tests/golden/make_gemm_scalar.py)."""
+    z = np.load(os.path.join(ROOT, "tests", "golden", "ref_gemm_scalar.npz"))
+    meta = json.loads(bytes(z["meta_json"]).decode())
+    assert len(meta) >= 7
+    for c in meta:
+        k = c["key"]
+        out = z[k + "_C"].copy()
+        oracle.port_mgemm(c["ta"], c["tb"], c["m"], c["n"], c["k"], z[k + "_alpha"], z[k + "_A"], c["lda"],
+                          z[k + "_B"], c["ldb"], z[k + "_beta"], out, c["ldc"], simd_order=0)
+        np.testing.assert_array_equal(out[:, :c["m"]], z[k + "_ref"][:, :c["m"]], err_msg=k)
+        np.testing.assert_array_equal(out[:, c["m"]:], z[k + "_C"][:, c["m"]:], err_msg=k)   # padding untouched
 
 
 @pytest.mark.skipif(ref_library() is None, reason="reference build not present (needs the reference sources)")
