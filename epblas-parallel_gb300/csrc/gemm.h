@@ -38,6 +38,8 @@ bool gemm_fixed_real(const GemmArgs &g, const char *routine);
 // error recorded on failure.
 bool gemm_ozaki_real(const GemmArgs &g, int bits, const char *routine);
 bool gemm_ozaki_cplx(const GemmArgs &g, int bits, const char *routine);
+// Wait limit of the FP64 engine's TMA pipeline (its own copy of the device word).
+void set_plain_wait_limit(uint64_t ns);
 int ozaki_last_moduli();
 int ozaki_last_bits(int operand);   // 0: op(A), 1: op(B)
 

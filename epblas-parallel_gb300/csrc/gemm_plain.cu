@@ -28,9 +28,16 @@
 // in the worst case, independent of k, and ~2^-106 relative in typical use;
 // the reference's own fuzz tolerance is max(10, 4k) * 2^-104 of the same norm
 // (fuzz_mgemm.fypp tolerance line).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <atomic>
+#include <string>
+
 #include "dd.cuh"
 #include "gemm.h"
 #include "runtime.h"
+#include "sm100.cuh"
 
 namespace mw {
 
@@ -308,6 +315,194 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
     }
 }
 
+// ---- the same kernel with TMA-staged operand tiles ---------------------------------------
+//
+// One thread issues 2-D tensor copies (cp.async.bulk.tensor) of the next
+// k-slabs of op(A) and op(B) into a ring of NS shared-memory stages while all
+// threads run the extraction MACs on the current one; completion is counted
+// on one mbarrier per stage. The tensor maps describe A and B as 2-D arrays of
+// doubles (a double-double is two consecutive doubles) bounded by the operand
+// sizes, so slabs past m, n or k are filled with zeros by the copy engine
+// instead of by per-element bounds checks. A tile arrives in the storage order
+// of its operand: op(A) = A and op(B) = B^T stage as [k][row] (rows
+// contiguous), op(A) = A^T and op(B) = B as [row][k]. The arithmetic, its
+// order and hence the results are those of k_gemm_plain, bit for bit.
+//
+// Every wait is bounded (sm100::mbar_wait); when one gives up, the whole
+// block leaves the k loop together (__syncthreads_or), the issuing thread
+// waits for the copies it still has in flight, and the routine reports
+// MWBLAS_ERR_TIMEOUT at its synchronisation.
+template <int BM, int BN, int TM, int TN, bool TA, bool TB, int KB, int NS, bool COMP>
+__global__ void __launch_bounds__((BM / TM) * (BN / TN))
+    k_gemm_plain_tma(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int64_t m,
+                     int64_t n, int64_t k, dd::real alpha, dd::real beta, int beta_kind, double2 *C, int64_t ldc,
+                     const int *__restrict__ ea, const int *__restrict__ eb, int uplo, int SHIFT, int *status)
+{
+    constexpr int NTX = BM / TM;
+    constexpr int NTY = BN / TN;
+    constexpr int BK = 8;
+    constexpr uint32_t A_BYTES = BM * BK * 16, B_BYTES = BN * BK * 16;
+    static_assert(KB % BK == 0, "fold interval must be a multiple of the k-slab");
+
+    extern __shared__ __align__(128) unsigned char plain_smem_raw[];
+    // stages on a 128-byte boundary (the launch reserves 128 bytes for this)
+    unsigned char *plain_smem = (unsigned char *)(((uintptr_t)plain_smem_raw + 127) & ~(uintptr_t)127);
+    double2 *sA = reinterpret_cast<double2 *>(plain_smem);                   // [NS][BM * BK]
+    double2 *sB = reinterpret_cast<double2 *>(plain_smem + NS * A_BYTES);    // [NS][BN * BK]
+    uint64_t *full = reinterpret_cast<uint64_t *>(plain_smem + NS * (A_BYTES + B_BYTES));
+
+    const int tid = threadIdx.x;
+    const int tx = tid % NTX, ty = tid / NTX;
+    const int64_t i0 = (int64_t)blockIdx.x * BM, j0 = (int64_t)blockIdx.y * BN;
+    if ((uplo == 1 && i0 > j0 + BN - 1) || (uplo == 2 && i0 + BM - 1 < j0)) return;
+
+    const int nslabs = (int)((k + BK - 1) / BK);
+    if (tid == 0) {
+        sm100::tma_prefetch_desc(&mapA);
+        sm100::tma_prefetch_desc(&mapB);
+        for (int st = 0; st < NS; ++st) sm100::mbar_init(&full[st], 1);
+        sm100::fence_mbar_init();
+    }
+    __syncthreads();
+    // slab t into stage t % NS: A at (x, y) = (2 i0, k0) or (2 k0, i0), B likewise
+    auto issue = [&](int t) {
+        const int st = t % NS;
+        const int32_t k0 = t * BK;
+        sm100::mbar_arrive_expect_tx(&full[st], A_BYTES + B_BYTES);
+        if (!TA) sm100::tma_load_2d(sA + st * (BM * BK), &mapA, &full[st], (int32_t)(2 * i0), k0);
+        else sm100::tma_load_2d(sA + st * (BM * BK), &mapA, &full[st], 2 * k0, (int32_t)i0);
+        if (TB) sm100::tma_load_2d(sB + st * (BN * BK), &mapB, &full[st], (int32_t)(2 * j0), k0);
+        else sm100::tma_load_2d(sB + st * (BN * BK), &mapB, &full[st], 2 * k0, (int32_t)j0);
+    };
+    if (tid == 0)
+        for (int t = 0; t < NS - 1 && t < nslabs; ++t) issue(t);
+
+    int eai[TM], ebj[TN];
+#pragma unroll
+    for (int a = 0; a < TM; ++a) {
+        int64_t i = i0 + tx + a * NTX;
+        eai[a] = (i < m) ? ea[i] : kNoExp;
+    }
+#pragma unroll
+    for (int b = 0; b < TN; ++b) {
+        int64_t j = j0 + ty + b * NTY;
+        ebj[b] = (j < n) ? eb[j] : kNoExp;
+    }
+
+    // X2 (the second extraction level) only exists in the short-k kernel
+    double X[TM][TN], X2[COMP ? TM : 1][COMP ? TN : 1], L[TM][TN], Ah[TM][TN], Al[TM][TN];
+#pragma unroll
+    for (int a = 0; a < TM; ++a)
+#pragma unroll
+        for (int b = 0; b < TN; ++b) {
+            X[a][b] = make_sigma(eai[a], ebj[b], SHIFT);
+            if (COMP) X2[COMP ? a : 0][COMP ? b : 0] = make_sigma2(eai[a], ebj[b], SHIFT);
+            L[a][b] = 0.0;
+            Ah[a][b] = 0.0;
+            Al[a][b] = 0.0;
+        }
+
+    int since_fold = 0, issued = min(NS - 1, nslabs), t = 0;
+    bool failed = false;
+    for (; t < nslabs; ++t) {
+        // the stage of slab t - 1 was released by the barrier that ended the
+        // previous iteration: refill it with slab t + NS - 1
+        if (tid == 0 && t + NS - 1 < nslabs) {
+            issue(t + NS - 1);
+            issued = t + NS;
+        }
+        const int st = t % NS;
+        const bool ok = sm100::mbar_wait(&full[st], (uint32_t)(t / NS) & 1u, status, 5);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        const double2 *tA = sA + st * (BM * BK);
+        const double2 *tB = sB + st * (BN * BK);
+#pragma unroll
+        for (int p = 0; p < BK; ++p) {
+            double2 av[TM], bv[TN];
+#pragma unroll
+            for (int a = 0; a < TM; ++a) av[a] = TA ? tA[(tx + a * NTX) * BK + p] : tA[p * BM + tx + a * NTX];
+#pragma unroll
+            for (int b = 0; b < TN; ++b) bv[b] = TB ? tB[p * BN + ty + b * NTY] : tB[(ty + b * NTY) * BK + p];
+#pragma unroll
+            for (int a = 0; a < TM; ++a)
+#pragma unroll
+                for (int b = 0; b < TN; ++b) {
+                    double tt = __fma_rn(av[a].x, bv[b].x, X[a][b]);
+                    double q = __dsub_rn(X[a][b], tt);
+                    double r = __fma_rn(av[a].x, bv[b].x, q);
+                    X[a][b] = tt;
+                    if (COMP) {
+                        double &x2 = X2[COMP ? a : 0][COMP ? b : 0];
+                        double t2 = __dadd_rn(x2, r);
+                        double q2 = __dsub_rn(x2, t2);
+                        r = __dadd_rn(q2, r);
+                        x2 = t2;
+                    }
+                    double l = __dadd_rn(L[a][b], r);
+                    l = __fma_rn(av[a].x, bv[b].y, l);
+                    L[a][b] = __fma_rn(av[a].y, bv[b].x, l);
+                }
+        }
+        __syncthreads();   // stage st is free for the refill at the top of iteration t + 1
+
+        since_fold += BK;
+        if (since_fold == KB || t + 1 == nslabs) {
+            since_fold = 0;
+#pragma unroll
+            for (int a = 0; a < TM; ++a)
+#pragma unroll
+                for (int b = 0; b < TN; ++b) {
+                    double sg = make_sigma(eai[a], ebj[b], SHIFT);
+                    double s = __dsub_rn(X[a][b], sg);   // exact
+                    double lsum = L[a][b];
+                    if (COMP) {
+                        double &x2 = X2[COMP ? a : 0][COMP ? b : 0];
+                        double sg2 = make_sigma2(eai[a], ebj[b], SHIFT);
+                        lsum = __dadd_rn(lsum, __dsub_rn(x2, sg2));
+                        x2 = sg2;
+                    }
+                    double h, e;
+                    dd::two_sum(Ah[a][b], s, h, e);
+                    double lo = __dadd_rn(Al[a][b], __dadd_rn(e, lsum));
+                    dd::fast_two_sum(h, lo, Ah[a][b], Al[a][b]);
+                    X[a][b] = sg;
+                    L[a][b] = 0.0;
+                }
+        }
+    }
+    if (failed) {
+        // never leave with copies in flight: the slabs issued but not consumed
+        if (tid == 0)
+            for (int u = t; u < issued; ++u) sm100::mbar_wait(&full[u % NS], (uint32_t)(u / NS) & 1u, nullptr, 0);
+        return;
+    }
+
+#pragma unroll
+    for (int b = 0; b < TN; ++b) {
+        int64_t j = j0 + ty + b * NTY;
+        if (j >= n) continue;
+#pragma unroll
+        for (int a = 0; a < TM; ++a) {
+            int64_t i = i0 + tx + a * NTX;
+            if (i >= m) continue;
+            if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
+            dd::real acc = dd::make(Ah[a][b], Al[a][b]);
+            dd::real r = dd::mul_fast(alpha, acc);
+            double2 *pc = C + i + j * ldc;
+            if (beta_kind == 0) {
+                dd::store(pc, r);
+            } else {
+                dd::real c0 = dd::load(pc);
+                if (beta_kind == 2) c0 = dd::mul_exact(c0, beta);
+                dd::store(pc, dd::add_exact(c0, r));
+            }
+        }
+    }
+}
+
 // C := beta*C over an m x n block (beta == 0 writes zeros without reading).
 __global__ void k_scale_matrix(int64_t m, int64_t n, dd::real beta, int beta_kind, double2 *C, int64_t ldc,
                                int uplo)
@@ -322,6 +517,64 @@ __global__ void k_scale_matrix(int64_t m, int64_t n, dd::real beta, int beta_kin
         else
             dd::store(p, dd::mul_exact(dd::load(p), beta));
     }
+}
+
+// A 2-D tensor map over a column-major double-double matrix (rows x cols,
+// leading dimension ld), in doubles: dimension 0 = 2 * rows, dimension 1 =
+// cols; box = (2 * box_rows, box_cols).
+bool dd_map(CUtensorMap *map, const void *base, int64_t rows, int64_t cols, int64_t ld, uint32_t box_rows,
+            uint32_t box_cols, const char *routine)
+{
+    auto enc = (PFN_cuTensorMapEncodeTiled_v12000)tensor_map_encoder();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)(2 * rows), (cuuint64_t)cols};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * 16};
+    cuuint32_t box[2] = {2 * box_rows, box_cols};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<void *>(base), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error(routine, MWBLAS_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+        return false;
+    }
+    return true;
+}
+
+// TMA staging of the FP64 engine's tiles (default on; 0 = plain loads).
+std::atomic<int> g_plain_tma{1};
+
+template <int BM, int BN, int TM, int TN, int KB>
+bool dispatch_plain_tma(const GemmArgs &g, const int *ea, const int *eb, const char *routine)
+{
+    constexpr int NS = 4, BK = 8;
+    constexpr size_t SMEM = NS * (size_t)(BM + BN) * BK * 16 + NS * sizeof(uint64_t) + 128;
+    // op(A) tiles: A (m x k) boxes of BM rows x BK columns, or A^T's storage (k x m) boxes of BK x BM
+    CUtensorMap ma, mb;
+    const bool ok = (g.ta ? dd_map(&ma, g.A, g.k, g.m, g.lda, BK, BM, routine)
+                          : dd_map(&ma, g.A, g.m, g.k, g.lda, BM, BK, routine)) &&
+                    (g.tb ? dd_map(&mb, g.B, g.n, g.k, g.ldb, BN, BK, routine)
+                          : dd_map(&mb, g.B, g.k, g.n, g.ldb, BK, BN, routine));
+    if (!ok) return false;
+    dim3 grid((unsigned)((g.m + BM - 1) / BM), (unsigned)((g.n + BN - 1) / BN));
+    dim3 block((BM / TM) * (BN / TN));
+    dd::real al = dd::make(g.alpha.hi, g.alpha.lo), be = dd::make(g.beta.hi, g.beta.lo);
+    double2 *C = (double2 *)g.C;
+#define MW_LAUNCH(TA, TB)                                                                                          \
+    {                                                                                                              \
+        auto kern = g.k <= kCompMaxK ? k_gemm_plain_tma<BM, BN, TM, TN, TA, TB, KB, NS, true>                      \
+                                     : k_gemm_plain_tma<BM, BN, TM, TN, TA, TB, KB, NS, false>;                    \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);                        \
+        kern<<<grid, block, SMEM, stream()>>>(ma, mb, g.m, g.n, g.k, al, be, g.beta_kind, C, g.ldc, ea, eb, g.uplo, \
+                                              sigma_shift(KB, g.k, 1), device_status_word());                      \
+    }
+    if (!g.ta && !g.tb) MW_LAUNCH(false, false)
+    else if (!g.ta && g.tb) MW_LAUNCH(false, true)
+    else if (g.ta && !g.tb) MW_LAUNCH(true, false)
+    else MW_LAUNCH(true, true)
+#undef MW_LAUNCH
+    count_launch();
+    return true;
 }
 
 template <int BM, int BN, int TM, int TN, int KB>
@@ -639,12 +892,32 @@ bool gemm_plain_real(const GemmArgs &g, const char *routine)
     // op(B) is k x n: B stored (tb ? n x k : k x n)
     launch_exp_cols_of_op(g.B, g.tb ? g.n : g.k, g.tb ? g.k : g.n, g.ldb, g.tb, 1, eb);
     int64_t tiles64 = ((g.m + 63) / 64) * ((g.n + 63) / 64);
-    if (tiles64 >= 2 * (int64_t)device_sm_count())
-        dispatch_plain<64, 64, 4, 4, 8>(g, ea, eb);
-    else
-        dispatch_plain<32, 32, 2, 2, 8>(g, ea, eb);
+    const bool big = tiles64 >= 2 * (int64_t)device_sm_count();
+    // TMA staging wants 16-byte aligned operands (always true of device
+    // double-double arrays) and dimensions a tensor map can describe
+    const bool tma = g_plain_tma.load() != 0 && ((uintptr_t)g.A & 15) == 0 && ((uintptr_t)g.B & 15) == 0 &&
+                     g.m < ((int64_t)1 << 31) && g.n < ((int64_t)1 << 31) && g.k < ((int64_t)1 << 31) &&
+                     tensor_map_encoder() != nullptr;
+    bool done = false;
+    if (tma) {
+        done = big ? dispatch_plain_tma<64, 64, 4, 4, 8>(g, ea, eb, routine)
+                   : dispatch_plain_tma<32, 32, 2, 2, 8>(g, ea, eb, routine);
+        if (!done) {
+            dev_free(ex);
+            return false;
+        }
+    }
+    if (!done) {
+        if (big) dispatch_plain<64, 64, 4, 4, 8>(g, ea, eb);
+        else dispatch_plain<32, 32, 2, 2, 8>(g, ea, eb);
+    }
     dev_free(ex);
     return true;
+}
+
+void set_plain_wait_limit(uint64_t ns)
+{
+    cudaMemcpyToSymbol(sm100::g_wait_limit_ns, &ns, sizeof(ns));
 }
 
 void launch_scale_matrix_c(int64_t m, int64_t n, cdd_host beta, int beta_kind, void *C, int64_t ldc, int uplo,
@@ -679,3 +952,8 @@ bool gemm_plain_cplx(const GemmArgs &g, const char *routine)
 }
 
 }  // namespace mw
+
+extern "C" int mwblas_set_plain_tma(int on)
+{
+    return mw::g_plain_tma.exchange(on ? 1 : 0);
+}

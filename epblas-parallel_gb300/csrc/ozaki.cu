@@ -1383,19 +1383,10 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
 // ---- host ---------------------------------------------------------------------------------
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-std::once_flag g_encode_once;
 
 bool get_encode()
 {
-    std::call_once(g_encode_once, [] {
-        cudaDriverEntryPointQueryResult q;
-        void *fn = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-        cudaGetLastError();
-    });
+    if (!g_encode) g_encode = (PFN_cuTensorMapEncodeTiled_v12000)tensor_map_encoder();
     return g_encode != nullptr;
 }
 
@@ -1911,6 +1902,7 @@ extern "C" uint64_t mwblas_set_wait_limit_ns(uint64_t ns)
     const uint64_t v = ns == 0 ? sm100::kWaitLimitNs : (ns < 1000000ull ? 1000000ull : ns);
     mw::clear_error();
     const cudaError_t st = cudaMemcpyToSymbol(sm100::g_wait_limit_ns, &v, sizeof(v));
+    if (st == cudaSuccess) mw::set_plain_wait_limit(v);
     if (st != cudaSuccess) {
         mw::cuda_ok(st, "mwblas_set_wait_limit_ns", "cudaMemcpyToSymbol");
         return current.load();

@@ -182,6 +182,21 @@ bool is_aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
 bool is_dd_device_pointer(const void *p) { return is_aligned16(p) && is_device_pointer(p); }
 
+void *tensor_map_encoder()
+{
+    static void *fn = [] {
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        cudaGetLastError();
+        return f;
+    }();
+    return fn;
+}
+
 bool stage_matrix(Staged &s, const void *host, int64_t rows, int64_t cols, int64_t ld, size_t elem,
                   bool copy_in, const char *routine)
 {

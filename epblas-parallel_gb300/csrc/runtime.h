@@ -57,6 +57,11 @@ bool is_aligned16(const void *p);
 // elements that the kernels may read in place with 16-byte loads.
 bool is_dd_device_pointer(const void *p);
 
+// The driver's cuTensorMapEncodeTiled (looked up once through the runtime's
+// entry-point query; null when unavailable), as an untyped pointer so that
+// this header needs no driver types.
+void *tensor_map_encoder();
+
 // A device view of a caller array. If the caller's pointer is already device
 // memory it is used in place; otherwise a scratch copy is made.
 struct Staged {

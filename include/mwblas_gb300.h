@@ -520,6 +520,11 @@ int mwblas_last_ozaki_bits(int operand);
  * previous value. */
 int mwblas_set_ozaki_mma(int kind);
 
+/* Operand staging of the FP64 error-free-transform engine: 1 (default) =
+ * TMA tensor copies into a ring of shared-memory stages, 0 = plain loads.
+ * Both give identical results. Returns the previous value. */
+int mwblas_set_plain_tma(int on);
+
 /* Per-phase device timing of the Ozaki engine (CUDA events on the library
  * stream; off by default). Phases: 0 exponent scan, 1 residue conversion,
  * 2 residue GEMMs (tensor cores), 3 CRT reconstruction. mwblas_last_phase_ms

@@ -305,3 +305,56 @@ def test_golden_reference_outputs(gpu, golden):
             opn = orc.dd_abs(z[k + "_alpha"]) * orc.dd_absmax(z[k + "_B"][:, :c["m"]])
             tol = max(20, 8 * na * na) * orc.EPS_DD
             assert orc.normwise_error(got[:, :c["m"]], z[k + "_q"][:, :c["m"]], opn) <= tol, k
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
+def test_plain_engine_tma_staging_bit_identical(gpu, oracle, rng, ta, tb):
+    """The FP64 engine's TMA-staged kernel (tensor copies into a ring of
+    shared-memory stages, zero fill past the operand edges) gives the bits of
+    the kernel that stages with plain loads: ragged m, n, k, padded leading
+    dimensions, both tile sizes, short k (second extraction level)."""
+    for (m, n, k) in [(1, 1, 1), (70, 33, 9), (130, 97, 64), (333, 301, 517), (1200, 700, 130)]:
+        lda = (m if ta == "N" else k) + 3
+        ldb = (k if tb == "N" else n) + 1
+        A = mwb.dd_matrix(rng, m if ta == "N" else k, k if ta == "N" else m, lda)
+        B = mwb.dd_matrix(rng, k if tb == "N" else n, n if tb == "N" else k, ldb)
+        C0 = mwb.dd_matrix(rng, m, n, m + 2, fill=SENT)
+        al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+        outs = []
+        for tma in (1, 0):
+            prev = gpu.lib.mwblas_set_plain_tma(tma)
+            try:
+                c = C0.copy()
+                gpu.mgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, c, m + 2, engine="plain")
+                assert gpu.last_error()[0] == 0, gpu.last_error()
+                outs.append(c)
+            finally:
+                gpu.lib.mwblas_set_plain_tma(prev)
+        np.testing.assert_array_equal(outs[0], outs[1])
+        check_sentinel(outs[0], m)
+        want = oracle.qgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0.copy(), m + 2)
+        err = orc.normwise_error(outs[0][:, :m], want[:, :m], op_norm(al, k, A, B, be, C0[:, :m]))
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (m, n, k, err)
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+def test_plain_engine_tma_syrk_bit_identical(gpu, rng, uplo):
+    n, k = 400, 300
+    A = mwb.dd_matrix(rng, n, k)
+    C0 = mwb.dd_matrix(rng, n, n)
+    al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+    outs = []
+    prev_e = gpu.lib.mwblas_set_gemm_engine(1)
+    try:
+        for tma in (1, 0):
+            prev = gpu.lib.mwblas_set_plain_tma(tma)
+            try:
+                c = C0.copy()
+                gpu.msyrk(uplo, "N", n, k, al, A, n, be, c, n)
+                assert gpu.last_error()[0] == 0
+                outs.append(c)
+            finally:
+                gpu.lib.mwblas_set_plain_tma(prev)
+    finally:
+        gpu.lib.mwblas_set_gemm_engine(prev_e)
+    np.testing.assert_array_equal(outs[0], outs[1])

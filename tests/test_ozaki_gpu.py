@@ -310,6 +310,18 @@ def _dev(torch, a):
     return torch.from_numpy(a).cuda()
 
 
+def _same_but_last_rounding(a, b):
+    """Equal up to the final rounding to double-double: the CRT fraction is
+    accurate to ~2^-145 of the moduli product, which differs between two
+    moduli sets, so an exact value next to a rounding boundary may round
+    either way (a few outputs in a million, one unit of the lo limb)."""
+    fin = np.isfinite(b[..., 0])
+    assert np.array_equal(np.isfinite(a[..., 0]), fin)
+    diff = orc.dd_diff_abs(a, b)[fin]
+    assert np.all(diff <= 2.0 ** -104 * np.abs(b[..., 0][fin])), float(np.max(diff))
+    assert np.mean(np.all(a == b, axis=-1)) > 0.999
+
+
 def _ozaki_dev(gpu, torch, ta, tb, m, n, k, al, dA, lda, dB, ldb, be, C0, bits=0):
     """One tensor-core GEMM on device arrays at a given bits setting; returns
     the output, the moduli count and the bits of op(A), op(B)."""
@@ -329,7 +341,8 @@ def _ozaki_dev(gpu, torch, ta, tb, m, n, k, al, dA, lda, dB, ldb, be, C0, bits=0
 def test_fp64_inputs_take_fewer_moduli_with_identical_results(gpu, oracle, rng, ta, tb):
     """lo = 0 operands are exact integers at about 60-70 bits after the row /
     column scaling, so the automatic width cuts the moduli count; the exact
-    integer product, hence the rounded result, is the same as at 106 bits."""
+    integer product is the same as at 106 bits, and so is the result up to
+    its final rounding."""
     import torch
     m, n, k = 512, 640, 1024
     A = _lo0(rng, m if ta == "N" else k, k if ta == "N" else m)
@@ -343,7 +356,7 @@ def test_fp64_inputs_take_fewer_moduli_with_identical_results(gpu, oracle, rng, 
     assert bw_full == (106, 106)
     assert 50 <= ba < 106 and 50 <= bb < 106, (ba, bb)
     assert md_auto <= md_full - 7, (md_auto, md_full)
-    np.testing.assert_array_equal(auto, full)
+    _same_but_last_rounding(auto, full)
     want = oracle.qgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0.copy(), m)
     err = orc.normwise_error(auto, want, op_norm(al, k, A, B, be, C0))
     assert err <= max(10, 4 * k) * orc.EPS_DD, err
@@ -382,7 +395,7 @@ def test_small_integer_inputs_use_few_moduli_and_are_exact(gpu, rng):
 def test_width_ignores_nonfinite_and_zero_rows(gpu, rng):
     """A row of op(A) holding an Inf (its outputs become NaN) and an all-zero
     row do not widen the operand; the other outputs equal the full-width
-    ones. One entry far below the rest of its row does widen it (to the full
+    ones up to the final rounding. One entry far below the rest of its row does widen it (to the full
     106 bits, as exactness would need ~950)."""
     import torch
     m, n, k = 512, 512, 600
@@ -397,7 +410,7 @@ def test_width_ignores_nonfinite_and_zero_rows(gpu, rng):
     full, md_full, _ = _ozaki_dev(gpu, torch, "N", "N", m, n, k, one, dA, m, dB, k, zero, C0, 106)
     assert ba < 106 and md_auto < md_full
     assert np.all(np.isnan(auto[:, 9, 0])) and np.all(np.isnan(full[:, 9, 0]))
-    np.testing.assert_array_equal(np.delete(auto, 9, axis=1), np.delete(full, 9, axis=1))
+    _same_but_last_rounding(np.delete(auto, 9, axis=1), np.delete(full, 9, axis=1))
     assert np.all(auto[:, 5] == 0)
     A[3, 11, 0] = 2.0 ** -900                    # row 11: one entry far below the others
     dA = _dev(torch, A)
@@ -427,7 +440,7 @@ def test_fp64_inputs_complex_and_syrk(gpu, oracle, rng):
             gpu.lib.mwblas_set_ozaki_bits(prev)
             gpu.lib.mwblas_set_gemm_engine(prev_e)
     assert got[0][1] < got[1][1]
-    np.testing.assert_array_equal(got[0][0], got[1][0])
+    _same_but_last_rounding(got[0][0], got[1][0])
     # complex, conjugate-transposed B
     m, n, k = 512, 512, 520
     Ac = mwb.dd_matrix(rng, m, k, cplx_=True); Ac[..., 1] = 0.0
@@ -448,7 +461,7 @@ def test_fp64_inputs_complex_and_syrk(gpu, oracle, rng):
             gpu.lib.mwblas_set_ozaki_bits(prev)
             gpu.lib.mwblas_set_gemm_engine(prev_e)
     assert outs[0][1] < outs[1][1]
-    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    _same_but_last_rounding(outs[0][0], outs[1][0])
     want = oracle.qwgemm("N", "C", m, n, k, cal, Ac, m, Bc, n, cbe, Cc.copy(), m)
     op = orc.dd_abs(cal) * k * orc.dd_absmax(Ac) * orc.dd_absmax(Bc) + orc.dd_abs(cbe) * orc.dd_absmax(Cc)
     assert orc.normwise_error(outs[0][0], want, op) <= max(10, 4 * k) * orc.EPS_DD
