@@ -174,6 +174,7 @@ void gemm_entry(const char *routine, bool cplx, int force_engine, const char *tr
     if (!c) { set_error(routine, 12, "null C"); return; }
 
     GemmArgs g;
+    g.width = true;
     g.m = M; g.n = N; g.k = K;
     g.ta = TA != 'N'; g.tb = TB != 'N';
     g.ca = TA == 'C'; g.cb = TB == 'C';
@@ -341,6 +342,7 @@ void syrk_entry(const char *routine, bool herm, const char *uplo, const char *tr
     } else {
         if (!stage_matrix(SA, a, nrowa, T == 'N' ? K : N, *lda, es, true, routine)) return;
         GemmArgs g;
+        g.width = true;
         g.alpha = al;
         g.beta = be;
         g.calpha = cdd_host{al, {0.0, 0.0}};
@@ -639,7 +641,8 @@ void gemmtr_entry(const char *routine, bool cplx, const char *uplo, const char *
     Staged SA, SB, SC;
     sc.add(SA); sc.add(SB); sc.add(SC);
     if (!stage_matrix(SC, c, N, N, *ldc, es, true, routine)) return;   // the other triangle is written back as read
-    const GemmArgs g = scalars(cplx, alpha, beta);
+    GemmArgs g = scalars(cplx, alpha, beta);
+    g.width = true;
     if (!compute) {
         if (cplx) launch_scale_matrix_c(N, N, g.cbeta, g.beta_kind, SC.dev, *ldc, ul);
         else launch_scale_matrix(N, N, g.beta, g.beta_kind, SC.dev, *ldc, ul);
@@ -684,6 +687,7 @@ void symm_entry(const char *routine, bool cplx, bool herm, const char *side, con
     if (!ensure_device(routine)) return;
     const size_t es = cplx ? 32 : 16;
     GemmArgs g = scalars(cplx, alpha, beta);
+    g.width = true;
     Staged SA, SB, SC;
     sc.add(SA); sc.add(SB); sc.add(SC);
     if (!stage_matrix(SC, c, M, N, *ldc, es, g.beta_kind != 0, routine)) return;
@@ -728,6 +732,7 @@ void syr2k_entry(const char *routine, bool cplx, bool herm, const char *uplo, co
     if (!c) { set_error(routine, 11, "null C"); return; }
     // scalars: HER2K has a complex alpha and a real beta
     GemmArgs g;
+    g.width = true;
     if (cplx) {
         g.calpha = cd((const mwblas_complex64x2 *)alpha);
         g.cbeta = herm ? cdd_host{rd((const mwblas_real64x2 *)beta), {0.0, 0.0}} : cd((const mwblas_complex64x2 *)beta);
@@ -785,6 +790,7 @@ void csyrk_entry(const char *routine, const char *uplo, const char *trans, const
     if (*ldc < (N > 1 ? N : 1)) { set_error(routine, 10, "ldc too small"); return; }
     if (!c) { set_error(routine, 9, "null C"); return; }
     GemmArgs g = scalars(true, alpha, beta);
+    g.width = true;
     const bool compute = !(ceq0(g.calpha) || K == 0);
     if (!compute && g.beta_kind == 1) return;   // wsyrk_parallel.cpp:57-58
     if (compute && !a) { set_error(routine, 6, "null A"); return; }

@@ -25,6 +25,11 @@ struct GemmArgs {
     int uplo = 0;                  // output triangle: 0 full, 1 upper (i <= j), 2 lower (i >= j)
     bool herm = false;             // complex: force a real diagonal (HERK)
     HostStage *hs = nullptr;       // operands still being uploaded (Ozaki engine only)
+    // The tensor-core engine may size its moduli from the operands' significant
+    // width (one readback of two integers). Set by the entry points whose
+    // product is the whole call (GEMM, the rank-k family, GEMMTR, SYMM), not by
+    // the blocked solvers, whose many internal products would each pay it.
+    bool width = false;
 };
 
 // Plain FP64 error-free-transform engine.

@@ -1481,8 +1481,9 @@ __global__ void k_width(int64_t rows, const int *__restrict__ e, const int *__re
 
 // Products at least this large (m n k) on device-resident operands size their
 // moduli from the operands' significant width; the readback of the two widths
-// costs one stream synchronisation (~20 us).
-constexpr double kWidthMinWork = 512.0 * 512.0 * 512.0;
+// costs one stream synchronisation (the GPU idles ~10-20 us meanwhile, about
+// 1 % of a 1024^3 product).
+constexpr double kWidthMinWork = 1024.0 * 1024.0 * 1024.0;
 
 // The significant widths of op(A)'s rows and op(B)'s columns, read back to the
 // host; false when they could not be (the caller then keeps the full width).
@@ -1568,7 +1569,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         cudaGetLastError();
         cap = cudaStreamCaptureStatusActive;
     }
-    const bool detect = bits_req <= 0 && !g.hs && cap == cudaStreamCaptureStatusNone &&
+    const bool detect = bits_req <= 0 && g.width && !g.hs && cap == cudaStreamCaptureStatusNone &&
                         (double)m * (double)n * (double)k >= kWidthMinWork;
     int *ex = (int *)dev_alloc(sizeof(int) * (size_t)(detect ? 2 * (m + n) + 4 : m + n + 2), routine);
     if (!ex) return false;

@@ -497,11 +497,12 @@ int mtrsm_grouped(int64_t count, char side, char uplo, char transa, char diag, c
  * entry of op(A) (or op(B)) is an exact integer at fewer bits after its
  * row's (column's) power-of-two scaling -- FP64 values with lo = 0 over a
  * limited exponent range, for instance; the result is then unchanged in
- * accuracy and computed with fewer moduli.  The width is measured on
- * device-resident operands of products with m*n*k >= 512^3 and costs one
- * stream synchronisation after the exponent scan; it is skipped while the
- * library's stream is being captured and for host arrays that are uploaded
- * block by block.  The number of moduli (integer GEMMs) follows from the two
+ * accuracy and computed with fewer moduli.  The width is measured for the
+ * products of GEMM, the rank-k family (SYRK/HERK/SYR2K/HER2K), GEMMTR and
+ * SYMM/HEMM with m*n*k >= 1024^3, and costs one stream synchronisation
+ * after the exponent scan; it is skipped while the library's stream is being
+ * captured, for host arrays that are uploaded block by block, and inside the
+ * blocked solvers.  The number of moduli (integer GEMMs) follows from the two
  * widths and k.  Returns the previous value. */
 int mwblas_set_ozaki_bits(int bits);
 /* Moduli count used by the most recent Ozaki GEMM (process-wide). */
