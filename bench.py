@@ -244,11 +244,25 @@ def run_ours(args, rank, world, local_rank):
         p1.record(stream)
         barrier()
         pms = p0.elapsed_time(p1)
-        # plain kernel: 6 FP64 instructions per DD multiply-add + 12 per 8-step fold
-        fp64_inst = n * n * n * (6.0 + 12.0 / 8.0)
+        # FP64 lane operations per DD multiply-add and FP64-pipe activity, from the
+        # ncu capture of the same kernel (sm__inst_executed_pipe_fp64 x 32 / MACs)
+        prof = plain_profile()
+        fp64_inst = n * n * n * prof.get("fp64_inst_per_mac", 7.5)
         plain = {"value": flops / (pms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pms,
-                 "fp64_inst_per_s": fp64_inst / (pms * 1e-3),
-                 "note": "FP64 pipe issue-bound; the probe measured 1.58 DFMA/clk/SM on this GPU"}
+                 "kernel": "k_gemm_plain_tma (TMA-staged tiles, FP64 error-free transforms)",
+                 "fp64_inst_per_s": fp64_inst / (pms * 1e-3), "fp64_inst_per_mac": prof.get("fp64_inst_per_mac"),
+                 "fp64_pipe_active_pct_ncu": prof.get("fp64_pipe_active_pct"),
+                 "profile": "profiles/k_gemm_plain_tma_2048_ncu.txt"}
+        if rank == 0 and world == 1 and not args.skip_check:
+            # its own error on 256 sampled entries, from the same C0 as the checked Ozaki step
+            pc = torch.from_numpy(C0).to(dev)
+            lib.mgemm("N", "N", n, n, n, alpha, dA.data_ptr(), n, dB.data_ptr(), n, beta, pc.data_ptr(), n,
+                      engine="plain")
+            torch.cuda.synchronize()
+            plain_rows, plain_cols = np.random.default_rng(98).integers(0, n, 256), np.random.default_rng(97).integers(0, n, 256)
+            plain["_check"] = (plain_rows, plain_cols, pc[torch.from_numpy(plain_cols).to(dev),
+                                                        torch.from_numpy(plain_rows).to(dev)].cpu().numpy())
+            del pc
 
     res = dict(value=value, ms=ms, launches=launches, moduli=moduli, phase_ms=phase.tolist(), e2e=e2e,
                e2e_pageable=e2e_pageable, plain=plain, clocks=clk.summary(),
@@ -277,6 +291,13 @@ def cpu_baseline_leg(n, res):
             + orc.dd_abs(res["beta"]) * orc.dd_absmax(res["C0"])
         out["normwise_err_sampled"] = orc.normwise_error(got, want, op)
         out["err_samples"] = 256
+        pl = res.get("plain") or {}
+        if "_check" in pl:
+            prow, pcol, pgot = pl.pop("_check")
+            pwant = o.qgemm("N", "N", n, n, n, res["alpha"], res["A"], n, res["B"], n, res["beta"], res["C0"], n,
+                            rows=prow, cols=pcol)
+            pl["normwise_err_vs_binary128"] = orc.normwise_error(pgot, pwant, op)
+            pl["err_samples"] = 256
     # CPU timing on a bounded sample of the same workload
     t = time_reference_cpu(sample=(4096, 4096, 256), reps=1)
     out["cpu"] = t
@@ -447,6 +468,18 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def plain_profile():
+    """fp64_inst_per_mac / fp64_pipe_active_pct lines of the FP64 kernel's ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_gemm_plain_tma_2048_ncu.txt")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            for key in ("fp64_inst_per_mac", "fp64_pipe_active_pct"):
+                if line.startswith(key + ":"):
+                    out[key] = float(line.split(":")[1].strip())
+    return out
 
 
 def tc_traffic_from_profile():
