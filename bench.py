@@ -1078,6 +1078,7 @@ def run_workload(args):
             value, unit = float(np.sum(2.0 * m_ * n_ * k_)) / ms / 1e6, "DD-GFLOP/s"
             metric = "batched DD-GEMM GFLOP/s, 20000 instances M,N,K log-uniform [8,512]"
             cfg = {"workload": "mgemm_grouped 20000 x NN, M,N,K ~ logU[8,512]", "split_k_min_chosen": chosen,
+                   "tile_chosen": int(lib.lib.mwblas_grouped_tuned_tile()),
                    "launch": "one persistent kernel from a cached CUDA graph"}
             if o:
                 arena.copy_(C0)
@@ -1115,7 +1116,9 @@ def run_workload(args):
             ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: arena.copy_(B0))
             value, unit = float(np.sum(m_.astype(np.float64) ** 2 * n_)) / ms / 1e6, "DD-GFLOP/s"
             metric = "batched DD-TRSM GFLOP/s, 5000 LLNN systems n logU[16,256], nrhs U[1,64]"
-            cfg = {"workload": "mtrsm_grouped 5000 x L L N N", "launch": "one kernel, warp per 32 right-hand sides"}
+            cfg = {"workload": "mtrsm_grouped 5000 x L L N N",
+                   "launch": "one persistent kernel from a cached CUDA graph, warps pull (instance, 32 right-hand "
+                             "sides) items longest first"}
             if o:
                 arena.copy_(B0)
                 fn()

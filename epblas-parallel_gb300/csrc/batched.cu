@@ -23,10 +23,14 @@
 // and caches the winner for batches of the same shape class.
 //
 // mtrsm_grouped: one persistent kernel; a work item is (instance, 32 right-hand
-// sides); a warp solves them by substitution in double-double, one lane per
-// right-hand side, using the double-double reciprocal of the diagonal as the
-// reference does (mtrsm_serial.cpp:144).
+// sides), pulled by a warp from an atomic counter (longest triangles first);
+// the warp solves them by substitution, one lane per right-hand side, each
+// row's sum exact in fixed point, using the double-double reciprocal of the
+// diagonal as the reference does (mtrsm_serial.cpp:144). Descriptors and
+// scratch are kept per batch layout and the launch is replayed from a CUDA
+// graph, as for the grouped GEMM.
 #include <algorithm>
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -41,8 +45,7 @@ namespace mw {
 namespace {
 
 constexpr int kNoExp = -30000;
-constexpr int GT = 32;         // output tile edge
-constexpr int GTHREADS = 256;  // 16 x 16 threads, 2 x 2 outputs each
+constexpr int GTHREADS = 256;  // 16 x 16 threads
 constexpr int GBK = 8;         // k-slab
 
 struct GemmDesc {
@@ -76,16 +79,36 @@ __device__ __forceinline__ double2 opB_at(const GemmDesc &d, int64_t p, int64_t 
     return d.tb ? d.B[j + p * d.ldb] : d.B[p + j * d.ldb];
 }
 
+// R consecutive digits of a staged row (R = 1, 2 or 4 ints, one vector load).
+template <int R>
+__device__ __forceinline__ void load_digits(const int *src, int (&dst)[R])
+{
+    if constexpr (R == 4) {
+        const int4 v = *reinterpret_cast<const int4 *>(src);
+        dst[0] = v.x; dst[1] = v.y; dst[2] = v.z; dst[3] = v.w;
+    } else if constexpr (R == 2) {
+        const int2 v = *reinterpret_cast<const int2 *>(src);
+        dst[0] = v.x; dst[1] = v.y;
+    } else {
+        dst[0] = *src;
+    }
+}
+
+// GT x GT output tiles (GT = 16, 32 or 64; chosen per batch by the tuner),
+// 256 threads as 16 x 16, each with R x R outputs (R = GT / 16): rows R tx ..,
+// columns R ty ...
+template <int GT>
 __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__restrict__ descs, int count,
                                                           int64_t total, unsigned long long *work_counter,
                                                           int *tile_counters, fx::XFPod *partials)
 {
+    constexpr int R = GT / 16;
     __shared__ __align__(16) int sA[GBK][5][GT], sB[GBK][5][GT];
     __shared__ int s_ea[GT], s_eb[GT];
     __shared__ long long s_item;
     __shared__ int s_last;
     const int tid = threadIdx.x;
-    const int tx = tid & 15, ty = tid >> 4;   // rows 2tx, 2tx+1; columns 2ty, 2ty+1
+    const int tx = tid & 15, ty = tid >> 4;
     for (;;) {
         if (tid == 0) s_item = (long long)atomicAdd(work_counter, 1ull);
         __syncthreads();
@@ -123,20 +146,17 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__res
         }
         __syncthreads();
 
-        long long acc[2][2][5];
+        long long acc[R][R][5];
 #pragma unroll
-        for (int a = 0; a < 2; ++a)
+        for (int a = 0; a < R; ++a)
 #pragma unroll
-            for (int b = 0; b < 2; ++b)
+            for (int b = 0; b < R; ++b)
 #pragma unroll
                 for (int q = 0; q < 5; ++q) acc[a][b][q] = 0;
 
         for (int64_t kk = k0; kk < k1; kk += GBK) {
-            // stage one element of the A tile and one of the B tile per thread
-            // as digits (GT * GBK == GTHREADS)
-            static_assert(GT * GBK == GTHREADS, "one staged element per thread");
-            {
-                const int idx = tid;
+            // stage the A and B tiles (GT x GBK elements each) as digits
+            for (int idx = tid; idx < GT * GBK; idx += GTHREADS) {
                 int dg[5];
                 {
                     int r, p;
@@ -164,30 +184,34 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__res
             __syncthreads();
 #pragma unroll 2
             for (int p = 0; p < GBK; ++p) {
-                int da[2][5], db[2][5];
+                int da[R][5], db[R][5];
 #pragma unroll
                 for (int t = 0; t < 5; ++t) {
-                    const int2 va = *reinterpret_cast<const int2 *>(&sA[p][t][2 * tx]);
-                    const int2 vb = *reinterpret_cast<const int2 *>(&sB[p][t][2 * ty]);
-                    da[0][t] = va.x; da[1][t] = va.y;
-                    db[0][t] = vb.x; db[1][t] = vb.y;
+                    int va[R], vb[R];
+                    load_digits<R>(&sA[p][t][R * tx], va);
+                    load_digits<R>(&sB[p][t][R * ty], vb);
+#pragma unroll
+                    for (int u = 0; u < R; ++u) {
+                        da[u][t] = va[u];
+                        db[u][t] = vb[u];
+                    }
                 }
 #pragma unroll
-                for (int a = 0; a < 2; ++a)
+                for (int a = 0; a < R; ++a)
 #pragma unroll
-                    for (int b = 0; b < 2; ++b) fxg::mac_digits(acc[a][b], da[a], db[b]);
+                    for (int b = 0; b < R; ++b) fxg::mac_digits(acc[a][b], da[a], db[b]);
             }
             __syncthreads();
         }
 
-        // the 2 x 2 outputs as extended floats (non-finite rows/columns flagged)
-        xfp::XF v[2][2];
-        bool badv[2][2];
+        // the R x R outputs as extended floats (non-finite rows/columns flagged)
+        xfp::XF v[R][R];
+        bool badv[R][R];
 #pragma unroll
-        for (int a = 0; a < 2; ++a)
+        for (int a = 0; a < R; ++a)
 #pragma unroll
-            for (int b = 0; b < 2; ++b) {
-                const int ei = s_ea[2 * tx + a], ej = s_eb[2 * ty + b];
+            for (int b = 0; b < R; ++b) {
+                const int ei = s_ea[R * tx + a], ej = s_eb[R * ty + b];
                 badv[a][b] = ei >= 1024 || ej >= 1024;
                 if (badv[a][b] || ei <= kNoExp / 2 || ej <= kNoExp / 2) {
                     v[a][b].zero = true; v[a][b].neg = false; v[a][b].m = 0; v[a][b].e = 0;
@@ -200,9 +224,9 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__res
             // write this split's partial tile, then let the last split finish
             fx::XFPod *pt = partials + (d.part_begin + tile * d.splitk + split) * (GT * GT);
 #pragma unroll
-            for (int a = 0; a < 2; ++a)
+            for (int a = 0; a < R; ++a)
 #pragma unroll
-                for (int b = 0; b < 2; ++b) pt[(2 * ty + b) * GT + 2 * tx + a] = fx::to_pod(v[a][b], badv[a][b]);
+                for (int b = 0; b < R; ++b) pt[(R * ty + b) * GT + R * tx + a] = fx::to_pod(v[a][b], badv[a][b]);
             __threadfence();
             __syncthreads();
             if (tid == 0) {
@@ -214,15 +238,15 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__res
             __threadfence();
             const fx::XFPod *base = partials + (d.part_begin + tile * d.splitk) * (GT * GT);
 #pragma unroll
-            for (int a = 0; a < 2; ++a)
+            for (int a = 0; a < R; ++a)
 #pragma unroll
-                for (int b = 0; b < 2; ++b) {
+                for (int b = 0; b < R; ++b) {
                     xfp::XF sum;
                     sum.zero = true; sum.neg = false; sum.m = 0; sum.e = 0;
                     bool bad = false;
                     for (int s2 = 0; s2 < d.splitk; ++s2) {
                         // partials written by other CTAs: read through L2
-                        const fx::XFPod *q = base + (int64_t)s2 * GT * GT + (2 * ty + b) * GT + 2 * tx + a;
+                        const fx::XFPod *q = base + (int64_t)s2 * GT * GT + (R * ty + b) * GT + R * tx + a;
                         fx::XFPod pv;
                         pv.hi = __ldcg(&q->hi);
                         pv.lo = __ldcg(&q->lo);
@@ -240,12 +264,12 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_grouped(const GemmDesc *__res
         const xfp::XF xa = xfp::xf_from_dd(d.alpha.x, d.alpha.y), xb = xfp::xf_from_dd(d.beta.x, d.beta.y);
         const bool alpha_one = d.alpha.x == 1.0 && d.alpha.y == 0.0;
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            const int64_t j = j0 + 2 * ty + b;
+        for (int b = 0; b < R; ++b) {
+            const int64_t j = j0 + R * ty + b;
             if (j >= d.n) continue;
 #pragma unroll
-            for (int a = 0; a < 2; ++a) {
-                const int64_t i = i0 + 2 * tx + a;
+            for (int a = 0; a < R; ++a) {
+                const int64_t i = i0 + R * tx + a;
                 if (i >= d.m) continue;
                 double2 *pc = d.C + i + j * d.ldc;
                 if (badv[a][b]) {
@@ -287,24 +311,11 @@ __device__ __forceinline__ dd::real dd_recip(dd::real b)
     return dd::add_exact(q, dd::make(q3, 0.0));
 }
 
-// side: 0 left, 1 right; lower: op(A) lower triangular; trans: op = A^T.
-// Warp per (instance, 32 right-hand sides), lane per right-hand side. The
-// reciprocals of the diagonal are computed 32 rows at a time, one row per
-// lane, and broadcast with shuffles; each row's sum alpha*b - sum_p A x is
-// accumulated exactly in fixed point (fixacc.cuh) and rounded once before the
-// multiplication by the reciprocal. All lanes stay in the loop (lanes past
-// the last right-hand side do the work on a clamped column and store
-// nothing) so that the shuffles see the whole warp.
-__global__ void __launch_bounds__(128, 4) k_trsm_grouped(const TrsmDesc *__restrict__ descs, int count, int64_t total,
-                                                     int side, int lower, int trans, int unit, fx::Op *xops)
+// One work item of the grouped TRSM: instance descs[*] (found by binary
+// search on work_begin), right-hand sides [32 chunk, 32 chunk + 32).
+__device__ __forceinline__ void trsm_item(const TrsmDesc *__restrict__ descs, int count, int64_t w, int side,
+                                          int lower, int trans, int unit, fx::Op *xops, fx::Dig *arow, int lane)
 {
-    // per warp: a tile of the current row of op(A), split into digits once
-    // for all 32 right-hand sides
-    __shared__ fx::Dig s_arow[4][kTrsmTile];
-    fx::Dig *arow = s_arow[(threadIdx.x >> 5) & 3];
-    const int lane = threadIdx.x & 31;
-    const int64_t w = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-    if (w >= total) return;   // whole warp leaves together
     int lo = 0, hi = count - 1;
     while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
@@ -395,15 +406,47 @@ __global__ void __launch_bounds__(128, 4) k_trsm_grouped(const TrsmDesc *__restr
 #undef OPA
 }
 
+// side: 0 left, 1 right; lower: op(A) lower triangular; trans: op = A^T.
+// Warp per (instance, 32 right-hand sides), lane per right-hand side. The
+// reciprocals of the diagonal are computed 32 rows at a time, one row per
+// lane, and broadcast with shuffles; each row's sum alpha*b - sum_p A x is
+// accumulated exactly in fixed point (fixacc.cuh) and rounded once before the
+// multiplication by the reciprocal. All lanes stay in the loop (lanes past
+// the last right-hand side do the work on a clamped column and store
+// nothing) so that the shuffles see the whole warp.
+// Persistent: every warp pulls work items (instance, 32 right-hand sides) from
+// an atomic counter until none is left; descriptors are sorted longest
+// triangle first, so the long solves start first and the short ones fill the
+// tail.
+__global__ void __launch_bounds__(128, 4) k_trsm_grouped(const TrsmDesc *__restrict__ descs, int count, int64_t total,
+                                                     int side, int lower, int trans, int unit, fx::Op *xops,
+                                                     unsigned long long *work_counter)
+{
+    // per warp: a tile of the current row of op(A), split into digits once
+    // for all 32 right-hand sides
+    __shared__ fx::Dig s_arow[4][kTrsmTile];
+    fx::Dig *arow = s_arow[(threadIdx.x >> 5) & 3];
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned long long wl = 0;
+        if (lane == 0) wl = atomicAdd(work_counter, 1ull);
+        const int64_t w = (int64_t)__shfl_sync(0xffffffffu, wl, 0);
+        if (w >= total) return;   // whole warp leaves together
+        trsm_item(descs, count, w, side, lower, trans, unit, xops, arow, lane);
+    }
+}
+
 // ---- host: plans, graphs, autotuner ----------------------------------------------
 
 struct Policy {
     int min_k_per_split = 0;   // 0: never split
     int max_tiles_split = 4;   // split only instances with at most this many tiles
+    int tile = 32;             // output tile edge: 16, 32 or 64
 };
 
 struct Plan {
     std::vector<GemmDesc> descs;
+    int tile = 32;
     int64_t total = 0, split_tiles = 0, partial_elems = 0;
     // device state
     void *dev = nullptr;
@@ -414,7 +457,9 @@ struct Plan {
 
 std::mutex g_batched_mu;
 std::map<uint64_t, Policy> g_policy_cache;   // shape class -> tuned policy
-Policy g_default_policy{512, 4};
+Policy g_default_policy{512, 4, 32};
+thread_local int t_tuned_tile = 0;   // tile chosen by this thread's most recent tuning
+std::atomic<int> g_forced_tile{0};   // mwblas_set_grouped_tile: 0 = tuned or default
 thread_local Plan t_plan;
 
 uint64_t mix(uint64_t h, uint64_t v)
@@ -448,6 +493,8 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
 {
     pl.descs.clear();
     pl.descs.reserve((size_t)count);
+    const int GT = pol.tile;
+    pl.tile = GT;
     int64_t work = 0, stiles = 0, pslots = 0;
     for (int64_t i = 0; i < count; ++i) {
         if (m[i] <= 0 || n[i] <= 0) continue;
@@ -506,7 +553,7 @@ uint64_t plan_key(const Plan &pl)
     const uint64_t *p = (const uint64_t *)pl.descs.data();
     const size_t nw = pl.descs.size() * sizeof(GemmDesc) / 8;
     for (size_t i = 0; i < nw; ++i) h = (h ^ p[i]) * 1099511628211ull;
-    return h;
+    return mix(h, (uint64_t)pl.tile);
 }
 
 // (Re)creates the device buffers and the graph when the batch layout changed.
@@ -560,8 +607,83 @@ bool prepare_and_launch(Plan &pl, const char *routine)
         if (ok) {
             // counters start at zero on every replay
             cudaMemsetAsync(counter, 0, cnt_bytes, cap);
-            k_gemm_grouped<<<grid, GTHREADS, 0, cap>>>(ddesc, (int)pl.descs.size(), pl.total, counter, tile_counters,
-                                                       partials);
+            auto kern = pl.tile == 64 ? k_gemm_grouped<64> : (pl.tile == 16 ? k_gemm_grouped<16> : k_gemm_grouped<32>);
+            kern<<<grid, GTHREADS, 0, cap>>>(ddesc, (int)pl.descs.size(), pl.total, counter, tile_counters, partials);
+            ok = cuda_ok(cudaStreamEndCapture(cap, &graph), routine, "end capture");
+        }
+        if (ok) {
+            ok = cuda_ok(cudaGraphInstantiate(&pl.exec, graph, 0), routine, "graph instantiate");
+            cudaGraphDestroy(graph);
+        }
+        cudaStreamDestroy(cap);
+        if (!ok) return false;
+        pl.key = key;
+    }
+    count_launch();
+    return cuda_ok(cudaGraphLaunch(pl.exec, s), routine, "graph launch");
+}
+
+// The grouped TRSM's per-thread plan: descriptors, work counter and decoded
+// solutions in one device buffer, kept while the batch layout is unchanged,
+// and a CUDA graph (counter reset + the persistent kernel) replayed per call.
+struct TrsmPlan {
+    std::vector<TrsmDesc> descs;
+    int64_t total = 0, xop_elems = 0;
+    int side = 0, lower = 0, trans = 0, unit = 0;
+    void *dev = nullptr;
+    size_t dev_bytes = 0;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t key = 0;
+};
+thread_local TrsmPlan t_tplan;
+
+bool trsm_prepare_and_launch(TrsmPlan &pl, const char *routine)
+{
+    if (pl.descs.empty() || pl.total == 0) return true;
+    const size_t d_bytes = (pl.descs.size() * sizeof(TrsmDesc) + 255) / 256 * 256;
+    const size_t need = d_bytes + 256 + (size_t)pl.xop_elems * sizeof(fx::Op);
+    static_assert(sizeof(TrsmDesc) % 8 == 0, "descriptor size");
+    uint64_t key = 1469598103934665603ull;
+    const uint64_t *w = (const uint64_t *)pl.descs.data();
+    for (size_t i = 0; i < pl.descs.size() * sizeof(TrsmDesc) / 8; ++i) key = (key ^ w[i]) * 1099511628211ull;
+    key = mix(key, (uint64_t)(pl.side | pl.lower << 1 | pl.trans << 2 | pl.unit << 3));
+    cudaStream_t s = stream();
+    if (pl.dev_bytes < need) {
+        if (pl.exec) {
+            cudaGraphExecDestroy(pl.exec);
+            pl.exec = nullptr;
+        }
+        if (pl.dev) cudaFree(pl.dev);
+        pl.dev = nullptr;
+        pl.dev_bytes = 0;
+        pl.key = 0;
+        if (!cuda_ok(cudaMalloc(&pl.dev, need), routine, "grouped TRSM plan buffer")) return false;
+        pl.dev_bytes = need;
+    }
+    // layout: [descriptors][work counter (256 B)][decoded solutions]
+    TrsmDesc *ddesc = (TrsmDesc *)pl.dev;
+    unsigned long long *counter = (unsigned long long *)((char *)pl.dev + d_bytes);
+    fx::Op *xops = (fx::Op *)((char *)pl.dev + d_bytes + 256);
+    if (pl.key != key) {
+        if (pl.exec) {
+            cudaGraphExecDestroy(pl.exec);
+            pl.exec = nullptr;
+        }
+        if (!cuda_ok(cudaMemcpyAsync(ddesc, pl.descs.data(), pl.descs.size() * sizeof(TrsmDesc),
+                                     cudaMemcpyHostToDevice, s),
+                     routine, "descriptor upload"))
+            return false;
+        // resident blocks: four 4-warp blocks per SM (the kernel's launch bounds)
+        const int warps = 4;
+        const int64_t grid = std::min<int64_t>((pl.total + warps - 1) / warps, (int64_t)device_sm_count() * 4);
+        cudaStream_t cap;
+        if (!cuda_ok(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), routine, "capture stream")) return false;
+        cudaGraph_t graph;
+        bool ok = cuda_ok(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), routine, "begin capture");
+        if (ok) {
+            cudaMemsetAsync(counter, 0, sizeof(unsigned long long), cap);
+            k_trsm_grouped<<<(unsigned)grid, warps * 32, 0, cap>>>(ddesc, (int)pl.descs.size(), pl.total, pl.side,
+                                                                 pl.lower, pl.trans, pl.unit, xops, counter);
             ok = cuda_ok(cudaStreamEndCapture(cap, &graph), routine, "end capture");
         }
         if (ok) {
@@ -651,6 +773,7 @@ extern "C" int mgemm_grouped(int64_t count, const char *transa, const char *tran
         auto it = g_policy_cache.find(shape_class(count, m, n, k));
         if (it != g_policy_cache.end()) pol = it->second;
     }
+    if (g_forced_tile.load() > 0) pol.tile = g_forced_tile.load();
     Plan &pl = t_plan;
     build_descs(pl, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, pol);
     if (!prepare_and_launch(pl, routine)) return mwblas_last_error();
@@ -658,10 +781,11 @@ extern "C" int mgemm_grouped(int64_t count, const char *transa, const char *tran
     return 0;
 }
 
-// Times the split-K policies on the caller's batch (outputs go to scratch
-// copies of C, the caller's C is not modified) and caches the fastest for
-// batches of the same shape class. Returns 0 and the chosen minimum K per
-// split in *chosen (0 = no split).
+// Times tile edges (16, 32, 64) and then split-K policies on the caller's
+// batch (outputs go to scratch copies of C, the caller's C is not modified)
+// and caches the fastest for batches of the same shape class. Returns 0 and
+// the chosen minimum K per split in *chosen (0 = no split); the chosen tile
+// edge is returned by mwblas_grouped_tuned_tile().
 extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char *transb, const int64_t *m,
                                   const int64_t *n, const int64_t *k, const mwblas_real64x2 *alpha,
                                   const mwblas_real64x2 *const *a, const int64_t *lda,
@@ -692,17 +816,17 @@ extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char 
             cudaMemcpyAsync(cs[(size_t)i], c[i], sizeof(double2) * (size_t)(ldc[i] * n[i]), cudaMemcpyDeviceToDevice,
                             stream());
     }
+    // two stages: the tile edge at the default split policy, then the split
+    // policy at that tile
+    const int tiles[] = {16, 32, 64};
     const int cands[] = {0, 2048, 1024, 512, 256, 128};
-    float best = 1e30f;
-    int best_k = 0;
     Plan pl;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (int cand : cands) {
-        Policy pol{cand, 4};
+    auto time_policy = [&](const Policy &pol) -> float {
         build_descs(pl, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, cs.data(), ldc, pol);
-        if (!prepare_and_launch(pl, routine)) break;   // warm + capture
+        if (!prepare_and_launch(pl, routine)) return 1e30f;   // warm + capture
         cudaEventRecord(e0, stream());
         const int reps = 3;
         for (int r = 0; r < reps; ++r) prepare_and_launch(pl, routine);
@@ -710,6 +834,20 @@ extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char 
         cudaEventSynchronize(e1);
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
+        return ms;
+    };
+    float best = 1e30f;
+    int best_tile = g_default_policy.tile, best_k = g_default_policy.min_k_per_split;
+    for (int t : tiles) {
+        const float ms = time_policy(Policy{g_default_policy.min_k_per_split, 4, t});
+        if (ms < best) {
+            best = ms;
+            best_tile = t;
+        }
+    }
+    for (int cand : cands) {
+        if (cand == g_default_policy.min_k_per_split) continue;   // timed above
+        const float ms = time_policy(Policy{cand, 4, best_tile});
         if (ms < best) {
             best = ms;
             best_k = cand;
@@ -722,8 +860,9 @@ extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char 
     cudaFree(scratch);
     {
         std::lock_guard<std::mutex> lk(g_batched_mu);
-        g_policy_cache[shape_class(count, m, n, k)] = Policy{best_k, 4};
+        g_policy_cache[shape_class(count, m, n, k)] = Policy{best_k, 4, best_tile};
     }
+    t_tuned_tile = best_tile;
     if (chosen) *chosen = best_k;
     return finish(routine) ? 0 : mwblas_last_error();
 }
@@ -788,20 +927,25 @@ extern "C" int mtrsm_grouped(int64_t count, char side, char uplo, char transa, c
         xop_elems += (int64_t)d.nchunks * (S == 'L' ? d.m : d.n) * 32;
     }
     if (!ensure_device(routine)) return mwblas_last_error();
-    const size_t bytes = (descs.size() * sizeof(TrsmDesc) + 255) / 256 * 256;
-    TrsmDesc *dd_ = (TrsmDesc *)dev_alloc(bytes + (size_t)xop_elems * sizeof(fx::Op), routine);
-    if (!dd_) return mwblas_last_error();
-    fx::Op *xops = (fx::Op *)((char *)dd_ + bytes);
-    cudaMemcpyAsync(dd_, descs.data(), descs.size() * sizeof(TrsmDesc), cudaMemcpyHostToDevice, stream());
     const bool trans = (T != 'N');
     const bool lower = ((U == 'L') != trans);
-    const int warps = 4;
-    const int64_t blocks = (work + warps - 1) / warps;
-    k_trsm_grouped<<<(unsigned)blocks, warps * 32, 0, stream()>>>(dd_, (int)descs.size(), work, S == 'L' ? 0 : 1,
-                                                                  lower ? 1 : 0, trans ? 1 : 0, D == 'U' ? 1 : 0,
-                                                                  xops);
-    count_launch();
-    dev_free(dd_);
+    TrsmPlan &pl = t_tplan;
+    pl.descs.swap(descs);
+    pl.total = work;
+    pl.xop_elems = xop_elems;
+    pl.side = S == 'L' ? 0 : 1;
+    pl.lower = lower ? 1 : 0;
+    pl.trans = trans ? 1 : 0;
+    pl.unit = D == 'U' ? 1 : 0;
+    if (!trsm_prepare_and_launch(pl, routine)) return mwblas_last_error();
     if (!finish(routine)) return mwblas_last_error();
     return 0;
+}
+
+extern "C" int mwblas_grouped_tuned_tile(void) { return mw::t_tuned_tile; }
+
+extern "C" int mwblas_set_grouped_tile(int tile)
+{
+    const int t = (tile == 16 || tile == 32 || tile == 64) ? tile : 0;
+    return mw::g_forced_tile.exchange(t);
 }

@@ -477,13 +477,22 @@ int mgemm_grouped(int64_t count, const char *transa, const char *transb, const i
                   const int64_t *k, const MWBLAS_R *alpha, const MWBLAS_R *const *a, const int64_t *lda,
                   const MWBLAS_R *const *b, const int64_t *ldb, const MWBLAS_R *beta, MWBLAS_R *const *c,
                   const int64_t *ldc);
-/* Autotuner for mgemm_grouped: times the split-K policies on this batch
- * (results go to scratch copies; C is not modified) and keeps the fastest for
- * batches of the same shape class. *chosen = minimum K per split (0 = none). */
+/* Autotuner for mgemm_grouped: times the output tile edge (16, 32, 64) and
+ * then the split-K policies on this batch (results go to scratch copies; C is
+ * not modified) and keeps the fastest for batches of the same shape class.
+ * *chosen = minimum K per split (0 = none); the tile edge is returned by
+ * mwblas_grouped_tuned_tile(). */
 int mgemm_grouped_tune(int64_t count, const char *transa, const char *transb, const int64_t *m,
                        const int64_t *n, const int64_t *k, const MWBLAS_R *alpha, const MWBLAS_R *const *a,
                        const int64_t *lda, const MWBLAS_R *const *b, const int64_t *ldb, const MWBLAS_R *beta,
                        MWBLAS_R *const *c, const int64_t *ldc, int *chosen);
+/* Tile edge (16, 32 or 64) chosen by this thread's most recent
+ * mgemm_grouped_tune call (0 before any). No counterpart in the reference. */
+int mwblas_grouped_tuned_tile(void);
+/* Forces mgemm_grouped's tile edge (16, 32 or 64; anything else = 0 = the
+ * tuned or default choice). All give results within the same bound. Returns
+ * the previous setting. */
+int mwblas_set_grouped_tile(int tile);
 /* Batched triangular solves with shared flags and per-instance sizes: for
  * i < count, op(A[i]) X = alpha[i] B[i] (side 'L') or X op(A[i]) = alpha[i] B[i]
  * ('R'); B[i] is overwritten. Device (or managed) matrix pointers. */

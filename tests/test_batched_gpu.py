@@ -116,7 +116,30 @@ def test_grouped_gemm_split_k_and_tuner(gpu, oracle, rng):
     inst = make_batch(rng, 30, maxdim=120, big_k=3000)
     arena, args, chosen = run_grouped(gpu, inst, tune=True)
     assert chosen in (0, 2048, 1024, 512, 256, 128)
+    assert gpu.lib.mwblas_grouped_tuned_tile() in (16, 32, 64)
     check(oracle, inst, arena)
+
+
+@pytest.mark.parametrize("tile", [16, 32, 64])
+def test_grouped_gemm_every_tile_shape(gpu, oracle, rng, tile):
+    """Each tile edge the tuner can choose: ragged instances (tiles cut by m, n),
+    split-K instances (partial tiles of tile^2 extended floats), and a graph
+    replay that gives the same bits."""
+    inst = make_batch(rng, 40, maxdim=150, big_k=2500)
+    prev = gpu.lib.mwblas_set_grouped_tile(tile)
+    try:
+        arena, args, _ = run_grouped(gpu, inst)
+        check(oracle, inst, arena)
+        first = [arena.get(3 * i + 2) for i in range(len(inst))]
+        import torch
+        for i, d in enumerate(inst):
+            o = arena.offsets[3 * i + 2]
+            arena.buf[o:o + d["C"].size] = torch.from_numpy(d["C"].reshape(-1)).cuda()
+        assert gpu.mgemm_grouped(**args) == 0
+        for i in range(len(inst)):
+            np.testing.assert_array_equal(arena.get(3 * i + 2), first[i])
+    finally:
+        gpu.lib.mwblas_set_grouped_tile(prev)
 
 
 @pytest.mark.parametrize("side", ["L", "R"])
@@ -191,3 +214,66 @@ class _Shift:
 
     def get(self, i):
         return self.arena.get(self.base + i)
+
+
+def _trsm_batch(rng, count, side, max_na=120):
+    inst = []
+    for t in range(count):
+        na = int(np.exp(rng.uniform(np.log(2), np.log(max_na))))
+        nrhs = int(rng.integers(1, 70))
+        m, n = (na, nrhs) if side == "L" else (nrhs, na)
+        lda, ldb = na + int(rng.integers(0, 2)), m + int(rng.integers(0, 2))
+        A = mwb.dd_matrix(rng, na, na, lda)
+        A[..., 0] /= na
+        A[..., 1] /= na
+        for d in range(na):
+            A[d, d] = (1.0 + rng.random(), 0.0)
+        B = mwb.dd_matrix(rng, m, n, ldb)
+        inst.append(dict(m=m, n=n, na=na, lda=lda, ldb=ldb, A=A, B=B, alpha=mwb.random_dd(rng, ())))
+    return inst
+
+
+def _trsm_call(gpu, side, inst, arena):
+    return gpu.mtrsm_grouped(side, "L", "N", "N", [d["m"] for d in inst], [d["n"] for d in inst],
+                             [d["alpha"] for d in inst], [arena.ptr(2 * i) for i in range(len(inst))],
+                             [d["lda"] for d in inst], [arena.ptr(2 * i + 1) for i in range(len(inst))],
+                             [d["ldb"] for d in inst])
+
+
+def test_grouped_trsm_graph_replay(gpu, oracle, rng):
+    """The persistent grouped TRSM is captured in a graph per batch layout: a
+    second call on the same layout replays it (same bits), new right-hand
+    sides in the same arrays are solved correctly by the replay, and a
+    different layout is captured anew."""
+    inst = _trsm_batch(rng, 40, "L")
+    arena = DeviceArena([x for d in inst for x in (d["A"], d["B"])])
+    b0 = arena.buf.clone()
+    outs = []
+    for _ in range(2):
+        arena.buf.copy_(b0)
+        assert _trsm_call(gpu, "L", inst, arena) == 0, gpu.last_error()
+        outs.append([arena.get(2 * i + 1) for i in range(len(inst))])
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a, b)
+    # new data, same layout (graph replay)
+    for i, d in enumerate(inst):
+        d["B"] = mwb.dd_matrix(rng, d["m"], d["n"], d["ldb"])
+    arena2 = DeviceArena([x for d in inst for x in (d["A"], d["B"])])
+    arena.buf.copy_(arena2.buf)
+    assert _trsm_call(gpu, "L", inst, arena) == 0, gpu.last_error()
+    for i, d in enumerate(inst):
+        want = d["B"].copy()
+        oracle.qtrsm("L", "L", "N", "N", d["m"], d["n"], d["alpha"], d["A"], d["lda"], want, d["ldb"])
+        err = orc.normwise_error(arena.get(2 * i + 1)[:, :d["m"]], want[:, :d["m"]],
+                                 orc.dd_abs(d["alpha"]) * orc.dd_absmax(d["B"]))
+        assert err <= max(20, 8 * d["na"] ** 2) * orc.EPS_DD, (i, err)
+    # a different layout: fewer instances, longer triangles
+    inst3 = _trsm_batch(rng, 7, "L", max_na=250)
+    arena3 = DeviceArena([x for d in inst3 for x in (d["A"], d["B"])])
+    assert _trsm_call(gpu, "L", inst3, arena3) == 0, gpu.last_error()
+    for i, d in enumerate(inst3):
+        want = d["B"].copy()
+        oracle.qtrsm("L", "L", "N", "N", d["m"], d["n"], d["alpha"], d["A"], d["lda"], want, d["ldb"])
+        err = orc.normwise_error(arena3.get(2 * i + 1)[:, :d["m"]], want[:, :d["m"]],
+                                 orc.dd_abs(d["alpha"]) * orc.dd_absmax(d["B"]))
+        assert err <= max(20, 8 * d["na"] ** 2) * orc.EPS_DD, (i, err)
