@@ -31,6 +31,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <atomic>
 #include <string>
 
@@ -102,15 +103,18 @@ __global__ void k_exp_rows(int64_t rows, int64_t cols, const double2 *M, int64_t
 }
 
 // Column exponent bound: out[j] = max over i of exp_bound(M[i + j*ld].hi)
-// (and low[j] = min of low_bit). Warp per column, lanes stride down the
+// (and low[j] = min of low_bit). Warp per column (or per rows_per-long piece
+// of a column along grid.y, combined with atomics), lanes stride down the
 // contiguous column.
-__global__ void k_exp_cols(int64_t rows, int64_t cols, const double2 *M, int64_t ld, int elem2, int *out, int *low)
+__global__ void k_exp_cols(int64_t rows, int64_t cols, const double2 *M, int64_t ld, int elem2, int *out, int *low,
+                           int64_t rows_per)
 {
     int64_t j = blockIdx.x * (int64_t)(blockDim.x / 32) + threadIdx.x / 32;
     int lane = threadIdx.x & 31;
     if (j >= cols) return;
     int e = kNoExp, lb = kLowNone;
-    for (int64_t i = lane; i < rows; i += 32) {
+    const int64_t i1 = min(rows, (int64_t)(blockIdx.y + 1) * rows_per);
+    for (int64_t i = (int64_t)blockIdx.y * rows_per + lane; i < i1; i += 32) {
         const double2 *p = M + elem2 * (i + j * ld);
         for (int w = 0; w < elem2; ++w) {
             const double2 v = p[w];
@@ -123,8 +127,13 @@ __global__ void k_exp_cols(int64_t rows, int64_t cols, const double2 *M, int64_t
         lb = min(lb, __shfl_down_sync(0xffffffffu, lb, off));
     }
     if (lane == 0) {
-        out[j] = e;
-        if (low) low[j] = lb;
+        if (gridDim.y == 1) {
+            out[j] = e;
+            if (low) low[j] = lb;
+        } else {
+            atomicMax(out + j, e);
+            if (low) atomicMin(low + j, lb);
+        }
     }
 }
 
@@ -856,9 +865,20 @@ void launch_exp_rows_of_op(const void *X, int64_t rows_x, int64_t cols_x, int64_
         if (low) cudaMemsetAsync(low, 0x3f, sizeof(int) * rows_x, stream());   // kLowNone
         k_exp_rows<<<grid, 256, 0, stream()>>>(rows_x, cols_x, (const double2 *)X, ld, elem2, out, per_y, low);
     } else {
-        // rows of X^T = columns of X
-        dim3 grid((unsigned)((cols_x + 7) / 8));
-        k_exp_cols<<<grid, 256, 0, stream()>>>(rows_x, cols_x, (const double2 *)X, ld, elem2, out, low);
+        // rows of X^T = columns of X: a warp per column, long columns cut into
+        // pieces of at least 256 rows when there are too few columns to cover
+        // the GPU a few times
+        const int64_t want = 32 * (int64_t)device_sm_count();
+        int64_t ys = (want + cols_x - 1) / cols_x;
+        ys = std::min<int64_t>(ys, (rows_x + 255) / 256);
+        ys = std::max<int64_t>(1, std::min<int64_t>(ys, 65535));
+        const int64_t rows_per = (rows_x + ys - 1) / ys;
+        if (ys > 1) {
+            cudaMemsetAsync(out, 0x80, sizeof(int) * cols_x, stream());
+            if (low) cudaMemsetAsync(low, 0x3f, sizeof(int) * cols_x, stream());   // kLowNone
+        }
+        dim3 grid((unsigned)((cols_x + 7) / 8), (unsigned)ys);
+        k_exp_cols<<<grid, 256, 0, stream()>>>(rows_x, cols_x, (const double2 *)X, ld, elem2, out, low, rows_per);
     }
     count_launch();
 }
