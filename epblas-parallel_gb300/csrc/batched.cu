@@ -31,6 +31,7 @@
 // graph, as for the grouped GEMM.
 #include <algorithm>
 #include <atomic>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <vector>
@@ -442,10 +443,13 @@ struct Policy {
     int min_k_per_split = 0;   // 0: never split
     int max_tiles_split = 4;   // split only instances with at most this many tiles
     int tile = 32;             // output tile edge: 16, 32 or 64
+    int oz_min = 0;            // instances with m, n >= oz_min and k >= 64 run on the tensor cores (0: none)
 };
 
 struct Plan {
     std::vector<GemmDesc> descs;
+    std::vector<OzGroupItem> oz_items;   // instances routed to the tensor-core engine
+    OzGroupPlan *oz = nullptr;
     int tile = 32;
     int64_t total = 0, split_tiles = 0, partial_elems = 0;
     // device state
@@ -457,9 +461,11 @@ struct Plan {
 
 std::mutex g_batched_mu;
 std::map<uint64_t, Policy> g_policy_cache;   // shape class -> tuned policy
-Policy g_default_policy{512, 4, 32};
+Policy g_default_policy{512, 4, 32, 128};
 thread_local int t_tuned_tile = 0;   // tile chosen by this thread's most recent tuning
+thread_local int t_tuned_oz = -1;    // tensor-core threshold chosen by it (0: none)
 std::atomic<int> g_forced_tile{0};   // mwblas_set_grouped_tile: 0 = tuned or default
+std::atomic<int> g_forced_oz{-1};    // mwblas_set_grouped_tensor_min: -1 = tuned or default
 thread_local Plan t_plan;
 
 uint64_t mix(uint64_t h, uint64_t v)
@@ -493,6 +499,8 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
 {
     pl.descs.clear();
     pl.descs.reserve((size_t)count);
+    pl.oz_items.clear();
+    const int oz_min = (pol.oz_min > 0 && ozaki_available()) ? pol.oz_min : 0;
     const int GT = pol.tile;
     pl.tile = GT;
     int64_t work = 0, stiles = 0, pslots = 0;
@@ -515,6 +523,20 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
         d.beta = make_double2(beta[i].limbs[0], beta[i].limbs[1]);
         const bool alpha0 = (d.alpha.x == 0.0 && d.alpha.y == 0.0);
         d.beta_kind = (d.beta.x == 0.0 && d.beta.y == 0.0) ? 0 : ((d.beta.x == 1.0 && d.beta.y == 0.0) ? 1 : 2);
+        if (oz_min > 0 && !alpha0 && d.m >= oz_min && d.n >= oz_min && d.k >= 64 && d.k <= 16384 && d.m <= 8192 &&
+            d.n <= 8192) {
+            OzGroupItem it;
+            memset(&it, 0, sizeof(it));   // the plan key hashes the bytes, padding included
+            it.A = d.A; it.B = d.B; it.C = d.C;
+            it.lda = d.lda; it.ldb = d.ldb; it.ldc = d.ldc;
+            it.m = d.m; it.n = d.n; it.k = d.k;
+            it.ta = d.ta != 0; it.tb = d.tb != 0;
+            it.alpha = dd_host{d.alpha.x, d.alpha.y};
+            it.beta = dd_host{d.beta.x, d.beta.y};
+            it.beta_kind = d.beta_kind;
+            pl.oz_items.push_back(it);
+            continue;
+        }
         if (alpha0 || d.k == 0) {
             // only the beta pass: run as a k = 0 product (sigma irrelevant)
             d.k = 0;
@@ -553,13 +575,17 @@ uint64_t plan_key(const Plan &pl)
     const uint64_t *p = (const uint64_t *)pl.descs.data();
     const size_t nw = pl.descs.size() * sizeof(GemmDesc) / 8;
     for (size_t i = 0; i < nw; ++i) h = (h ^ p[i]) * 1099511628211ull;
-    return mix(h, (uint64_t)pl.tile);
+    static_assert(sizeof(OzGroupItem) % 8 == 0, "item size");
+    const uint64_t *q = (const uint64_t *)pl.oz_items.data();
+    const size_t nq = pl.oz_items.size() * sizeof(OzGroupItem) / 8;
+    for (size_t i = 0; i < nq; ++i) h = (h ^ q[i]) * 1099511628211ull;
+    return mix(mix(h, (uint64_t)pl.tile), (uint64_t)pl.oz_items.size());
 }
 
 // (Re)creates the device buffers and the graph when the batch layout changed.
 bool prepare_and_launch(Plan &pl, const char *routine)
 {
-    if (pl.descs.empty() || pl.total == 0) return true;
+    if ((pl.descs.empty() || pl.total == 0) && pl.oz_items.empty()) return true;
     const size_t d_bytes = pl.descs.size() * sizeof(GemmDesc);
     const size_t cnt_bytes = 256 + (size_t)(pl.split_tiles + 1) * sizeof(int);
     const size_t part_bytes = (size_t)pl.partial_elems * sizeof(fx::XFPod);
@@ -591,9 +617,14 @@ bool prepare_and_launch(Plan &pl, const char *routine)
     const int grid = (int)std::min<int64_t>(pl.total, (int64_t)sms * 16);
     if (pl.key != key) {
         // descriptors change only with the batch layout; upload outside the graph
-        if (!cuda_ok(cudaMemcpyAsync(ddesc, pl.descs.data(), d_bytes, cudaMemcpyHostToDevice, s), routine,
+        if (!pl.descs.empty() &&
+            !cuda_ok(cudaMemcpyAsync(ddesc, pl.descs.data(), d_bytes, cudaMemcpyHostToDevice, s), routine,
                      "descriptor upload"))
             return false;
+        if (!pl.oz_items.empty() || pl.oz) {
+            if (!pl.oz) pl.oz = ozgroup_create();
+            if (!ozgroup_prepare(pl.oz, pl.oz_items, routine)) return false;
+        }
     }
     if (!pl.exec || pl.key != key) {
         if (pl.exec) {
@@ -606,9 +637,14 @@ bool prepare_and_launch(Plan &pl, const char *routine)
         bool ok = cuda_ok(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), routine, "begin capture");
         if (ok) {
             // counters start at zero on every replay
-            cudaMemsetAsync(counter, 0, cnt_bytes, cap);
-            auto kern = pl.tile == 64 ? k_gemm_grouped<64> : (pl.tile == 16 ? k_gemm_grouped<16> : k_gemm_grouped<32>);
-            kern<<<grid, GTHREADS, 0, cap>>>(ddesc, (int)pl.descs.size(), pl.total, counter, tile_counters, partials);
+            if (pl.total > 0) {
+                cudaMemsetAsync(counter, 0, cnt_bytes, cap);
+                auto kern = pl.tile == 64 ? k_gemm_grouped<64> : (pl.tile == 16 ? k_gemm_grouped<16> : k_gemm_grouped<32>);
+                kern<<<grid, GTHREADS, 0, cap>>>(ddesc, (int)pl.descs.size(), pl.total, counter, tile_counters,
+                                                 partials);
+            }
+            // the large instances on the tensor cores, in the same graph
+            if (pl.oz && ozgroup_count(pl.oz) > 0) ozgroup_launch(pl.oz, cap);
             ok = cuda_ok(cudaStreamEndCapture(cap, &graph), routine, "end capture");
         }
         if (ok) {
@@ -745,7 +781,9 @@ bool grouped_gemm_device(int64_t count, const char *ta, const char *tb, const in
 {
     if (count == 0) return true;
     static thread_local Plan internal;
-    build_descs(internal, count, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, g_default_policy);
+    Policy pol = g_default_policy;
+    pol.oz_min = 0;   // the solvers' small merges stay on the integer pipes
+    build_descs(internal, count, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, pol);
     return prepare_and_launch(internal, routine);
 }
 
@@ -774,6 +812,7 @@ extern "C" int mgemm_grouped(int64_t count, const char *transa, const char *tran
         if (it != g_policy_cache.end()) pol = it->second;
     }
     if (g_forced_tile.load() > 0) pol.tile = g_forced_tile.load();
+    if (g_forced_oz.load() >= 0) pol.oz_min = g_forced_oz.load();
     Plan &pl = t_plan;
     build_descs(pl, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, pol);
     if (!prepare_and_launch(pl, routine)) return mwblas_last_error();
@@ -836,10 +875,12 @@ extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char 
         cudaEventElapsedTime(&ms, e0, e1);
         return ms;
     };
+    // stages: the tile edge (integer path only), the split policy at that
+    // tile, then the size from which instances run on the tensor cores
     float best = 1e30f;
-    int best_tile = g_default_policy.tile, best_k = g_default_policy.min_k_per_split;
+    int best_tile = g_default_policy.tile, best_k = g_default_policy.min_k_per_split, best_oz = 0;
     for (int t : tiles) {
-        const float ms = time_policy(Policy{g_default_policy.min_k_per_split, 4, t});
+        const float ms = time_policy(Policy{g_default_policy.min_k_per_split, 4, t, 0});
         if (ms < best) {
             best = ms;
             best_tile = t;
@@ -847,21 +888,33 @@ extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char 
     }
     for (int cand : cands) {
         if (cand == g_default_policy.min_k_per_split) continue;   // timed above
-        const float ms = time_policy(Policy{cand, 4, best_tile});
+        const float ms = time_policy(Policy{cand, 4, best_tile, 0});
         if (ms < best) {
             best = ms;
             best_k = cand;
+        }
+    }
+    if (ozaki_available()) {
+        const int ozc[] = {64, 128, 256};
+        for (int oz : ozc) {
+            const float ms = time_policy(Policy{best_k, 4, best_tile, oz});
+            if (ms < best) {
+                best = ms;
+                best_oz = oz;
+            }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (pl.exec) cudaGraphExecDestroy(pl.exec);
     if (pl.dev) cudaFree(pl.dev);
+    ozgroup_destroy(pl.oz);
     cudaFree(scratch);
     {
         std::lock_guard<std::mutex> lk(g_batched_mu);
-        g_policy_cache[shape_class(count, m, n, k)] = Policy{best_k, 4, best_tile};
+        g_policy_cache[shape_class(count, m, n, k)] = Policy{best_k, 4, best_tile, best_oz};
     }
+    t_tuned_oz = best_oz;
     t_tuned_tile = best_tile;
     if (chosen) *chosen = best_k;
     return finish(routine) ? 0 : mwblas_last_error();
@@ -943,6 +996,12 @@ extern "C" int mtrsm_grouped(int64_t count, char side, char uplo, char transa, c
 }
 
 extern "C" int mwblas_grouped_tuned_tile(void) { return mw::t_tuned_tile; }
+extern "C" int mwblas_grouped_tuned_tensor_min(void) { return mw::t_tuned_oz; }
+
+extern "C" int mwblas_set_grouped_tensor_min(int size)
+{
+    return mw::g_forced_oz.exchange(size < 0 ? -1 : size);
+}
 
 extern "C" int mwblas_set_grouped_tile(int tile)
 {

@@ -1,5 +1,6 @@
 // Internal interface of the GEMM engines (device pointers only).
 #pragma once
+#include <vector>
 #include <stdint.h>
 
 #include "l1.h"
@@ -46,6 +47,26 @@ bool gemm_ozaki_cplx(const GemmArgs &g, int bits, const char *routine);
 // Wait limit of the FP64 engine's TMA pipeline (its own copy of the device word).
 void set_plain_wait_limit(uint64_t ns);
 int ozaki_last_moduli();
+
+// Grouped products on the tensor cores (large instances of mgemm_grouped):
+// ozgroup_prepare allocates and uploads everything for a list of real
+// products (outside any stream capture); ozgroup_launch enqueues the batched
+// exponent scan, residue conversion, one residue GEMM per padding class and
+// the batched reconstruction on s (capturable: no host round trip).
+struct OzGroupItem {
+    const void *A, *B;
+    void *C;
+    int64_t lda, ldb, ldc, m, n, k;
+    bool ta, tb;
+    dd_host alpha, beta;
+    int beta_kind;
+};
+struct OzGroupPlan;
+OzGroupPlan *ozgroup_create();
+void ozgroup_destroy(OzGroupPlan *p);
+int64_t ozgroup_count(const OzGroupPlan *p);
+bool ozgroup_prepare(OzGroupPlan *p, const std::vector<OzGroupItem> &items, const char *routine);
+void ozgroup_launch(OzGroupPlan *p, cudaStream_t s);
 int ozaki_last_bits(int operand);   // 0: op(A), 1: op(B)
 
 // C := beta*C over an m x n block (beta_kind 0 writes zeros, 1 is a no-op).

@@ -36,8 +36,11 @@
 #include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <map>
+#include <tuple>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -303,6 +306,79 @@ constexpr size_t residue_smem_bytes()
     return 2 * 32 * 33 * (CPLX ? 2 : 1) * sizeof(double2);
 }
 
+// Signed 11-bit limbs of the four elements cg .. cg + 3 of one staged tile row
+// (E double2 per element: E = 2 complex, the imaginary part negated when
+// conj), scaled by 2^(bits - 2 - e); rows without a live exponent give zeros.
+// Elements (cg, cg+1) and (cg+2, cg+3) share the two lanes of fr[0] / fr[1].
+template <bool CPLX>
+__device__ __forceinline__ void tile_limbs(const double2 (*row)[CPLX ? 2 : 1], int cg, int e, int bits, int conj,
+                                           float2 (&fr)[2][kResLimbs], float2 (&fi)[CPLX ? 2 : 1][kResLimbs])
+{
+    constexpr int E = CPLX ? 2 : 1;
+    const bool live = e > kNoExp / 2;
+    const int sc = bits - 2 - e;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        float f[kResLimbs];
+        bool ng = false;
+        if (live) {
+            to_limbs(row[cg + v][0], sc, f, ng);
+        } else {
+#pragma unroll
+            for (int q = 0; q < kResLimbs; ++q) f[q] = 0.0f;
+        }
+#pragma unroll
+        for (int q = 0; q < kResLimbs; ++q) {
+            const float sv = ng ? -f[q] : f[q];
+            if (v & 1) fr[v >> 1][q].y = sv;
+            else fr[v >> 1][q].x = sv;
+        }
+        if (CPLX) {
+            bool ngi = false;
+            if (live) {
+                to_limbs(row[cg + v][E - 1], sc, f, ngi);
+                if (conj) ngi = !ngi;
+            }
+#pragma unroll
+            for (int q = 0; q < kResLimbs; ++q) {
+                const float sv = ngi ? -f[q] : f[q];
+                if (v & 1) fi[CPLX ? v >> 1 : 0][q].y = sv;
+                else fi[CPLX ? v >> 1 : 0][q].x = sv;
+            }
+        }
+    }
+}
+
+// The residues of those four elements for every modulus (constants in shared
+// memory), four fp16 per 8-byte store at o + l * plane; complex also writes
+// the imaginary part and the sum (Karatsuba) at o + cstride and o + 2 cstride.
+template <bool CPLX>
+__device__ __forceinline__ void store_residues(const float2 (&fr)[2][kResLimbs],
+                                               const float2 (&fi)[CPLX ? 2 : 1][kResLimbs], int nmod,
+                                               const float2 (*s_t)[12], const float4 *s_pp, __half *o, int64_t plane,
+                                               int64_t cstride)
+{
+    for (int l = 0; l < nmod; ++l) {
+        float2 t[12];
+#pragma unroll
+        for (int q = 0; q < 12; q += 2) {
+            const float4 u = *reinterpret_cast<const float4 *>(&s_t[l][q]);
+            t[q] = make_float2(u.x, u.y);
+            t[q + 1] = make_float2(u.z, u.w);
+        }
+        const float4 pp = s_pp[l];
+        const float2 negp = make_float2(pp.x, pp.y), invp = make_float2(pp.z, pp.w);
+        const float2 ra = sym_residue2(fr[0], t, negp, invp), rb = sym_residue2(fr[1], t, negp, invp);
+        store4h(o, ra, rb);
+        if (CPLX) {
+            const float2 ia = sym_residue2(fi[0], t, negp, invp), ib = sym_residue2(fi[CPLX ? 1 : 0], t, negp, invp);
+            store4h(o + cstride, ia, ib);
+            store4h(o + 2 * cstride, sym_wrap2(ra, ia, negp, invp), sym_wrap2(rb, ib, negp, invp));
+        }
+        o += plane;
+    }
+}
+
 template <bool ROWC, bool CPLX>
 __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim, const double2 *__restrict__ X,
                                                      int64_t ld, const int *__restrict__ rexp, int bits,
@@ -352,62 +428,12 @@ __global__ void __launch_bounds__(256) k_oz_residues(int64_t rows, int64_t kdim,
         __syncthreads();
         const int64_t r = (int64_t)(tile / ntc) * 32 + s, cb = (int64_t)(tile % ntc) * 32 + cg;
         const int e = (r < rows) ? rexp[r] : kNoExp;
-        const bool live = e > kNoExp / 2;
-        const int sc = bits - 2 - e;
         // signed limbs of elements (cg, cg+1) and (cg+2, cg+3) in the two lanes
         float2 fr[2][kResLimbs], fi[CPLX ? 2 : 1][kResLimbs];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-            float f[kResLimbs];
-            bool ng = false;
-            if (live) {
-                to_limbs(tiles[buf][s][cg + v][0], sc, f, ng);
-            } else {
-#pragma unroll
-                for (int q = 0; q < kResLimbs; ++q) f[q] = 0.0f;
-            }
-#pragma unroll
-            for (int q = 0; q < kResLimbs; ++q) {
-                const float sv = ng ? -f[q] : f[q];
-                if (v & 1) fr[v >> 1][q].y = sv;
-                else fr[v >> 1][q].x = sv;
-            }
-            if (CPLX) {
-                bool ngi = false;
-                if (live) {
-                    to_limbs(tiles[buf][s][cg + v][E - 1], sc, f, ngi);
-                    if (conj) ngi = !ngi;
-                }
-#pragma unroll
-                for (int q = 0; q < kResLimbs; ++q) {
-                    const float sv = ngi ? -f[q] : f[q];
-                    if (v & 1) fi[CPLX ? v >> 1 : 0][q].y = sv;
-                    else fi[CPLX ? v >> 1 : 0][q].x = sv;
-                }
-            }
-        }
+        tile_limbs<CPLX>(tiles[buf][s], cg, e, bits, conj, fr, fi);
         __syncthreads();   // the buffer is refilled two iterations on; the limbs are in registers
-        const int64_t cstride = (int64_t)nmod * plane_rows * kpad;
-        __half *o = out + (r * kpad + cb);
-        for (int l = 0; l < nmod; ++l) {
-            float2 t[12];
-#pragma unroll
-            for (int q = 0; q < 12; q += 2) {
-                const float4 u = *reinterpret_cast<const float4 *>(&s_t[l][q]);
-                t[q] = make_float2(u.x, u.y);
-                t[q + 1] = make_float2(u.z, u.w);
-            }
-            const float4 pp = s_pp[l];
-            const float2 negp = make_float2(pp.x, pp.y), invp = make_float2(pp.z, pp.w);
-            const float2 ra = sym_residue2(fr[0], t, negp, invp), rb = sym_residue2(fr[1], t, negp, invp);
-            store4h(o, ra, rb);
-            if (CPLX) {
-                const float2 ia = sym_residue2(fi[0], t, negp, invp), ib = sym_residue2(fi[CPLX ? 1 : 0], t, negp, invp);
-                store4h(o + cstride, ia, ib);
-                store4h(o + 2 * cstride, sym_wrap2(ra, ia, negp, invp), sym_wrap2(rb, ib, negp, invp));
-            }
-            o += plane_rows * kpad;
-        }
+        store_residues<CPLX>(fr, fi, nmod, s_t, s_pp, out + (r * kpad + cb), plane_rows * kpad,
+                             (int64_t)nmod * plane_rows * kpad);
     }
 }
 
@@ -875,7 +901,8 @@ constexpr int T2_SMEM = T2_STAGES * (T2_A_BYTES + T2_B_BYTES) + 1024 + 256;
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TCP_THREADS, 1)
     k_oz_gemm_tc_2sm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int64_t Mp,
                      int64_t Np, int64_t Kp, int64_t M, int64_t N, OzModParams P, uint16_t *__restrict__ R,
-                     int *status, int uplo, int tiles_m2, int tiles_n, int nz, int tn0, int tm0, int lose_loads)
+                     int *status, int uplo, int tiles_m2, int tiles_n, int nz, int tn0, int tm0, int lose_loads,
+                     int zmod)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -1038,7 +1065,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(TCP_THREADS, 1)
                 for (int b = 0; b < nu; ++b) {
                     int tn, tm2, l;
                     unit_at(b ? ub : ua, tn, tm2, l);
-                    const float p = P.p[l], invp = P.invp[l];
+                    const float p = P.p[l % zmod], invp = P.invp[l % zmod];   // plane l holds modulus l % zmod
                     if (!__all_sync(0xffffffffu, sm100::mbar_wait(&accf[b], fcnt[b] & 1, status, 4))) {
                         ok = false;
                         break;
@@ -1174,6 +1201,79 @@ __device__ __forceinline__ bool finite_hi(double x)
     return ((__double2hiint(x) >> 20) & 0x7FF) != 0x7FF;   // exponent field test, no FP64 compare
 }
 
+// Output rows i0 and i0 + 1 (when `two`) of column j: the CRT sums of their
+// residues over the nmod planes (rcol points at row i0, column j of plane 0;
+// planes `plane` entries apart), then alpha M (folded into Mx), the power-of-
+// two scaling and beta C (beta as the extended float xb), one rounding to
+// double-double. pc points at C(i0, j).
+__device__ __forceinline__ void reconstruct_pair(const CrtSmem &sm, int nmod, const uint16_t *rcol, int64_t plane,
+                                                 int i0, bool two, int ea0, int ea1, int j, int ebj, int bsum,
+                                                 const xw::XW &Mx, const xw::XW &xb, dd::real beta, int beta_kind,
+                                                 double2 *pc, int uplo)
+{
+    // both rows outside the stored triangle: nothing to compute
+    if ((uplo == 1 && i0 > j) || (uplo == 2 && i0 + 1 < j)) return;
+    crt::Frac acc0, acc1;
+    acc0.reset();
+    acc1.reset();
+    const bool live0 = ea0 > kNoExp / 2 && ea0 < 1024 && ebj > kNoExp / 2 && ebj < 1024;
+    const bool live1 = two && ea1 > kNoExp / 2 && ea1 < 1024 && ebj > kNoExp / 2 && ebj < 1024;
+    if (live0 || live1) {
+        // residues of all moduli for both rows: the loads of 8 planes are
+        // issued together so that their latencies overlap
+        const uint32_t *q = reinterpret_cast<const uint32_t *>(rcol);
+        const int64_t qstep = plane / 2;
+        int l = 0;
+        for (; l + 8 <= nmod; l += 8) {
+            uint32_t c[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                c[u] = __ldcs(q);
+                q += qstep;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                acc0.add(sm.F[l + u], c[u] & 0xFFFFu);
+                acc1.add(sm.F[l + u], c[u] >> 16);
+            }
+        }
+        for (; l < nmod; ++l, q += qstep) {
+            const uint32_t c = __ldcs(q);
+            acc0.add(sm.F[l], c & 0xFFFFu);
+            acc1.add(sm.F[l], c >> 16);
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int i = i0 + h;
+        if (h == 1 && !two) break;
+        if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
+        const int eai = h ? ea1 : ea0;
+        double2 *pe = pc + h;
+        if (eai >= 1024 || ebj >= 1024) {   // a non-finite entry in row i of op(A) or column j of op(B)
+            const double qnan = __longlong_as_double(0x7ff8000000000000ll);
+            *pe = make_double2(qnan, qnan);
+            continue;
+        }
+        xw::XW v = xw::zero();
+        if (h ? live1 : live0) v = (h ? acc1 : acc0).finish_xw(Mx, bsum - 4 - eai - ebj);
+        if (beta_kind != 0) {
+            const double2 c0 = *pe;
+            if (!finite_hi(c0.x)) {
+                // non-finite C: the double-double operators propagate it
+                dd::real cv = dd::make(c0.x, c0.y);
+                if (beta_kind == 2) cv = dd::mul_exact(cv, beta);
+                dd::store(pe, dd::add_exact(cv, xw_dd(v)));
+                continue;
+            }
+            xw::XW xc = xw::from_dd(c0.x, c0.y);
+            if (beta_kind == 2) xc = xw::mul(xb, xc);
+            v = xw::add(v, xc);
+        }
+        dd::store(pe, xw_dd(v));
+    }
+}
+
 // C(i, j) := alpha * X(i, j) * 2^-S2 + beta * C(i, j), real. Thread per pair
 // of rows, columns j = blockIdx.y, blockIdx.y + gridDim.y, ...; m and n below 2^31
 // (the host routes larger sizes elsewhere), so the per-element index work is
@@ -1199,70 +1299,8 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
     const uint16_t *rcol = R + (int64_t)blockIdx.y * Mp + i0;
     double2 *pc = C + i0 + (int64_t)blockIdx.y * ldc;
     const int64_t rstep = (int64_t)jstep * Mp, cstep = (int64_t)jstep * ldc;
-    for (int j = blockIdx.y; j < n; j += jstep, rcol += rstep, pc += cstep) {
-        // both rows outside the stored triangle: nothing to compute
-        if ((uplo == 1 && i0 > j) || (uplo == 2 && i0 + 1 < j)) continue;
-        const int ebj = eb[j];
-        crt::Frac acc0, acc1;
-        acc0.reset();
-        acc1.reset();
-        const bool live0 = ea0 > kNoExp / 2 && ea0 < 1024 && ebj > kNoExp / 2 && ebj < 1024;
-        const bool live1 = two && ea1 > kNoExp / 2 && ea1 < 1024 && ebj > kNoExp / 2 && ebj < 1024;
-        if (live0 || live1) {
-            // residues of all moduli for both rows: the loads of 8 planes are
-            // issued together so that their latencies overlap
-            const uint32_t *q = reinterpret_cast<const uint32_t *>(rcol);
-            const int64_t qstep = plane / 2;
-            int l = 0;
-            for (; l + 8 <= nmod; l += 8) {
-                uint32_t c[8];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    c[u] = __ldcs(q);
-                    q += qstep;
-                }
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    acc0.add(sm.F[l + u], c[u] & 0xFFFFu);
-                    acc1.add(sm.F[l + u], c[u] >> 16);
-                }
-            }
-            for (; l < nmod; ++l, q += qstep) {
-                const uint32_t c = __ldcs(q);
-                acc0.add(sm.F[l], c & 0xFFFFu);
-                acc1.add(sm.F[l], c >> 16);
-            }
-        }
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int i = i0 + h;
-            if (h == 1 && !two) break;
-            if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
-            const int eai = h ? ea1 : ea0;
-            double2 *pe = pc + h;
-            if (eai >= 1024 || ebj >= 1024) {   // a non-finite entry in row i of op(A) or column j of op(B)
-                const double qnan = __longlong_as_double(0x7ff8000000000000ll);
-                *pe = make_double2(qnan, qnan);
-                continue;
-            }
-            xw::XW v = xw::zero();
-            if (h ? live1 : live0) v = (h ? acc1 : acc0).finish_xw(Mx, bsum - 4 - eai - ebj);
-            if (beta_kind != 0) {
-                const double2 c0 = *pe;
-                if (!finite_hi(c0.x)) {
-                    // non-finite C: the double-double operators propagate it
-                    dd::real cv = dd::make(c0.x, c0.y);
-                    if (beta_kind == 2) cv = dd::mul_exact(cv, beta);
-                    dd::store(pe, dd::add_exact(cv, xw_dd(v)));
-                    continue;
-                }
-                xw::XW xc = xw::from_dd(c0.x, c0.y);
-                if (beta_kind == 2) xc = xw::mul(xb, xc);
-                v = xw::add(v, xc);
-            }
-            dd::store(pe, xw_dd(v));
-        }
-    }
+    for (int j = blockIdx.y; j < n; j += jstep, rcol += rstep, pc += cstep)
+        reconstruct_pair(sm, nmod, rcol, plane, i0, two, ea0, ea1, j, eb[j], bsum, Mx, xb, beta, beta_kind, pc, uplo);
 }
 
 // Complex: R holds the residues of P1 = Ar*Br, P2 = Ai*Bi and
@@ -1708,7 +1746,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         const unsigned grid = 2u * (unsigned)(units < pairs ? units : pairs);
         k_oz_gemm_tc_2sm<<<grid, TCP_THREADS, T2_SMEM, stream()>>>(ma, mb, Mp, Np, Kp, m, n, mp, R,
                                                                    device_status_word(), g.uplo, tiles_m2, ntn, nz,
-                                                                   tn0, tm0, take_lost_load_injection());
+                                                                   tn0, tm0, take_lost_load_injection(), nz);
     };
     if (blocked) {
         // launched block by block with the reconstruction below
@@ -1877,6 +1915,352 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
     phase_collect();
     return true;
 }
+
+// ---- grouped products on the tensor cores (large instances of mgemm_grouped) ----------
+//
+// Instances are padded to classes (Mp, Np multiples of 256, Kp of 64) and every
+// class runs as one CTA-pair residue GEMM over count x L planes: plane
+// slot * L + l holds modulus l of the instance in that slot. Exponents,
+// residues and the reconstruction run as one batched launch each over all
+// instances. Everything is enqueued without host round trips (full 106-bit
+// width), so the whole sequence can be captured in a CUDA graph.
+
+struct OzGrpDesc {
+    const double2 *A, *B;
+    double2 *C;
+    int64_t lda, ldb, ldc;
+    int m, n, k, ta, tb;
+    int cls, slot;
+    int64_t ea_off, eb_off;   // row exponents of op(A), column exponents of op(B)
+    int64_t line_begin;       // first exponent line: m rows of op(A), then n columns of op(B)
+    int64_t tile_begin;       // first conversion tile: op(A)'s (Mp/32)(Kp/32), then op(B)'s (Np/32)(Kp/32)
+    int64_t rec_begin;        // first reconstruction item: ceil(m/512) row slabs x ceil(n/8) column groups
+    xw::XW aM, xb;            // alpha * M and beta as extended floats
+    double2 beta;
+    int beta_kind, pad;
+};
+
+struct OzGrpClass {
+    int64_t Mp, Np, Kp;
+    __half *Ares, *Bres;      // [slot][l][row][k]
+    uint16_t *R;              // [slot][l][col][row]
+};
+
+__device__ __forceinline__ int grp_find(const OzGrpDesc *__restrict__ d, int count, int64_t w, int which)
+{
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const int64_t b = which == 0 ? d[mid].line_begin : (which == 1 ? d[mid].tile_begin : d[mid].rec_begin);
+        if (b <= w) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int grp_exp_bound(double x)
+{
+    const uint64_t b = (uint64_t)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    return b == 0 ? kNoExp : (int)(b >> 52) - 1023;
+}
+
+// Exponent bound of every row of op(A) and column of op(B), thread per line.
+__global__ void k_grp_exp(const OzGrpDesc *__restrict__ descs, int count, int64_t lines, int *__restrict__ ex)
+{
+    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < lines; w += (int64_t)gridDim.x * blockDim.x) {
+        const OzGrpDesc &d = descs[grp_find(descs, count, w, 0)];
+        const int64_t t = w - d.line_begin;
+        int e = kNoExp;
+        if (t < d.m) {   // row t of op(A)
+            const double2 *p = d.ta ? d.A + t * d.lda : d.A + t;
+            const int64_t step = d.ta ? 1 : d.lda;
+            for (int q = 0; q < d.k; ++q, p += step) e = max(e, grp_exp_bound(p->x));
+            ex[d.ea_off + t] = e;
+        } else {         // column t - m of op(B)
+            const int64_t j = t - d.m;
+            const double2 *p = d.tb ? d.B + j : d.B + j * d.ldb;
+            const int64_t step = d.tb ? d.ldb : 1;
+            for (int q = 0; q < d.k; ++q, p += step) e = max(e, grp_exp_bound(p->x));
+            ex[d.eb_off + j] = e;
+        }
+    }
+}
+
+// Residues of op(A) and op(B) of every instance into its class planes, one
+// 32 x 32 tile (padding included: zeros) per block and step.
+__global__ void __launch_bounds__(256) k_grp_residues(const OzGrpDesc *__restrict__ descs, int count, int64_t tiles,
+                                                      const OzGrpClass *__restrict__ classes, const int *__restrict__ ex,
+                                                      int bits, OzResParams P)
+{
+    __shared__ __align__(16) double2 tile[32][33][1];
+    __shared__ __align__(16) float2 s_t[kMaxMod][12];
+    __shared__ __align__(16) float4 s_pp[kMaxMod];
+    const int nmod = P.nmod;
+    for (int i = threadIdx.x; i < nmod * 12; i += blockDim.x) {
+        const int l = i / 12, q = i % 12;
+        const float t = (q < kResLimbs) ? P.t[l][q] : 0.0f;
+        s_t[l][q] = make_float2(t, t);
+    }
+    for (int i = threadIdx.x; i < nmod; i += blockDim.x) s_pp[i] = make_float4(-P.p[i], -P.p[i], P.invp[i], P.invp[i]);
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int s = threadIdx.x >> 3, cg = (threadIdx.x & 7) * 4;
+    for (int64_t w = blockIdx.x; w < tiles; w += gridDim.x) {
+        const OzGrpDesc &d = descs[grp_find(descs, count, w, 1)];
+        const OzGrpClass &c = classes[d.cls];
+        const int64_t ntc = c.Kp / 32, ta_tiles = (c.Mp / 32) * ntc;
+        int64_t t = w - d.tile_begin;
+        const bool isA = t < ta_tiles;
+        if (!isA) t -= ta_tiles;
+        const int64_t r0 = (t / ntc) * 32, c0 = (t % ntc) * 32;
+        // op(X) element (r, c): op(A) = A or A^T; op(B)^T rows are B's columns (B) or rows (B^T)
+        const double2 *X = isA ? d.A : d.B;
+        const int64_t ld = isA ? d.lda : d.ldb;
+        const int rows = isA ? d.m : d.n;
+        const bool rowc = isA ? !d.ta : d.tb;   // rows contiguous in memory
+        __syncthreads();   // the previous tile's limbs are taken
+        for (int u = ty; u < 32; u += 8) {
+            const int64_t r = rowc ? r0 + tx : r0 + u, col = rowc ? c0 + u : c0 + tx;
+            double2 v = make_double2(0.0, 0.0);
+            if (r < rows && col < d.k) v = rowc ? X[r + col * ld] : X[col + r * ld];
+            if (rowc) tile[tx][u][0] = v;
+            else tile[u][tx][0] = v;
+        }
+        __syncthreads();
+        const int64_t r = r0 + s;
+        const int e = r < rows ? ex[(isA ? d.ea_off : d.eb_off) + r] : kNoExp;
+        float2 fr[2][kResLimbs], fi[1][kResLimbs];
+        tile_limbs<false>(tile[s], cg, e, bits, 0, fr, fi);
+        const int64_t prow = isA ? c.Mp : c.Np;
+        __half *base = isA ? c.Ares : c.Bres;
+        __half *o = base + ((int64_t)d.slot * nmod * prow + r) * c.Kp + c0 + cg;
+        store_residues<false>(fr, fi, nmod, s_t, s_pp, o, prow * c.Kp, 0);
+    }
+}
+
+// alpha * X * 2^-S2 + beta C for every instance: a thread per row pair of a
+// 512-row slab and 8 columns per work item.
+__global__ void __launch_bounds__(256) k_grp_reconstruct(const OzGrpDesc *__restrict__ descs, int count,
+                                                         int64_t items, const OzGrpClass *__restrict__ classes,
+                                                         const int *__restrict__ ex, int bsum, OzCrtParams K)
+{
+    __shared__ CrtSmem sm;
+    crt_smem_fill(sm, K);
+    __syncthreads();
+    const int nmod = K.nmod;
+    for (int64_t w = blockIdx.x; w < items; w += gridDim.x) {
+        const OzGrpDesc &d = descs[grp_find(descs, count, w, 2)];
+        const OzGrpClass &c = classes[d.cls];
+        const int64_t t = w - d.rec_begin, ncg = (d.n + 7) / 8;
+        const int slab = (int)(t / ncg), j0 = (int)(t % ncg) * 8;
+        const int i0 = slab * 512 + 2 * threadIdx.x;
+        if (i0 >= d.m) continue;
+        const bool two = i0 + 1 < d.m;
+        const int ea0 = ex[d.ea_off + i0], ea1 = two ? ex[d.ea_off + i0 + 1] : kNoExp;
+        const int64_t plane = c.Np * c.Mp;
+        const uint16_t *R0 = c.R + (int64_t)d.slot * nmod * plane + i0;
+        const dd::real beta = dd::make(d.beta.x, d.beta.y);
+        for (int j = j0; j < min(d.n, j0 + 8); ++j)
+            reconstruct_pair(sm, nmod, R0 + (int64_t)j * c.Mp, plane, i0, two, ea0, ea1, j, ex[d.eb_off + j], bsum,
+                             d.aM, d.xb, beta, d.beta_kind, d.C + i0 + (int64_t)j * d.ldc, 0);
+    }
+}
+
+}  // namespace
+
+struct OzGroupPlan {
+    std::vector<OzGrpDesc> descs;
+    std::vector<OzGrpClass> classes;
+    std::vector<int64_t> class_count;
+    int64_t lines = 0, tiles = 0, items = 0;
+    Moduli md;
+    OzResParams rp;
+    OzModParams mp;
+    OzCrtParams cp;
+    std::vector<CUtensorMap> maps;   // two per class
+    void *dev = nullptr;
+    size_t dev_bytes = 0;
+    OzGrpDesc *d_descs = nullptr;
+    OzGrpClass *d_classes = nullptr;
+    int *d_ex = nullptr;
+};
+
+OzGroupPlan *ozgroup_create() { return new OzGroupPlan(); }
+
+void ozgroup_destroy(OzGroupPlan *p)
+{
+    if (!p) return;
+    if (p->dev) cudaFree(p->dev);
+    delete p;
+}
+
+int64_t ozgroup_count(const OzGroupPlan *p) { return p ? (int64_t)p->descs.size() : 0; }
+
+namespace {
+
+constexpr int kGroupBits = 106;
+
+int64_t round_up(int64_t v, int64_t q) { return (v + q - 1) / q * q; }
+
+// Kp of a class: 64, 128, 256, 512, then multiples of 512 (fewer classes)
+int64_t class_kp(int64_t k)
+{
+    int64_t kp = 64;
+    while (kp < k && kp < 512) kp *= 2;
+    return kp >= k ? kp : round_up(k, 512);
+}
+
+}  // namespace
+
+bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, const char *routine)
+{
+    pl->descs.clear();
+    pl->classes.clear();
+    pl->class_count.clear();
+    pl->lines = pl->tiles = pl->items = 0;
+    if (items.empty()) return true;
+    if (!ozaki_available() || !get_encode()) {
+        set_error(routine, MWBLAS_ERR_UNSUPPORTED, "tensor-core engine unavailable on this device");
+        return false;
+    }
+    // moduli for the longest k (full width: no readback inside the graph)
+    int64_t kmax = 1;
+    for (const OzGroupItem &it : items) kmax = std::max<int64_t>(kmax, it.k);
+    pl->md = choose_moduli(2.0 * (kGroupBits - 1) + std::log2((double)kmax) + 1.0 + 4.0);
+    fill_res_params(pl->md, pl->rp, pl->mp);
+    fill_crt_params(pl->md, pl->cp);
+    const int L = pl->md.n;
+    xw::XW Mx;
+    Mx.w[3] = (uint32_t)(pl->cp.Mhi >> 32);
+    Mx.w[2] = (uint32_t)pl->cp.Mhi;
+    Mx.w[1] = (uint32_t)(pl->cp.Mlo >> 32);
+    Mx.w[0] = (uint32_t)pl->cp.Mlo;
+    Mx.e = pl->cp.Me;
+    Mx.neg = 0u;
+    // classes and slots
+    std::map<std::tuple<int64_t, int64_t, int64_t>, int> cls_of;
+    int64_t exn = 0;
+    for (const OzGroupItem &it : items) {
+        const auto key = std::make_tuple(round_up(it.m, 256), round_up(it.n, 256), class_kp(it.k));
+        auto f = cls_of.find(key);
+        int ci;
+        if (f == cls_of.end()) {
+            ci = (int)pl->classes.size();
+            cls_of[key] = ci;
+            OzGrpClass c{};
+            c.Mp = std::get<0>(key);
+            c.Np = std::get<1>(key);
+            c.Kp = std::get<2>(key);
+            pl->classes.push_back(c);
+            pl->class_count.push_back(0);
+        } else {
+            ci = f->second;
+        }
+        OzGrpDesc d{};
+        d.A = (const double2 *)it.A;
+        d.B = (const double2 *)it.B;
+        d.C = (double2 *)it.C;
+        d.lda = it.lda;
+        d.ldb = it.ldb;
+        d.ldc = it.ldc;
+        d.m = (int)it.m;
+        d.n = (int)it.n;
+        d.k = (int)it.k;
+        d.ta = it.ta ? 1 : 0;
+        d.tb = it.tb ? 1 : 0;
+        d.cls = ci;
+        d.slot = (int)pl->class_count[ci]++;
+        d.ea_off = exn;
+        d.eb_off = exn + it.m;
+        exn += it.m + it.n;
+        const OzGrpClass &c = pl->classes[ci];
+        d.line_begin = pl->lines;
+        pl->lines += it.m + it.n;
+        d.tile_begin = pl->tiles;
+        pl->tiles += (c.Mp / 32 + c.Np / 32) * (c.Kp / 32);
+        d.rec_begin = pl->items;
+        pl->items += ((it.m + 511) / 512) * ((it.n + 7) / 8);
+        const bool alpha_one = it.alpha.hi == 1.0 && it.alpha.lo == 0.0;
+        d.aM = alpha_one ? Mx : xw::mul(xw::from_dd(it.alpha.hi, it.alpha.lo), Mx);
+        d.xb = xw::from_dd(it.beta.hi, it.beta.lo);
+        d.beta = make_double2(it.beta.hi, it.beta.lo);
+        d.beta_kind = it.beta_kind;
+        pl->descs.push_back(d);
+    }
+    // one buffer: [descriptors][classes][exponents][per class: A residues, B residues, products]
+    const size_t d_bytes = round_up((int64_t)(pl->descs.size() * sizeof(OzGrpDesc)), 256);
+    const size_t c_bytes = round_up((int64_t)(pl->classes.size() * sizeof(OzGrpClass)), 256);
+    const size_t e_bytes = round_up(exn * (int64_t)sizeof(int), 256);
+    size_t need = d_bytes + c_bytes + e_bytes;
+    std::vector<size_t> off(pl->classes.size());
+    for (size_t ci = 0; ci < pl->classes.size(); ++ci) {
+        const OzGrpClass &c = pl->classes[ci];
+        const int64_t planes = pl->class_count[ci] * L;
+        off[ci] = need;
+        need += round_up(planes * c.Mp * c.Kp * 2, 256) + round_up(planes * c.Np * c.Kp * 2, 256) +
+                round_up(planes * c.Np * c.Mp * 2, 256);
+    }
+    if (pl->dev_bytes < need) {
+        if (pl->dev) cudaFree(pl->dev);
+        pl->dev = nullptr;
+        pl->dev_bytes = 0;
+        if (!cuda_ok(cudaMalloc(&pl->dev, need), routine, "grouped tensor-core plan buffer")) return false;
+        pl->dev_bytes = need;
+    }
+    char *base = (char *)pl->dev;
+    pl->d_descs = (OzGrpDesc *)base;
+    pl->d_classes = (OzGrpClass *)(base + d_bytes);
+    pl->d_ex = (int *)(base + d_bytes + c_bytes);
+    pl->maps.assign(2 * pl->classes.size(), CUtensorMap{});
+    for (size_t ci = 0; ci < pl->classes.size(); ++ci) {
+        OzGrpClass &c = pl->classes[ci];
+        const int64_t planes = pl->class_count[ci] * L;
+        char *p = base + off[ci];
+        c.Ares = (__half *)p;
+        p += round_up(planes * c.Mp * c.Kp * 2, 256);
+        c.Bres = (__half *)p;
+        p += round_up(planes * c.Np * c.Kp * 2, 256);
+        c.R = (uint16_t *)p;
+        if (!make_map(&pl->maps[2 * ci], c.Ares, (uint64_t)c.Kp, (uint64_t)(planes * c.Mp), TC_BM, routine) ||
+            !make_map(&pl->maps[2 * ci + 1], c.Bres, (uint64_t)c.Kp, (uint64_t)(planes * c.Np), 128, routine))
+            return false;
+    }
+    cudaFuncSetAttribute(k_oz_gemm_tc_2sm, cudaFuncAttributeMaxDynamicSharedMemorySize, T2_SMEM);
+    cudaStream_t st = stream();
+    return cuda_ok(cudaMemcpyAsync(pl->d_descs, pl->descs.data(), pl->descs.size() * sizeof(OzGrpDesc),
+                                   cudaMemcpyHostToDevice, st),
+                   routine, "grouped descriptor upload") &&
+           cuda_ok(cudaMemcpyAsync(pl->d_classes, pl->classes.data(), pl->classes.size() * sizeof(OzGrpClass),
+                                   cudaMemcpyHostToDevice, st),
+                   routine, "grouped class upload");
+}
+
+void ozgroup_launch(OzGroupPlan *pl, cudaStream_t s)
+{
+    if (pl->descs.empty()) return;
+    const int count = (int)pl->descs.size();
+    const int sms = device_sm_count();
+    const int L = pl->md.n;
+    k_grp_exp<<<(unsigned)std::min<int64_t>((pl->lines + 255) / 256, (int64_t)sms * 8), 256, 0, s>>>(
+        pl->d_descs, count, pl->lines, pl->d_ex);
+    k_grp_residues<<<(unsigned)std::min<int64_t>(pl->tiles, (int64_t)sms * 8), 256, 0, s>>>(
+        pl->d_descs, count, pl->tiles, pl->d_classes, pl->d_ex, kGroupBits, pl->rp);
+    for (size_t ci = 0; ci < pl->classes.size(); ++ci) {
+        const OzGrpClass &c = pl->classes[ci];
+        const int nz = (int)(pl->class_count[ci] * L);
+        const int tiles_m2 = (int)(c.Mp / 256), tiles_n = (int)(c.Np / TC_BN);
+        const int64_t units = (int64_t)nz * tiles_m2 * tiles_n;
+        const int64_t pairs = sms / 2;
+        const unsigned grid = 2u * (unsigned)(units < pairs ? units : pairs);
+        k_oz_gemm_tc_2sm<<<grid, TCP_THREADS, T2_SMEM, s>>>(pl->maps[2 * ci], pl->maps[2 * ci + 1], c.Mp, c.Np, c.Kp,
+                                                             c.Mp, c.Np, pl->mp, c.R, device_status_word(), 0,
+                                                             tiles_m2, tiles_n, nz, 0, 0, take_lost_load_injection(), L);
+    }
+    k_grp_reconstruct<<<(unsigned)std::min<int64_t>(pl->items, (int64_t)sms * 8), 256, 0, s>>>(
+        pl->d_descs, count, pl->items, pl->d_classes, pl->d_ex, 2 * kGroupBits, pl->cp);
+    count_launch(3 + (int64_t)pl->classes.size());
+}
+
+namespace {
 
 }  // namespace
 

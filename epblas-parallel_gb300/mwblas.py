@@ -168,6 +168,8 @@ class MWBlas:
             self._sig("mgemm_grouped_tune", _i32, [_i64, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p])
             self._sig("mwblas_grouped_tuned_tile", _i32, [])
             self._sig("mwblas_set_grouped_tile", _i32, [_i32])
+            self._sig("mwblas_set_grouped_tensor_min", _i32, [_i32])
+            self._sig("mwblas_grouped_tuned_tensor_min", _i32, [])
             self._sig("mtrsm_grouped", _i32, [_i64, C.c_char, C.c_char, C.c_char, C.c_char, _p, _p, _p, _p, _p,
                                               _p, _p])
 

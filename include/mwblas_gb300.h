@@ -493,6 +493,15 @@ int mwblas_grouped_tuned_tile(void);
  * tuned or default choice). All give results within the same bound. Returns
  * the previous setting. */
 int mwblas_set_grouped_tile(int tile);
+/* mgemm_grouped runs instances with m, n >= size and 64 <= k <= 16384 on the
+ * tensor cores (Ozaki scheme, full 106-bit width, padded to classes of
+ * 256-row/column and 64..512-deep tiles, one residue GEMM per class) and the
+ * rest on the integer pipes; 0 = none, -1 = the tuned or default choice
+ * (default 128). Returns the previous setting. mwblas_grouped_tuned_tensor_min
+ * returns the size this thread's most recent mgemm_grouped_tune chose (0 =
+ * integer pipes only). No counterpart in the reference. */
+int mwblas_set_grouped_tensor_min(int size);
+int mwblas_grouped_tuned_tensor_min(void);
 /* Batched triangular solves with shared flags and per-instance sizes: for
  * i < count, op(A[i]) X = alpha[i] B[i] (side 'L') or X op(A[i]) = alpha[i] B[i]
  * ('R'); B[i] is overwritten. Device (or managed) matrix pointers. */

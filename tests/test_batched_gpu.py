@@ -277,3 +277,75 @@ def test_grouped_trsm_graph_replay(gpu, oracle, rng):
         err = orc.normwise_error(arena3.get(2 * i + 1)[:, :d["m"]], want[:, :d["m"]],
                                  orc.dd_abs(d["alpha"]) * orc.dd_absmax(d["B"]))
         assert err <= max(20, 8 * d["na"] ** 2) * orc.EPS_DD, (i, err)
+
+
+def _mixed_batch(rng, count, fill=None):
+    """Large instances (m, n >= 128, k >= 64: the tensor-core path) mixed with
+    small ones, every transpose pair, padded leading dimensions, beta = 0 / 1 /
+    random, and an Inf in one large instance."""
+    inst = []
+    for t in range(count):
+        big = t % 2 == 0
+        if big:
+            m, n = (int(x) for x in rng.integers(128, 530, 2))
+            k = int(rng.integers(64, 600))
+        else:
+            m, n, k = (int(x) for x in rng.integers(1, 100, 3))
+        ta, tb = str(rng.choice(["N", "T", "C"])), str(rng.choice(["N", "T"]))
+        lda = (m if ta == "N" else k) + int(rng.integers(0, 3))
+        ldb = (k if tb == "N" else n) + int(rng.integers(0, 3))
+        ldc = m + int(rng.integers(0, 3))
+        A = mwb.dd_matrix(rng, m if ta == "N" else k, k if ta == "N" else m, lda)
+        B = mwb.dd_matrix(rng, k if tb == "N" else n, n if tb == "N" else k, ldb)
+        Cm = mwb.dd_matrix(rng, m, n, ldc, fill=fill)
+        be = [mwb.random_dd(rng, ()), np.zeros(2), np.array([1.0, 0.0])][t % 3]
+        if t == 4:
+            A[0, 0] = (np.inf, 0.0)     # row 0 of op(A) (or column 0) holds an Inf
+        inst.append(dict(m=m, n=n, k=k, ta=ta, tb=tb, lda=lda, ldb=ldb, ldc=ldc, A=A, B=B, C=Cm,
+                         alpha=mwb.random_dd(rng, ()), beta=be))
+    return inst
+
+
+def test_grouped_gemm_tensor_core_path(gpu, oracle, rng):
+    """Instances with m, n >= 128 and k >= 64 run on the tensor cores (padding
+    classes, one residue GEMM per class, batched conversion and
+    reconstruction), the rest on the integer pipes, in one graph; results
+    within the GEMM tolerance, non-finite rows/columns NaN, padding rows of C
+    untouched, and a replay that gives the same bits."""
+    import torch
+    inst = _mixed_batch(rng, 24, fill=-7.37e18)
+    prev = gpu.lib.mwblas_set_grouped_tensor_min(128)
+    try:
+        arena, args, _ = run_grouped(gpu, inst)
+        first = [arena.get(3 * i + 2) for i in range(len(inst))]
+        for i, d in enumerate(inst):
+            o = arena.offsets[3 * i + 2]
+            arena.buf[o:o + d["C"].size] = torch.from_numpy(d["C"].reshape(-1)).cuda()
+        assert gpu.mgemm_grouped(**args) == 0, gpu.last_error()
+        for i in range(len(inst)):
+            np.testing.assert_array_equal(arena.get(3 * i + 2), first[i])
+    finally:
+        gpu.lib.mwblas_set_grouped_tensor_min(prev)
+    for i, d in enumerate(inst):
+        got = first[i]
+        m, n, k = d["m"], d["n"], d["k"]
+        want = oracle.qgemm(d["ta"], d["tb"], m, n, k, d["alpha"], d["A"], d["lda"], d["B"], d["ldb"], d["beta"],
+                            d["C"].copy(), d["ldc"])
+        if d["ldc"] > m:
+            assert np.all(got[:, m:] == -7.37e18), i
+        if i == 4:
+            bad = ~np.isfinite(want[:, :m, 0])
+            assert bad.any() and np.all(np.isnan(got[:, :m, 0][bad])), i
+            continue
+        opn = orc.dd_abs(d["alpha"]) * max(k, 1) * orc.dd_absmax(d["A"]) * orc.dd_absmax(d["B"]) \
+            + orc.dd_abs(d["beta"]) * orc.dd_absmax(d["C"][:, :m])
+        err = orc.normwise_error(got[:, :m], want[:, :m], opn)
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (i, m, n, k, err)
+
+
+def test_grouped_gemm_tuner_chooses_tensor_threshold(gpu, oracle, rng):
+    inst = _mixed_batch(rng, 16)
+    inst[4]["A"][0, 0] = (0.5, 0.0)
+    arena, args, chosen = run_grouped(gpu, inst, tune=True)
+    assert gpu.lib.mwblas_grouped_tuned_tensor_min() in (0, 64, 128, 256)
+    check(oracle, inst, arena)
