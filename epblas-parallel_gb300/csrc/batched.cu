@@ -583,7 +583,9 @@ uint64_t plan_key(const Plan &pl)
 }
 
 // (Re)creates the device buffers and the graph when the batch layout changed.
-bool prepare_and_launch(Plan &pl, const char *routine)
+// use_graph = false (the library's own calls, whose layouts change from call
+// to call): the kernels are enqueued directly instead of capturing a graph.
+bool prepare_and_launch(Plan &pl, const char *routine, bool use_graph = true)
 {
     if ((pl.descs.empty() || pl.total == 0) && pl.oz_items.empty()) return true;
     const size_t d_bytes = pl.descs.size() * sizeof(GemmDesc);
@@ -625,6 +627,17 @@ bool prepare_and_launch(Plan &pl, const char *routine)
             if (!pl.oz) pl.oz = ozgroup_create();
             if (!ozgroup_prepare(pl.oz, pl.oz_items, routine)) return false;
         }
+    }
+    if (!use_graph) {
+        pl.key = key;
+        if (pl.total > 0) {
+            cudaMemsetAsync(counter, 0, cnt_bytes, s);
+            auto kern = pl.tile == 64 ? k_gemm_grouped<64> : (pl.tile == 16 ? k_gemm_grouped<16> : k_gemm_grouped<32>);
+            kern<<<grid, GTHREADS, 0, s>>>(ddesc, (int)pl.descs.size(), pl.total, counter, tile_counters, partials);
+            count_launch();
+        }
+        if (pl.oz && ozgroup_count(pl.oz) > 0) ozgroup_launch(pl.oz, s);
+        return cuda_ok(cudaGetLastError(), routine, "grouped launch");
     }
     if (!pl.exec || pl.key != key) {
         if (pl.exec) {
@@ -777,14 +790,14 @@ bool grouped_gemm_device(int64_t count, const char *ta, const char *tb, const in
                          const int64_t *k, const mwblas_real64x2 *alpha, const mwblas_real64x2 *const *a,
                          const int64_t *lda, const mwblas_real64x2 *const *b, const int64_t *ldb,
                          const mwblas_real64x2 *beta, mwblas_real64x2 *const *c, const int64_t *ldc,
-                         const char *routine)
+                         int tensor_min, const char *routine)
 {
     if (count == 0) return true;
     static thread_local Plan internal;
     Policy pol = g_default_policy;
-    pol.oz_min = 0;   // the solvers' small merges stay on the integer pipes
+    pol.oz_min = tensor_min;
     build_descs(internal, count, ta, tb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, pol);
-    return prepare_and_launch(internal, routine);
+    return prepare_and_launch(internal, routine, false);
 }
 
 }  // namespace mw

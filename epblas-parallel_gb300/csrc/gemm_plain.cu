@@ -59,14 +59,23 @@ __device__ __forceinline__ int exp_bound(double x)
 // hi's, so it is lo's when lo != 0. Non-finite values give kLowNone too (their
 // rows are NaN in the output whatever the width).
 constexpr int kLowNone = 0x3f3f3f3f;   // also the byte-wise memset value below
+// A row holding one entry that alone spans >= 104 bits (hi's top bit to lo's
+// lowest) needs the full width whatever the rest holds: its low bound is set
+// to this, and its remaining entries are not examined.
+constexpr int kLowFull = -(1 << 28);
 __device__ __forceinline__ int low_bit(double2 v)
 {
-    const uint64_t bl = (uint64_t)__double_as_longlong(v.y) & 0x7fffffffffffffffull;
-    const uint64_t b = bl ? bl : ((uint64_t)__double_as_longlong(v.x) & 0x7fffffffffffffffull);
-    const uint32_t bx = (uint32_t)(b >> 52);
-    if (b == 0 || bx == 0x7ff) return kLowNone;
-    const uint64_t sig = bx ? ((b & 0xfffffffffffffull) | (1ull << 52)) : b;
-    return (bx ? (int)bx : 1) - 1075 + (__ffsll((long long)sig) - 1);
+    // 32-bit words only (64-bit shifts and bit scans issue at the FP64 rate here)
+    uint32_t w1 = (uint32_t)__double2hiint(v.y) & 0x7fffffffu, w0 = (uint32_t)__double2loint(v.y);
+    if ((w1 | w0) == 0) {
+        w1 = (uint32_t)__double2hiint(v.x) & 0x7fffffffu;
+        w0 = (uint32_t)__double2loint(v.x);
+    }
+    const uint32_t bx = w1 >> 20;
+    if ((w1 | w0) == 0 || bx == 0x7ffu) return kLowNone;
+    const uint32_t mh = (w1 & 0xfffffu) | (bx ? 0x100000u : 0u);
+    const int tz = w0 ? __ffs((int)w0) - 1 : 32 + __ffs((int)mh) - 1;
+    return (bx ? (int)bx : 1) - 1075 + tz;
 }
 
 // Row exponent bound of a column-major matrix M (rows x cols, ld): out[i] =
@@ -87,8 +96,12 @@ __global__ void k_exp_rows(int64_t rows, int64_t cols, const double2 *M, int64_t
             const double2 *p = M + elem2 * (i + j * ld);
             for (int w = 0; w < elem2; ++w) {
                 const double2 v = p[w];
-                e = max(e, exp_bound(v.x));
-                lb = min(lb, low_bit(v));
+                const int ev = exp_bound(v.x);
+                e = max(e, ev);
+                if (lb != kLowFull) {
+                    const int lv = low_bit(v);
+                    lb = (lv != kLowNone && ev - lv >= 104) ? kLowFull : min(lb, lv);
+                }
             }
         }
         atomicMin(low + i, lb);
@@ -118,8 +131,12 @@ __global__ void k_exp_cols(int64_t rows, int64_t cols, const double2 *M, int64_t
         const double2 *p = M + elem2 * (i + j * ld);
         for (int w = 0; w < elem2; ++w) {
             const double2 v = p[w];
-            e = max(e, exp_bound(v.x));
-            if (low) lb = min(lb, low_bit(v));
+            const int ev = exp_bound(v.x);
+            e = max(e, ev);
+            if (low && lb != kLowFull) {
+                const int lv = low_bit(v);
+                lb = (lv != kLowNone && ev - lv >= 104) ? kLowFull : min(lb, lv);
+            }
         }
     }
     for (int off = 16; off > 0; off >>= 1) {

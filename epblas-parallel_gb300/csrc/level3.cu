@@ -404,11 +404,15 @@ bool trsm_merge_inverses(int64_t na, int64_t h, const void *A, int64_t lda, bool
     if (cnt == 0) return true;
     std::vector<mwblas_real64x2> one((size_t)cnt, mwblas_real64x2{{1.0, 0.0}}),
         mone((size_t)cnt, mwblas_real64x2{{-1.0, 0.0}}), zero((size_t)cnt, mwblas_real64x2{{0.0, 0.0}});
+    // merges of 128 x 128 blocks and larger run on the tensor cores
+    const int tensor_min = h >= 128 && ozaki_available() ? 128 : 0;
     if (!grouped_gemm_device(cnt, t1a.data(), t1b.data(), m1.data(), n1.data(), k1.data(), one.data(), a1.data(),
-                             lda1.data(), b1.data(), ldb1.data(), zero.data(), c1.data(), ldc1.data(), routine))
+                             lda1.data(), b1.data(), ldb1.data(), zero.data(), c1.data(), ldc1.data(), tensor_min,
+                             routine))
         return false;
     return grouped_gemm_device(cnt, t2a.data(), t2b.data(), m2.data(), n2.data(), k2.data(), mone.data(), a2.data(),
-                               lda2.data(), b2.data(), ldb2.data(), zero.data(), c2.data(), ldc2.data(), routine);
+                               lda2.data(), b2.data(), ldb2.data(), zero.data(), c2.data(), ldc2.data(), tensor_min,
+                               routine);
 }
 
 }  // namespace
@@ -438,7 +442,11 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
         // leaf order 64, or 256 when the right-hand sides make the leaf GEMMs
         // worth it or there are only a few of them; the 32 x 32 inverses are
         // doubled up to it by merging with grouped GEMMs
-        const int64_t nb = (na >= 1024 && (nrhs >= 256 || nrhs < 2 * kTrsmLeaf)) ? 256 : kTrsmLeaf;
+        // (512 for large triangles with many right-hand sides: half the GEMMs
+        // of 256 leaves, the two extra merge levels on the tensor cores)
+        const int64_t nb = (na >= 2048 && nrhs >= 512 && ozaki_available())                        ? 512
+                           : (na >= 1024 && (nrhs >= 256 || nrhs < 2 * kTrsmLeaf)) ? 256
+                                                                                    : kTrsmLeaf;
         const int64_t nblk64 = (na + kInvNB - 1) / kInvNB;
         const int64_t nblk = (na + nb - 1) / nb;
         const size_t inv64_bytes = (size_t)nblk64 * kInvNB * kInvNB * sizeof(double2);

@@ -27,12 +27,14 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
                  int64_t lda, void *B, int64_t ldb, const char *routine);
 void launch_zero_matrix(int64_t m, int64_t n, void *B, int64_t ldb);
 
-// Grouped GEMM on device arrays for internal use (arguments valid, no sync).
+// Grouped GEMM on device arrays for internal use (arguments valid, no sync,
+// launched directly); instances with m, n >= tensor_min (> 0) and k >= 64 run
+// on the tensor cores.
 bool grouped_gemm_device(int64_t count, const char *ta, const char *tb, const int64_t *m, const int64_t *n,
                          const int64_t *k, const mwblas_real64x2 *alpha, const mwblas_real64x2 *const *a,
                          const int64_t *lda, const mwblas_real64x2 *const *b, const int64_t *ldb,
                          const mwblas_real64x2 *beta, mwblas_real64x2 *const *c, const int64_t *ldc,
-                         const char *routine);
+                         int tensor_min, const char *routine);
 
 // y := alpha*op(A)*x + beta*y on device arrays (increments may be negative).
 bool gemv_device(bool trans, int64_t m, int64_t n, dd_host alpha, const void *A, int64_t lda, const void *x,

@@ -239,6 +239,37 @@ def test_mtrsm_merged_inverse_leaves(gpu, oracle, rng, side, uplo, ta, diag):
     assert err <= 1e-28, err   # well conditioned: far inside the reference's na^2 bound
 
 
+@pytest.mark.parametrize("side", ["L", "R"])
+@pytest.mark.parametrize("uplo", ["U", "L"])
+@pytest.mark.parametrize("ta", ["N", "T"])
+@pytest.mark.parametrize("diag", ["N", "U"])
+def test_mtrsm_512_leaves(gpu, oracle, rng, side, uplo, ta, diag):
+    """order >= 2048 with >= 512 right-hand sides: 512 x 512 leaf inverses,
+    the merges of 128 and 256 blocks on the tensor cores (grouped residue
+    GEMMs), the last leaf partial; 4 sampled right-hand sides against the
+    oracle."""
+    na, nr = 2100, 520
+    m, n = (na, nr) if side == "L" else (nr, na)
+    A = dominant_triangle(rng, na, na)
+    B0 = mwb.dd_matrix(rng, m, n, m)
+    al = mwb.random_dd(rng, ())
+    got = B0.copy()
+    gpu.mtrsm(side, uplo, ta, diag, m, n, al, A, na, got, m)
+    assert gpu.last_error()[0] == 0, gpu.last_error()
+    pick = np.sort(rng.choice(nr, 4, replace=False))
+    if side == "L":
+        sub = np.ascontiguousarray(B0[pick])
+        oracle.qtrsm("L", uplo, ta, diag, na, 4, al, A, na, sub, na)
+        g = got[pick]
+    else:
+        sub = np.ascontiguousarray(B0[:, pick])
+        oracle.qtrsm("R", uplo, ta, diag, 4, na, al, A, na, sub, 4)
+        g = got[:, pick]
+    err = orc.normwise_error(g, sub, orc.dd_abs(al) * orc.dd_absmax(B0))
+    assert err <= max(20, 8 * na * na) * orc.EPS_DD, err
+    assert err <= 1e-28, err
+
+
 @pytest.mark.parametrize("trans", ["N", "T"])
 def test_mgemv(gpu, oracle, rng, trans):
     for (m, n, incx, incy) in [(1, 1, 1, 1), (17, 9, 1, 1), (300, 70, 2, -1), (70, 300, -3, 2), (1000, 4000, 1, 1)]:
