@@ -1079,7 +1079,10 @@ def run_workload(args):
             metric = "batched DD-GEMM GFLOP/s, 20000 instances M,N,K log-uniform [8,512]"
             cfg = {"workload": "mgemm_grouped 20000 x NN, M,N,K ~ logU[8,512]", "split_k_min_chosen": chosen,
                    "tile_chosen": int(lib.lib.mwblas_grouped_tuned_tile()),
-                   "launch": "one persistent kernel from a cached CUDA graph"}
+                   "tensor_core_min_size_chosen": int(lib.lib.mwblas_grouped_tuned_tensor_min()),
+                   "launch": "one CUDA graph per batch layout: the persistent integer-pipe kernel for the small "
+                             "instances, the grouped tensor-core residue GEMMs (one per padding class) for those "
+                             "with m, n >= the chosen size and k >= 64"}
             if o:
                 arena.copy_(C0)
                 fn()
