@@ -833,8 +833,9 @@ extern "C" int mgemm_grouped(int64_t count, const char *transa, const char *tran
     return 0;
 }
 
-// Times tile edges (16, 32, 64) and then split-K policies on the caller's
-// batch (outputs go to scratch copies of C, the caller's C is not modified)
+// Times the tensor-core size threshold (none, 64, 128, 256), then tile edges
+// (16, 32, 64) and split-K policies for the rest, on the caller's batch
+// (outputs go to scratch copies of C, the caller's C is not modified)
 // and caches the fastest for batches of the same shape class. Returns 0 and
 // the chosen minimum K per split in *chosen (0 = no split); the chosen tile
 // edge is returned by mwblas_grouped_tuned_tile().
@@ -888,33 +889,33 @@ extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char 
         cudaEventElapsedTime(&ms, e0, e1);
         return ms;
     };
-    // stages: the tile edge (integer path only), the split policy at that
-    // tile, then the size from which instances run on the tensor cores
+    // stages: the size from which instances run on the tensor cores, then
+    // the tile edge of the rest (integer pipes), then its split policy
     float best = 1e30f;
     int best_tile = g_default_policy.tile, best_k = g_default_policy.min_k_per_split, best_oz = 0;
+    const int ozc[] = {0, 64, 128, 256};
+    for (int oz : ozc) {
+        if (oz > 0 && !ozaki_available()) break;
+        const float ms = time_policy(Policy{best_k, 4, best_tile, oz});
+        if (ms < best) {
+            best = ms;
+            best_oz = oz;
+        }
+    }
     for (int t : tiles) {
-        const float ms = time_policy(Policy{g_default_policy.min_k_per_split, 4, t, 0});
+        if (t == best_tile) continue;   // timed above
+        const float ms = time_policy(Policy{best_k, 4, t, best_oz});
         if (ms < best) {
             best = ms;
             best_tile = t;
         }
     }
     for (int cand : cands) {
-        if (cand == g_default_policy.min_k_per_split) continue;   // timed above
-        const float ms = time_policy(Policy{cand, 4, best_tile, 0});
+        if (cand == best_k) continue;   // timed above
+        const float ms = time_policy(Policy{cand, 4, best_tile, best_oz});
         if (ms < best) {
             best = ms;
             best_k = cand;
-        }
-    }
-    if (ozaki_available()) {
-        const int ozc[] = {64, 128, 256};
-        for (int oz : ozc) {
-            const float ms = time_policy(Policy{best_k, 4, best_tile, oz});
-            if (ms < best) {
-                best = ms;
-                best_oz = oz;
-            }
         }
     }
     cudaEventDestroy(e0);

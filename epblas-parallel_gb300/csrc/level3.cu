@@ -328,7 +328,7 @@ bool trsm_rec(bool left, bool lower, bool trans, bool unit, int64_t o, int64_t n
 
 // Copies the two half-block inverses into the diagonal of each merged block
 // and zeroes its off-diagonal triangle (upper right for lower, lower left for
-// upper). One CTA per merged block.
+// upper). CTAs (merged block, 32-column group).
 __global__ void k_inv_merge_copy(int64_t na, int64_t S, const double2 *__restrict__ src, double2 *__restrict__ dst,
                                  bool lower)
 {
@@ -341,7 +341,8 @@ __global__ void k_inv_merge_copy(int64_t na, int64_t S, const double2 *__restric
     const int nt = (int)(n1 + n2), n1i = (int)n1, hi = (int)h, Si = (int)S;
     // column per warp-strided loop, rows across the threads of a warp (coalesced)
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int c = wid; c < nt; c += nw) {
+    const int cend = min(nt, (int)(blockIdx.y + 1) * 32);
+    for (int c = (int)blockIdx.y * 32 + wid; c < cend; c += nw) {
         for (int r = lane; r < nt; r += 32) {
             double2 v = make_double2(0.0, 0.0);
             if (r < n1i && c < n1i) v = i1[r + c * hi];
@@ -361,7 +362,7 @@ bool trsm_merge_inverses(int64_t na, int64_t h, const void *A, int64_t lda, bool
 {
     const int64_t S = 2 * h;
     const int64_t nblk = (na + S - 1) / S;
-    k_inv_merge_copy<<<(unsigned)nblk, 256, 0, stream()>>>(na, S, src, dst, lower);
+    k_inv_merge_copy<<<dim3((unsigned)nblk, (unsigned)((S + 31) / 32)), 256, 0, stream()>>>(na, S, src, dst, lower);
     count_launch();
     std::vector<int64_t> m1, n1, k1, lda1, ldb1, ldc1, m2, n2, k2, lda2, ldb2, ldc2;
     std::vector<const mwblas_real64x2 *> a1, b1, a2, b2;

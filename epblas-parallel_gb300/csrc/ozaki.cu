@@ -1933,8 +1933,8 @@ struct OzGrpDesc {
     int cls, slot;
     int64_t ea_off, eb_off;   // row exponents of op(A), column exponents of op(B)
     int64_t line_begin;       // first exponent line: m rows of op(A), then n columns of op(B)
-    int64_t tile_begin;       // first conversion tile: op(A)'s (Mp/32)(Kp/32), then op(B)'s (Np/32)(Kp/32)
-    int64_t rec_begin;        // first reconstruction item: ceil(m/512) row slabs x ceil(n/8) column groups
+    int64_t tile_begin;       // first conversion tile: op(A)'s ceil(m/32) ceil(k/32), then op(B)'s ceil(n/32) ceil(k/32)
+    int64_t rec_begin;        // first reconstruction item: ceil(m/64) row slabs x ceil(n/8) column groups
     xw::XW aM, xb;            // alpha * M and beta as extended floats
     double2 beta;
     int beta_kind, pad;
@@ -1964,30 +1964,30 @@ __device__ __forceinline__ int grp_exp_bound(double x)
     return b == 0 ? kNoExp : (int)(b >> 52) - 1023;
 }
 
-// Exponent bound of every row of op(A) and column of op(B), thread per line.
+// Exponent bound of every row of op(A) and column of op(B): a warp per line,
+// lanes over its k entries.
 __global__ void k_grp_exp(const OzGrpDesc *__restrict__ descs, int count, int64_t lines, int *__restrict__ ex)
 {
-    for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < lines; w += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t w = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); w < lines; w += warps) {
         const OzGrpDesc &d = descs[grp_find(descs, count, w, 0)];
         const int64_t t = w - d.line_begin;
+        const bool row = t < d.m;   // row t of op(A), else column t - m of op(B)
+        const int64_t j = t - d.m;
+        const double2 *p = row ? (d.ta ? d.A + t * d.lda : d.A + t) : (d.tb ? d.B + j : d.B + j * d.ldb);
+        const int64_t step = row ? (d.ta ? 1 : d.lda) : (d.tb ? d.ldb : 1);
         int e = kNoExp;
-        if (t < d.m) {   // row t of op(A)
-            const double2 *p = d.ta ? d.A + t * d.lda : d.A + t;
-            const int64_t step = d.ta ? 1 : d.lda;
-            for (int q = 0; q < d.k; ++q, p += step) e = max(e, grp_exp_bound(p->x));
-            ex[d.ea_off + t] = e;
-        } else {         // column t - m of op(B)
-            const int64_t j = t - d.m;
-            const double2 *p = d.tb ? d.B + j : d.B + j * d.ldb;
-            const int64_t step = d.tb ? d.ldb : 1;
-            for (int q = 0; q < d.k; ++q, p += step) e = max(e, grp_exp_bound(p->x));
-            ex[d.eb_off + j] = e;
-        }
+        for (int q = lane; q < d.k; q += 32) e = max(e, grp_exp_bound(p[q * step].x));
+        for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_down_sync(0xffffffffu, e, off));
+        if (lane == 0) ex[row ? d.ea_off + t : d.eb_off + j] = e;
     }
 }
 
 // Residues of op(A) and op(B) of every instance into its class planes, one
-// 32 x 32 tile (padding included: zeros) per block and step.
+// 32 x 32 tile per block and step. Tiles cover each operand's own rows and k
+// (rounded up to 32, the excess filled with zeros); the rest of the class
+// padding is zeroed once when the plan is prepared and never written.
 __global__ void __launch_bounds__(256) k_grp_residues(const OzGrpDesc *__restrict__ descs, int count, int64_t tiles,
                                                       const OzGrpClass *__restrict__ classes, const int *__restrict__ ex,
                                                       int bits, OzResParams P)
@@ -2007,7 +2007,8 @@ __global__ void __launch_bounds__(256) k_grp_residues(const OzGrpDesc *__restric
     for (int64_t w = blockIdx.x; w < tiles; w += gridDim.x) {
         const OzGrpDesc &d = descs[grp_find(descs, count, w, 1)];
         const OzGrpClass &c = classes[d.cls];
-        const int64_t ntc = c.Kp / 32, ta_tiles = (c.Mp / 32) * ntc;
+        // tiles cover op(X)'s own rows and k (the class padding was zeroed once)
+        const int64_t ntc = (d.k + 31) / 32, ta_tiles = ((d.m + 31) / 32) * ntc;
         int64_t t = w - d.tile_begin;
         const bool isA = t < ta_tiles;
         if (!isA) t -= ta_tiles;
@@ -2037,8 +2038,9 @@ __global__ void __launch_bounds__(256) k_grp_residues(const OzGrpDesc *__restric
     }
 }
 
-// alpha * X * 2^-S2 + beta C for every instance: a thread per row pair of a
-// 512-row slab and 8 columns per work item.
+// alpha * X * 2^-S2 + beta C for every instance. A work item is 64 rows x 8
+// columns of one instance; thread t takes the row pair t % 32 of column t / 32
+// (the 32 threads of a column read consecutive residue words).
 __global__ void __launch_bounds__(256) k_grp_reconstruct(const OzGrpDesc *__restrict__ descs, int count,
                                                          int64_t items, const OzGrpClass *__restrict__ classes,
                                                          const int *__restrict__ ex, int bsum, OzCrtParams K)
@@ -2051,17 +2053,16 @@ __global__ void __launch_bounds__(256) k_grp_reconstruct(const OzGrpDesc *__rest
         const OzGrpDesc &d = descs[grp_find(descs, count, w, 2)];
         const OzGrpClass &c = classes[d.cls];
         const int64_t t = w - d.rec_begin, ncg = (d.n + 7) / 8;
-        const int slab = (int)(t / ncg), j0 = (int)(t % ncg) * 8;
-        const int i0 = slab * 512 + 2 * threadIdx.x;
-        if (i0 >= d.m) continue;
+        const int slab = (int)(t / ncg), j = (int)(t % ncg) * 8 + (threadIdx.x >> 5);
+        const int i0 = slab * 64 + 2 * (threadIdx.x & 31);
+        if (i0 >= d.m || j >= d.n) continue;
         const bool two = i0 + 1 < d.m;
         const int ea0 = ex[d.ea_off + i0], ea1 = two ? ex[d.ea_off + i0 + 1] : kNoExp;
         const int64_t plane = c.Np * c.Mp;
         const uint16_t *R0 = c.R + (int64_t)d.slot * nmod * plane + i0;
         const dd::real beta = dd::make(d.beta.x, d.beta.y);
-        for (int j = j0; j < min(d.n, j0 + 8); ++j)
-            reconstruct_pair(sm, nmod, R0 + (int64_t)j * c.Mp, plane, i0, two, ea0, ea1, j, ex[d.eb_off + j], bsum,
-                             d.aM, d.xb, beta, d.beta_kind, d.C + i0 + (int64_t)j * d.ldc, 0);
+        reconstruct_pair(sm, nmod, R0 + (int64_t)j * c.Mp, plane, i0, two, ea0, ea1, j, ex[d.eb_off + j], bsum,
+                         d.aM, d.xb, beta, d.beta_kind, d.C + i0 + (int64_t)j * d.ldc, 0);
     }
 }
 
@@ -2176,9 +2177,10 @@ bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, con
         d.line_begin = pl->lines;
         pl->lines += it.m + it.n;
         d.tile_begin = pl->tiles;
-        pl->tiles += (c.Mp / 32 + c.Np / 32) * (c.Kp / 32);
+        pl->tiles += ((it.m + 31) / 32 + (it.n + 31) / 32) * ((it.k + 31) / 32);
         d.rec_begin = pl->items;
-        pl->items += ((it.m + 511) / 512) * ((it.n + 7) / 8);
+        pl->items += ((it.m + 63) / 64) * ((it.n + 7) / 8);
+        (void)c;
         const bool alpha_one = it.alpha.hi == 1.0 && it.alpha.lo == 0.0;
         d.aM = alpha_one ? Mx : xw::mul(xw::from_dd(it.alpha.hi, it.alpha.lo), Mx);
         d.xb = xw::from_dd(it.beta.hi, it.beta.lo);
@@ -2222,6 +2224,11 @@ bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, con
         c.R = (uint16_t *)p;
         if (!make_map(&pl->maps[2 * ci], c.Ares, (uint64_t)c.Kp, (uint64_t)(planes * c.Mp), TC_BM, routine) ||
             !make_map(&pl->maps[2 * ci + 1], c.Bres, (uint64_t)c.Kp, (uint64_t)(planes * c.Np), 128, routine))
+            return false;
+        // the padding of the residue planes (rows past m or n, k past the 32-rounded k) is never
+        // converted: zero it once
+        if (!cuda_ok(cudaMemsetAsync(c.Ares, 0, (char *)c.R - (char *)c.Ares, stream()), routine,
+                     "grouped residue clear"))
             return false;
     }
     cudaFuncSetAttribute(k_oz_gemm_tc_2sm, cudaFuncAttributeMaxDynamicSharedMemorySize, T2_SMEM);
