@@ -1201,6 +1201,37 @@ __device__ __forceinline__ bool finite_hi(double x)
     return ((__double2hiint(x) >> 20) & 0x7FF) != 0x7FF;   // exponent field test, no FP64 compare
 }
 
+// Triangular outputs (uplo 1: i <= j, 2: i >= j) are walked as a list of
+// (row slab x, column j) tasks holding stored entries: slab x (rows
+// [S x, S x + S)) needs columns [S x, n) of an upper triangle and
+// [0, min(n, S x + S)) of a lower one. The blocks of a grid stride over that
+// list, so every block gets about the same share of the triangle (a slab per
+// block and all columns would leave the top slabs of an upper triangle with
+// 16 times the work of the bottom ones at n = 8192).
+__device__ __forceinline__ int64_t tri_prefix(int uplo, int64_t x, int64_t n, int64_t S)
+{
+    if (uplo == 1) {   // sum over x' < x of n - min(n, S x')
+        const int64_t q = min(x, (n + S - 1) / S);
+        return q * n - S * q * (q - 1) / 2;
+    }
+    const int64_t qf = n / S;   // sum over x' < x of min(n, S (x' + 1)); the first qf terms are S (x' + 1)
+    const int64_t q = min(x, qf);
+    return S * q * (q + 1) / 2 + max((int64_t)0, x - qf) * n;
+}
+
+__device__ __forceinline__ void tri_task(int uplo, int64_t t, int64_t slabs, int64_t n, int64_t S, int64_t &x,
+                                         int64_t &j)
+{
+    int64_t lo = 0, hi = slabs - 1;   // the first slab whose tasks extend past t
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (tri_prefix(uplo, mid + 1, n, S) > t) hi = mid;
+        else lo = mid + 1;
+    }
+    x = lo;
+    j = t - tri_prefix(uplo, x, n, S) + (uplo == 1 ? min(n, S * x) : 0);
+}
+
 // Output rows i0 and i0 + 1 (when `two`) of column j: the CRT sums of their
 // residues over the nmod planes (rcol points at row i0, column j of plane 0;
 // planes `plane` entries apart), then alpha M (folded into Mx), the power-of-
@@ -1289,12 +1320,27 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct(int m, int n, const uint
     __shared__ CrtSmem sm;
     crt_smem_fill(sm, K);
     __syncthreads();
+    const int nmod = K.nmod;
+    const int64_t plane = Np * Mp;
+    if (uplo != 0) {
+        // a triangle: (512-row slab, column) tasks shared evenly by all blocks
+        const int64_t S = 2 * (int64_t)blockDim.x, slabs = (m + S - 1) / S, total = tri_prefix(uplo, slabs, n, S);
+        for (int64_t t = (int64_t)blockIdx.y * gridDim.x + blockIdx.x; t < total;
+             t += (int64_t)gridDim.x * gridDim.y) {
+            int64_t x, j;
+            tri_task(uplo, t, slabs, n, S, x, j);
+            const int i0 = (int)(x * S) + 2 * threadIdx.x;
+            if (i0 >= m) continue;
+            const bool two = i0 + 1 < m;
+            reconstruct_pair(sm, nmod, R + j * Mp + i0, plane, i0, two, ea[i0], two ? ea[i0 + 1] : kNoExp, (int)j,
+                             eb[j], bsum, Mx, xb, beta, beta_kind, C + i0 + j * ldc, uplo);
+        }
+        return;
+    }
     const int i0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
     if (i0 >= m) return;
-    const int nmod = K.nmod;
     const bool two = i0 + 1 < m;
     const int ea0 = ea[i0], ea1 = two ? ea[i0 + 1] : kNoExp;
-    const int64_t plane = Np * Mp;
     const int jstep = gridDim.y;
     const uint16_t *rcol = R + (int64_t)blockIdx.y * Mp + i0;
     double2 *pc = C + i0 + (int64_t)blockIdx.y * ldc;
@@ -1316,18 +1362,17 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
     __shared__ CrtSmem sm;
     crt_smem_fill(sm, K);
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m) return;
     const int nmod = K.nmod;
     const int64_t cstride = (int64_t)nmod * Np * Mp;
-    for (int j = blockIdx.y; j < n; j += gridDim.y) {
-        if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) continue;
+    // output (i, j)
+    auto one = [&](const int i, const int j) {
+        if ((uplo == 1 && i > j) || (uplo == 2 && i < j)) return;
         if (ea[i] >= 1024 || eb[j] >= 1024) {
             const double qnan = __longlong_as_double(0x7ff8000000000000ll);
             double2 *pc = C + 2 * (i + (int64_t)j * ldc);
             pc[0] = make_double2(qnan, qnan);
             pc[1] = make_double2(qnan, qnan);
-            continue;
+            return;
         }
         xw::XW vr, vi;
         vr = vi = xw::zero();
@@ -1392,7 +1437,7 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
                 out.im = dd::add_exact(c0.im, xw_dd(ri));
                 if (herm && i == j) out.im = dd::make(0.0, 0.0);
                 dd::cstore(pc, out);
-                continue;
+                return;
             }
             xw::XW cr = xw::from_dd(c0r.x, c0r.y), ci = xw::from_dd(c0i.x, c0i.y);
             if (beta_kind == 2) {
@@ -1415,7 +1460,22 @@ __global__ void __launch_bounds__(256) k_oz_reconstruct_c(int m, int n, const ui
         out.re = xw_dd(rr);
         out.im = (herm && i == j) ? dd::make(0.0, 0.0) : xw_dd(ri);
         dd::cstore(pc, out);
+    };
+    if (uplo != 0) {
+        // a triangle: (256-row slab, column) tasks shared evenly by all blocks
+        const int64_t S = blockDim.x, slabs = (m + S - 1) / S, total = tri_prefix(uplo, slabs, n, S);
+        for (int64_t t = (int64_t)blockIdx.y * gridDim.x + blockIdx.x; t < total;
+             t += (int64_t)gridDim.x * gridDim.y) {
+            int64_t x, j;
+            tri_task(uplo, t, slabs, n, S, x, j);
+            const int i = (int)(x * S) + threadIdx.x;
+            if (i < m) one(i, (int)j);
+        }
+        return;
     }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    for (int j = blockIdx.y; j < n; j += gridDim.y) one(i, j);
 }
 
 // ---- host ---------------------------------------------------------------------------------
