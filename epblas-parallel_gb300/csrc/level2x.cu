@@ -133,7 +133,6 @@ __global__ void k_pack(int64_t n, double2 *AP, int e2, bool upper, double2 *dens
 // Kernel parameters of smv_device (vectors contiguous).
 struct SmvParams {
     int64_t rows, cols, n, kl, ku, ldab;
-    int64_t col0;        // band storage: first column held at A (0, or the first staged column)
     const double2 *A;
     int fmt, kind, op;   // op 0 'N', 1 'T', 2 'C'
     bool upper, unit;
@@ -184,7 +183,7 @@ __device__ __forceinline__ int64_t smv_addr(const SmvParams &p, int64_t i, int64
 {
     if (p.fmt == 0) return i + j * p.ldab;
     if (p.fmt == 2) return p.upper ? i + j * (j + 1) / 2 : i + j * (2 * p.n - j - 1) / 2;
-    return (p.ku + i - j) + (j - p.col0) * p.ldab;
+    return (p.ku + i - j) + j * p.ldab;
 }
 
 template <bool CX>
@@ -247,118 +246,86 @@ __device__ __forceinline__ double2 smv_round(dd::real b, bool have_b, xfp::XF t)
     return make_double2(h, l);
 }
 
-// Row r of op(A) (or, with T = 32, this lane's share of it; lane 0 writes y).
-template <bool CX, int T>
-__device__ __forceinline__ void smv_row(const SmvParams &p, int64_t r, int lane)
-{
-    const double nan = __longlong_as_double(0x7ff8000000000000ll);
-    int64_t c0, c1;
-    smv_range(p, r, c0, c1);
-    fx::Acc acc[CX ? 2 : 1];
-    xfp::XF tot[CX ? 2 : 1];
-    bool bad = false;
-    for (int w = 0; w < (CX ? 2 : 1); ++w) {
-        acc[w].reset();
-        tot[w] = xzero();
-    }
-    int cnt = 0;
-    for (int64_t c = c0 + lane; c <= c1; c += T) {
-        fx::Op er, ei;
-        smv_elem<CX>(p, r, c, er, ei);
-        if (CX) {
-            const fx::Dig xr = p.xd[2 * c], xi = p.xd[2 * c + 1];
-            fx::Op nei = ei;
-            nei.flags ^= fx::kNeg;
-            acc[0].add_dig(er, xr);
-            acc[0].add_dig(nei, xi);
-            acc[1].add_dig(er, xi);
-            acc[1].add_dig(ei, xr);
-            cnt += 2;
-        } else {
-            acc[0].add_dig(er, p.xd[c]);
-            ++cnt;
-        }
-        if (cnt >= fx::kMaxAdds - 2) {
-            for (int w = 0; w < (CX ? 2 : 1); ++w) {
-                bad |= acc[w].bad;
-                tot[w] = xfp::xf_add(tot[w], acc[w].finish());
-                acc[w].reset();
-            }
-            cnt = 0;
-        }
-    }
-    for (int w = 0; w < (CX ? 2 : 1); ++w) {
-        bad |= acc[w].bad;
-        tot[w] = xfp::xf_add(tot[w], acc[w].finish());
-        if (T == 32) tot[w] = fx::xf_warp_sum(tot[w]);
-    }
-    if (T == 32) bad = __any_sync(0xffffffffu, bad);
-    if (lane != 0) return;
-    double2 *py = p.y + (CX ? 2 : 1) * r;
-    if (bad) {
-        py[0] = make_double2(nan, nan);
-        if (CX) py[1] = make_double2(nan, nan);
-        return;
-    }
-    const xfp::XF xar = xfp::xf_from_dd(p.ar.hi, p.ar.lo);
-    if (!CX) {
-        dd::real b = dd::make(0.0, 0.0);
-        if (p.beta_kind == 1) b = dd::load(py);
-        else if (p.beta_kind == 2) b = dd::mul_exact(p.br, dd::load(py));
-        py[0] = smv_round(b, p.beta_kind != 0, xfp::xf_mul(xar, tot[0]));
-    } else {
-        const xfp::XF xai = xfp::xf_from_dd(p.ai.hi, p.ai.lo);
-        const xfp::XF tr = xfp::xf_add(xfp::xf_mul(xar, tot[0]), xneg(xfp::xf_mul(xai, tot[1])));
-        const xfp::XF ti = xfp::xf_add(xfp::xf_mul(xar, tot[1]), xfp::xf_mul(xai, tot[0]));
-        dd::cplx b;
-        b.re = b.im = dd::make(0.0, 0.0);
-        if (p.beta_kind == 1) {
-            b = dd::cload(py);
-        } else if (p.beta_kind == 2) {
-            dd::cplx be;
-            be.re = p.br;
-            be.im = p.bi;
-            b = dd::cmul_exact(be, dd::cload(py));
-        }
-        const double2 yr = smv_round(b.re, p.beta_kind != 0, tr);
-        const double2 yi = smv_round(b.im, p.beta_kind != 0, ti);
-        py[0] = yr;
-        py[1] = yi;
-    }
-}
-
 template <bool CX, int T>
 __global__ void __launch_bounds__(256) k_smv(SmvParams p)
 {
+    const double nan = __longlong_as_double(0x7ff8000000000000ll);
     const int lane = T == 1 ? 0 : (threadIdx.x & 31);
     const int64_t teams = (int64_t)gridDim.x * blockDim.x / T;
-    for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / T; r < p.rows; r += teams)
-        smv_row<CX, T>(p, r, lane);
-}
-
-// Band formats, a thread per row: a block takes 256 consecutive rows, whose
-// stored entries lie in band columns [r0 - K, r0 + 256 + K) (K the wider
-// half-bandwidth), one contiguous stretch of the band storage. The block
-// copies it into shared memory with coalesced loads and the rows read their
-// entries there (a thread per row reading the band in place touches a
-// different line per lane).
-template <bool CX>
-__global__ void __launch_bounds__(256) k_smv_band_staged(SmvParams p, int64_t K, int64_t scols)
-{
-    extern __shared__ __align__(16) double2 smv_stage[];
-    constexpr int E = CX ? 2 : 1;
-    for (int64_t r0 = (int64_t)blockIdx.x * 256; r0 < p.rows; r0 += (int64_t)gridDim.x * 256) {
-        const int64_t jlo = max((int64_t)0, r0 - K), jhi = min(scols, r0 + 256 + K);
-        const int64_t cnt = (jhi - jlo) * p.ldab * E;
-        const double2 *src = p.A + jlo * p.ldab * E;
-        __syncthreads();   // the previous rows are done with the stage
-        for (int64_t t = threadIdx.x; t < cnt; t += blockDim.x) smv_stage[t] = src[t];
-        __syncthreads();
-        SmvParams ps = p;
-        ps.A = smv_stage;
-        ps.col0 = jlo;
-        const int64_t r = r0 + threadIdx.x;
-        if (r < p.rows) smv_row<CX, 1>(ps, r, 0);
+    for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / T; r < p.rows; r += teams) {
+        int64_t c0, c1;
+        smv_range(p, r, c0, c1);
+        fx::Acc acc[CX ? 2 : 1];
+        xfp::XF tot[CX ? 2 : 1];
+        bool bad = false;
+        for (int w = 0; w < (CX ? 2 : 1); ++w) {
+            acc[w].reset();
+            tot[w] = xzero();
+        }
+        int cnt = 0;
+        for (int64_t c = c0 + lane; c <= c1; c += T) {
+            fx::Op er, ei;
+            smv_elem<CX>(p, r, c, er, ei);
+            if (CX) {
+                const fx::Dig xr = p.xd[2 * c], xi = p.xd[2 * c + 1];
+                fx::Op nei = ei;
+                nei.flags ^= fx::kNeg;
+                acc[0].add_dig(er, xr);
+                acc[0].add_dig(nei, xi);
+                acc[1].add_dig(er, xi);
+                acc[1].add_dig(ei, xr);
+                cnt += 2;
+            } else {
+                acc[0].add_dig(er, p.xd[c]);
+                ++cnt;
+            }
+            if (cnt >= fx::kMaxAdds - 2) {
+                for (int w = 0; w < (CX ? 2 : 1); ++w) {
+                    bad |= acc[w].bad;
+                    tot[w] = xfp::xf_add(tot[w], acc[w].finish());
+                    acc[w].reset();
+                }
+                cnt = 0;
+            }
+        }
+        for (int w = 0; w < (CX ? 2 : 1); ++w) {
+            bad |= acc[w].bad;
+            tot[w] = xfp::xf_add(tot[w], acc[w].finish());
+            if (T == 32) tot[w] = fx::xf_warp_sum(tot[w]);
+        }
+        if (T == 32) bad = __any_sync(0xffffffffu, bad);
+        if (lane != 0) continue;
+        double2 *py = p.y + (CX ? 2 : 1) * r;
+        if (bad) {
+            py[0] = make_double2(nan, nan);
+            if (CX) py[1] = make_double2(nan, nan);
+            continue;
+        }
+        const xfp::XF xar = xfp::xf_from_dd(p.ar.hi, p.ar.lo);
+        if (!CX) {
+            dd::real b = dd::make(0.0, 0.0);
+            if (p.beta_kind == 1) b = dd::load(py);
+            else if (p.beta_kind == 2) b = dd::mul_exact(p.br, dd::load(py));
+            py[0] = smv_round(b, p.beta_kind != 0, xfp::xf_mul(xar, tot[0]));
+        } else {
+            const xfp::XF xai = xfp::xf_from_dd(p.ai.hi, p.ai.lo);
+            const xfp::XF tr = xfp::xf_add(xfp::xf_mul(xar, tot[0]), xneg(xfp::xf_mul(xai, tot[1])));
+            const xfp::XF ti = xfp::xf_add(xfp::xf_mul(xar, tot[1]), xfp::xf_mul(xai, tot[0]));
+            dd::cplx b;
+            b.re = b.im = dd::make(0.0, 0.0);
+            if (p.beta_kind == 1) {
+                b = dd::cload(py);
+            } else if (p.beta_kind == 2) {
+                dd::cplx be;
+                be.re = p.br;
+                be.im = p.bi;
+                b = dd::cmul_exact(be, dd::cload(py));
+            }
+            const double2 yr = smv_round(b.re, p.beta_kind != 0, tr);
+            const double2 yi = smv_round(b.im, p.beta_kind != 0, ti);
+            py[0] = yr;
+            py[1] = yi;
+        }
     }
 }
 
@@ -732,7 +699,6 @@ bool smv_device(const SmvArgs &a, const char *routine)
     p.kl = a.kl;
     p.ku = a.ku;
     p.ldab = a.ldab;
-    p.col0 = 0;
     p.A = (const double2 *)a.A;
     p.fmt = a.fmt;
     p.kind = a.kind;
@@ -765,23 +731,7 @@ bool smv_device(const SmvArgs &a, const char *routine)
     const int64_t cap = (int64_t)device_sm_count() * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    // band formats with short rows: 256 rows per block staged through shared
-    // memory when their stretch of the band storage fits in 96 KB
-    const int64_t K = a.kl > a.ku ? a.kl : a.ku;
-    const int64_t scols = a.kind == 0 ? (p.op == 0 ? a.cols : a.rows) : a.n;
-    const size_t stage_bytes = (size_t)(256 + 2 * K) * (size_t)a.ldab * 16 * e2;
-    const bool staged = a.fmt == 1 && !warp && stage_bytes <= 96 * 1024 && a.ldab > 0;
-    if (staged) {
-        int64_t sblocks = (a.rows + 255) / 256;
-        if (sblocks > cap) sblocks = cap;
-        if (a.cplx) {
-            cudaFuncSetAttribute(k_smv_band_staged<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-            k_smv_band_staged<true><<<(unsigned)sblocks, 256, stage_bytes, stream()>>>(p, K, scols);
-        } else {
-            cudaFuncSetAttribute(k_smv_band_staged<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-            k_smv_band_staged<false><<<(unsigned)sblocks, 256, stage_bytes, stream()>>>(p, K, scols);
-        }
-    } else if (a.cplx) {
+    if (a.cplx) {
         if (warp) k_smv<true, 32><<<(unsigned)blocks, 256, 0, stream()>>>(p);
         else k_smv<true, 1><<<(unsigned)blocks, 256, 0, stream()>>>(p);
     } else {
