@@ -293,3 +293,59 @@ def test_symmetric_rank_updates(gpu, oracle, rng, name, uplo):
         assert gpu.last_error()[0] == 0, gpu.last_error()
         scale = 2 * orc.dd_abs(al) * orc.dd_absmax(x) * orc.dd_absmax(y if two else x) + orc.dd_absmax(A)
         assert err_ok(got, want, scale, 10 * orc.EPS_DD), (n,)
+
+
+def _padded(AB, ldab):
+    """Band storage with ldab rows per column (the band in the first rows)."""
+    out = np.zeros((AB.shape[0], ldab) + AB.shape[2:])
+    out[:, :AB.shape[1]] = AB
+    return np.ascontiguousarray(out)
+
+
+@pytest.mark.parametrize("c", [False, True])
+@pytest.mark.parametrize("uplo", ["U", "L"])
+def test_band_rows_over_many_blocks(gpu, oracle, rng, c, uplo):
+    """A symmetric (Hermitian) band product over many row blocks, read in
+    place from band storage with a tight and with a padded leading dimension:
+    both agree bit for bit and with the oracle."""
+    name = "whbmv" if c else "msbmv"
+    n, k = 1100, 7
+    A = dense(rng, n, n, c)
+    S = band_keep(sym_from_tri(A, n, uplo, c), k, k)
+    kl, ku = (0, k) if uplo == "U" else (k, 0)
+    AB = np.ascontiguousarray(to_band(S, kl, ku))
+    ix, iy = 1, -2
+    x, y = vecs(rng, n, ix, c), vecs(rng, n, iy, c)
+    al, be = scal(rng, c), scal(rng, c)
+    outs = []
+    for ldab in (k + 1, k + 1 + 400):
+        got = y.copy()
+        gpu.l2(name, uplo, n, k, al, _padded(AB, ldab), ldab, x, ix, be, got, iy)
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        outs.append(got)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    want = matvec(oracle, c, "N", np.ascontiguousarray(S), n, n, gather(x, n, ix), al, be, gather(y, n, iy))
+    scale = orc.dd_abs(al) * n * orc.dd_absmax(S) * orc.dd_absmax(x) + orc.dd_abs(be) * orc.dd_absmax(y)
+    assert err_ok(gather(outs[0], n, iy), want, scale, max(10, 4 * n) * orc.EPS_DD)
+
+
+@pytest.mark.parametrize("trans", ["N", "T"])
+def test_general_band_rows_over_many_blocks(gpu, oracle, rng, trans):
+    """GBMV with op(A) = A and A^T over many row blocks, tight and padded
+    leading dimension."""
+    m, n, kl, ku = 700, 900, 3, 6
+    F = band_keep(dense(rng, m, n, False), kl, ku)
+    AB = np.ascontiguousarray(to_band(F, kl, ku))
+    lx, ly = (n, m) if trans == "N" else (m, n)
+    x, y = vecs(rng, lx, 1, False), vecs(rng, ly, 1, False)
+    al, be = scal(rng, False), scal(rng, False)
+    outs = []
+    for ldab in (kl + ku + 1, kl + ku + 1 + 500):
+        got = y.copy()
+        gpu.l2("mgbmv", trans, m, n, kl, ku, al, _padded(AB, ldab), ldab, x, 1, be, got, 1)
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        outs.append(got)
+    np.testing.assert_array_equal(outs[0], outs[1])
+    want = matvec(oracle, False, trans, F, ly, lx, x, al, be, y)
+    scale = orc.dd_abs(al) * lx * orc.dd_absmax(F) * orc.dd_absmax(x) + orc.dd_abs(be) * orc.dd_absmax(y)
+    assert err_ok(outs[0], want, scale, max(10, 4 * max(m, n)) * orc.EPS_DD)
