@@ -444,6 +444,7 @@ struct Policy {
     int max_tiles_split = 4;   // split only instances with at most this many tiles
     int tile = 32;             // output tile edge: 16, 32 or 64
     int oz_min = 0;            // instances with m, n >= oz_min and k >= 64 run on the tensor cores (0: none)
+    int pack_k = 0;            // the other instances with m, n <= 256 and k >= pack_k share tensor-core slots (0: none)
 };
 
 struct Plan {
@@ -461,11 +462,13 @@ struct Plan {
 
 std::mutex g_batched_mu;
 std::map<uint64_t, Policy> g_policy_cache;   // shape class -> tuned policy
-Policy g_default_policy{512, 4, 32, 128};
+Policy g_default_policy{512, 4, 32, 128, 0};
 thread_local int t_tuned_tile = 0;   // tile chosen by this thread's most recent tuning
 thread_local int t_tuned_oz = -1;    // tensor-core threshold chosen by it (0: none)
 std::atomic<int> g_forced_tile{0};   // mwblas_set_grouped_tile: 0 = tuned or default
 std::atomic<int> g_forced_oz{-1};    // mwblas_set_grouped_tensor_min: -1 = tuned or default
+std::atomic<int> g_forced_pack{-1};  // mwblas_set_grouped_tensor_pack: -1 = tuned or default
+thread_local int t_tuned_pack = -1;  // shared-slot depth chosen by this thread's most recent tuning
 thread_local Plan t_plan;
 
 uint64_t mix(uint64_t h, uint64_t v)
@@ -501,6 +504,7 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
     pl.descs.reserve((size_t)count);
     pl.oz_items.clear();
     const int oz_min = (pol.oz_min > 0 && ozaki_available()) ? pol.oz_min : 0;
+    const int pack_k = (pol.pack_k > 0 && ozaki_available()) ? pol.pack_k : 0;
     const int GT = pol.tile;
     pl.tile = GT;
     int64_t work = 0, stiles = 0, pslots = 0;
@@ -523,8 +527,9 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
         d.beta = make_double2(beta[i].limbs[0], beta[i].limbs[1]);
         const bool alpha0 = (d.alpha.x == 0.0 && d.alpha.y == 0.0);
         d.beta_kind = (d.beta.x == 0.0 && d.beta.y == 0.0) ? 0 : ((d.beta.x == 1.0 && d.beta.y == 0.0) ? 1 : 2);
-        if (oz_min > 0 && !alpha0 && d.m >= oz_min && d.n >= oz_min && d.k >= 64 && d.k <= 16384 && d.m <= 8192 &&
-            d.n <= 8192) {
+        const bool own_slot = oz_min > 0 && d.m >= oz_min && d.n >= oz_min && d.k >= 64;
+        const bool shared_slot = pack_k > 0 && d.m <= 256 && d.n <= 256 && d.k >= pack_k;
+        if (!alpha0 && (own_slot || shared_slot) && d.k <= 16384 && d.m <= 8192 && d.n <= 8192) {
             OzGroupItem it;
             memset(&it, 0, sizeof(it));   // the plan key hashes the bytes, padding included
             it.A = d.A; it.B = d.B; it.C = d.C;
@@ -534,6 +539,7 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
             it.alpha = dd_host{d.alpha.x, d.alpha.y};
             it.beta = dd_host{d.beta.x, d.beta.y};
             it.beta_kind = d.beta_kind;
+            it.pack = own_slot ? 0 : 1;
             pl.oz_items.push_back(it);
             continue;
         }
@@ -826,6 +832,7 @@ extern "C" int mgemm_grouped(int64_t count, const char *transa, const char *tran
     }
     if (g_forced_tile.load() > 0) pol.tile = g_forced_tile.load();
     if (g_forced_oz.load() >= 0) pol.oz_min = g_forced_oz.load();
+    if (g_forced_pack.load() >= 0) pol.pack_k = g_forced_pack.load();
     Plan &pl = t_plan;
     build_descs(pl, count, transa, transb, m, n, k, alpha, a, lda, b, ldb, beta, c, ldc, pol);
     if (!prepare_and_launch(pl, routine)) return mwblas_last_error();
@@ -833,8 +840,10 @@ extern "C" int mgemm_grouped(int64_t count, const char *transa, const char *tran
     return 0;
 }
 
-// Times the tensor-core size threshold (none, 64, 128, 256), then tile edges
-// (16, 32, 64) and split-K policies for the rest, on the caller's batch
+// Times the tensor-core size threshold (none, 64, 128, 256), the depth from
+// which the remaining small instances share tensor-core slots (none, 16, 32,
+// 64), then tile edges (16, 32, 64) and split-K policies for the rest, on the
+// caller's batch
 // (outputs go to scratch copies of C, the caller's C is not modified)
 // and caches the fastest for batches of the same shape class. Returns 0 and
 // the chosen minimum K per split in *chosen (0 = no split); the chosen tile
@@ -889,22 +898,33 @@ extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char 
         cudaEventElapsedTime(&ms, e0, e1);
         return ms;
     };
-    // stages: the size from which instances run on the tensor cores, then
-    // the tile edge of the rest (integer pipes), then its split policy
+    // stages: the size from which instances run on the tensor cores, the
+    // depth from which the smaller ones share slots there, then the tile edge
+    // of the rest (integer pipes), then its split policy
     float best = 1e30f;
     int best_tile = g_default_policy.tile, best_k = g_default_policy.min_k_per_split, best_oz = 0;
     const int ozc[] = {0, 64, 128, 256};
     for (int oz : ozc) {
         if (oz > 0 && !ozaki_available()) break;
-        const float ms = time_policy(Policy{best_k, 4, best_tile, oz});
+        const float ms = time_policy(Policy{best_k, 4, best_tile, oz, 0});
         if (ms < best) {
             best = ms;
             best_oz = oz;
         }
     }
+    int best_pack = 0;
+    const int packc[] = {16, 32, 64};
+    for (int pk : packc) {
+        if (!ozaki_available()) break;
+        const float ms = time_policy(Policy{best_k, 4, best_tile, best_oz, pk});
+        if (ms < best) {
+            best = ms;
+            best_pack = pk;
+        }
+    }
     for (int t : tiles) {
         if (t == best_tile) continue;   // timed above
-        const float ms = time_policy(Policy{best_k, 4, t, best_oz});
+        const float ms = time_policy(Policy{best_k, 4, t, best_oz, best_pack});
         if (ms < best) {
             best = ms;
             best_tile = t;
@@ -912,7 +932,7 @@ extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char 
     }
     for (int cand : cands) {
         if (cand == best_k) continue;   // timed above
-        const float ms = time_policy(Policy{cand, 4, best_tile, best_oz});
+        const float ms = time_policy(Policy{cand, 4, best_tile, best_oz, best_pack});
         if (ms < best) {
             best = ms;
             best_k = cand;
@@ -926,9 +946,10 @@ extern "C" int mgemm_grouped_tune(int64_t count, const char *transa, const char 
     cudaFree(scratch);
     {
         std::lock_guard<std::mutex> lk(g_batched_mu);
-        g_policy_cache[shape_class(count, m, n, k)] = Policy{best_k, 4, best_tile, best_oz};
+        g_policy_cache[shape_class(count, m, n, k)] = Policy{best_k, 4, best_tile, best_oz, best_pack};
     }
     t_tuned_oz = best_oz;
+    t_tuned_pack = best_pack;
     t_tuned_tile = best_tile;
     if (chosen) *chosen = best_k;
     return finish(routine) ? 0 : mwblas_last_error();
@@ -1011,6 +1032,12 @@ extern "C" int mtrsm_grouped(int64_t count, char side, char uplo, char transa, c
 
 extern "C" int mwblas_grouped_tuned_tile(void) { return mw::t_tuned_tile; }
 extern "C" int mwblas_grouped_tuned_tensor_min(void) { return mw::t_tuned_oz; }
+extern "C" int mwblas_grouped_tuned_tensor_pack(void) { return mw::t_tuned_pack; }
+
+extern "C" int mwblas_set_grouped_tensor_pack(int kmin)
+{
+    return mw::g_forced_pack.exchange(kmin < 0 ? -1 : kmin);
+}
 
 extern "C" int mwblas_set_grouped_tensor_min(int size)
 {

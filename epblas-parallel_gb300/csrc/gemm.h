@@ -48,7 +48,7 @@ bool gemm_ozaki_cplx(const GemmArgs &g, int bits, const char *routine);
 void set_plain_wait_limit(uint64_t ns);
 int ozaki_last_moduli();
 
-// Grouped products on the tensor cores (large instances of mgemm_grouped):
+// Grouped products on the tensor cores (instances of mgemm_grouped):
 // ozgroup_prepare allocates and uploads everything for a list of real
 // products (outside any stream capture); ozgroup_launch enqueues the batched
 // exponent scan, residue conversion, one residue GEMM per padding class and
@@ -60,6 +60,7 @@ struct OzGroupItem {
     bool ta, tb;
     dd_host alpha, beta;
     int beta_kind;
+    int pack;   // share a 256 x 256 slot with other small instances (m, n <= 256)
 };
 struct OzGroupPlan;
 OzGroupPlan *ozgroup_create();

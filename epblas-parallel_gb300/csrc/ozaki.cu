@@ -1980,10 +1980,19 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
 //
 // Instances are padded to classes (Mp, Np multiples of 256, Kp of 64) and every
 // class runs as one CTA-pair residue GEMM over count x L planes: plane
-// slot * L + l holds modulus l of the instance in that slot. Exponents,
-// residues and the reconstruction run as one batched launch each over all
-// instances. Everything is enqueued without host round trips (full 106-bit
-// width), so the whole sequence can be captured in a CUDA graph.
+// slot * L + l holds modulus l of the slot's product. Exponents, residues and
+// the reconstruction run as one batched launch each over all instances.
+// Everything is enqueued without host round trips (full 106-bit width), so
+// the whole sequence can be captured in a CUDA graph.
+//
+// Small instances share slots: in a 256 x 256 slot, instance t takes rows
+// [r_t, r_t + m_t) of op(A)'s plane and of the product, columns
+// [c_t, c_t + n_t) (rows of op(B)'s plane), disjoint from the other
+// instances', and K columns [0, k_t). The slot product is then
+// block-diagonal where it is read: its (r_t, c_t) block sums only over
+// instance t's own K range (its rows are zero beyond k_t), and the blocks
+// mixing two instances are never read. Only an instance's own rows are
+// written; the rest of every plane was zeroed when the plan was prepared.
 
 struct OzGrpDesc {
     const double2 *A, *B;
@@ -1997,7 +2006,8 @@ struct OzGrpDesc {
     int64_t rec_begin;        // first reconstruction item: ceil(m/64) row slabs x ceil(n/8) column groups
     xw::XW aM, xb;            // alpha * M and beta as extended floats
     double2 beta;
-    int beta_kind, pad;
+    int beta_kind;
+    int r_off, c_off;         // first row of op(A) / of op(B)^T (= output column) in the slot
 };
 
 struct OzGrpClass {
@@ -2091,10 +2101,12 @@ __global__ void __launch_bounds__(256) k_grp_residues(const OzGrpDesc *__restric
         const int e = r < rows ? ex[(isA ? d.ea_off : d.eb_off) + r] : kNoExp;
         float2 fr[2][kResLimbs], fi[1][kResLimbs];
         tile_limbs<false>(tile[s], cg, e, bits, 0, fr, fi);
-        const int64_t prow = isA ? c.Mp : c.Np;
-        __half *base = isA ? c.Ares : c.Bres;
-        __half *o = base + ((int64_t)d.slot * nmod * prow + r) * c.Kp + c0 + cg;
-        store_residues<false>(fr, fi, nmod, s_t, s_pp, o, prow * c.Kp, 0);
+        if (r < rows) {   // rows past the instance belong to the next one in a shared slot (or stay zero)
+            const int64_t prow = isA ? c.Mp : c.Np;
+            __half *base = isA ? c.Ares : c.Bres;
+            __half *o = base + ((int64_t)d.slot * nmod * prow + (isA ? d.r_off : d.c_off) + r) * c.Kp + c0 + cg;
+            store_residues<false>(fr, fi, nmod, s_t, s_pp, o, prow * c.Kp, 0);
+        }
     }
 }
 
@@ -2119,10 +2131,10 @@ __global__ void __launch_bounds__(256) k_grp_reconstruct(const OzGrpDesc *__rest
         const bool two = i0 + 1 < d.m;
         const int ea0 = ex[d.ea_off + i0], ea1 = two ? ex[d.ea_off + i0 + 1] : kNoExp;
         const int64_t plane = c.Np * c.Mp;
-        const uint16_t *R0 = c.R + (int64_t)d.slot * nmod * plane + i0;
+        const uint16_t *R0 = c.R + (int64_t)d.slot * nmod * plane + d.r_off + i0;
         const dd::real beta = dd::make(d.beta.x, d.beta.y);
-        reconstruct_pair(sm, nmod, R0 + (int64_t)j * c.Mp, plane, i0, two, ea0, ea1, j, ex[d.eb_off + j], bsum,
-                         d.aM, d.xb, beta, d.beta_kind, d.C + i0 + (int64_t)j * d.ldc, 0);
+        reconstruct_pair(sm, nmod, R0 + (int64_t)(d.c_off + j) * c.Mp, plane, i0, two, ea0, ea1, j,
+                         ex[d.eb_off + j], bsum, d.aM, d.xb, beta, d.beta_kind, d.C + i0 + (int64_t)j * d.ldc, 0);
     }
 }
 
@@ -2197,11 +2209,21 @@ bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, con
     Mx.w[0] = (uint32_t)pl->cp.Mlo;
     Mx.e = pl->cp.Me;
     Mx.neg = 0u;
-    // classes and slots
-    std::map<std::tuple<int64_t, int64_t, int64_t>, int> cls_of;
+    // classes and slots; shared slots are filled next-fit (rows and columns
+    // in steps of 8) per class of Kp, deepest instances first
+    std::map<std::tuple<int64_t, int64_t, int64_t, int>, int> cls_of;
+    std::vector<int> pack_rows, pack_cols;   // per class: rows / columns used in its open shared slot
+    std::vector<size_t> order(items.size());
+    for (size_t t = 0; t < items.size(); ++t) order[t] = t;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+        return items[a].pack != items[b].pack ? items[a].pack < items[b].pack : items[a].k > items[b].k;
+    });
     int64_t exn = 0;
-    for (const OzGroupItem &it : items) {
-        const auto key = std::make_tuple(round_up(it.m, 256), round_up(it.n, 256), class_kp(it.k));
+    for (const size_t t : order) {
+        const OzGroupItem &it = items[t];
+        const bool shared = it.pack && it.m <= 256 && it.n <= 256;
+        const auto key = shared ? std::make_tuple((int64_t)256, (int64_t)256, class_kp(it.k), 1)
+                                : std::make_tuple(round_up(it.m, 256), round_up(it.n, 256), class_kp(it.k), 0);
         auto f = cls_of.find(key);
         int ci;
         if (f == cls_of.end()) {
@@ -2213,8 +2235,25 @@ bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, con
             c.Kp = std::get<2>(key);
             pl->classes.push_back(c);
             pl->class_count.push_back(0);
+            pack_rows.push_back(256);   // no open slot yet
+            pack_cols.push_back(256);
         } else {
             ci = f->second;
+        }
+        int slot, r_off = 0, c_off = 0;
+        if (shared) {
+            const int fm = (int)round_up(it.m, 8), fn = (int)round_up(it.n, 8);
+            if (pack_rows[ci] + fm > 256 || pack_cols[ci] + fn > 256) {   // open the next slot
+                pl->class_count[ci]++;
+                pack_rows[ci] = pack_cols[ci] = 0;
+            }
+            slot = (int)pl->class_count[ci] - 1;
+            r_off = pack_rows[ci];
+            c_off = pack_cols[ci];
+            pack_rows[ci] += fm;
+            pack_cols[ci] += fn;
+        } else {
+            slot = (int)pl->class_count[ci]++;
         }
         OzGrpDesc d{};
         d.A = (const double2 *)it.A;
@@ -2229,7 +2268,9 @@ bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, con
         d.ta = it.ta ? 1 : 0;
         d.tb = it.tb ? 1 : 0;
         d.cls = ci;
-        d.slot = (int)pl->class_count[ci]++;
+        d.slot = slot;
+        d.r_off = r_off;
+        d.c_off = c_off;
         d.ea_off = exn;
         d.eb_off = exn + it.m;
         exn += it.m + it.n;

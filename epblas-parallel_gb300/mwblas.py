@@ -170,6 +170,8 @@ class MWBlas:
             self._sig("mwblas_set_grouped_tile", _i32, [_i32])
             self._sig("mwblas_set_grouped_tensor_min", _i32, [_i32])
             self._sig("mwblas_grouped_tuned_tensor_min", _i32, [])
+            self._sig("mwblas_set_grouped_tensor_pack", _i32, [_i32])
+            self._sig("mwblas_grouped_tuned_tensor_pack", _i32, [])
             self._sig("mtrsm_grouped", _i32, [_i64, C.c_char, C.c_char, C.c_char, C.c_char, _p, _p, _p, _p, _p,
                                               _p, _p])
 

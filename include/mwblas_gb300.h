@@ -502,6 +502,15 @@ int mwblas_set_grouped_tile(int tile);
  * integer pipes only). No counterpart in the reference. */
 int mwblas_set_grouped_tensor_min(int size);
 int mwblas_grouped_tuned_tensor_min(void);
+/* mgemm_grouped packs the remaining instances with m, n <= 256 and k >= kmin
+ * several to a 256 x 256 tensor-core slot (block-diagonal: each instance owns
+ * its rows and output columns; the blocks mixing two instances are computed
+ * and never read); 0 = none, -1 = the tuned or default choice. Returns the
+ * previous setting; mwblas_grouped_tuned_tensor_pack returns the depth this
+ * thread's most recent mgemm_grouped_tune chose (0 = none). No counterpart in
+ * the reference. */
+int mwblas_set_grouped_tensor_pack(int kmin);
+int mwblas_grouped_tuned_tensor_pack(void);
 /* Batched triangular solves with shared flags and per-instance sizes: for
  * i < count, op(A[i]) X = alpha[i] B[i] (side 'L') or X op(A[i]) = alpha[i] B[i]
  * ('R'); B[i] is overwritten. Device (or managed) matrix pointers. */

@@ -349,3 +349,70 @@ def test_grouped_gemm_tuner_chooses_tensor_threshold(gpu, oracle, rng):
     arena, args, chosen = run_grouped(gpu, inst, tune=True)
     assert gpu.lib.mwblas_grouped_tuned_tensor_min() in (0, 64, 128, 256)
     check(oracle, inst, arena)
+
+
+def _small_batch(rng, count):
+    """Small instances (m, n <= 200) with k from 4 to 300: those with k >= the
+    packing depth share 256 x 256 tensor-core slots, the rest stay on the
+    integer pipes; odd m and n (a row pair straddles two instances of a slot),
+    every transpose pair, padded ldc, an Inf in one instance."""
+    inst = []
+    for t in range(count):
+        m, n = (int(x) for x in rng.integers(1, 201, 2))
+        k = int(rng.integers(4, 301))
+        if t % 5 == 0:
+            m, n = 2 * int(rng.integers(1, 30)) + 1, 2 * int(rng.integers(1, 30)) + 1
+        ta, tb = str(rng.choice(["N", "T", "C"])), str(rng.choice(["N", "T"]))
+        lda = (m if ta == "N" else k) + int(rng.integers(0, 3))
+        ldb = (k if tb == "N" else n) + int(rng.integers(0, 3))
+        ldc = m + int(rng.integers(0, 3))
+        A = mwb.dd_matrix(rng, m if ta == "N" else k, k if ta == "N" else m, lda)
+        B = mwb.dd_matrix(rng, k if tb == "N" else n, n if tb == "N" else k, ldb)
+        Cm = mwb.dd_matrix(rng, m, n, ldc, fill=-7.37e18)
+        be = [mwb.random_dd(rng, ()), np.zeros(2), np.array([1.0, 0.0])][t % 3]
+        inst.append(dict(m=m, n=n, k=k, ta=ta, tb=tb, lda=lda, ldb=ldb, ldc=ldc, A=A, B=B, C=Cm,
+                         alpha=mwb.random_dd(rng, ()), beta=be))
+    inst[7]["A"][0, 0] = (np.inf, 0.0)
+    return inst
+
+
+def _check_small(oracle, inst, outs):
+    for i, d in enumerate(inst):
+        got, m, n, k = outs[i], d["m"], d["n"], d["k"]
+        want = oracle.qgemm(d["ta"], d["tb"], m, n, k, d["alpha"], d["A"], d["lda"], d["B"], d["ldb"], d["beta"],
+                            d["C"].copy(), d["ldc"])
+        if d["ldc"] > m:
+            assert np.all(got[:, m:] == -7.37e18), i
+        if i == 7:
+            bad = ~np.isfinite(want[:, :m, 0])
+            assert bad.any() and np.all(np.isnan(got[:, :m, 0][bad])), i
+            continue
+        opn = orc.dd_abs(d["alpha"]) * max(k, 1) * orc.dd_absmax(d["A"]) * orc.dd_absmax(d["B"]) \
+            + orc.dd_abs(d["beta"]) * orc.dd_absmax(d["C"][:, :m])
+        err = orc.normwise_error(got[:, :m], want[:, :m], opn)
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (i, m, n, k, err)
+
+
+@pytest.mark.parametrize("oz_min,pack_k", [(0, 16), (128, 32)])
+def test_grouped_gemm_shared_tensor_slots(gpu, oracle, rng, oz_min, pack_k):
+    """Small instances packed several to a tensor-core slot (block-diagonal:
+    own rows and output columns, K from 0), alone or beside instances with
+    slots of their own; within the GEMM tolerance, and a graph replay gives
+    the same bits."""
+    import torch
+    inst = _small_batch(rng, 60)
+    prev_oz = gpu.lib.mwblas_set_grouped_tensor_min(oz_min)
+    prev_pk = gpu.lib.mwblas_set_grouped_tensor_pack(pack_k)
+    try:
+        arena, args, _ = run_grouped(gpu, inst)
+        first = [arena.get(3 * i + 2) for i in range(len(inst))]
+        for i, d in enumerate(inst):
+            o = arena.offsets[3 * i + 2]
+            arena.buf[o:o + d["C"].size] = torch.from_numpy(d["C"].reshape(-1)).cuda()
+        assert gpu.mgemm_grouped(**args) == 0, gpu.last_error()
+        for i in range(len(inst)):
+            np.testing.assert_array_equal(arena.get(3 * i + 2), first[i])
+    finally:
+        gpu.lib.mwblas_set_grouped_tensor_min(prev_oz)
+        gpu.lib.mwblas_set_grouped_tensor_pack(prev_pk)
+    _check_small(oracle, inst, first)
