@@ -1080,6 +1080,7 @@ def run_workload(args):
             cfg = {"workload": "mgemm_grouped 20000 x NN, M,N,K ~ logU[8,512]", "split_k_min_chosen": chosen,
                    "tile_chosen": int(lib.lib.mwblas_grouped_tuned_tile()),
                    "tensor_core_min_size_chosen": int(lib.lib.mwblas_grouped_tuned_tensor_min()),
+                   "tensor_core_pack_depth_chosen": int(lib.lib.mwblas_grouped_tuned_tensor_pack()),
                    "launch": "one CUDA graph per batch layout: the persistent integer-pipe kernel for the small "
                              "instances, the grouped tensor-core residue GEMMs (one per padding class) for those "
                              "with m, n >= the chosen size and k >= 64"}

@@ -465,6 +465,312 @@ void launch_residues(int64_t rows, int64_t kdim, const double2 *X, int64_t ld, c
     count_launch();
 }
 
+// ---- device: residues on the tensor cores -------------------------------------------------
+//
+// The limb dot products x_l = sum_q c_q * t_lq (c_q the 10-bit limbs of the
+// scaled integer, t_lq = 2^(10q) mod p_l, symmetric) are a small matrix
+// product, so they run as tcgen05 MMAs instead of FMAs per element and
+// modulus. Row i of the A operand (K = 64 fp16, 128-byte swizzled rows,
+// written by thread i) holds four consecutive elements of op(X), 16 halves
+// each: the limbs as s * (1024 + c_q) for q < 13 (fp16 0x6400 | c_q with the
+// element's sign bit: no conversion instruction), then -s * 1024 twice, then
+// a zero. B is block-diagonal: row v * 32 + l holds, at halves 16 v .. 16 v +
+// 15, t_l0 .. t_l12, then T1, T2 with T1 + T2 = sum_q t_lq (|T1|, |T2| <=
+// 1170, exact in fp16), then 0, so the offsets cancel exactly:
+//     x = s * sum_q (1024 + c_q) t_lq - s * 1024 (T1 + T2) = s * sum_q c_q t_lq.
+// Every partial sum is an integer below 13 * 2047 * 180 + 2 * 1024 * 1170 <
+// 2^23 (exact in fp32) and |x| <= 13 * 1023 * 180 < 2^22, so the symmetric
+// reduction of the FMA path (quotient estimate, no correction step) applies
+// and both paths store the same residues.
+//
+// Four MMAs of M = 128, N = 32, K = 16 (one per element slot v) leave x for
+// element v, modulus l in TMEM column v * 32 + l of lane i. A tile is 16 rows
+// x 32 k of op(X) (thread i: row i / 8, k 4 (i % 8) .. + 3; a warp stores 4
+// rows x 64 bytes per modulus). Up to four CTAs share an SM (128 TMEM columns
+// each); in each CTA the limbs of tile t + 1 are written while the MMA of
+// tile t runs (two A tiles), and the epilogue of tile t runs before the MMA
+// of tile t + 1 reuses the TMEM columns.
+constexpr int RT_ROWS = 16, RT_COLS = 32, RT_THREADS = 128;
+constexpr int RT_TILE_BYTES = 128 * 128;   // 128 rows x 64 fp16
+// Two A tiles and B, barriers; sized so that at most four CTAs (4 x 128 TMEM
+// columns) share an SM.
+constexpr int RT_SMEM = 56 * 1024;
+constexpr int RT_MAX_MOD = 32;
+constexpr int RT_LIMBS = 13;   // 10-bit limbs of |F| < 2^121 (bits <= 120)
+
+// Chunk j (halves 8j .. 8j + 7) of a 128-byte operand row, 128-byte swizzle.
+__device__ __forceinline__ void st_row_chunk(uint8_t *tile, int row, int j, uint4 v)
+{
+    *reinterpret_cast<uint4 *>(tile + row * 128 + ((j ^ (row & 7)) << 4)) = v;
+}
+
+__device__ __forceinline__ uint32_t h2_bits(float a, float b)
+{
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// F = round(|v| * 2^sc) as four words (0 for zero and non-finite entries;
+// the caller's exponent bound keeps F below 2^121), and the sign of v.
+__device__ __forceinline__ void scaled_int(double2 v, int sc, uint32_t (&y)[4], bool &neg)
+{
+    const fx::Op o = fx::decode(v);
+    neg = (o.flags & fx::kNeg) != 0;
+    y[0] = y[1] = y[2] = y[3] = 0u;
+    const int r = -(o.e + sc);
+    if (!(o.flags & (fx::kZero | fx::kBad)) && r >= 1 && r < 128) {
+        fx::shr128(o.w, r, y);
+        const int rb = r - 1, wq = rb >> 5;
+        const uint32_t word = wq == 0 ? o.w[0] : (wq == 1 ? o.w[1] : (wq == 2 ? o.w[2] : o.w[3]));
+        asm("add.cc.u32 %0, %0, %4;\n\t"
+            "addc.cc.u32 %1, %1, 0;\n\t"
+            "addc.cc.u32 %2, %2, 0;\n\t"
+            "addc.u32 %3, %3, 0;"
+            : "+r"(y[0]), "+r"(y[1]), "+r"(y[2]), "+r"(y[3])
+            : "r"((word >> (rb & 31)) & 1u));
+    }
+}
+
+// Halves 2w, 2w + 1 of an element's A row: limbs 2w, 2w + 1 as 0x6400 | c
+// with the sign bit s; past limb 12 the two offset corrections and a zero.
+template <int W>
+__device__ __forceinline__ uint32_t limb_word(const uint32_t (&y)[4], uint32_t s)
+{
+    constexpr int b = 20 * W, wd = b >> 5, sh = b & 31;
+    const uint32_t corr = 0xE400u ^ (s & 0xFFFFu);   // -s * 1024
+    if (W < 6) {
+        const uint32_t g = __funnelshift_r(y[wd], wd + 1 < 4 ? y[wd + 1] : 0u, sh);   // bits b .. b + 31
+        return ((g & 0x3FFu) | ((g & 0xFFC00u) << 6) | 0x64006400u) ^ s;
+    } else if (W == 6) {
+        const uint32_t c12 = (__funnelshift_r(y[3], 0u, 120 - 96) & 0x3FFu);   // bits 120 .. 129
+        return ((c12 | 0x6400u) ^ (s & 0xFFFFu)) | (corr << 16);
+    } else {
+        return corr;
+    }
+}
+
+template <bool ROWC>
+__global__ void __launch_bounds__(RT_THREADS, 4)
+    k_oz_residues_tc(int64_t rows, int64_t kdim, const double2 *__restrict__ X, int64_t ld,
+                     const int *__restrict__ rexp, int bits, OzResParams P, __half *__restrict__ out, int64_t rows_pad,
+                     int64_t kpad, int64_t plane_rows, int *status)
+{
+    extern __shared__ uint8_t rt_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)rt_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;                        // [2] limb tiles
+    uint8_t *sB = smem + 2 * RT_TILE_BYTES;    // constants
+    uint64_t *done = (uint64_t *)(sB + RT_TILE_BYTES);   // the MMA of the latest tile retired
+    uint64_t *drain = done + 1;
+    uint32_t *tslot = (uint32_t *)(drain + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int nmod = P.nmod;
+
+    // B: row tid = v * 32 + l
+    {
+        const int v = tid >> 5, l = tid & 31;
+        float t[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) t[q] = 0.0f;
+        if (l < nmod) {
+            const int p = (int)P.p[l];
+            int pw = 1, sum = 0;
+#pragma unroll
+            for (int q = 0; q < RT_LIMBS; ++q) {
+                const int ts = pw > p / 2 ? pw - p : pw;
+                t[q] = (float)ts;
+                sum += ts;
+                pw = (pw * 1024) % p;
+            }
+            t[RT_LIMBS] = (float)(sum / 2);
+            t[RT_LIMBS + 1] = (float)(sum - sum / 2);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            uint4 w = make_uint4(0u, 0u, 0u, 0u);
+            if ((j >> 1) == v) {
+                const int q0 = (j & 1) * 8;
+                w = make_uint4(h2_bits(t[q0], t[q0 + 1]), h2_bits(t[q0 + 2], t[q0 + 3]), h2_bits(t[q0 + 4], t[q0 + 5]),
+                               h2_bits(t[q0 + 6], t[q0 + 7]));
+            }
+            st_row_chunk(sB, tid, j, w);
+        }
+    }
+    if (tid == 0) {
+        sm100::mbar_init(done, 1);
+        sm100::mbar_init(drain, 1);
+        sm100::fence_mbar_init();
+    }
+    if (warp == 0) {
+        sm100::tmem_alloc(tslot, 128);
+        sm100::tmem_relinquish();
+    }
+    sm100::fence_proxy_async_smem();
+    sm100::tc_fence_before();
+    __syncthreads();
+    sm100::tc_fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t idesc = sm100::idesc_f16_f32(128, 32);
+
+    // tiles t = blockIdx.x + i * gridDim.x as (row, column) tile pairs, stepped
+    // without divisions (32-bit: fewer than 2^31 tiles)
+    const int nct = (int)(kpad / RT_COLS);
+    const int ntr = (int)((rows_pad + RT_ROWS - 1) / RT_ROWS);
+    const int rl = tid >> 3, cq = (tid & 7) * 4;
+    const int64_t plane = plane_rows * kpad;
+    const int step_r = (int)(gridDim.x / (unsigned)nct), step_c = (int)(gridDim.x % (unsigned)nct);
+    auto advance = [&](int &tr, int &tc) {
+        tc += step_c;
+        tr += step_r;
+        if (tc >= nct) {
+            tc -= nct;
+            tr += 1;
+        }
+    };
+
+    auto fetch = [&](int tr, int tc, double2 (&v)[4]) {
+        const int r = tr * RT_ROWS + rl, c = tc * RT_COLS + cq;
+        const bool rok = r < rows;
+        const double2 *x = ROWC ? X + r + (int64_t)c * ld : X + c + (int64_t)r * ld;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            v[u] = (rok && c + u < kdim) ? x[ROWC ? u * ld : u] : make_double2(0.0, 0.0);
+    };
+    // residues of the tile whose sums are in TMEM, 16 moduli at a time
+    auto epilogue = [&](int tr, int tc) {
+        const int r = tr * RT_ROWS + rl, c = tc * RT_COLS + cq;
+        __half *o = out + (int64_t)r * kpad + c;
+        const bool row_ok = r < rows_pad;
+#pragma unroll
+        for (int l0 = 0; l0 < RT_MAX_MOD; l0 += 16) {
+            if (l0 >= nmod) break;   // uniform
+            uint32_t x[4][16];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) sm100::tmem_ld16(lane_base + v * 32 + l0, x[v]);
+            sm100::tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int l = l0 + i;
+                if (l < nmod && row_ok) {
+                    const float2 negp = make_float2(-P.p[l], -P.p[l]), invp = make_float2(P.invp[l], P.invp[l]);
+                    float2 s[2];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const float2 xv = make_float2(__uint_as_float(x[2 * h][i]), __uint_as_float(x[2 * h + 1][i]));
+                        float2 y = __fmul2_rn(xv, invp);
+                        y = __fadd2_rn(y, make_float2(12582912.0f, 12582912.0f));
+                        y = __fadd2_rn(y, make_float2(-12582912.0f, -12582912.0f));
+                        s[h] = __ffma2_rn(y, negp, xv);
+                    }
+                    store4h(o, s[0], s[1]);
+                }
+                o += plane;
+            }
+        }
+    };
+
+    double2 cur[4];
+    int tr = (int)(blockIdx.x / (unsigned)nct), tc = (int)(blockIdx.x % (unsigned)nct);
+    if (tr < ntr) fetch(tr, tc, cur);
+    int ptr = -1, ptc = 0;   // the previous tile, its sums in TMEM
+    int it = 0, failed = 0;
+    for (; tr < ntr; ++it) {
+        const int b = it & 1;
+        // limbs of this tile into A[b] (the MMA that read it, two tiles back, has retired)
+        {
+            const int r = tr * RT_ROWS + rl;
+            const int e = r < rows ? rexp[r] : kNoExp;
+            const bool live = e > kNoExp / 2;
+            const int sc = bits - 2 - e;
+            uint8_t *a = sA + b * RT_TILE_BYTES;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                uint32_t y[4] = {0u, 0u, 0u, 0u};
+                bool ng = false;
+                if (live) scaled_int(cur[u], sc, y, ng);
+                const uint32_t s = ng ? 0x80008000u : 0u;
+                st_row_chunk(a, tid, 2 * u,
+                             make_uint4(limb_word<0>(y, s), limb_word<1>(y, s), limb_word<2>(y, s), limb_word<3>(y, s)));
+                st_row_chunk(a, tid, 2 * u + 1,
+                             make_uint4(limb_word<4>(y, s), limb_word<5>(y, s), limb_word<6>(y, s), limb_word<7>(y, s)));
+            }
+        }
+        int ntr_ = tr, ntc_ = tc;
+        advance(ntr_, ntc_);
+        if (ntr_ < ntr) fetch(ntr_, ntc_, cur);   // in flight during the epilogue and the MMA below
+        if (ptr >= 0) {
+            if (__all_sync(0xffffffffu, sm100::mbar_wait(done, (it - 1) & 1, status, 21))) {
+                sm100::tc_fence_after();
+                epilogue(ptr, ptc);
+            } else {
+                failed = 1;
+            }
+        }
+        sm100::fence_proxy_async_smem();
+        sm100::tc_fence_before();
+        if (__syncthreads_or(failed)) break;
+        sm100::tc_fence_after();
+        if (tid == 0) {
+            const uint64_t ad = sm100::smem_desc_sw128(sm100::smem_u32(sA + b * RT_TILE_BYTES));
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const uint64_t bd = sm100::smem_desc_sw128(sm100::smem_u32(sB + v * 32 * 128));
+                sm100::mma_f16(tmem + v * 32, ad + 2 * v, bd + 2 * v, idesc, 0u);
+            }
+            sm100::mma_commit(done);
+        }
+        __syncwarp();
+        ptr = tr;
+        ptc = tc;
+        tr = ntr_;
+        tc = ntc_;
+    }
+    if (!failed && ptr >= 0) {
+        if (__all_sync(0xffffffffu, sm100::mbar_wait(done, (it - 1) & 1, status, 21))) {
+            sm100::tc_fence_after();
+            epilogue(ptr, ptc);
+        }
+    }
+    // no MMA may still be writing TMEM when it is freed
+    if (tid == 0) {
+        sm100::mma_commit(drain);
+        sm100::mbar_wait(drain, 0, nullptr, 0);
+    }
+    sm100::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        sm100::tc_fence_after();
+        sm100::tmem_dealloc(tmem, 128);
+    }
+}
+
+std::atomic<int> g_res_tc{1};   // mwblas_set_residue_tc
+
+// Real operands on the tensor-core path when the layout allows it (k padded
+// to the tile width, at most 32 moduli); false: the caller uses the FMA path.
+template <bool ROWC>
+bool launch_residues_tc(int64_t rows, int64_t kdim, const double2 *X, int64_t ld, const int *rexp, int bits,
+                        const OzResParams &rp, __half *out, int64_t rows_pad, int64_t kpad, int64_t plane_rows)
+{
+    if (g_res_tc.load() == 0 || rp.nmod > RT_MAX_MOD || kpad % RT_COLS != 0 || rows_pad <= 0 || !ozaki_available())
+        return false;
+    static int attr_set[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!attr_set[dev & 63]) {
+        cudaFuncSetAttribute(k_oz_residues_tc<ROWC>, cudaFuncAttributeMaxDynamicSharedMemorySize, RT_SMEM);
+        attr_set[dev & 63] = 1;
+    }
+    const int64_t ntiles = ((rows_pad + RT_ROWS - 1) / RT_ROWS) * (kpad / RT_COLS);
+    if (ntiles >= ((int64_t)1 << 31) || rows_pad >= ((int64_t)1 << 31)) return false;
+    int64_t grid = 4 * (int64_t)device_sm_count();
+    if (grid > ntiles) grid = ntiles;
+    k_oz_residues_tc<ROWC><<<(unsigned)grid, RT_THREADS, RT_SMEM, stream()>>>(
+        rows, kdim, X, ld, rexp, bits, rp, out, rows_pad, kpad, plane_rows, device_status_word());
+    count_launch();
+    return true;
+}
+
 // ---- device: residue GEMM, tensor cores ---------------------------------------------------
 
 constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64, TC_STAGES = 4;
@@ -1748,6 +2054,9 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
             if (!g.ta) launch_residues<true, true>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, g.ca, Mp);
             else launch_residues<false, true>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, g.ca, Mp);
         } else {
+            const bool tc = !g.ta ? launch_residues_tc<true>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, Mp)
+                                  : launch_residues_tc<false>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, Mp);
+            if (tc) return;
             if (!g.ta) launch_residues<true, false>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, 0, Mp);
             else launch_residues<false, false>(ni, k, Ai, g.lda, ea + i0, bits_a, rp, Ao, rpad, Kp, 0, Mp);
         }
@@ -1779,6 +2088,9 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
             if (!g.tb) launch_residues<false, true>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, g.cb, Np);
             else launch_residues<true, true>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, g.cb, Np);
         } else {
+            const bool tc = !g.tb ? launch_residues_tc<false>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, Np)
+                                  : launch_residues_tc<true>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, Np);
+            if (tc) return;
             if (!g.tb) launch_residues<false, false>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, 0, Np);
             else launch_residues<true, false>(nn, k, Bj, g.ldb, eb + j0, bits_b, rp, Bo, rpad, Kp, 0, Np);
         }
@@ -2402,6 +2714,8 @@ extern "C" uint64_t mwblas_set_wait_limit_ns(uint64_t ns)
     }
     return current.exchange(v);
 }
+
+extern "C" int mwblas_set_residue_tc(int on) { return mw::g_res_tc.exchange(on ? 1 : 0); }
 
 extern "C" void mwblas_debug_lose_operand_loads(int count) { mw::g_lose_loads.store(count > 0 ? count : 0); }
 

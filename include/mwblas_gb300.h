@@ -553,6 +553,11 @@ int mwblas_set_ozaki_mma(int kind);
  * Both give identical results. Returns the previous value. */
 int mwblas_set_plain_tma(int on);
 
+/* Residue conversion of real operands in the Ozaki engine: 1 (default) = the
+ * limb dot products as tcgen05 MMAs, 0 = FP32 FMAs on the CUDA cores. Both
+ * write identical residues. Returns the previous value. */
+int mwblas_set_residue_tc(int on);
+
 /* Per-phase device timing of the Ozaki engine (CUDA events on the library
  * stream; off by default). Phases: 0 exponent scan, 1 residue conversion,
  * 2 residue GEMMs (tensor cores), 3 CRT reconstruction. mwblas_last_phase_ms

@@ -470,3 +470,113 @@ def test_fp64_inputs_complex_and_syrk(gpu, oracle, rng):
     want = oracle.qwgemm("N", "C", m, n, k, cal, Ac, m, Bc, n, cbe, Cc, m, rows=rows, cols=cols)
     op = orc.dd_abs(cal) * k * orc.dd_absmax(Ac) * orc.dd_absmax(Bc) + orc.dd_abs(cbe) * orc.dd_absmax(Cc)
     assert orc.normwise_error(outs[0][0][cols, rows], want, op) <= max(10, 4 * k) * orc.EPS_DD
+
+
+# ---- residue conversion on the tensor cores ----------------------------------------------------
+
+class residue_path:
+    """Selects the residue conversion of real operands: 1 tcgen05 MMAs, 0 FP32 FMAs."""
+
+    def __init__(self, lib, on):
+        self.lib, self.on = lib, on
+
+    def __enter__(self):
+        self.prev = self.lib.lib.mwblas_set_residue_tc(self.on)
+
+    def __exit__(self, *a):
+        self.lib.lib.mwblas_set_residue_tc(self.prev)
+
+
+def _both_residue_paths(gpu, run):
+    outs = []
+    for on in (1, 0):
+        with residue_path(gpu, on):
+            outs.append(run())
+            assert gpu.last_error()[0] == 0, gpu.last_error()
+    assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
+    return outs[0]
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
+def test_residue_conversion_tensor_cores_bit_identical(gpu, oracle, rng, ta, tb):
+    """The limb dot products as tcgen05 MMAs give the FMA path's residues,
+    hence the same output bits: ragged m, n, k (rows past the operand and k
+    past its end are zero residues), padded leading dimensions, one to many
+    16 x 32 tiles per CTA."""
+    for (m, n, k) in [(1, 1, 1), (5, 3, 70), (37, 300, 33), (130, 97, 1500), (257, 129, 2100), (700, 520, 130)]:
+        lda = (m if ta == "N" else k) + 3
+        ldb = (k if tb == "N" else n) + 1
+        A = mwb.dd_matrix(rng, m if ta == "N" else k, k if ta == "N" else m, lda)
+        B = mwb.dd_matrix(rng, k if tb == "N" else n, n if tb == "N" else k, ldb)
+        C0 = mwb.dd_matrix(rng, m, n, m + 2, fill=-7.37e18)
+        al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+
+        def run():
+            c = C0.copy()
+            gpu.mgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, c, m + 2, engine="ozaki")
+            return c
+        got = _both_residue_paths(gpu, run)
+        assert np.all(got[:, m:] == -7.37e18)
+        want = oracle.qgemm(ta, tb, m, n, k, al, A, lda, B, ldb, be, C0.copy(), m + 2)
+        err = orc.normwise_error(got[:, :m], want[:, :m], op_norm(al, k, A, B, be, C0[:, :m]))
+        assert err <= max(10, 4 * k) * orc.EPS_DD, (ta, tb, m, n, k, err)
+
+
+def test_residue_conversion_tensor_cores_special_operands(gpu, oracle, rng):
+    """Exponent-spread rows and columns, zero rows, non-finite entries, a
+    device-resident product over 2048 x 2048, the shared conversion of SYRK
+    and 30 moduli (bits = 120): identical bits on both residue paths."""
+    import torch
+    m, n, k = 192, 160, 777
+    A = mwb.dd_matrix(rng, m, k)
+    B = mwb.dd_matrix(rng, k, n)
+    A *= (2.0 ** rng.integers(-30, 31, size=m).astype(float))[None, :, None]
+    B *= (2.0 ** rng.integers(-30, 31, size=n).astype(float))[:, None, None]
+    A[:, 7] = 0.0
+    B[11, :] = 0.0
+    A[5, 20] = (np.inf, 0.0)
+    al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+
+    def run():
+        c = np.zeros((n, m, 2))
+        gpu.mgemm("N", "N", m, n, k, al, A, m, B, k, be, c, m, engine="ozaki")
+        return c
+    got = _both_residue_paths(gpu, run)
+    assert np.all(np.isnan(got[:, 20, 0])) and np.isfinite(got[:, 19, 0]).all()
+
+    m, n, k = 2100, 2300, 300
+    dev = torch.device("cuda", 0)
+    dA = torch.from_numpy(mwb.dd_matrix(rng, m, k)).to(dev)
+    dB = torch.from_numpy(mwb.dd_matrix(rng, k, n)).to(dev)
+    C0 = torch.from_numpy(mwb.dd_matrix(rng, m, n)).to(dev)
+
+    def run_dev():
+        C = C0.clone()
+        gpu.mgemm("N", "N", m, n, k, al, dA.data_ptr(), m, dB.data_ptr(), k, be, C.data_ptr(), m, engine="ozaki")
+        return C.cpu().numpy()
+    _both_residue_paths(gpu, run_dev)
+
+    n, k = 300, 700
+    A = mwb.dd_matrix(rng, n, k)
+    C0 = mwb.dd_matrix(rng, n, n)
+
+    def run_syrk():
+        c = C0.copy()
+        with engine(gpu, OZAKI):
+            gpu.msyrk("U", "N", n, k, al, A, n, be, c, n)
+        return c
+    _both_residue_paths(gpu, run_syrk)
+
+    m, n, k = 100, 90, 1500
+    A = mwb.dd_matrix(rng, m, k)
+    B = mwb.dd_matrix(rng, k, n)
+    prev = gpu.lib.mwblas_set_ozaki_bits(120)
+    try:
+        def run_bits():
+            c = np.zeros((n, m, 2))
+            gpu.mgemm("N", "N", m, n, k, al, A, m, B, k, be, c, m, engine="ozaki")
+            return c
+        _both_residue_paths(gpu, run_bits)
+        assert 28 < gpu.lib.mwblas_last_ozaki_moduli() <= 32
+    finally:
+        gpu.lib.mwblas_set_ozaki_bits(prev)
