@@ -444,7 +444,7 @@ struct Policy {
     int max_tiles_split = 4;   // split only instances with at most this many tiles
     int tile = 32;             // output tile edge: 16, 32 or 64
     int oz_min = 0;            // instances with m, n >= oz_min and k >= 64 run on the tensor cores (0: none)
-    int pack_k = 0;            // the other instances with m, n <= 256 and k >= pack_k share tensor-core slots (0: none)
+    int pack_k = 0;            // the other instances with k >= pack_k share tensor-core slots, in pieces of <= 256 x 256 (0: none)
 };
 
 struct Plan {
@@ -528,19 +528,31 @@ void build_descs(Plan &pl, int64_t count, const char *ta, const char *tb, const 
         const bool alpha0 = (d.alpha.x == 0.0 && d.alpha.y == 0.0);
         d.beta_kind = (d.beta.x == 0.0 && d.beta.y == 0.0) ? 0 : ((d.beta.x == 1.0 && d.beta.y == 0.0) ? 1 : 2);
         const bool own_slot = oz_min > 0 && d.m >= oz_min && d.n >= oz_min && d.k >= 64;
-        const bool shared_slot = pack_k > 0 && d.m <= 256 && d.n <= 256 && d.k >= pack_k;
+        // the other instances of depth >= pack_k share slots; those with m or
+        // n above 256 (the skinny ones) as pieces of at most 256 x 256
+        const bool shared_slot = pack_k > 0 && d.k >= pack_k;
         if (!alpha0 && (own_slot || shared_slot) && d.k <= 16384 && d.m <= 8192 && d.n <= 8192) {
             OzGroupItem it;
             memset(&it, 0, sizeof(it));   // the plan key hashes the bytes, padding included
-            it.A = d.A; it.B = d.B; it.C = d.C;
             it.lda = d.lda; it.ldb = d.ldb; it.ldc = d.ldc;
-            it.m = d.m; it.n = d.n; it.k = d.k;
+            it.k = d.k;
             it.ta = d.ta != 0; it.tb = d.tb != 0;
             it.alpha = dd_host{d.alpha.x, d.alpha.y};
             it.beta = dd_host{d.beta.x, d.beta.y};
             it.beta_kind = d.beta_kind;
             it.pack = own_slot ? 0 : 1;
-            pl.oz_items.push_back(it);
+            const int pm = own_slot ? d.m : 256, pn = own_slot ? d.n : 256;
+            for (int r0 = 0; r0 < d.m; r0 += pm) {
+                for (int c0 = 0; c0 < d.n; c0 += pn) {
+                    // rows r0.. of op(A), columns c0.. of op(B) and C
+                    it.A = d.A + (d.ta ? (int64_t)r0 * d.lda : r0);
+                    it.B = d.B + (d.tb ? c0 : (int64_t)c0 * d.ldb);
+                    it.C = d.C + r0 + (int64_t)c0 * d.ldc;
+                    it.m = std::min(pm, d.m - r0);
+                    it.n = std::min(pn, d.n - c0);
+                    pl.oz_items.push_back(it);
+                }
+            }
             continue;
         }
         if (alpha0 || d.k == 0) {

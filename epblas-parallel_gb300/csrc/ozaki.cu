@@ -549,55 +549,125 @@ __device__ __forceinline__ uint32_t limb_word(const uint32_t (&y)[4], uint32_t s
     }
 }
 
-template <bool ROWC>
-__global__ void __launch_bounds__(RT_THREADS, 4)
-    k_oz_residues_tc(int64_t rows, int64_t kdim, const double2 *__restrict__ X, int64_t ld,
-                     const int *__restrict__ rexp, int bits, OzResParams P, __half *__restrict__ out, int64_t rows_pad,
-                     int64_t kpad, int64_t plane_rows, int *status)
+// B of the tensor-core residue conversion, row tid = v * 32 + l (block-diagonal).
+__device__ __forceinline__ void rt_constants(uint8_t *sB, const OzResParams &P, int tid)
 {
-    extern __shared__ uint8_t rt_raw[];
-    uint8_t *smem = (uint8_t *)(((uintptr_t)rt_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem;                        // [2] limb tiles
-    uint8_t *sB = smem + 2 * RT_TILE_BYTES;    // constants
-    uint64_t *done = (uint64_t *)(sB + RT_TILE_BYTES);   // the MMA of the latest tile retired
-    uint64_t *drain = done + 1;
-    uint32_t *tslot = (uint32_t *)(drain + 1);
-    const int tid = threadIdx.x, warp = tid >> 5;
-    const int nmod = P.nmod;
-
-    // B: row tid = v * 32 + l
-    {
-        const int v = tid >> 5, l = tid & 31;
-        float t[16];
+    const int v = tid >> 5, l = tid & 31;
+    float t[16];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) t[q] = 0.0f;
-        if (l < nmod) {
-            const int p = (int)P.p[l];
-            int pw = 1, sum = 0;
+    for (int q = 0; q < 16; ++q) t[q] = 0.0f;
+    if (l < P.nmod) {
+        const int p = (int)P.p[l];
+        int pw = 1, sum = 0;
 #pragma unroll
-            for (int q = 0; q < RT_LIMBS; ++q) {
-                const int ts = pw > p / 2 ? pw - p : pw;
-                t[q] = (float)ts;
-                sum += ts;
-                pw = (pw * 1024) % p;
-            }
-            t[RT_LIMBS] = (float)(sum / 2);
-            t[RT_LIMBS + 1] = (float)(sum - sum / 2);
+        for (int q = 0; q < RT_LIMBS; ++q) {
+            const int ts = pw > p / 2 ? pw - p : pw;
+            t[q] = (float)ts;
+            sum += ts;
+            pw = (pw * 1024) % p;
         }
+        t[RT_LIMBS] = (float)(sum / 2);
+        t[RT_LIMBS + 1] = (float)(sum - sum / 2);
+    }
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            uint4 w = make_uint4(0u, 0u, 0u, 0u);
-            if ((j >> 1) == v) {
-                const int q0 = (j & 1) * 8;
-                w = make_uint4(h2_bits(t[q0], t[q0 + 1]), h2_bits(t[q0 + 2], t[q0 + 3]), h2_bits(t[q0 + 4], t[q0 + 5]),
-                               h2_bits(t[q0 + 6], t[q0 + 7]));
+    for (int j = 0; j < 8; ++j) {
+        uint4 w = make_uint4(0u, 0u, 0u, 0u);
+        if ((j >> 1) == v) {
+            const int q0 = (j & 1) * 8;
+            w = make_uint4(h2_bits(t[q0], t[q0 + 1]), h2_bits(t[q0 + 2], t[q0 + 3]), h2_bits(t[q0 + 4], t[q0 + 5]),
+                           h2_bits(t[q0 + 6], t[q0 + 7]));
+        }
+        st_row_chunk(sB, tid, j, w);
+    }
+}
+
+// A row tid: the limbs of four elements scaled by 2^(bits - 2 - e) (zeros
+// when the row has no live exponent).
+__device__ __forceinline__ void rt_limbs(uint8_t *a, int tid, const double2 (&cur)[4], int e, int bits)
+{
+    const bool live = e > kNoExp / 2;
+    const int sc = bits - 2 - e;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        uint32_t y[4] = {0u, 0u, 0u, 0u};
+        bool ng = false;
+        if (live) scaled_int(cur[u], sc, y, ng);
+        const uint32_t s = ng ? 0x80008000u : 0u;
+        st_row_chunk(a, tid, 2 * u,
+                     make_uint4(limb_word<0>(y, s), limb_word<1>(y, s), limb_word<2>(y, s), limb_word<3>(y, s)));
+        st_row_chunk(a, tid, 2 * u + 1,
+                     make_uint4(limb_word<4>(y, s), limb_word<5>(y, s), limb_word<6>(y, s), limb_word<7>(y, s)));
+    }
+}
+
+// The tile's four MMAs (one thread), completion on `done`.
+__device__ __forceinline__ void rt_mma(uint32_t tmem, const uint8_t *a, const uint8_t *sB, uint64_t *done)
+{
+    const uint32_t idesc = sm100::idesc_f16_f32(128, 32);
+    const uint64_t ad = sm100::smem_desc_sw128(sm100::smem_u32(a));
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        const uint64_t bd = sm100::smem_desc_sw128(sm100::smem_u32(sB + v * 32 * 128));
+        sm100::mma_f16(tmem + v * 32, ad + 2 * v, bd + 2 * v, idesc, 0u);
+    }
+    sm100::mma_commit(done);
+}
+
+// Residues of this thread's four elements for every modulus from the sums in
+// TMEM, 16 moduli at a time, four fp16 per 8-byte store at o + l * plane
+// (nothing stored when !ok; the TMEM loads are warp-wide either way).
+__device__ __forceinline__ void rt_store(uint32_t lane_base, const OzResParams &P, __half *o, int64_t plane, bool ok)
+{
+    const int nmod = P.nmod;
+#pragma unroll
+    for (int l0 = 0; l0 < RT_MAX_MOD; l0 += 16) {
+        if (l0 >= nmod) break;   // uniform
+        uint32_t x[4][16];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sm100::tmem_ld16(lane_base + v * 32 + l0, x[v]);
+        sm100::tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int l = l0 + i;
+            if (l < nmod && ok) {
+                const float2 negp = make_float2(-P.p[l], -P.p[l]), invp = make_float2(P.invp[l], P.invp[l]);
+                float2 s[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float2 xv = make_float2(__uint_as_float(x[2 * h][i]), __uint_as_float(x[2 * h + 1][i]));
+                    float2 y = __fmul2_rn(xv, invp);
+                    y = __fadd2_rn(y, make_float2(12582912.0f, 12582912.0f));
+                    y = __fadd2_rn(y, make_float2(-12582912.0f, -12582912.0f));
+                    s[h] = __ffma2_rn(y, negp, xv);
+                }
+                store4h(o, s[0], s[1]);
             }
-            st_row_chunk(sB, tid, j, w);
+            o += plane;
         }
     }
+}
+
+// Shared-memory layout, barriers and TMEM of the tensor-core residue kernels.
+struct RtCta {
+    uint8_t *sA, *sB;
+    uint64_t *done, *drain;
+    uint32_t tmem, lane_base;
+};
+
+__device__ __forceinline__ RtCta rt_setup(uint8_t *raw, const OzResParams &P)
+{
+    RtCta c;
+    uint8_t *smem = (uint8_t *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
+    c.sA = smem;                          // [2] limb tiles
+    c.sB = smem + 2 * RT_TILE_BYTES;      // constants
+    c.done = (uint64_t *)(c.sB + RT_TILE_BYTES);   // the MMA of the latest tile retired
+    c.drain = c.done + 1;
+    uint32_t *tslot = (uint32_t *)(c.drain + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    rt_constants(c.sB, P, tid);
     if (tid == 0) {
-        sm100::mbar_init(done, 1);
-        sm100::mbar_init(drain, 1);
+        sm100::mbar_init(c.done, 1);
+        sm100::mbar_init(c.drain, 1);
         sm100::fence_mbar_init();
     }
     if (warp == 0) {
@@ -608,10 +678,69 @@ __global__ void __launch_bounds__(RT_THREADS, 4)
     sm100::tc_fence_before();
     __syncthreads();
     sm100::tc_fence_after();
-    const uint32_t tmem = *tslot;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    const uint32_t idesc = sm100::idesc_f16_f32(128, 32);
+    c.tmem = *tslot;
+    c.lane_base = c.tmem + ((uint32_t)(warp * 32) << 16);
+    return c;
+}
 
+// No MMA may still be writing TMEM when it is freed.
+__device__ __forceinline__ void rt_teardown(const RtCta &c)
+{
+    if (threadIdx.x == 0) {
+        sm100::mma_commit(c.drain);
+        sm100::mbar_wait(c.drain, 0, nullptr, 0);
+    }
+    sm100::tc_fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) {
+        sm100::tc_fence_after();
+        sm100::tmem_dealloc(c.tmem, 128);
+    }
+}
+
+// One step of the tile pipeline: the limbs of the current tile are in A[b];
+// waits for the previous tile's MMA and stores its residues, then issues the
+// current tile's MMA. Returns false (on every thread) once a wait gave up.
+__device__ __forceinline__ bool rt_step(const RtCta &c, const OzResParams &P, int b, int it, bool have_prev,
+                                        __half *po, int64_t pplane, bool pok, int *status, int &failed)
+{
+    if (have_prev) {
+        if (__all_sync(0xffffffffu, sm100::mbar_wait(c.done, (it - 1) & 1, status, 21))) {
+            sm100::tc_fence_after();
+            rt_store(c.lane_base, P, po, pplane, pok);
+        } else {
+            failed = 1;
+        }
+    }
+    sm100::fence_proxy_async_smem();
+    sm100::tc_fence_before();
+    if (__syncthreads_or(failed)) return false;
+    sm100::tc_fence_after();
+    if (threadIdx.x == 0) rt_mma(c.tmem, c.sA + b * RT_TILE_BYTES, c.sB, c.done);
+    __syncwarp();
+    return true;
+}
+
+// The last tile's residues (after its MMA).
+__device__ __forceinline__ void rt_finish(const RtCta &c, const OzResParams &P, int it, bool have_prev, __half *po,
+                                          int64_t pplane, bool pok, int *status, int failed)
+{
+    if (failed || !have_prev) return;
+    if (__all_sync(0xffffffffu, sm100::mbar_wait(c.done, (it - 1) & 1, status, 21))) {
+        sm100::tc_fence_after();
+        rt_store(c.lane_base, P, po, pplane, pok);
+    }
+}
+
+template <bool ROWC>
+__global__ void __launch_bounds__(RT_THREADS, 4)
+    k_oz_residues_tc(int64_t rows, int64_t kdim, const double2 *__restrict__ X, int64_t ld,
+                     const int *__restrict__ rexp, int bits, OzResParams P, __half *__restrict__ out, int64_t rows_pad,
+                     int64_t kpad, int64_t plane_rows, int *status)
+{
+    extern __shared__ uint8_t rt_raw[];
+    const RtCta cta = rt_setup(rt_raw, P);
+    const int tid = threadIdx.x;
     // tiles t = blockIdx.x + i * gridDim.x as (row, column) tile pairs, stepped
     // without divisions (32-bit: fewer than 2^31 tiles)
     const int nct = (int)(kpad / RT_COLS);
@@ -619,14 +748,6 @@ __global__ void __launch_bounds__(RT_THREADS, 4)
     const int rl = tid >> 3, cq = (tid & 7) * 4;
     const int64_t plane = plane_rows * kpad;
     const int step_r = (int)(gridDim.x / (unsigned)nct), step_c = (int)(gridDim.x % (unsigned)nct);
-    auto advance = [&](int &tr, int &tc) {
-        tc += step_c;
-        tr += step_r;
-        if (tc >= nct) {
-            tc -= nct;
-            tr += 1;
-        }
-    };
 
     auto fetch = [&](int tr, int tc, double2 (&v)[4]) {
         const int r = tr * RT_ROWS + rl, c = tc * RT_COLS + cq;
@@ -636,112 +757,34 @@ __global__ void __launch_bounds__(RT_THREADS, 4)
         for (int u = 0; u < 4; ++u)
             v[u] = (rok && c + u < kdim) ? x[ROWC ? u * ld : u] : make_double2(0.0, 0.0);
     };
-    // residues of the tile whose sums are in TMEM, 16 moduli at a time
-    auto epilogue = [&](int tr, int tc) {
-        const int r = tr * RT_ROWS + rl, c = tc * RT_COLS + cq;
-        __half *o = out + (int64_t)r * kpad + c;
-        const bool row_ok = r < rows_pad;
-#pragma unroll
-        for (int l0 = 0; l0 < RT_MAX_MOD; l0 += 16) {
-            if (l0 >= nmod) break;   // uniform
-            uint32_t x[4][16];
-#pragma unroll
-            for (int v = 0; v < 4; ++v) sm100::tmem_ld16(lane_base + v * 32 + l0, x[v]);
-            sm100::tmem_wait_ld();
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const int l = l0 + i;
-                if (l < nmod && row_ok) {
-                    const float2 negp = make_float2(-P.p[l], -P.p[l]), invp = make_float2(P.invp[l], P.invp[l]);
-                    float2 s[2];
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const float2 xv = make_float2(__uint_as_float(x[2 * h][i]), __uint_as_float(x[2 * h + 1][i]));
-                        float2 y = __fmul2_rn(xv, invp);
-                        y = __fadd2_rn(y, make_float2(12582912.0f, 12582912.0f));
-                        y = __fadd2_rn(y, make_float2(-12582912.0f, -12582912.0f));
-                        s[h] = __ffma2_rn(y, negp, xv);
-                    }
-                    store4h(o, s[0], s[1]);
-                }
-                o += plane;
-            }
-        }
-    };
 
     double2 cur[4];
     int tr = (int)(blockIdx.x / (unsigned)nct), tc = (int)(blockIdx.x % (unsigned)nct);
     if (tr < ntr) fetch(tr, tc, cur);
-    int ptr = -1, ptc = 0;   // the previous tile, its sums in TMEM
+    __half *po = nullptr;   // the previous tile (its sums in TMEM): this thread's output
+    bool pok = false, have_prev = false;
     int it = 0, failed = 0;
     for (; tr < ntr; ++it) {
         const int b = it & 1;
-        // limbs of this tile into A[b] (the MMA that read it, two tiles back, has retired)
-        {
-            const int r = tr * RT_ROWS + rl;
-            const int e = r < rows ? rexp[r] : kNoExp;
-            const bool live = e > kNoExp / 2;
-            const int sc = bits - 2 - e;
-            uint8_t *a = sA + b * RT_TILE_BYTES;
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                uint32_t y[4] = {0u, 0u, 0u, 0u};
-                bool ng = false;
-                if (live) scaled_int(cur[u], sc, y, ng);
-                const uint32_t s = ng ? 0x80008000u : 0u;
-                st_row_chunk(a, tid, 2 * u,
-                             make_uint4(limb_word<0>(y, s), limb_word<1>(y, s), limb_word<2>(y, s), limb_word<3>(y, s)));
-                st_row_chunk(a, tid, 2 * u + 1,
-                             make_uint4(limb_word<4>(y, s), limb_word<5>(y, s), limb_word<6>(y, s), limb_word<7>(y, s)));
-            }
+        const int r = tr * RT_ROWS + rl;
+        rt_limbs(cta.sA + b * RT_TILE_BYTES, tid, cur, r < rows ? rexp[r] : kNoExp, bits);
+        __half *o = out + (int64_t)r * kpad + tc * RT_COLS + cq;
+        const bool ok = r < rows_pad;
+        int tr2 = tr + step_r, tc2 = tc + step_c;
+        if (tc2 >= nct) {
+            tc2 -= nct;
+            tr2 += 1;
         }
-        int ntr_ = tr, ntc_ = tc;
-        advance(ntr_, ntc_);
-        if (ntr_ < ntr) fetch(ntr_, ntc_, cur);   // in flight during the epilogue and the MMA below
-        if (ptr >= 0) {
-            if (__all_sync(0xffffffffu, sm100::mbar_wait(done, (it - 1) & 1, status, 21))) {
-                sm100::tc_fence_after();
-                epilogue(ptr, ptc);
-            } else {
-                failed = 1;
-            }
-        }
-        sm100::fence_proxy_async_smem();
-        sm100::tc_fence_before();
-        if (__syncthreads_or(failed)) break;
-        sm100::tc_fence_after();
-        if (tid == 0) {
-            const uint64_t ad = sm100::smem_desc_sw128(sm100::smem_u32(sA + b * RT_TILE_BYTES));
-#pragma unroll
-            for (int v = 0; v < 4; ++v) {
-                const uint64_t bd = sm100::smem_desc_sw128(sm100::smem_u32(sB + v * 32 * 128));
-                sm100::mma_f16(tmem + v * 32, ad + 2 * v, bd + 2 * v, idesc, 0u);
-            }
-            sm100::mma_commit(done);
-        }
-        __syncwarp();
-        ptr = tr;
-        ptc = tc;
-        tr = ntr_;
-        tc = ntc_;
+        if (tr2 < ntr) fetch(tr2, tc2, cur);   // in flight during the epilogue and the MMA below
+        if (!rt_step(cta, P, b, it, have_prev, po, plane, pok, status, failed)) break;
+        po = o;
+        pok = ok;
+        have_prev = true;
+        tr = tr2;
+        tc = tc2;
     }
-    if (!failed && ptr >= 0) {
-        if (__all_sync(0xffffffffu, sm100::mbar_wait(done, (it - 1) & 1, status, 21))) {
-            sm100::tc_fence_after();
-            epilogue(ptr, ptc);
-        }
-    }
-    // no MMA may still be writing TMEM when it is freed
-    if (tid == 0) {
-        sm100::mma_commit(drain);
-        sm100::mbar_wait(drain, 0, nullptr, 0);
-    }
-    sm100::tc_fence_before();
-    __syncthreads();
-    if (warp == 0) {
-        sm100::tc_fence_after();
-        sm100::tmem_dealloc(tmem, 128);
-    }
+    rt_finish(cta, P, it, have_prev, po, plane, pok, status, failed);
+    rt_teardown(cta);
 }
 
 std::atomic<int> g_res_tc{1};   // mwblas_set_residue_tc
@@ -2314,7 +2357,7 @@ struct OzGrpDesc {
     int cls, slot;
     int64_t ea_off, eb_off;   // row exponents of op(A), column exponents of op(B)
     int64_t line_begin;       // first exponent line: m rows of op(A), then n columns of op(B)
-    int64_t tile_begin;       // first conversion tile: op(A)'s ceil(m/32) ceil(k/32), then op(B)'s ceil(n/32) ceil(k/32)
+    int64_t tile_begin;       // first conversion tile: op(A)'s ceil(m/R) ceil(k/32), then op(B)'s ceil(n/R) ceil(k/32) (R = 16 on the tensor cores, else 32)
     int64_t rec_begin;        // first reconstruction item: ceil(m/64) row slabs x ceil(n/8) column groups
     xw::XW aM, xb;            // alpha * M and beta as extended floats
     double2 beta;
@@ -2422,6 +2465,74 @@ __global__ void __launch_bounds__(256) k_grp_residues(const OzGrpDesc *__restric
     }
 }
 
+// The same conversion on the tensor cores (the tile pipeline of
+// k_oz_residues_tc): tiles of 16 rows x 32 k of one operand of one instance,
+// listed per instance as op(A)'s ceil(m/16) ceil(k/32), then op(B)'s; rows
+// past the instance are not stored (they belong to the next instance of a
+// shared slot, or stay zero).
+__global__ void __launch_bounds__(RT_THREADS, 4)
+    k_grp_residues_tc(const OzGrpDesc *__restrict__ descs, int count, int64_t tiles,
+                      const OzGrpClass *__restrict__ classes, const int *__restrict__ ex, int bits, OzResParams P,
+                      int *status)
+{
+    extern __shared__ uint8_t rt_raw[];
+    const RtCta cta = rt_setup(rt_raw, P);
+    const int tid = threadIdx.x;
+    const int rl = tid >> 3, cq = (tid & 7) * 4;
+    const int nmod = P.nmod;
+    struct Tile {
+        __half *o;
+        int64_t plane;
+        int e;
+        bool ok;
+    };
+    // loads this thread's four elements of tile w and locates their residues
+    auto fetch = [&](int64_t w, double2 (&v)[4]) {
+        const OzGrpDesc &d = descs[grp_find(descs, count, w, 1)];
+        const OzGrpClass &c = classes[d.cls];
+        const int ntc = (d.k + RT_COLS - 1) / RT_COLS, ta_tiles = ((d.m + RT_ROWS - 1) / RT_ROWS) * ntc;
+        int t = (int)(w - d.tile_begin);
+        const bool isA = t < ta_tiles;
+        if (!isA) t -= ta_tiles;
+        const int r = (t / ntc) * RT_ROWS + rl, col = (t % ntc) * RT_COLS + cq;
+        const int rows = isA ? d.m : d.n;
+        const bool rowc = isA ? !d.ta : d.tb;   // rows contiguous in memory
+        const int64_t ld = isA ? d.lda : d.ldb;
+        const bool ok = r < rows;
+        const double2 *x = (isA ? d.A : d.B) + (rowc ? r + (int64_t)col * ld : col + (int64_t)r * ld);
+        const int64_t step = rowc ? ld : 1;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = (ok && col + u < d.k) ? x[u * step] : make_double2(0.0, 0.0);
+        const int64_t prow = isA ? c.Mp : c.Np;
+        Tile T;
+        T.plane = prow * c.Kp;
+        T.o = (isA ? c.Ares : c.Bres) + ((int64_t)d.slot * nmod * prow + (isA ? d.r_off : d.c_off) + r) * c.Kp + col;
+        T.e = ok ? ex[(isA ? d.ea_off : d.eb_off) + r] : kNoExp;
+        T.ok = ok;
+        return T;
+    };
+    double2 cur[4];
+    int64_t w = blockIdx.x;
+    Tile T{}, Tp{};
+    if (w < tiles) T = fetch(w, cur);
+    bool have_prev = false;
+    int it = 0, failed = 0;
+    for (; w < tiles; ++it) {
+        const int b = it & 1;
+        rt_limbs(cta.sA + b * RT_TILE_BYTES, tid, cur, T.e, bits);
+        const int64_t w2 = w + gridDim.x;
+        Tile T2{};
+        if (w2 < tiles) T2 = fetch(w2, cur);   // in flight during the epilogue and the MMA below
+        if (!rt_step(cta, P, b, it, have_prev, Tp.o, Tp.plane, Tp.ok, status, failed)) break;
+        Tp = T;
+        have_prev = true;
+        T = T2;
+        w = w2;
+    }
+    rt_finish(cta, P, it, have_prev, Tp.o, Tp.plane, Tp.ok, status, failed);
+    rt_teardown(cta);
+}
+
 // alpha * X * 2^-S2 + beta C for every instance. A work item is 64 rows x 8
 // columns of one instance; thread t takes the row pair t % 32 of column t / 32
 // (the 32 threads of a column read consecutive residue words).
@@ -2457,6 +2568,7 @@ struct OzGroupPlan {
     std::vector<OzGrpClass> classes;
     std::vector<int64_t> class_count;
     int64_t lines = 0, tiles = 0, items = 0;
+    bool res_tc = false;   // residues on the tensor cores (16-row conversion tiles)
     Moduli md;
     OzResParams rp;
     OzModParams mp;
@@ -2511,6 +2623,8 @@ bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, con
     int64_t kmax = 1;
     for (const OzGroupItem &it : items) kmax = std::max<int64_t>(kmax, it.k);
     pl->md = choose_moduli(2.0 * (kGroupBits - 1) + std::log2((double)kmax) + 1.0 + 4.0);
+    pl->res_tc = g_res_tc.load() != 0 && pl->md.n <= RT_MAX_MOD;
+    const int trows = pl->res_tc ? RT_ROWS : 32;   // conversion tile rows
     fill_res_params(pl->md, pl->rp, pl->mp);
     fill_crt_params(pl->md, pl->cp);
     const int L = pl->md.n;
@@ -2590,7 +2704,7 @@ bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, con
         d.line_begin = pl->lines;
         pl->lines += it.m + it.n;
         d.tile_begin = pl->tiles;
-        pl->tiles += ((it.m + 31) / 32 + (it.n + 31) / 32) * ((it.k + 31) / 32);
+        pl->tiles += ((it.m + trows - 1) / trows + (it.n + trows - 1) / trows) * ((it.k + 31) / 32);
         d.rec_begin = pl->items;
         pl->items += ((it.m + 63) / 64) * ((it.n + 7) / 8);
         (void)c;
@@ -2645,6 +2759,7 @@ bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, con
             return false;
     }
     cudaFuncSetAttribute(k_oz_gemm_tc_2sm, cudaFuncAttributeMaxDynamicSharedMemorySize, T2_SMEM);
+    if (pl->res_tc) cudaFuncSetAttribute(k_grp_residues_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, RT_SMEM);
     cudaStream_t st = stream();
     return cuda_ok(cudaMemcpyAsync(pl->d_descs, pl->descs.data(), pl->descs.size() * sizeof(OzGrpDesc),
                                    cudaMemcpyHostToDevice, st),
@@ -2662,8 +2777,12 @@ void ozgroup_launch(OzGroupPlan *pl, cudaStream_t s)
     const int L = pl->md.n;
     k_grp_exp<<<(unsigned)std::min<int64_t>((pl->lines + 255) / 256, (int64_t)sms * 8), 256, 0, s>>>(
         pl->d_descs, count, pl->lines, pl->d_ex);
-    k_grp_residues<<<(unsigned)std::min<int64_t>(pl->tiles, (int64_t)sms * 8), 256, 0, s>>>(
-        pl->d_descs, count, pl->tiles, pl->d_classes, pl->d_ex, kGroupBits, pl->rp);
+    if (pl->res_tc)
+        k_grp_residues_tc<<<(unsigned)std::min<int64_t>(pl->tiles, (int64_t)sms * 4), RT_THREADS, RT_SMEM, s>>>(
+            pl->d_descs, count, pl->tiles, pl->d_classes, pl->d_ex, kGroupBits, pl->rp, device_status_word());
+    else
+        k_grp_residues<<<(unsigned)std::min<int64_t>(pl->tiles, (int64_t)sms * 8), 256, 0, s>>>(
+            pl->d_descs, count, pl->tiles, pl->d_classes, pl->d_ex, kGroupBits, pl->rp);
     for (size_t ci = 0; ci < pl->classes.size(); ++ci) {
         const OzGrpClass &c = pl->classes[ci];
         const int nz = (int)(pl->class_count[ci] * L);

@@ -502,10 +502,11 @@ int mwblas_set_grouped_tile(int tile);
  * integer pipes only). No counterpart in the reference. */
 int mwblas_set_grouped_tensor_min(int size);
 int mwblas_grouped_tuned_tensor_min(void);
-/* mgemm_grouped packs the remaining instances with m, n <= 256 and k >= kmin
- * several to a 256 x 256 tensor-core slot (block-diagonal: each instance owns
- * its rows and output columns; the blocks mixing two instances are computed
- * and never read); 0 = none, -1 = the tuned or default choice. Returns the
+/* mgemm_grouped packs the remaining instances with k >= kmin several to a
+ * 256 x 256 tensor-core slot (block-diagonal: each instance owns its rows and
+ * output columns; the blocks mixing two instances are computed and never
+ * read), an instance with m or n above 256 as pieces of at most 256 x 256;
+ * 0 = none, -1 = the tuned or default choice. Returns the
  * previous setting; mwblas_grouped_tuned_tensor_pack returns the depth this
  * thread's most recent mgemm_grouped_tune chose (0 = none). No counterpart in
  * the reference. */

@@ -351,17 +351,20 @@ def test_grouped_gemm_tuner_chooses_tensor_threshold(gpu, oracle, rng):
     check(oracle, inst, arena)
 
 
-def _small_batch(rng, count):
+def _small_batch(rng, count, skinny=()):
     """Small instances (m, n <= 200) with k from 4 to 300: those with k >= the
     packing depth share 256 x 256 tensor-core slots, the rest stay on the
     integer pipes; odd m and n (a row pair straddles two instances of a slot),
-    every transpose pair, padded ldc, an Inf in one instance."""
+    every transpose pair, padded ldc, an Inf in one instance. `skinny` appends
+    instances of the given (m, n, k), shared as pieces of at most 256 x 256."""
     inst = []
-    for t in range(count):
+    for t in range(count + len(skinny)):
         m, n = (int(x) for x in rng.integers(1, 201, 2))
         k = int(rng.integers(4, 301))
         if t % 5 == 0:
             m, n = 2 * int(rng.integers(1, 30)) + 1, 2 * int(rng.integers(1, 30)) + 1
+        if t >= count:
+            m, n, k = skinny[t - count]
         ta, tb = str(rng.choice(["N", "T", "C"])), str(rng.choice(["N", "T"]))
         lda = (m if ta == "N" else k) + int(rng.integers(0, 3))
         ldb = (k if tb == "N" else n) + int(rng.integers(0, 3))
@@ -397,10 +400,11 @@ def _check_small(oracle, inst, outs):
 def test_grouped_gemm_shared_tensor_slots(gpu, oracle, rng, oz_min, pack_k):
     """Small instances packed several to a tensor-core slot (block-diagonal:
     own rows and output columns, K from 0), alone or beside instances with
-    slots of their own; within the GEMM tolerance, and a graph replay gives
-    the same bits."""
+    slots of their own, and skinny instances (m or n above 256) split into
+    pieces of at most 256 x 256; within the GEMM tolerance, and a graph replay
+    gives the same bits."""
     import torch
-    inst = _small_batch(rng, 60)
+    inst = _small_batch(rng, 60, skinny=[(600, 37, 100), (20, 530, 290), (513, 300, 40), (257, 1, 64)])
     prev_oz = gpu.lib.mwblas_set_grouped_tensor_min(oz_min)
     prev_pk = gpu.lib.mwblas_set_grouped_tensor_pack(pack_k)
     try:
