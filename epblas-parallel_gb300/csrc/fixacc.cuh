@@ -60,7 +60,10 @@ __device__ __forceinline__ void shl53(uint32_t hi, uint32_t lo, int s, uint32_t 
     t[3] = q ? a2 : 0u;
 }
 
-__device__ __forceinline__ Op decode(double2 v)
+// Every case: zeros, non-finite limbs, subnormals, lo far below or (not
+// normalised) above hi. Kept out of line: decode() calls it only off its fast
+// path, so the common case does not pay for these branches.
+static __device__ __noinline__ Op decode_general(double2 v)
 {
     Op o;
     const uint32_t hl = (uint32_t)__double2loint(v.x), hh = (uint32_t)__double2hiint(v.x);
@@ -118,6 +121,53 @@ __device__ __forceinline__ Op decode(double2 v)
                 : "r"(t[0]), "r"(t[1]), "r"(t[2]), "r"(t[3]));
         }
     }
+    return o;
+}
+
+// The same result as decode_general, with a straight-line path for the common
+// operands: hi normal and finite, and lo zero, or normal with its exponent 33
+// to 64 below hi's (lo's mantissa then lands in the low three words with a
+// left shift s = 64 - gap below 32; a normalised double-double has gap >= 53).
+// The sum W = hi's mantissa * 2^64 +- lo's shifted mantissa is formed as
+// W + (t ^ mask) + (mask & 1), mask = all ones when the signs differ.
+__device__ __forceinline__ Op decode(double2 v)
+{
+    const uint32_t hl = (uint32_t)__double2loint(v.x), hh = (uint32_t)__double2hiint(v.x);
+    const uint32_t ll = (uint32_t)__double2loint(v.y), lh = (uint32_t)__double2hiint(v.y);
+    const uint32_t eh = (hh >> 20) & 0x7FFu, el = (lh >> 20) & 0x7FFu;
+    const bool lo_zero = ((lh << 1) | ll) == 0u;
+    const uint32_t gap = eh - el;   // unsigned: wraps when lo's exponent is above hi's
+    const bool fast = (eh - 1u) < 0x7FEu && (lo_zero || ((el - 1u) < 0x7FEu && gap - 33u <= 31u));
+    if (!fast) {
+        if (((hh << 1) | hl) == 0u && el != 0x7FFu) {   // hi == +-0 (lo finite): zero
+            Op z;
+            z.w[0] = z.w[1] = z.w[2] = z.w[3] = 0u;
+            z.e = 0;
+            z.flags = (hh >> 31) | kZero;
+            return z;
+        }
+        return decode_general(v);
+    }
+    Op o;
+    o.flags = hh >> 31;
+    o.e = (int)eh - 1075 - 64;
+    const uint32_t mlh = lo_zero ? 0u : ((lh & 0xFFFFFu) | 0x100000u);
+    const uint32_t lw = lo_zero ? 0u : ll;
+    const int s = (int)(64u - gap) & 31;
+    const uint32_t t0 = lw << s, t1 = __funnelshift_l(lw, mlh, s), t2 = __funnelshift_l(mlh, 0u, s);
+    const uint32_t mask = 0u - ((hh ^ lh) >> 31);
+    uint32_t w0, w1, w2, w3;
+    asm("add.cc.u32 %0, %4, %8;\n\t"
+        "addc.cc.u32 %1, %5, 0;\n\t"
+        "addc.cc.u32 %2, %6, %9;\n\t"
+        "addc.u32 %3, %7, %10;"
+        : "=r"(w0), "=r"(w1), "=r"(w2), "=r"(w3)
+        : "r"(t0 ^ mask), "r"(t1 ^ mask), "r"(t2 ^ mask), "r"((hh & 0xFFFFFu) | 0x100000u), "r"(mask & 1u),
+          "r"(hl), "r"(mask));
+    o.w[0] = w0;
+    o.w[1] = w1;
+    o.w[2] = w2;
+    o.w[3] = w3;
     return o;
 }
 
