@@ -333,6 +333,14 @@ struct Acc {
     // += x * y, y given as digits
     __device__ __forceinline__ void add_dig(const Op &x, const Dig &y)
     {
+        add_core(x, y);
+        if (++cnt >= 2048) normalize();
+    }
+
+    // add_dig without the carry bookkeeping: the caller runs normalize()
+    // after at most 2048 of these (the column sums stay below 2^63).
+    __device__ __forceinline__ void add_core(const Op &x, const Dig &y)
+    {
         const uint32_t f = x.flags | y.flags;
         if (f & kBad) {
             bad = true;
@@ -360,14 +368,19 @@ struct Acc {
             for (int t = 0; t < 5; ++t) a[t] = -a[t];
         }
         const int *b = y.d;
-        c[0] += (long long)a[0] * b[3] + (long long)a[1] * b[2] + (long long)a[2] * b[1] + (long long)a[3] * b[0];
-        c[1] += (long long)a[0] * b[4] + (long long)a[1] * b[3] + (long long)a[2] * b[2] + (long long)a[3] * b[1] +
-                (long long)a[4] * b[0];
-        c[2] += (long long)a[1] * b[4] + (long long)a[2] * b[3] + (long long)a[3] * b[2] + (long long)a[4] * b[1];
-        c[3] += (long long)a[2] * b[4] + (long long)a[3] * b[3] + (long long)a[4] * b[2];
-        c[4] += (long long)a[3] * b[4] + (long long)a[4] * b[3];
-        c[5] += (long long)a[4] * b[4];
-        if (++cnt >= 2048) normalize();
+        // one 32 x 32 -> 64-bit multiply-add per digit product
+        madw(c[0], a[0], b[3]); madw(c[0], a[1], b[2]); madw(c[0], a[2], b[1]); madw(c[0], a[3], b[0]);
+        madw(c[1], a[0], b[4]); madw(c[1], a[1], b[3]); madw(c[1], a[2], b[2]); madw(c[1], a[3], b[1]);
+        madw(c[1], a[4], b[0]);
+        madw(c[2], a[1], b[4]); madw(c[2], a[2], b[3]); madw(c[2], a[3], b[2]); madw(c[2], a[4], b[1]);
+        madw(c[3], a[2], b[4]); madw(c[3], a[3], b[3]); madw(c[3], a[4], b[2]);
+        madw(c[4], a[3], b[4]); madw(c[4], a[4], b[3]);
+        madw(c[5], a[4], b[4]);
+    }
+
+    __device__ __forceinline__ static void madw(long long &acc, int x, int y)
+    {
+        asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(acc) : "r"(x), "r"(y));
     }
 
     // += a * b (decoded operands)

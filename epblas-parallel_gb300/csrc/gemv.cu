@@ -107,10 +107,18 @@ __global__ void __launch_bounds__(256) k_gemv_n_fx(int64_t m, int64_t n, const d
     acc.reset();
     const double2 *a = A + i;
     int64_t j = j0;
-    for (; j + 2 <= j1; j += 2) {
-        const double2 a0 = __ldcs(a + j * lda), a1 = __ldcs(a + (j + 1) * lda);
-        acc.add_dig(fx::decode(a0), xo[j]);
-        acc.add_dig(fx::decode(a1), xo[j + 1]);
+    // four columns in flight; carries propagated after each 2048 columns
+    while (j + 4 <= j1) {
+        const int64_t jend = min(j1, j + 2048);
+        for (; j + 4 <= jend; j += 4) {
+            const double2 a0 = __ldcs(a + j * lda), a1 = __ldcs(a + (j + 1) * lda);
+            const double2 a2 = __ldcs(a + (j + 2) * lda), a3 = __ldcs(a + (j + 3) * lda);
+            acc.add_core(fx::decode(a0), xo[j]);
+            acc.add_core(fx::decode(a1), xo[j + 1]);
+            acc.add_core(fx::decode(a2), xo[j + 2]);
+            acc.add_core(fx::decode(a3), xo[j + 3]);
+        }
+        acc.normalize();
     }
     for (; j < j1; ++j) acc.add_dig(fx::decode(a[j * lda]), xo[j]);
     part[blockIdx.y * m + i] = fx::to_pod(acc.finish(), acc.bad);

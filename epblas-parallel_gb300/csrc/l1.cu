@@ -456,7 +456,7 @@ __device__ bool block_any(bool b)
     return __syncthreads_or(b ? 1 : 0) != 0;
 }
 
-__global__ void __launch_bounds__(kThreads) k_mdot_partial(int64_t n, const double2 *__restrict__ x, int64_t incx,
+__global__ void __launch_bounds__(kThreads, 4) k_mdot_partial(int64_t n, const double2 *__restrict__ x, int64_t incx,
                                                           const double2 *__restrict__ y, int64_t incy,
                                                           fx::XFPod *part)
 {
@@ -475,13 +475,18 @@ __global__ void __launch_bounds__(kThreads) k_mdot_partial(int64_t n, const doub
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (incx == 1 && incy == 1) {
-        // two elements in flight per thread
-        for (; i + stride < n; i += 2 * stride) {
-            const double2 x0 = __ldcs(x + i), y0 = __ldcs(y + i);
-            const double2 x1 = __ldcs(x + i + stride), y1 = __ldcs(y + i + stride);
-            acc.add_prod(fx::decode(x0), fx::decode(y0));
-            acc.add_prod(fx::decode(x1), fx::decode(y1));
-            if ((cnt += 2) >= fx::kMaxAdds) fold();
+        // two elements in flight per thread; the column carries are
+        // propagated after each run of 2048 products, outside the inner loop
+        while (i + stride < n) {
+            const int64_t iend = i + 2 * stride * 1024;
+            for (; i + stride < n && i < iend; i += 2 * stride) {
+                const double2 x0 = __ldcs(x + i), y0 = __ldcs(y + i);
+                const double2 x1 = __ldcs(x + i + stride), y1 = __ldcs(y + i + stride);
+                acc.add_core(fx::decode(x0), fx::to_dig(fx::decode(y0)));
+                acc.add_core(fx::decode(x1), fx::to_dig(fx::decode(y1)));
+            }
+            acc.normalize();
+            if ((cnt += 2048) >= fx::kMaxAdds) fold();
         }
     }
     for (; i < n; i += stride) {
