@@ -96,21 +96,25 @@ __global__ void k_trsm_diag_right(int64_t c0, int nb, int64_t nrows, const doubl
 }
 
 // Inverses of the 32 x 32 diagonal blocks of op(A) (the last block may be
-// shorter), one CTA per block, thread per column c of the inverse: solve
-// op(A)_blk x = e_c by substitution over all rows (x is zero above c for a
-// lower triangle, so every thread walks the same rows and the block entries
-// are shared-memory broadcasts). The sums sum_p L(r,p) x(p) are accumulated
-// in integer fixed point (fixacc.cuh) and rounded once; each row is then
-// multiplied by the double-double reciprocal of the diagonal, as the
+// shorter), one CTA per block, four threads per column c of the inverse:
+// solve op(A)_blk x = e_c by substitution over all rows (x is zero above c
+// for a lower triangle, so every thread walks the same rows and the block
+// entries are shared-memory broadcasts). The four threads of a column split
+// each sum sum_p L(r,p) x(p) by p mod 4, accumulate their shares in integer
+// fixed point (fixacc.cuh) and add the four results as extended floats in a
+// fixed order (lanes 0 + 2, 1 + 3, then the two), rounded once; each row is
+// then multiplied by the double-double reciprocal of the diagonal, as the
 // reference's substitution does (mtrsm_serial.cpp:144).
-// Inv: block b at Inv + b*64*64, column-major with leading dimension 64.
+// Inv: block b at Inv + b*32*32, column-major with leading dimension 32.
 constexpr int kInvNB = 32;   // order of the directly inverted blocks (merged up to the leaf order)
+constexpr int kInvSplit = 4;  // threads per column
 
-__global__ void __launch_bounds__(kInvNB) k_trsm_diag_inv(int64_t na, const double2 *__restrict__ A, int64_t lda,
-                                                          bool trans, bool lower, bool unit, double2 *Inv)
+__global__ void __launch_bounds__(kInvNB * kInvSplit) k_trsm_diag_inv(int64_t na, const double2 *__restrict__ A,
+                                                                      int64_t lda, bool trans, bool lower, bool unit,
+                                                                      double2 *Inv)
 {
     extern __shared__ fx::OpPod smem_inv[];
-    fx::OpPod *sA = smem_inv;                    // [p][r]: sA[p * 64 + r] = -op(A)(o + r, o + p)
+    fx::OpPod *sA = smem_inv;                    // [p][r]: sA[p * 32 + r] = -op(A)(o + r, o + p)
     fx::OpPod *sX = smem_inv + kInvNB * kInvNB;  // [r][c]: x_c(r)
     __shared__ double2 sInvDiag[kInvNB];
     const int64_t o = (int64_t)blockIdx.x * kInvNB;
@@ -128,22 +132,31 @@ __global__ void __launch_bounds__(kInvNB) k_trsm_diag_inv(int64_t na, const doub
         sInvDiag[r] = make_double2(iv.hi, iv.lo);
     }
     __syncthreads();
-    const int c = threadIdx.x;
-    if (c >= nb) return;
+    const int c = threadIdx.x / kInvSplit, part = threadIdx.x % kInvSplit;
+    const bool active = c < nb;   // every lane stays for the shuffles
     const fx::Op one = fx::decode(make_double2(1.0, 0.0));
     double2 *out = Inv + (int64_t)blockIdx.x * kInvNB * kInvNB + (int64_t)c * kInvNB;
     for (int s = 0; s < nb; ++s) {
         const int r = lower ? s : nb - 1 - s;
         fx::Acc acc;
         acc.reset();
-        if (r == c) acc.add_prod(one, one);
-        const int p0 = lower ? 0 : r + 1, p1 = lower ? r : nb;
-        for (int p = p0; p < p1; ++p) acc.add_prod(fx::from_pod(sA[p * kInvNB + r]), fx::from_pod(sX[p * kInvNB + c]));
-        double h, l;
-        xfp::xf_to_dd(acc.finish(), h, l);
-        const dd::real v = dd::mul_fast(dd::make(h, l), dd::load(&sInvDiag[r]));
-        sX[r * kInvNB + c] = fx::to_pod(fx::decode(make_double2(v.hi, v.lo)));
-        out[r] = make_double2(v.hi, v.lo);
+        if (active) {
+            if (r == c && part == 0) acc.add_prod(one, one);
+            const int p0 = lower ? 0 : r + 1, p1 = lower ? r : nb;
+            for (int p = p0 + part; p < p1; p += kInvSplit)
+                acc.add_prod(fx::from_pod(sA[p * kInvNB + r]), fx::from_pod(sX[p * kInvNB + c]));
+        }
+        xfp::XF v = acc.finish();
+        v = xfp::xf_add(v, fx::xf_shfl_down(v, 2));   // parts 0 + 2, 1 + 3
+        v = xfp::xf_add(v, fx::xf_shfl_down(v, 1));   // (0 + 2) + (1 + 3)
+        if (active && part == 0) {
+            double h, l;
+            xfp::xf_to_dd(v, h, l);
+            const dd::real x = dd::mul_fast(dd::make(h, l), dd::load(&sInvDiag[r]));
+            sX[r * kInvNB + c] = fx::to_pod(fx::decode(make_double2(x.hi, x.lo)));
+            out[r] = make_double2(x.hi, x.lo);
+        }
+        __syncwarp();   // x_c(r) is read by the column's other three threads (same warp) from the next row on
     }
 }
 
@@ -444,8 +457,11 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
         // worth it or there are only a few of them; the 32 x 32 inverses are
         // doubled up to it by merging with grouped GEMMs
         // (512 for large triangles with many right-hand sides: half the GEMMs
-        // of 256 leaves, the two extra merge levels on the tensor cores)
-        const int64_t nb = (na >= 2048 && nrhs >= 512 && ozaki_available())                        ? 512
+        // of 256 leaves, the two extra merge levels on the tensor cores;
+        // 1024 from na = 4096: 7 instead of 15 GEMMs for one more merge level)
+        const bool big = nrhs >= 512 && ozaki_available();
+        const int64_t nb = (na >= 4096 && big)                                       ? 1024
+                           : (na >= 2048 && big)                                     ? 512
                            : (na >= 1024 && (nrhs >= 256 || nrhs < 2 * kTrsmLeaf)) ? 256
                                                                                     : kTrsmLeaf;
         const int64_t nblk64 = (na + kInvNB - 1) / kInvNB;
@@ -467,7 +483,7 @@ bool trsm_device(char side, char uplo, char transa, char diag, int64_t m, int64_
         w.T = (double2 *)((char *)scratch + 2 * buf_bytes + m_bytes);
         const size_t smem = 2 * (size_t)kInvNB * kInvNB * sizeof(fx::OpPod);
         cudaFuncSetAttribute(k_trsm_diag_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_trsm_diag_inv<<<(unsigned)nblk64, kInvNB, smem, stream()>>>(na, (const double2 *)A, lda, trans, lower,
+        k_trsm_diag_inv<<<(unsigned)nblk64, kInvNB * kInvSplit, smem, stream()>>>(na, (const double2 *)A, lda, trans, lower,
                                                                      unit, bufA);
         count_launch();
         double2 *cur = bufA, *nxt = bufB;

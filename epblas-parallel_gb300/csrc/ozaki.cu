@@ -2356,7 +2356,7 @@ struct OzGrpDesc {
     int m, n, k, ta, tb;
     int cls, slot;
     int64_t ea_off, eb_off;   // row exponents of op(A), column exponents of op(B)
-    int64_t line_begin;       // first exponent line: m rows of op(A), then n columns of op(B)
+    int64_t line_begin;       // first exponent work item: ceil(m/32) row groups of op(A), then ceil(n/32) column groups of op(B)
     int64_t tile_begin;       // first conversion tile: op(A)'s ceil(m/R) ceil(k/32), then op(B)'s ceil(n/R) ceil(k/32) (R = 16 on the tensor cores, else 32)
     int64_t rec_begin;        // first reconstruction item: ceil(m/64) row slabs x ceil(n/8) column groups
     xw::XW aM, xb;            // alpha * M and beta as extended floats
@@ -2389,23 +2389,55 @@ __device__ __forceinline__ int grp_exp_bound(double x)
     return b == 0 ? kNoExp : (int)(b >> 52) - 1023;
 }
 
-// Exponent bound of every row of op(A) and column of op(B): a warp per line,
-// lanes over its k entries.
-__global__ void k_grp_exp(const OzGrpDesc *__restrict__ descs, int count, int64_t lines, int *__restrict__ ex)
+// Exponent bound of every row of op(A) and column of op(B). A work item is a
+// group of 32 consecutive lines of one operand (line_begin counts groups:
+// ceil(m/32) of op(A), then ceil(n/32) of op(B)), taken by a block of eight
+// warps: lines contiguous along k are split among the warps, each walked with
+// the lanes over k; lines strided along k (rows of A, columns of B^T) take a
+// lane each and the warps split k, so every load reads 32 neighbouring lines
+// of one k (coalesced either way), and the eight partial maxima meet in
+// shared memory.
+__global__ void __launch_bounds__(256) k_grp_exp(const OzGrpDesc *__restrict__ descs, int count, int64_t lines,
+                                                 int *__restrict__ ex)
 {
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t w = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); w < lines; w += warps) {
+    __shared__ int part[8][33];
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    for (int64_t w = blockIdx.x; w < lines; w += gridDim.x) {
         const OzGrpDesc &d = descs[grp_find(descs, count, w, 0)];
-        const int64_t t = w - d.line_begin;
-        const bool row = t < d.m;   // row t of op(A), else column t - m of op(B)
-        const int64_t j = t - d.m;
-        const double2 *p = row ? (d.ta ? d.A + t * d.lda : d.A + t) : (d.tb ? d.B + j : d.B + j * d.ldb);
-        const int64_t step = row ? (d.ta ? 1 : d.lda) : (d.tb ? d.ldb : 1);
-        int e = kNoExp;
-        for (int q = lane; q < d.k; q += 32) e = max(e, grp_exp_bound(p[q * step].x));
-        for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_down_sync(0xffffffffu, e, off));
-        if (lane == 0) ex[row ? d.ea_off + t : d.eb_off + j] = e;
+        const int ga = (d.m + 31) / 32;
+        int g = (int)(w - d.line_begin);
+        const bool isA = g < ga;
+        if (!isA) g -= ga;
+        const int nl = isA ? d.m : d.n, l0 = 32 * g, l1 = min(nl, l0 + 32);
+        const double2 *X = isA ? d.A : d.B;
+        const int64_t ld = isA ? d.lda : d.ldb;
+        // line t of op(A) is A's column t (A^T) or row t; line j of op(B) is B's column j or row j (B^T)
+        const bool along_k = isA ? d.ta : !d.tb;
+        int *out = ex + (isA ? d.ea_off : d.eb_off);
+        if (along_k) {
+            for (int t = l0 + wq; t < l1; t += 8) {
+                const double2 *p = X + (int64_t)t * ld;
+                int e = kNoExp;
+                for (int q = lane; q < d.k; q += 32) e = max(e, grp_exp_bound(p[q].x));
+                for (int off = 16; off > 0; off >>= 1) e = max(e, __shfl_down_sync(0xffffffffu, e, off));
+                if (lane == 0) out[t] = e;
+            }
+        } else {
+            const int t = l0 + lane;
+            int e = kNoExp;
+            if (t < l1) {
+                const double2 *p = X + t;
+                for (int q = wq; q < d.k; q += 8) e = max(e, grp_exp_bound(p[(int64_t)q * ld].x));
+            }
+            part[wq][lane] = e;
+            __syncthreads();
+            if (wq == 0 && t < l1) {
+#pragma unroll
+                for (int u = 1; u < 8; ++u) e = max(e, part[u][lane]);
+                out[t] = e;
+            }
+            __syncthreads();   // part is reused by the next item
+        }
     }
 }
 
@@ -2702,7 +2734,7 @@ bool ozgroup_prepare(OzGroupPlan *pl, const std::vector<OzGroupItem> &items, con
         exn += it.m + it.n;
         const OzGrpClass &c = pl->classes[ci];
         d.line_begin = pl->lines;
-        pl->lines += it.m + it.n;
+        pl->lines += (it.m + 31) / 32 + (it.n + 31) / 32;
         d.tile_begin = pl->tiles;
         pl->tiles += ((it.m + trows - 1) / trows + (it.n + trows - 1) / trows) * ((it.k + 31) / 32);
         d.rec_begin = pl->items;
@@ -2775,7 +2807,7 @@ void ozgroup_launch(OzGroupPlan *pl, cudaStream_t s)
     const int count = (int)pl->descs.size();
     const int sms = device_sm_count();
     const int L = pl->md.n;
-    k_grp_exp<<<(unsigned)std::min<int64_t>((pl->lines + 255) / 256, (int64_t)sms * 8), 256, 0, s>>>(
+    k_grp_exp<<<(unsigned)std::min<int64_t>(pl->lines, (int64_t)sms * 8), 256, 0, s>>>(
         pl->d_descs, count, pl->lines, pl->d_ex);
     if (pl->res_tc)
         k_grp_residues_tc<<<(unsigned)std::min<int64_t>(pl->tiles, (int64_t)sms * 4), RT_THREADS, RT_SMEM, s>>>(

@@ -270,6 +270,33 @@ def test_mtrsm_512_leaves(gpu, oracle, rng, side, uplo, ta, diag):
     assert err <= 1e-28, err
 
 
+@pytest.mark.parametrize("side,uplo,ta,diag", [("L", "L", "N", "N"), ("L", "U", "T", "U"), ("R", "U", "N", "N"),
+                                               ("R", "L", "T", "N")])
+def test_mtrsm_1024_leaves(gpu, oracle, rng, side, uplo, ta, diag):
+    """order >= 4096 with >= 512 right-hand sides: 1024 x 1024 leaf inverses
+    (five merge levels, the last three on the tensor cores), a partial last
+    leaf; 4 sampled right-hand sides against the oracle."""
+    na, nr = 4100, 512
+    m, n = (na, nr) if side == "L" else (nr, na)
+    A = dominant_triangle(rng, na, na)
+    B0 = mwb.dd_matrix(rng, m, n, m)
+    al = mwb.random_dd(rng, ())
+    got = B0.copy()
+    gpu.mtrsm(side, uplo, ta, diag, m, n, al, A, na, got, m)
+    assert gpu.last_error()[0] == 0, gpu.last_error()
+    pick = np.sort(rng.choice(nr, 4, replace=False))
+    if side == "L":
+        sub = np.ascontiguousarray(B0[pick])
+        oracle.qtrsm("L", uplo, ta, diag, na, 4, al, A, na, sub, na)
+        g = got[pick]
+    else:
+        sub = np.ascontiguousarray(B0[:, pick])
+        oracle.qtrsm("R", uplo, ta, diag, 4, na, al, A, na, sub, 4)
+        g = got[:, pick]
+    err = orc.normwise_error(g, sub, orc.dd_abs(al) * orc.dd_absmax(B0))
+    assert err <= 1e-28, err
+
+
 @pytest.mark.parametrize("trans", ["N", "T"])
 def test_mgemv(gpu, oracle, rng, trans):
     for (m, n, incx, incy) in [(1, 1, 1, 1), (17, 9, 1, 1), (300, 70, 2, -1), (70, 300, -3, 2), (1000, 4000, 1, 1)]:
