@@ -487,7 +487,7 @@ def tc_traffic_from_profile():
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("dram_bytes_per_launch_scaled:"):
+        if line.startswith("dram_bytes_per_launch_8192:"):
             return float(line.split(":")[1].strip())
     return None
 
