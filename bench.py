@@ -299,13 +299,25 @@ def cpu_baseline_leg(n, res):
             pl["normwise_err_vs_binary128"] = orc.normwise_error(pgot, pwant, op)
             pl["err_samples"] = 256
     # CPU timing on a bounded sample of the same workload
-    t = time_reference_cpu(sample=(4096, 4096, 256), reps=1)
+    t = time_reference_cpu(sample=(4096, 4096, 256), reps=1, single_thread=True)
     out["cpu"] = t
     return out
 
 
-def time_reference_cpu(sample=(4096, 4096, 256), reps=1):
-    """Times the reference's GEMM on the host cores with all threads."""
+def _omp_threads(nt):
+    """Sets the OpenMP team size of this process (libgomp: the oracle and the
+    reference build share it); False where no libgomp is loaded."""
+    try:
+        import ctypes
+        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(nt))
+        return True
+    except (OSError, AttributeError):
+        return False
+
+
+def _cpu_gemm_runner(sample):
+    """The reference's GEMM on the host cores: its own build where present
+    (x86), else the C port of its algorithm; returns (runner, kind)."""
     m, n, k = sample
     rng = np.random.default_rng(5)
     mwb = ge._load("mwblas", os.path.join(ge.PKG, "mwblas.py"))
@@ -314,25 +326,20 @@ def time_reference_cpu(sample=(4096, 4096, 256), reps=1):
     C = mwb.dd_matrix(rng, m, n)
     al, be = np.array([1.1, 0.0]), np.array([0.9, 0.0])
     ref_so = os.path.join(ROOT, "oracle", "_ref", "libmwblas_ref.so")
-    kind = "port"
-    runner = None
     try:
         if os.path.exists(ref_so):
             ref = mwb.MWBlas(ref_so, extensions=False)
-
-            def runner():
-                ref.mgemm("N", "N", m, n, k, al, A, m, B, k, be, C, m)
-            kind = "reference"
+            return (lambda: ref.mgemm("N", "N", m, n, k, al, A, m, B, k, be, C, m)), "reference"
     except OSError:
-        runner = None
-    if runner is None:
-        orc = ge._load("oracle", os.path.join(ROOT, "oracle", "oracle.py"))
-        o = orc.Oracle()
-        import platform
-        simd = 1 if platform.machine() in ("x86_64", "AMD64") else 0
+        pass
+    orc = ge._load("oracle", os.path.join(ROOT, "oracle", "oracle.py"))
+    o = orc.Oracle()
+    import platform
+    simd = 1 if platform.machine() in ("x86_64", "AMD64") else 0
+    return (lambda: o.port_mgemm("N", "N", m, n, k, al, A, m, B, k, be, C, m, simd_order=simd)), "port"
 
-        def runner():
-            o.port_mgemm("N", "N", m, n, k, al, A, m, B, k, be, C, m, simd_order=simd)
+
+def _best_seconds(runner, reps):
     runner()   # warm
     best = None
     for _ in range(reps):
@@ -340,11 +347,30 @@ def time_reference_cpu(sample=(4096, 4096, 256), reps=1):
         runner()
         dt = time.perf_counter() - t0
         best = dt if best is None else min(best, dt)
+    return best
+
+
+def time_reference_cpu(sample=(4096, 4096, 256), reps=1, single_thread=False):
+    """Times the reference's GEMM on the host cores with all threads (and, on
+    request, with one thread on a 512 x 512 x 256 sample)."""
+    m, n, k = sample
+    runner, kind = _cpu_gemm_runner(sample)
+    best = _best_seconds(runner, reps)
     cores = int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or os.cpu_count()
     import platform
-    return {"value": 2.0 * m * n * k / best / 1e9, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": f"mgemm_ {m}x{n}x{k} NN alpha=1.1 beta=0.9 ({platform.machine()}, min of {reps} after 1 warm-up,"
-                      f" {best:.2f} s per call)"}
+    out = {"value": 2.0 * m * n * k / best / 1e9, "unit": UNIT, "cores": cores, "kind": kind,
+           "sample": f"mgemm_ {m}x{n}x{k} NN alpha=1.1 beta=0.9 ({platform.machine()}, min of {reps} after 1 warm-up,"
+                     f" {best:.2f} s per call)"}
+    if single_thread and _omp_threads(1):
+        try:
+            s1 = (512, 512, 256)
+            r1, _ = _cpu_gemm_runner(s1)
+            b1 = _best_seconds(r1, 3)
+            out["single_thread"] = {"value": 2.0 * s1[0] * s1[1] * s1[2] / b1 / 1e9, "unit": UNIT, "cores": 1,
+                                    "sample": "mgemm_ 512x512x256, min of 3 after 1 warm-up"}
+        finally:
+            _omp_threads(cores)
+    return out
 
 
 def main():
@@ -387,11 +413,14 @@ def main():
         steps = []
         for _ in range(args.warmup):
             time_reference_cpu(reps=1)
-        for _ in range(args.steps):
-            steps.append(time_reference_cpu(reps=1))
+        for i in range(args.steps):
+            steps.append(time_reference_cpu(reps=1, single_thread=(i == args.steps - 1)))
         v = float(np.median([s["value"] for s in steps]))
         cb = dict(steps[-1])
         cb["value"] = v
+        cb["sample"] += f"; median of {args.steps} steps"
+        # the rate does not hinge on the K = 256 slab: on 8 x86 cores the reference's own
+        # build ran 17.2 GFLOP/s at 2048x2048x256 and 16.4 at 1536^3
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 2.0 * 4096 * 4096 * 256 / v / 1e6,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64x2 (double-double)",
