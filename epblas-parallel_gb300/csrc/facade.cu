@@ -274,7 +274,9 @@ void gemm_entry(const char *routine, bool cplx, int force_engine, const char *tr
         g.hs = &hs;
         const bool ok = run_gemm(g, cplx, force_engine, routine);
         // whatever happened, nothing may be freed before the copies are done
-        const bool joined = hs.wait_all(routine) && join_copy_stream(routine);
+        // (copies back still noted after a failure are queued all the same)
+        const bool flushed = flush_columns_back(SC, routine);
+        const bool joined = hs.wait_all(routine) && join_copy_stream(routine) && flushed;
         if (!ok || !joined) return;
         if (!hs.c_written && !unstage_matrix(SC, routine)) return;
         finish(routine);

@@ -2300,6 +2300,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
         }
         // the buffers are freed on this stream: order that after the side
         // stream's kernels and the copies back
+        if (hs && !flush_columns_back(*hs->c, routine)) ok = false;
         if (!order_streams(side, main_s, routine)) ok = false;
         if (ok && hs) {
             ok = join_copy_stream(routine);
@@ -2316,6 +2317,7 @@ bool gemm_ozaki(const GemmArgs &g0, bool cplx, int bits_req, const char *routine
             reconstruct_cols(j0, nn);
             if (chunked) ok = unstage_columns_async(*hs->c, j0, j0 + nn, routine);
         }
+        if (chunked && !flush_columns_back(*hs->c, routine)) ok = false;
         if (ok && chunked) {
             ok = join_copy_stream(routine);
             hs->c_written = ok;

@@ -1,6 +1,7 @@
 // Host runtime: errors, streams, device scratch and host<->device staging.
 #include "runtime.h"
 
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
@@ -197,6 +198,83 @@ void *tensor_map_encoder()
     return fn;
 }
 
+namespace {
+
+// Whether kernels of the current device may read pageable host memory through
+// the system's page tables (coherent CPU-GPU systems); per device, cached.
+bool device_reads_pageable()
+{
+    static int cached[64];   // 0 unknown, 1 yes, 2 no
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int &c = cached[dev & 63];
+    if (c == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+            cudaGetLastError();
+            v = 0;
+        }
+        c = v ? 1 : 2;
+    }
+    return c == 1;
+}
+
+bool is_pageable_host(const void *p)
+{
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeUnregistered;
+}
+
+// Columns of 16-byte words from pageable host memory into device memory, read
+// by the kernel in place. Few blocks: it runs beside the product's kernels
+// and only needs enough loads in flight to cover the host link.
+__global__ void __launch_bounds__(512) k_copy_from_host(const uint4 *__restrict__ src, int64_t spitch,
+                                                        uint4 *__restrict__ dst, int64_t dpitch, int64_t words,
+                                                        int64_t cols)
+{
+    for (int64_t c = blockIdx.y; c < cols; c += gridDim.y) {
+        const uint4 *s = src + c * spitch;
+        uint4 *d = dst + c * dpitch;
+        const int64_t step = (int64_t)gridDim.x * blockDim.x;
+        int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        for (; i + 3 * step < words; i += 4 * step) {
+            const uint4 a = s[i], b = s[i + step], e = s[i + 2 * step], f = s[i + 3 * step];
+            d[i] = a;
+            d[i + step] = b;
+            d[i + 2 * step] = e;
+            d[i + 3 * step] = f;
+        }
+        for (; i < words; i += step) d[i] = s[i];
+    }
+}
+
+// Rows [r0, r1) x columns [c0, c1) of a staged matrix from its pageable host
+// array on stream cs; false (nothing queued) when the layout is not in
+// 16-byte words.
+bool copy_block_from_pageable(Staged &s, int64_t r0, int64_t r1, int64_t c0, int64_t c1, cudaStream_t cs,
+                              const char *routine)
+{
+    const size_t pitch = (size_t)s.ld * s.elem, off = (size_t)c0 * pitch + (size_t)r0 * s.elem;
+    const size_t wbytes = (size_t)(r1 - r0) * s.elem;
+    if ((((uintptr_t)s.host + off) & 15) || (pitch & 15) || (wbytes & 15)) return false;
+    const int64_t words = (int64_t)(wbytes / 16), cols = c1 - c0;
+    // 128 blocks at most (2 x 8 gave 34.8 ms per 8192^3 call on pageable arrays,
+    // 4 x 32 32.7, 8 x 64 36.2: more blocks take SMs from the product)
+    const unsigned gx = (unsigned)std::min<int64_t>(4, (words + 511) / 512);
+    const unsigned gy = (unsigned)std::min<int64_t>(cols, 32);
+    k_copy_from_host<<<dim3(gx, gy), 512, 0, cs>>>((const uint4 *)((const char *)s.host + off), (int64_t)(pitch / 16),
+                                                   (uint4 *)((char *)s.dev + off), (int64_t)(pitch / 16), words,
+                                                   cols);
+    count_launch();
+    return cuda_ok(cudaGetLastError(), routine, "copy kernel launch");
+}
+
+}  // namespace
+
 bool stage_matrix(Staged &s, const void *host, int64_t rows, int64_t cols, int64_t ld, size_t elem,
                   bool copy_in, const char *routine)
 {
@@ -215,6 +293,7 @@ bool stage_matrix(Staged &s, const void *host, int64_t rows, int64_t cols, int64
     s.dev = dev_alloc(bytes, routine);
     if (!s.dev) return false;
     s.owned = true;
+    s.pageable = device_reads_pageable() && is_pageable_host(host);
     if (copy_in) {
         if (!cuda_ok(cudaMemcpy2DAsync(s.dev, (size_t)ld * elem, host, (size_t)ld * elem, (size_t)rows * elem,
                                        (size_t)cols, cudaMemcpyDefault, stream()),
@@ -298,9 +377,10 @@ bool stage_matrix_async(Staged &s, const void *host, int64_t rows, int64_t cols,
         return false;
     }
     if (!order(stream(), cs, routine)) return false;
-    if (!cuda_ok(cudaMemcpy2DAsync(s.dev, (size_t)ld * elem, host, (size_t)ld * elem, (size_t)rows * elem,
-                                   (size_t)cols, cudaMemcpyDefault, cs),
-                 routine, "copy matrix to device"))
+    const bool direct = s.pageable && copy_block_from_pageable(s, 0, rows, 0, cols, cs, routine);
+    if (!direct && !cuda_ok(cudaMemcpy2DAsync(s.dev, (size_t)ld * elem, host, (size_t)ld * elem,
+                                              (size_t)rows * elem, (size_t)cols, cudaMemcpyDefault, cs),
+                            routine, "copy matrix to device"))
         return false;
     if (!cuda_ok(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), routine, "event create")) {
         ready = nullptr;
@@ -312,6 +392,16 @@ bool stage_matrix_async(Staged &s, const void *host, int64_t rows, int64_t cols,
 bool unstage_columns_async(Staged &s, int64_t j0, int64_t j1, const char *routine)
 {
     if (!s.owned || s.rows <= 0 || j1 <= j0) return true;
+    if (s.pageable) {
+        cudaEvent_t e = nullptr;
+        if (!cuda_ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), routine, "event create")) return false;
+        if (!cuda_ok(cudaEventRecord(e, stream()), routine, "event record")) {
+            cudaEventDestroy(e);
+            return false;
+        }
+        s.deferred.push_back(Staged::Deferred{j0, j1, e});
+        return true;
+    }
     cudaStream_t cs = copy_stream();
     if (!order(stream(), cs, routine)) return false;
     const size_t pitch = (size_t)s.ld * s.elem;
@@ -319,6 +409,23 @@ bool unstage_columns_async(Staged &s, int64_t j0, int64_t j1, const char *routin
                                      (char *)s.dev + (size_t)j0 * pitch, pitch, (size_t)s.rows * s.elem,
                                      (size_t)(j1 - j0), cudaMemcpyDefault, cs),
                    routine, "copy matrix columns to host");
+}
+
+bool flush_columns_back(Staged &s, const char *routine)
+{
+    bool ok = true;
+    cudaStream_t cs = copy_stream();
+    const size_t pitch = (size_t)s.ld * s.elem;
+    for (Staged::Deferred &d : s.deferred) {
+        ok = ok && cuda_ok(cudaStreamWaitEvent(cs, d.after, 0), routine, "stream wait") &&
+             cuda_ok(cudaMemcpy2DAsync((char *)const_cast<void *>(s.host) + (size_t)d.j0 * pitch, pitch,
+                                       (char *)s.dev + (size_t)d.j0 * pitch, pitch, (size_t)s.rows * s.elem,
+                                       (size_t)(d.j1 - d.j0), cudaMemcpyDefault, cs),
+                     routine, "copy matrix columns to host");
+        cudaEventDestroy(d.after);
+    }
+    s.deferred.clear();
+    return ok;
 }
 
 bool wait_event(cudaEvent_t e, const char *routine)
@@ -348,9 +455,10 @@ bool upload_block_async(Staged &s, int64_t r0, int64_t r1, int64_t c0, int64_t c
     cudaStream_t cs = copy_stream();
     if (!order(stream(), cs, routine)) return false;
     const size_t pitch = (size_t)s.ld * s.elem, off = (size_t)c0 * pitch + (size_t)r0 * s.elem;
-    if (!cuda_ok(cudaMemcpy2DAsync((char *)s.dev + off, pitch, (const char *)s.host + off, pitch,
-                                   (size_t)(r1 - r0) * s.elem, (size_t)(c1 - c0), cudaMemcpyDefault, cs),
-                 routine, "copy matrix block to device"))
+    const bool direct = s.pageable && copy_block_from_pageable(s, r0, r1, c0, c1, cs, routine);
+    if (!direct && !cuda_ok(cudaMemcpy2DAsync((char *)s.dev + off, pitch, (const char *)s.host + off, pitch,
+                                              (size_t)(r1 - r0) * s.elem, (size_t)(c1 - c0), cudaMemcpyDefault, cs),
+                            routine, "copy matrix block to device"))
         return false;
     if (!cuda_ok(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), routine, "event create")) {
         ready = nullptr;

@@ -72,6 +72,15 @@ struct Staged {
     int64_t rows = 0, cols = 0, ld = 0;   // matrix shape (column-major)
     int64_t n = 0, inc = 0;               // vector shape
     bool is_vector = false;
+    // Pageable host memory that the device reads in place (system page
+    // tables): uploads run as copy kernels, which never block the host,
+    // and the column copies back are queued once the product is enqueued.
+    bool pageable = false;
+    struct Deferred {
+        int64_t j0, j1;
+        cudaEvent_t after;
+    };
+    std::vector<Deferred> deferred;
 };
 
 // Matrix rows x cols with leading dimension ld (elements of `elem` bytes).
@@ -92,8 +101,13 @@ cudaStream_t copy_stream();
 bool stage_matrix_async(Staged &s, const void *host, int64_t rows, int64_t cols, int64_t ld, size_t elem,
                         bool copy_in, cudaEvent_t &ready, const char *routine);
 // Queues the copy of columns [j0, j1) of a staged matrix back to the caller's
-// array on copy_stream(), after the work queued so far on stream().
+// array on copy_stream(), after the work queued so far on stream(). For
+// pageable host memory (a copy to it returns only when done) the copy is
+// noted and queued by flush_columns_back.
 bool unstage_columns_async(Staged &s, int64_t j0, int64_t j1, const char *routine);
+// Queues the noted copies back, in order (each returns once its columns are
+// on the host; the kernels queued before keep the device busy meanwhile).
+bool flush_columns_back(Staged &s, const char *routine);
 // A third per-thread stream, for kernels that run beside those of stream()
 // (created on first use, per device).
 cudaStream_t side_stream();
