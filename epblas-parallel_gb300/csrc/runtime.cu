@@ -198,8 +198,6 @@ void *tensor_map_encoder()
     return fn;
 }
 
-namespace {
-
 // Whether kernels of the current device may read pageable host memory through
 // the system's page tables (coherent CPU-GPU systems); per device, cached.
 bool device_reads_pageable()
@@ -218,6 +216,8 @@ bool device_reads_pageable()
     }
     return c == 1;
 }
+
+namespace {
 
 bool is_pageable_host(const void *p)
 {
@@ -580,6 +580,12 @@ void mwblas_clear_error(void) { mw::clear_error(); }
 void mwblas_debug_fail_alloc_after(int64_t count) { mw::g_fail_alloc_after.store(count); }
 int64_t mwblas_launch_count(void) { return mw::g_launches.load(); }
 int64_t mwblas_set_l1_partition(int64_t team) { return mw::g_l1_team.exchange(team < 0 ? 0 : team); }
+
+int mwblas_pageable_direct(void)
+{
+    mw::clear_error();
+    return mw::ensure_device("mwblas_pageable_direct") && mw::device_reads_pageable() ? 1 : 0;
+}
 
 int mwblas_set_stream(void *cuda_stream)
 {

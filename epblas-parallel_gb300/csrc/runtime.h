@@ -108,6 +108,9 @@ bool unstage_columns_async(Staged &s, int64_t j0, int64_t j1, const char *routin
 // Queues the noted copies back, in order (each returns once its columns are
 // on the host; the kernels queued before keep the device busy meanwhile).
 bool flush_columns_back(Staged &s, const char *routine);
+// Whether kernels of the current device read pageable host memory through the
+// system page tables (then uploads from pageable arrays run as copy kernels).
+bool device_reads_pageable();
 // A third per-thread stream, for kernels that run beside those of stream()
 // (created on first use, per device).
 cudaStream_t side_stream();

@@ -153,6 +153,7 @@ class MWBlas:
             self._sig("mwblas_set_l1_partition", _i64, [_i64])
             self._sig("mwblas_set_stream", _i32, [_p])
             self._sig("mwblas_set_sync", _i32, [_i32])
+            self._sig("mwblas_pageable_direct", _i32, [])
             self._sig("mwblas_last_error", _i32, [])
             self._sig("mwblas_last_error_message", _ch, [])
             self._sig("mwblas_last_error_routine", _ch, [])

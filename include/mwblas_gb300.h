@@ -580,6 +580,11 @@ int64_t mwblas_set_l1_partition(int64_t team);
  * their work is enqueued (host-pointer calls always synchronise). */
 int mwblas_set_stream(void *cuda_stream);       /* cudaStream_t; NULL = default */
 int mwblas_set_sync(int sync);                  /* returns previous */
+/* 1 when the current device reads pageable host memory in place (through the
+ * system page tables, as on the GB300's coherent host link): the pipelined
+ * GEMM then uploads ordinary (pageable) host arrays with device reads that
+ * overlap its kernels. 0 otherwise. No counterpart in the reference. */
+int mwblas_pageable_direct(void);
 
 /* Errors. */
 enum {

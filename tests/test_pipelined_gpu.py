@@ -101,3 +101,32 @@ def test_host_pipeline_allocation_failure(gpu, rng, fail_at):
     gpu.mgemm("N", "N", m, n, k, al, A, m, B, k, be, C, m, engine="ozaki")
     assert gpu.last_error()[0] == 0, gpu.last_error()
     assert np.array_equal(C.view(np.uint64), want.view(np.uint64))
+
+
+def test_pageable_arrays_read_in_place(gpu, rng):
+    """Where the device reads pageable host memory through the system page
+    tables, the pipelined GEMM uploads ordinary numpy arrays with copy
+    kernels (one per operand block, counted among the library's launches)
+    rather than with copies that would stall the host; pinned arrays keep the
+    copy engines. The results are the same bits either way."""
+    m, n, k = 1531, 1283, 1100
+    A = mwb.random_dd(rng, (k, m))
+    B = mwb.random_dd(rng, (n, k))
+    C0 = mwb.random_dd(rng, (n, m))
+    al, be = mwb.random_dd(rng, ()), mwb.random_dd(rng, ())
+    outs, launches = [], []
+    for pinned in (True, False):
+        hA, pa = _host(A, pinned)
+        hB, pb = _host(B, pinned)
+        hC, pc = _host(C0.copy(), pinned)
+        l0 = gpu.lib.mwblas_launch_count()
+        gpu.mgemm("N", "N", m, n, k, al, pa, m, pb, k, be, pc, m, engine="ozaki")
+        assert gpu.last_error()[0] == 0, gpu.last_error()
+        launches.append(gpu.lib.mwblas_launch_count() - l0)
+        outs.append((hC.numpy() if pinned else hC).copy())
+    assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
+    if gpu.lib.mwblas_pageable_direct():
+        # A whole, B and C in three column blocks each: at least 5 copy kernels
+        assert launches[1] >= launches[0] + 5, launches
+    else:
+        assert launches[1] == launches[0], launches
