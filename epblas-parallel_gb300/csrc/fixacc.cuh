@@ -357,7 +357,33 @@ struct Acc {
             raise(nb - B);
             B = nb;
         }
-        const int sh = B - ep;   // >= 2: X' = X >> sh < 2^116
+        mul_at(x, y, B - ep);   // B - ep >= 2: X' = X >> sh < 2^116
+    }
+
+    // The block exponent set beforehand: B = ep_max + 4 for a bound ep_max on
+    // the exponents x.e + y.e of every product that follows (then add_at
+    // never has to move it).
+    __device__ __forceinline__ void preset(int ep_max)
+    {
+        B = ep_max + 4;
+        init = true;
+    }
+
+    // add_core after preset(): no first-term or raise branches
+    __device__ __forceinline__ void add_at(const Op &x, const Dig &y)
+    {
+        const uint32_t f = x.flags | y.flags;
+        if (f & kBad) {
+            bad = true;
+            return;
+        }
+        if (f & kZero) return;
+        mul_at(x, y, B - (x.e + y.e));
+    }
+
+    // += X' * Y at the block, X' = X >> sh (sh >= 2)
+    __device__ __forceinline__ void mul_at(const Op &x, const Dig &y, int sh)
+    {
         if (sh >= 118) return;
         uint32_t xs[4];
         shr128(x.w, sh, xs);

@@ -13,6 +13,9 @@
 // one right-hand side or a rank of one, so the arithmetic is the engines'
 // (exact fixed point or tensor-core residues) and the error bounds are the
 // level-3 ones.
+#include <atomic>
+#include <climits>
+
 #include "dd.cuh"
 #include "fixacc.cuh"
 #include "level2x.h"
@@ -246,6 +249,16 @@ __device__ __forceinline__ double2 smv_round(dd::real b, bool have_b, xfp::XF t)
     return make_double2(h, l);
 }
 
+// y := beta*y + alpha*s for a real row sum s (alpha as an extended float).
+__device__ __forceinline__ void smv_store_real(double2 *py, const xfp::XF &xar, dd::real br, int beta_kind,
+                                               const xfp::XF &s)
+{
+    dd::real b = dd::make(0.0, 0.0);
+    if (beta_kind == 1) b = dd::load(py);
+    else if (beta_kind == 2) b = dd::mul_exact(br, dd::load(py));
+    py[0] = smv_round(b, beta_kind != 0, xfp::xf_mul(xar, s));
+}
+
 template <bool CX, int T>
 __global__ void __launch_bounds__(256) k_smv(SmvParams p)
 {
@@ -303,10 +316,7 @@ __global__ void __launch_bounds__(256) k_smv(SmvParams p)
         }
         const xfp::XF xar = xfp::xf_from_dd(p.ar.hi, p.ar.lo);
         if (!CX) {
-            dd::real b = dd::make(0.0, 0.0);
-            if (p.beta_kind == 1) b = dd::load(py);
-            else if (p.beta_kind == 2) b = dd::mul_exact(p.br, dd::load(py));
-            py[0] = smv_round(b, p.beta_kind != 0, xfp::xf_mul(xar, tot[0]));
+            smv_store_real(py, xar, p.br, p.beta_kind, tot[0]);
         } else {
             const xfp::XF xai = xfp::xf_from_dd(p.ai.hi, p.ai.lo);
             const xfp::XF tr = xfp::xf_add(xfp::xf_mul(xar, tot[0]), xneg(xfp::xf_mul(xai, tot[1])));
@@ -327,6 +337,122 @@ __global__ void __launch_bounds__(256) k_smv(SmvParams p)
             py[1] = yi;
         }
     }
+}
+
+// ---- real symmetric band product from a shared-memory tile ---------------------------
+// For bandwidth k <= kSbMaxK. A thread per row reading its band row straight
+// from band storage walks the array at a stride of ldab entries (every warp
+// load touches 32 lines), which bounds k_smv on the L1. Here a block of
+// kSbRows threads owns kSbRows consecutive rows and first copies, with
+// coalesced loads, every stored column those rows touch (upper storage:
+// columns [r0, r0 + R + k); lower: [r0 - k, r0 + R)) into shared memory, and
+// decodes x_c for columns [r0 - k, r0 + R + k) into digit sets there (x read
+// in place, any increment). Each thread then forms its row's 2k + 1 products
+// from shared memory. A first pass over the row's exponents fixes the
+// accumulator's block exponent, so no product has to move it (with rows this
+// short, moving it as larger terms arrive, the way the long sums of DOT and
+// GEMV do, would cost more than the products).
+constexpr int kSbRows = 128;
+constexpr int kSbMaxK = 32;
+std::atomic<int> g_band_tile{1};   // mwblas_set_band_tile
+
+struct SbParams {
+    int64_t n, ldab;
+    int k;
+    bool upper;
+    const double2 *AB;
+    const double2 *x;
+    int64_t incx;
+    double2 *y;   // y itself (any increment) or a contiguous copy (incy 1)
+    int64_t incy;
+    dd::real ar, br;
+    int beta_kind;
+};
+
+// Shared bytes of a tile for bandwidth k: the band columns at an odd stride
+// (16-byte reads of consecutive rows then fall in distinct banks) and the
+// digit sets of x as two arrays of 16-byte halves.
+constexpr size_t sb_smem_bytes(int k)
+{
+    return (size_t)(kSbRows + k) * ((k + 1) | 1) * sizeof(double2) + (size_t)(kSbRows + 2 * k) * 2 * sizeof(int4);
+}
+
+__global__ void __launch_bounds__(kSbRows) k_sbmv_tile(SbParams p)
+{
+    extern __shared__ int4 sb_smem[];
+    const int k = p.k, kp = k + 1, sp = kp | 1, t = threadIdx.x;
+    const int64_t r0 = (int64_t)blockIdx.x * kSbRows;
+    const int64_t cb = p.upper ? r0 : (r0 > k ? r0 - k : 0);
+    const int64_t cend = p.upper ? r0 + kSbRows + k : r0 + kSbRows;
+    const int64_t ce = cend < p.n ? cend : p.n;
+    const int64_t xb = r0 > k ? r0 - k : 0;
+    const int64_t xe = r0 + kSbRows + k < p.n ? r0 + kSbRows + k : p.n;
+    double2 *S = reinterpret_cast<double2 *>(sb_smem);
+    int4 *X0 = sb_smem + (size_t)(kSbRows + k) * sp;   // digits 0..3 of x_c
+    int4 *X1 = X0 + (kSbRows + 2 * k);                 // digit 4, exponent, flags
+    // band columns [cb, ce): entry b of column c goes to S[(c - cb) * sp + b];
+    // idx / kp by a multiply-shift, exact while idx * (m * kp - 2^20) < 2^20
+    // (idx < (R + k) kp <= 160 * 33 and m * kp - 2^20 < kp; idx * m < 2^28)
+    const int total = (int)(ce - cb) * kp;
+    const uint32_t m = ((1u << 20) + kp - 1) / kp;
+    const double2 *src = p.AB + cb * p.ldab;
+    for (int idx = t; idx < total; idx += kSbRows) {
+        const int col = (int)(((uint32_t)idx * m) >> 20), b = idx - col * kp;
+        S[col * sp + b] = src[(int64_t)col * p.ldab + b];
+    }
+    for (int c = t; c < (int)(xe - xb); c += kSbRows) {
+        const fx::Dig g = fx::to_dig(fx::decode(p.x[vpos(xb + c, p.n, p.incx)]));
+        X0[c] = make_int4(g.d[0], g.d[1], g.d[2], g.d[3]);
+        X1[c] = make_int4(g.d[4], g.e, (int)g.flags, 0);
+    }
+    __syncthreads();
+    const int64_t r = r0 + t;
+    if (r >= p.n) return;
+    const int lo = (int)(r < k ? r : k), hi = (int)(p.n - 1 - r < k ? p.n - 1 - r : k);
+    const int cofs = (int)(r0 - cb), xofs = (int)(r0 - xb) + t;
+    // stored entry (min(r, c), max(r, c)) (upper) or (max, min) (lower) of
+    // c = r + d: column max (upper) / min (lower), band row k - |d| / |d|
+    auto at = [&](int d) {
+        const int ad = d < 0 ? -d : d;
+        const int lj = t + cofs + (p.upper ? (d > 0 ? d : 0) : (d < 0 ? d : 0));
+        return lj * sp + (p.upper ? k - ad : ad);
+    };
+    // block exponent: the largest exponent of a product with a finite,
+    // nonzero factor pair (hi's exponent field as decode takes it)
+    int emax = INT_MIN;
+    for (int d = -lo; d <= hi; ++d) {
+        const uint32_t hh = (uint32_t)__double2hiint(S[at(d)].x);
+        const int eh = (int)((hh >> 20) & 0x7FFu);
+        const int4 g1 = X1[xofs + d];
+        if (eh == 0x7FF || (g1.z & (int)(fx::kZero | fx::kBad))) continue;
+        const int ep = (eh ? eh : 1) - 1139 + g1.y;
+        emax = ep > emax ? ep : emax;
+    }
+    fx::Acc acc;
+    acc.reset();
+    if (emax != INT_MIN) acc.preset(emax);
+#pragma unroll 2
+    for (int d = -lo; d <= hi; ++d) {
+        const int4 g0 = X0[xofs + d], g1 = X1[xofs + d];
+        fx::Dig g;
+        g.d[0] = g0.x;
+        g.d[1] = g0.y;
+        g.d[2] = g0.z;
+        g.d[3] = g0.w;
+        g.d[4] = g1.x;
+        g.e = g1.y;
+        g.flags = (uint32_t)g1.z;
+        g.pad = 0;
+        acc.add_at(fx::decode(S[at(d)]), g);
+    }
+    double2 *py = p.y + vpos(r, p.n, p.incy);
+    if (acc.bad) {
+        const double nan = __longlong_as_double(0x7ff8000000000000ll);
+        py[0] = make_double2(nan, nan);
+        return;
+    }
+    const xfp::XF tot = xfp::xf_add(xzero(), acc.finish());
+    smv_store_real(py, xfp::xf_from_dd(p.ar.hi, p.ar.lo), p.br, p.beta_kind, tot);
 }
 
 // ---- triangular band solve, read in place ----------------------------------------------
@@ -681,8 +807,64 @@ void pack_move(int64_t n, void *AP, int e2, bool upper, void *dense, bool unpack
     count_launch();
 }
 
+// Real symmetric band of bandwidth <= kSbMaxK on the shared-memory tile
+// kernel, x read in place; y too unless it overlaps x (then through a
+// contiguous copy).
+bool sbmv_tile(const SmvArgs &a, const char *routine)
+{
+    SbParams q;
+    q.n = a.n;
+    q.ldab = a.ldab;
+    q.k = (int)(a.upper ? a.ku : a.kl);
+    q.upper = a.upper;
+    q.AB = (const double2 *)a.A;
+    q.x = (const double2 *)a.x;
+    q.incx = a.incx;
+    q.ar = dd::make(a.alpha.hi, a.alpha.lo);
+    q.br = dd::make(a.beta.hi, a.beta.lo);
+    q.beta_kind = a.beta_kind;
+    // byte ranges of the two vectors
+    auto span = [&](const void *v, int64_t inc, uintptr_t &lo, uintptr_t &hi) {
+        const int64_t ext = (a.n - 1) * (inc < 0 ? -inc : inc);
+        lo = (uintptr_t)v;
+        hi = lo + (uintptr_t)(ext + 1) * sizeof(double2);
+    };
+    uintptr_t xl, xh, yl, yh;
+    span(a.x, a.incx, xl, xh);
+    span(a.y, a.incy, yl, yh);
+    const bool direct = xh <= yl || yh <= xl;
+    void *yb = nullptr;
+    if (direct) {
+        q.y = (double2 *)a.y;
+        q.incy = a.incy;
+    } else {
+        yb = dev_alloc((size_t)a.n * sizeof(double2), routine);
+        if (!yb) return false;
+        if (a.beta_kind != 0) vgather(a.n, a.y, a.incy, 1, yb, true);
+        q.y = (double2 *)yb;
+        q.incy = 1;
+    }
+    static int attr_set[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (!attr_set[dev & 63]) {
+        cudaFuncSetAttribute(k_sbmv_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb_smem_bytes(kSbMaxK));
+        attr_set[dev & 63] = 1;
+    }
+    k_sbmv_tile<<<(unsigned)((a.n + kSbRows - 1) / kSbRows), kSbRows, sb_smem_bytes(q.k), stream()>>>(q);
+    count_launch();
+    if (!direct) {
+        vgather(a.n, a.y, a.incy, 1, yb, false);
+        dev_free(yb);
+    }
+    return true;
+}
+
 bool smv_device(const SmvArgs &a, const char *routine)
 {
+    if (!a.cplx && a.kind == 1 && a.fmt == 1 && a.n > 0 && (a.upper ? a.ku : a.kl) <= kSbMaxK &&
+        g_band_tile.load() != 0)
+        return sbmv_tile(a, routine);
     const int e2 = a.cplx ? 2 : 1;
     const size_t es = 16 * (size_t)e2;
     Buf xb((size_t)(a.cols > 0 ? a.cols : 1) * e2 * sizeof(fx::Dig), routine),
@@ -932,3 +1114,5 @@ bool rank_update_device(const RankArgs &r, const char *routine)
 }
 
 }  // namespace mw
+
+extern "C" int mwblas_set_band_tile(int on) { return mw::g_band_tile.exchange(on ? 1 : 0); }

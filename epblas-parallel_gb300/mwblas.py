@@ -162,6 +162,7 @@ class MWBlas:
             self._sig("mwblas_set_wait_limit_ns", C.c_uint64, [C.c_uint64])
             self._sig("mwblas_set_plain_tma", _i32, [_i32])
             self._sig("mwblas_set_residue_tc", _i32, [_i32])
+            self._sig("mwblas_set_band_tile", _i32, [_i32])
             self._sig("mwblas_debug_lose_operand_loads", None, [_i32])
             self._sig("mwblas_launch_count", _i64, [])
             self._sig("mwblas_version", _ch, [])

@@ -349,3 +349,75 @@ def test_general_band_rows_over_many_blocks(gpu, oracle, rng, trans):
     want = matvec(oracle, False, trans, F, ly, lx, x, al, be, y)
     scale = orc.dd_abs(al) * lx * orc.dd_absmax(F) * orc.dd_absmax(x) + orc.dd_abs(be) * orc.dd_absmax(y)
     assert err_ok(outs[0], want, scale, max(10, 4 * max(m, n)) * orc.EPS_DD)
+
+
+def _sbmv_both(gpu, *args):
+    """msbmv through the shared-memory band tiles and through a thread per
+    row reading band storage in place."""
+    outs = []
+    prev = gpu.lib.mwblas_set_band_tile(1)
+    try:
+        for on in (1, 0):
+            gpu.lib.mwblas_set_band_tile(on)
+            got = args[-2].copy()
+            gpu.l2("msbmv", *args[:-2], got, args[-1])
+            assert gpu.last_error()[0] == 0, gpu.last_error()
+            outs.append(got)
+    finally:
+        gpu.lib.mwblas_set_band_tile(prev)
+    return outs
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+def test_band_tile_matches_thread_per_row(gpu, oracle, rng, uplo):
+    """Real symmetric band products from shared-memory tiles of 128 rows and
+    from band storage read in place both agree with the oracle, over
+    bandwidths 0..32 (33 takes the in-place kernels on both settings), orders
+    around the tile size, padded leading dimensions, negative and strided
+    increments and the three kinds of beta. Band-storage entries outside the
+    matrix hold NaN, so reading one would show. (The two need not agree bit
+    for bit: the tiles fix each row's block exponent before the products,
+    the in-place kernels move it as larger terms arrive, and both keep the
+    sum exact to about 2^-130 of its largest term before the one rounding.)"""
+    cases = [(1, 0), (5, 3), (127, 1), (128, 16), (129, 31), (700, 32), (1100, 16), (300, 33)]
+    for t, (n, k) in enumerate(cases):
+        S = band_keep(sym_from_tri(dense(rng, n, n, False), n, uplo, False), k, k)
+        kl, ku = (0, k) if uplo == "U" else (k, 0)
+        AB = to_band(S, kl, ku)
+        for j in range(n):
+            for b in range(k + 1):
+                i = j - k + b if uplo == "U" else j + b
+                if i < 0 or i >= n:
+                    AB[j, b] = np.nan
+        ldab = k + 1 + (t % 3)
+        ABp = _padded(AB, ldab)
+        ix, iy = [(1, 1), (-2, 3), (3, -1)][t % 3]
+        x, y = vecs(rng, n, ix, False), vecs(rng, n, iy, False)
+        al = scal(rng, False)
+        be = [ZERO[False], ONE[False], scal(rng, False)][t % 3]
+        tile, rows = _sbmv_both(gpu, uplo, n, k, al, ABp, ldab, x, ix, be, y, iy)
+        want = matvec(oracle, False, "N", np.ascontiguousarray(S), n, n, gather(x, n, ix), al, be,
+                      gather(y, n, iy))
+        scale = orc.dd_abs(al) * n * orc.dd_absmax(S) * orc.dd_absmax(x) + orc.dd_abs(be) * orc.dd_absmax(y)
+        for got in (tile, rows):
+            assert err_ok(gather(got, n, iy), want, scale, max(10, 4 * n) * orc.EPS_DD), (n, k)
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+def test_band_tile_non_finite_entry(gpu, rng, uplo):
+    """An infinity stored at band entry (i0, j0) makes exactly rows i0 and j0
+    of the result NaN (the reference's double-double product of an infinity
+    is NaN), on both kernels, and leaves the other rows finite."""
+    n, k, i0, j0 = 300, 16, 130, 140
+    S = band_keep(sym_from_tri(dense(rng, n, n, False), n, uplo, False), k, k)
+    kl, ku = (0, k) if uplo == "U" else (k, 0)
+    AB = to_band(S, kl, ku)
+    si, sj = (i0, j0) if uplo == "U" else (j0, i0)       # the stored triangle's entry
+    AB[sj, (k + si - sj) if uplo == "U" else (si - sj)] = np.array([np.inf, 0.0])
+    x, y = vecs(rng, n, 1, False), vecs(rng, n, 1, False)
+    tile, rows = _sbmv_both(gpu, uplo, n, k, scal(rng, False), np.ascontiguousarray(AB), k + 1, x, 1,
+                            scal(rng, False), y, 1)
+    for got in (tile, rows):
+        bad = np.flatnonzero(np.isnan(got[:, 0]))
+        assert list(bad) == [i0, j0], bad
+        assert np.isfinite(np.delete(got, bad, axis=0)).all()
