@@ -124,12 +124,56 @@ static __device__ __noinline__ Op decode_general(double2 v)
     return o;
 }
 
-// The same result as decode_general, with a straight-line path for the common
-// operands: hi normal and finite, and lo zero, or normal with its exponent 33
-// to 64 below hi's (lo's mantissa then lands in the low three words with a
-// left shift s = 64 - gap below 32; a normalised double-double has gap >= 53).
-// The sum W = hi's mantissa * 2^64 +- lo's shifted mantissa is formed as
-// W + (t ^ mask) + (mask & 1), mask = all ones when the signs differ.
+// The operands decode takes on its straight-line path: hi normal and finite,
+// and lo zero, or normal with its exponent 33 to 64 below hi's (lo's mantissa
+// then lands in the low three words with a left shift s = 64 - gap below 32;
+// a normalised double-double has gap >= 53).
+__device__ __forceinline__ bool decode_is_fast(double2 v)
+{
+    const uint32_t hh = (uint32_t)__double2hiint(v.x);
+    const uint32_t ll = (uint32_t)__double2loint(v.y), lh = (uint32_t)__double2hiint(v.y);
+    const uint32_t eh = (hh >> 20) & 0x7FFu, el = (lh >> 20) & 0x7FFu;
+    const bool lo_zero = ((lh << 1) | ll) == 0u;
+    const uint32_t gap = eh - el;   // unsigned: wraps when lo's exponent is above hi's
+    return (eh - 1u) < 0x7FEu && (lo_zero || ((el - 1u) < 0x7FEu && gap - 33u <= 31u));
+}
+
+// decode for an operand that passes decode_is_fast (so finite and nonzero:
+// the flags hold only the sign). The sum W = hi's mantissa * 2^64 +- lo's
+// shifted mantissa is formed as W + (t ^ mask) + (mask & 1), mask = all ones
+// when the signs differ; W < 2^118.
+__device__ __forceinline__ Op decode_fast(double2 v)
+{
+    const uint32_t hl = (uint32_t)__double2loint(v.x), hh = (uint32_t)__double2hiint(v.x);
+    const uint32_t ll = (uint32_t)__double2loint(v.y), lh = (uint32_t)__double2hiint(v.y);
+    const uint32_t eh = (hh >> 20) & 0x7FFu, el = (lh >> 20) & 0x7FFu;
+    const bool lo_zero = ((lh << 1) | ll) == 0u;
+    const uint32_t gap = eh - el;
+    Op o;
+    o.flags = hh >> 31;
+    o.e = (int)eh - 1075 - 64;
+    const uint32_t mlh = lo_zero ? 0u : ((lh & 0xFFFFFu) | 0x100000u);
+    const uint32_t lw = lo_zero ? 0u : ll;
+    const int s = (int)(64u - gap) & 31;
+    const uint32_t t0 = lw << s, t1 = __funnelshift_l(lw, mlh, s), t2 = __funnelshift_l(mlh, 0u, s);
+    const uint32_t mask = 0u - ((hh ^ lh) >> 31);
+    uint32_t w0, w1, w2, w3;
+    asm("add.cc.u32 %0, %4, %8;\n\t"
+        "addc.cc.u32 %1, %5, 0;\n\t"
+        "addc.cc.u32 %2, %6, %9;\n\t"
+        "addc.u32 %3, %7, %10;"
+        : "=r"(w0), "=r"(w1), "=r"(w2), "=r"(w3)
+        : "r"(t0 ^ mask), "r"(t1 ^ mask), "r"(t2 ^ mask), "r"((hh & 0xFFFFFu) | 0x100000u), "r"(mask & 1u),
+          "r"(hl), "r"(mask));
+    o.w[0] = w0;
+    o.w[1] = w1;
+    o.w[2] = w2;
+    o.w[3] = w3;
+    return o;
+}
+
+// The same result as decode_general, with decode_fast's straight-line path
+// inline for the operands that pass decode_is_fast.
 __device__ __forceinline__ Op decode(double2 v)
 {
     const uint32_t hl = (uint32_t)__double2loint(v.x), hh = (uint32_t)__double2hiint(v.x);
@@ -393,8 +437,49 @@ struct Acc {
 #pragma unroll
             for (int t = 0; t < 5; ++t) a[t] = -a[t];
         }
-        const int *b = y.d;
-        // one 32 x 32 -> 64-bit multiply-add per digit product
+        mads(a, y.d);
+    }
+
+    // Room for a group of products of exponents up to ep_max (the first
+    // group fixes the block, later ones move it up when needed); the group
+    // then goes in with mul_fast(x, y, B - ep), one test per group. (Where a
+    // group moves the block, its smaller products are aligned to the new
+    // block rather than shifted with the sum: the dropped bits, below 2^-130
+    // of the block, can differ from add_core's one product at a time.)
+    __device__ __forceinline__ void admit(int ep_max)
+    {
+        if (!init) {
+            B = ep_max + 4;
+            init = true;
+        } else if (ep_max > B - 2) {
+            const int nb = ep_max + 4;
+            if (cnt) normalize();
+            raise(nb - B);
+            B = nb;
+        }
+    }
+
+    // += X' * Y at the block, X' = X >> sh, for an operand from decode_fast
+    // and the digit set of a finite nonzero value: no flag tests, the sign as
+    // a factor of the digits, and the shift clamped instead of tested
+    // (X < 2^118, so X >> sh is zero for every sh >= 118). At the same block,
+    // the same sum as add_core.
+    __device__ __forceinline__ void mul_fast(const Op &x, const Dig &y, int sh)
+    {
+        uint32_t xs[4];
+        shr128(x.w, sh < 127 ? sh : 127, xs);
+        int a[5];
+        digits24(xs, a);
+        const int sg = 1 - 2 * (int)((x.flags ^ y.flags) & kNeg);
+#pragma unroll
+        for (int t = 0; t < 5; ++t) a[t] *= sg;
+        mads(a, y.d);
+    }
+
+    // the 19 digit products of weight >= 2^72, one 32 x 32 -> 64-bit
+    // multiply-add each
+    __device__ __forceinline__ void mads(const int a[5], const int *b)
+    {
         madw(c[0], a[0], b[3]); madw(c[0], a[1], b[2]); madw(c[0], a[2], b[1]); madw(c[0], a[3], b[0]);
         madw(c[1], a[0], b[4]); madw(c[1], a[1], b[3]); madw(c[1], a[2], b[2]); madw(c[1], a[3], b[1]);
         madw(c[1], a[4], b[0]);

@@ -96,9 +96,9 @@ __global__ void k_dig_convert(int64_t n, const double2 *x, int64_t incx, fx::Dig
 
 // NoTrans partial sums: row per thread, columns [j0, j1) of chunk blockIdx.y
 // (at most fx::kMaxAdds columns per chunk).
-__global__ void __launch_bounds__(256) k_gemv_n_fx(int64_t m, int64_t n, const double2 *__restrict__ A, int64_t lda,
-                                                  const fx::Dig *__restrict__ xo, int64_t chunk,
-                                                  fx::XFPod *__restrict__ part)
+__global__ void __launch_bounds__(256, 4) k_gemv_n_fx(int64_t m, int64_t n, const double2 *__restrict__ A,
+                                                     int64_t lda, const fx::Dig *__restrict__ xo, int64_t chunk,
+                                                     fx::XFPod *__restrict__ part)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= m) return;
@@ -113,10 +113,25 @@ __global__ void __launch_bounds__(256) k_gemv_n_fx(int64_t m, int64_t n, const d
         for (; j + 4 <= jend; j += 4) {
             const double2 a0 = __ldcs(a + j * lda), a1 = __ldcs(a + (j + 1) * lda);
             const double2 a2 = __ldcs(a + (j + 2) * lda), a3 = __ldcs(a + (j + 3) * lda);
-            acc.add_core(fx::decode(a0), xo[j]);
-            acc.add_core(fx::decode(a1), xo[j + 1]);
-            acc.add_core(fx::decode(a2), xo[j + 2]);
-            acc.add_core(fx::decode(a3), xo[j + 3]);
+            const fx::Dig x0 = xo[j], x1 = xo[j + 1], x2 = xo[j + 2], x3 = xo[j + 3];
+            if (fx::decode_is_fast(a0) && fx::decode_is_fast(a1) && fx::decode_is_fast(a2) && fx::decode_is_fast(a3) &&
+                ((x0.flags | x1.flags | x2.flags | x3.flags) & (fx::kZero | fx::kBad)) == 0) {
+                // normal operands (the common case): no per-product flag
+                // tests, one block-exponent test per four products
+                const fx::Op o0 = fx::decode_fast(a0), o1 = fx::decode_fast(a1);
+                const fx::Op o2 = fx::decode_fast(a2), o3 = fx::decode_fast(a3);
+                const int e0 = o0.e + x0.e, e1 = o1.e + x1.e, e2 = o2.e + x2.e, e3 = o3.e + x3.e;
+                acc.admit(max(max(e0, e1), max(e2, e3)));
+                acc.mul_fast(o0, x0, acc.B - e0);
+                acc.mul_fast(o1, x1, acc.B - e1);
+                acc.mul_fast(o2, x2, acc.B - e2);
+                acc.mul_fast(o3, x3, acc.B - e3);
+            } else {
+                acc.add_core(fx::decode(a0), x0);
+                acc.add_core(fx::decode(a1), x1);
+                acc.add_core(fx::decode(a2), x2);
+                acc.add_core(fx::decode(a3), x3);
+            }
         }
         acc.normalize();
     }
