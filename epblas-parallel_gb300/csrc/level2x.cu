@@ -455,6 +455,141 @@ __global__ void __launch_bounds__(kSbRows) k_sbmv_tile(SbParams p)
     smv_store_real(py, xfp::xf_from_dd(p.ar.hi, p.ar.lo), p.br, p.beta_kind, tot);
 }
 
+// ---- real symmetric packed product in two coalesced halves ----------------------------
+// Row r of a symmetric packed matrix takes half of its entries from row r of
+// the stored triangle and half from column r. k_smv's warp per row reads the
+// column half contiguously but the row half at a stride of about r entries
+// (32 lines per warp load). Here the row half goes GEMV-style, a thread per
+// row over a chunk of kSpChunk columns, where for a fixed column consecutive
+// rows are consecutive entries (k_spmv_rows, one partial sum per row and
+// chunk), and the column half a warp per row, lanes over the contiguous
+// column (k_spmv_cols). k_spmv_final adds each row's partial sums in a fixed
+// order and forms y := beta*y + alpha*s with one rounding.
+//   upper: AP[i + j(j+1)/2], i <= j: row half c >= r, column half c < r;
+//   lower: AP[i + j(2n-j-1)/2], i >= j: row half c <= r, column half c > r.
+constexpr int kSpChunk = 512;   // columns per row-half partial (<= 2048: no carry propagation needed)
+
+template <bool UPPER>
+__global__ void __launch_bounds__(256, 3) k_spmv_rows(int64_t n, const double2 *__restrict__ AP,
+                                                      const fx::Dig *__restrict__ xd, fx::XFPod *__restrict__ part)
+{
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t c0 = (int64_t)blockIdx.y * kSpChunk, c1 = min(n, c0 + kSpChunk);
+    if (r >= n) return;
+    // the row's columns in this chunk: upper [max(c0, r), c1), lower [c0, min(c1, r + 1))
+    const int64_t cb = UPPER ? max(c0, r) : c0, ce = UPPER ? c1 : min(c1, r + 1);
+    if (cb >= ce) return;   // no entries here (the final sum skips this chunk for row r)
+    // entry (r, c): upper c(c+1)/2 + r, stepping by c + 1; lower r + c(2n-c-1)/2, stepping by n - c - 1
+    int64_t at = UPPER ? cb * (cb + 1) / 2 + r : r + cb * (2 * n - cb - 1) / 2;
+    auto step = [&](int64_t c) { return UPPER ? c + 1 : n - c - 1; };
+    fx::Acc acc;
+    acc.reset();
+    int64_t c = cb;
+    for (; c + 4 <= ce; c += 4) {
+        const int64_t at1 = at + step(c), at2 = at1 + step(c + 1), at3 = at2 + step(c + 2);
+        const double2 a0 = __ldcs(AP + at), a1 = __ldcs(AP + at1), a2 = __ldcs(AP + at2), a3 = __ldcs(AP + at3);
+        at = at3 + step(c + 3);
+        const fx::Dig x0 = xd[c], x1 = xd[c + 1], x2 = xd[c + 2], x3 = xd[c + 3];
+        if (fx::decode_is_fast(a0) && fx::decode_is_fast(a1) && fx::decode_is_fast(a2) && fx::decode_is_fast(a3) &&
+            ((x0.flags | x1.flags | x2.flags | x3.flags) & (fx::kZero | fx::kBad)) == 0) {
+            const fx::Op o0 = fx::decode_fast(a0), o1 = fx::decode_fast(a1);
+            const fx::Op o2 = fx::decode_fast(a2), o3 = fx::decode_fast(a3);
+            const int e0 = o0.e + x0.e, e1 = o1.e + x1.e, e2 = o2.e + x2.e, e3 = o3.e + x3.e;
+            acc.admit(max(max(e0, e1), max(e2, e3)));
+            acc.mul_fast(o0, x0, acc.B - e0);
+            acc.mul_fast(o1, x1, acc.B - e1);
+            acc.mul_fast(o2, x2, acc.B - e2);
+            acc.mul_fast(o3, x3, acc.B - e3);
+        } else {
+            acc.add_core(fx::decode(a0), x0);
+            acc.add_core(fx::decode(a1), x1);
+            acc.add_core(fx::decode(a2), x2);
+            acc.add_core(fx::decode(a3), x3);
+        }
+    }
+    for (; c < ce; ++c) {
+        acc.add_core(fx::decode(__ldcs(AP + at)), xd[c]);
+        at += step(c);
+    }
+    part[blockIdx.y * n + r] = fx::to_pod(acc.finish(), acc.bad);
+}
+
+template <bool UPPER>
+__global__ void __launch_bounds__(256, 3) k_spmv_cols(int64_t n, const double2 *__restrict__ AP,
+                                                   const fx::Dig *__restrict__ xd, fx::XFPod *__restrict__ partc)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * blockDim.x / 32;
+    for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32; r < n; r += warps) {
+        // column r of the stored triangle: upper rows [0, r) at r(r+1)/2,
+        // lower rows (r, n) at r + 1 + r(2n-r-1)/2, both contiguous
+        const int64_t cb = UPPER ? 0 : r + 1, ce = UPPER ? r : n;
+        const double2 *col = AP + (UPPER ? r * (r + 1) / 2 : r * (2 * n - r - 1) / 2 + r + 1) - cb;
+        // fewer than fx::kMaxAdds products per lane (the host keeps n below
+        // 2^25); four loads in flight per lane, carries propagated after
+        // each run of 2048 products
+        fx::Acc acc;
+        acc.reset();
+        int64_t c = cb + lane;
+        while (c + 96 < ce) {
+            const int64_t cend = c + 128 * 512;
+            for (; c + 96 < ce && c < cend; c += 128) {
+                const double2 a0 = __ldcs(col + c), a1 = __ldcs(col + c + 32);
+                const double2 a2 = __ldcs(col + c + 64), a3 = __ldcs(col + c + 96);
+                const fx::Dig x0 = xd[c], x1 = xd[c + 32], x2 = xd[c + 64], x3 = xd[c + 96];
+                if (fx::decode_is_fast(a0) && fx::decode_is_fast(a1) && fx::decode_is_fast(a2) &&
+                    fx::decode_is_fast(a3) && ((x0.flags | x1.flags | x2.flags | x3.flags) & (fx::kZero | fx::kBad)) == 0) {
+                    const fx::Op o0 = fx::decode_fast(a0), o1 = fx::decode_fast(a1);
+                    const fx::Op o2 = fx::decode_fast(a2), o3 = fx::decode_fast(a3);
+                    const int e0 = o0.e + x0.e, e1 = o1.e + x1.e, e2 = o2.e + x2.e, e3 = o3.e + x3.e;
+                    acc.admit(max(max(e0, e1), max(e2, e3)));
+                    acc.mul_fast(o0, x0, acc.B - e0);
+                    acc.mul_fast(o1, x1, acc.B - e1);
+                    acc.mul_fast(o2, x2, acc.B - e2);
+                    acc.mul_fast(o3, x3, acc.B - e3);
+                } else {
+                    acc.add_core(fx::decode(a0), x0);
+                    acc.add_core(fx::decode(a1), x1);
+                    acc.add_core(fx::decode(a2), x2);
+                    acc.add_core(fx::decode(a3), x3);
+                }
+            }
+            acc.normalize();
+        }
+        for (; c < ce; c += 32) acc.add_core(fx::decode(__ldcs(col + c)), xd[c]);
+        const xfp::XF tot = fx::xf_warp_sum(xfp::xf_add(xzero(), acc.finish()));
+        const bool bad = __any_sync(0xffffffffu, acc.bad);
+        if (lane == 0) partc[r] = fx::to_pod(tot, bad);
+    }
+}
+
+// y(r) := beta*y(r) + alpha*(column half + row-half chunks in ascending order)
+__global__ void k_spmv_final(int64_t n, bool upper, const fx::XFPod *__restrict__ part,
+                             const fx::XFPod *__restrict__ partc, dd::real ar, dd::real br, int beta_kind, double2 *y,
+                             int64_t incy)
+{
+    const xfp::XF xar = xfp::xf_from_dd(ar.hi, ar.lo);
+    const int64_t nch = (n + kSpChunk - 1) / kSpChunk;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const fx::XFPod pc = partc[r];
+        bool bad = (pc.flags & 4) != 0;
+        xfp::XF s = fx::from_pod(pc);
+        const int64_t q0 = upper ? r / kSpChunk : 0, q1 = upper ? nch : r / kSpChunk + 1;
+        for (int64_t q = q0; q < q1; ++q) {
+            const fx::XFPod p = part[q * n + r];
+            bad |= (p.flags & 4) != 0;
+            s = xfp::xf_add(s, fx::from_pod(p));
+        }
+        double2 *py = y + vpos(r, n, incy);
+        if (bad) {
+            const double nan = __longlong_as_double(0x7ff8000000000000ll);
+            *py = make_double2(nan, nan);
+            continue;
+        }
+        smv_store_real(py, xar, br, beta_kind, s);
+    }
+}
+
 // ---- triangular band solve, read in place ----------------------------------------------
 // op(A) x = b for a band triangle of bandwidth k, by one warp: rows are taken
 // 32 at a time in solve order (lane l owns the l-th row of the tile). Each
@@ -860,11 +995,63 @@ bool sbmv_tile(const SmvArgs &a, const char *routine)
     return true;
 }
 
+// Real symmetric packed matrix: the row halves in column chunks, the column
+// halves a warp per row, then the per-row sums (x as digit sets; y in place
+// unless it overlaps x).
+bool spmv_split(const SmvArgs &a, const char *routine)
+{
+    const int64_t n = a.n, nch = (n + kSpChunk - 1) / kSpChunk;
+    const size_t xd_bytes = ((size_t)n * sizeof(fx::Dig) + 255) / 256 * 256;
+    const size_t part_bytes = ((size_t)(nch * n) * sizeof(fx::XFPod) + 255) / 256 * 256;
+    char *buf = (char *)dev_alloc(xd_bytes + part_bytes + (size_t)n * sizeof(fx::XFPod), routine);
+    if (!buf) return false;
+    fx::Dig *xd = (fx::Dig *)buf;
+    fx::XFPod *part = (fx::XFPod *)(buf + xd_bytes), *partc = (fx::XFPod *)(buf + xd_bytes + part_bytes);
+    k_vdig<<<blocks_for(n), kThreads, 0, stream()>>>(n, (const double2 *)a.x, a.incx, 1, xd);
+    const double2 *AP = (const double2 *)a.A;
+    const dim3 grid((unsigned)((n + 255) / 256), (unsigned)nch);
+    int64_t wblocks = (n * 32 + 255) / 256;
+    const int64_t cap = (int64_t)device_sm_count() * 8;
+    if (wblocks > cap) wblocks = cap;
+    if (a.upper) {
+        k_spmv_rows<true><<<grid, 256, 0, stream()>>>(n, AP, xd, part);
+        k_spmv_cols<true><<<(unsigned)wblocks, 256, 0, stream()>>>(n, AP, xd, partc);
+    } else {
+        k_spmv_rows<false><<<grid, 256, 0, stream()>>>(n, AP, xd, part);
+        k_spmv_cols<false><<<(unsigned)wblocks, 256, 0, stream()>>>(n, AP, xd, partc);
+    }
+    // y in place unless it overlaps x
+    const uintptr_t xl = (uintptr_t)a.x, xh = xl + (uintptr_t)((n - 1) * (a.incx < 0 ? -a.incx : a.incx) + 1) * 16;
+    const uintptr_t yl = (uintptr_t)a.y, yh = yl + (uintptr_t)((n - 1) * (a.incy < 0 ? -a.incy : a.incy) + 1) * 16;
+    const bool direct = xh <= yl || yh <= xl;
+    void *yb = nullptr;
+    if (!direct) {
+        yb = dev_alloc((size_t)n * sizeof(double2), routine);
+        if (!yb) {
+            dev_free(buf);
+            return false;
+        }
+        if (a.beta_kind != 0) vgather(n, a.y, a.incy, 1, yb, true);
+    }
+    k_spmv_final<<<blocks_for(n), kThreads, 0, stream()>>>(
+        n, a.upper, part, partc, dd::make(a.alpha.hi, a.alpha.lo), dd::make(a.beta.hi, a.beta.lo), a.beta_kind,
+        direct ? (double2 *)a.y : (double2 *)yb, direct ? a.incy : 1);
+    count_launch(4);
+    if (!direct) {
+        vgather(n, a.y, a.incy, 1, yb, false);
+        dev_free(yb);
+    }
+    dev_free(buf);
+    return true;
+}
+
 bool smv_device(const SmvArgs &a, const char *routine)
 {
     if (!a.cplx && a.kind == 1 && a.fmt == 1 && a.n > 0 && (a.upper ? a.ku : a.kl) <= kSbMaxK &&
         g_band_tile.load() != 0)
         return sbmv_tile(a, routine);
+    if (!a.cplx && a.kind == 1 && a.fmt == 2 && a.n > 0 && a.n < ((int64_t)1 << 25) && g_band_tile.load() != 0)
+        return spmv_split(a, routine);
     const int e2 = a.cplx ? 2 : 1;
     const size_t es = 16 * (size_t)e2;
     Buf xb((size_t)(a.cols > 0 ? a.cols : 1) * e2 * sizeof(fx::Dig), routine),

@@ -559,11 +559,14 @@ int mwblas_set_plain_tma(int on);
  * write identical residues. Returns the previous value. */
 int mwblas_set_residue_tc(int on);
 
-/* Real symmetric band products (msbmv) of bandwidth k <= 32: 1 (default) =
- * a block of rows per shared-memory tile of the band, copied with coalesced
- * loads, 0 = band storage read in place (a thread or a warp per row). Both
- * keep each row's sum exact to about 2^-130 of its largest term and round
- * once; the last bit of the low word may differ. Returns the previous value. */
+/* Real symmetric band (msbmv, bandwidth k <= 32) and packed (mspmv)
+ * products: 1 (default) = band: a block of rows per shared-memory tile of the
+ * band, copied with coalesced loads; packed: the row halves of the rows in
+ * column chunks (a thread per row) and the column halves a warp per row, both
+ * read with coalesced loads. 0 = the stored triangle read in place, a thread
+ * or a warp per row. Both keep each row's sum exact to about 2^-130 of its
+ * largest term and round once; the last bit of the low word may differ.
+ * Returns the previous value. */
 int mwblas_set_band_tile(int on);
 
 /* Per-phase device timing of the Ozaki engine (CUDA events on the library

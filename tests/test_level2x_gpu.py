@@ -351,16 +351,17 @@ def test_general_band_rows_over_many_blocks(gpu, oracle, rng, trans):
     assert err_ok(outs[0], want, scale, max(10, 4 * max(m, n)) * orc.EPS_DD)
 
 
-def _sbmv_both(gpu, *args):
-    """msbmv through the shared-memory band tiles and through a thread per
-    row reading band storage in place."""
+def _sbmv_both(gpu, *args, name="msbmv"):
+    """msbmv (mspmv) through the shared-memory band tiles (the two coalesced
+    halves of the packed kernels) and through a thread or warp per row
+    reading the stored triangle in place."""
     outs = []
     prev = gpu.lib.mwblas_set_band_tile(1)
     try:
         for on in (1, 0):
             gpu.lib.mwblas_set_band_tile(on)
             got = args[-2].copy()
-            gpu.l2("msbmv", *args[:-2], got, args[-1])
+            gpu.l2(name, *args[:-2], got, args[-1])
             assert gpu.last_error()[0] == 0, gpu.last_error()
             outs.append(got)
     finally:
@@ -421,3 +422,51 @@ def test_band_tile_non_finite_entry(gpu, rng, uplo):
         bad = np.flatnonzero(np.isnan(got[:, 0]))
         assert list(bad) == [i0, j0], bad
         assert np.isfinite(np.delete(got, bad, axis=0)).all()
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+def test_packed_halves_match_oracle(gpu, oracle, rng, uplo):
+    """Real symmetric packed products from the two coalesced halves (row
+    halves in 512-column chunks, column halves a warp per row) and from a
+    warp per row in place both agree with the oracle, over orders around the
+    chunk size, negative and strided increments, y overlapping x (through a
+    copy) and the three kinds of beta."""
+    for t, n in enumerate([1, 2, 33, 511, 512, 513, 1100, 2049]):
+        S = sym_from_tri(dense(rng, n, n, False), n, uplo, False)
+        AP = to_packed(S, n, uplo)
+        ix, iy = [(1, 1), (-2, 3), (3, -1)][t % 3]
+        x, y = vecs(rng, n, ix, False), vecs(rng, n, iy, False)
+        al = scal(rng, False)
+        be = [ZERO[False], ONE[False], scal(rng, False)][t % 3]
+        packed, rows = _sbmv_both(gpu, uplo, n, al, AP, x, ix, be, y, iy, name="mspmv")
+        want = matvec(oracle, False, "N", np.ascontiguousarray(S), n, n, gather(x, n, ix), al, be,
+                      gather(y, n, iy))
+        scale = orc.dd_abs(al) * n * orc.dd_absmax(S) * orc.dd_absmax(x) + orc.dd_abs(be) * orc.dd_absmax(y)
+        for got in (packed, rows):
+            assert err_ok(gather(got, n, iy), want, scale, max(10, 4 * n) * orc.EPS_DD), (n, uplo)
+
+
+@pytest.mark.parametrize("uplo", ["U", "L"])
+def test_packed_halves_non_finite_and_zero(gpu, rng, uplo):
+    """An infinity at packed entry (i0, j0) makes exactly rows i0 and j0 NaN on
+    both paths; zero entries and a zero x take the general decode and leave
+    the other rows finite and in agreement."""
+    n, i0, j0 = 700, 600, 650
+    S = sym_from_tri(dense(rng, n, n, False), n, uplo, False)
+    S[10:20, :] = 0.0
+    S[:, 10:20] = 0.0
+    si, sj = (i0, j0) if uplo == "U" else (j0, i0)
+    S[sj, si] = np.array([np.inf, 0.0])           # column sj, row si of the stored triangle
+    AP = to_packed(S, n, uplo)
+    x, y = vecs(rng, n, 1, False), vecs(rng, n, 1, False)
+    x[5] = 0.0
+    al, be = scal(rng, False), scal(rng, False)
+    packed, rows = _sbmv_both(gpu, uplo, n, al, AP, x, 1, be, y, 1, name="mspmv")
+    for got in (packed, rows):
+        bad = np.flatnonzero(np.isnan(got[:, 0]))
+        assert list(bad) == [i0, j0], bad
+    ok = np.setdiff1d(np.arange(n), [i0, j0])
+    finite = np.where(np.isfinite(S), S, 0.0)
+    scale = orc.dd_abs(al) * n * orc.dd_absmax(finite) * orc.dd_absmax(x) + orc.dd_abs(be) * orc.dd_absmax(y)
+    d = float(np.max(orc.dd_diff_abs(packed[ok], rows[ok])))
+    assert d <= 8 * n * orc.EPS_DD * scale, d
