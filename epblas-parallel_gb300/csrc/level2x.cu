@@ -525,9 +525,9 @@ __global__ void __launch_bounds__(256, 3) k_spmv_cols(int64_t n, const double2 *
         // lower rows (r, n) at r + 1 + r(2n-r-1)/2, both contiguous
         const int64_t cb = UPPER ? 0 : r + 1, ce = UPPER ? r : n;
         const double2 *col = AP + (UPPER ? r * (r + 1) / 2 : r * (2 * n - r - 1) / 2 + r + 1) - cb;
-        // fewer than fx::kMaxAdds products per lane (the host keeps n below
-        // 2^25); four loads in flight per lane, carries propagated after
-        // each run of 2048 products
+        // fewer than fx::kMaxAdds products per lane (the host keeps n within
+        // 65535 chunks, below 2^25); four loads in flight per lane, carries
+        // propagated after each run of 2048 products
         fx::Acc acc;
         acc.reset();
         int64_t c = cb + lane;
@@ -1050,7 +1050,7 @@ bool smv_device(const SmvArgs &a, const char *routine)
     if (!a.cplx && a.kind == 1 && a.fmt == 1 && a.n > 0 && (a.upper ? a.ku : a.kl) <= kSbMaxK &&
         g_band_tile.load() != 0)
         return sbmv_tile(a, routine);
-    if (!a.cplx && a.kind == 1 && a.fmt == 2 && a.n > 0 && a.n < ((int64_t)1 << 25) && g_band_tile.load() != 0)
+    if (!a.cplx && a.kind == 1 && a.fmt == 2 && a.n > 0 && a.n <= (int64_t)65535 * kSpChunk && g_band_tile.load() != 0)
         return spmv_split(a, routine);
     const int e2 = a.cplx ? 2 : 1;
     const size_t es = 16 * (size_t)e2;
