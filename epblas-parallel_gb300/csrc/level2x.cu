@@ -520,7 +520,11 @@ __global__ void __launch_bounds__(256, 3) k_spmv_cols(int64_t n, const double2 *
 {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * blockDim.x / 32;
-    for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32; r < n; r += warps) {
+    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / 32; w < n; w += warps) {
+        // longest columns first (upper: row r's column has r entries, lower
+        // n - 1 - r), so that the blocks the scheduler hands out last are the
+        // short ones
+        const int64_t r = UPPER ? n - 1 - w : w;
         // column r of the stored triangle: upper rows [0, r) at r(r+1)/2,
         // lower rows (r, n) at r + 1 + r(2n-r-1)/2, both contiguous
         const int64_t cb = UPPER ? 0 : r + 1, ce = UPPER ? r : n;
@@ -1010,9 +1014,9 @@ bool spmv_split(const SmvArgs &a, const char *routine)
     k_vdig<<<blocks_for(n), kThreads, 0, stream()>>>(n, (const double2 *)a.x, a.incx, 1, xd);
     const double2 *AP = (const double2 *)a.A;
     const dim3 grid((unsigned)((n + 255) / 256), (unsigned)nch);
-    int64_t wblocks = (n * 32 + 255) / 256;
-    const int64_t cap = (int64_t)device_sm_count() * 8;
-    if (wblocks > cap) wblocks = cap;
+    // a warp per row, every row in the grid: the block scheduler balances
+    // the uneven column lengths
+    const int64_t wblocks = (n * 32 + 255) / 256;
     if (a.upper) {
         k_spmv_rows<true><<<grid, 256, 0, stream()>>>(n, AP, xd, part);
         k_spmv_cols<true><<<(unsigned)wblocks, 256, 0, stream()>>>(n, AP, xd, partc);
