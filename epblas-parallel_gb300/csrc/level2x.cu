@@ -5,14 +5,18 @@
 //   TRMV/TBMV/TPMV, TRSV/TBSV/TPSV    A triangular               (mtrmv.cpp, mtrsv.cpp, mtbmv.cpp, ...)
 //   GER/GERU/GERC, SYR/HER, SYR2/HER2, SPR/HPR, SPR2/HPR2  rank-1/2 updates (mger.cpp, msyr.cpp, ...)
 //
-// Band and packed operands are first expanded into a dense scratch matrix by
-// one bandwidth-bound kernel (packed outputs are packed back); vectors with
-// any increment are gathered into contiguous scratch in BLAS order (a
-// negative increment walks backwards) and written back the same way. The
-// products then run as GEMM/SYMM/TRMM/TRSM/SYRK/SYR2K on the engines with
-// one right-hand side or a rank of one, so the arithmetic is the engines'
-// (exact fixed point or tensor-core residues) and the error bounds are the
-// level-3 ones.
+// Band and packed matrix-vector products read the operand in place from its
+// storage, in the fixed point of fixacc.cuh (k_smv; real symmetric bands of
+// small bandwidth from shared-memory tiles, k_sbmv_tile; real symmetric
+// packed matrices in two coalesced halves, k_spmv_*). Band solves of small
+// bandwidth run in place (k_tbsv, k_spike_*). Otherwise band and packed
+// operands are expanded into a dense scratch matrix by one bandwidth-bound
+// kernel (packed outputs are packed back); vectors with any increment are
+// gathered into contiguous scratch in BLAS order (a negative increment walks
+// backwards) and written back the same way. Those products then run as
+// GEMM/SYMM/TRMM/TRSM/SYRK/SYR2K on the engines with one right-hand side or a
+// rank of one, so the arithmetic is the engines' (exact fixed point or
+// tensor-core residues) and the error bounds are the level-3 ones.
 #include <atomic>
 #include <climits>
 
