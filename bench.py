@@ -512,11 +512,17 @@ def plain_profile():
 
 
 def tc_traffic_from_profile():
-    p = os.path.join(ROOT, "profiles", "k_oz_gemm_tc_2sm_4096_ncu.txt")
+    return traffic_from_profile("k_oz_gemm_tc_2sm_4096_ncu.txt", "dram_bytes_per_launch_8192")
+
+
+def traffic_from_profile(name, key="dram_bytes_per_launch"):
+    """DRAM bytes (read + write) per launch recorded by an ncu capture in
+    profiles/ (a `key: value` line), or None."""
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("dram_bytes_per_launch_8192:"):
+        if line.startswith(key + ":"):
             return float(line.split(":")[1].strip())
     return None
 
@@ -948,8 +954,12 @@ def run_workload(args):
         metric = (f"DD-{'SBMV' if band else 'SPMV'} HBM GB/s n={n}" + (f" k={k}" if band else "")
                   + " (16(stored + 3n) bytes)")
         cfg = {"workload": f"m{w}_ U n={n}" + (f" k={k}" if band else "") + " incx=incy=1"}
+        # traffic: the band kernel's, or the two packed halves' per call, at these sizes
+        traffic = None
+        if not args.size:
+            traffic = traffic_from_profile("k_sbmv_tile_n4M_k16_ncu.txt" if band else "mspmv_16384_launches.txt")
         roof = {"bound": "hbm", "achieved": value, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": value / pk["hbm_gbs"], "peak_kind": pk_kind, "traffic": None}
+                "frac": value / pk["hbm_gbs"], "peak_kind": pk_kind, "traffic": traffic}
         if o:
             y.copy_(y0)
             fn()
