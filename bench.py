@@ -532,7 +532,8 @@ def traffic_from_profile(name, key="dram_bytes_per_launch"):
 # workloads, each printed as one JSON line of the same shape as the headline.
 # ---------------------------------------------------------------------------
 
-WORKLOADS = ("gemm", "stress", "gemm_fp64", "wgemm", "gemm_t", "gemm_fixed", "gemm_plain", "syrk", "herk", "trsm", "gemv", "dot",
+WORKLOADS = ("gemm", "stress", "gemm_fp64", "wgemm", "gemm_t", "gemm_fixed", "gemm_plain", "syrk", "herk", "trsm", "gemv",
+             "gemv_t", "dot",
              "axpy", "scal", "copy", "swap", "iamax", "batched_gemm", "batched_trsm", "gemmtr", "symm", "syr2k",
              "trmm", "wtrsm", "sbmv", "spmv", "tbsv")
 
@@ -907,27 +908,33 @@ def run_workload(args):
             scale = m * orc.dd_absmax(tri) * orc.dd_absmax(X) + orc.dd_abs(ca) * orc.dd_absmax(hB0)
             check["normwise_residual_sampled"] = orc.normwise_error(AX, rhs, scale)
             check["entries_checked"] = 256
-    elif w == "gemv":
+    elif w in ("gemv", "gemv_t"):
+        # square GEMV, op(A) = A (a thread per row) or A^T (a block per column)
+        tr = "T" if w == "gemv_t" else "N"
         m = n = args.size or 16384
         A = _dev_dd(torch, (n, m), gen, dev)
         x = _dev_dd(torch, (n,), gen, dev)
         y = _dev_dd(torch, (m,), gen, dev)
         y0 = y.clone()
-        fn = lambda: lib.mgemv("N", m, n, al, A.data_ptr(), m, x.data_ptr(), 1, be, y.data_ptr(), 1)
+        fn = lambda: lib.mgemv(tr, m, n, al, A.data_ptr(), m, x.data_ptr(), 1, be, y.data_ptr(), 1)
         ms, clk = _timed(torch, fn, args.steps, args.warmup, stream, reset=lambda: y.copy_(y0))
         nbytes = 16.0 * (m * n + n + 2 * m)
         value, unit = nbytes / ms / 1e6, "GB/s"
-        metric = f"DD-GEMV HBM GB/s m=n={n} (16(mn+n+2m) bytes)"
-        cfg = {"workload": f"mgemv_ N m=n={n} incx=incy=1"}
+        metric = f"DD-GEMV{'-T' if tr == 'T' else ''} HBM GB/s m=n={n} (16(mn+n+2m) bytes)"
+        cfg = {"workload": f"mgemv_ {tr} m=n={n} incx=incy=1"}
         roof = {"bound": "hbm", "achieved": value, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": value / pk["hbm_gbs"], "peak_kind": pk_kind, "traffic": None}
         if o:
             y.copy_(y0)
             fn()
             rows = np.sort(rng.choice(m, 64, replace=False))
-            sub = np.ascontiguousarray(hb(A[:, torch.as_tensor(rows, device=dev)]))
             want = hb(y0)[rows].copy()
-            o.qgemv("N", len(rows), n, al, sub, len(rows), hb(x), 1, be, want, 1)
+            if tr == "N":
+                sub = np.ascontiguousarray(hb(A[:, torch.as_tensor(rows, device=dev)]))
+                o.qgemv("N", len(rows), n, al, sub, len(rows), hb(x), 1, be, want, 1)
+            else:   # entries rows of y = columns of A
+                sub = np.ascontiguousarray(hb(A[torch.as_tensor(rows, device=dev)]))
+                o.qgemv("T", m, len(rows), al, sub, m, hb(x), 1, be, want, 1)
             got = hb(y)[rows]
             amax = float(A[..., 0].abs().max())
             op = orc.dd_abs(al) * n * amax * orc.dd_absmax(hb(x)) + orc.dd_abs(be) * orc.dd_absmax(hb(y0))

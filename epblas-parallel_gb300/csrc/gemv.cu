@@ -179,9 +179,9 @@ __global__ void k_gemv_n_fx_final(int64_t m, int nchunks, const fx::XFPod *part,
 
 // Trans: block per column j of A (contiguous), threads over rows; every
 // fx::kMaxAdds products a thread's accumulator is folded into an extended float.
-__global__ void __launch_bounds__(256) k_gemv_t_fx(int64_t m, int64_t n, const double2 *__restrict__ A, int64_t lda,
-                                                  const fx::Dig *__restrict__ xo, dd::real alpha, double2 *y,
-                                                  int64_t incy)
+__global__ void __launch_bounds__(256, 3) k_gemv_t_fx(int64_t m, int64_t n, const double2 *__restrict__ A,
+                                                     int64_t lda, const fx::Dig *__restrict__ xo, dd::real alpha,
+                                                     double2 *y, int64_t incy)
 {
     __shared__ fx::XFPod sh[8];
     const int64_t j = blockIdx.x;
@@ -192,14 +192,45 @@ __global__ void __launch_bounds__(256) k_gemv_t_fx(int64_t m, int64_t n, const d
     total.zero = true; total.neg = false; total.m = 0; total.e = 0;
     bool bad = false;
     int cnt = 0;
-    for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
-        acc.add_dig(fx::decode(__ldcs(col + i)), xo[i]);
-        if (++cnt >= fx::kMaxAdds) {
-            bad |= acc.bad;
-            total = xfp::xf_add(total, acc.finish());
-            acc.reset();
-            cnt = 0;
+    auto fold = [&]() {
+        bad |= acc.bad;
+        total = xfp::xf_add(total, acc.finish());
+        acc.reset();
+        cnt = 0;
+    };
+    // four rows in flight per thread (GEMV N's flag-free groups of four);
+    // carries propagated after each run of 2048 products
+    const int64_t bs = blockDim.x;
+    int64_t i = threadIdx.x;
+    while (i + 3 * bs < m) {
+        const int64_t iend = i + 4 * bs * 512;
+        for (; i + 3 * bs < m && i < iend; i += 4 * bs) {
+            const double2 a0 = __ldcs(col + i), a1 = __ldcs(col + i + bs);
+            const double2 a2 = __ldcs(col + i + 2 * bs), a3 = __ldcs(col + i + 3 * bs);
+            const fx::Dig x0 = xo[i], x1 = xo[i + bs], x2 = xo[i + 2 * bs], x3 = xo[i + 3 * bs];
+            if (fx::decode_is_fast(a0) && fx::decode_is_fast(a1) && fx::decode_is_fast(a2) && fx::decode_is_fast(a3) &&
+                ((x0.flags | x1.flags | x2.flags | x3.flags) & (fx::kZero | fx::kBad)) == 0) {
+                const fx::Op o0 = fx::decode_fast(a0), o1 = fx::decode_fast(a1);
+                const fx::Op o2 = fx::decode_fast(a2), o3 = fx::decode_fast(a3);
+                const int e0 = o0.e + x0.e, e1 = o1.e + x1.e, e2 = o2.e + x2.e, e3 = o3.e + x3.e;
+                acc.admit(max(max(e0, e1), max(e2, e3)));
+                acc.mul_fast(o0, x0, acc.B - e0);
+                acc.mul_fast(o1, x1, acc.B - e1);
+                acc.mul_fast(o2, x2, acc.B - e2);
+                acc.mul_fast(o3, x3, acc.B - e3);
+            } else {
+                acc.add_core(fx::decode(a0), x0);
+                acc.add_core(fx::decode(a1), x1);
+                acc.add_core(fx::decode(a2), x2);
+                acc.add_core(fx::decode(a3), x3);
+            }
         }
+        acc.normalize();
+        if ((cnt += 2048) >= fx::kMaxAdds) fold();
+    }
+    for (; i < m; i += bs) {
+        acc.add_dig(fx::decode(__ldcs(col + i)), xo[i]);
+        if (++cnt >= fx::kMaxAdds) fold();
     }
     bad |= acc.bad;
     total = xfp::xf_add(total, acc.finish());
